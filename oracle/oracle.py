@@ -1,0 +1,193 @@
+"""ctypes front-end of the CPU oracle (oracle/qlpiv_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the CPU
+legs of bench.py, as the checker or the timed CPU baseline.  The product never
+imports this module.
+"""
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libqlpiv_oracle.so"
+
+# orc_vector (48 bytes): the product's qlpiv_vector (first 32 bytes) plus the
+# double-precision displacement of the FP64 twin.
+VECTOR_DTYPE = np.dtype([
+    ("u", "<f4"), ("v", "<f4"), ("sub_i", "<f4"), ("sub_j", "<f4"),
+    ("peak_value", "<f4"), ("min_floor", "<f4"), ("peak_i", "<i2"), ("peak_j", "<i2"),
+    ("flags", "<u4"), ("u64", "<f8"), ("v64", "<f8"),
+])
+
+F_SUB_I, F_SUB_J, F_PARABOLIC, F_EDGE, F_NO_PEAK = 1, 2, 4, 8, 16
+
+NORM_MAX_A, NORM_OWN_MAX, NORM_FIXED, NORM_NONE = 0, 1, 2, 3
+
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle with its Makefile (gcc only; seconds)."""
+    src = [HERE / "qlpiv_oracle.c", HERE / "oracle_impl.h"]
+    if not force and LIB_PATH.exists() and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in src):
+        return LIB_PATH
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(str(LIB_PATH))
+        fp = ctypes.POINTER(ctypes.c_float)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        vp = ctypes.c_void_p
+        c_int, c_float, c_long = ctypes.c_int, ctypes.c_float, ctypes.c_long
+        L.orc_xcorr_fft_f32.argtypes = [fp, fp, c_int, c_float, c_float, c_int, fp]
+        L.orc_xcorr_fft_f64.argtypes = [fp, fp, c_int, c_float, c_float, c_int, dp]
+        L.orc_xcorr_direct_f64.argtypes = [fp, fp, c_int, c_float, c_float, c_int, dp]
+        L.orc_find_max_from_center_f32.argtypes = [fp, c_int, c_int, ip, ip, fp, fp]
+        L.orc_find_max_from_center_f64.argtypes = [dp, c_int, c_int, ip, ip, dp, dp]
+        L.orc_subpixel_gauss3_f32.argtypes = [fp, c_int, c_int, c_int, c_int, fp, fp, ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_subpixel_gauss3_f64.argtypes = [dp, c_int, c_int, c_int, c_int, dp, dp, ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_clip_tile.argtypes = [vp, c_int, c_int, c_int, c_int, c_int, c_int, fp]
+        L.orc_clip_tile.restype = c_float
+        L.orc_grid_superposition.argtypes = [c_int] * 8 + [c_float, vp, ip, ip, c_int]
+        L.orc_grid_nosuperposition.argtypes = [c_int] * 8 + [vp, ip, ip, c_int]
+        L.orc_piv_pass.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_long, ip, ip, ip, ip, c_int,
+                                   c_float, c_float, c_int, c_int, vp, c_int]
+        L.orc_vector_size.restype = c_int
+        assert L.orc_vector_size() == VECTOR_DTYPE.itemsize
+        _lib = L
+    return _lib
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def xcorr_fft(ta, tb, max_a, max_b, normalize=True, precision=32):
+    """(2N-1)^2 correlation plane by the restated SimpleFFT path."""
+    ta, tb = _f32(ta), _f32(tb)
+    n = ta.shape[0]
+    d = 2 * n - 1
+    if precision == 32:
+        out = np.zeros((d, d), np.float32)
+        lib().orc_xcorr_fft_f32(_ptr(ta, ctypes.c_float), _ptr(tb, ctypes.c_float), n, max_a, max_b,
+                                int(normalize), _ptr(out, ctypes.c_float))
+    else:
+        out = np.zeros((d, d), np.float64)
+        lib().orc_xcorr_fft_f64(_ptr(ta, ctypes.c_float), _ptr(tb, ctypes.c_float), n, max_a, max_b,
+                                int(normalize), _ptr(out, ctypes.c_double))
+    return out
+
+
+def xcorr_direct(ta, tb, max_a, max_b, normalize=True):
+    ta, tb = _f32(ta), _f32(tb)
+    n = ta.shape[0]
+    out = np.zeros((2 * n - 1, 2 * n - 1), np.float64)
+    lib().orc_xcorr_direct_f64(_ptr(ta, ctypes.c_float), _ptr(tb, ctypes.c_float), n, max_a, max_b,
+                               int(normalize), _ptr(out, ctypes.c_double))
+    return out
+
+
+def find_max_from_center(plane):
+    plane = np.ascontiguousarray(plane)
+    di, dj = plane.shape
+    oi, oj = ctypes.c_int(), ctypes.c_int()
+    if plane.dtype == np.float32:
+        ov, om = ctypes.c_float(), ctypes.c_float()
+        lib().orc_find_max_from_center_f32(_ptr(plane, ctypes.c_float), di, dj, ctypes.byref(oi),
+                                           ctypes.byref(oj), ctypes.byref(ov), ctypes.byref(om))
+    else:
+        plane = plane.astype(np.float64)
+        ov, om = ctypes.c_double(), ctypes.c_double()
+        lib().orc_find_max_from_center_f64(_ptr(plane, ctypes.c_double), di, dj, ctypes.byref(oi),
+                                           ctypes.byref(oj), ctypes.byref(ov), ctypes.byref(om))
+    return oi.value, oj.value, ov.value, om.value
+
+
+def subpixel_gauss3(plane, mi, mj):
+    plane = np.ascontiguousarray(plane)
+    di, dj = plane.shape
+    fl = ctypes.c_uint32()
+    if plane.dtype == np.float32:
+        pi, pj = ctypes.c_float(), ctypes.c_float()
+        lib().orc_subpixel_gauss3_f32(_ptr(plane, ctypes.c_float), di, dj, mi, mj, ctypes.byref(pi),
+                                      ctypes.byref(pj), ctypes.byref(fl))
+    else:
+        plane = plane.astype(np.float64)
+        pi, pj = ctypes.c_double(), ctypes.c_double()
+        lib().orc_subpixel_gauss3_f64(_ptr(plane, ctypes.c_double), di, dj, mi, mj, ctypes.byref(pi),
+                                      ctypes.byref(pj), ctypes.byref(fl))
+    return pi.value, pj.value, fl.value
+
+
+def clip_tile(img, top, left, n):
+    img = np.ascontiguousarray(img)
+    tile = np.zeros((n, n), np.float32)
+    mx = lib().orc_clip_tile(img.ctypes.data, img.shape[0], img.shape[1], img.dtype.itemsize, top, left, n,
+                             _ptr(tile, ctypes.c_float))
+    return tile, mx
+
+
+class _Grid(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int) for k in
+                ("n", "tiles_i", "tiles_j", "margin_top", "margin_left", "margin_bottom", "margin_right")]
+
+
+def grid(h, w, n_start, level=0, overlap_factor=0.5, margins=(0, 0, 0, 0), superposition=True):
+    """IA grid of one adaptive level.  margins = (top, bottom, left, right).
+    Returns (dict of grid scalars, tops[tiles_i], lefts[tiles_j])."""
+    cap = 65536
+    tops = np.zeros(cap, np.int32)
+    lefts = np.zeros(cap, np.int32)
+    g = _Grid()
+    mt, mb, ml, mr = margins
+    if superposition:
+        rc = lib().orc_grid_superposition(h, w, mt, mb, ml, mr, n_start, level, overlap_factor, ctypes.byref(g),
+                                          _ptr(tops, ctypes.c_int), _ptr(lefts, ctypes.c_int), cap)
+    else:
+        rc = lib().orc_grid_nosuperposition(h, w, mt, mb, ml, mr, n_start, level, ctypes.byref(g),
+                                            _ptr(tops, ctypes.c_int), _ptr(lefts, ctypes.c_int), cap)
+    if rc != 0:
+        raise ValueError("grid too large")
+    d = {k: getattr(g, k) for k, _ in _Grid._fields_}
+    return d, tops[:g.tiles_i].copy(), lefts[:g.tiles_j].copy()
+
+
+def piv_pass(img_a, img_b, n, a_top, a_left, b_top=None, b_left=None, norm_mode=NORM_MAX_A,
+             fixed_max=(255.0, 255.0), subpix=True, precision=32, nthreads=None):
+    """One correlation pass over all IAs (vectors in IA order)."""
+    img_a = np.ascontiguousarray(img_a)
+    img_b = np.ascontiguousarray(img_b)
+    assert img_a.dtype == img_b.dtype and img_a.dtype in (np.uint8, np.uint16)
+    a_top = np.ascontiguousarray(a_top, np.int32)
+    a_left = np.ascontiguousarray(a_left, np.int32)
+    b_top = a_top if b_top is None else np.ascontiguousarray(b_top, np.int32)
+    b_left = a_left if b_left is None else np.ascontiguousarray(b_left, np.int32)
+    count = a_top.shape[0]
+    out = np.zeros(count, VECTOR_DTYPE)
+    if nthreads is None:
+        nthreads = os.cpu_count() or 1
+    lib().orc_piv_pass(img_a.ctypes.data, img_b.ctypes.data, img_a.shape[0], img_a.shape[1], img_a.dtype.itemsize,
+                       n, count, _ptr(a_top, ctypes.c_int), _ptr(a_left, ctypes.c_int), _ptr(b_top, ctypes.c_int),
+                       _ptr(b_left, ctypes.c_int), norm_mode, fixed_max[0], fixed_max[1], int(subpix),
+                       0 if precision == 32 else 1, out.ctypes.data, nthreads)
+    return out
+
+
+def grid_origins(h, w, n, overlap_factor=0.5, level=0, n_start=None, margins=(0, 0, 0, 0), superposition=True):
+    """Flattened (row-major) tile origins of one grid."""
+    g, tops, lefts = grid(h, w, n if n_start is None else n_start, level, overlap_factor, margins, superposition)
+    tt, ll = np.meshgrid(tops, lefts, indexing="ij")
+    return g, tt.ravel().astype(np.int32), ll.ravel().astype(np.int32)

@@ -1,0 +1,180 @@
+"""Generate the small golden fixtures under tests/golden/ from the reference tree.
+
+Run once in a checkout that has the QuickLabPIV-ng reference next to it:
+    python tests/golden/make_golden.py /path/to/QuickLabPIV-ng
+The outputs are committed; no test reads the reference tree at run time.
+
+Fixtures written (all from files shipped in the reference project):
+  rankine_pair.npz     resources/fftBenchmark/rankine_vortex01_{0,1}.tif (512x512 u8,
+                       PackBits TIFF), decoded here.
+  gpu_fft_golden.npz   every 16th of the 1024 31x31 correlation planes in
+                       resources/fftBenchmark/gpuFFTBenchmarkValidationData.matFloat
+                       (16x16 IAs, no overlap, own-max normalisation), with their
+                       IA indices.
+  shift_kat.npz        testFiles/img1.png, img2.png: the synthetic pair shifted by
+                       10 px used by ImageCrossCorrelationRealFFTParStdJobTests.
+  filter_golden.npz    testFiles/GaussianFilter2D_*.matFloat (Gaussian prefilter
+                       outputs) cropped to a 96x96 window.
+"""
+import struct
+import sys
+import zlib
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+
+
+def read_matfloat(path):
+    """SimpleFloatMatrixImporterExporter format (big-endian): 'MATFloat\\0', u16 count,
+    count x (u16 len, name), then per matrix u16 cols, u16 rows, u16 depth, rows*cols f32."""
+    b = Path(path).read_bytes()
+    if b[:9] != b"MATFloat\x00":
+        raise ValueError("not a .matFloat file")
+    p = 9
+    (cnt,) = struct.unpack(">H", b[p:p + 2])
+    p += 2
+    names = []
+    for _ in range(cnt):
+        (ln,) = struct.unpack(">H", b[p:p + 2])
+        p += 2
+        names.append(b[p:p + ln].decode())
+        p += ln
+    mats = []
+    for _ in range(cnt):
+        sx, sy, _sz = struct.unpack(">HHH", b[p:p + 6])
+        p += 6
+        mats.append(np.frombuffer(b[p:p + 4 * sx * sy], dtype=">f4").reshape(sy, sx).astype(np.float32))
+        p += 4 * sx * sy
+    if p != len(b):
+        raise ValueError("trailing bytes in .matFloat")
+    return names, mats
+
+
+def read_tiff_gray(path):
+    """Baseline grey TIFF, 8/16 bit, uncompressed or PackBits, strip organised."""
+    b = Path(path).read_bytes()
+    e = "<" if b[:2] == b"II" else ">"
+    (off,) = struct.unpack(e + "I", b[4:8])
+    (n,) = struct.unpack(e + "H", b[off:off + 2])
+    tags = {}
+    for k in range(n):
+        ent = b[off + 2 + 12 * k: off + 14 + 12 * k]
+        t, typ, cnt = struct.unpack(e + "HHI", ent[:8])
+        tags[t] = (typ, cnt, ent[8:12])
+
+    def values(t):
+        typ, cnt, raw = tags[t]
+        size = {3: 2, 4: 4}[typ]
+        fmt = e + ("H" if typ == 3 else "I") * cnt
+        if cnt * size <= 4:
+            return list(struct.unpack(fmt, raw[:cnt * size]))
+        (ptr,) = struct.unpack(e + "I", raw)
+        return list(struct.unpack(fmt, b[ptr:ptr + cnt * size]))
+
+    w, h = values(256)[0], values(257)[0]
+    bps, comp = values(258)[0], values(259)[0]
+    data = bytearray()
+    for o, c in zip(values(273), values(279)):
+        s = b[o:o + c]
+        if comp == 1:
+            data += s
+        elif comp == 32773:
+            i = 0
+            while i < len(s):
+                hdr = s[i] - 256 if s[i] > 127 else s[i]
+                i += 1
+                if hdr >= 0:
+                    data += s[i:i + hdr + 1]
+                    i += hdr + 1
+                elif hdr != -128:
+                    data += bytes([s[i]]) * (1 - hdr)
+                    i += 1
+        else:
+            raise ValueError(f"TIFF compression {comp} not supported")
+    dt = np.uint8 if bps == 8 else np.dtype(e + "u2")
+    return np.frombuffer(bytes(data), dtype=dt)[: w * h].reshape(h, w).copy()
+
+
+def read_png_gray(path):
+    """8/16-bit greyscale or RGB(A) PNG (non-interlaced); colour images are reduced to
+    the first channel.  16-bit samples are big-endian in the file."""
+    b = Path(path).read_bytes()
+    assert b[:8] == b"\x89PNG\r\n\x1a\n"
+    p = 8
+    idat = b""
+    while p < len(b):
+        (ln,) = struct.unpack(">I", b[p:p + 4])
+        typ = b[p + 4:p + 8]
+        body = b[p + 8:p + 8 + ln]
+        p += 12 + ln
+        if typ == b"IHDR":
+            w, h, depth, ctype, _c, _f, inter = struct.unpack(">IIBBBBB", body)
+            assert depth in (8, 16) and inter == 0
+        elif typ == b"IDAT":
+            idat += body
+    ch = {0: 1, 2: 3, 4: 2, 6: 4}[ctype] * (depth // 8)
+    raw = zlib.decompress(idat)
+    stride = w * ch
+    out = np.zeros((h, stride), dtype=np.uint8)
+    prev = np.zeros(stride, dtype=np.int32)
+    pos = 0
+    for r in range(h):
+        f = raw[pos]
+        line = np.frombuffer(raw[pos + 1:pos + 1 + stride], dtype=np.uint8).astype(np.int32)
+        pos += 1 + stride
+        cur = np.zeros(stride, dtype=np.int32)
+        for x in range(stride):
+            a = cur[x - ch] if x >= ch else 0
+            up = prev[x]
+            c = prev[x - ch] if x >= ch else 0
+            if f == 0:
+                v = line[x]
+            elif f == 1:
+                v = line[x] + a
+            elif f == 2:
+                v = line[x] + up
+            elif f == 3:
+                v = line[x] + ((a + up) >> 1)
+            else:
+                pa, pb, pc = abs(up - c), abs(a - c), abs(a + up - 2 * c)
+                pr = a if (pa <= pb and pa <= pc) else (up if pb <= pc else c)
+                v = line[x] + pr
+            cur[x] = v & 0xFF
+        out[r] = cur
+        prev = cur
+    if depth == 16:
+        return (out[:, 0::ch].astype(np.uint16) << 8) | out[:, 1::ch].astype(np.uint16)
+    return out[:, ::ch].copy()
+
+
+def main(ref):
+    ref = Path(ref)
+    a = read_tiff_gray(ref / "resources/fftBenchmark/rankine_vortex01_0.tif")
+    b = read_tiff_gray(ref / "resources/fftBenchmark/rankine_vortex01_1.tif")
+    np.savez_compressed(HERE / "rankine_pair.npz", a=a, b=b)
+
+    names, mats = read_matfloat(ref / "resources/fftBenchmark/gpuFFTBenchmarkValidationData.matFloat")
+    idx = np.arange(0, len(mats), 16)
+    sel_names = [names[i] for i in idx]
+    np.savez_compressed(HERE / "gpu_fft_golden.npz", index=idx, planes=np.stack([mats[i] for i in idx]),
+                        names=np.array(sel_names))
+
+    i1 = read_png_gray(ref / "testFiles/img1.png")
+    i2 = read_png_gray(ref / "testFiles/img2.png")
+    np.savez_compressed(HERE / "shift_kat.npz", img1=i1, img2=i2)
+
+    fn1, fm1 = read_matfloat(ref / "testFiles/GaussianFilter2D_3px_2.0f_rankine_vortex01_0.matFloat")
+    fn2, fm2 = read_matfloat(ref / "testFiles/GaussianFilter2D_5px_0.48f_rankine_vortex01_0_1.matFloat")
+    win = (slice(200, 296), slice(200, 296))
+    np.savez_compressed(HERE / "filter_golden.npz", window=np.array([200, 296, 200, 296]),
+                        names1=np.array(fn1), names2=np.array(fn2),
+                        **{f"f1_{k}": m[win] for k, m in enumerate(fm1)},
+                        **{f"f2_{k}": m[win] for k, m in enumerate(fm2)})
+    print("shapes:", a.shape, b.shape, i1.shape, i2.shape, [m.shape for m in fm1], [m.shape for m in fm2],
+          fn1, fn2)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
