@@ -1,0 +1,159 @@
+/*
+ * qlpiv -- C ABI of the GB300 FFT-PIV hot path (libqlpiv_gpu.so).
+ *
+ * Drop-in boundary for QuickLabPIV-ng's PIV stage plugins.  Every entry point takes
+ * plain pointers and sizes, returns a qlpiv_status, and on failure leaves a message
+ * for qlpiv_last_error() (thread-local).  Host pointers are borrowed for the duration
+ * of the call; device buffers, streams and pinned staging belong to the handle.
+ * Calls on one handle are serialised by the handle; distinct handles are
+ * independent (the reference runs one job instance per host thread,
+ * S/jobs/managers/OpenClGpuManager.java:121-148).
+ *
+ * Citations: paths inside QuickLabPIV-ng, S/ = src/main/java/pt/quickLabPIV/.
+ */
+#ifndef QLPIV_H
+#define QLPIV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QLPIV_ABI_VERSION 1
+
+/* Status codes.  The Java shim maps QLPIV_E_SHAPE/QLPIV_E_ARG to JobAnalyzeException
+ * (S/jobs/xcorr/CrossCorrelationFFTTemplate.java:594-642 shape checks) and the others
+ * to JobComputeException. */
+typedef enum {
+    QLPIV_OK = 0,
+    QLPIV_E_ARG = 1,         /* null pointer, bad enum, count < 0 */
+    QLPIV_E_SHAPE = 2,       /* unsupported IA size, tiles of different size */
+    QLPIV_E_OOM = 3,         /* device or pinned allocation failed */
+    QLPIV_E_CUDA = 4,        /* a CUDA runtime call failed */
+    QLPIV_E_TIMEOUT = 5,     /* a bounded device wait expired */
+    QLPIV_E_CANCELLED = 6,   /* request cancelled */
+    QLPIV_E_UNSUPPORTED = 7, /* feature not available in this build */
+    QLPIV_E_NO_DEVICE = 8    /* no CUDA device */
+} qlpiv_status;
+
+/* Pixel type of images and tiles. */
+typedef enum {
+    QLPIV_PIX_U8 = 0,  /* MatrixByte, 8-bit images */
+    QLPIV_PIX_U16 = 1, /* MatrixInt16, 10/12/16-bit images */
+    QLPIV_PIX_F32 = 2  /* MatrixFloat */
+} qlpiv_pixel;
+
+/* Tile normalisation v/max*16+1 (no mean subtraction). */
+typedef enum {
+    QLPIV_NORM_MAX_A = 0,   /* both tiles by tile A's max: FastRealFFTXCorr.java:53-54 (CPU job) */
+    QLPIV_NORM_OWN_MAX = 1, /* each tile by its own max: CrossCorrelationRealFFTParStdJob.java:128-129 */
+    QLPIV_NORM_NONE = 3     /* raw values */
+} qlpiv_norm;
+
+/* Where the tile maxima come from. */
+typedef enum {
+    QLPIV_MAX_COMPUTE = 0, /* max of the clipped tile, floored at 16 (MatrixByte.java:16-33) */
+    QLPIV_MAX_GIVEN = 1,   /* per-IA arrays supplied by the caller (Matrix.getMaxValue()) */
+    QLPIV_MAX_FIXED = 2    /* one constant per image (full-image warp tiles, MatrixByte.java:366-384) */
+} qlpiv_max_mode;
+
+typedef enum {
+    QLPIV_SUBPIX_NONE = 0,
+    QLPIV_SUBPIX_GAUSS3 = 1 /* Gaussian1DPolynomialInterpolator (3-point, 1D-1D) */
+} qlpiv_subpix;
+
+/* qlpiv_vector.flags */
+#define QLPIV_F_SUB_I 1u     /* sub-pixel fit accepted along I (rows) */
+#define QLPIV_F_SUB_J 2u     /* sub-pixel fit accepted along J (columns) */
+#define QLPIV_F_PARABOLIC 4u /* a stencil value was negative: parabolic fallback */
+#define QLPIV_F_EDGE 8u      /* 3-point stencil leaves the plane: integer peak kept */
+#define QLPIV_F_NO_PEAK 16u  /* no non-negative cell: peak left at (0,0) */
+
+/* One IA result (32 bytes): MaxCrossResult main peak after interpolation.
+ * u/v are the displacement increments along rows/columns
+ * (MaxCrossResult.getNthDisplacementU/V, S/maximum/MaxCrossResult.java:304-326,412-437);
+ * sub_i/sub_j the sub-pixel peak in plane coordinates; peak_i/peak_j the integer peak
+ * of FindMaximumFromCenter; min_floor the minimum over the visited cells. */
+typedef struct qlpiv_vector {
+    float u, v;
+    float sub_i, sub_j;
+    float peak_value;
+    float min_floor;
+    int16_t peak_i, peak_j;
+    uint32_t flags;
+} qlpiv_vector;
+
+/* One correlation pass: IA side and tile/peak semantics. */
+typedef struct qlpiv_pass_desc {
+    int n;              /* IA side: 16, 32 or 64 */
+    int norm_mode;      /* qlpiv_norm */
+    int max_mode;       /* qlpiv_max_mode */
+    float fixed_max_a;  /* QLPIV_MAX_FIXED: max of every A tile */
+    float fixed_max_b;  /* QLPIV_MAX_FIXED: max of every B tile */
+    int subpix_mode;    /* qlpiv_subpix */
+    int reserved[6];
+} qlpiv_pass_desc;
+
+typedef struct qlpiv_params {
+    int device;         /* CUDA device ordinal */
+    int reserved[7];
+} qlpiv_params;
+
+typedef struct qlpiv_handle qlpiv_handle;
+
+int qlpiv_abi_version(void);
+const char *qlpiv_last_error(void);
+
+/* Creates a handle bound to one device: a non-blocking stream, device workspace and
+ * pinned staging that grow on demand.  Replaces the device set-up of the xcorr job
+ * constructors (S/jobs/xcorr/CrossCorrelationRealFFTParStdJob.java:58-78). */
+qlpiv_status qlpiv_create(const qlpiv_params *params, qlpiv_handle **out);
+/* Job.dispose() (S/jobs/Job.java:58): frees everything the handle owns. */
+qlpiv_status qlpiv_destroy(qlpiv_handle *h);
+/* Waits for all work queued on the handle's stream. */
+qlpiv_status qlpiv_synchronize(qlpiv_handle *h);
+
+/* Job<List<Tile>, XCorrelationResults> compute() for the cross-correlation job:
+ * `count` tile pairs of n x n pixels (row-major, contiguous per tile) in host memory,
+ * tile maxima per IA (max_a/max_b; NULL = compute, floor 16), normalisation mode.
+ * Writes count (2n-1)^2 float planes, the JOB_RESULT_CROSS_MATRICES of
+ * CrossCorrelationRealFFTParStdJob / CrossCorrelationSoftRealFFTJob
+ * (S/jobs/xcorr/XCorrelationResults.java:14-55). */
+qlpiv_status qlpiv_xcorr_planes(qlpiv_handle *h, int n, long count, int pixel_type, const void *tiles_a,
+                                const void *tiles_b, const float *max_a, const float *max_b, int norm_mode,
+                                float *planes_out);
+
+/* Fused xcorr + FindMaximumFromCenter.findMaximum (S/maximum/FindMaximumFromCenter.java:47-183)
+ * + ICrossCorrelationInterpolator.interpolate (Gaussian1DPolynomialInterpolator.java:25-106)
+ * on host tiles; writes count vectors.  Same tile arguments as qlpiv_xcorr_planes. */
+qlpiv_status qlpiv_xcorr_peaks(qlpiv_handle *h, int n, long count, int pixel_type, const void *tiles_a,
+                               const void *tiles_b, const float *max_a, const float *max_b, int norm_mode,
+                               int subpix_mode, qlpiv_vector *out);
+
+/* One correlation pass over an image pair in host memory (height x width, row-major):
+ * warp/clip (IImageWarpingStrategy.warpAndClipImage, S/images/NoImageWarpingStrategy.java:27-89,
+ * tiles partially outside the image are zero-filled), xcorr, peak and sub-pixel for
+ * `count` IAs whose tile origins are given per IA (a_top/a_left in image A,
+ * b_top/b_left in image B: rounded displaced origins, FastMath.round).  Synchronous;
+ * writes count vectors to host memory. */
+qlpiv_status qlpiv_pass(qlpiv_handle *h, const qlpiv_pass_desc *desc, const void *img_a, const void *img_b,
+                        int height, int width, int pixel_type, long count, const int32_t *a_top,
+                        const int32_t *a_left, const int32_t *b_top, const int32_t *b_left, qlpiv_vector *out);
+
+/* Same as qlpiv_pass with every pointer in device memory (inputs resident in HBM);
+ * queued on the handle's stream and returns without waiting. */
+qlpiv_status qlpiv_pass_device(qlpiv_handle *h, const qlpiv_pass_desc *desc, const void *img_a,
+                               const void *img_b, int height, int width, int pixel_type, long count,
+                               const int32_t *a_top, const int32_t *a_left, const int32_t *b_top,
+                               const int32_t *b_left, qlpiv_vector *out);
+
+/* Number of kernel launches issued by this handle since creation (instrumentation). */
+long qlpiv_launch_count(qlpiv_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QLPIV_H */

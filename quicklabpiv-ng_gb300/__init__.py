@@ -1,0 +1,237 @@
+"""quicklabpiv-ng_gb300: GB300-native FFT-PIV hot path of QuickLabPIV-ng.
+
+The compute path is libqlpiv_gpu.so (hand-written sm_103a CUDA behind the C ABI of
+include/qlpiv.h).  This package is the Python host side of that boundary: a ctypes
+binding (`Handle`) and mirrors of the reference's stage plugins (`jobs`, `grid`).
+There is no CPU fallback: without the built library every entry point raises.
+"""
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = _build.LIB
+
+# include/qlpiv.h enums
+OK, E_ARG, E_SHAPE, E_OOM, E_CUDA, E_TIMEOUT, E_CANCELLED, E_UNSUPPORTED, E_NO_DEVICE = range(9)
+PIX_U8, PIX_U16, PIX_F32 = 0, 1, 2
+NORM_MAX_A, NORM_OWN_MAX, NORM_NONE = 0, 1, 3
+MAX_COMPUTE, MAX_GIVEN, MAX_FIXED = 0, 1, 2
+SUBPIX_NONE, SUBPIX_GAUSS3 = 0, 1
+F_SUB_I, F_SUB_J, F_PARABOLIC, F_EDGE, F_NO_PEAK = 1, 2, 4, 8, 16
+
+VECTOR_DTYPE = np.dtype([
+    ("u", "<f4"), ("v", "<f4"), ("sub_i", "<f4"), ("sub_j", "<f4"),
+    ("peak_value", "<f4"), ("min_floor", "<f4"), ("peak_i", "<i2"), ("peak_j", "<i2"), ("flags", "<u4"),
+])
+assert VECTOR_DTYPE.itemsize == 32
+
+SUPPORTED_IA = (16, 32, 64)
+
+_STATUS_NAMES = {OK: "OK", E_ARG: "E_ARG", E_SHAPE: "E_SHAPE", E_OOM: "E_OOM", E_CUDA: "E_CUDA",
+                 E_TIMEOUT: "E_TIMEOUT", E_CANCELLED: "E_CANCELLED", E_UNSUPPORTED: "E_UNSUPPORTED",
+                 E_NO_DEVICE: "E_NO_DEVICE"}
+
+
+class QlpivError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{_STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class PassDesc(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("norm_mode", ctypes.c_int), ("max_mode", ctypes.c_int),
+                ("fixed_max_a", ctypes.c_float), ("fixed_max_b", ctypes.c_float), ("subpix_mode", ctypes.c_int),
+                ("reserved", ctypes.c_int * 6)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+
+
+# C ABI symbol table: name -> (restype, argtypes).  Kept beside include/qlpiv.h.
+_vp, _i, _l, _f = ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_float
+_SIGNATURES = {
+    "qlpiv_abi_version": (_i, []),
+    "qlpiv_last_error": (ctypes.c_char_p, []),
+    "qlpiv_create": (_i, [ctypes.POINTER(Params), ctypes.POINTER(_vp)]),
+    "qlpiv_destroy": (_i, [_vp]),
+    "qlpiv_synchronize": (_i, [_vp]),
+    "qlpiv_launch_count": (_l, [_vp]),
+    "qlpiv_xcorr_planes": (_i, [_vp, _i, _l, _i, _vp, _vp, _vp, _vp, _i, _vp]),
+    "qlpiv_xcorr_peaks": (_i, [_vp, _i, _l, _i, _vp, _vp, _vp, _vp, _i, _i, _vp]),
+    "qlpiv_pass": (_i, [_vp, ctypes.POINTER(PassDesc), _vp, _vp, _i, _i, _i, _l, _vp, _vp, _vp, _vp, _vp]),
+    "qlpiv_pass_device": (_i, [_vp, ctypes.POINTER(PassDesc), _vp, _vp, _i, _i, _i, _l, _vp, _vp, _vp, _vp, _vp]),
+}
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load libqlpiv_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with `python quicklabpiv-ng_gb300/build.py` "
+                           "(or __graft_entry__.build()); there is no CPU fallback")
+    lib = ctypes.CDLL(str(p))
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.qlpiv_abi_version() != 1:
+        raise RuntimeError("libqlpiv_gpu.so ABI version mismatch")
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(_SIGNATURES)
+
+
+def _check(status):
+    if status != OK:
+        raise QlpivError(status, load_library().qlpiv_last_error().decode())
+
+
+def pixel_type_of(dtype):
+    dtype = np.dtype(dtype)
+    if dtype == np.uint8:
+        return PIX_U8
+    if dtype == np.uint16:
+        return PIX_U16
+    if dtype == np.float32:
+        return PIX_F32
+    raise ValueError(f"unsupported pixel dtype {dtype}")
+
+
+def _addr(x):
+    """Address of a contiguous numpy array or torch tensor."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+class Handle:
+    """One device context of the library (qlpiv_create / qlpiv_destroy)."""
+
+    def __init__(self, device=0):
+        lib = load_library()
+        self._lib = lib
+        p = Params()
+        p.device = device
+        h = ctypes.c_void_p()
+        _check(lib.qlpiv_create(ctypes.byref(p), ctypes.byref(h)))
+        self._h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.qlpiv_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def launches(self):
+        return self._lib.qlpiv_launch_count(self._h)
+
+    def synchronize(self):
+        _check(self._lib.qlpiv_synchronize(self._h))
+
+    # -- tile API (Job<List<Tile>, XCorrelationResults>) -------------------------
+    @staticmethod
+    def _tiles(tiles_a, tiles_b):
+        ta = np.ascontiguousarray(tiles_a)
+        tb = np.ascontiguousarray(tiles_b)
+        if ta.ndim == 2:
+            ta, tb = ta[None], tb[None]
+        if ta.shape != tb.shape or ta.ndim != 3 or ta.shape[1] != ta.shape[2] or ta.dtype != tb.dtype:
+            raise ValueError("tiles must be two (count, n, n) arrays of one dtype")
+        return ta, tb
+
+    @staticmethod
+    def _maxes(max_a, max_b, count):
+        if max_a is None and max_b is None:
+            return None, None
+        ma = np.ascontiguousarray(np.broadcast_to(np.asarray(max_a, np.float32), (count,)))
+        mb = np.ascontiguousarray(np.broadcast_to(np.asarray(max_b, np.float32), (count,)))
+        return ma, mb
+
+    def xcorr_planes(self, tiles_a, tiles_b, max_a=None, max_b=None, norm_mode=NORM_MAX_A):
+        ta, tb = self._tiles(tiles_a, tiles_b)
+        count, n = ta.shape[0], ta.shape[1]
+        ma, mb = self._maxes(max_a, max_b, count)
+        d = 2 * n - 1
+        out = np.empty((count, d, d), np.float32)
+        _check(self._lib.qlpiv_xcorr_planes(self._h, n, count, pixel_type_of(ta.dtype), _addr(ta), _addr(tb),
+                                            _addr(ma), _addr(mb), norm_mode, _addr(out)))
+        return out
+
+    def xcorr_peaks(self, tiles_a, tiles_b, max_a=None, max_b=None, norm_mode=NORM_MAX_A, subpix_mode=SUBPIX_GAUSS3):
+        ta, tb = self._tiles(tiles_a, tiles_b)
+        count, n = ta.shape[0], ta.shape[1]
+        ma, mb = self._maxes(max_a, max_b, count)
+        out = np.empty(count, VECTOR_DTYPE)
+        _check(self._lib.qlpiv_xcorr_peaks(self._h, n, count, pixel_type_of(ta.dtype), _addr(ta), _addr(tb),
+                                           _addr(ma), _addr(mb), norm_mode, subpix_mode, _addr(out)))
+        return out
+
+    # -- frame API ---------------------------------------------------------------
+    @staticmethod
+    def desc(n, norm_mode=NORM_MAX_A, max_mode=MAX_COMPUTE, fixed_max=(255.0, 255.0), subpix_mode=SUBPIX_GAUSS3):
+        d = PassDesc()
+        d.n, d.norm_mode, d.max_mode = n, norm_mode, max_mode
+        d.fixed_max_a, d.fixed_max_b = fixed_max
+        d.subpix_mode = subpix_mode
+        return d
+
+    def piv_pass(self, img_a, img_b, n, a_top, a_left, b_top=None, b_left=None, **kw):
+        """One correlation pass over host images; origins per IA (int32)."""
+        ia = np.ascontiguousarray(img_a)
+        ib = np.ascontiguousarray(img_b)
+        if ia.shape != ib.shape or ia.dtype != ib.dtype or ia.ndim != 2:
+            raise ValueError("images must be two 2-D arrays of one shape and dtype")
+        at = np.ascontiguousarray(a_top, np.int32)
+        al = np.ascontiguousarray(a_left, np.int32)
+        bt = at if b_top is None else np.ascontiguousarray(b_top, np.int32)
+        bl = al if b_left is None else np.ascontiguousarray(b_left, np.int32)
+        count = at.shape[0]
+        if not (al.shape[0] == bt.shape[0] == bl.shape[0] == count):
+            raise ValueError("origin arrays differ in length")
+        out = np.empty(count, VECTOR_DTYPE)
+        d = self.desc(n, **kw)
+        _check(self._lib.qlpiv_pass(self._h, ctypes.byref(d), _addr(ia), _addr(ib), ia.shape[0], ia.shape[1],
+                                    pixel_type_of(ia.dtype), count, _addr(at), _addr(al), _addr(bt), _addr(bl),
+                                    _addr(out)))
+        return out
+
+    def piv_pass_device(self, img_a, img_b, height, width, pixel_type, n, count, a_top, a_left, b_top, b_left, out,
+                        **kw):
+        """Queue one pass on device-resident buffers (torch tensors or raw addresses);
+        does not wait."""
+        d = self.desc(n, **kw)
+        a = [x if isinstance(x, int) else _addr(x) for x in (img_a, img_b, a_top, a_left, b_top, b_left, out)]
+        _check(self._lib.qlpiv_pass_device(self._h, ctypes.byref(d), a[0], a[1], height, width, pixel_type, count,
+                                           a[2], a[3], a[4], a[5], a[6]))
+
+
+from . import grid, jobs, synth  # noqa: E402,F401

@@ -1,0 +1,344 @@
+// C ABI of libqlpiv_gpu.so: handles, workspace, argument checking, transfers.
+// Declarations and reference citations: include/qlpiv.h.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "qlpiv_internal.h"
+#include "qlpiv_xcorr.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+qlpiv_status fail(qlpiv_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+qlpiv_status cuda_fail(cudaError_t e, const char *what) {
+    if (e == cudaErrorMemoryAllocation) return fail(QLPIV_E_OOM, "%s: %s", what, cudaGetErrorString(e));
+    return fail(QLPIV_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Device buffer that only grows.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes < 256 ? 256 : bytes;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+struct qlpiv_handle {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    long launches = 0;
+    DevBuf tiles_a, tiles_b, max_a, max_b, origins, vectors, planes;
+};
+
+namespace {
+
+// Makes the handle's device current for the calling thread and restores the previous
+// device on scope exit.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceScope(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) err = cudaSetDevice(dev);
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+qlpiv_status check_desc(const qlpiv_pass_desc *d) {
+    if (!d) return fail(QLPIV_E_ARG, "pass descriptor is NULL");
+    if (!qlpiv::xcorr_size_supported(d->n))
+        return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64)", d->n);
+    if (d->norm_mode != QLPIV_NORM_MAX_A && d->norm_mode != QLPIV_NORM_OWN_MAX && d->norm_mode != QLPIV_NORM_NONE)
+        return fail(QLPIV_E_ARG, "unknown normalisation mode %d", d->norm_mode);
+    if (d->max_mode != QLPIV_MAX_COMPUTE && d->max_mode != QLPIV_MAX_FIXED)
+        return fail(QLPIV_E_ARG, "max mode %d not valid for a frame pass", d->max_mode);
+    if (d->max_mode == QLPIV_MAX_FIXED && !(d->fixed_max_a > 0.0f && d->fixed_max_b > 0.0f))
+        return fail(QLPIV_E_ARG, "fixed tile maxima must be positive");
+    if (d->subpix_mode != QLPIV_SUBPIX_NONE && d->subpix_mode != QLPIV_SUBPIX_GAUSS3)
+        return fail(QLPIV_E_ARG, "unknown sub-pixel mode %d", d->subpix_mode);
+    return QLPIV_OK;
+}
+
+qlpiv_status check_pixel(int pixel_type) {
+    if (pixel_type != QLPIV_PIX_U8 && pixel_type != QLPIV_PIX_U16 && pixel_type != QLPIV_PIX_F32)
+        return fail(QLPIV_E_ARG, "unknown pixel type %d", pixel_type);
+    return QLPIV_OK;
+}
+
+qlpiv_status launch(qlpiv_handle *h, const qlpiv::IaJob &job, int n, int pixel_type) {
+    cudaError_t e = qlpiv::launch_xcorr(job, n, pixel_type, h->stream, h->num_sms);
+    if (e != cudaSuccess) return cuda_fail(e, "xcorr kernel launch");
+    h->launches++;
+    return QLPIV_OK;
+}
+
+// Shared body of qlpiv_xcorr_planes / qlpiv_xcorr_peaks: tiles of n x n pixels,
+// contiguous per tile, form a virtual image of count*n rows and n columns.
+qlpiv_status tiles_call(qlpiv_handle *h, int n, long count, int pixel_type, const void *ta, const void *tb,
+                        const float *max_a, const float *max_b, int norm_mode, int subpix_mode,
+                        qlpiv_vector *vec_out, float *planes_out) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    if (count < 0) return fail(QLPIV_E_ARG, "count < 0");
+    if (count == 0) return QLPIV_OK;
+    if (!ta || !tb) return fail(QLPIV_E_ARG, "tile arrays are NULL");
+    if ((max_a == nullptr) != (max_b == nullptr)) return fail(QLPIV_E_ARG, "give both tile max arrays or none");
+    if (!qlpiv::xcorr_size_supported(n)) return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64)", n);
+    qlpiv_status st = check_pixel(pixel_type);
+    if (st != QLPIV_OK) return st;
+    if (norm_mode != QLPIV_NORM_MAX_A && norm_mode != QLPIV_NORM_OWN_MAX && norm_mode != QLPIV_NORM_NONE)
+        return fail(QLPIV_E_ARG, "unknown normalisation mode %d", norm_mode);
+    if ((long)n * n * count > (1L << 31) - 1) return fail(QLPIV_E_SHAPE, "tile batch too large for one call");
+
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    const size_t tile_bytes = (size_t)n * n * qlpiv::pixel_bytes(pixel_type) * count;
+    const int d = 2 * n - 1;
+    cudaError_t e;
+    if ((e = h->tiles_a.ensure(tile_bytes)) != cudaSuccess) return cuda_fail(e, "tile buffer");
+    if ((e = h->tiles_b.ensure(tile_bytes)) != cudaSuccess) return cuda_fail(e, "tile buffer");
+    if (max_a) {
+        if ((e = h->max_a.ensure(sizeof(float) * count)) != cudaSuccess) return cuda_fail(e, "max buffer");
+        if ((e = h->max_b.ensure(sizeof(float) * count)) != cudaSuccess) return cuda_fail(e, "max buffer");
+    }
+    if ((e = h->vectors.ensure(sizeof(qlpiv_vector) * count)) != cudaSuccess) return cuda_fail(e, "vector buffer");
+    if (planes_out && (e = h->planes.ensure(sizeof(float) * (size_t)d * d * count)) != cudaSuccess)
+        return cuda_fail(e, "plane buffer");
+
+    if ((e = cudaMemcpyAsync(h->tiles_a.p, ta, tile_bytes, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(h->tiles_b.p, tb, tile_bytes, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
+        return cuda_fail(e, "tile upload");
+    if (max_a) {
+        if ((e = cudaMemcpyAsync(h->max_a.p, max_a, sizeof(float) * count, cudaMemcpyHostToDevice, h->stream)) !=
+                cudaSuccess ||
+            (e = cudaMemcpyAsync(h->max_b.p, max_b, sizeof(float) * count, cudaMemcpyHostToDevice, h->stream)) !=
+                cudaSuccess)
+            return cuda_fail(e, "max upload");
+    }
+
+    qlpiv::IaJob job{};
+    job.img_a = h->tiles_a.p;
+    job.img_b = h->tiles_b.p;
+    job.pitch_a = job.pitch_b = n;
+    job.h = (int)(count * n);
+    job.w = n;
+    job.a_top = job.a_left = job.b_top = job.b_left = nullptr;  // tile k at row k*n
+    job.max_a = max_a ? (const float *)h->max_a.p : nullptr;
+    job.max_b = max_b ? (const float *)h->max_b.p : nullptr;
+    job.count = count;
+    job.norm_mode = norm_mode;
+    job.max_mode = max_a ? QLPIV_MAX_GIVEN : QLPIV_MAX_COMPUTE;
+    job.subpix = subpix_mode == QLPIV_SUBPIX_GAUSS3;
+    job.out = (qlpiv_vector *)h->vectors.p;
+    job.planes = planes_out ? (float *)h->planes.p : nullptr;
+    if ((st = launch(h, job, n, pixel_type)) != QLPIV_OK) return st;
+
+    if (vec_out && (e = cudaMemcpyAsync(vec_out, h->vectors.p, sizeof(qlpiv_vector) * count, cudaMemcpyDeviceToHost,
+                                        h->stream)) != cudaSuccess)
+        return cuda_fail(e, "vector download");
+    if (planes_out && (e = cudaMemcpyAsync(planes_out, h->planes.p, sizeof(float) * (size_t)d * d * count,
+                                           cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess)
+        return cuda_fail(e, "plane download");
+    if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(e, "xcorr");
+    return QLPIV_OK;
+}
+
+qlpiv::IaJob frame_job(const qlpiv_pass_desc *desc, const void *img_a, const void *img_b, int height, int width,
+                       long count, const int32_t *at, const int32_t *al, const int32_t *bt, const int32_t *bl,
+                       qlpiv_vector *out) {
+    qlpiv::IaJob job{};
+    job.img_a = img_a;
+    job.img_b = img_b;
+    job.pitch_a = job.pitch_b = width;
+    job.h = height;
+    job.w = width;
+    job.a_top = at;
+    job.a_left = al;
+    job.b_top = bt;
+    job.b_left = bl;
+    job.max_a = job.max_b = nullptr;
+    job.count = count;
+    job.norm_mode = desc->norm_mode;
+    job.max_mode = desc->max_mode;
+    job.fixed_max_a = desc->fixed_max_a;
+    job.fixed_max_b = desc->fixed_max_b;
+    job.subpix = desc->subpix_mode == QLPIV_SUBPIX_GAUSS3;
+    job.out = out;
+    job.planes = nullptr;
+    return job;
+}
+
+qlpiv_status check_frame(qlpiv_handle *h, const qlpiv_pass_desc *desc, const void *img_a, const void *img_b,
+                         int height, int width, int pixel_type, long count, const int32_t *at, const int32_t *al,
+                         const int32_t *bt, const int32_t *bl, const void *out) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    qlpiv_status st = check_desc(desc);
+    if (st != QLPIV_OK) return st;
+    if ((st = check_pixel(pixel_type)) != QLPIV_OK) return st;
+    if (count < 0) return fail(QLPIV_E_ARG, "count < 0");
+    if (height <= 0 || width <= 0) return fail(QLPIV_E_SHAPE, "image size %d x %d", height, width);
+    if (count > 0 && (!img_a || !img_b || !at || !al || !bt || !bl || !out))
+        return fail(QLPIV_E_ARG, "NULL image, origin or output pointer");
+    return QLPIV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qlpiv_abi_version(void) { return QLPIV_ABI_VERSION; }
+
+const char *qlpiv_last_error(void) { return g_last_error.c_str(); }
+
+qlpiv_status qlpiv_create(const qlpiv_params *params, qlpiv_handle **out) {
+    if (!out) return fail(QLPIV_E_ARG, "output handle pointer is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return fail(QLPIV_E_NO_DEVICE, "no CUDA device (%s)", cudaGetErrorString(e));
+    const int dev = params ? params->device : 0;
+    if (dev < 0 || dev >= ndev || dev >= qlpiv::kMaxDevices) return fail(QLPIV_E_ARG, "device %d out of range", dev);
+    qlpiv_handle *h = new qlpiv_handle();
+    h->device = dev;
+    DeviceScope ds(dev);
+    if (ds.err != cudaSuccess) {
+        delete h;
+        return cuda_fail(ds.err, "cudaSetDevice");
+    }
+    if ((e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        delete h;
+        return cuda_fail(e, "handle set-up");
+    }
+    *out = h;
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_destroy(qlpiv_handle *h) {
+    if (!h) return QLPIV_OK;
+    {
+        DeviceScope ds(h->device);
+        if (h->stream) {
+            cudaStreamSynchronize(h->stream);
+            cudaStreamDestroy(h->stream);
+        }
+        for (DevBuf *b : {&h->tiles_a, &h->tiles_b, &h->max_a, &h->max_b, &h->origins, &h->vectors, &h->planes})
+            b->release();
+    }
+    delete h;
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_synchronize(qlpiv_handle *h) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    DeviceScope ds(h->device);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "synchronize");
+    return QLPIV_OK;
+}
+
+long qlpiv_launch_count(qlpiv_handle *h) { return h ? h->launches : -1; }
+
+qlpiv_status qlpiv_xcorr_planes(qlpiv_handle *h, int n, long count, int pixel_type, const void *tiles_a,
+                                const void *tiles_b, const float *max_a, const float *max_b, int norm_mode,
+                                float *planes_out) {
+    if (count > 0 && !planes_out) return fail(QLPIV_E_ARG, "planes_out is NULL");
+    return tiles_call(h, n, count, pixel_type, tiles_a, tiles_b, max_a, max_b, norm_mode, QLPIV_SUBPIX_NONE, nullptr,
+                      planes_out);
+}
+
+qlpiv_status qlpiv_xcorr_peaks(qlpiv_handle *h, int n, long count, int pixel_type, const void *tiles_a,
+                               const void *tiles_b, const float *max_a, const float *max_b, int norm_mode,
+                               int subpix_mode, qlpiv_vector *out) {
+    if (count > 0 && !out) return fail(QLPIV_E_ARG, "output vector array is NULL");
+    if (subpix_mode != QLPIV_SUBPIX_NONE && subpix_mode != QLPIV_SUBPIX_GAUSS3)
+        return fail(QLPIV_E_ARG, "unknown sub-pixel mode %d", subpix_mode);
+    return tiles_call(h, n, count, pixel_type, tiles_a, tiles_b, max_a, max_b, norm_mode, subpix_mode, out, nullptr);
+}
+
+qlpiv_status qlpiv_pass(qlpiv_handle *h, const qlpiv_pass_desc *desc, const void *img_a, const void *img_b,
+                        int height, int width, int pixel_type, long count, const int32_t *a_top,
+                        const int32_t *a_left, const int32_t *b_top, const int32_t *b_left, qlpiv_vector *out) {
+    qlpiv_status st = check_frame(h, desc, img_a, img_b, height, width, pixel_type, count, a_top, a_left, b_top,
+                                  b_left, out);
+    if (st != QLPIV_OK || count == 0) return st;
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    const size_t img_bytes = (size_t)height * width * qlpiv::pixel_bytes(pixel_type);
+    cudaError_t e;
+    if ((e = h->tiles_a.ensure(img_bytes)) != cudaSuccess || (e = h->tiles_b.ensure(img_bytes)) != cudaSuccess ||
+        (e = h->origins.ensure(sizeof(int32_t) * 4 * count)) != cudaSuccess ||
+        (e = h->vectors.ensure(sizeof(qlpiv_vector) * count)) != cudaSuccess)
+        return cuda_fail(e, "workspace");
+    int32_t *org = (int32_t *)h->origins.p;
+    if ((e = cudaMemcpyAsync(h->tiles_a.p, img_a, img_bytes, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(h->tiles_b.p, img_b, img_bytes, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(org, a_top, sizeof(int32_t) * count, cudaMemcpyHostToDevice, h->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(org + count, a_left, sizeof(int32_t) * count, cudaMemcpyHostToDevice, h->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(org + 2 * count, b_top, sizeof(int32_t) * count, cudaMemcpyHostToDevice, h->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(org + 3 * count, b_left, sizeof(int32_t) * count, cudaMemcpyHostToDevice, h->stream)) !=
+            cudaSuccess)
+        return cuda_fail(e, "upload");
+    qlpiv::IaJob job = frame_job(desc, h->tiles_a.p, h->tiles_b.p, height, width, count, org, org + count,
+                                 org + 2 * count, org + 3 * count, (qlpiv_vector *)h->vectors.p);
+    if ((st = launch(h, job, desc->n, pixel_type)) != QLPIV_OK) return st;
+    if ((e = cudaMemcpyAsync(out, h->vectors.p, sizeof(qlpiv_vector) * count, cudaMemcpyDeviceToHost, h->stream)) !=
+        cudaSuccess)
+        return cuda_fail(e, "download");
+    if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(e, "pass");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_pass_device(qlpiv_handle *h, const qlpiv_pass_desc *desc, const void *img_a,
+                               const void *img_b, int height, int width, int pixel_type, long count,
+                               const int32_t *a_top, const int32_t *a_left, const int32_t *b_top,
+                               const int32_t *b_left, qlpiv_vector *out) {
+    qlpiv_status st = check_frame(h, desc, img_a, img_b, height, width, pixel_type, count, a_top, a_left, b_top,
+                                  b_left, out);
+    if (st != QLPIV_OK || count == 0) return st;
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    qlpiv::IaJob job = frame_job(desc, img_a, img_b, height, width, count, a_top, a_left, b_top, b_left, out);
+    return launch(h, job, desc->n, pixel_type);
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+"""Host-side checks that need no GPU: the C-ABI library builds, loads and exports every
+symbol of include/qlpiv.h; host mirrors (IA grids, Job shape checks, synthetic data)
+behave like the reference."""
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_package
+
+
+@pytest.fixture(scope="module")
+def qp():
+    pkg = load_package()
+    pkg.build.build()
+    return pkg
+
+
+def header_symbols():
+    text = (ROOT / "include" / "qlpiv.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_]+\s*\*?\s*(qlpiv_[a-z_0-9]+)\s*\(", text, re.M)))
+
+
+def test_library_exports_header_symbols(qp):
+    import ctypes
+    lib = ctypes.CDLL(str(qp.LIB_PATH))
+    syms = header_symbols()
+    assert len(syms) >= 10
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert sorted(qp.exported_symbols()) == syms
+    assert qp.load_library().qlpiv_abi_version() == 1
+
+
+def test_create_without_gpu_reports_no_device(qp):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    with pytest.raises(qp.QlpivError) as ei:
+        qp.Handle(0)
+    assert ei.value.status in (qp.E_NO_DEVICE, qp.E_CUDA)
+
+
+@pytest.mark.parametrize("h,w,n,levels,ofac,margins", [
+    (512, 512, 32, 1, 0.5, (0, 0, 0, 0)),
+    (1024, 1024, 64, 3, 0.25, (0, 0, 0, 0)),
+    (139, 139, 64, 2, 1.0 / 3.0, (16, 16, 16, 16)),
+    (600, 800, 128, 4, 0.5, (3, 5, 7, 11)),
+    (2048, 1536, 16, 1, 0.75, (0, 0, 0, 0)),
+])
+def test_grid_mirror_matches_oracle(qp, oracle, h, w, n, levels, ofac, margins):
+    for lv in range(levels):
+        g = qp.grid.superposition(h, w, n, lv, ofac, margins)
+        o, tops, lefts = oracle.grid(h, w, n, lv, ofac, margins)
+        assert (g.n, g.tiles_i, g.tiles_j, g.margin_top, g.margin_bottom, g.margin_left, g.margin_right) == (
+            o["n"], o["tiles_i"], o["tiles_j"], o["margin_top"], o["margin_bottom"], o["margin_left"],
+            o["margin_right"])
+        assert (g.tops == tops).all() and (g.lefts == lefts).all()
+        g2 = qp.grid.nosuperposition(h, w, n, lv, margins)
+        o2, t2, l2 = oracle.grid(h, w, n, lv, margins=margins, superposition=False)
+        assert (g2.tiles_i, g2.tiles_j, g2.margin_top, g2.margin_left) == (o2["tiles_i"], o2["tiles_j"],
+                                                                           o2["margin_top"], o2["margin_left"])
+        assert (g2.tops == t2).all() and (g2.lefts == l2).all()
+
+
+def test_grid_rejects_bad_overlap_and_levels(qp):
+    with pytest.raises(ValueError):
+        qp.grid.superposition(512, 512, 32, 0, 0.95)
+    assert qp.grid.adaptive_levels(64, 16) == 3
+    with pytest.raises(ValueError):
+        qp.grid.adaptive_levels(48, 16)
+
+
+def test_job_analyze_shape_errors(qp):
+    J = qp.jobs
+    job = J.CrossCorrelationGpuJob()
+    t32 = J.Tile(np.zeros((32, 32), np.uint8))
+    job.setInputParameters(J.JobResultEnum.JOB_RESULT_CLIPPED_TILES_A, [t32, J.Tile(np.zeros((16, 32), np.uint8))])
+    job.setInputParameters(J.JobResultEnum.JOB_RESULT_CLIPPED_TILES_B, [t32, t32])
+    with pytest.raises(J.JobAnalyzeException, match="along I"):
+        job.analyze()
+    job.setInputParameters(J.JobResultEnum.JOB_RESULT_CLIPPED_TILES_A, [J.Tile(np.zeros((32, 16), np.uint8))] * 2)
+    job.setInputParameters(J.JobResultEnum.JOB_RESULT_CLIPPED_TILES_B, [J.Tile(np.zeros((32, 16), np.uint8))] * 2)
+    with pytest.raises(J.JobAnalyzeException, match="square"):
+        job.analyze()
+    job.setInputParameters(J.JobResultEnum.JOB_RESULT_CLIPPED_TILES_A, [t32] * 3)
+    job.setInputParameters(J.JobResultEnum.JOB_RESULT_CLIPPED_TILES_B, [t32] * 2)
+    with pytest.raises(J.JobAnalyzeException, match="number of matrices"):
+        job.analyze()
+    job.setInputParameters(J.JobResultEnum.JOB_RESULT_CLIPPED_TILES_A, [J.Tile(np.zeros((24, 24), np.uint8))])
+    job.setInputParameters(J.JobResultEnum.JOB_RESULT_CLIPPED_TILES_B, [J.Tile(np.zeros((24, 24), np.uint8))])
+    with pytest.raises(J.JobAnalyzeException, match="not supported"):
+        job.analyze()
+    job.setInputParameters(J.JobResultEnum.JOB_RESULT_CLIPPED_TILES_A, [])
+    job.analyze()   # empty input: nothing to do, like the reference
+    job.dispose()
+
+
+def test_synthetic_pair_is_seeded(qp):
+    a1, b1 = qp.synth.particle_pair((64, 80), qp.synth.Flow(vmax=2.0, rc=10.0), seed=3)
+    a2, b2 = qp.synth.particle_pair((64, 80), qp.synth.Flow(vmax=2.0, rc=10.0), seed=3)
+    a3, _ = qp.synth.particle_pair((64, 80), qp.synth.Flow(vmax=2.0, rc=10.0), seed=4)
+    assert a1.dtype == np.uint8 and (a1 == a2).all() and (b1 == b2).all() and not (a1 == a3).all()
+    a, b = qp.synth.particle_pair((64, 64), qp.synth.Flow(), bits=12, seed=1)
+    assert a.dtype == np.uint16 and a.max() < 4096 and a.max() > 255
+    f = qp.synth.Flow(vmax=4.0, rc=64.0)
+    rows, cols = np.meshgrid(np.arange(512.0), np.arange(512.0), indexing="ij")
+    dr, dc = f.displacement(rows, cols, (512, 512))
+    assert abs(np.hypot(dr, dc).max() - 4.0) < 0.05
+
+
+def test_oracle_recovers_synthetic_flow(qp, oracle):
+    """Sanity of the generator + oracle: 32 px IAs recover the vortex within 0.2 px."""
+    a, b = qp.synth.config1_pair(seed=1)
+    g = qp.grid.superposition(512, 512, 32, 0, 0.5)
+    at, al = g.origins()
+    vec = oracle.piv_pass(a, b, 32, at, al)
+    cy = at + 15.5
+    cx = al + 15.5
+    dr, dc = qp.synth.Flow(vmax=4.0, rc=64.0).displacement(cy, cx, (512, 512))
+    err = np.hypot(vec["u"] - dr, vec["v"] - dc)
+    assert np.median(err) < 0.2
