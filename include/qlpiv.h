@@ -96,6 +96,16 @@ typedef struct qlpiv_pass_desc {
     int reserved[6];
 } qlpiv_pass_desc;
 
+/* One image pair of a batch.  Pixels are row-major with `pitch` elements per row; both
+ * frames share height, width, pitch and the batch's pixel type. */
+typedef struct qlpiv_frame {
+    const void *img_a;
+    const void *img_b;
+    int32_t height;
+    int32_t width;
+    int64_t pitch;
+} qlpiv_frame;
+
 typedef struct qlpiv_params {
     int device;         /* CUDA device ordinal */
     int reserved[7];
@@ -148,6 +158,33 @@ qlpiv_status qlpiv_pass_device(qlpiv_handle *h, const qlpiv_pass_desc *desc, con
                                const void *img_b, int height, int width, int pixel_type, long count,
                                const int32_t *a_top, const int32_t *a_left, const int32_t *b_top,
                                const int32_t *b_left, qlpiv_vector *out);
+
+/* Batched pass over many image pairs of possibly different sizes (one launch for the
+ * whole flattened IA work list): IA k belongs to frames[frame_of_ia[k]].  This replaces
+ * the reference's fan-out of one job per frame pair and thread
+ * (S/InputFiles.java:215-224, S/jobs/managers/OpenClGpuManager.java:85-186).  Host
+ * variant: frames[] point to host images, all other arrays are host arrays; synchronous. */
+qlpiv_status qlpiv_pass_batch(qlpiv_handle *h, const qlpiv_pass_desc *desc, int pixel_type, int num_frames,
+                              const qlpiv_frame *frames, long count, const int32_t *frame_of_ia,
+                              const int32_t *a_top, const int32_t *a_left, const int32_t *b_top,
+                              const int32_t *b_left, qlpiv_vector *out);
+
+/* Device variant: `frames` is a device array of num_frames entries whose image pointers
+ * are device pointers; every other array is in device memory; queued on the handle's
+ * stream. */
+qlpiv_status qlpiv_pass_batch_device(qlpiv_handle *h, const qlpiv_pass_desc *desc, int pixel_type,
+                                     int num_frames, const qlpiv_frame *frames, long count,
+                                     const int32_t *frame_of_ia, const int32_t *a_top, const int32_t *a_left,
+                                     const int32_t *b_top, const int32_t *b_left, qlpiv_vector *out);
+
+/* The CUDA stream (cudaStream_t) the handle queues work on. */
+qlpiv_status qlpiv_get_stream(qlpiv_handle *h, void **stream);
+/* Queue subsequent work on a caller-owned stream (NULL restores the handle's own). */
+qlpiv_status qlpiv_set_stream(qlpiv_handle *h, void *stream);
+
+/* Instrumentation: FP32 FMA throughput of `device` measured with a short probe kernel
+ * (TFLOP/s, best of three), the compute roofline denominator of the FFT kernels. */
+qlpiv_status qlpiv_measure_fp32_peak(int device, double *tflops);
 
 /* Number of kernel launches issued by this handle since creation (instrumentation). */
 long qlpiv_launch_count(qlpiv_handle *h);

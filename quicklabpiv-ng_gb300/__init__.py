@@ -48,6 +48,15 @@ class PassDesc(ctypes.Structure):
                 ("reserved", ctypes.c_int * 6)]
 
 
+class Frame(ctypes.Structure):
+    _fields_ = [("img_a", ctypes.c_void_p), ("img_b", ctypes.c_void_p), ("height", ctypes.c_int32),
+                ("width", ctypes.c_int32), ("pitch", ctypes.c_int64)]
+
+
+FRAME_DTYPE = np.dtype([("img_a", "<u8"), ("img_b", "<u8"), ("height", "<i4"), ("width", "<i4"), ("pitch", "<i8")])
+assert FRAME_DTYPE.itemsize == 32
+
+
 class Params(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
@@ -65,6 +74,11 @@ _SIGNATURES = {
     "qlpiv_xcorr_peaks": (_i, [_vp, _i, _l, _i, _vp, _vp, _vp, _vp, _i, _i, _vp]),
     "qlpiv_pass": (_i, [_vp, ctypes.POINTER(PassDesc), _vp, _vp, _i, _i, _i, _l, _vp, _vp, _vp, _vp, _vp]),
     "qlpiv_pass_device": (_i, [_vp, ctypes.POINTER(PassDesc), _vp, _vp, _i, _i, _i, _l, _vp, _vp, _vp, _vp, _vp]),
+    "qlpiv_pass_batch": (_i, [_vp, ctypes.POINTER(PassDesc), _i, _i, _vp, _l, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "qlpiv_pass_batch_device": (_i, [_vp, ctypes.POINTER(PassDesc), _i, _i, _vp, _l, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "qlpiv_get_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
+    "qlpiv_set_stream": (_i, [_vp, _vp]),
+    "qlpiv_measure_fp32_peak": (_i, [_i, ctypes.POINTER(ctypes.c_double)]),
 }
 
 _lib = None
@@ -98,6 +112,13 @@ def exported_symbols():
 def _check(status):
     if status != OK:
         raise QlpivError(status, load_library().qlpiv_last_error().decode())
+
+
+def measure_fp32_peak(device=0):
+    """Live FP32 FMA throughput (TFLOP/s) of the device."""
+    t = ctypes.c_double()
+    _check(load_library().qlpiv_measure_fp32_peak(device, ctypes.byref(t)))
+    return t.value
 
 
 def pixel_type_of(dtype):
@@ -156,6 +177,16 @@ class Handle:
 
     def synchronize(self):
         _check(self._lib.qlpiv_synchronize(self._h))
+
+    @property
+    def stream(self):
+        """cudaStream_t (as an int) the handle queues work on."""
+        s = ctypes.c_void_p()
+        _check(self._lib.qlpiv_get_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    def set_stream(self, stream):
+        _check(self._lib.qlpiv_set_stream(self._h, stream))
 
     # -- tile API (Job<List<Tile>, XCorrelationResults>) -------------------------
     @staticmethod
@@ -232,6 +263,37 @@ class Handle:
         a = [x if isinstance(x, int) else _addr(x) for x in (img_a, img_b, a_top, a_left, b_top, b_left, out)]
         _check(self._lib.qlpiv_pass_device(self._h, ctypes.byref(d), a[0], a[1], height, width, pixel_type, count,
                                            a[2], a[3], a[4], a[5], a[6]))
+
+    def piv_pass_batch(self, frames_a, frames_b, n, frame_of_ia, a_top, a_left, b_top=None, b_left=None, **kw):
+        """Batched pass over host image pairs (lists of 2-D arrays, sizes may differ)."""
+        if len(frames_a) != len(frames_b):
+            raise ValueError("frames_a and frames_b differ in length")
+        fa = [np.ascontiguousarray(x) for x in frames_a]
+        fb = [np.ascontiguousarray(x) for x in frames_b]
+        dt = fa[0].dtype
+        table = (Frame * len(fa))()
+        for k, (x, y) in enumerate(zip(fa, fb)):
+            if x.shape != y.shape or x.dtype != dt or y.dtype != dt:
+                raise ValueError("all frames must share the pixel dtype and pair shapes must match")
+            table[k] = Frame(x.ctypes.data, y.ctypes.data, x.shape[0], x.shape[1], x.shape[1])
+        fi = np.ascontiguousarray(frame_of_ia, np.int32)
+        at = np.ascontiguousarray(a_top, np.int32)
+        al = np.ascontiguousarray(a_left, np.int32)
+        bt = at if b_top is None else np.ascontiguousarray(b_top, np.int32)
+        bl = al if b_left is None else np.ascontiguousarray(b_left, np.int32)
+        out = np.empty(len(at), VECTOR_DTYPE)
+        d = self.desc(n, **kw)
+        _check(self._lib.qlpiv_pass_batch(self._h, ctypes.byref(d), pixel_type_of(dt), len(fa), table, len(at),
+                                          _addr(fi), _addr(at), _addr(al), _addr(bt), _addr(bl), _addr(out)))
+        return out
+
+    def piv_pass_batch_device(self, pixel_type, num_frames, frames, n, count, frame_of_ia, a_top, a_left, b_top,
+                              b_left, out, **kw):
+        """Queue a batched pass; every argument is a device buffer (torch tensor or address)."""
+        d = self.desc(n, **kw)
+        a = [x if isinstance(x, int) else _addr(x) for x in (frames, frame_of_ia, a_top, a_left, b_top, b_left, out)]
+        _check(self._lib.qlpiv_pass_batch_device(self._h, ctypes.byref(d), pixel_type, num_frames, a[0], count, a[1],
+                                                 a[2], a[3], a[4], a[5], a[6]))
 
 
 from . import grid, jobs, synth  # noqa: E402,F401

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "qlpiv_internal.h"
 #include "qlpiv_xcorr.cuh"
@@ -56,10 +57,11 @@ struct DevBuf {
 struct qlpiv_handle {
     int device = 0;
     int num_sms = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;       // stream work is queued on
+    cudaStream_t own_stream = nullptr;   // the handle's own non-blocking stream
     std::mutex mu;
     long launches = 0;
-    DevBuf tiles_a, tiles_b, max_a, max_b, origins, vectors, planes;
+    DevBuf tiles_a, tiles_b, max_a, max_b, origins, vectors, planes, frames;
 };
 
 namespace {
@@ -156,6 +158,8 @@ qlpiv_status tiles_call(qlpiv_handle *h, int n, long count, int pixel_type, cons
     job.pitch_a = job.pitch_b = n;
     job.h = (int)(count * n);
     job.w = n;
+    job.frames = nullptr;
+    job.frame_idx = nullptr;
     job.a_top = job.a_left = job.b_top = job.b_left = nullptr;  // tile k at row k*n
     job.max_a = max_a ? (const float *)h->max_a.p : nullptr;
     job.max_b = max_b ? (const float *)h->max_b.p : nullptr;
@@ -186,6 +190,8 @@ qlpiv::IaJob frame_job(const qlpiv_pass_desc *desc, const void *img_a, const voi
     job.pitch_a = job.pitch_b = width;
     job.h = height;
     job.w = width;
+    job.frames = nullptr;
+    job.frame_idx = nullptr;
     job.a_top = at;
     job.a_left = al;
     job.b_top = bt;
@@ -216,6 +222,29 @@ qlpiv_status check_frame(qlpiv_handle *h, const qlpiv_pass_desc *desc, const voi
     return QLPIV_OK;
 }
 
+
+qlpiv_status check_batch(qlpiv_handle *h, const qlpiv_pass_desc *desc, int pixel_type, int num_frames,
+                         const qlpiv_frame *frames, long count, const int32_t *fi, const int32_t *at,
+                         const int32_t *al, const int32_t *bt, const int32_t *bl, const void *out) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    qlpiv_status st = check_desc(desc);
+    if (st != QLPIV_OK) return st;
+    if ((st = check_pixel(pixel_type)) != QLPIV_OK) return st;
+    if (count < 0 || num_frames < 0) return fail(QLPIV_E_ARG, "negative count");
+    if (count > 0 && (num_frames == 0 || !frames || !fi || !at || !al || !bt || !bl || !out))
+        return fail(QLPIV_E_ARG, "NULL frame table, work list or output pointer");
+    return QLPIV_OK;
+}
+
+qlpiv::IaJob batch_job(const qlpiv_pass_desc *desc, const qlpiv_frame *frames_dev, long count, const int32_t *fi,
+                       const int32_t *at, const int32_t *al, const int32_t *bt, const int32_t *bl,
+                       qlpiv_vector *out) {
+    qlpiv::IaJob job = frame_job(desc, nullptr, nullptr, 0, 0, count, at, al, bt, bl, out);
+    job.frames = frames_dev;
+    job.frame_idx = fi;
+    return job;
+}
+
 }  // namespace
 
 extern "C" {
@@ -240,10 +269,11 @@ qlpiv_status qlpiv_create(const qlpiv_params *params, qlpiv_handle **out) {
         return cuda_fail(ds.err, "cudaSetDevice");
     }
     if ((e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        (e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking)) != cudaSuccess) {
         delete h;
         return cuda_fail(e, "handle set-up");
     }
+    h->stream = h->own_stream;
     *out = h;
     return QLPIV_OK;
 }
@@ -252,11 +282,13 @@ qlpiv_status qlpiv_destroy(qlpiv_handle *h) {
     if (!h) return QLPIV_OK;
     {
         DeviceScope ds(h->device);
-        if (h->stream) {
-            cudaStreamSynchronize(h->stream);
-            cudaStreamDestroy(h->stream);
+        if (h->stream) cudaStreamSynchronize(h->stream);
+        if (h->own_stream) {
+            cudaStreamSynchronize(h->own_stream);
+            cudaStreamDestroy(h->own_stream);
         }
-        for (DevBuf *b : {&h->tiles_a, &h->tiles_b, &h->max_a, &h->max_b, &h->origins, &h->vectors, &h->planes})
+        for (DevBuf *b : {&h->tiles_a, &h->tiles_b, &h->max_a, &h->max_b, &h->origins, &h->vectors, &h->planes,
+                          &h->frames})
             b->release();
     }
     delete h;
@@ -339,6 +371,94 @@ qlpiv_status qlpiv_pass_device(qlpiv_handle *h, const qlpiv_pass_desc *desc, con
     if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
     qlpiv::IaJob job = frame_job(desc, img_a, img_b, height, width, count, a_top, a_left, b_top, b_left, out);
     return launch(h, job, desc->n, pixel_type);
+}
+
+qlpiv_status qlpiv_pass_batch(qlpiv_handle *h, const qlpiv_pass_desc *desc, int pixel_type, int num_frames,
+                              const qlpiv_frame *frames, long count, const int32_t *frame_of_ia,
+                              const int32_t *a_top, const int32_t *a_left, const int32_t *b_top,
+                              const int32_t *b_left, qlpiv_vector *out) {
+    qlpiv_status st = check_batch(h, desc, pixel_type, num_frames, frames, count, frame_of_ia, a_top, a_left, b_top,
+                                  b_left, out);
+    if (st != QLPIV_OK || count == 0) return st;
+    const size_t pb = qlpiv::pixel_bytes(pixel_type);
+    size_t total = 0;
+    for (int f = 0; f < num_frames; f++) {
+        const qlpiv_frame &fr = frames[f];
+        if (fr.height <= 0 || fr.width <= 0 || fr.pitch < fr.width || !fr.img_a || !fr.img_b)
+            return fail(QLPIV_E_SHAPE, "frame %d: bad geometry or NULL image", f);
+        total += 2 * (((size_t)fr.height * fr.width * pb + 255) & ~(size_t)255);
+    }
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaError_t e;
+    if ((e = h->tiles_a.ensure(total)) != cudaSuccess || (e = h->frames.ensure(sizeof(qlpiv_frame) * num_frames)) !=
+        cudaSuccess || (e = h->origins.ensure(sizeof(int32_t) * 5 * count)) != cudaSuccess ||
+        (e = h->vectors.ensure(sizeof(qlpiv_vector) * count)) != cudaSuccess)
+        return cuda_fail(e, "workspace");
+    // pack the images densely (pitch = width) and rebuild the frame table for the device
+    std::vector<qlpiv_frame> dev_frames(num_frames);
+    char *base = (char *)h->tiles_a.p;
+    size_t off = 0;
+    for (int f = 0; f < num_frames; f++) {
+        const qlpiv_frame &fr = frames[f];
+        const size_t row = (size_t)fr.width * pb, bytes = row * fr.height;
+        char *da = base + off;
+        off += (bytes + 255) & ~(size_t)255;
+        char *db = base + off;
+        off += (bytes + 255) & ~(size_t)255;
+        if ((e = cudaMemcpy2DAsync(da, row, fr.img_a, (size_t)fr.pitch * pb, row, fr.height, cudaMemcpyHostToDevice,
+                                   h->stream)) != cudaSuccess ||
+            (e = cudaMemcpy2DAsync(db, row, fr.img_b, (size_t)fr.pitch * pb, row, fr.height, cudaMemcpyHostToDevice,
+                                   h->stream)) != cudaSuccess)
+            return cuda_fail(e, "frame upload");
+        dev_frames[f] = {da, db, fr.height, fr.width, (int64_t)fr.width};
+    }
+    int32_t *org = (int32_t *)h->origins.p;
+    const int32_t *src[5] = {frame_of_ia, a_top, a_left, b_top, b_left};
+    for (int k = 0; k < 5; k++)
+        if ((e = cudaMemcpyAsync(org + k * count, src[k], sizeof(int32_t) * count, cudaMemcpyHostToDevice,
+                                 h->stream)) != cudaSuccess)
+            return cuda_fail(e, "work list upload");
+    if ((e = cudaMemcpyAsync(h->frames.p, dev_frames.data(), sizeof(qlpiv_frame) * num_frames,
+                             cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
+        return cuda_fail(e, "frame table upload");
+    qlpiv::IaJob job = batch_job(desc, (const qlpiv_frame *)h->frames.p, count, org, org + count, org + 2 * count,
+                                 org + 3 * count, org + 4 * count, (qlpiv_vector *)h->vectors.p);
+    if ((st = launch(h, job, desc->n, pixel_type)) != QLPIV_OK) return st;
+    if ((e = cudaMemcpyAsync(out, h->vectors.p, sizeof(qlpiv_vector) * count, cudaMemcpyDeviceToHost, h->stream)) !=
+        cudaSuccess)
+        return cuda_fail(e, "download");
+    // the frame table lives in pageable host memory: wait before it goes out of scope
+    if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(e, "batch pass");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_pass_batch_device(qlpiv_handle *h, const qlpiv_pass_desc *desc, int pixel_type,
+                                     int num_frames, const qlpiv_frame *frames, long count,
+                                     const int32_t *frame_of_ia, const int32_t *a_top, const int32_t *a_left,
+                                     const int32_t *b_top, const int32_t *b_left, qlpiv_vector *out) {
+    qlpiv_status st = check_batch(h, desc, pixel_type, num_frames, frames, count, frame_of_ia, a_top, a_left, b_top,
+                                  b_left, out);
+    if (st != QLPIV_OK || count == 0) return st;
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    qlpiv::IaJob job = batch_job(desc, frames, count, frame_of_ia, a_top, a_left, b_top, b_left, out);
+    return launch(h, job, desc->n, pixel_type);
+}
+
+qlpiv_status qlpiv_get_stream(qlpiv_handle *h, void **stream) {
+    if (!h || !stream) return fail(QLPIV_E_ARG, "NULL argument");
+    *stream = (void *)h->stream;
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_set_stream(qlpiv_handle *h, void *stream) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lock(h->mu);
+    h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+    return QLPIV_OK;
 }
 
 }  // extern "C"

@@ -79,6 +79,8 @@ struct IaJob {
     const void *img_a, *img_b;   // pixel planes (Pix), row pitch in elements
     long pitch_a, pitch_b;
     int h, w;
+    const qlpiv_frame *frames;   // batched: per-IA frame table entry (NULL: img_a/img_b)
+    const int *frame_idx;
     const int *a_top, *a_left, *b_top, *b_left;  // per IA origins
     const float *max_a, *max_b;  // per IA maxima (max_mode == QLPIV_MAX_GIVEN)
     long count;
@@ -115,10 +117,25 @@ xcorr_kernel(IaJob job) {
     }
     __syncthreads();
 
-    const Pix *imgA = reinterpret_cast<const Pix *>(job.img_a);
-    const Pix *imgB = reinterpret_cast<const Pix *>(job.img_b);
-
     for (long ia = blockIdx.x; ia < job.count; ia += gridDim.x) {
+        const Pix *imgA, *imgB;
+        long pitch_a, pitch_b;
+        int img_h, img_w;
+        if (job.frames != nullptr) {
+            const qlpiv_frame fr = job.frames[job.frame_idx[ia]];
+            imgA = reinterpret_cast<const Pix *>(fr.img_a);
+            imgB = reinterpret_cast<const Pix *>(fr.img_b);
+            pitch_a = pitch_b = (long)fr.pitch;
+            img_h = fr.height;
+            img_w = fr.width;
+        } else {
+            imgA = reinterpret_cast<const Pix *>(job.img_a);
+            imgB = reinterpret_cast<const Pix *>(job.img_b);
+            pitch_a = job.pitch_a;
+            pitch_b = job.pitch_b;
+            img_h = job.h;
+            img_w = job.w;
+        }
         int at, al, bt, bl;
         if (job.a_top != nullptr) {
             at = job.a_top[ia]; al = job.a_left[ia];
@@ -137,8 +154,8 @@ xcorr_kernel(IaJob job) {
 #pragma unroll
             for (int m = 0; m < 4; m++) {
                 const int n2 = g + G * m;
-                ra[r][m] = load_pix(imgA, job.pitch_a, job.h, job.w, at + (N - 1 - n1), al + (N - 1 - n2));
-                rb[r][m] = load_pix(imgB, job.pitch_b, job.h, job.w, bt + n1, bl + n2);
+                ra[r][m] = load_pix(imgA, pitch_a, img_h, img_w, at + (N - 1 - n1), al + (N - 1 - n2));
+                rb[r][m] = load_pix(imgB, pitch_b, img_h, img_w, bt + n1, bl + n2);
                 mxa = fmaxf(mxa, ra[r][m]);
                 mxb = fmaxf(mxb, rb[r][m]);
             }

@@ -225,3 +225,33 @@ def test_device_resident_pass(qp, handle):
     handle.synchronize()
     res = np.frombuffer(out.cpu().numpy().tobytes(), qp.VECTOR_DTYPE)
     assert res.tobytes() == host.tobytes()
+
+
+def test_batched_frames_equal_single_passes(qp, handle):
+    """A flattened work list over pairs of different sizes gives, IA by IA, exactly the
+    vectors of the per-pair calls (deterministic per-IA computation)."""
+    shapes = [(256, 256), (300, 200), (128, 512)]
+    pairs = [qp.synth.particle_pair(s, qp.synth.Flow(vmax=3.0, rc=30.0), seed=20 + k) for k, s in enumerate(shapes)]
+    fi, at, al, singles = [], [], [], []
+    for k, (a, b) in enumerate(pairs):
+        g = qp.grid.superposition(a.shape[0], a.shape[1], 32, 0, 0.5)
+        t, l = g.origins()
+        fi.append(np.full(len(t), k, np.int32))
+        at.append(t)
+        al.append(l)
+        singles.append(handle.piv_pass(a, b, 32, t, l))
+    fi, at, al = np.concatenate(fi), np.concatenate(at), np.concatenate(al)
+    batch = handle.piv_pass_batch([p[0] for p in pairs], [p[1] for p in pairs], 32, fi, at, al)
+    assert batch.tobytes() == np.concatenate(singles).tobytes()
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    keep = [(torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)) for a, b in pairs]
+    table = np.zeros(len(pairs), qp.FRAME_DTYPE)
+    for k, (ta, tb) in enumerate(keep):
+        table[k] = (ta.data_ptr(), tb.data_ptr(), ta.shape[0], ta.shape[1], ta.shape[1])
+    ttab = torch.from_numpy(table.view(np.uint8)).to(dev)
+    wl = [torch.from_numpy(x).to(dev) for x in (fi, at, al)]
+    out = torch.empty(len(at) * 32, dtype=torch.uint8, device=dev)
+    handle.piv_pass_batch_device(qp.PIX_U8, len(pairs), ttab, 32, len(at), wl[0], wl[1], wl[2], wl[1], wl[2], out)
+    handle.synchronize()
+    assert out.cpu().numpy().tobytes() == batch.tobytes()
