@@ -106,6 +106,34 @@ typedef struct qlpiv_frame {
     int64_t pitch;
 } qlpiv_frame;
 
+/* Geometry of one adaptive level's IA grid (IterationStepTiles). */
+typedef struct qlpiv_grid {
+    int n;            /* IA side */
+    int tiles_i, tiles_j;
+    int margin_top, margin_left, margin_bottom, margin_right;
+} qlpiv_grid;
+
+typedef enum {
+    QLPIV_WARP_NONE = 0,          /* NoImageWarping: B tiles at round(origin + displacement) */
+    QLPIV_WARP_BOTH_BILINEAR = 1  /* BothImagesBiLinearWarping (BiLinearImageWarpingStrategy) */
+} qlpiv_warp_mode;
+
+/* Adaptive multi-pass PIV parameters (PIVInputParameters fields of the path). */
+typedef struct qlpiv_adaptive_desc {
+    int ia_start;          /* IA side of the first level (getInterrogationAreaStartIPixels) */
+    int ia_end;            /* IA side of the last level; ia_start / ia_end a power of two */
+    float overlap_factor;  /* 1 - overlap% / 100, in [0.1, 0.9] (SuperPosition division) */
+    int margins[4];        /* top, bottom, left, right */
+    int warp_mode;         /* qlpiv_warp_mode */
+    int norm_mode;         /* qlpiv_norm */
+    int max_mode;          /* QLPIV_MAX_COMPUTE or QLPIV_MAX_FIXED */
+    float fixed_max;       /* QLPIV_MAX_FIXED tile max, 0 = full scale (255 / 65535) */
+    int subpix_mode;       /* qlpiv_subpix */
+    int int16_warp_quirk;  /* 1: store warped 16-bit pixels through a signed byte like
+                              MatrixInt16.setElement(float) (S/MatrixInt16.java:95-101) */
+    int reserved[8];
+} qlpiv_adaptive_desc;
+
 typedef struct qlpiv_params {
     int device;         /* CUDA device ordinal */
     int reserved[7];
@@ -181,6 +209,56 @@ qlpiv_status qlpiv_pass_batch_device(qlpiv_handle *h, const qlpiv_pass_desc *des
 qlpiv_status qlpiv_get_stream(qlpiv_handle *h, void **stream);
 /* Queue subsequent work on a caller-owned stream (NULL restores the handle's own). */
 qlpiv_status qlpiv_set_stream(qlpiv_handle *h, void *stream);
+
+/* IA grid of one level: AdaptiveInterAreaStrategySuperPosition / NoSuperPosition
+ * (S/iareas/AdaptiveInterAreaStrategySuperPosition.java:31-197,
+ *  S/iareas/AdaptiveInterAreaStrategyNoSuperPosition.java:32-157).  margins = top, bottom,
+ * left, right.  tops/lefts (capacity `cap`) may be NULL to query the size only.  Host only. */
+qlpiv_status qlpiv_grid_superposition(int height, int width, const int margins[4], int ia_start, int level,
+                                      float overlap_factor, qlpiv_grid *grid, int32_t *tops, int32_t *lefts,
+                                      int cap);
+qlpiv_status qlpiv_grid_nosuperposition(int height, int width, const int margins[4], int ia_start, int level,
+                                        qlpiv_grid *grid, int32_t *tops, int32_t *lefts, int cap);
+
+/* Number of adaptive levels and the grid of each (`grids` may be NULL).  Host only. */
+qlpiv_status qlpiv_adaptive_levels(const qlpiv_adaptive_desc *desc, int height, int width, int *levels,
+                                   qlpiv_grid *grids, int max_levels);
+
+/* Velocity inheritance between levels, IterationStepTiles.reuseTiles with the
+ * BiCubicSpline strategy (S/iareas/AdaptiveInterVelocityInheritanceStrategyBiCubicSpline.java:27-136):
+ * parent displacements pu/pv (pni x pnj) at parent centres p_ci/p_cj, child centres
+ * c_ci/c_cj (float, top + N/2 - 0.5); round_int for non-warping modes.  Host arrays. */
+qlpiv_status qlpiv_inherit(qlpiv_handle *h, int pni, int pnj, const double *p_ci, const double *p_cj, const float *pu,
+                           const float *pv, int cni, int cnj, const float *c_ci, const float *c_cj, int round_int,
+                           float *cu, float *cv);
+
+/* Per-pixel displacement field of a level (BiCubicSplineInterpolatorWithBiLinearBackup.
+ * interpolateDisplacements, S/iareas/BiCubicSplineInterpolatorWithBiLinearBackup.java:57-107):
+ * tile displacements u/v (ni x nj) at centres ci/cj -> fu/fv (height x width).  Host arrays. */
+qlpiv_status qlpiv_displacement_field(qlpiv_handle *h, int height, int width, int ni, int nj, const double *ci,
+                                      const double *cj, const float *u, const float *v, float *fu, float *fv);
+
+/* IImageWarpingStrategy.warpAndClipImage for BothImages bilinear warping
+ * (S/images/BiLinearImageWarpingStrategy.java:38-265): both images warped by half the
+ * field through the level's tile displacements.  Host arrays, out_a/out_b as the input
+ * pixel type (u8 or u16). */
+qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, const void *img_a, const void *img_b, int height,
+                             int width, int ni, int nj, const double *ci, const double *cj, const float *u,
+                             const float *v, int int16_quirk, void *out_a, void *out_b);
+
+/* Whole adaptive PIV of num_pairs image pairs of one size (LocalPIVOpenCLGpuJob's level
+ * loop, S/jobs/LocalPIVOpenCLGpuJob.java:188-411, SimpleStrategy, no validation):
+ * per level grid -> inheritance -> warp/clip -> xcorr + peak + sub-pixel -> accumulate,
+ * all on the device.  frames[] are host images (pitch in elements); out_u/out_v receive
+ * num_pairs x (tiles_i x tiles_j) displacements of the last level (rows, columns). */
+qlpiv_status qlpiv_piv_adaptive(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int pixel_type, int height,
+                                int width, int num_pairs, const qlpiv_frame *frames, float *out_u, float *out_v);
+
+/* Device variant: frames is a device frame table, out_u/out_v device buffers; queued
+ * on the handle's stream. */
+qlpiv_status qlpiv_piv_adaptive_device(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int pixel_type, int height,
+                                       int width, int num_pairs, const qlpiv_frame *frames, float *out_u,
+                                       float *out_v);
 
 /* Instrumentation: FP32 FMA throughput of `device` measured with a short probe kernel
  * (TFLOP/s, best of three), the compute roofline denominator of the FFT kernels. */

@@ -31,7 +31,7 @@ _lib = None
 
 def build(force=False):
     """Compile the oracle with its Makefile (gcc only; seconds)."""
-    src = [HERE / "qlpiv_oracle.c", HERE / "oracle_impl.h"]
+    src = [HERE / "qlpiv_oracle.c", HERE / "qlpiv_oracle_adaptive.c", HERE / "oracle_impl.h", HERE / "Makefile"]
     if not force and LIB_PATH.exists() and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in src):
         return LIB_PATH
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
@@ -61,6 +61,11 @@ def lib():
         L.orc_grid_nosuperposition.argtypes = [c_int] * 8 + [vp, ip, ip, c_int]
         L.orc_piv_pass.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_long, ip, ip, ip, ip, c_int,
                                    c_float, c_float, c_int, c_int, vp, c_int]
+        L.orc_displacement_field.argtypes = [dp, c_int, dp, c_int, fp, fp, c_int, c_int, fp, fp]
+        L.orc_warp_both.argtypes = [vp, vp, c_int, c_int, c_int, fp, fp, c_int, vp, vp]
+        L.orc_inherit.argtypes = [dp, c_int, dp, c_int, fp, fp, fp, c_int, fp, c_int, c_int, fp, fp]
+        L.orc_piv_adaptive.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_float,
+                                       c_int, c_int, c_int, fp, fp, ip, ip, vp]
         L.orc_vector_size.restype = c_int
         assert L.orc_vector_size() == VECTOR_DTYPE.itemsize
         _lib = L
@@ -191,3 +196,70 @@ def grid_origins(h, w, n, overlap_factor=0.5, level=0, n_start=None, margins=(0,
     g, tops, lefts = grid(h, w, n if n_start is None else n_start, level, overlap_factor, margins, superposition)
     tt, ll = np.meshgrid(tops, lefts, indexing="ij")
     return g, tt.ravel().astype(np.int32), ll.ravel().astype(np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def displacement_field(ys, xs, u, v, h, w):
+    """Per-pixel (u, v) from tile displacements at tile centres (bicubic spline)."""
+    ys, xs = _f64(ys), _f64(xs)
+    u, v = _f32(u), _f32(v)
+    fu = np.zeros((h, w), np.float32)
+    fv = np.zeros((h, w), np.float32)
+    lib().orc_displacement_field(_ptr(ys, ctypes.c_double), len(ys), _ptr(xs, ctypes.c_double), len(xs),
+                                 _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), h, w, _ptr(fu, ctypes.c_float),
+                                 _ptr(fv, ctypes.c_float))
+    return fu, fv
+
+
+def warp_both(img_a, img_b, fu, fv, int16_quirk=False):
+    img_a, img_b = np.ascontiguousarray(img_a), np.ascontiguousarray(img_b)
+    fu, fv = _f32(fu), _f32(fv)
+    oa, ob = np.zeros_like(img_a), np.zeros_like(img_b)
+    lib().orc_warp_both(img_a.ctypes.data, img_b.ctypes.data, img_a.shape[0], img_a.shape[1], img_a.dtype.itemsize,
+                        _ptr(fu, ctypes.c_float), _ptr(fv, ctypes.c_float), int(int16_quirk), oa.ctypes.data,
+                        ob.ctypes.data)
+    return oa, ob
+
+
+def inherit(py, px, pu, pv, cy, cx, round_int=False):
+    py, px = _f64(py), _f64(px)
+    pu, pv, cy, cx = _f32(pu), _f32(pv), _f32(cy), _f32(cx)
+    cu = np.zeros((len(cy), len(cx)), np.float32)
+    cv = np.zeros((len(cy), len(cx)), np.float32)
+    lib().orc_inherit(_ptr(py, ctypes.c_double), len(py), _ptr(px, ctypes.c_double), len(px), _ptr(pu, ctypes.c_float),
+                      _ptr(pv, ctypes.c_float), _ptr(cy, ctypes.c_float), len(cy), _ptr(cx, ctypes.c_float), len(cx),
+                      int(round_int), _ptr(cu, ctypes.c_float), _ptr(cv, ctypes.c_float))
+    return cu, cv
+
+
+def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MAX_A, fixed_max=None,
+                 int16_quirk=False, precision=32, nthreads=None, return_levels=False, warp=True):
+    """Adaptive multi-pass PIV (BothImages bilinear warping, or none); returns (u, v) of
+    the last level, shaped (tiles_i, tiles_j), and optionally all levels' vectors."""
+    img_a, img_b = np.ascontiguousarray(img_a), np.ascontiguousarray(img_b)
+    h, w = img_a.shape
+    cap = 65536 * 16
+    u = np.zeros(cap, np.float32)
+    v = np.zeros(cap, np.float32)
+    ni, nj = ctypes.c_int(), ctypes.c_int()
+    total = 0
+    lv, n = 0, n_start
+    while n >= n_end:
+        g, _, _ = grid(h, w, n_start, lv, overlap_factor)
+        total += g["tiles_i"] * g["tiles_j"]
+        n >>= 1
+        lv += 1
+    vec = np.zeros(total, VECTOR_DTYPE) if return_levels else None
+    rc = lib().orc_piv_adaptive(img_a.ctypes.data, img_b.ctypes.data, h, w, img_a.dtype.itemsize, n_start, n_end,
+                                overlap_factor, int(warp), norm_mode, float(fixed_max or 0.0), int(int16_quirk),
+                                0 if precision == 32 else 1, nthreads or (os.cpu_count() or 1),
+                                _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), ctypes.byref(ni), ctypes.byref(nj),
+                                vec.ctypes.data if vec is not None else None)
+    if rc != 0:
+        raise ValueError("adaptive PIV failed")
+    shape = (ni.value, nj.value)
+    out = (u[:ni.value * nj.value].reshape(shape).copy(), v[:ni.value * nj.value].reshape(shape).copy())
+    return (out, vec) if return_levels else out

@@ -1,0 +1,418 @@
+/*
+ * qlpiv oracle, adaptive multi-pass stages -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Restates, from the reference sources and the published mathematics of the
+ * third-party routines they call (commons-math3 3.6.1 is not part of the reference
+ * tree, so its interpolators are written here from their mathematical definitions):
+ *
+ *  B-field   BiCubicSplineInterpolatorWithBiLinearBackup.interpolateDisplacements
+ *            (S/iareas/BiCubicSplineInterpolatorWithBiLinearBackup.java:57-107, 224-249):
+ *            commons-math3 BicubicSplineInterpolator = natural cubic splines along each
+ *            grid line give the first derivatives at the knots, central finite
+ *            differences (one-sided at the border) give the cross derivative, and each
+ *            grid cell is a bicubic Hermite patch; pixel coordinates are clamped to the
+ *            tile-centre box.
+ *  B-inherit AdaptiveInterVelocityInheritanceStrategyBiCubicSpline
+ *            (S/iareas/AdaptiveInterVelocityInheritanceStrategyBiCubicSpline.java:27-136):
+ *            commons-math3 PiecewiseBicubicSplineInterpolator = for every evaluation a
+ *            5x5 knot window around the point, Akima splines (Akima 1970) along the first
+ *            coordinate for each of the 5 second-coordinate knots, then one along the
+ *            second coordinate; end derivatives from the parabola through 3 knots.
+ *  B-warp    BiLinearImageWarpingStrategy.doBiLinearWarp / warpPixelOnImage
+ *            (S/images/BiLinearImageWarpingStrategy.java:143-265), BothImages mode: the
+ *            field is halved, image A sampled at (i-u, j-v), image B at (i+u, j+v).
+ *  A-accum   Tile.accumulateDisplacement (S/iareas/Tile.java:103-136), clipping mode
+ *            AllowedOutOfBoundClipping (the UI converter's default).
+ *  A-loop    LocalPIVOpenCLGpuJob (S/jobs/LocalPIVOpenCLGpuJob.java:188-411) with
+ *            SimpleStrategy (one correlation per level), no validation.
+ */
+#define _GNU_SOURCE
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct {
+    float u, v;
+    float sub_i, sub_j;
+    float peak_value, min_floor;
+    int16_t peak_i, peak_j;
+    uint32_t flags;
+    double u64, v64;
+} orc_vector;
+
+/* from qlpiv_oracle.c */
+typedef struct {
+    int n, tiles_i, tiles_j, margin_top, margin_left, margin_bottom, margin_right;
+} orc_grid;
+int orc_grid_superposition(int h, int w, int mtop, int mbottom, int mleft, int mright, int n_start, int level,
+                           float overlap_factor, orc_grid *g, int *tops, int *lefts, int cap);
+int orc_piv_pass(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,
+                 const int *a_top, const int *a_left, const int *b_top, const int *b_left, int norm_mode,
+                 float fixed_max_a, float fixed_max_b, int subpix, int precision, orc_vector *out, int nthreads);
+
+/* ---------------- natural cubic spline: first derivative at every knot ---------------- */
+static void natural_spline_deriv(const double *x, const double *y, long ys, int n, double *d) {
+    /* second derivatives m[0] = m[n-1] = 0, tridiagonal solve (Thomas) */
+    double *m = (double *)calloc((size_t)n, sizeof(double));
+    double *cp = (double *)calloc((size_t)n, sizeof(double));
+    double *dp = (double *)calloc((size_t)n, sizeof(double));
+    for (int i = 1; i < n - 1; i++) {
+        const double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
+        const double a = h0, b = 2.0 * (h0 + h1), c = h1;
+        const double r = 6.0 * ((y[(i + 1) * ys] - y[i * ys]) / h1 - (y[i * ys] - y[(i - 1) * ys]) / h0);
+        const double den = b - a * cp[i - 1];
+        cp[i] = c / den;
+        dp[i] = (r - a * dp[i - 1]) / den;
+    }
+    for (int i = n - 2; i >= 1; i--) m[i] = dp[i] - cp[i] * m[i + 1];
+    for (int i = 0; i < n - 1; i++) {
+        const double h = x[i + 1] - x[i];
+        d[i] = (y[(i + 1) * ys] - y[i * ys]) / h - h * (2.0 * m[i] + m[i + 1]) / 6.0;
+    }
+    {
+        const double h = x[n - 1] - x[n - 2];
+        d[n - 1] = (y[(n - 1) * ys] - y[(n - 2) * ys]) / h + h * (m[n - 2] + 2.0 * m[n - 1]) / 6.0;
+    }
+    free(m); free(cp); free(dp);
+}
+
+/* Bicubic spline surface over knots ys[ni] (first coordinate) x xs[nj]. */
+typedef struct {
+    int ni, nj;
+    const double *ys, *xs;
+    double *f, *fy, *fx, *fyx; /* ni*nj each, row-major */
+} bicubic;
+
+static void bicubic_build(bicubic *s, const double *ys, int ni, const double *xs, int nj, const double *f) {
+    s->ni = ni; s->nj = nj; s->ys = ys; s->xs = xs;
+    const size_t nn = (size_t)ni * nj;
+    s->f = (double *)malloc(nn * sizeof(double));
+    s->fy = (double *)malloc(nn * sizeof(double));
+    s->fx = (double *)malloc(nn * sizeof(double));
+    s->fyx = (double *)malloc(nn * sizeof(double));
+    memcpy(s->f, f, nn * sizeof(double));
+    double *tmp = (double *)malloc(sizeof(double) * (ni > nj ? ni : nj));
+    for (int j = 0; j < nj; j++) {            /* along the first coordinate, per column */
+        natural_spline_deriv(ys, f + j, nj, ni, tmp);
+        for (int i = 0; i < ni; i++) s->fy[(size_t)i * nj + j] = tmp[i];
+    }
+    for (int i = 0; i < ni; i++) {            /* along the second coordinate, per row */
+        natural_spline_deriv(xs, f + (size_t)i * nj, 1, nj, tmp);
+        for (int j = 0; j < nj; j++) s->fx[(size_t)i * nj + j] = tmp[j];
+    }
+    for (int i = 0; i < ni; i++) {
+        const int ni_ = i + 1 < ni ? i + 1 : ni - 1, pi = i - 1 >= 0 ? i - 1 : 0;
+        for (int j = 0; j < nj; j++) {
+            const int nj_ = j + 1 < nj ? j + 1 : nj - 1, pj = j - 1 >= 0 ? j - 1 : 0;
+            s->fyx[(size_t)i * nj + j] =
+                (f[(size_t)ni_ * nj + nj_] - f[(size_t)ni_ * nj + pj] - f[(size_t)pi * nj + nj_] + f[(size_t)pi * nj + pj]) /
+                ((ys[ni_] - ys[pi]) * (xs[nj_] - xs[pj]));
+        }
+    }
+    free(tmp);
+}
+
+static void bicubic_free(bicubic *s) { free(s->f); free(s->fy); free(s->fx); free(s->fyx); }
+
+/* Index of the knot interval holding c (c inside [v0, v_{n-1}]); the last knot maps to
+ * the last interval. */
+static int knot_interval(const double *v, int n, double c) {
+    int lo = 0, hi = n - 1;
+    if (c >= v[n - 1]) return n - 2;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (v[mid] <= c) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+static void hermite_basis(double t, double h0[2], double h1[2]) {
+    const double t2 = t * t, t3 = t2 * t;
+    h0[0] = 2.0 * t3 - 3.0 * t2 + 1.0;
+    h0[1] = -2.0 * t3 + 3.0 * t2;
+    h1[0] = t3 - 2.0 * t2 + t;
+    h1[1] = t3 - t2;
+}
+
+/* Canonical evaluation order (shared bit-for-bit with the CUDA warp kernel): column
+ * basis X = (h00, h01, dx*h10, dx*h11)(tx), row basis Y likewise in ty; first the four
+ * column sums w, then p = ((w0*Y0 + w1*Y1) + w2*Y2) + w3*Y3. */
+static double bicubic_value(const bicubic *s, double y, double x) {
+    const int i = knot_interval(s->ys, s->ni, y), j = knot_interval(s->xs, s->nj, x);
+    const double dy = s->ys[i + 1] - s->ys[i], dx = s->xs[j + 1] - s->xs[j];
+    const double ty = (y - s->ys[i]) / dy, tx = (x - s->xs[j]) / dx;
+    double ay0[2], ay1[2], ax0[2], ax1[2];
+    hermite_basis(ty, ay0, ay1);
+    hermite_basis(tx, ax0, ax1);
+    const double X0 = ax0[0], X1 = ax0[1], X2 = dx * ax1[0], X3 = dx * ax1[1];
+    const double Y0 = ay0[0], Y1 = ay0[1], Y2 = dy * ay1[0], Y3 = dy * ay1[1];
+    double w[4];
+    for (int a = 0; a < 2; a++) {
+        const size_t k0 = (size_t)(i + a) * s->nj + j, k1 = k0 + 1;
+        w[a] = s->f[k0] * X0 + s->f[k1] * X1 + s->fx[k0] * X2 + s->fx[k1] * X3;
+        w[2 + a] = s->fy[k0] * X0 + s->fy[k1] * X1 + s->fyx[k0] * X2 + s->fyx[k1] * X3;
+    }
+    return w[0] * Y0 + w[1] * Y1 + w[2] * Y2 + w[3] * Y3;
+}
+
+/* ---------------- Akima spline on a 5-knot window ---------------- */
+static double parabola_deriv(const double *x, const double *y, int at, int i0, int i1, int i2) {
+    const double X = x[at];
+    const double x0 = x[i0], x1 = x[i1], x2 = x[i2];
+    return y[i0] * ((X - x1) + (X - x2)) / ((x0 - x1) * (x0 - x2)) +
+           y[i1] * ((X - x0) + (X - x2)) / ((x1 - x0) * (x1 - x2)) +
+           y[i2] * ((X - x0) + (X - x1)) / ((x2 - x0) * (x2 - x1));
+}
+
+static double akima5_value(const double *x, const double *y, double t) {
+    double d[4], w[4] = {0, 0, 0, 0}, fd[5];
+    for (int k = 0; k < 4; k++) d[k] = (y[k + 1] - y[k]) / (x[k + 1] - x[k]);
+    for (int k = 1; k < 4; k++) w[k] = fabs(d[k] - d[k - 1]);
+    {
+        const double wp = w[3], wm = w[1];
+        if (fabs(wp) <= 4.9e-324 && fabs(wm) <= 4.9e-324)
+            fd[2] = ((x[3] - x[2]) * d[1] + (x[2] - x[1]) * d[2]) / (x[3] - x[1]);
+        else
+            fd[2] = (wp * d[1] + wm * d[2]) / (wp + wm);
+    }
+    fd[0] = parabola_deriv(x, y, 0, 0, 1, 2);
+    fd[1] = parabola_deriv(x, y, 1, 0, 1, 2);
+    fd[3] = parabola_deriv(x, y, 3, 2, 3, 4);
+    fd[4] = parabola_deriv(x, y, 4, 2, 3, 4);
+    const int k = knot_interval(x, 5, t);
+    const double h = x[k + 1] - x[k], s = t - x[k];
+    const double c2 = (3.0 * (y[k + 1] - y[k]) / h - 2.0 * fd[k] - fd[k + 1]) / h;
+    const double c3 = (2.0 * (y[k] - y[k + 1]) / h + fd[k] + fd[k + 1]) / (h * h);
+    return y[k] + s * (fd[k] + s * (c2 + s * c3));
+}
+
+/* start of the 5-knot window for c (binary search, the window centred on the hit or
+ * the interval, clamped to the knot range) */
+static int akima_window(const double *v, int n, double c) {
+    int lo = 0, hi = n;                      /* first index with v[idx] > c */
+    while (lo < hi) {
+        const int mid = (lo + hi) / 2;
+        if (v[mid] <= c) lo = mid + 1; else hi = mid;
+    }
+    int r;
+    if (lo > 0 && v[lo - 1] == c) r = (lo - 1) - 2;   /* exact knot */
+    else r = lo - 2;                                    /* inside (v[lo-1], v[lo]) */
+    if (r < 0) r = 0;
+    if (r + 5 >= n) r = n - 5;
+    return r;
+}
+
+static double akima2d_value(const double *ys, int ni, const double *xs, int nj, const double *f, double y, double x) {
+    const int i = akima_window(ys, ni, y), j = akima_window(xs, nj, x);
+    double col[5], row[5];
+    for (int b = 0; b < 5; b++) {
+        for (int a = 0; a < 5; a++) col[a] = f[(size_t)(i + a) * nj + (j + b)];
+        row[b] = akima5_value(ys + i, col, y);
+    }
+    return akima5_value(xs + j, row, x);
+}
+
+/* ---------------- warp ---------------- */
+static float read_pix(const void *img, int pix_bytes, int w, int y, int x) {
+    return pix_bytes == 1 ? (float)((const uint8_t *)img)[(size_t)y * w + x]
+                          : (float)((const uint16_t *)img)[(size_t)y * w + x];
+}
+
+static int java_round(float x) { return (int)floorf(x + 0.5f); }
+
+/* warpPixelOnImage (BiLinearImageWarpingStrategy.java:185-265) */
+static float warp_pixel(const void *img, int pix_bytes, int h, int w, float u, float v, int i, int j, int first) {
+    float sI = first ? (float)i - u : (float)i + u;
+    float sJ = first ? (float)j - v : (float)j + v;
+    int pI = (int)(short)java_round(sI), pJ = (int)(short)java_round(sJ);
+    if (pI < 0) { sI = 0.0f; pI = 0; }
+    else if (pI >= h) { sI = (float)(h - 1); pI = h - 1; }
+    if (pJ < 0) { sJ = 0.0f; pJ = 0; }
+    else if (pJ >= w) { sJ = (float)(w - 1); pJ = w - 1; }
+    const float dU = sI - (float)pI, dV = sJ - (float)pJ;
+    int oI = dU >= 0.0f ? 1 : -1, oJ = dV >= 0.0f ? 1 : -1;
+    if (oI + pI < 0 || oI + pI >= h) oI = 0;
+    if (oJ + pJ < 0 || oJ + pJ >= w) oJ = 0;
+    const float wU = fabsf(dU), wV = fabsf(dV);
+    const float tl = read_pix(img, pix_bytes, w, pI, pJ);
+    const float tr = read_pix(img, pix_bytes, w, pI, pJ + oJ);
+    const float bl = read_pix(img, pix_bytes, w, pI + oI, pJ);
+    const float br = read_pix(img, pix_bytes, w, pI + oI, pJ + oJ);
+    const float a = (1.0f - wU) * (1.0f - wV) * tl;
+    const float b = (1.0f - wU) * wV * tr;
+    const float c = wU * (1.0f - wV) * bl;
+    const float d = wU * wV * br;
+    const float fv = a + b + c + d;
+    return (float)java_round(fv);
+}
+
+/* Stores a warped value as MatrixByte/MatrixInt16.setElement(float) would.  The reference's
+ * 16-bit matrix narrows through a signed byte (S/MatrixInt16.java:95-101); int16_quirk = 1
+ * reproduces that, 0 stores the rounded 16-bit value. */
+static void store_pix(void *img, int pix_bytes, int w, int y, int x, float v, int int16_quirk) {
+    const int r = java_round(v);
+    if (pix_bytes == 1) {
+        ((uint8_t *)img)[(size_t)y * w + x] = (uint8_t)(int8_t)r;
+    } else if (int16_quirk) {
+        ((uint16_t *)img)[(size_t)y * w + x] = (uint16_t)(int16_t)(int8_t)r;
+    } else {
+        ((uint16_t *)img)[(size_t)y * w + x] = (uint16_t)r;
+    }
+}
+
+/* Exported pieces (ctypes) ------------------------------------------------------- */
+
+/* Per-pixel field of one level: tile displacements u, v (ni x nj, row-major) at tile
+ * centres ys[ni], xs[nj] -> fu, fv (h x w float).  Coordinates clamped to the centre box. */
+void orc_displacement_field(const double *ys, int ni, const double *xs, int nj, const float *u, const float *v, int h,
+                            int w, float *fu, float *fv) {
+    const size_t nn = (size_t)ni * nj;
+    double *du = (double *)malloc(nn * sizeof(double)), *dv = (double *)malloc(nn * sizeof(double));
+    for (size_t k = 0; k < nn; k++) { du[k] = u[k]; dv[k] = v[k]; }
+    bicubic su, sv;
+    bicubic_build(&su, ys, ni, xs, nj, du);
+    bicubic_build(&sv, ys, ni, xs, nj, dv);
+    const float ymin = (float)ys[0], ymax = (float)ys[ni - 1], xmin = (float)xs[0], xmax = (float)xs[nj - 1];
+    for (int i = 0; i < h; i++) {
+        float y = (float)i;
+        if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
+        for (int j = 0; j < w; j++) {
+            float x = (float)j;
+            if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
+            fu[(size_t)i * w + j] = (float)bicubic_value(&su, (double)y, (double)x);
+            fv[(size_t)i * w + j] = (float)bicubic_value(&sv, (double)y, (double)x);
+        }
+    }
+    bicubic_free(&su); bicubic_free(&sv);
+    free(du); free(dv);
+}
+
+/* BothImages bilinear warp of a pair with a per-pixel field (halved inside). */
+void orc_warp_both(const void *img_a, const void *img_b, int h, int w, int pix_bytes, const float *fu, const float *fv,
+                   int int16_quirk, void *out_a, void *out_b) {
+    for (int i = 0; i < h; i++)
+        for (int j = 0; j < w; j++) {
+            const float u = fu[(size_t)i * w + j] / 2.0f, v = fv[(size_t)i * w + j] / 2.0f;
+            store_pix(out_a, pix_bytes, w, i, j, warp_pixel(img_a, pix_bytes, h, w, u, v, i, j, 1), int16_quirk);
+            store_pix(out_b, pix_bytes, w, i, j, warp_pixel(img_b, pix_bytes, h, w, u, v, i, j, 0), int16_quirk);
+        }
+}
+
+/* Inherited displacement of child tiles at centres (cy[ci], cx[cj]) from parent tiles
+ * (pu, pv at centres py[pi], px[pj]), clamped to the parent box; needs >= 5 parent
+ * tiles per axis, otherwise nothing is inherited (the reference computes a bilinear
+ * value in that case but does not apply it). */
+void orc_inherit(const double *py, int pni, const double *px, int pnj, const float *pu, const float *pv, const float *cy,
+                 int cni, const float *cx, int cnj, int round_int, float *cu, float *cv) {
+    if (pni < 5 || pnj < 5) {
+        memset(cu, 0, sizeof(float) * cni * cnj);
+        memset(cv, 0, sizeof(float) * cni * cnj);
+        return;
+    }
+    const size_t nn = (size_t)pni * pnj;
+    double *du = (double *)malloc(nn * sizeof(double)), *dv = (double *)malloc(nn * sizeof(double));
+    for (size_t k = 0; k < nn; k++) { du[k] = pu[k]; dv[k] = pv[k]; }
+    const float ymin = (float)py[0], ymax = (float)py[pni - 1], xmin = (float)px[0], xmax = (float)px[pnj - 1];
+    for (int i = 0; i < cni; i++) {
+        float y = cy[i];
+        if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
+        for (int j = 0; j < cnj; j++) {
+            float x = cx[j];
+            if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
+            /* Tile.accumulateDisplacement on a reset tile: 0 + (float)value, rounded
+             * first for non-warping modes (FastMath.round(float)) */
+            const float iu = (float)akima2d_value(py, pni, px, pnj, du, (double)y, (double)x);
+            const float iv = (float)akima2d_value(py, pni, px, pnj, dv, (double)y, (double)x);
+            cu[(size_t)i * cnj + j] = 0.0f + (round_int ? (float)java_round(iu) : iu);
+            cv[(size_t)i * cnj + j] = 0.0f + (round_int ? (float)java_round(iv) : iv);
+        }
+    }
+    free(du); free(dv);
+}
+
+/* Adaptive multi-pass PIV with BothImages bilinear warping (SuperPosition grids, SimpleStrategy).
+ * Level L uses IA n_start >> L.  warp_mode 1 = BothImages bilinear warping, 0 = no
+ * warping (B tiles displaced by the rounded inherited displacement).  Tile maxima are
+ * fixed_max when > 0 (full-image-warp tiles: 255 / 65535), else the tile max.
+ * Outputs the last level's displacement (u rows, v columns) and, optionally, every
+ * level's vectors concatenated (level_vectors, sized by the caller). */
+int orc_piv_adaptive(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n_start, int n_end,
+                     float overlap_factor, int warp_mode, int norm_mode, float fixed_max, int int16_quirk, int precision,
+                     int nthreads, float *out_u, float *out_v, int *out_ni, int *out_nj, orc_vector *level_vectors) {
+    int levels = 0;
+    for (int n = n_start; n >= n_end; n >>= 1) levels++;
+    const int cap = 65536;
+    int *tops = (int *)malloc(sizeof(int) * cap), *lefts = (int *)malloc(sizeof(int) * cap);
+    int *ptops = (int *)malloc(sizeof(int) * cap), *plefts = (int *)malloc(sizeof(int) * cap);
+    float *pu = NULL, *pv = NULL;
+    int pni = 0, pnj = 0, pn = 0;
+    const size_t ib = (size_t)h * w * pix_bytes;
+    void *wa = malloc(ib), *wb = malloc(ib);
+    float *fu = (float *)malloc(sizeof(float) * h * w), *fv = (float *)malloc(sizeof(float) * h * w);
+    long vec_off = 0;
+    int rc = 0;
+    for (int lv = 0; lv < levels; lv++) {
+        orc_grid g;
+        if (orc_grid_superposition(h, w, 0, 0, 0, 0, n_start, lv, overlap_factor, &g, tops, lefts, cap) != 0) {
+            rc = -1;
+            break;
+        }
+        const int n = g.n, ni = g.tiles_i, nj = g.tiles_j;
+        const long cnt = (long)ni * nj;
+        float *cu = (float *)calloc((size_t)cnt, sizeof(float)), *cv = (float *)calloc((size_t)cnt, sizeof(float));
+        double *cyd = (double *)malloc(sizeof(double) * ni), *cxd = (double *)malloc(sizeof(double) * nj);
+        float *cyf = (float *)malloc(sizeof(float) * ni), *cxf = (float *)malloc(sizeof(float) * nj);
+        for (int i = 0; i < ni; i++) { cyf[i] = (float)tops[i] + (float)n / 2.0f - 0.5f; cyd[i] = cyf[i]; }
+        for (int j = 0; j < nj; j++) { cxf[j] = (float)lefts[j] + (float)n / 2.0f - 0.5f; cxd[j] = cxf[j]; }
+        const void *sa = img_a, *sb = img_b;
+        if (lv > 0) {
+            double *pyd = (double *)malloc(sizeof(double) * pni), *pxd = (double *)malloc(sizeof(double) * pnj);
+            for (int i = 0; i < pni; i++) pyd[i] = (double)((float)ptops[i] + (float)pn / 2.0f - 0.5f);
+            for (int j = 0; j < pnj; j++) pxd[j] = (double)((float)plefts[j] + (float)pn / 2.0f - 0.5f);
+            orc_inherit(pyd, pni, pxd, pnj, pu, pv, cyf, ni, cxf, nj, warp_mode == 0, cu, cv);
+            free(pyd); free(pxd);
+            if (warp_mode == 1) {
+                orc_displacement_field(cyd, ni, cxd, nj, cu, cv, h, w, fu, fv);
+                orc_warp_both(img_a, img_b, h, w, pix_bytes, fu, fv, int16_quirk, wa, wb);
+                sa = wa; sb = wb;
+            }
+        }
+        int *at = (int *)malloc(sizeof(int) * cnt), *al = (int *)malloc(sizeof(int) * cnt);
+        int *bt = (int *)malloc(sizeof(int) * cnt), *bl = (int *)malloc(sizeof(int) * cnt);
+        for (int i = 0; i < ni; i++)
+            for (int j = 0; j < nj; j++) {
+                const size_t k = (size_t)i * nj + j;
+                at[k] = tops[i];
+                al[k] = lefts[j];
+                /* NoImageWarpingStrategy: B tile at round(top + u), round(left + v) */
+                bt[k] = warp_mode == 0 ? java_round((float)tops[i] + cu[k]) : tops[i];
+                bl[k] = warp_mode == 0 ? java_round((float)lefts[j] + cv[k]) : lefts[j];
+            }
+        orc_vector *vec = (orc_vector *)malloc(sizeof(orc_vector) * cnt);
+        const float fm = fixed_max > 0.0f ? fixed_max : 0.0f;
+        orc_piv_pass(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, fixed_max > 0.0f ? 2 : norm_mode, fm, fm, 1,
+                     precision, vec, nthreads);
+        if (level_vectors) memcpy(level_vectors + vec_off, vec, sizeof(orc_vector) * cnt);
+        vec_off += cnt;
+        for (long k = 0; k < cnt; k++) {
+            if (precision == 0) { cu[k] += vec[k].u; cv[k] += vec[k].v; }
+            else { cu[k] = (float)((double)cu[k] + vec[k].u64); cv[k] = (float)((double)cv[k] + vec[k].v64); }
+        }
+        free(at); free(al); free(bt); free(bl); free(vec); free(cyd); free(cxd); free(cyf); free(cxf);
+        free(pu); free(pv);
+        pu = cu; pv = cv;
+        pni = ni; pnj = nj; pn = n;
+        memcpy(ptops, tops, sizeof(int) * ni);
+        memcpy(plefts, lefts, sizeof(int) * nj);
+    }
+    if (rc == 0) {
+        memcpy(out_u, pu, sizeof(float) * pni * pnj);
+        memcpy(out_v, pv, sizeof(float) * pni * pnj);
+        *out_ni = pni;
+        *out_nj = pnj;
+    }
+    free(pu); free(pv); free(tops); free(lefts); free(ptops); free(plefts); free(wa); free(wb); free(fu); free(fv);
+    return rc;
+}

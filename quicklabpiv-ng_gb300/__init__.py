@@ -57,6 +57,34 @@ FRAME_DTYPE = np.dtype([("img_a", "<u8"), ("img_b", "<u8"), ("height", "<i4"), (
 assert FRAME_DTYPE.itemsize == 32
 
 
+class Grid(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int) for k in
+                ("n", "tiles_i", "tiles_j", "margin_top", "margin_left", "margin_bottom", "margin_right")]
+
+
+WARP_NONE, WARP_BOTH_BILINEAR = 0, 1
+
+
+class AdaptiveDesc(ctypes.Structure):
+    _fields_ = [("ia_start", ctypes.c_int), ("ia_end", ctypes.c_int), ("overlap_factor", ctypes.c_float),
+                ("margins", ctypes.c_int * 4), ("warp_mode", ctypes.c_int), ("norm_mode", ctypes.c_int),
+                ("max_mode", ctypes.c_int), ("fixed_max", ctypes.c_float), ("subpix_mode", ctypes.c_int),
+                ("int16_warp_quirk", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+
+
+def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_mode=WARP_BOTH_BILINEAR,
+                  norm_mode=NORM_MAX_A, max_mode=MAX_FIXED, fixed_max=0.0, subpix_mode=SUBPIX_GAUSS3,
+                  int16_warp_quirk=False):
+    """Adaptive PIV parameters; the defaults follow the reference's BothImages bilinear
+    warping (tiles copied from the warped image keep the full-scale maximum)."""
+    d = AdaptiveDesc()
+    d.ia_start, d.ia_end, d.overlap_factor = ia_start, ia_end, overlap_factor
+    d.margins[:] = list(margins)
+    d.warp_mode, d.norm_mode, d.max_mode, d.fixed_max = warp_mode, norm_mode, max_mode, fixed_max
+    d.subpix_mode, d.int16_warp_quirk = subpix_mode, int(int16_warp_quirk)
+    return d
+
+
 class Params(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
@@ -79,6 +107,14 @@ _SIGNATURES = {
     "qlpiv_get_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
     "qlpiv_set_stream": (_i, [_vp, _vp]),
     "qlpiv_measure_fp32_peak": (_i, [_i, ctypes.POINTER(ctypes.c_double)]),
+    "qlpiv_grid_superposition": (_i, [_i, _i, _vp, _i, _i, _f, ctypes.POINTER(Grid), _vp, _vp, _i]),
+    "qlpiv_grid_nosuperposition": (_i, [_i, _i, _vp, _i, _i, ctypes.POINTER(Grid), _vp, _vp, _i]),
+    "qlpiv_adaptive_levels": (_i, [ctypes.POINTER(AdaptiveDesc), _i, _i, ctypes.POINTER(_i), _vp, _i]),
+    "qlpiv_inherit": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp]),
+    "qlpiv_displacement_field": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "qlpiv_warp_pair": (_i, [_vp, _i, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
+    "qlpiv_piv_adaptive": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
+    "qlpiv_piv_adaptive_device": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
 }
 
 _lib = None
@@ -112,6 +148,31 @@ def exported_symbols():
 def _check(status):
     if status != OK:
         raise QlpivError(status, load_library().qlpiv_last_error().decode())
+
+
+def library_grid(height, width, ia_start, level, overlap_factor, margins=(0, 0, 0, 0), superposition=True):
+    """IA grid computed by the library (host code of libqlpiv_gpu.so)."""
+    lib = load_library()
+    g = Grid()
+    m = (ctypes.c_int * 4)(*margins)
+    cap = 1 << 16
+    tops = np.zeros(cap, np.int32)
+    lefts = np.zeros(cap, np.int32)
+    if superposition:
+        _check(lib.qlpiv_grid_superposition(height, width, m, ia_start, level, overlap_factor, ctypes.byref(g),
+                                            _addr(tops), _addr(lefts), cap))
+    else:
+        _check(lib.qlpiv_grid_nosuperposition(height, width, m, ia_start, level, ctypes.byref(g), _addr(tops),
+                                              _addr(lefts), cap))
+    return {k: getattr(g, k) for k, _ in Grid._fields_}, tops[:g.tiles_i].copy(), lefts[:g.tiles_j].copy()
+
+
+def adaptive_levels(desc, height, width):
+    lib = load_library()
+    n = ctypes.c_int()
+    grids = (Grid * 16)()
+    _check(lib.qlpiv_adaptive_levels(ctypes.byref(desc), height, width, ctypes.byref(n), grids, 16))
+    return [{k: getattr(grids[i], k) for k, _ in Grid._fields_} for i in range(n.value)]
 
 
 def measure_fp32_peak(device=0):
@@ -294,6 +355,72 @@ class Handle:
         a = [x if isinstance(x, int) else _addr(x) for x in (frames, frame_of_ia, a_top, a_left, b_top, b_left, out)]
         _check(self._lib.qlpiv_pass_batch_device(self._h, ctypes.byref(d), pixel_type, num_frames, a[0], count, a[1],
                                                  a[2], a[3], a[4], a[5], a[6]))
+
+    # -- stages between passes --------------------------------------------------
+    def inherit(self, p_ci, p_cj, pu, pv, c_ci, c_cj, round_int=False):
+        """Velocity inheritance from a parent grid to a child grid (host arrays)."""
+        p_ci = np.ascontiguousarray(p_ci, np.float64)
+        p_cj = np.ascontiguousarray(p_cj, np.float64)
+        pu = np.ascontiguousarray(pu, np.float32)
+        pv = np.ascontiguousarray(pv, np.float32)
+        c_ci = np.ascontiguousarray(c_ci, np.float32)
+        c_cj = np.ascontiguousarray(c_cj, np.float32)
+        cu = np.empty((len(c_ci), len(c_cj)), np.float32)
+        cv = np.empty_like(cu)
+        _check(self._lib.qlpiv_inherit(self._h, len(p_ci), len(p_cj), _addr(p_ci), _addr(p_cj), _addr(pu), _addr(pv),
+                                       len(c_ci), len(c_cj), _addr(c_ci), _addr(c_cj), int(round_int), _addr(cu),
+                                       _addr(cv)))
+        return cu, cv
+
+    def displacement_field(self, ci, cj, u, v, height, width):
+        ci = np.ascontiguousarray(ci, np.float64)
+        cj = np.ascontiguousarray(cj, np.float64)
+        u = np.ascontiguousarray(u, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        fu = np.empty((height, width), np.float32)
+        fv = np.empty_like(fu)
+        _check(self._lib.qlpiv_displacement_field(self._h, height, width, len(ci), len(cj), _addr(ci), _addr(cj),
+                                                  _addr(u), _addr(v), _addr(fu), _addr(fv)))
+        return fu, fv
+
+    def warp_pair(self, img_a, img_b, ci, cj, u, v, int16_quirk=False):
+        ia = np.ascontiguousarray(img_a)
+        ib = np.ascontiguousarray(img_b)
+        ci = np.ascontiguousarray(ci, np.float64)
+        cj = np.ascontiguousarray(cj, np.float64)
+        u = np.ascontiguousarray(u, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        oa = np.empty_like(ia)
+        ob = np.empty_like(ib)
+        _check(self._lib.qlpiv_warp_pair(self._h, pixel_type_of(ia.dtype), _addr(ia), _addr(ib), ia.shape[0],
+                                         ia.shape[1], len(ci), len(cj), _addr(ci), _addr(cj), _addr(u), _addr(v),
+                                         int(int16_quirk), _addr(oa), _addr(ob)))
+        return oa, ob
+
+    def piv_adaptive(self, frames_a, frames_b, desc):
+        """Adaptive multi-pass PIV of image pairs of one size; returns (u, v) of the last
+        level shaped (pairs, tiles_i, tiles_j)."""
+        fa = [np.ascontiguousarray(x) for x in frames_a]
+        fb = [np.ascontiguousarray(x) for x in frames_b]
+        h, w = fa[0].shape
+        dt = fa[0].dtype
+        table = (Frame * len(fa))()
+        for k, (x, y) in enumerate(zip(fa, fb)):
+            if x.shape != (h, w) or y.shape != (h, w) or x.dtype != dt or y.dtype != dt:
+                raise ValueError("all frames must share shape and dtype")
+            table[k] = Frame(x.ctypes.data, y.ctypes.data, h, w, w)
+        last = adaptive_levels(desc, h, w)[-1]
+        u = np.empty((len(fa), last["tiles_i"], last["tiles_j"]), np.float32)
+        v = np.empty_like(u)
+        _check(self._lib.qlpiv_piv_adaptive(self._h, ctypes.byref(desc), pixel_type_of(dt), h, w, len(fa), table,
+                                            _addr(u), _addr(v)))
+        return u, v
+
+    def piv_adaptive_device(self, desc, pixel_type, height, width, num_pairs, frames, out_u, out_v):
+        """Queue adaptive PIV over a device frame table into device outputs."""
+        a = [x if isinstance(x, int) else _addr(x) for x in (frames, out_u, out_v)]
+        _check(self._lib.qlpiv_piv_adaptive_device(self._h, ctypes.byref(desc), pixel_type, height, width, num_pairs,
+                                                   a[0], a[1], a[2]))
 
 
 from . import grid, jobs, synth  # noqa: E402,F401

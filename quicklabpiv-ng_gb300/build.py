@@ -16,8 +16,13 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libqlpiv_gpu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3", "-I", str(ROOT / "include"),
-                     "-I", str(CSRC)]
+# Host code is compiled without FMA contraction (-ffp-contract=off) so float/double host
+# expressions round the same way on x86_64 and aarch64.
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3,-ffp-contract=off",
+                     "-I", str(ROOT / "include"), "-I", str(CSRC)]
+# Per-file device flags: the adaptive stages are bit-identical to the CPU oracle only
+# without FMA contraction.
+FILE_FLAGS = {"qlpiv_adaptive.cu": ["--fmad=false"]}
 
 
 def _nvcc():
@@ -52,7 +57,7 @@ def build(force=False, verbose=False, ptxas_info=False):
 
     def compile_one(src):
         obj = BUILD / (src.stem + ".o")
-        cmd = [nvcc, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc, *NVCC_FLAGS, *FILE_FLAGS.get(src.name, []), *extra, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

@@ -1,0 +1,409 @@
+// Adaptive multi-pass stages between correlation passes (device code).
+//
+//   B-inherit  AdaptiveInterVelocityInheritanceStrategyBiCubicSpline
+//              (S/iareas/AdaptiveInterVelocityInheritanceStrategyBiCubicSpline.java:27-136):
+//              child tile displacement = piecewise bicubic (Akima, 5x5 knot window)
+//              interpolation of the parent tiles' displacement at the child centre,
+//              clamped to the parent centre box; rounded for non-warping modes.
+//   B-field    BiCubicSplineInterpolatorWithBiLinearBackup (S/iareas/...:57-107,224-249):
+//              bicubic spline surface through the current level's tile displacements
+//              (natural-spline knot derivatives, finite-difference cross derivatives,
+//              Hermite patches), evaluated per pixel with coordinates clamped to the
+//              tile-centre box.  Computed in double like the reference.
+//   B-warp     BiLinearImageWarpingStrategy.warpPixelOnImage (S/images/...:143-265),
+//              BothImages mode: field halved, A sampled at (i-u, j-v), B at (i+u, j+v),
+//              nearest-pixel anchor plus the neighbour on the residual's side, output
+//              rounded.
+// The commons-math3 interpolators the reference calls are restated from their
+// mathematics.  This translation unit is compiled with --fmad=false so every double
+// and float expression rounds exactly like the CPU oracle's restatement (same
+// operand order, no contraction): the warp stage is bit-identical to the oracle.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "qlpiv_adaptive.h"
+
+namespace qlpiv {
+
+// ---------------- shared device helpers ----------------
+
+__device__ __forceinline__ int knot_interval(const double *v, int n, double c) {
+    int lo = 0, hi = n - 1;
+    if (c >= v[n - 1]) return n - 2;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (v[mid] <= c) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void hermite_basis(double t, double h0[2], double h1[2]) {
+    const double t2 = t * t, t3 = t2 * t;
+    h0[0] = 2.0 * t3 - 3.0 * t2 + 1.0;
+    h0[1] = -2.0 * t3 + 3.0 * t2;
+    h1[0] = t3 - 2.0 * t2 + t;
+    h1[1] = t3 - t2;
+}
+
+__device__ __forceinline__ double parabola_deriv(const double *x, const double *y, int at, int i0, int i1, int i2) {
+    const double X = x[at];
+    const double x0 = x[i0], x1 = x[i1], x2 = x[i2];
+    return y[i0] * ((X - x1) + (X - x2)) / ((x0 - x1) * (x0 - x2)) +
+           y[i1] * ((X - x0) + (X - x2)) / ((x1 - x0) * (x1 - x2)) +
+           y[i2] * ((X - x0) + (X - x1)) / ((x2 - x0) * (x2 - x1));
+}
+
+// Akima spline through 5 knots, evaluated at t (knots ascending, t inside).
+__device__ double akima5_value(const double *x, const double *y, double t) {
+    double d[4], w[4] = {0.0, 0.0, 0.0, 0.0}, fd[5];
+    for (int k = 0; k < 4; k++) d[k] = (y[k + 1] - y[k]) / (x[k + 1] - x[k]);
+    for (int k = 1; k < 4; k++) w[k] = fabs(d[k] - d[k - 1]);
+    {
+        const double wp = w[3], wm = w[1];
+        if (fabs(wp) <= 4.9e-324 && fabs(wm) <= 4.9e-324)
+            fd[2] = ((x[3] - x[2]) * d[1] + (x[2] - x[1]) * d[2]) / (x[3] - x[1]);
+        else
+            fd[2] = (wp * d[1] + wm * d[2]) / (wp + wm);
+    }
+    fd[0] = parabola_deriv(x, y, 0, 0, 1, 2);
+    fd[1] = parabola_deriv(x, y, 1, 0, 1, 2);
+    fd[3] = parabola_deriv(x, y, 3, 2, 3, 4);
+    fd[4] = parabola_deriv(x, y, 4, 2, 3, 4);
+    const int k = knot_interval(x, 5, t);
+    const double h = x[k + 1] - x[k], s = t - x[k];
+    const double c2 = (3.0 * (y[k + 1] - y[k]) / h - 2.0 * fd[k] - fd[k + 1]) / h;
+    const double c3 = (2.0 * (y[k] - y[k + 1]) / h + fd[k] + fd[k + 1]) / (h * h);
+    return y[k] + s * (fd[k] + s * (c2 + s * c3));
+}
+
+__device__ __forceinline__ int akima_window(const double *v, int n, double c) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) / 2;
+        if (v[mid] <= c) lo = mid + 1; else hi = mid;
+    }
+    int r;
+    if (lo > 0 && v[lo - 1] == c) r = (lo - 1) - 2;
+    else r = lo - 2;
+    if (r < 0) r = 0;
+    if (r + 5 >= n) r = n - 5;
+    return r;
+}
+
+__device__ __forceinline__ int java_round(float x) { return (int)floorf(x + 0.5f); }
+
+// ---------------- B-inherit ----------------
+
+// One thread per (pair, child tile).  Parent arrays are [pairs][pni*pnj].
+__global__ void inherit_kernel(int pairs, const double *py, int pni, const double *px, int pnj, const float *pu,
+                               const float *pv, const float *cy, int cni, const float *cx, int cnj, int round_int,
+                               float *cu, float *cv) {
+    const long cnt = (long)cni * cnj;
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= cnt * pairs) return;
+    const int pair = (int)(gid / cnt);
+    const long k = gid - (long)pair * cnt;
+    const int i = (int)(k / cnj), j = (int)(k - (long)i * cnj);
+    if (pni < 5 || pnj < 5) {  // the reference computes a bilinear value here but never applies it
+        cu[gid] = 0.0f;
+        cv[gid] = 0.0f;
+        return;
+    }
+    const float ymin = (float)py[0], ymax = (float)py[pni - 1], xmin = (float)px[0], xmax = (float)px[pnj - 1];
+    float y = cy[i], x = cx[j];
+    if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
+    if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
+    const int wi = akima_window(py, pni, (double)y), wj = akima_window(px, pnj, (double)x);
+    const float *fu = pu + (long)pair * pni * pnj;
+    const float *fv = pv + (long)pair * pni * pnj;
+    double rowu[5], rowv[5], colu[5], colv[5];
+    for (int b = 0; b < 5; b++) {
+        for (int a = 0; a < 5; a++) {
+            const long kk = (long)(wi + a) * pnj + (wj + b);
+            colu[a] = (double)fu[kk];
+            colv[a] = (double)fv[kk];
+        }
+        rowu[b] = akima5_value(py + wi, colu, (double)y);
+        rowv[b] = akima5_value(py + wi, colv, (double)y);
+    }
+    const float iu = (float)akima5_value(px + wj, rowu, (double)x);
+    const float iv = (float)akima5_value(px + wj, rowv, (double)x);
+    if (round_int) {
+        cu[gid] = 0.0f + (float)java_round(iu);
+        cv[gid] = 0.0f + (float)java_round(iv);
+    } else {
+        cu[gid] = 0.0f + iu;
+        cv[gid] = 0.0f + iv;
+    }
+}
+
+// ---------------- B-field spline set-up ----------------
+
+// cp[i] of the natural-spline tridiagonal elimination for knots v[n] (one thread).
+__global__ void spline_factor_kernel(const double *v, int n, double *cp) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    cp[0] = 0.0;
+    for (int i = 1; i < n - 1; i++) {
+        const double h0 = v[i] - v[i - 1], h1 = v[i + 1] - v[i];
+        const double a = h0, b = 2.0 * (h0 + h1), c = h1;
+        const double den = b - a * cp[i - 1];
+        cp[i] = c / den;
+    }
+    if (n > 1) cp[n - 1] = 0.0;
+}
+
+// Knot derivatives of one grid line of f (float values, stride fs) into out (stride os).
+__device__ void spline_line(const double *x, const double *cp, int n, const float *f, long fs, double *out, long os) {
+    auto Y = [&](int i) -> double { return (double)f[(long)i * fs]; };
+    out[0] = 0.0;
+    double dprev = 0.0;
+    for (int i = 1; i < n - 1; i++) {
+        const double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
+        const double a = h0, b = 2.0 * (h0 + h1);
+        const double r = 6.0 * ((Y(i + 1) - Y(i)) / h1 - (Y(i) - Y(i - 1)) / h0);
+        const double den = b - a * cp[i - 1];
+        const double dp = (r - a * dprev) / den;
+        out[(long)i * os] = dp;
+        dprev = dp;
+    }
+    out[(long)(n - 1) * os] = 0.0;
+    double mnext = 0.0;  // m[n-1]
+    for (int i = n - 2; i >= 1; i--) {
+        const double m = out[(long)i * os] - cp[i] * mnext;
+        out[(long)i * os] = m;
+        mnext = m;
+    }
+    // out now holds m[]; convert to first derivatives in place
+    double mi = out[0];
+    double mlast_prev = 0.0;
+    for (int i = 0; i < n - 1; i++) {
+        const double mi1 = out[(long)(i + 1) * os];
+        const double h = x[i + 1] - x[i];
+        out[(long)i * os] = (Y(i + 1) - Y(i)) / h - h * (2.0 * mi + mi1) / 6.0;
+        mlast_prev = mi;
+        mi = mi1;
+    }
+    {
+        // mi == m[n-1], mlast_prev == m[n-2]
+        const double h = x[n - 1] - x[n - 2];
+        out[(long)(n - 1) * os] = (Y(n - 1) - Y(n - 2)) / h + h * (mlast_prev + 2.0 * mi) / 6.0;
+    }
+}
+
+// Threads: pairs x 2 components x (nj column lines + ni row lines).
+__global__ void spline_lines_kernel(int pairs, const double *ys, const double *cpy, int ni, const double *xs,
+                                    const double *cpx, int nj, const float *u, const float *v, SplineCoef coef) {
+    const long lines = (long)nj + ni;
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= lines * 2 * pairs) return;
+    const int pair = (int)(gid / (lines * 2));
+    const long rem = gid - (long)pair * lines * 2;
+    const int comp = (int)(rem / lines);
+    const long line = rem - (long)comp * lines;
+    const long base = (long)pair * ni * nj;
+    const float *f = (comp == 0 ? u : v) + base;
+    if (line < nj) {  // along the first coordinate, column j
+        const int j = (int)line;
+        double *out = (comp == 0 ? coef.fy_u : coef.fy_v) + base + j;
+        spline_line(ys, cpy, ni, f + j, nj, out, nj);
+    } else {          // along the second coordinate, row i
+        const int i = (int)(line - nj);
+        double *out = (comp == 0 ? coef.fx_u : coef.fx_v) + base + (long)i * nj;
+        spline_line(xs, cpx, nj, f + (long)i * nj, 1, out, 1);
+    }
+}
+
+// Cross derivatives by central differences (one-sided at the border).
+__global__ void spline_cross_kernel(int pairs, const double *ys, int ni, const double *xs, int nj, const float *u,
+                                    const float *v, SplineCoef coef) {
+    const long cnt = (long)ni * nj;
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= cnt * pairs) return;
+    const int pair = (int)(gid / cnt);
+    const long k = gid - (long)pair * cnt;
+    const int i = (int)(k / nj), j = (int)(k - (long)i * nj);
+    const int ni_ = i + 1 < ni ? i + 1 : ni - 1, pi = i - 1 >= 0 ? i - 1 : 0;
+    const int nj_ = j + 1 < nj ? j + 1 : nj - 1, pj = j - 1 >= 0 ? j - 1 : 0;
+    const long base = (long)pair * cnt;
+    const double den = (ys[ni_] - ys[pi]) * (xs[nj_] - xs[pj]);
+    for (int comp = 0; comp < 2; comp++) {
+        const float *f = (comp == 0 ? u : v) + base;
+        const double a = (double)f[(long)ni_ * nj + nj_], b = (double)f[(long)ni_ * nj + pj];
+        const double c = (double)f[(long)pi * nj + nj_], d = (double)f[(long)pi * nj + pj];
+        (comp == 0 ? coef.fyx_u : coef.fyx_v)[base + k] = (a - b - c + d) / den;
+    }
+}
+
+// ---------------- B-field evaluation + B-warp ----------------
+
+template <typename Pix>
+__device__ __forceinline__ float warp_read(const Pix *img, int w, int y, int x) {
+    return (float)img[(long)y * w + x];
+}
+
+template <typename Pix>
+__device__ float warp_pixel(const Pix *img, int h, int w, float u, float v, int i, int j, bool first) {
+    float sI = first ? (float)i - u : (float)i + u;
+    float sJ = first ? (float)j - v : (float)j + v;
+    int pI = (int)(short)java_round(sI), pJ = (int)(short)java_round(sJ);
+    if (pI < 0) { sI = 0.0f; pI = 0; }
+    else if (pI >= h) { sI = (float)(h - 1); pI = h - 1; }
+    if (pJ < 0) { sJ = 0.0f; pJ = 0; }
+    else if (pJ >= w) { sJ = (float)(w - 1); pJ = w - 1; }
+    const float dU = sI - (float)pI, dV = sJ - (float)pJ;
+    int oI = dU >= 0.0f ? 1 : -1, oJ = dV >= 0.0f ? 1 : -1;
+    if (oI + pI < 0 || oI + pI >= h) oI = 0;
+    if (oJ + pJ < 0 || oJ + pJ >= w) oJ = 0;
+    const float wU = fabsf(dU), wV = fabsf(dV);
+    const float tl = warp_read(img, w, pI, pJ);
+    const float tr = warp_read(img, w, pI, pJ + oJ);
+    const float bl = warp_read(img, w, pI + oI, pJ);
+    const float br = warp_read(img, w, pI + oI, pJ + oJ);
+    const float a = (1.0f - wU) * (1.0f - wV) * tl;
+    const float b = (1.0f - wU) * wV * tr;
+    const float c = wU * (1.0f - wV) * bl;
+    const float d = wU * wV * br;
+    return (float)java_round(a + b + c + d);
+}
+
+template <typename Pix>
+__device__ __forceinline__ Pix warp_store(float value, int int16_quirk) {
+    const int r = java_round(value);
+    if (sizeof(Pix) == 1) return (Pix)(uint8_t)(int8_t)r;
+    if (int16_quirk) return (Pix)(uint16_t)(int16_t)(int8_t)r;  // MatrixInt16.setElement(float) narrows via byte
+    return (Pix)(uint16_t)r;
+}
+
+// Canonical field evaluation order shared with the oracle.
+__device__ __forceinline__ double field_value(const double *ys, int ni, const double *xs, int nj, const float *f,
+                                              const double *fy, const double *fx, const double *fyx, double y,
+                                              double x) {
+    const int i = knot_interval(ys, ni, y), j = knot_interval(xs, nj, x);
+    const double dy = ys[i + 1] - ys[i], dx = xs[j + 1] - xs[j];
+    const double ty = (y - ys[i]) / dy, tx = (x - xs[j]) / dx;
+    double ay0[2], ay1[2], ax0[2], ax1[2];
+    hermite_basis(ty, ay0, ay1);
+    hermite_basis(tx, ax0, ax1);
+    const double X0 = ax0[0], X1 = ax0[1], X2 = dx * ax1[0], X3 = dx * ax1[1];
+    const double Y0 = ay0[0], Y1 = ay0[1], Y2 = dy * ay1[0], Y3 = dy * ay1[1];
+    double w[4];
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+        const long k0 = (long)(i + a) * nj + j, k1 = k0 + 1;
+        w[a] = (double)f[k0] * X0 + (double)f[k1] * X1 + fx[k0] * X2 + fx[k1] * X3;
+        w[2 + a] = fy[k0] * X0 + fy[k1] * X1 + fyx[k0] * X2 + fyx[k1] * X3;
+    }
+    return w[0] * Y0 + w[1] * Y1 + w[2] * Y2 + w[3] * Y3;
+}
+
+// One thread per pixel of one pair (blockIdx.z = pair).  src/dst frame tables hold the
+// original and the warped images.
+template <typename Pix>
+__global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, const qlpiv_frame *dst,
+                                                        const double *ys, int ni, const double *xs, int nj,
+                                                        const float *u, const float *v, SplineCoef coef,
+                                                        int int16_quirk) {
+    const int pair = blockIdx.z;
+    const qlpiv_frame fs = src[pair];
+    const int h = fs.height, w = fs.width;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= h || j >= w) return;
+    const qlpiv_frame fd = dst[pair];
+    const long base = (long)pair * ni * nj;
+    const float ymin = (float)ys[0], ymax = (float)ys[ni - 1], xmin = (float)xs[0], xmax = (float)xs[nj - 1];
+    float y = (float)i, x = (float)j;
+    if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
+    if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
+    const float fu = (float)field_value(ys, ni, xs, nj, u + base, coef.fy_u + base, coef.fx_u + base,
+                                        coef.fyx_u + base, (double)y, (double)x);
+    const float fv = (float)field_value(ys, ni, xs, nj, v + base, coef.fy_v + base, coef.fx_v + base,
+                                        coef.fyx_v + base, (double)y, (double)x);
+    const float hu = fu / 2.0f, hv = fv / 2.0f;
+    const Pix *ia = reinterpret_cast<const Pix *>(fs.img_a);
+    const Pix *ib = reinterpret_cast<const Pix *>(fs.img_b);
+    Pix *oa = reinterpret_cast<Pix *>(const_cast<void *>(fd.img_a));
+    Pix *ob = reinterpret_cast<Pix *>(const_cast<void *>(fd.img_b));
+    oa[(long)i * fd.pitch + j] = warp_store<Pix>(warp_pixel(ia, h, w, hu, hv, i, j, true), int16_quirk);
+    ob[(long)i * fd.pitch + j] = warp_store<Pix>(warp_pixel(ib, h, w, hu, hv, i, j, false), int16_quirk);
+}
+
+// Per-pixel field only (test hook for the field stage): pair 0, outputs h x w floats.
+__global__ void field_kernel(int h, int w, const double *ys, int ni, const double *xs, int nj, const float *u,
+                             const float *v, SplineCoef coef, float *fu_out, float *fv_out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= h || j >= w) return;
+    const float ymin = (float)ys[0], ymax = (float)ys[ni - 1], xmin = (float)xs[0], xmax = (float)xs[nj - 1];
+    float y = (float)i, x = (float)j;
+    if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
+    if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
+    fu_out[(long)i * w + j] =
+        (float)field_value(ys, ni, xs, nj, u, coef.fy_u, coef.fx_u, coef.fyx_u, (double)y, (double)x);
+    fv_out[(long)i * w + j] =
+        (float)field_value(ys, ni, xs, nj, v, coef.fy_v, coef.fx_v, coef.fyx_v, (double)y, (double)x);
+}
+
+// B tile origins for non-warping modes: round(top + u), round(left + v)
+// (NoImageWarpingStrategy.java:80, FastMath.round of Tile.getDisplacedTileTop()).
+__global__ void displaced_origins_kernel(long count, const int *a_top, const int *a_left, const float *u,
+                                         const float *v, int *b_top, int *b_left) {
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    b_top[k] = java_round((float)a_top[k] + u[k]);
+    b_left[k] = java_round((float)a_left[k] + v[k]);
+}
+
+// ---------------- launchers ----------------
+
+static inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+cudaError_t launch_inherit(cudaStream_t s, int pairs, const double *py, int pni, const double *px, int pnj,
+                           const float *pu, const float *pv, const float *cy, int cni, const float *cx, int cnj,
+                           int round_int, float *cu, float *cv) {
+    const long n = (long)pairs * cni * cnj;
+    if (n == 0) return cudaSuccess;
+    inherit_kernel<<<blocks_for(n, 128), 128, 0, s>>>(pairs, py, pni, px, pnj, pu, pv, cy, cni, cx, cnj, round_int,
+                                                      cu, cv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const double *cpy, int ni, const double *xs,
+                          const double *cpx, int nj, const float *u, const float *v, SplineCoef coef) {
+    spline_factor_kernel<<<1, 1, 0, s>>>(ys, ni, const_cast<double *>(cpy));
+    spline_factor_kernel<<<1, 1, 0, s>>>(xs, nj, const_cast<double *>(cpx));
+    const long lines = (long)pairs * 2 * (ni + nj);
+    spline_lines_kernel<<<blocks_for(lines, 64), 64, 0, s>>>(pairs, ys, cpy, ni, xs, cpx, nj, u, v, coef);
+    const long nodes = (long)pairs * ni * nj;
+    spline_cross_kernel<<<blocks_for(nodes, 256), 256, 0, s>>>(pairs, ys, ni, xs, nj, u, v, coef);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
+                        const qlpiv_frame *dst, const double *ys, int ni, const double *xs, int nj, const float *u,
+                        const float *v, SplineCoef coef, int int16_quirk) {
+    dim3 blk(32, 8), grd(blocks_for(w, 32), blocks_for(h, 8), pairs);
+    if (pixel_type == QLPIV_PIX_U8)
+        warp_both_kernel<uint8_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, u, v, coef, int16_quirk);
+    else if (pixel_type == QLPIV_PIX_U16)
+        warp_both_kernel<uint16_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, u, v, coef, int16_quirk);
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_field(cudaStream_t s, int h, int w, const double *ys, int ni, const double *xs, int nj,
+                         const float *u, const float *v, SplineCoef coef, float *fu, float *fv) {
+    dim3 blk(32, 8), grd(blocks_for(w, 32), blocks_for(h, 8), 1);
+    field_kernel<<<grd, blk, 0, s>>>(h, w, ys, ni, xs, nj, u, v, coef, fu, fv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_displaced_origins(cudaStream_t s, long count, const int *a_top, const int *a_left, const float *u,
+                                     const float *v, int *b_top, int *b_left) {
+    if (count == 0) return cudaSuccess;
+    displaced_origins_kernel<<<blocks_for(count, 256), 256, 0, s>>>(count, a_top, a_left, u, v, b_top, b_left);
+    return cudaGetLastError();
+}
+
+}  // namespace qlpiv

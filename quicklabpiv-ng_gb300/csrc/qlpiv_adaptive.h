@@ -1,0 +1,35 @@
+// Adaptive multi-pass stage launchers (qlpiv_adaptive.cu) and host-side grids
+// (qlpiv_grid.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "qlpiv.h"
+
+namespace qlpiv {
+
+// Knot derivatives of the bicubic displacement surfaces, [pairs][ni*nj] doubles each.
+struct SplineCoef {
+    double *fy_u, *fx_u, *fyx_u;
+    double *fy_v, *fx_v, *fyx_v;
+};
+
+cudaError_t launch_inherit(cudaStream_t s, int pairs, const double *py, int pni, const double *px, int pnj,
+                           const float *pu, const float *pv, const float *cy, int cni, const float *cx, int cnj,
+                           int round_int, float *cu, float *cv);
+// cpy/cpx: scratch of ni/nj doubles for the elimination factors.
+cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const double *cpy, int ni, const double *xs,
+                          const double *cpx, int nj, const float *u, const float *v, SplineCoef coef);
+cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
+                        const qlpiv_frame *dst, const double *ys, int ni, const double *xs, int nj, const float *u,
+                        const float *v, SplineCoef coef, int int16_quirk);
+cudaError_t launch_field(cudaStream_t s, int h, int w, const double *ys, int ni, const double *xs, int nj,
+                         const float *u, const float *v, SplineCoef coef, float *fu, float *fv);
+cudaError_t launch_displaced_origins(cudaStream_t s, long count, const int *a_top, const int *a_left, const float *u,
+                                     const float *v, int *b_top, int *b_left);
+
+int grid_superposition(int h, int w, const int margins[4], int ia_start, int level, float ofac, qlpiv_grid *g,
+                       int32_t *tops, int32_t *lefts, int cap);
+int grid_nosuperposition(int h, int w, const int margins[4], int ia_start, int level, qlpiv_grid *g, int32_t *tops,
+                         int32_t *lefts, int cap);
+
+}  // namespace qlpiv

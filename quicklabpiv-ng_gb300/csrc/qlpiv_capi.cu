@@ -9,12 +9,17 @@
 #include <string>
 #include <vector>
 
+#include "qlpiv_handle.h"
 #include "qlpiv_internal.h"
 #include "qlpiv_xcorr.cuh"
 
 namespace {
 
 thread_local std::string g_last_error;
+
+}  // namespace
+
+namespace qlpiv {
 
 qlpiv_status fail(qlpiv_status st, const char *fmt, ...) {
     char buf[512];
@@ -31,54 +36,15 @@ qlpiv_status cuda_fail(cudaError_t e, const char *what) {
     return fail(QLPIV_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
-// Device buffer that only grows.
-struct DevBuf {
-    void *p = nullptr;
-    size_t cap = 0;
-    cudaError_t ensure(size_t bytes) {
-        if (bytes <= cap) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        size_t want = bytes < 256 ? 256 : bytes;
-        cudaError_t e = cudaMalloc(&p, want);
-        if (e == cudaSuccess) cap = want;
-        return e;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
+}  // namespace qlpiv
 
-}  // namespace
-
-struct qlpiv_handle {
-    int device = 0;
-    int num_sms = 0;
-    cudaStream_t stream = nullptr;       // stream work is queued on
-    cudaStream_t own_stream = nullptr;   // the handle's own non-blocking stream
-    std::mutex mu;
-    long launches = 0;
-    DevBuf tiles_a, tiles_b, max_a, max_b, origins, vectors, planes, frames;
-};
+using qlpiv::cuda_fail;
+using qlpiv::DeviceScope;
+using qlpiv::DevBuf;
+using qlpiv::fail;
 
 namespace {
 
-// Makes the handle's device current for the calling thread and restores the previous
-// device on scope exit.
-struct DeviceScope {
-    int prev = -1;
-    cudaError_t err = cudaSuccess;
-    explicit DeviceScope(int dev) {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) err = cudaSetDevice(dev);
-    }
-    ~DeviceScope() {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
 
 qlpiv_status check_desc(const qlpiv_pass_desc *d) {
     if (!d) return fail(QLPIV_E_ARG, "pass descriptor is NULL");
@@ -290,6 +256,9 @@ qlpiv_status qlpiv_destroy(qlpiv_handle *h) {
         for (DevBuf *b : {&h->tiles_a, &h->tiles_b, &h->max_a, &h->max_b, &h->origins, &h->vectors, &h->planes,
                           &h->frames})
             b->release();
+        for (DevBuf &b : h->scratch) b.release();
+        if (h->plan) qlpiv::destroy_plan(h->plan);
+        h->plan = nullptr;
     }
     delete h;
     return QLPIV_OK;

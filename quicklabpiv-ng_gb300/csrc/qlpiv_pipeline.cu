@@ -1,0 +1,498 @@
+// Adaptive multi-pass PIV on the device (host orchestration) and the C ABI of the
+// stages around the correlation: grids, velocity inheritance, displacement field,
+// image warping.  Declarations and reference citations: include/qlpiv.h.
+//
+// Level loop (LocalPIVOpenCLGpuJob.java:188-411, SimpleStrategy): for each level L
+//   tiles of L (grid)          -> host, cached in the plan
+//   inheritance from L-1       -> inherit kernel (level 0: zero)
+//   warp / clip                -> spline + warp kernels (BothImages), or displaced B
+//                                 origins (no warping)
+//   xcorr + peak + sub-pixel   -> K1, which also accumulates the increment into the
+//                                 level's tile displacements
+// Everything stays on the device; only the last level's displacements leave it.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "qlpiv_adaptive.h"
+#include "qlpiv_handle.h"
+#include "qlpiv_internal.h"
+#include "qlpiv_xcorr.cuh"
+
+namespace qlpiv {
+
+struct LevelPlan {
+    qlpiv_grid g{};
+    std::vector<int32_t> tops, lefts;
+    std::vector<double> cy, cx;      // tile centres (top + N/2 - 0.5), double
+    std::vector<float> cyf, cxf;     // same, float
+    DevBuf d_cy, d_cx, d_cyf, d_cxf, d_cpy, d_cpx;
+    DevBuf d_fi, d_at, d_al, d_bt, d_bl;  // flattened work list, pairs x count
+    DevBuf d_u, d_v;                       // tile displacements, pairs x count
+    DevBuf coef;                           // 6 x pairs x count doubles
+    long count() const { return (long)g.tiles_i * g.tiles_j; }
+};
+
+struct AdaptivePlan {
+    qlpiv_adaptive_desc desc{};
+    int pixel_type = -1, height = 0, width = 0, pairs = 0;
+    std::vector<LevelPlan> levels;
+    DevBuf warped;        // 2 x pairs x height x width pixels
+    DevBuf warped_table;  // pairs qlpiv_frame entries
+    DevBuf host_frames;   // images uploaded by qlpiv_piv_adaptive (host variant)
+    DevBuf host_table;
+};
+
+void destroy_plan(AdaptivePlan *p) {
+    if (!p) return;
+    for (LevelPlan &l : p->levels)
+        for (DevBuf *b : {&l.d_cy, &l.d_cx, &l.d_cyf, &l.d_cxf, &l.d_cpy, &l.d_cpx, &l.d_fi, &l.d_at, &l.d_al, &l.d_bt,
+                          &l.d_bl, &l.d_u, &l.d_v, &l.coef})
+            b->release();
+    for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table}) b->release();
+    delete p;
+}
+
+static float full_scale(int pixel_type) { return pixel_type == QLPIV_PIX_U8 ? 255.0f : 65535.0f; }
+
+static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type, int height, int width) {
+    if (!d) return fail(QLPIV_E_ARG, "adaptive descriptor is NULL");
+    if (pixel_type != QLPIV_PIX_U8 && pixel_type != QLPIV_PIX_U16)
+        return fail(QLPIV_E_ARG, "adaptive PIV takes u8 or u16 images");
+    if (height <= 0 || width <= 0) return fail(QLPIV_E_SHAPE, "image size %d x %d", height, width);
+    if (d->ia_end <= 0 || d->ia_start < d->ia_end || d->ia_start % d->ia_end != 0)
+        return fail(QLPIV_E_ARG, "IA start %d must be a multiple of IA end %d", d->ia_start, d->ia_end);
+    int r = d->ia_start / d->ia_end;
+    if ((r & (r - 1)) != 0) return fail(QLPIV_E_ARG, "IA start / end ratio is not a power of two");
+    for (int n = d->ia_start; n >= d->ia_end; n >>= 1)
+        if (!xcorr_size_supported(n)) return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64)", n);
+    if (d->warp_mode != QLPIV_WARP_NONE && d->warp_mode != QLPIV_WARP_BOTH_BILINEAR)
+        return fail(QLPIV_E_ARG, "unknown warp mode %d", d->warp_mode);
+    if (d->norm_mode != QLPIV_NORM_MAX_A && d->norm_mode != QLPIV_NORM_OWN_MAX && d->norm_mode != QLPIV_NORM_NONE)
+        return fail(QLPIV_E_ARG, "unknown normalisation mode %d", d->norm_mode);
+    if (d->max_mode != QLPIV_MAX_COMPUTE && d->max_mode != QLPIV_MAX_FIXED)
+        return fail(QLPIV_E_ARG, "max mode %d not valid for adaptive PIV", d->max_mode);
+    if (d->subpix_mode != QLPIV_SUBPIX_NONE && d->subpix_mode != QLPIV_SUBPIX_GAUSS3)
+        return fail(QLPIV_E_ARG, "unknown sub-pixel mode %d", d->subpix_mode);
+    if (!(d->overlap_factor >= 0.1f && d->overlap_factor <= 0.9f))
+        return fail(QLPIV_E_ARG, "Overlap factor must greater than 1/10 and less than 9/10");
+    return QLPIV_OK;
+}
+
+static int level_count(const qlpiv_adaptive_desc *d) {
+    int k = 0;
+    for (int n = d->ia_start; n >= d->ia_end; n >>= 1) k++;
+    return k;
+}
+
+static cudaError_t upload(DevBuf &b, const void *src, size_t bytes, cudaStream_t s) {
+    cudaError_t e = b.ensure(bytes);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, s);
+}
+
+// (Re)builds the plan for this geometry.  Host arrays uploaded here are consumed by
+// the stream before the next rebuild (the caller synchronises on rebuild).
+static qlpiv_status build_plan(qlpiv_handle *h, const qlpiv_adaptive_desc *d, int pixel_type, int height, int width,
+                               int pairs) {
+    AdaptivePlan *p = h->plan;
+    if (p && p->pixel_type == pixel_type && p->height == height && p->width == width && p->pairs == pairs &&
+        std::memcmp(&p->desc, d, sizeof(*d)) == 0)
+        return QLPIV_OK;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "plan rebuild");
+    if (p) destroy_plan(p);
+    h->plan = p = new AdaptivePlan();
+    p->desc = *d;
+    p->pixel_type = pixel_type;
+    p->height = height;
+    p->width = width;
+    p->pairs = pairs;
+    const int nlev = level_count(d);
+    p->levels.resize(nlev);
+    for (int lv = 0; lv < nlev; lv++) {
+        LevelPlan &L = p->levels[lv];
+        if (grid_superposition(height, width, d->margins, d->ia_start, lv, d->overlap_factor, &L.g, nullptr, nullptr,
+                               0) < -1)
+            return fail(QLPIV_E_SHAPE, "image too small for IA %d at level %d", d->ia_start >> lv, lv);
+        if (d->warp_mode == QLPIV_WARP_BOTH_BILINEAR && lv > 0 && (L.g.tiles_i < 3 || L.g.tiles_j < 3))
+            return fail(QLPIV_E_SHAPE, "level %d has %d x %d tiles: the warp spline needs at least 3 per axis", lv,
+                        L.g.tiles_i, L.g.tiles_j);
+        L.tops.resize(L.g.tiles_i);
+        L.lefts.resize(L.g.tiles_j);
+        grid_superposition(height, width, d->margins, d->ia_start, lv, d->overlap_factor, &L.g, L.tops.data(),
+                           L.lefts.data(), 1 << 30);
+        const int n = L.g.n, ni = L.g.tiles_i, nj = L.g.tiles_j;
+        L.cyf.resize(ni);
+        L.cxf.resize(nj);
+        L.cy.resize(ni);
+        L.cx.resize(nj);
+        for (int i = 0; i < ni; i++) {
+            L.cyf[i] = (float)L.tops[i] + (float)n / 2.0f - 0.5f;
+            L.cy[i] = (double)L.cyf[i];
+        }
+        for (int j = 0; j < nj; j++) {
+            L.cxf[j] = (float)L.lefts[j] + (float)n / 2.0f - 0.5f;
+            L.cx[j] = (double)L.cxf[j];
+        }
+        const long cnt = L.count(), total = cnt * pairs;
+        std::vector<int32_t> fi(total), at(total), al(total);
+        for (int q = 0; q < pairs; q++)
+            for (int i = 0; i < ni; i++)
+                for (int j = 0; j < nj; j++) {
+                    const long k = (long)q * cnt + (long)i * nj + j;
+                    fi[k] = q;
+                    at[k] = L.tops[i];
+                    al[k] = L.lefts[j];
+                }
+        cudaStream_t s = h->stream;
+        if ((e = upload(L.d_cy, L.cy.data(), sizeof(double) * ni, s)) != cudaSuccess ||
+            (e = upload(L.d_cx, L.cx.data(), sizeof(double) * nj, s)) != cudaSuccess ||
+            (e = upload(L.d_cyf, L.cyf.data(), sizeof(float) * ni, s)) != cudaSuccess ||
+            (e = upload(L.d_cxf, L.cxf.data(), sizeof(float) * nj, s)) != cudaSuccess ||
+            (e = L.d_cpy.ensure(sizeof(double) * ni)) != cudaSuccess ||
+            (e = L.d_cpx.ensure(sizeof(double) * nj)) != cudaSuccess ||
+            (e = upload(L.d_fi, fi.data(), sizeof(int32_t) * total, s)) != cudaSuccess ||
+            (e = upload(L.d_at, at.data(), sizeof(int32_t) * total, s)) != cudaSuccess ||
+            (e = upload(L.d_al, al.data(), sizeof(int32_t) * total, s)) != cudaSuccess ||
+            (e = L.d_bt.ensure(sizeof(int32_t) * total)) != cudaSuccess ||
+            (e = L.d_bl.ensure(sizeof(int32_t) * total)) != cudaSuccess ||
+            (e = L.d_u.ensure(sizeof(float) * total)) != cudaSuccess ||
+            (e = L.d_v.ensure(sizeof(float) * total)) != cudaSuccess ||
+            (e = L.coef.ensure(sizeof(double) * 6 * total)) != cudaSuccess)
+            return cuda_fail(e, "adaptive plan");
+        // the host vectors above die at scope exit: make the copies complete first
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "adaptive plan upload");
+    }
+    if (d->warp_mode == QLPIV_WARP_BOTH_BILINEAR) {
+        const size_t img = (size_t)height * width * pixel_bytes(pixel_type);
+        const size_t stride = (img + 255) & ~(size_t)255;
+        if ((e = p->warped.ensure(2 * stride * pairs)) != cudaSuccess ||
+            (e = p->warped_table.ensure(sizeof(qlpiv_frame) * pairs)) != cudaSuccess)
+            return cuda_fail(e, "warp buffers");
+        std::vector<qlpiv_frame> t(pairs);
+        char *base = p->warped.as<char>();
+        for (int q = 0; q < pairs; q++)
+            t[q] = {base + 2 * q * stride, base + (2 * q + 1) * stride, height, width, (int64_t)width};
+        if ((e = cudaMemcpyAsync(p->warped_table.p, t.data(), sizeof(qlpiv_frame) * pairs, cudaMemcpyHostToDevice,
+                                 h->stream)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
+            return cuda_fail(e, "warp table");
+    }
+    return QLPIV_OK;
+}
+
+static SplineCoef coef_of(LevelPlan &L, int pairs) {
+    double *c = L.coef.as<double>();
+    const long n = L.count() * pairs;
+    return SplineCoef{c, c + n, c + 2 * n, c + 3 * n, c + 4 * n, c + 5 * n};
+}
+
+// Queues the whole level loop; the last level's displacements end in levels.back().d_u/d_v.
+static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
+    AdaptivePlan *p = h->plan;
+    const qlpiv_adaptive_desc &d = p->desc;
+    cudaStream_t s = h->stream;
+    cudaError_t e;
+    const int pairs = p->pairs;
+    const float fm = d.fixed_max > 0.0f ? d.fixed_max : full_scale(p->pixel_type);
+    for (size_t lv = 0; lv < p->levels.size(); lv++) {
+        LevelPlan &L = p->levels[lv];
+        const long total = L.count() * pairs;
+        float *u = L.d_u.as<float>(), *v = L.d_v.as<float>();
+        if (lv == 0) {
+            if ((e = cudaMemsetAsync(u, 0, sizeof(float) * total, s)) != cudaSuccess ||
+                (e = cudaMemsetAsync(v, 0, sizeof(float) * total, s)) != cudaSuccess)
+                return cuda_fail(e, "level 0 reset");
+        } else {
+            LevelPlan &P = p->levels[lv - 1];
+            if ((e = launch_inherit(s, pairs, P.d_cy.as<double>(), P.g.tiles_i, P.d_cx.as<double>(), P.g.tiles_j,
+                                    P.d_u.as<float>(), P.d_v.as<float>(), L.d_cyf.as<float>(), L.g.tiles_i,
+                                    L.d_cxf.as<float>(), L.g.tiles_j, d.warp_mode == QLPIV_WARP_NONE, u, v)) !=
+                cudaSuccess)
+                return cuda_fail(e, "inheritance");
+            h->launches++;
+        }
+        const qlpiv_frame *src = frames_dev;
+        const int *bt = L.d_at.as<int>(), *bl = L.d_al.as<int>();
+        if (d.warp_mode == QLPIV_WARP_BOTH_BILINEAR) {
+            if (lv > 0) {  // no warping at the first level: displacements are all zero
+                SplineCoef c = coef_of(L, pairs);
+                if ((e = launch_spline(s, pairs, L.d_cy.as<double>(), L.d_cpy.as<double>(), L.g.tiles_i,
+                                       L.d_cx.as<double>(), L.d_cpx.as<double>(), L.g.tiles_j, u, v, c)) !=
+                        cudaSuccess ||
+                    (e = launch_warp(s, p->pixel_type, pairs, p->height, p->width, frames_dev,
+                                     p->warped_table.as<qlpiv_frame>(), L.d_cy.as<double>(), L.g.tiles_i,
+                                     L.d_cx.as<double>(), L.g.tiles_j, u, v, c, d.int16_warp_quirk)) != cudaSuccess)
+                    return cuda_fail(e, "warp");
+                h->launches += 5;
+                src = p->warped_table.as<qlpiv_frame>();
+            }
+        } else {
+            if ((e = launch_displaced_origins(s, total, L.d_at.as<int>(), L.d_al.as<int>(), u, v, L.d_bt.as<int>(),
+                                              L.d_bl.as<int>())) != cudaSuccess)
+                return cuda_fail(e, "displaced origins");
+            h->launches++;
+            bt = L.d_bt.as<int>();
+            bl = L.d_bl.as<int>();
+        }
+        IaJob job{};
+        job.frames = src;
+        job.frame_idx = L.d_fi.as<int>();
+        job.a_top = L.d_at.as<int>();
+        job.a_left = L.d_al.as<int>();
+        job.b_top = bt;
+        job.b_left = bl;
+        job.count = total;
+        job.norm_mode = d.norm_mode;
+        job.max_mode = d.max_mode;
+        job.fixed_max_a = job.fixed_max_b = fm;
+        job.subpix = d.subpix_mode == QLPIV_SUBPIX_GAUSS3;
+        job.acc_u = u;
+        job.acc_v = v;
+        if ((e = launch_xcorr(job, L.g.n, p->pixel_type, s, h->num_sms)) != cudaSuccess)
+            return cuda_fail(e, "xcorr");
+        h->launches++;
+    }
+    return QLPIV_OK;
+}
+
+}  // namespace qlpiv
+
+using namespace qlpiv;
+
+extern "C" {
+
+qlpiv_status qlpiv_grid_superposition(int height, int width, const int margins[4], int ia_start, int level,
+                                      float overlap_factor, qlpiv_grid *grid, int32_t *tops, int32_t *lefts,
+                                      int cap) {
+    if (!grid || !margins) return fail(QLPIV_E_ARG, "NULL argument");
+    const int r = qlpiv::grid_superposition(height, width, margins, ia_start, level, overlap_factor, grid, tops, lefts,
+                                            cap);
+    if (r == -2) return fail(QLPIV_E_ARG, "Overlap factor must greater than 1/10 and less than 9/10");
+    if (r == -3) return fail(QLPIV_E_SHAPE, "no IA of size %d fits the image", ia_start >> level);
+    if (r == -1) return fail(QLPIV_E_SHAPE, "grid larger than the given capacity %d", cap);
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_grid_nosuperposition(int height, int width, const int margins[4], int ia_start, int level,
+                                        qlpiv_grid *grid, int32_t *tops, int32_t *lefts, int cap) {
+    if (!grid || !margins) return fail(QLPIV_E_ARG, "NULL argument");
+    const int r = qlpiv::grid_nosuperposition(height, width, margins, ia_start, level, grid, tops, lefts, cap);
+    if (r == -3) return fail(QLPIV_E_SHAPE, "no IA of size %d fits the image", ia_start >> level);
+    if (r == -1) return fail(QLPIV_E_SHAPE, "grid larger than the given capacity %d", cap);
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_adaptive_levels(const qlpiv_adaptive_desc *desc, int height, int width, int *levels,
+                                   qlpiv_grid *grids, int max_levels) {
+    if (!levels) return fail(QLPIV_E_ARG, "levels is NULL");
+    qlpiv_status st = check_adaptive(desc, QLPIV_PIX_U8, height, width);
+    if (st != QLPIV_OK) return st;
+    *levels = level_count(desc);
+    if (grids) {
+        for (int lv = 0; lv < *levels && lv < max_levels; lv++)
+            if (qlpiv::grid_superposition(height, width, desc->margins, desc->ia_start, lv, desc->overlap_factor,
+                                          &grids[lv], nullptr, nullptr, 0) < -1)
+                return fail(QLPIV_E_SHAPE, "image too small for level %d", lv);
+    }
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_inherit(qlpiv_handle *h, int pni, int pnj, const double *p_ci, const double *p_cj, const float *pu,
+                           const float *pv, int cni, int cnj, const float *c_ci, const float *c_cj, int round_int,
+                           float *cu, float *cv) {
+    if (!h || !p_ci || !p_cj || !pu || !pv || !c_ci || !c_cj || !cu || !cv) return fail(QLPIV_E_ARG, "NULL argument");
+    if (pni < 1 || pnj < 1 || cni < 1 || cnj < 1) return fail(QLPIV_E_SHAPE, "empty grid");
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaStream_t s = h->stream;
+    const long pc = (long)pni * pnj, cc = (long)cni * cnj;
+    DevBuf *b = h->scratch;
+    cudaError_t e;
+    if ((e = upload(b[0], p_ci, sizeof(double) * pni, s)) != cudaSuccess ||
+        (e = upload(b[1], p_cj, sizeof(double) * pnj, s)) != cudaSuccess ||
+        (e = upload(b[2], pu, sizeof(float) * pc, s)) != cudaSuccess ||
+        (e = upload(b[3], pv, sizeof(float) * pc, s)) != cudaSuccess ||
+        (e = upload(b[4], c_ci, sizeof(float) * cni, s)) != cudaSuccess ||
+        (e = upload(b[5], c_cj, sizeof(float) * cnj, s)) != cudaSuccess ||
+        (e = b[6].ensure(sizeof(float) * cc)) != cudaSuccess || (e = b[7].ensure(sizeof(float) * cc)) != cudaSuccess)
+        return cuda_fail(e, "inherit upload");
+    if ((e = launch_inherit(s, 1, b[0].as<double>(), pni, b[1].as<double>(), pnj, b[2].as<float>(), b[3].as<float>(),
+                            b[4].as<float>(), cni, b[5].as<float>(), cnj, round_int, b[6].as<float>(),
+                            b[7].as<float>())) != cudaSuccess)
+        return cuda_fail(e, "inherit");
+    h->launches++;
+    if ((e = cudaMemcpyAsync(cu, b[6].p, sizeof(float) * cc, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(cv, b[7].p, sizeof(float) * cc, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "inherit download");
+    return QLPIV_OK;
+}
+
+// Shared set-up of qlpiv_displacement_field / qlpiv_warp_pair: knots and displacements
+// uploaded, spline coefficients computed.  Uses scratch[0..7].
+static qlpiv_status field_setup(qlpiv_handle *h, int ni, int nj, const double *ci, const double *cj, const float *u,
+                                const float *v, SplineCoef *coef) {
+    cudaStream_t s = h->stream;
+    DevBuf *b = h->scratch;
+    const long cnt = (long)ni * nj;
+    cudaError_t e;
+    if ((e = upload(b[0], ci, sizeof(double) * ni, s)) != cudaSuccess ||
+        (e = upload(b[1], cj, sizeof(double) * nj, s)) != cudaSuccess ||
+        (e = upload(b[2], u, sizeof(float) * cnt, s)) != cudaSuccess ||
+        (e = upload(b[3], v, sizeof(float) * cnt, s)) != cudaSuccess ||
+        (e = b[4].ensure(sizeof(double) * (ni + nj))) != cudaSuccess ||
+        (e = b[5].ensure(sizeof(double) * 6 * cnt)) != cudaSuccess)
+        return cuda_fail(e, "field upload");
+    double *c = b[5].as<double>();
+    *coef = SplineCoef{c, c + cnt, c + 2 * cnt, c + 3 * cnt, c + 4 * cnt, c + 5 * cnt};
+    if ((e = launch_spline(s, 1, b[0].as<double>(), b[4].as<double>(), ni, b[1].as<double>(), b[4].as<double>() + ni,
+                           nj, b[2].as<float>(), b[3].as<float>(), *coef)) != cudaSuccess)
+        return cuda_fail(e, "spline");
+    h->launches += 4;
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_displacement_field(qlpiv_handle *h, int height, int width, int ni, int nj, const double *ci,
+                                      const double *cj, const float *u, const float *v, float *fu, float *fv) {
+    if (!h || !ci || !cj || !u || !v || !fu || !fv) return fail(QLPIV_E_ARG, "NULL argument");
+    if (ni < 3 || nj < 3) return fail(QLPIV_E_SHAPE, "the spline needs at least 3 tiles per axis");
+    if (height <= 0 || width <= 0) return fail(QLPIV_E_SHAPE, "image size %d x %d", height, width);
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    SplineCoef coef;
+    qlpiv_status st = field_setup(h, ni, nj, ci, cj, u, v, &coef);
+    if (st != QLPIV_OK) return st;
+    cudaStream_t s = h->stream;
+    DevBuf *b = h->scratch;
+    const size_t px = (size_t)height * width;
+    cudaError_t e;
+    if ((e = b[6].ensure(sizeof(float) * px)) != cudaSuccess || (e = b[7].ensure(sizeof(float) * px)) != cudaSuccess)
+        return cuda_fail(e, "field buffers");
+    if ((e = launch_field(s, height, width, b[0].as<double>(), ni, b[1].as<double>(), nj, b[2].as<float>(),
+                          b[3].as<float>(), coef, b[6].as<float>(), b[7].as<float>())) != cudaSuccess)
+        return cuda_fail(e, "field");
+    h->launches++;
+    if ((e = cudaMemcpyAsync(fu, b[6].p, sizeof(float) * px, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(fv, b[7].p, sizeof(float) * px, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "field download");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, const void *img_a, const void *img_b, int height,
+                             int width, int ni, int nj, const double *ci, const double *cj, const float *u,
+                             const float *v, int int16_quirk, void *out_a, void *out_b) {
+    if (!h || !img_a || !img_b || !ci || !cj || !u || !v || !out_a || !out_b) return fail(QLPIV_E_ARG, "NULL argument");
+    if (pixel_type != QLPIV_PIX_U8 && pixel_type != QLPIV_PIX_U16) return fail(QLPIV_E_ARG, "u8 or u16 images only");
+    if (ni < 3 || nj < 3) return fail(QLPIV_E_SHAPE, "the spline needs at least 3 tiles per axis");
+    if (height <= 0 || width <= 0) return fail(QLPIV_E_SHAPE, "image size %d x %d", height, width);
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    SplineCoef coef;
+    qlpiv_status st = field_setup(h, ni, nj, ci, cj, u, v, &coef);
+    if (st != QLPIV_OK) return st;
+    cudaStream_t s = h->stream;
+    const size_t bytes = (size_t)height * width * pixel_bytes(pixel_type);
+    const size_t stride = (bytes + 255) & ~(size_t)255;
+    cudaError_t e;
+    if ((e = h->tiles_a.ensure(4 * stride)) != cudaSuccess || (e = h->frames.ensure(2 * sizeof(qlpiv_frame))) !=
+        cudaSuccess)
+        return cuda_fail(e, "warp buffers");
+    char *base = h->tiles_a.as<char>();
+    qlpiv_frame t[2] = {{base, base + stride, height, width, (int64_t)width},
+                        {base + 2 * stride, base + 3 * stride, height, width, (int64_t)width}};
+    if ((e = cudaMemcpyAsync(base, img_a, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(base + stride, img_b, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(h->frames.p, t, sizeof(t), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "warp upload");
+    const qlpiv_frame *dt = h->frames.as<qlpiv_frame>();
+    DevBuf *b = h->scratch;
+    if ((e = launch_warp(s, pixel_type, 1, height, width, dt, dt + 1, b[0].as<double>(), ni, b[1].as<double>(), nj,
+                         b[2].as<float>(), b[3].as<float>(), coef, int16_quirk)) != cudaSuccess)
+        return cuda_fail(e, "warp");
+    h->launches++;
+    if ((e = cudaMemcpyAsync(out_a, base + 2 * stride, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(out_b, base + 3 * stride, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "warp download");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_piv_adaptive_device(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int pixel_type, int height,
+                                       int width, int num_pairs, const qlpiv_frame *frames, float *out_u,
+                                       float *out_v) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    qlpiv_status st = check_adaptive(desc, pixel_type, height, width);
+    if (st != QLPIV_OK) return st;
+    if (num_pairs < 0) return fail(QLPIV_E_ARG, "num_pairs < 0");
+    if (num_pairs == 0) return QLPIV_OK;
+    if (!frames || !out_u || !out_v) return fail(QLPIV_E_ARG, "NULL frame table or output");
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    if ((st = build_plan(h, desc, pixel_type, height, width, num_pairs)) != QLPIV_OK) return st;
+    if ((st = run_levels(h, frames)) != QLPIV_OK) return st;
+    LevelPlan &L = h->plan->levels.back();
+    const size_t bytes = sizeof(float) * L.count() * num_pairs;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(out_u, L.d_u.p, bytes, cudaMemcpyDeviceToDevice, h->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(out_v, L.d_v.p, bytes, cudaMemcpyDeviceToDevice, h->stream)) != cudaSuccess)
+        return cuda_fail(e, "adaptive output");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_piv_adaptive(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int pixel_type, int height,
+                                int width, int num_pairs, const qlpiv_frame *frames, float *out_u, float *out_v) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    qlpiv_status st = check_adaptive(desc, pixel_type, height, width);
+    if (st != QLPIV_OK) return st;
+    if (num_pairs < 0) return fail(QLPIV_E_ARG, "num_pairs < 0");
+    if (num_pairs == 0) return QLPIV_OK;
+    if (!frames || !out_u || !out_v) return fail(QLPIV_E_ARG, "NULL frame table or output");
+    for (int q = 0; q < num_pairs; q++)
+        if (!frames[q].img_a || !frames[q].img_b || frames[q].height != height || frames[q].width != width ||
+            frames[q].pitch < width)
+            return fail(QLPIV_E_SHAPE, "frame %d: NULL image or size differs from %d x %d", q, height, width);
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    if ((st = build_plan(h, desc, pixel_type, height, width, num_pairs)) != QLPIV_OK) return st;
+    AdaptivePlan *p = h->plan;
+    cudaStream_t s = h->stream;
+    const size_t pb = pixel_bytes(pixel_type), row = (size_t)width * pb, img = row * height;
+    const size_t stride = (img + 255) & ~(size_t)255;
+    cudaError_t e;
+    if ((e = p->host_frames.ensure(2 * stride * num_pairs)) != cudaSuccess ||
+        (e = p->host_table.ensure(sizeof(qlpiv_frame) * num_pairs)) != cudaSuccess)
+        return cuda_fail(e, "frame buffers");
+    std::vector<qlpiv_frame> t(num_pairs);
+    char *base = p->host_frames.as<char>();
+    for (int q = 0; q < num_pairs; q++) {
+        char *da = base + 2 * q * stride, *db = base + (2 * q + 1) * stride;
+        if ((e = cudaMemcpy2DAsync(da, row, frames[q].img_a, (size_t)frames[q].pitch * pb, row, height,
+                                   cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpy2DAsync(db, row, frames[q].img_b, (size_t)frames[q].pitch * pb, row, height,
+                                   cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return cuda_fail(e, "frame upload");
+        t[q] = {da, db, height, width, (int64_t)width};
+    }
+    if ((e = cudaMemcpyAsync(p->host_table.p, t.data(), sizeof(qlpiv_frame) * num_pairs, cudaMemcpyHostToDevice,
+                             s)) != cudaSuccess)
+        return cuda_fail(e, "frame table upload");
+    if ((st = run_levels(h, p->host_table.as<qlpiv_frame>())) != QLPIV_OK) return st;
+    LevelPlan &L = p->levels.back();
+    const size_t bytes = sizeof(float) * L.count() * num_pairs;
+    if ((e = cudaMemcpyAsync(out_u, L.d_u.p, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(out_v, L.d_v.p, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "adaptive PIV");
+    return QLPIV_OK;
+}
+
+}  // extern "C"

@@ -86,8 +86,9 @@ struct IaJob {
     long count;
     int norm_mode, max_mode, subpix;
     float fixed_max_a, fixed_max_b;
-    qlpiv_vector *out;
+    qlpiv_vector *out;           // optional per-IA vectors
     float *planes;               // optional (2N-1)^2 planes per IA
+    float *acc_u, *acc_v;        // optional: tile displacements += (u, v)  (Tile.accumulateDisplacement)
 };
 
 template <int N, typename Pix>
@@ -394,7 +395,11 @@ xcorr_kernel(IaJob job) {
             o.peak_i = (int16_t)pi;
             o.peak_j = (int16_t)pj;
             o.flags = flags;
-            job.out[ia] = o;
+            if (job.out != nullptr) job.out[ia] = o;
+            if (job.acc_u != nullptr) {
+                job.acc_u[ia] += o.u;
+                job.acc_v[ia] += o.v;
+            }
         }
         __syncthreads();  // regions are rewritten by the next IA
     }

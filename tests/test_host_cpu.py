@@ -120,3 +120,32 @@ def test_oracle_recovers_synthetic_flow(qp, oracle):
     dr, dc = qp.synth.Flow(vmax=4.0, rc=64.0).displacement(cy, cx, (512, 512))
     err = np.hypot(vec["u"] - dr, vec["v"] - dc)
     assert np.median(err) < 0.2
+
+
+@pytest.mark.parametrize("h,w,n,levels,ofac,margins", [
+    (512, 512, 32, 1, 0.5, (0, 0, 0, 0)),
+    (1024, 1024, 64, 3, 0.25, (0, 0, 0, 0)),
+    (139, 139, 64, 2, 1.0 / 3.0, (16, 16, 16, 16)),
+    (600, 800, 128, 4, 0.5, (3, 5, 7, 11)),
+    (777, 333, 32, 2, 0.3, (1, 2, 3, 4)),
+])
+def test_library_grid_matches_oracle(qp, oracle, h, w, n, levels, ofac, margins):
+    """The C++ grid of libqlpiv_gpu.so (used by the device pipeline) is the reference's
+    geometry; checked on the host without a GPU."""
+    for lv in range(levels):
+        g, tops, lefts = qp.library_grid(h, w, n, lv, ofac, margins)
+        o, ot, ol = oracle.grid(h, w, n, lv, ofac, margins)
+        assert g == o and (tops == ot).all() and (lefts == ol).all()
+        g2, t2, l2 = qp.library_grid(h, w, n, lv, ofac, margins, superposition=False)
+        o2, ot2, ol2 = oracle.grid(h, w, n, lv, margins=margins, superposition=False)
+        assert g2 == o2 and (t2 == ot2).all() and (l2 == ol2).all()
+
+
+def test_adaptive_levels_config2(qp):
+    d = qp.adaptive_desc(64, 16, 0.25)
+    lv = qp.adaptive_levels(d, 1024, 1024)
+    assert [(g["n"], g["tiles_i"], g["tiles_j"]) for g in lv] == [(64, 61, 61), (32, 125, 125), (16, 253, 253)]
+    with pytest.raises(qp.QlpivError):
+        qp.adaptive_levels(qp.adaptive_desc(64, 24, 0.25), 1024, 1024)
+    with pytest.raises(qp.QlpivError):
+        qp.adaptive_levels(qp.adaptive_desc(128, 16, 0.25), 1024, 1024)   # IA 128 not built yet
