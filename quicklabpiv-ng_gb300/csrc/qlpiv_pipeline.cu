@@ -94,8 +94,8 @@ static cudaError_t upload(DevBuf &b, const void *src, size_t bytes, cudaStream_t
 
 // (Re)builds the plan for this geometry.  Host arrays uploaded here are consumed by
 // the stream before the next rebuild (the caller synchronises on rebuild).
-static qlpiv_status build_plan(qlpiv_handle *h, const qlpiv_adaptive_desc *d, int pixel_type, int height, int width,
-                               int pairs) {
+static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc *d, int pixel_type, int height,
+                                     int width, int pairs) {
     AdaptivePlan *p = h->plan;
     if (p && p->pixel_type == pixel_type && p->height == height && p->width == width && p->pairs == pairs &&
         std::memcmp(&p->desc, d, sizeof(*d)) == 0)
@@ -181,6 +181,16 @@ static qlpiv_status build_plan(qlpiv_handle *h, const qlpiv_adaptive_desc *d, in
             return cuda_fail(e, "warp table");
     }
     return QLPIV_OK;
+}
+
+static qlpiv_status build_plan(qlpiv_handle *h, const qlpiv_adaptive_desc *d, int pixel_type, int height, int width,
+                               int pairs) {
+    qlpiv_status st = build_plan_inner(h, d, pixel_type, height, width, pairs);
+    if (st != QLPIV_OK && h->plan) {  // never leave a half-built plan behind
+        destroy_plan(h->plan);
+        h->plan = nullptr;
+    }
+    return st;
 }
 
 static SplineCoef coef_of(LevelPlan &L, int pairs) {
