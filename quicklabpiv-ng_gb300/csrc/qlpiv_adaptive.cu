@@ -27,7 +27,7 @@ namespace qlpiv {
 
 // ---------------- shared device helpers ----------------
 
-__device__ __forceinline__ int knot_interval(const double *v, int n, double c) {
+__host__ __device__ __forceinline__ int knot_interval(const double *v, int n, double c) {
     int lo = 0, hi = n - 1;
     if (c >= v[n - 1]) return n - 2;
     while (hi - lo > 1) {
@@ -37,7 +37,7 @@ __device__ __forceinline__ int knot_interval(const double *v, int n, double c) {
     return lo;
 }
 
-__device__ __forceinline__ void hermite_basis(double t, double h0[2], double h1[2]) {
+__host__ __device__ __forceinline__ void hermite_basis(double t, double h0[2], double h1[2]) {
     const double t2 = t * t, t3 = t2 * t;
     h0[0] = 2.0 * t3 - 3.0 * t2 + 1.0;
     h0[1] = -2.0 * t3 + 3.0 * t2;
@@ -45,7 +45,7 @@ __device__ __forceinline__ void hermite_basis(double t, double h0[2], double h1[
     h1[1] = t3 - t2;
 }
 
-__device__ __forceinline__ double parabola_deriv(const double *x, const double *y, int at, int i0, int i1, int i2) {
+__host__ __device__ __forceinline__ double parabola_deriv(const double *x, const double *y, int at, int i0, int i1, int i2) {
     const double X = x[at];
     const double x0 = x[i0], x1 = x[i1], x2 = x[i2];
     return y[i0] * ((X - x1) + (X - x2)) / ((x0 - x1) * (x0 - x2)) +
@@ -54,7 +54,7 @@ __device__ __forceinline__ double parabola_deriv(const double *x, const double *
 }
 
 // Akima spline through 5 knots, evaluated at t (knots ascending, t inside).
-__device__ double akima5_value(const double *x, const double *y, double t) {
+__host__ __device__ double akima5_value(const double *x, const double *y, double t) {
     double d[4], w[4] = {0.0, 0.0, 0.0, 0.0}, fd[5];
     for (int k = 0; k < 4; k++) d[k] = (y[k + 1] - y[k]) / (x[k + 1] - x[k]);
     for (int k = 1; k < 4; k++) w[k] = fabs(d[k] - d[k - 1]);
@@ -76,7 +76,7 @@ __device__ double akima5_value(const double *x, const double *y, double t) {
     return y[k] + s * (fd[k] + s * (c2 + s * c3));
 }
 
-__device__ __forceinline__ int akima_window(const double *v, int n, double c) {
+__host__ __device__ __forceinline__ int akima_window(const double *v, int n, double c) {
     int lo = 0, hi = n;
     while (lo < hi) {
         const int mid = (lo + hi) / 2;
@@ -90,17 +90,15 @@ __device__ __forceinline__ int akima_window(const double *v, int n, double c) {
     return r;
 }
 
-__device__ __forceinline__ int java_round(float x) { return (int)floorf(x + 0.5f); }
+__host__ __device__ __forceinline__ int java_round(float x) { return (int)floorf(x + 0.5f); }
 
 // ---------------- B-inherit ----------------
 
-// One thread per (pair, child tile).  Parent arrays are [pairs][pni*pnj].
-__global__ void inherit_kernel(int pairs, const double *py, int pni, const double *px, int pnj, const float *pu,
-                               const float *pv, const float *cy, int cni, const float *cx, int cnj, int round_int,
-                               float *cu, float *cv) {
+// Inherited displacement of child tile gid = pair * cni*cnj + i * cnj + j.
+__host__ __device__ void inherit_one(long gid, const double *py, int pni, const double *px, int pnj, const float *pu,
+                                     const float *pv, const float *cy, int cni, const float *cx, int cnj,
+                                     int round_int, float *cu, float *cv) {
     const long cnt = (long)cni * cnj;
-    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= cnt * pairs) return;
     const int pair = (int)(gid / cnt);
     const long k = gid - (long)pair * cnt;
     const int i = (int)(k / cnj), j = (int)(k - (long)i * cnj);
@@ -137,11 +135,19 @@ __global__ void inherit_kernel(int pairs, const double *py, int pni, const doubl
     }
 }
 
+// One thread per (pair, child tile).  Parent arrays are [pairs][pni*pnj].
+__global__ void inherit_kernel(int pairs, const double *py, int pni, const double *px, int pnj, const float *pu,
+                               const float *pv, const float *cy, int cni, const float *cx, int cnj, int round_int,
+                               float *cu, float *cv) {
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long)cni * cnj * pairs) return;
+    inherit_one(gid, py, pni, px, pnj, pu, pv, cy, cni, cx, cnj, round_int, cu, cv);
+}
+
 // ---------------- B-field spline set-up ----------------
 
-// cp[i] of the natural-spline tridiagonal elimination for knots v[n] (one thread).
-__global__ void spline_factor_kernel(const double *v, int n, double *cp) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// cp[i] of the natural-spline tridiagonal elimination for knots v[n].
+__host__ __device__ void spline_factor(const double *v, int n, double *cp) {
     cp[0] = 0.0;
     for (int i = 1; i < n - 1; i++) {
         const double h0 = v[i] - v[i - 1], h1 = v[i + 1] - v[i];
@@ -152,8 +158,13 @@ __global__ void spline_factor_kernel(const double *v, int n, double *cp) {
     if (n > 1) cp[n - 1] = 0.0;
 }
 
+__global__ void spline_factor_kernel(const double *v, int n, double *cp) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    spline_factor(v, n, cp);
+}
+
 // Knot derivatives of one grid line of f (float values, stride fs) into out (stride os).
-__device__ void spline_line(const double *x, const double *cp, int n, const float *f, long fs, double *out, long os) {
+__host__ __device__ void spline_line(const double *x, const double *cp, int n, const float *f, long fs, double *out, long os) {
     auto Y = [&](int i) -> double { return (double)f[(long)i * fs]; };
     out[0] = 0.0;
     double dprev = 0.0;
@@ -190,12 +201,10 @@ __device__ void spline_line(const double *x, const double *cp, int n, const floa
     }
 }
 
-// Threads: pairs x 2 components x (nj column lines + ni row lines).
-__global__ void spline_lines_kernel(int pairs, const double *ys, const double *cpy, int ni, const double *xs,
-                                    const double *cpx, int nj, const float *u, const float *v, SplineCoef coef) {
+// Line gid of pairs x 2 components x (nj column lines + ni row lines).
+__host__ __device__ void spline_lines_one(long gid, const double *ys, const double *cpy, int ni, const double *xs,
+                                          const double *cpx, int nj, const float *u, const float *v, SplineCoef coef) {
     const long lines = (long)nj + ni;
-    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= lines * 2 * pairs) return;
     const int pair = (int)(gid / (lines * 2));
     const long rem = gid - (long)pair * lines * 2;
     const int comp = (int)(rem / lines);
@@ -213,12 +222,17 @@ __global__ void spline_lines_kernel(int pairs, const double *ys, const double *c
     }
 }
 
-// Cross derivatives by central differences (one-sided at the border).
-__global__ void spline_cross_kernel(int pairs, const double *ys, int ni, const double *xs, int nj, const float *u,
-                                    const float *v, SplineCoef coef) {
-    const long cnt = (long)ni * nj;
+__global__ void spline_lines_kernel(int pairs, const double *ys, const double *cpy, int ni, const double *xs,
+                                    const double *cpx, int nj, const float *u, const float *v, SplineCoef coef) {
     const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= cnt * pairs) return;
+    if (gid >= ((long)nj + ni) * 2 * pairs) return;
+    spline_lines_one(gid, ys, cpy, ni, xs, cpx, nj, u, v, coef);
+}
+
+// Cross derivatives by central differences (one-sided at the border), node gid.
+__host__ __device__ void spline_cross_one(long gid, const double *ys, int ni, const double *xs, int nj, const float *u,
+                                          const float *v, SplineCoef coef) {
+    const long cnt = (long)ni * nj;
     const int pair = (int)(gid / cnt);
     const long k = gid - (long)pair * cnt;
     const int i = (int)(k / nj), j = (int)(k - (long)i * nj);
@@ -234,15 +248,22 @@ __global__ void spline_cross_kernel(int pairs, const double *ys, int ni, const d
     }
 }
 
+__global__ void spline_cross_kernel(int pairs, const double *ys, int ni, const double *xs, int nj, const float *u,
+                                    const float *v, SplineCoef coef) {
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long)ni * nj * pairs) return;
+    spline_cross_one(gid, ys, ni, xs, nj, u, v, coef);
+}
+
 // ---------------- B-field evaluation + B-warp ----------------
 
 template <typename Pix>
-__device__ __forceinline__ float warp_read(const Pix *img, int w, int y, int x) {
+__host__ __device__ __forceinline__ float warp_read(const Pix *img, int w, int y, int x) {
     return (float)img[(long)y * w + x];
 }
 
 template <typename Pix>
-__device__ float warp_pixel(const Pix *img, int h, int w, float u, float v, int i, int j, bool first) {
+__host__ __device__ float warp_pixel(const Pix *img, int h, int w, float u, float v, int i, int j, bool first) {
     float sI = first ? (float)i - u : (float)i + u;
     float sJ = first ? (float)j - v : (float)j + v;
     int pI = (int)(short)java_round(sI), pJ = (int)(short)java_round(sJ);
@@ -267,7 +288,7 @@ __device__ float warp_pixel(const Pix *img, int h, int w, float u, float v, int 
 }
 
 template <typename Pix>
-__device__ __forceinline__ Pix warp_store(float value, int int16_quirk) {
+__host__ __device__ __forceinline__ Pix warp_store(float value, int int16_quirk) {
     const int r = java_round(value);
     if (sizeof(Pix) == 1) return (Pix)(uint8_t)(int8_t)r;
     if (int16_quirk) return (Pix)(uint16_t)(int16_t)(int8_t)r;  // MatrixInt16.setElement(float) narrows via byte
@@ -275,7 +296,7 @@ __device__ __forceinline__ Pix warp_store(float value, int int16_quirk) {
 }
 
 // Canonical field evaluation order shared with the oracle.
-__device__ __forceinline__ double field_value(const double *ys, int ni, const double *xs, int nj, const float *f,
+__host__ __device__ __forceinline__ double field_value(const double *ys, int ni, const double *xs, int nj, const float *f,
                                               const double *fy, const double *fx, const double *fyx, double y,
                                               double x) {
     const int i = knot_interval(ys, ni, y), j = knot_interval(xs, nj, x);
@@ -296,18 +317,14 @@ __device__ __forceinline__ double field_value(const double *ys, int ni, const do
     return w[0] * Y0 + w[1] * Y1 + w[2] * Y2 + w[3] * Y3;
 }
 
-// One thread per pixel of one pair (blockIdx.z = pair).  src/dst frame tables hold the
-// original and the warped images.
+// Pixel (i, j) of pair `pair`: field, then both warped pixels.
 template <typename Pix>
-__global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, const qlpiv_frame *dst,
-                                                        const double *ys, int ni, const double *xs, int nj,
-                                                        const float *u, const float *v, SplineCoef coef,
-                                                        int int16_quirk) {
-    const int pair = blockIdx.z;
+__host__ __device__ __forceinline__ void warp_one(int pair, int i, int j, const qlpiv_frame *src,
+                                                  const qlpiv_frame *dst, const double *ys, int ni, const double *xs,
+                                                  int nj, const float *u, const float *v, SplineCoef coef,
+                                                  int int16_quirk) {
     const qlpiv_frame fs = src[pair];
     const int h = fs.height, w = fs.width;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= h || j >= w) return;
     const qlpiv_frame fd = dst[pair];
     const long base = (long)pair * ni * nj;
@@ -326,6 +343,18 @@ __global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, 
     Pix *ob = reinterpret_cast<Pix *>(const_cast<void *>(fd.img_b));
     oa[(long)i * fd.pitch + j] = warp_store<Pix>(warp_pixel(ia, h, w, hu, hv, i, j, true), int16_quirk);
     ob[(long)i * fd.pitch + j] = warp_store<Pix>(warp_pixel(ib, h, w, hu, hv, i, j, false), int16_quirk);
+}
+
+// One thread per pixel of one pair (blockIdx.z = pair).  src/dst frame tables hold the
+// original and the warped images.
+template <typename Pix>
+__global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, const qlpiv_frame *dst,
+                                                        const double *ys, int ni, const double *xs, int nj,
+                                                        const float *u, const float *v, SplineCoef coef,
+                                                        int int16_quirk) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    warp_one<Pix>(blockIdx.z, i, j, src, dst, ys, ni, xs, nj, u, v, coef, int16_quirk);
 }
 
 // Per-pixel field only (test hook for the field stage): pair 0, outputs h x w floats.

@@ -41,7 +41,8 @@ struct XcorrShape {
     static constexpr int ROUNDS = N / NG;              // tasks per group per phase
     static constexpr int RP = M + M / 8 + 1;           // region pitch (complex), odd
     static constexpr int MIN_BLOCKS = N == 16 ? 16 : (N == 32 ? 4 : 2);
-    static constexpr size_t SMEM = sizeof(cplx) * (size_t)(M + N * RP + NG * RP) + 64 * sizeof(uint64_t);
+    static constexpr size_t SMEM =
+        sizeof(cplx) * (size_t)(M + N * RP + NG * RP) + 64 * sizeof(uint64_t) + 32 * 48;  // + fit queue
 };
 
 template <typename Pix>
@@ -91,6 +92,68 @@ struct IaJob {
     float *acc_u, *acc_v;        // optional: tile displacements += (u, v)  (Tile.accumulateDisplacement)
 };
 
+// Integer peak and 3-point stencil of one IA, queued for the sub-pixel fit.
+struct FitRec {
+    long ia;
+    int pi, pj, kind;   // kind: 0 fit, 1 no peak, 2 stencil off the plane, 3 no sub-pixel
+    float pv, mn, c0, yu, yd, xl, xr;
+};
+
+// Gaussian1DPolynomialInterpolator.interpolate (S/interpolators/Gaussian1DPolynomialInterpolator.java:25-106)
+// for q[0..n): lane k handles record k, so the double logarithms of 32 IAs share one
+// warp instruction.  Called by one full warp.
+template <int D>
+__device__ void fit_flush(const FitRec *q, int n, int lane, const IaJob &job) {
+    __syncwarp();
+    if (lane < n) {
+        const FitRec r = q[lane];
+        float si = (float)r.pi, sj = (float)r.pj;
+        uint32_t flags = 0;
+        if (r.kind == 1) {
+            flags |= QLPIV_F_NO_PEAK;
+        } else if (r.kind == 2) {
+            flags |= QLPIV_F_EDGE;
+        } else if (r.kind == 0) {
+            const bool neg = r.c0 < 0.0f || r.yu < 0.0f || r.yd < 0.0f || r.xl < 0.0f || r.xr < 0.0f;
+            const float y0 = r.yu + 1e-8f, y1 = r.c0 + 1e-8f, y2 = r.yd + 1e-8f;
+            const float x0 = r.xl + 1e-8f, x1 = r.c0 + 1e-8f, x2 = r.xr + 1e-8f;
+            float ti, tj;
+            if (!neg) {
+                const double ly0 = log((double)y0), ly1 = log((double)y1), ly2 = log((double)y2);
+                const double lx0 = log((double)x0), lx1 = log((double)x1), lx2 = log((double)x2);
+                const double di = __dadd_rn(__dadd_rn(__dmul_rn(2.0, ly0), -__dmul_rn(4.0, ly1)), __dmul_rn(2.0, ly2));
+                const double dj = __dadd_rn(__dadd_rn(__dmul_rn(2.0, lx0), -__dmul_rn(4.0, lx1)), __dmul_rn(2.0, lx2));
+                ti = __fadd_rn((float)r.pi, __fdiv_rn((float)(ly0 - ly2), (float)di));
+                tj = __fadd_rn((float)r.pj, __fdiv_rn((float)(lx0 - lx2), (float)dj));
+            } else {
+                flags |= QLPIV_F_PARABOLIC;
+                const float dy = __fadd_rn(__fadd_rn(__fmul_rn(2.0f, y0), -__fmul_rn(4.0f, y1)), __fmul_rn(2.0f, y2));
+                const float dx = __fadd_rn(__fadd_rn(__fmul_rn(2.0f, x0), -__fmul_rn(4.0f, x1)), __fmul_rn(2.0f, x2));
+                ti = __fadd_rn((float)r.pi, __fdiv_rn(y0 - y2, dy));
+                tj = __fadd_rn((float)r.pj, __fdiv_rn(x0 - x2, dx));
+            }
+            if (isfinite(ti) && fabsf(ti - (float)r.pi) <= 1.0f) { si = ti; flags |= QLPIV_F_SUB_I; }
+            if (isfinite(tj) && fabsf(tj - (float)r.pj) <= 1.0f) { sj = tj; flags |= QLPIV_F_SUB_J; }
+        }
+        qlpiv_vector o;
+        o.u = si - (float)(D / 2);
+        o.v = sj - (float)(D / 2);
+        o.sub_i = si;
+        o.sub_j = sj;
+        o.peak_value = r.pv;
+        o.min_floor = r.mn;
+        o.peak_i = (int16_t)r.pi;
+        o.peak_j = (int16_t)r.pj;
+        o.flags = flags;
+        if (job.out != nullptr) job.out[r.ia] = o;
+        if (job.acc_u != nullptr) {
+            job.acc_u[r.ia] += o.u;
+            job.acc_v[r.ia] += o.v;
+        }
+    }
+    __syncwarp();
+}
+
 template <int N, typename Pix>
 __global__ void __launch_bounds__(XcorrShape<N>::T, XcorrShape<N>::MIN_BLOCKS)
 xcorr_kernel(IaJob job) {
@@ -101,6 +164,8 @@ xcorr_kernel(IaJob job) {
     cplx *reg = tw + M;           // N regions of RP complex
     cplx *scr = reg + N * RP;     // NG scratch buffers of RP complex
     uint64_t *red = reinterpret_cast<uint64_t *>(scr + NG * RP);  // 64 words
+    FitRec *fitq = reinterpret_cast<FitRec *>(red + 64);           // 32 queued fits
+    int qn = 0;                                                    // uniform across the CTA
 
     const int tid = threadIdx.x;
     const int g = tid % G;
@@ -327,7 +392,7 @@ xcorr_kernel(IaJob job) {
             }
         }
 
-        // ---- 5. CTA reduction, sub-pixel fit ----
+        // ---- 5. CTA reduction; the fit is queued and run 32 IAs at a time ----
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const uint64_t ok = __shfl_xor_sync(0xffffffffu, best, o);
@@ -341,68 +406,58 @@ xcorr_kernel(IaJob job) {
             red[32 + warp] = ((uint64_t)best_ij << 32) | (uint64_t)__float_as_uint(minf);
         }
         __syncthreads();
-        if (tid == 0) {
-            uint64_t bk = red[0];
-            uint32_t bij = (uint32_t)(red[32] >> 32);
-            float mn = __uint_as_float((uint32_t)red[32]);
-            for (int k = 1; k < NWARPS; k++) {
-                if (red[k] > bk) { bk = red[k]; bij = (uint32_t)(red[32 + k] >> 32); }
-                mn = fminf(mn, __uint_as_float((uint32_t)red[32 + k]));
+        if (warp == 0) {
+            uint64_t bk = 0ull;
+            uint32_t bij = 0u;
+            float mn = 3.402823466e38f;
+            if (lane < NWARPS) {
+                bk = red[lane];
+                bij = (uint32_t)(red[32 + lane] >> 32);
+                mn = __uint_as_float((uint32_t)red[32 + lane]);
             }
-            int pi = 0, pj = 0;
-            float pv = 0.0f;
-            if (bk != 0ull) {
-                pi = (int)(bij >> 16);
-                pj = (int)(bij & 0xffffu);
-                pv = __uint_as_float((uint32_t)(bk >> 32));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const uint64_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
+                const uint32_t oij = __shfl_xor_sync(0xffffffffu, bij, o);
+                // ties on the full key cannot occur between distinct cells (the rank is unique)
+                if (ok > bk) { bk = ok; bij = oij; }
+                mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
             }
-            auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)]; };
-            float si = (float)pi, sj = (float)pj;
-            uint32_t flags = 0;
-            if (!job.subpix) {
-            } else if (pi == 0 && pj == 0) {
-                flags |= QLPIV_F_NO_PEAK;
-            } else if (pi - 1 < 0 || pi + 1 >= D || pj - 1 < 0 || pj + 1 >= D) {
-                flags |= QLPIV_F_EDGE;
-            } else {
-                const float c0 = P(pi, pj);
-                const float yu = P(pi - 1, pj), yd = P(pi + 1, pj);
-                const float xl = P(pi, pj - 1), xr = P(pi, pj + 1);
-                const bool neg = c0 < 0.0f || yu < 0.0f || yd < 0.0f || xl < 0.0f || xr < 0.0f;
-                const float y0 = yu + 1e-8f, y1 = c0 + 1e-8f, y2 = yd + 1e-8f;
-                const float x0 = xl + 1e-8f, x1 = c0 + 1e-8f, x2 = xr + 1e-8f;
-                float ti, tj;
-                if (!neg) {
-                    const double ly0 = log((double)y0), ly1 = log((double)y1), ly2 = log((double)y2);
-                    const double lx0 = log((double)x0), lx1 = log((double)x1), lx2 = log((double)x2);
-                    ti = (float)pi + __fdiv_rn((float)(ly0 - ly2), (float)(2.0 * ly0 - 4.0 * ly1 + 2.0 * ly2));
-                    tj = (float)pj + __fdiv_rn((float)(lx0 - lx2), (float)(2.0 * lx0 - 4.0 * lx1 + 2.0 * lx2));
-                } else {
-                    flags |= QLPIV_F_PARABOLIC;
-                    ti = (float)pi + __fdiv_rn(y0 - y2, 2.0f * y0 - 4.0f * y1 + 2.0f * y2);
-                    tj = (float)pj + __fdiv_rn(x0 - x2, 2.0f * x0 - 4.0f * x1 + 2.0f * x2);
+            if (lane == 0) {
+                FitRec r;
+                r.ia = ia;
+                r.mn = mn;
+                r.pi = 0;
+                r.pj = 0;
+                r.pv = 0.0f;
+                if (bk != 0ull) {
+                    r.pi = (int)(bij >> 16);
+                    r.pj = (int)(bij & 0xffffu);
+                    r.pv = __uint_as_float((uint32_t)(bk >> 32));
                 }
-                if (isfinite(ti) && fabsf(ti - (float)pi) <= 1.0f) { si = ti; flags |= QLPIV_F_SUB_I; }
-                if (isfinite(tj) && fabsf(tj - (float)pj) <= 1.0f) { sj = tj; flags |= QLPIV_F_SUB_J; }
+                auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)]; };
+                r.kind = 0;
+                if (!job.subpix) r.kind = 3;
+                else if (r.pi == 0 && r.pj == 0) r.kind = 1;
+                else if (r.pi - 1 < 0 || r.pi + 1 >= D || r.pj - 1 < 0 || r.pj + 1 >= D) r.kind = 2;
+                if (r.kind == 0) {
+                    r.c0 = P(r.pi, r.pj);
+                    r.yu = P(r.pi - 1, r.pj);
+                    r.yd = P(r.pi + 1, r.pj);
+                    r.xl = P(r.pi, r.pj - 1);
+                    r.xr = P(r.pi, r.pj + 1);
+                }
+                fitq[qn] = r;
             }
-            qlpiv_vector o;
-            o.u = si - (float)(D / 2);
-            o.v = sj - (float)(D / 2);
-            o.sub_i = si;
-            o.sub_j = sj;
-            o.peak_value = pv;
-            o.min_floor = mn;
-            o.peak_i = (int16_t)pi;
-            o.peak_j = (int16_t)pj;
-            o.flags = flags;
-            if (job.out != nullptr) job.out[ia] = o;
-            if (job.acc_u != nullptr) {
-                job.acc_u[ia] += o.u;
-                job.acc_v[ia] += o.v;
-            }
+        }
+        qn++;
+        if (qn == 32) {
+            if (warp == 0) fit_flush<D>(fitq, qn, lane, job);
+            qn = 0;
         }
         __syncthreads();  // regions are rewritten by the next IA
     }
+    if (qn > 0 && warp == 0) fit_flush<D>(fitq, qn, lane, job);
 }
 
 }  // namespace qlpiv

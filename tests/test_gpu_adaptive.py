@@ -93,25 +93,31 @@ def _true_flow(qp, flow, g, shape):
     return flow.displacement(yy, xx, shape)
 
 
-@pytest.mark.parametrize("bits,warp", [(8, True), (12, True), (8, False)])
-def test_adaptive_pipeline_matches_fp64_oracle(qp, handle, oracle, bits, warp):
+@pytest.mark.parametrize("bits,warp,tile_max", [(8, True, "full"), (12, True, "full"), (12, True, "tile"),
+                                                 (8, False, "tile")])
+def test_adaptive_pipeline_matches_fp64_oracle(qp, handle, oracle, bits, warp, tile_max):
+    """tile_max "full": tiles cut from the warped images keep the full-scale maximum, as in
+    the reference (copyMatrixRegion); with 12-bit data the v/65535*16+1 map leaves the +1
+    pedestal dominant and the vectors are biased toward zero, so only parity is checked.
+    "tile": the per-tile maximum (floor 16)."""
     h, w = 256, 320
     flow = qp.synth.Flow(vmax=5.0, rc=48.0, shear=0.004)
     pairs = [qp.synth.particle_pair((h, w), flow, ppp=0.03, diam=2.5, diam_sd=0.0, bits=bits, seed=40 + k)
              for k in range(3)]
-    fixed = 255.0 if bits == 8 else 65535.0
+    fixed = (255.0 if bits == 8 else 65535.0) if tile_max == "full" else 0.0
     desc = qp.adaptive_desc(64, 16, 0.25, warp_mode=qp.WARP_BOTH_BILINEAR if warp else qp.WARP_NONE,
-                            max_mode=qp.MAX_FIXED if warp else qp.MAX_COMPUTE, fixed_max=fixed if warp else 0.0)
+                            max_mode=qp.MAX_FIXED if fixed else qp.MAX_COMPUTE, fixed_max=fixed)
     u, v = handle.piv_adaptive([p[0] for p in pairs], [p[1] for p in pairs], desc)
     g = qp.grid.superposition(h, w, 64, 2, 0.25)
     assert u.shape == (3, g.tiles_i, g.tiles_j)
     for k, (a, b) in enumerate(pairs):
-        ou, ov = oracle.piv_adaptive(a, b, 64, 16, 0.25, fixed_max=fixed if warp else None, precision=64, warp=warp)
+        ou, ov = oracle.piv_adaptive(a, b, 64, 16, 0.25, fixed_max=fixed or None, precision=64, warp=warp)
         err = np.maximum(np.abs(u[k] - ou), np.abs(v[k] - ov))
         # tiles downstream of a tie or a rounding-boundary pixel may differ; they must be rare
         assert np.mean(err <= 1e-3) >= 0.99, (k, float(np.mean(err <= 1e-3)), float(err.max()))
-        tr, tc = _true_flow(qp, flow, g, (h, w))
-        assert np.median(np.hypot(u[k] - tr, v[k] - tc)) < 0.15
+        if bits == 8 or tile_max == "tile":
+            tr, tc = _true_flow(qp, flow, g, (h, w))
+            assert np.median(np.hypot(u[k] - tr, v[k] - tc)) < 0.15
 
 
 def test_adaptive_device_variant_and_repeatability(qp, handle):
