@@ -2,16 +2,19 @@
 """FFT-PIV throughput benchmark (one JSON line on rank 0).
 
 Workload ("adaptive-1024-u12"): 1024x1024 12-bit-in-uint16 synthetic particle pairs
-(0.03 ppp, d = 2.5 px, shear 0.005 + Rankine vortex, max 6 px), three correlation
-passes with IA 64 -> 32 -> 16 at 75 % overlap (61^2 + 125^2 + 253^2 = 83,355 vectors
-per pair), FP32, 3-point Gaussian sub-pixel fit.  A step processes a batch of `pairs`
-pairs resident in HBM (inputs larger than L2), one batched launch per pass.
+(0.03 ppp, d = 2.5 px, shear 0.005 + Rankine vortex, max 6 px), adaptive PIV with
+IA 64 -> 32 -> 16 at 75 % overlap (61^2 + 125^2 + 253^2 = 83,355 vectors per pair):
+velocity inheritance, bicubic displacement field and BothImages bilinear warp between
+passes, FP32, 3-point Gaussian sub-pixel fit.  A step processes a batch of `pairs`
+pairs resident in HBM (inputs larger than L2) through the whole level loop.
 
   value      frame-pairs/s with inputs resident in HBM (CUDA events on the library's
              stream, max over ranks);
-  e2e        frame-pairs/s through the public host API (qlpiv_pass_batch): pinned host
-             images copied to the device and vectors copied back inside the timed region;
-  roofline   dominant kernel (the pass with the largest device time): algorithmic bytes
+  e2e        frame-pairs/s through the public host API (qlpiv_piv_adaptive): pinned host
+             images copied to the device and the displacements copied back inside the
+             timed region;
+  roofline   dominant kernel (the stage with the largest device time, from CUDA events
+             around every launch): for the correlation, algorithmic bytes
              2*N^2*bytes_per_px + 16 per IA against the measured HBM copy bandwidth, and
              (compute_roofline) formula flops 10*M^2*log2(M^2) + 8*M^2 (M = 2N) per IA
              against the live FP32 FMA peak;
@@ -121,19 +124,26 @@ def make_pairs(pkg, unique):
     return [pkg.synth.config2_pair(seed=2, pair_id=k) for k in range(unique)]
 
 
+FULL_SCALE = 65535.0   # tiles copied from warped 16-bit images keep the full-scale max
+
+
 def cpu_baseline(pkg, pair, threads, reps=1):
-    """Oracle FP32 restatement of the reference CPU path on one pair (all passes)."""
+    """Oracle FP32 restatement of the reference CPU path on one pair: the same adaptive
+    loop (inheritance, bicubic field, bilinear warp, three correlation passes)."""
     orc = load_oracle()
     a, b = pair
-    grids = level_grids(pkg)
     times = []
     for _ in range(reps):
         t0 = time.perf_counter()
-        for g in grids:
-            at, al = g.origins()
-            orc.piv_pass(a, b, g.n, at, al, norm_mode=orc.NORM_MAX_A, precision=32, nthreads=threads)
+        orc.piv_adaptive(a, b, LEVELS[0], LEVELS[-1], OVERLAP_FACTOR, norm_mode=orc.NORM_MAX_A, fixed_max=FULL_SCALE,
+                         precision=32, nthreads=threads)
         times.append(time.perf_counter() - t0)
     return min(times)
+
+
+WORKLOAD = ("adaptive-1024-u12: 1024x1024 12-bit pairs, IA 64 -> 32 -> 16 at 75 % overlap, BothImages bilinear "
+            "warp between passes (velocity inheritance + bicubic displacement field), tile A max normalisation, "
+            "3-point Gaussian sub-pixel; vector validation not included")
 
 
 def run_reference(args, rank):
@@ -151,10 +161,10 @@ def run_reference(args, rank):
         "impl": "reference", "metric": "frame-pairs/s", "value": v, "unit": "frame-pairs/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "adaptive-1024-u12 (IA 64/32/16 at 75 %), one pair per step",
+        "config": {"workload": WORKLOAD + "; one pair per step",
                    "pairs_per_step": 1, "ia_vectors_per_pair": sum(g.count for g in level_grids(pkg))},
         "cpu_baseline": {"value": v, "unit": "frame-pairs/s", "cores": threads, "kind": "port",
-                         "sample": "one 1024x1024 pair, all three correlation passes"},
+                         "sample": "one 1024x1024 pair through the whole adaptive loop (FP32 oracle)"},
         "e2e": {"value": v, "unit": "frame-pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -170,9 +180,13 @@ def run_gpu(args, rank, world):
     stream = torch.cuda.ExternalStream(h.stream, device=dev)
 
     grids = level_grids(pkg)
+    last = grids[-1]
     pairs_host = make_pairs(pkg, args.unique)
     P = args.pairs
     bpp = 2
+    desc = pkg.adaptive_desc(LEVELS[0], LEVELS[-1], OVERLAP_FACTOR, warp_mode=pkg.WARP_BOTH_BILINEAR,
+                             norm_mode=pkg.NORM_MAX_A, max_mode=pkg.MAX_FIXED, fixed_max=FULL_SCALE,
+                             subpix_mode=pkg.SUBPIX_GAUSS3)
     # device-resident frames: P slots filled from `unique` distinct synthetic pairs
     imgs = torch.empty((P, 2, H, W), dtype=torch.int16, device=dev)
     for k in range(P):
@@ -183,31 +197,18 @@ def run_gpu(args, rank, world):
     for k in range(P):
         table[k] = (imgs[k, 0].data_ptr(), imgs[k, 1].data_ptr(), H, W, W)
     dtable = torch.from_numpy(table.view(np.uint8)).to(dev)
-    work = []
-    for g in grids:
-        at, al = g.origins()
-        fi = np.repeat(np.arange(P, dtype=np.int32), len(at))
-        wl = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (fi, np.tile(at, P), np.tile(al, P))]
-        out = torch.empty(len(fi) * 32, dtype=torch.uint8, device=dev)
-        work.append((g.n, len(fi), wl, out))
-    total_ia = sum(c for _, c, _, _ in work)
+    out_u = torch.empty(P * last.count, dtype=torch.float32, device=dev)
+    out_v = torch.empty_like(out_u)
+    ia_per_pair = sum(g.count for g in grids)
 
-    def step(evs=None):
-        for lv, (n, count, wl, out) in enumerate(work):
-            if evs is not None:
-                evs[lv][0].record(stream)
-            h.piv_pass_batch_device(pkg.PIX_U16, P, dtable, n, count, wl[0], wl[1], wl[2], wl[1], wl[2], out,
-                                    norm_mode=pkg.NORM_MAX_A)
-            if evs is not None:
-                evs[lv][1].record(stream)
+    def step():
+        h.piv_adaptive_device(desc, pkg.PIX_U16, H, W, P, dtable, out_u, out_v)
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    lev_ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in work]
-              for _ in range(args.steps)]
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
     launches0 = h.launches
@@ -215,8 +216,8 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     with sampler:
         t_start.record(stream)
-        for s in range(args.steps):
-            step(lev_ev[s])
+        for _ in range(args.steps):
+            step()
         t_end.record(stream)
         torch.cuda.synchronize()
     launches = h.launches - launches0
@@ -227,75 +228,83 @@ def run_gpu(args, rank, world):
         ms = float(t.item())
     ms_per_step = ms / args.steps
     pairs_per_s = world * P * args.steps / (ms * 1e-3)
-    lev_ms = [sum(lev_ev[s][lv][0].elapsed_time(lev_ev[s][lv][1]) for s in range(args.steps)) / args.steps
-              for lv in range(len(work))]
 
-    # ---- e2e through the host API: pinned host frames in, vectors out ----
+    # ---- per-stage device time (events around every launch), two extra steps ----
+    h.profile(True)
+    h.profile_read()
+    prof_steps = 2
+    for _ in range(prof_steps):
+        step()
+    stages = h.profile_read()
+    h.profile(False)
+    for st in stages:
+        st["ms_per_step"] = st["ms"] / prof_steps
+
+    # ---- e2e through the host API: pinned host frames in, displacements out ----
     host_frames = [(torch.from_numpy(a).pin_memory(), torch.from_numpy(b).pin_memory()) for a, b in pairs_host]
     fa = [host_frames[k % len(host_frames)][0].numpy() for k in range(P)]
     fb = [host_frames[k % len(host_frames)][1].numpy() for k in range(P)]
-    host_work = []
-    for g in grids:
-        at, al = g.origins()
-        host_work.append((g.n, np.repeat(np.arange(P, dtype=np.int32), len(at)), np.tile(at, P), np.tile(al, P)))
     e2e_steps = max(1, min(args.steps, 5))
     for _ in range(2):
-        for n, fi, at, al in host_work:
-            h.piv_pass_batch(fa, fb, n, fi, at, al, norm_mode=pkg.NORM_MAX_A)
+        h.piv_adaptive(fa, fb, desc)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for n, fi, at, al in host_work:
-            h.piv_pass_batch(fa, fb, n, fi, at, al, norm_mode=pkg.NORM_MAX_A)
+        u_host, v_host = h.piv_adaptive(fa, fb, desc)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_val = world * P / e2e_s
-    h2d = len(host_work) * P * 2 * H * W * bpp + sum(len(fi) * 20 for _, fi, _, _ in host_work)
-    d2h = total_ia * 32
+    h2d = P * 2 * H * W * bpp
+    d2h = 2 * P * last.count * 4
 
     # ---- roofline of the dominant kernel ----
-    dom = int(np.argmax(lev_ms))
-    n_dom, cnt_dom = work[dom][0], work[dom][1]
-    t_launch = lev_ms[dom] * 1e-3
+    dom = max(stages, key=lambda s_: s_["ms"])
+    t_launch = dom["ms"] / dom["launches"] * 1e-3
+    items_per_launch = dom["items"] / dom["launches"]
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     fp32_peak = pkg.measure_fp32_peak(dev.index)
-    alg_bytes = bytes_per_ia(n_dom, bpp) * cnt_dom
-    alg_flops = flops_per_ia(n_dom) * cnt_dom
     traffic = None
-    tfile = ROOT / "profiles" / "k1_traffic.json"
-    if tfile.exists():
-        tj = json.loads(tfile.read_text())
-        per_ia = tj.get("dram_bytes_per_ia", {}).get(str(n_dom))
-        if per_ia is not None:
-            traffic = per_ia * cnt_dom
-
+    if dom["stage"] == "xcorr":
+        n_dom = dom["ia_side"]
+        alg_bytes = bytes_per_ia(n_dom, bpp) * items_per_launch
+        alg_flops = flops_per_ia(n_dom) * items_per_launch
+        tfile = ROOT / "profiles" / "k1_traffic.json"
+        if tfile.exists():
+            per_ia = json.loads(tfile.read_text()).get("dram_bytes_per_ia", {}).get(str(n_dom))
+            if per_ia is not None:
+                traffic = per_ia * items_per_launch
+        kernel = f"xcorr_kernel<{n_dom}>"
+    else:
+        alg_bytes = 4.0 * bpp * items_per_launch   # warp: read A, B; write A', B'
+        alg_flops = 0.0
+        kernel = dom["stage"]
     result = {
         "metric": "frame-pairs/s", "value": pairs_per_s, "unit": "frame-pairs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "adaptive-1024-u12: 1024x1024 12-bit pairs, IA 64/32/16 at 75 % overlap, "
-                               "3-point Gaussian; passes correlated at the grid origins (no warp/validation stage "
-                               "between passes)",
-                   "pairs_per_step": P, "unique_pairs": len(pairs_host), "ia_vectors_per_pair": total_ia // P,
+        "config": {"workload": WORKLOAD,
+                   "pairs_per_step": P, "unique_pairs": len(pairs_host), "ia_vectors_per_pair": ia_per_pair,
                    "inputs_exceed_l2": P * 2 * H * W * bpp > 129e6, "l2_flush": "inputs larger than L2",
-                   "norm": "tile A max (CPU path)", "parallelism": f"replicas x{world}"},
-        "ia_vectors_per_s": world * total_ia * args.steps / (ms * 1e-3),
-        "pass_ms": {str(work[k][0]): lev_ms[k] for k in range(len(work))},
+                   "tile_max": "full scale 65535 (warped tiles, reference semantics)",
+                   "parallelism": f"replicas x{world}"},
+        "ia_vectors_per_s": world * ia_per_pair * P * args.steps / (ms * 1e-3),
+        "stages": [{k: st[k] for k in ("stage", "level", "ia_side", "ms_per_step")} for st in stages],
         "e2e": {"value": e2e_val, "unit": "frame-pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": alg_bytes / t_launch / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": alg_bytes / t_launch / 1e9 / hbm_peak, "traffic": traffic,
-                     "kernel": f"xcorr_kernel<{n_dom}>", "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
-        "compute_roofline": {"bound": "fp32", "achieved": alg_flops / t_launch / 1e12, "peak": fp32_peak,
-                             "unit": "TFLOP/s", "frac": alg_flops / t_launch / 1e12 / fp32_peak,
-                             "peak_source": "live FP32 FMA probe (qlpiv_measure_fp32_peak)"},
+                     "frac": alg_bytes / t_launch / 1e9 / hbm_peak, "traffic": traffic, "kernel": kernel,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "clocks": sampler.summary(),
     }
+    if alg_flops:
+        result["compute_roofline"] = {"bound": "fp32", "achieved": alg_flops / t_launch / 1e12, "peak": fp32_peak,
+                                      "unit": "TFLOP/s", "frac": alg_flops / t_launch / 1e12 / fp32_peak,
+                                      "kernel": kernel, "peak_source": "live FP32 FMA probe (qlpiv_measure_fp32_peak)"}
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         t_cpu = cpu_baseline(pkg, pairs_host[0], threads)
         result["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "frame-pairs/s", "cores": threads, "kind": "port",
-                                  "sample": "one 1024x1024 pair, all three correlation passes (FP32 oracle)"}
+                                  "sample": "one 1024x1024 pair through the whole adaptive loop (FP32 oracle)"}
     h.close()
     if rank == 0:
         print(json.dumps(result), flush=True)

@@ -260,6 +260,21 @@ qlpiv_status qlpiv_piv_adaptive_device(qlpiv_handle *h, const qlpiv_adaptive_des
                                        int width, int num_pairs, const qlpiv_frame *frames, float *out_u,
                                        float *out_v);
 
+/* Stage timing of the adaptive pipeline (CUDA events around every launch on the
+ * handle's stream).  Accumulates while enabled; qlpiv_profile_read synchronises the
+ * stream, returns the totals per (stage, level) and clears them. */
+typedef struct qlpiv_stage_time {
+    char stage[24];     /* "inherit", "spline", "warp", "xcorr", "origins" */
+    int level;          /* adaptive level, IA side = ia_start >> level */
+    int ia_side;
+    long launches;      /* kernel launches accumulated */
+    long items;         /* IAs (xcorr) or pixels (warp) or tiles processed */
+    double ms;          /* summed device time */
+} qlpiv_stage_time;
+
+qlpiv_status qlpiv_profile_enable(qlpiv_handle *h, int enable);
+qlpiv_status qlpiv_profile_read(qlpiv_handle *h, qlpiv_stage_time *out, int cap, int *count);
+
 /* Instrumentation: FP32 FMA throughput of `device` measured with a short probe kernel
  * (TFLOP/s, best of three), the compute roofline denominator of the FFT kernels. */
 qlpiv_status qlpiv_measure_fp32_peak(int device, double *tflops);

@@ -85,6 +85,11 @@ def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_m
     return d
 
 
+class StageTime(ctypes.Structure):
+    _fields_ = [("stage", ctypes.c_char * 24), ("level", ctypes.c_int), ("ia_side", ctypes.c_int),
+                ("launches", ctypes.c_long), ("items", ctypes.c_long), ("ms", ctypes.c_double)]
+
+
 class Params(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
@@ -115,6 +120,8 @@ _SIGNATURES = {
     "qlpiv_warp_pair": (_i, [_vp, _i, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "qlpiv_piv_adaptive": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
     "qlpiv_piv_adaptive_device": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
+    "qlpiv_profile_enable": (_i, [_vp, _i]),
+    "qlpiv_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(_i)]),
 }
 
 _lib = None
@@ -248,6 +255,17 @@ class Handle:
 
     def set_stream(self, stream):
         _check(self._lib.qlpiv_set_stream(self._h, stream))
+
+    def profile(self, enable=True):
+        _check(self._lib.qlpiv_profile_enable(self._h, int(enable)))
+
+    def profile_read(self):
+        """Per (stage, level) device time accumulated since the last read."""
+        n = ctypes.c_int()
+        buf = (StageTime * 64)()
+        _check(self._lib.qlpiv_profile_read(self._h, buf, 64, ctypes.byref(n)))
+        return [{"stage": buf[k].stage.decode(), "level": buf[k].level, "ia_side": buf[k].ia_side,
+                 "launches": buf[k].launches, "items": buf[k].items, "ms": buf[k].ms} for k in range(min(n.value, 64))]
 
     # -- tile API (Job<List<Tile>, XCorrelationResults>) -------------------------
     @staticmethod

@@ -257,6 +257,10 @@ qlpiv_status qlpiv_destroy(qlpiv_handle *h) {
                           &h->frames})
             b->release();
         for (DevBuf &b : h->scratch) b.release();
+        for (qlpiv::StageEvent &ev : h->prof_pending) {
+            cudaEventDestroy(ev.begin);
+            cudaEventDestroy(ev.end);
+        }
         if (h->plan) qlpiv::destroy_plan(h->plan);
         h->plan = nullptr;
     }

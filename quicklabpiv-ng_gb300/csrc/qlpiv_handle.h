@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <string>
+#include <vector>
 
 #include "qlpiv.h"
 
@@ -53,6 +55,21 @@ struct DeviceScope {
 struct AdaptivePlan;
 void destroy_plan(AdaptivePlan *p);
 
+// One pending stage timing (events recorded, not yet read back).
+struct StageEvent {
+    std::string stage;
+    int level, ia_side;
+    long launches, items;
+    cudaEvent_t begin, end;
+};
+
+struct StageTotal {
+    std::string stage;
+    int level, ia_side;
+    long launches, items;
+    double ms;
+};
+
 }  // namespace qlpiv
 
 struct qlpiv_handle {
@@ -65,4 +82,7 @@ struct qlpiv_handle {
     qlpiv::DevBuf tiles_a, tiles_b, max_a, max_b, origins, vectors, planes, frames;
     qlpiv::DevBuf scratch[8];            // stage test hooks
     qlpiv::AdaptivePlan *plan = nullptr; // cached adaptive PIV plan
+    bool profiling = false;
+    std::vector<qlpiv::StageEvent> prof_pending;
+    std::vector<qlpiv::StageTotal> prof_totals;
 };

@@ -193,6 +193,32 @@ static qlpiv_status build_plan(qlpiv_handle *h, const qlpiv_adaptive_desc *d, in
     return st;
 }
 
+// Stage timing: events recorded around a stage's launches when profiling is on.
+struct StageScope {
+    qlpiv_handle *h;
+    StageEvent ev{};
+    bool on;
+    StageScope(qlpiv_handle *h_, const char *stage, int level, int ia_side, long launches, long items)
+        : h(h_), on(h_->profiling) {
+        if (!on) return;
+        ev.stage = stage;
+        ev.level = level;
+        ev.ia_side = ia_side;
+        ev.launches = launches;
+        ev.items = items;
+        if (cudaEventCreate(&ev.begin) != cudaSuccess || cudaEventCreate(&ev.end) != cudaSuccess) {
+            on = false;
+            return;
+        }
+        cudaEventRecord(ev.begin, h->stream);
+    }
+    ~StageScope() {
+        if (!on) return;
+        cudaEventRecord(ev.end, h->stream);
+        h->prof_pending.push_back(ev);
+    }
+};
+
 static SplineCoef coef_of(LevelPlan &L, int pairs) {
     double *c = L.coef.as<double>();
     const long n = L.count() * pairs;
@@ -217,6 +243,7 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
                 return cuda_fail(e, "level 0 reset");
         } else {
             LevelPlan &P = p->levels[lv - 1];
+            StageScope sc(h, "inherit", (int)lv, L.g.n, 1, total);
             if ((e = launch_inherit(s, pairs, P.d_cy.as<double>(), P.g.tiles_i, P.d_cx.as<double>(), P.g.tiles_j,
                                     P.d_u.as<float>(), P.d_v.as<float>(), L.d_cyf.as<float>(), L.g.tiles_i,
                                     L.d_cxf.as<float>(), L.g.tiles_j, d.warp_mode == QLPIV_WARP_NONE, u, v)) !=
@@ -229,17 +256,26 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
         if (d.warp_mode == QLPIV_WARP_BOTH_BILINEAR) {
             if (lv > 0) {  // no warping at the first level: displacements are all zero
                 SplineCoef c = coef_of(L, pairs);
-                if ((e = launch_spline(s, pairs, L.d_cy.as<double>(), L.d_cpy.as<double>(), L.g.tiles_i,
-                                       L.d_cx.as<double>(), L.d_cpx.as<double>(), L.g.tiles_j, u, v, c)) !=
-                        cudaSuccess ||
-                    (e = launch_warp(s, p->pixel_type, pairs, p->height, p->width, frames_dev,
-                                     p->warped_table.as<qlpiv_frame>(), L.d_cy.as<double>(), L.g.tiles_i,
-                                     L.d_cx.as<double>(), L.g.tiles_j, u, v, c, d.int16_warp_quirk)) != cudaSuccess)
-                    return cuda_fail(e, "warp");
+                {
+                    StageScope sc(h, "spline", (int)lv, L.g.n, 4, total);
+                    if ((e = launch_spline(s, pairs, L.d_cy.as<double>(), L.d_cpy.as<double>(), L.g.tiles_i,
+                                           L.d_cx.as<double>(), L.d_cpx.as<double>(), L.g.tiles_j, u, v, c)) !=
+                        cudaSuccess)
+                        return cuda_fail(e, "spline");
+                }
+                {
+                    StageScope sc(h, "warp", (int)lv, L.g.n, 1, (long)pairs * p->height * p->width);
+                    if ((e = launch_warp(s, p->pixel_type, pairs, p->height, p->width, frames_dev,
+                                         p->warped_table.as<qlpiv_frame>(), L.d_cy.as<double>(), L.g.tiles_i,
+                                         L.d_cx.as<double>(), L.g.tiles_j, u, v, c, d.int16_warp_quirk)) !=
+                        cudaSuccess)
+                        return cuda_fail(e, "warp");
+                }
                 h->launches += 5;
                 src = p->warped_table.as<qlpiv_frame>();
             }
         } else {
+            StageScope sc(h, "origins", (int)lv, L.g.n, 1, total);
             if ((e = launch_displaced_origins(s, total, L.d_at.as<int>(), L.d_al.as<int>(), u, v, L.d_bt.as<int>(),
                                               L.d_bl.as<int>())) != cudaSuccess)
                 return cuda_fail(e, "displaced origins");
@@ -261,8 +297,11 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
         job.subpix = d.subpix_mode == QLPIV_SUBPIX_GAUSS3;
         job.acc_u = u;
         job.acc_v = v;
-        if ((e = launch_xcorr(job, L.g.n, p->pixel_type, s, h->num_sms)) != cudaSuccess)
-            return cuda_fail(e, "xcorr");
+        {
+            StageScope sc(h, "xcorr", (int)lv, L.g.n, 1, total);
+            if ((e = launch_xcorr(job, L.g.n, p->pixel_type, s, h->num_sms)) != cudaSuccess)
+                return cuda_fail(e, "xcorr");
+        }
         h->launches++;
     }
     return QLPIV_OK;
@@ -502,6 +541,55 @@ qlpiv_status qlpiv_piv_adaptive(qlpiv_handle *h, const qlpiv_adaptive_desc *desc
         (e = cudaMemcpyAsync(out_v, L.d_v.p, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
         return cuda_fail(e, "adaptive PIV");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_profile_enable(qlpiv_handle *h, int enable) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lock(h->mu);
+    h->profiling = enable != 0;
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_profile_read(qlpiv_handle *h, qlpiv_stage_time *out, int cap, int *count) {
+    if (!h || !count) return fail(QLPIV_E_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "profile read");
+    for (StageEvent &ev : h->prof_pending) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ev.begin, ev.end);
+        cudaEventDestroy(ev.begin);
+        cudaEventDestroy(ev.end);
+        bool found = false;
+        for (StageTotal &t : h->prof_totals)
+            if (t.stage == ev.stage && t.level == ev.level) {
+                t.launches += ev.launches;
+                t.items += ev.items;
+                t.ms += ms;
+                found = true;
+                break;
+            }
+        if (!found) h->prof_totals.push_back({ev.stage, ev.level, ev.ia_side, ev.launches, ev.items, (double)ms});
+    }
+    h->prof_pending.clear();
+    const int n = (int)h->prof_totals.size();
+    *count = n;
+    if (out) {
+        for (int k = 0; k < n && k < cap; k++) {
+            const StageTotal &t = h->prof_totals[k];
+            std::memset(out[k].stage, 0, sizeof(out[k].stage));
+            std::strncpy(out[k].stage, t.stage.c_str(), sizeof(out[k].stage) - 1);
+            out[k].level = t.level;
+            out[k].ia_side = t.ia_side;
+            out[k].launches = t.launches;
+            out[k].items = t.items;
+            out[k].ms = t.ms;
+        }
+    }
+    h->prof_totals.clear();
     return QLPIV_OK;
 }
 
