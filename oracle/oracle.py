@@ -31,7 +31,8 @@ _lib = None
 
 def build(force=False):
     """Compile the oracle with its Makefile (gcc only; seconds)."""
-    src = [HERE / "qlpiv_oracle.c", HERE / "qlpiv_oracle_adaptive.c", HERE / "oracle_impl.h", HERE / "Makefile"]
+    src = [HERE / "qlpiv_oracle.c", HERE / "qlpiv_oracle_adaptive.c", HERE / "oracle_impl.h", HERE / "oracle_interp_impl.h",
+           HERE / "Makefile"]
     if not force and LIB_PATH.exists() and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in src):
         return LIB_PATH
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
@@ -61,9 +62,9 @@ def lib():
         L.orc_grid_nosuperposition.argtypes = [c_int] * 8 + [vp, ip, ip, c_int]
         L.orc_piv_pass.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_long, ip, ip, ip, ip, c_int,
                                    c_float, c_float, c_int, c_int, vp, c_int]
-        L.orc_displacement_field.argtypes = [dp, c_int, dp, c_int, fp, fp, c_int, c_int, fp, fp]
+        L.orc_displacement_field.argtypes = [dp, c_int, dp, c_int, fp, fp, c_int, c_int, c_int, fp, fp]
         L.orc_warp_both.argtypes = [vp, vp, c_int, c_int, c_int, fp, fp, c_int, vp, vp]
-        L.orc_inherit.argtypes = [dp, c_int, dp, c_int, fp, fp, fp, c_int, fp, c_int, c_int, fp, fp]
+        L.orc_inherit.argtypes = [dp, c_int, dp, c_int, fp, fp, fp, c_int, fp, c_int, c_int, c_int, fp, fp]
         L.orc_piv_adaptive.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_float,
                                        c_int, c_int, c_int, fp, fp, ip, ip, vp]
         L.orc_vector_size.restype = c_int
@@ -202,14 +203,16 @@ def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
-def displacement_field(ys, xs, u, v, h, w):
-    """Per-pixel (u, v) from tile displacements at tile centres (bicubic spline)."""
+def displacement_field(ys, xs, u, v, h, w, precision=32):
+    """Per-pixel (u, v) from tile displacements at tile centres (bicubic spline), evaluated
+    in float (precision=32, the CUDA formulation) or double."""
     ys, xs = _f64(ys), _f64(xs)
     u, v = _f32(u), _f32(v)
     fu = np.zeros((h, w), np.float32)
     fv = np.zeros((h, w), np.float32)
     lib().orc_displacement_field(_ptr(ys, ctypes.c_double), len(ys), _ptr(xs, ctypes.c_double), len(xs),
-                                 _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), h, w, _ptr(fu, ctypes.c_float),
+                                 _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), h, w, 0 if precision == 32 else 1,
+                                 _ptr(fu, ctypes.c_float),
                                  _ptr(fv, ctypes.c_float))
     return fu, fv
 
@@ -224,14 +227,15 @@ def warp_both(img_a, img_b, fu, fv, int16_quirk=False):
     return oa, ob
 
 
-def inherit(py, px, pu, pv, cy, cx, round_int=False):
+def inherit(py, px, pu, pv, cy, cx, round_int=False, precision=32):
     py, px = _f64(py), _f64(px)
     pu, pv, cy, cx = _f32(pu), _f32(pv), _f32(cy), _f32(cx)
     cu = np.zeros((len(cy), len(cx)), np.float32)
     cv = np.zeros((len(cy), len(cx)), np.float32)
     lib().orc_inherit(_ptr(py, ctypes.c_double), len(py), _ptr(px, ctypes.c_double), len(px), _ptr(pu, ctypes.c_float),
                       _ptr(pv, ctypes.c_float), _ptr(cy, ctypes.c_float), len(cy), _ptr(cx, ctypes.c_float), len(cx),
-                      int(round_int), _ptr(cu, ctypes.c_float), _ptr(cv, ctypes.c_float))
+                      int(round_int), 0 if precision == 32 else 1, _ptr(cu, ctypes.c_float),
+                      _ptr(cv, ctypes.c_float))
     return cu, cv
 
 

@@ -25,6 +25,11 @@
  *            AllowedOutOfBoundClipping (the UI converter's default).
  *  A-loop    LocalPIVOpenCLGpuJob (S/jobs/LocalPIVOpenCLGpuJob.java:188-411) with
  *            SimpleStrategy (one correlation per level), no validation.
+ *
+ * The reference evaluates both interpolators in double.  The FP32 pipeline here
+ * evaluates them in float (spline knot derivatives still solved in double), the
+ * formulation of the CUDA kernels, so the GPU stages can be checked bit for bit; the
+ * FP64 twin evaluates them in double.
  */
 #define _GNU_SOURCE
 #include <math.h>
@@ -78,35 +83,26 @@ static void natural_spline_deriv(const double *x, const double *y, long ys, int 
     free(m); free(cp); free(dp);
 }
 
-/* Bicubic spline surface over knots ys[ni] (first coordinate) x xs[nj]. */
-typedef struct {
-    int ni, nj;
-    const double *ys, *xs;
-    double *f, *fy, *fx, *fyx; /* ni*nj each, row-major */
-} bicubic;
-
-static void bicubic_build(bicubic *s, const double *ys, int ni, const double *xs, int nj, const double *f) {
-    s->ni = ni; s->nj = nj; s->ys = ys; s->xs = xs;
+/* Node quadruples (f, fy, fx, fyx) of the bicubic spline surface through f (ni x nj) at
+ * knots ys x xs: natural-spline knot derivatives along each grid line (double) and
+ * central-difference cross derivatives (one-sided at the border). */
+static void bicubic_nodes(const double *ys, int ni, const double *xs, int nj, const double *f, double *c4) {
     const size_t nn = (size_t)ni * nj;
-    s->f = (double *)malloc(nn * sizeof(double));
-    s->fy = (double *)malloc(nn * sizeof(double));
-    s->fx = (double *)malloc(nn * sizeof(double));
-    s->fyx = (double *)malloc(nn * sizeof(double));
-    memcpy(s->f, f, nn * sizeof(double));
     double *tmp = (double *)malloc(sizeof(double) * (ni > nj ? ni : nj));
+    for (size_t k = 0; k < nn; k++) c4[4 * k] = f[k];
     for (int j = 0; j < nj; j++) {            /* along the first coordinate, per column */
         natural_spline_deriv(ys, f + j, nj, ni, tmp);
-        for (int i = 0; i < ni; i++) s->fy[(size_t)i * nj + j] = tmp[i];
+        for (int i = 0; i < ni; i++) c4[4 * ((size_t)i * nj + j) + 1] = tmp[i];
     }
     for (int i = 0; i < ni; i++) {            /* along the second coordinate, per row */
         natural_spline_deriv(xs, f + (size_t)i * nj, 1, nj, tmp);
-        for (int j = 0; j < nj; j++) s->fx[(size_t)i * nj + j] = tmp[j];
+        for (int j = 0; j < nj; j++) c4[4 * ((size_t)i * nj + j) + 2] = tmp[j];
     }
     for (int i = 0; i < ni; i++) {
         const int ni_ = i + 1 < ni ? i + 1 : ni - 1, pi = i - 1 >= 0 ? i - 1 : 0;
         for (int j = 0; j < nj; j++) {
             const int nj_ = j + 1 < nj ? j + 1 : nj - 1, pj = j - 1 >= 0 ? j - 1 : 0;
-            s->fyx[(size_t)i * nj + j] =
+            c4[4 * ((size_t)i * nj + j) + 3] =
                 (f[(size_t)ni_ * nj + nj_] - f[(size_t)ni_ * nj + pj] - f[(size_t)pi * nj + nj_] + f[(size_t)pi * nj + pj]) /
                 ((ys[ni_] - ys[pi]) * (xs[nj_] - xs[pj]));
         }
@@ -114,105 +110,17 @@ static void bicubic_build(bicubic *s, const double *ys, int ni, const double *xs
     free(tmp);
 }
 
-static void bicubic_free(bicubic *s) { free(s->f); free(s->fy); free(s->fx); free(s->fyx); }
+#define REAL float
+#define SUFFIX _f32
+#include "oracle_interp_impl.h"
+#undef REAL
+#undef SUFFIX
 
-/* Index of the knot interval holding c (c inside [v0, v_{n-1}]); the last knot maps to
- * the last interval. */
-static int knot_interval(const double *v, int n, double c) {
-    int lo = 0, hi = n - 1;
-    if (c >= v[n - 1]) return n - 2;
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) / 2;
-        if (v[mid] <= c) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
-static void hermite_basis(double t, double h0[2], double h1[2]) {
-    const double t2 = t * t, t3 = t2 * t;
-    h0[0] = 2.0 * t3 - 3.0 * t2 + 1.0;
-    h0[1] = -2.0 * t3 + 3.0 * t2;
-    h1[0] = t3 - 2.0 * t2 + t;
-    h1[1] = t3 - t2;
-}
-
-/* Canonical evaluation order (shared bit-for-bit with the CUDA warp kernel): column
- * basis X = (h00, h01, dx*h10, dx*h11)(tx), row basis Y likewise in ty; first the four
- * column sums w, then p = ((w0*Y0 + w1*Y1) + w2*Y2) + w3*Y3. */
-static double bicubic_value(const bicubic *s, double y, double x) {
-    const int i = knot_interval(s->ys, s->ni, y), j = knot_interval(s->xs, s->nj, x);
-    const double dy = s->ys[i + 1] - s->ys[i], dx = s->xs[j + 1] - s->xs[j];
-    const double ty = (y - s->ys[i]) / dy, tx = (x - s->xs[j]) / dx;
-    double ay0[2], ay1[2], ax0[2], ax1[2];
-    hermite_basis(ty, ay0, ay1);
-    hermite_basis(tx, ax0, ax1);
-    const double X0 = ax0[0], X1 = ax0[1], X2 = dx * ax1[0], X3 = dx * ax1[1];
-    const double Y0 = ay0[0], Y1 = ay0[1], Y2 = dy * ay1[0], Y3 = dy * ay1[1];
-    double w[4];
-    for (int a = 0; a < 2; a++) {
-        const size_t k0 = (size_t)(i + a) * s->nj + j, k1 = k0 + 1;
-        w[a] = s->f[k0] * X0 + s->f[k1] * X1 + s->fx[k0] * X2 + s->fx[k1] * X3;
-        w[2 + a] = s->fy[k0] * X0 + s->fy[k1] * X1 + s->fyx[k0] * X2 + s->fyx[k1] * X3;
-    }
-    return w[0] * Y0 + w[1] * Y1 + w[2] * Y2 + w[3] * Y3;
-}
-
-/* ---------------- Akima spline on a 5-knot window ---------------- */
-static double parabola_deriv(const double *x, const double *y, int at, int i0, int i1, int i2) {
-    const double X = x[at];
-    const double x0 = x[i0], x1 = x[i1], x2 = x[i2];
-    return y[i0] * ((X - x1) + (X - x2)) / ((x0 - x1) * (x0 - x2)) +
-           y[i1] * ((X - x0) + (X - x2)) / ((x1 - x0) * (x1 - x2)) +
-           y[i2] * ((X - x0) + (X - x1)) / ((x2 - x0) * (x2 - x1));
-}
-
-static double akima5_value(const double *x, const double *y, double t) {
-    double d[4], w[4] = {0, 0, 0, 0}, fd[5];
-    for (int k = 0; k < 4; k++) d[k] = (y[k + 1] - y[k]) / (x[k + 1] - x[k]);
-    for (int k = 1; k < 4; k++) w[k] = fabs(d[k] - d[k - 1]);
-    {
-        const double wp = w[3], wm = w[1];
-        if (fabs(wp) <= 4.9e-324 && fabs(wm) <= 4.9e-324)
-            fd[2] = ((x[3] - x[2]) * d[1] + (x[2] - x[1]) * d[2]) / (x[3] - x[1]);
-        else
-            fd[2] = (wp * d[1] + wm * d[2]) / (wp + wm);
-    }
-    fd[0] = parabola_deriv(x, y, 0, 0, 1, 2);
-    fd[1] = parabola_deriv(x, y, 1, 0, 1, 2);
-    fd[3] = parabola_deriv(x, y, 3, 2, 3, 4);
-    fd[4] = parabola_deriv(x, y, 4, 2, 3, 4);
-    const int k = knot_interval(x, 5, t);
-    const double h = x[k + 1] - x[k], s = t - x[k];
-    const double c2 = (3.0 * (y[k + 1] - y[k]) / h - 2.0 * fd[k] - fd[k + 1]) / h;
-    const double c3 = (2.0 * (y[k] - y[k + 1]) / h + fd[k] + fd[k + 1]) / (h * h);
-    return y[k] + s * (fd[k] + s * (c2 + s * c3));
-}
-
-/* start of the 5-knot window for c (binary search, the window centred on the hit or
- * the interval, clamped to the knot range) */
-static int akima_window(const double *v, int n, double c) {
-    int lo = 0, hi = n;                      /* first index with v[idx] > c */
-    while (lo < hi) {
-        const int mid = (lo + hi) / 2;
-        if (v[mid] <= c) lo = mid + 1; else hi = mid;
-    }
-    int r;
-    if (lo > 0 && v[lo - 1] == c) r = (lo - 1) - 2;   /* exact knot */
-    else r = lo - 2;                                    /* inside (v[lo-1], v[lo]) */
-    if (r < 0) r = 0;
-    if (r + 5 >= n) r = n - 5;
-    return r;
-}
-
-static double akima2d_value(const double *ys, int ni, const double *xs, int nj, const double *f, double y, double x) {
-    const int i = akima_window(ys, ni, y), j = akima_window(xs, nj, x);
-    double col[5], row[5];
-    for (int b = 0; b < 5; b++) {
-        for (int a = 0; a < 5; a++) col[a] = f[(size_t)(i + a) * nj + (j + b)];
-        row[b] = akima5_value(ys + i, col, y);
-    }
-    return akima5_value(xs + j, row, x);
-}
+#define REAL double
+#define SUFFIX _f64
+#include "oracle_interp_impl.h"
+#undef REAL
+#undef SUFFIX
 
 /* ---------------- warp ---------------- */
 static float read_pix(const void *img, int pix_bytes, int w, int y, int x) {
@@ -265,28 +173,38 @@ static void store_pix(void *img, int pix_bytes, int w, int y, int x, float v, in
 /* Exported pieces (ctypes) ------------------------------------------------------- */
 
 /* Per-pixel field of one level: tile displacements u, v (ni x nj, row-major) at tile
- * centres ys[ni], xs[nj] -> fu, fv (h x w float).  Coordinates clamped to the centre box. */
+ * centres ys[ni], xs[nj] -> fu, fv (h x w float).  Coordinates clamped to the centre box.
+ * precision 0: the surface is evaluated in float (the CUDA formulation); 1: in double. */
 void orc_displacement_field(const double *ys, int ni, const double *xs, int nj, const float *u, const float *v, int h,
-                            int w, float *fu, float *fv) {
+                            int w, int precision, float *fu, float *fv) {
     const size_t nn = (size_t)ni * nj;
     double *du = (double *)malloc(nn * sizeof(double)), *dv = (double *)malloc(nn * sizeof(double));
+    double *cu = (double *)malloc(4 * nn * sizeof(double)), *cv = (double *)malloc(4 * nn * sizeof(double));
     for (size_t k = 0; k < nn; k++) { du[k] = u[k]; dv[k] = v[k]; }
-    bicubic su, sv;
-    bicubic_build(&su, ys, ni, xs, nj, du);
-    bicubic_build(&sv, ys, ni, xs, nj, dv);
+    bicubic_nodes(ys, ni, xs, nj, du, cu);
+    bicubic_nodes(ys, ni, xs, nj, dv, cv);
     const float ymin = (float)ys[0], ymax = (float)ys[ni - 1], xmin = (float)xs[0], xmax = (float)xs[nj - 1];
+    float *fcu = (float *)malloc(4 * nn * sizeof(float)), *fcv = (float *)malloc(4 * nn * sizeof(float));
+    float *fys = (float *)malloc(ni * sizeof(float)), *fxs = (float *)malloc(nj * sizeof(float));
+    for (size_t k = 0; k < 4 * nn; k++) { fcu[k] = (float)cu[k]; fcv[k] = (float)cv[k]; }
+    for (int i = 0; i < ni; i++) fys[i] = (float)ys[i];
+    for (int j = 0; j < nj; j++) fxs[j] = (float)xs[j];
     for (int i = 0; i < h; i++) {
         float y = (float)i;
         if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
         for (int j = 0; j < w; j++) {
             float x = (float)j;
             if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
-            fu[(size_t)i * w + j] = (float)bicubic_value(&su, (double)y, (double)x);
-            fv[(size_t)i * w + j] = (float)bicubic_value(&sv, (double)y, (double)x);
+            if (precision == 0) {
+                fu[(size_t)i * w + j] = bicubic_value_f32(fys, ni, fxs, nj, fcu, y, x);
+                fv[(size_t)i * w + j] = bicubic_value_f32(fys, ni, fxs, nj, fcv, y, x);
+            } else {
+                fu[(size_t)i * w + j] = (float)bicubic_value_f64(ys, ni, xs, nj, cu, (double)y, (double)x);
+                fv[(size_t)i * w + j] = (float)bicubic_value_f64(ys, ni, xs, nj, cv, (double)y, (double)x);
+            }
         }
     }
-    bicubic_free(&su); bicubic_free(&sv);
-    free(du); free(dv);
+    free(du); free(dv); free(cu); free(cv); free(fcu); free(fcv); free(fys); free(fxs);
 }
 
 /* BothImages bilinear warp of a pair with a per-pixel field (halved inside). */
@@ -303,9 +221,10 @@ void orc_warp_both(const void *img_a, const void *img_b, int h, int w, int pix_b
 /* Inherited displacement of child tiles at centres (cy[ci], cx[cj]) from parent tiles
  * (pu, pv at centres py[pi], px[pj]), clamped to the parent box; needs >= 5 parent
  * tiles per axis, otherwise nothing is inherited (the reference computes a bilinear
- * value in that case but does not apply it). */
+ * value in that case but does not apply it).  precision 0: Akima splines in float (the
+ * CUDA formulation); 1: in double. */
 void orc_inherit(const double *py, int pni, const double *px, int pnj, const float *pu, const float *pv, const float *cy,
-                 int cni, const float *cx, int cnj, int round_int, float *cu, float *cv) {
+                 int cni, const float *cx, int cnj, int round_int, int precision, float *cu, float *cv) {
     if (pni < 5 || pnj < 5) {
         memset(cu, 0, sizeof(float) * cni * cnj);
         memset(cv, 0, sizeof(float) * cni * cnj);
@@ -313,7 +232,10 @@ void orc_inherit(const double *py, int pni, const double *px, int pnj, const flo
     }
     const size_t nn = (size_t)pni * pnj;
     double *du = (double *)malloc(nn * sizeof(double)), *dv = (double *)malloc(nn * sizeof(double));
+    float *fpy = (float *)malloc(pni * sizeof(float)), *fpx = (float *)malloc(pnj * sizeof(float));
     for (size_t k = 0; k < nn; k++) { du[k] = pu[k]; dv[k] = pv[k]; }
+    for (int i = 0; i < pni; i++) fpy[i] = (float)py[i];
+    for (int j = 0; j < pnj; j++) fpx[j] = (float)px[j];
     const float ymin = (float)py[0], ymax = (float)py[pni - 1], xmin = (float)px[0], xmax = (float)px[pnj - 1];
     for (int i = 0; i < cni; i++) {
         float y = cy[i];
@@ -321,15 +243,21 @@ void orc_inherit(const double *py, int pni, const double *px, int pnj, const flo
         for (int j = 0; j < cnj; j++) {
             float x = cx[j];
             if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
-            /* Tile.accumulateDisplacement on a reset tile: 0 + (float)value, rounded
-             * first for non-warping modes (FastMath.round(float)) */
-            const float iu = (float)akima2d_value(py, pni, px, pnj, du, (double)y, (double)x);
-            const float iv = (float)akima2d_value(py, pni, px, pnj, dv, (double)y, (double)x);
+            float iu, iv;
+            if (precision == 0) {
+                iu = akima2d_value_f32(fpy, pni, fpx, pnj, pu, y, x);
+                iv = akima2d_value_f32(fpy, pni, fpx, pnj, pv, y, x);
+            } else {
+                iu = (float)akima2d_value_f64(py, pni, px, pnj, du, (double)y, (double)x);
+                iv = (float)akima2d_value_f64(py, pni, px, pnj, dv, (double)y, (double)x);
+            }
+            /* Tile.accumulateDisplacement on a reset tile: 0 + value, rounded first for
+             * non-warping modes (FastMath.round(float)) */
             cu[(size_t)i * cnj + j] = 0.0f + (round_int ? (float)java_round(iu) : iu);
             cv[(size_t)i * cnj + j] = 0.0f + (round_int ? (float)java_round(iv) : iv);
         }
     }
-    free(du); free(dv);
+    free(du); free(dv); free(fpy); free(fpx);
 }
 
 /* Adaptive multi-pass PIV with BothImages bilinear warping (SuperPosition grids, SimpleStrategy).
@@ -371,10 +299,10 @@ int orc_piv_adaptive(const void *img_a, const void *img_b, int h, int w, int pix
             double *pyd = (double *)malloc(sizeof(double) * pni), *pxd = (double *)malloc(sizeof(double) * pnj);
             for (int i = 0; i < pni; i++) pyd[i] = (double)((float)ptops[i] + (float)pn / 2.0f - 0.5f);
             for (int j = 0; j < pnj; j++) pxd[j] = (double)((float)plefts[j] + (float)pn / 2.0f - 0.5f);
-            orc_inherit(pyd, pni, pxd, pnj, pu, pv, cyf, ni, cxf, nj, warp_mode == 0, cu, cv);
+            orc_inherit(pyd, pni, pxd, pnj, pu, pv, cyf, ni, cxf, nj, warp_mode == 0, precision, cu, cv);
             free(pyd); free(pxd);
             if (warp_mode == 1) {
-                orc_displacement_field(cyd, ni, cxd, nj, cu, cv, h, w, fu, fv);
+                orc_displacement_field(cyd, ni, cxd, nj, cu, cv, h, w, precision, fu, fv);
                 orc_warp_both(img_a, img_b, h, w, pix_bytes, fu, fv, int16_quirk, wa, wb);
                 sa = wa; sb = wb;
             }

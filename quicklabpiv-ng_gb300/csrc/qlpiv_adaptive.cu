@@ -9,7 +9,9 @@
 //              bicubic spline surface through the current level's tile displacements
 //              (natural-spline knot derivatives, finite-difference cross derivatives,
 //              Hermite patches), evaluated per pixel with coordinates clamped to the
-//              tile-centre box.  Computed in double like the reference.
+//              tile-centre box.  Knot derivatives are solved in double; the surface is
+//              evaluated in float (the reference evaluates it in double: GB300's FP64 rate
+//              is ~1/60 of FP32, and float keeps the field within ~1e-6 px).
 //   B-warp     BiLinearImageWarpingStrategy.warpPixelOnImage (S/images/...:143-265),
 //              BothImages mode: field halved, A sampled at (i-u, j-v), B at (i+u, j+v),
 //              nearest-pixel anchor plus the neighbour on the residual's side, output
@@ -27,7 +29,9 @@ namespace qlpiv {
 
 // ---------------- shared device helpers ----------------
 
-__host__ __device__ __forceinline__ int knot_interval(const double *v, int n, double c) {
+// Interpolators in float, same formulation and operand order as the CPU oracle's
+// float path (oracle/oracle_interp_impl.h).
+__host__ __device__ __forceinline__ int knot_interval(const float *v, int n, float c) {
     int lo = 0, hi = n - 1;
     if (c >= v[n - 1]) return n - 2;
     while (hi - lo > 1) {
@@ -37,30 +41,30 @@ __host__ __device__ __forceinline__ int knot_interval(const double *v, int n, do
     return lo;
 }
 
-__host__ __device__ __forceinline__ void hermite_basis(double t, double h0[2], double h1[2]) {
-    const double t2 = t * t, t3 = t2 * t;
-    h0[0] = 2.0 * t3 - 3.0 * t2 + 1.0;
-    h0[1] = -2.0 * t3 + 3.0 * t2;
-    h1[0] = t3 - 2.0 * t2 + t;
+__host__ __device__ __forceinline__ void hermite_basis(float t, float h0[2], float h1[2]) {
+    const float t2 = t * t, t3 = t2 * t;
+    h0[0] = 2.0f * t3 - 3.0f * t2 + 1.0f;
+    h0[1] = -2.0f * t3 + 3.0f * t2;
+    h1[0] = t3 - 2.0f * t2 + t;
     h1[1] = t3 - t2;
 }
 
-__host__ __device__ __forceinline__ double parabola_deriv(const double *x, const double *y, int at, int i0, int i1, int i2) {
-    const double X = x[at];
-    const double x0 = x[i0], x1 = x[i1], x2 = x[i2];
+__host__ __device__ __forceinline__ float parabola_deriv(const float *x, const float *y, int at, int i0, int i1, int i2) {
+    const float X = x[at];
+    const float x0 = x[i0], x1 = x[i1], x2 = x[i2];
     return y[i0] * ((X - x1) + (X - x2)) / ((x0 - x1) * (x0 - x2)) +
            y[i1] * ((X - x0) + (X - x2)) / ((x1 - x0) * (x1 - x2)) +
            y[i2] * ((X - x0) + (X - x1)) / ((x2 - x0) * (x2 - x1));
 }
 
 // Akima spline through 5 knots, evaluated at t (knots ascending, t inside).
-__host__ __device__ double akima5_value(const double *x, const double *y, double t) {
-    double d[4], w[4] = {0.0, 0.0, 0.0, 0.0}, fd[5];
+__host__ __device__ float akima5_value(const float *x, const float *y, float t) {
+    float d[4], w[4] = {0.0f, 0.0f, 0.0f, 0.0f}, fd[5];
     for (int k = 0; k < 4; k++) d[k] = (y[k + 1] - y[k]) / (x[k + 1] - x[k]);
-    for (int k = 1; k < 4; k++) w[k] = fabs(d[k] - d[k - 1]);
+    for (int k = 1; k < 4; k++) w[k] = fabsf(d[k] - d[k - 1]);
     {
-        const double wp = w[3], wm = w[1];
-        if (fabs(wp) <= 4.9e-324 && fabs(wm) <= 4.9e-324)
+        const float wp = w[3], wm = w[1];
+        if (wp == 0.0f && wm == 0.0f)
             fd[2] = ((x[3] - x[2]) * d[1] + (x[2] - x[1]) * d[2]) / (x[3] - x[1]);
         else
             fd[2] = (wp * d[1] + wm * d[2]) / (wp + wm);
@@ -70,13 +74,13 @@ __host__ __device__ double akima5_value(const double *x, const double *y, double
     fd[3] = parabola_deriv(x, y, 3, 2, 3, 4);
     fd[4] = parabola_deriv(x, y, 4, 2, 3, 4);
     const int k = knot_interval(x, 5, t);
-    const double h = x[k + 1] - x[k], s = t - x[k];
-    const double c2 = (3.0 * (y[k + 1] - y[k]) / h - 2.0 * fd[k] - fd[k + 1]) / h;
-    const double c3 = (2.0 * (y[k] - y[k + 1]) / h + fd[k] + fd[k + 1]) / (h * h);
+    const float h = x[k + 1] - x[k], s = t - x[k];
+    const float c2 = (3.0f * (y[k + 1] - y[k]) / h - 2.0f * fd[k] - fd[k + 1]) / h;
+    const float c3 = (2.0f * (y[k] - y[k + 1]) / h + fd[k] + fd[k + 1]) / (h * h);
     return y[k] + s * (fd[k] + s * (c2 + s * c3));
 }
 
-__host__ __device__ __forceinline__ int akima_window(const double *v, int n, double c) {
+__host__ __device__ __forceinline__ int akima_window(const float *v, int n, float c) {
     int lo = 0, hi = n;
     while (lo < hi) {
         const int mid = (lo + hi) / 2;
@@ -94,38 +98,45 @@ __host__ __device__ __forceinline__ int java_round(float x) { return (int)floorf
 
 // ---------------- B-inherit ----------------
 
-// Inherited displacement of child tile gid = pair * cni*cnj + i * cnj + j.
-__host__ __device__ void inherit_one(long gid, const double *py, int pni, const double *px, int pnj, const float *pu,
-                                     const float *pv, const float *cy, int cni, const float *cx, int cnj,
-                                     int round_int, float *cu, float *cv) {
+// Stage 1, entry gid = (pair, child row i, parent column pj): Akima spline along the
+// first coordinate through parent column pj (5-knot window around the clamped child
+// centre y), evaluated at y.  These are the row[] values of every child tile of row i.
+__host__ __device__ void inherit_rows_one(long gid, const float *py, int pni, int pnj, const float *pu, const float *pv,
+                                          const float *cy, int cni, float *ru, float *rv) {
+    const long per = (long)cni * pnj;
+    const int pair = (int)(gid / per);
+    const long k = gid - (long)pair * per;
+    const int i = (int)(k / pnj), pj = (int)(k - (long)i * pnj);
+    const float ymin = py[0], ymax = py[pni - 1];
+    float y = cy[i];
+    if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
+    const int wi = akima_window(py, pni, y);
+    const float *fu = pu + (long)pair * pni * pnj;
+    const float *fv = pv + (long)pair * pni * pnj;
+    float cu[5], cv[5];
+    for (int a = 0; a < 5; a++) {
+        cu[a] = fu[(long)(wi + a) * pnj + pj];
+        cv[a] = fv[(long)(wi + a) * pnj + pj];
+    }
+    ru[gid] = akima5_value(py + wi, cu, y);
+    rv[gid] = akima5_value(py + wi, cv, y);
+}
+
+// Stage 2, child tile gid = (pair, i, j): Akima spline along the second coordinate
+// through the 5 stage-1 values of the window around the clamped child centre x.
+__host__ __device__ void inherit_cols_one(long gid, const float *px, int pnj, const float *cx, int cni, int cnj,
+                                          const float *ru, const float *rv, int round_int, float *cu, float *cv) {
     const long cnt = (long)cni * cnj;
     const int pair = (int)(gid / cnt);
     const long k = gid - (long)pair * cnt;
     const int i = (int)(k / cnj), j = (int)(k - (long)i * cnj);
-    if (pni < 5 || pnj < 5) {  // the reference computes a bilinear value here but never applies it
-        cu[gid] = 0.0f;
-        cv[gid] = 0.0f;
-        return;
-    }
-    const float ymin = (float)py[0], ymax = (float)py[pni - 1], xmin = (float)px[0], xmax = (float)px[pnj - 1];
-    float y = cy[i], x = cx[j];
-    if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
+    const float xmin = px[0], xmax = px[pnj - 1];
+    float x = cx[j];
     if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
-    const int wi = akima_window(py, pni, (double)y), wj = akima_window(px, pnj, (double)x);
-    const float *fu = pu + (long)pair * pni * pnj;
-    const float *fv = pv + (long)pair * pni * pnj;
-    double rowu[5], rowv[5], colu[5], colv[5];
-    for (int b = 0; b < 5; b++) {
-        for (int a = 0; a < 5; a++) {
-            const long kk = (long)(wi + a) * pnj + (wj + b);
-            colu[a] = (double)fu[kk];
-            colv[a] = (double)fv[kk];
-        }
-        rowu[b] = akima5_value(py + wi, colu, (double)y);
-        rowv[b] = akima5_value(py + wi, colv, (double)y);
-    }
-    const float iu = (float)akima5_value(px + wj, rowu, (double)x);
-    const float iv = (float)akima5_value(px + wj, rowv, (double)x);
+    const int wj = akima_window(px, pnj, x);
+    const long row = ((long)pair * cni + i) * pnj + wj;
+    const float iu = akima5_value(px + wj, ru + row, x);
+    const float iv = akima5_value(px + wj, rv + row, x);
     if (round_int) {
         cu[gid] = 0.0f + (float)java_round(iu);
         cv[gid] = 0.0f + (float)java_round(iv);
@@ -135,13 +146,18 @@ __host__ __device__ void inherit_one(long gid, const double *py, int pni, const 
     }
 }
 
-// One thread per (pair, child tile).  Parent arrays are [pairs][pni*pnj].
-__global__ void inherit_kernel(int pairs, const double *py, int pni, const double *px, int pnj, const float *pu,
-                               const float *pv, const float *cy, int cni, const float *cx, int cnj, int round_int,
-                               float *cu, float *cv) {
+__global__ void inherit_rows_kernel(int pairs, const float *py, int pni, int pnj, const float *pu, const float *pv,
+                                    const float *cy, int cni, float *ru, float *rv) {
     const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long)cni * cnj * pairs) return;
-    inherit_one(gid, py, pni, px, pnj, pu, pv, cy, cni, cx, cnj, round_int, cu, cv);
+    if (gid >= (long)pairs * cni * pnj) return;
+    inherit_rows_one(gid, py, pni, pnj, pu, pv, cy, cni, ru, rv);
+}
+
+__global__ void inherit_cols_kernel(int pairs, const float *px, int pnj, const float *cx, int cni, int cnj,
+                                    const float *ru, const float *rv, int round_int, float *cu, float *cv) {
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long)pairs * cni * cnj) return;
+    inherit_cols_one(gid, px, pnj, cx, cni, cnj, ru, rv, round_int, cu, cv);
 }
 
 // ---------------- B-field spline set-up ----------------
@@ -229,7 +245,8 @@ __global__ void spline_lines_kernel(int pairs, const double *ys, const double *c
     spline_lines_one(gid, ys, cpy, ni, xs, cpx, nj, u, v, coef);
 }
 
-// Cross derivatives by central differences (one-sided at the border), node gid.
+// Cross derivatives by central differences (one-sided at the border), node gid; then
+// the node quadruple (f, fy, fx, fyx) rounded to float for the evaluation.
 __host__ __device__ void spline_cross_one(long gid, const double *ys, int ni, const double *xs, int nj, const float *u,
                                           const float *v, SplineCoef coef) {
     const long cnt = (long)ni * nj;
@@ -244,7 +261,10 @@ __host__ __device__ void spline_cross_one(long gid, const double *ys, int ni, co
         const float *f = (comp == 0 ? u : v) + base;
         const double a = (double)f[(long)ni_ * nj + nj_], b = (double)f[(long)ni_ * nj + pj];
         const double c = (double)f[(long)pi * nj + nj_], d = (double)f[(long)pi * nj + pj];
-        (comp == 0 ? coef.fyx_u : coef.fyx_v)[base + k] = (a - b - c + d) / den;
+        const double fyx = (a - b - c + d) / den;
+        const double fy = (comp == 0 ? coef.fy_u : coef.fy_v)[base + k];
+        const double fx = (comp == 0 ? coef.fx_u : coef.fx_v)[base + k];
+        (comp == 0 ? coef.c4_u : coef.c4_v)[base + k] = make_float4(f[k], (float)fy, (float)fx, (float)fyx);
     }
 }
 
@@ -295,24 +315,26 @@ __host__ __device__ __forceinline__ Pix warp_store(float value, int int16_quirk)
     return (Pix)(uint16_t)r;
 }
 
-// Canonical field evaluation order shared with the oracle.
-__host__ __device__ __forceinline__ double field_value(const double *ys, int ni, const double *xs, int nj, const float *f,
-                                              const double *fy, const double *fx, const double *fyx, double y,
-                                              double x) {
+// Canonical field evaluation order shared with the oracle's float path: column basis
+// X = (h00, h01, dx*h10, dx*h11)(tx), row basis Y likewise; the four column sums w
+// first, then ((w0*Y0 + w1*Y1) + w2*Y2) + w3*Y3.
+__host__ __device__ __forceinline__ float field_value(const float *ys, int ni, const float *xs, int nj,
+                                                      const float4 *c4, float y, float x) {
     const int i = knot_interval(ys, ni, y), j = knot_interval(xs, nj, x);
-    const double dy = ys[i + 1] - ys[i], dx = xs[j + 1] - xs[j];
-    const double ty = (y - ys[i]) / dy, tx = (x - xs[j]) / dx;
-    double ay0[2], ay1[2], ax0[2], ax1[2];
+    const float dy = ys[i + 1] - ys[i], dx = xs[j + 1] - xs[j];
+    const float ty = (y - ys[i]) / dy, tx = (x - xs[j]) / dx;
+    float ay0[2], ay1[2], ax0[2], ax1[2];
     hermite_basis(ty, ay0, ay1);
     hermite_basis(tx, ax0, ax1);
-    const double X0 = ax0[0], X1 = ax0[1], X2 = dx * ax1[0], X3 = dx * ax1[1];
-    const double Y0 = ay0[0], Y1 = ay0[1], Y2 = dy * ay1[0], Y3 = dy * ay1[1];
-    double w[4];
+    const float X0 = ax0[0], X1 = ax0[1], X2 = dx * ax1[0], X3 = dx * ax1[1];
+    const float Y0 = ay0[0], Y1 = ay0[1], Y2 = dy * ay1[0], Y3 = dy * ay1[1];
+    float w[4];
 #pragma unroll
     for (int a = 0; a < 2; a++) {
-        const long k0 = (long)(i + a) * nj + j, k1 = k0 + 1;
-        w[a] = (double)f[k0] * X0 + (double)f[k1] * X1 + fx[k0] * X2 + fx[k1] * X3;
-        w[2 + a] = fy[k0] * X0 + fy[k1] * X1 + fyx[k0] * X2 + fyx[k1] * X3;
+        const long k0 = (long)(i + a) * nj + j;
+        const float4 n0 = c4[k0], n1 = c4[k0 + 1];
+        w[a] = n0.x * X0 + n1.x * X1 + n0.z * X2 + n1.z * X3;
+        w[2 + a] = n0.y * X0 + n1.y * X1 + n0.w * X2 + n1.w * X3;
     }
     return w[0] * Y0 + w[1] * Y1 + w[2] * Y2 + w[3] * Y3;
 }
@@ -320,22 +342,19 @@ __host__ __device__ __forceinline__ double field_value(const double *ys, int ni,
 // Pixel (i, j) of pair `pair`: field, then both warped pixels.
 template <typename Pix>
 __host__ __device__ __forceinline__ void warp_one(int pair, int i, int j, const qlpiv_frame *src,
-                                                  const qlpiv_frame *dst, const double *ys, int ni, const double *xs,
-                                                  int nj, const float *u, const float *v, SplineCoef coef,
-                                                  int int16_quirk) {
+                                                  const qlpiv_frame *dst, const float *ys, int ni, const float *xs,
+                                                  int nj, const float4 *c4u, const float4 *c4v, int int16_quirk) {
     const qlpiv_frame fs = src[pair];
     const int h = fs.height, w = fs.width;
     if (i >= h || j >= w) return;
     const qlpiv_frame fd = dst[pair];
     const long base = (long)pair * ni * nj;
-    const float ymin = (float)ys[0], ymax = (float)ys[ni - 1], xmin = (float)xs[0], xmax = (float)xs[nj - 1];
+    const float ymin = ys[0], ymax = ys[ni - 1], xmin = xs[0], xmax = xs[nj - 1];
     float y = (float)i, x = (float)j;
     if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
     if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
-    const float fu = (float)field_value(ys, ni, xs, nj, u + base, coef.fy_u + base, coef.fx_u + base,
-                                        coef.fyx_u + base, (double)y, (double)x);
-    const float fv = (float)field_value(ys, ni, xs, nj, v + base, coef.fy_v + base, coef.fx_v + base,
-                                        coef.fyx_v + base, (double)y, (double)x);
+    const float fu = field_value(ys, ni, xs, nj, c4u + base, y, x);
+    const float fv = field_value(ys, ni, xs, nj, c4v + base, y, x);
     const float hu = fu / 2.0f, hv = fv / 2.0f;
     const Pix *ia = reinterpret_cast<const Pix *>(fs.img_a);
     const Pix *ib = reinterpret_cast<const Pix *>(fs.img_b);
@@ -349,28 +368,25 @@ __host__ __device__ __forceinline__ void warp_one(int pair, int i, int j, const 
 // original and the warped images.
 template <typename Pix>
 __global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, const qlpiv_frame *dst,
-                                                        const double *ys, int ni, const double *xs, int nj,
-                                                        const float *u, const float *v, SplineCoef coef,
-                                                        int int16_quirk) {
+                                                        const float *ys, int ni, const float *xs, int nj,
+                                                        const float4 *c4u, const float4 *c4v, int int16_quirk) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    warp_one<Pix>(blockIdx.z, i, j, src, dst, ys, ni, xs, nj, u, v, coef, int16_quirk);
+    warp_one<Pix>(blockIdx.z, i, j, src, dst, ys, ni, xs, nj, c4u, c4v, int16_quirk);
 }
 
 // Per-pixel field only (test hook for the field stage): pair 0, outputs h x w floats.
-__global__ void field_kernel(int h, int w, const double *ys, int ni, const double *xs, int nj, const float *u,
-                             const float *v, SplineCoef coef, float *fu_out, float *fv_out) {
+__global__ void field_kernel(int h, int w, const float *ys, int ni, const float *xs, int nj, const float4 *c4u,
+                             const float4 *c4v, float *fu_out, float *fv_out) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= h || j >= w) return;
-    const float ymin = (float)ys[0], ymax = (float)ys[ni - 1], xmin = (float)xs[0], xmax = (float)xs[nj - 1];
+    const float ymin = ys[0], ymax = ys[ni - 1], xmin = xs[0], xmax = xs[nj - 1];
     float y = (float)i, x = (float)j;
     if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
     if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
-    fu_out[(long)i * w + j] =
-        (float)field_value(ys, ni, xs, nj, u, coef.fy_u, coef.fx_u, coef.fyx_u, (double)y, (double)x);
-    fv_out[(long)i * w + j] =
-        (float)field_value(ys, ni, xs, nj, v, coef.fy_v, coef.fx_v, coef.fyx_v, (double)y, (double)x);
+    fu_out[(long)i * w + j] = field_value(ys, ni, xs, nj, c4u, y, x);
+    fv_out[(long)i * w + j] = field_value(ys, ni, xs, nj, c4v, y, x);
 }
 
 // B tile origins for non-warping modes: round(top + u), round(left + v)
@@ -387,13 +403,19 @@ __global__ void displaced_origins_kernel(long count, const int *a_top, const int
 
 static inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
-cudaError_t launch_inherit(cudaStream_t s, int pairs, const double *py, int pni, const double *px, int pnj,
+cudaError_t launch_inherit(cudaStream_t s, int pairs, const float *py, int pni, const float *px, int pnj,
                            const float *pu, const float *pv, const float *cy, int cni, const float *cx, int cnj,
-                           int round_int, float *cu, float *cv) {
+                           int round_int, float *ru, float *rv, float *cu, float *cv) {
     const long n = (long)pairs * cni * cnj;
     if (n == 0) return cudaSuccess;
-    inherit_kernel<<<blocks_for(n, 128), 128, 0, s>>>(pairs, py, pni, px, pnj, pu, pv, cy, cni, cx, cnj, round_int,
-                                                      cu, cv);
+    if (pni < 5 || pnj < 5) {  // the reference computes a bilinear value here but never applies it
+        cudaError_t e = cudaMemsetAsync(cu, 0, sizeof(float) * n, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(cv, 0, sizeof(float) * n, s);
+        return e;
+    }
+    const long nr = (long)pairs * cni * pnj;
+    inherit_rows_kernel<<<blocks_for(nr, 128), 128, 0, s>>>(pairs, py, pni, pnj, pu, pv, cy, cni, ru, rv);
+    inherit_cols_kernel<<<blocks_for(n, 128), 128, 0, s>>>(pairs, px, pnj, cx, cni, cnj, ru, rv, round_int, cu, cv);
     return cudaGetLastError();
 }
 
@@ -409,22 +431,22 @@ cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const dou
 }
 
 cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
-                        const qlpiv_frame *dst, const double *ys, int ni, const double *xs, int nj, const float *u,
-                        const float *v, SplineCoef coef, int int16_quirk) {
+                        const qlpiv_frame *dst, const float *ys, int ni, const float *xs, int nj, SplineCoef coef,
+                        int int16_quirk) {
     dim3 blk(32, 8), grd(blocks_for(w, 32), blocks_for(h, 8), pairs);
     if (pixel_type == QLPIV_PIX_U8)
-        warp_both_kernel<uint8_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, u, v, coef, int16_quirk);
+        warp_both_kernel<uint8_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk);
     else if (pixel_type == QLPIV_PIX_U16)
-        warp_both_kernel<uint16_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, u, v, coef, int16_quirk);
+        warp_both_kernel<uint16_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 
-cudaError_t launch_field(cudaStream_t s, int h, int w, const double *ys, int ni, const double *xs, int nj,
-                         const float *u, const float *v, SplineCoef coef, float *fu, float *fv) {
+cudaError_t launch_field(cudaStream_t s, int h, int w, const float *ys, int ni, const float *xs, int nj,
+                         SplineCoef coef, float *fu, float *fv) {
     dim3 blk(32, 8), grd(blocks_for(w, 32), blocks_for(h, 8), 1);
-    field_kernel<<<grd, blk, 0, s>>>(h, w, ys, ni, xs, nj, u, v, coef, fu, fv);
+    field_kernel<<<grd, blk, 0, s>>>(h, w, ys, ni, xs, nj, coef.c4_u, coef.c4_v, fu, fv);
     return cudaGetLastError();
 }
 

@@ -7,23 +7,27 @@
 
 namespace qlpiv {
 
-// Knot derivatives of the bicubic displacement surfaces, [pairs][ni*nj] doubles each.
+// Knot derivatives of the bicubic displacement surfaces, [pairs][ni*nj] each: the
+// double line solves (fy, fx; fyx unused) and the float node quadruples
+// (f, fy, fx, fyx) the evaluation reads.
 struct SplineCoef {
     double *fy_u, *fx_u, *fyx_u;
     double *fy_v, *fx_v, *fyx_v;
+    float4 *c4_u, *c4_v;
 };
 
-cudaError_t launch_inherit(cudaStream_t s, int pairs, const double *py, int pni, const double *px, int pnj,
+// ru/rv: scratch of pairs x cni x pnj floats (stage-1 row values).
+cudaError_t launch_inherit(cudaStream_t s, int pairs, const float *py, int pni, const float *px, int pnj,
                            const float *pu, const float *pv, const float *cy, int cni, const float *cx, int cnj,
-                           int round_int, float *cu, float *cv);
+                           int round_int, float *ru, float *rv, float *cu, float *cv);
 // cpy/cpx: scratch of ni/nj doubles for the elimination factors.
 cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const double *cpy, int ni, const double *xs,
                           const double *cpx, int nj, const float *u, const float *v, SplineCoef coef);
 cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
-                        const qlpiv_frame *dst, const double *ys, int ni, const double *xs, int nj, const float *u,
-                        const float *v, SplineCoef coef, int int16_quirk);
-cudaError_t launch_field(cudaStream_t s, int h, int w, const double *ys, int ni, const double *xs, int nj,
-                         const float *u, const float *v, SplineCoef coef, float *fu, float *fv);
+                        const qlpiv_frame *dst, const float *ys, int ni, const float *xs, int nj, SplineCoef coef,
+                        int int16_quirk);
+cudaError_t launch_field(cudaStream_t s, int h, int w, const float *ys, int ni, const float *xs, int nj,
+                         SplineCoef coef, float *fu, float *fv);
 cudaError_t launch_displaced_origins(cudaStream_t s, long count, const int *a_top, const int *a_left, const float *u,
                                      const float *v, int *b_top, int *b_left);
 

@@ -80,7 +80,7 @@ struct qlpiv_handle {
     std::mutex mu;
     long launches = 0;
     qlpiv::DevBuf tiles_a, tiles_b, max_a, max_b, origins, vectors, planes, frames;
-    qlpiv::DevBuf scratch[8];            // stage test hooks
+    qlpiv::DevBuf scratch[12];           // stage test hooks
     qlpiv::AdaptivePlan *plan = nullptr; // cached adaptive PIV plan
     bool profiling = false;
     std::vector<qlpiv::StageEvent> prof_pending;

@@ -30,7 +30,8 @@ struct LevelPlan {
     DevBuf d_cy, d_cx, d_cyf, d_cxf, d_cpy, d_cpx;
     DevBuf d_fi, d_at, d_al, d_bt, d_bl;  // flattened work list, pairs x count
     DevBuf d_u, d_v;                       // tile displacements, pairs x count
-    DevBuf coef;                           // 6 x pairs x count doubles
+    DevBuf coef;                           // 6 doubles + 2 float4 per tile and pair
+    DevBuf d_rows;                         // inheritance stage 1: 2 x pairs x tiles_i x parent tiles_j
     long count() const { return (long)g.tiles_i * g.tiles_j; }
 };
 
@@ -48,10 +49,19 @@ void destroy_plan(AdaptivePlan *p) {
     if (!p) return;
     for (LevelPlan &l : p->levels)
         for (DevBuf *b : {&l.d_cy, &l.d_cx, &l.d_cyf, &l.d_cxf, &l.d_cpy, &l.d_cpx, &l.d_fi, &l.d_at, &l.d_al, &l.d_bt,
-                          &l.d_bl, &l.d_u, &l.d_v, &l.coef})
+                          &l.d_bl, &l.d_u, &l.d_v, &l.coef, &l.d_rows})
             b->release();
     for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table}) b->release();
     delete p;
+}
+
+// 6 double line-solve arrays followed by 2 float4 node arrays, n entries each.
+static size_t coef_bytes(long n) { return (size_t)n * (6 * sizeof(double) + 2 * sizeof(float4)); }
+
+static SplineCoef coef_at(void *base, long n) {
+    double *c = reinterpret_cast<double *>(base);
+    float4 *q = reinterpret_cast<float4 *>(c + 6 * n);
+    return SplineCoef{c, c + n, c + 2 * n, c + 3 * n, c + 4 * n, c + 5 * n, q, q + n};
 }
 
 static float full_scale(int pixel_type) { return pixel_type == QLPIV_PIX_U8 ? 255.0f : 65535.0f; }
@@ -160,7 +170,9 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
             (e = L.d_bl.ensure(sizeof(int32_t) * total)) != cudaSuccess ||
             (e = L.d_u.ensure(sizeof(float) * total)) != cudaSuccess ||
             (e = L.d_v.ensure(sizeof(float) * total)) != cudaSuccess ||
-            (e = L.coef.ensure(sizeof(double) * 6 * total)) != cudaSuccess)
+            (e = L.coef.ensure(coef_bytes(total))) != cudaSuccess ||
+            (lv > 0 && (e = L.d_rows.ensure(sizeof(float) * 2 * (long)pairs * ni *
+                                            p->levels[lv - 1].g.tiles_j)) != cudaSuccess))
             return cuda_fail(e, "adaptive plan");
         // the host vectors above die at scope exit: make the copies complete first
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "adaptive plan upload");
@@ -219,11 +231,7 @@ struct StageScope {
     }
 };
 
-static SplineCoef coef_of(LevelPlan &L, int pairs) {
-    double *c = L.coef.as<double>();
-    const long n = L.count() * pairs;
-    return SplineCoef{c, c + n, c + 2 * n, c + 3 * n, c + 4 * n, c + 5 * n};
-}
+static SplineCoef coef_of(LevelPlan &L, int pairs) { return coef_at(L.coef.p, L.count() * pairs); }
 
 // Queues the whole level loop; the last level's displacements end in levels.back().d_u/d_v.
 static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
@@ -243,13 +251,14 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
                 return cuda_fail(e, "level 0 reset");
         } else {
             LevelPlan &P = p->levels[lv - 1];
-            StageScope sc(h, "inherit", (int)lv, L.g.n, 1, total);
-            if ((e = launch_inherit(s, pairs, P.d_cy.as<double>(), P.g.tiles_i, P.d_cx.as<double>(), P.g.tiles_j,
+            StageScope sc(h, "inherit", (int)lv, L.g.n, 2, total);
+            float *ru = L.d_rows.as<float>(), *rv = ru + (long)pairs * L.g.tiles_i * P.g.tiles_j;
+            if ((e = launch_inherit(s, pairs, P.d_cyf.as<float>(), P.g.tiles_i, P.d_cxf.as<float>(), P.g.tiles_j,
                                     P.d_u.as<float>(), P.d_v.as<float>(), L.d_cyf.as<float>(), L.g.tiles_i,
-                                    L.d_cxf.as<float>(), L.g.tiles_j, d.warp_mode == QLPIV_WARP_NONE, u, v)) !=
-                cudaSuccess)
+                                    L.d_cxf.as<float>(), L.g.tiles_j, d.warp_mode == QLPIV_WARP_NONE, ru, rv, u,
+                                    v)) != cudaSuccess)
                 return cuda_fail(e, "inheritance");
-            h->launches++;
+            h->launches += 2;
         }
         const qlpiv_frame *src = frames_dev;
         const int *bt = L.d_at.as<int>(), *bl = L.d_al.as<int>();
@@ -266,9 +275,8 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
                 {
                     StageScope sc(h, "warp", (int)lv, L.g.n, 1, (long)pairs * p->height * p->width);
                     if ((e = launch_warp(s, p->pixel_type, pairs, p->height, p->width, frames_dev,
-                                         p->warped_table.as<qlpiv_frame>(), L.d_cy.as<double>(), L.g.tiles_i,
-                                         L.d_cx.as<double>(), L.g.tiles_j, u, v, c, d.int16_warp_quirk)) !=
-                        cudaSuccess)
+                                         p->warped_table.as<qlpiv_frame>(), L.d_cyf.as<float>(), L.g.tiles_i,
+                                         L.d_cxf.as<float>(), L.g.tiles_j, c, d.int16_warp_quirk)) != cudaSuccess)
                         return cuda_fail(e, "warp");
                 }
                 h->launches += 5;
@@ -359,49 +367,58 @@ qlpiv_status qlpiv_inherit(qlpiv_handle *h, int pni, int pnj, const double *p_ci
     if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
     cudaStream_t s = h->stream;
     const long pc = (long)pni * pnj, cc = (long)cni * cnj;
+    std::vector<float> fpy(p_ci, p_ci + pni), fpx(p_cj, p_cj + pnj);  // tile centres are exact in float
     DevBuf *b = h->scratch;
     cudaError_t e;
-    if ((e = upload(b[0], p_ci, sizeof(double) * pni, s)) != cudaSuccess ||
-        (e = upload(b[1], p_cj, sizeof(double) * pnj, s)) != cudaSuccess ||
+    if ((e = upload(b[0], fpy.data(), sizeof(float) * pni, s)) != cudaSuccess ||
+        (e = upload(b[1], fpx.data(), sizeof(float) * pnj, s)) != cudaSuccess ||
         (e = upload(b[2], pu, sizeof(float) * pc, s)) != cudaSuccess ||
         (e = upload(b[3], pv, sizeof(float) * pc, s)) != cudaSuccess ||
         (e = upload(b[4], c_ci, sizeof(float) * cni, s)) != cudaSuccess ||
         (e = upload(b[5], c_cj, sizeof(float) * cnj, s)) != cudaSuccess ||
-        (e = b[6].ensure(sizeof(float) * cc)) != cudaSuccess || (e = b[7].ensure(sizeof(float) * cc)) != cudaSuccess)
+        (e = b[6].ensure(sizeof(float) * 2 * cc)) != cudaSuccess ||
+        (e = b[7].ensure(sizeof(float) * 2 * (long)cni * pnj)) != cudaSuccess)
         return cuda_fail(e, "inherit upload");
-    if ((e = launch_inherit(s, 1, b[0].as<double>(), pni, b[1].as<double>(), pnj, b[2].as<float>(), b[3].as<float>(),
-                            b[4].as<float>(), cni, b[5].as<float>(), cnj, round_int, b[6].as<float>(),
-                            b[7].as<float>())) != cudaSuccess)
+    float *out = b[6].as<float>(), *rows = b[7].as<float>();
+    if ((e = launch_inherit(s, 1, b[0].as<float>(), pni, b[1].as<float>(), pnj, b[2].as<float>(), b[3].as<float>(),
+                            b[4].as<float>(), cni, b[5].as<float>(), cnj, round_int, rows, rows + (long)cni * pnj,
+                            out, out + cc)) != cudaSuccess)
         return cuda_fail(e, "inherit");
-    h->launches++;
-    if ((e = cudaMemcpyAsync(cu, b[6].p, sizeof(float) * cc, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(cv, b[7].p, sizeof(float) * cc, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+    h->launches += 2;
+    if ((e = cudaMemcpyAsync(cu, out, sizeof(float) * cc, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(cv, out + cc, sizeof(float) * cc, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
         return cuda_fail(e, "inherit download");
     return QLPIV_OK;
 }
 
-// Shared set-up of qlpiv_displacement_field / qlpiv_warp_pair: knots and displacements
-// uploaded, spline coefficients computed.  Uses scratch[0..7].
+// Shared set-up of qlpiv_displacement_field / qlpiv_warp_pair: knots (double for the
+// solve, float for the evaluation) and displacements uploaded, spline nodes computed.
+// Uses scratch[0..5] and scratch[8] (float knots: ni row knots then nj column knots).
 static qlpiv_status field_setup(qlpiv_handle *h, int ni, int nj, const double *ci, const double *cj, const float *u,
                                 const float *v, SplineCoef *coef) {
     cudaStream_t s = h->stream;
     DevBuf *b = h->scratch;
     const long cnt = (long)ni * nj;
+    std::vector<float> fk(ni + nj);
+    for (int i = 0; i < ni; i++) fk[i] = (float)ci[i];
+    for (int j = 0; j < nj; j++) fk[ni + j] = (float)cj[j];
     cudaError_t e;
     if ((e = upload(b[0], ci, sizeof(double) * ni, s)) != cudaSuccess ||
         (e = upload(b[1], cj, sizeof(double) * nj, s)) != cudaSuccess ||
         (e = upload(b[2], u, sizeof(float) * cnt, s)) != cudaSuccess ||
         (e = upload(b[3], v, sizeof(float) * cnt, s)) != cudaSuccess ||
         (e = b[4].ensure(sizeof(double) * (ni + nj))) != cudaSuccess ||
-        (e = b[5].ensure(sizeof(double) * 6 * cnt)) != cudaSuccess)
+        (e = b[5].ensure(coef_bytes(cnt))) != cudaSuccess ||
+        (e = upload(b[8], fk.data(), sizeof(float) * (ni + nj), s)) != cudaSuccess)
         return cuda_fail(e, "field upload");
-    double *c = b[5].as<double>();
-    *coef = SplineCoef{c, c + cnt, c + 2 * cnt, c + 3 * cnt, c + 4 * cnt, c + 5 * cnt};
+    *coef = coef_at(b[5].p, cnt);
     if ((e = launch_spline(s, 1, b[0].as<double>(), b[4].as<double>(), ni, b[1].as<double>(), b[4].as<double>() + ni,
                            nj, b[2].as<float>(), b[3].as<float>(), *coef)) != cudaSuccess)
         return cuda_fail(e, "spline");
     h->launches += 4;
+    // the float knots must outlive this function's host vector: wait for the upload
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "field set-up");
     return QLPIV_OK;
 }
 
@@ -422,8 +439,8 @@ qlpiv_status qlpiv_displacement_field(qlpiv_handle *h, int height, int width, in
     cudaError_t e;
     if ((e = b[6].ensure(sizeof(float) * px)) != cudaSuccess || (e = b[7].ensure(sizeof(float) * px)) != cudaSuccess)
         return cuda_fail(e, "field buffers");
-    if ((e = launch_field(s, height, width, b[0].as<double>(), ni, b[1].as<double>(), nj, b[2].as<float>(),
-                          b[3].as<float>(), coef, b[6].as<float>(), b[7].as<float>())) != cudaSuccess)
+    if ((e = launch_field(s, height, width, b[8].as<float>(), ni, b[8].as<float>() + ni, nj, coef, b[6].as<float>(),
+                          b[7].as<float>())) != cudaSuccess)
         return cuda_fail(e, "field");
     h->launches++;
     if ((e = cudaMemcpyAsync(fu, b[6].p, sizeof(float) * px, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
@@ -462,8 +479,8 @@ qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, const void *img_a,
         return cuda_fail(e, "warp upload");
     const qlpiv_frame *dt = h->frames.as<qlpiv_frame>();
     DevBuf *b = h->scratch;
-    if ((e = launch_warp(s, pixel_type, 1, height, width, dt, dt + 1, b[0].as<double>(), ni, b[1].as<double>(), nj,
-                         b[2].as<float>(), b[3].as<float>(), coef, int16_quirk)) != cudaSuccess)
+    if ((e = launch_warp(s, pixel_type, 1, height, width, dt, dt + 1, b[8].as<float>(), ni, b[8].as<float>() + ni, nj,
+                         coef, int16_quirk)) != cudaSuccess)
         return cuda_fail(e, "warp");
     h->launches++;
     if ((e = cudaMemcpyAsync(out_a, base + 2 * stride, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||

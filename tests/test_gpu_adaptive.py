@@ -53,6 +53,9 @@ def test_inherit_bit_exact(qp, handle, oracle, round_int):
     ou, ov = oracle.inherit(py.astype(np.float64), px.astype(np.float64), pu, pv, cy, cx, round_int)
     assert cu.tobytes() == ou.tobytes() and cv.tobytes() == ov.tobytes()
     assert np.abs(cu).max() > 1.0
+    # float evaluation stays within 1e-5 px of the double-precision interpolation
+    du, dv = oracle.inherit(py.astype(np.float64), px.astype(np.float64), pu, pv, cy, cx, round_int, precision=64)
+    assert np.abs(cu - du).max() <= (0.0 if round_int else 1e-5) + (1.0 if round_int else 0.0)
 
 
 def test_inherit_small_parent_grid_gives_zero(qp, handle):
@@ -69,6 +72,8 @@ def test_displacement_field_bit_exact(qp, handle, oracle):
     fu, fv = handle.displacement_field(cy.astype(np.float64), cx.astype(np.float64), u, v, h, w)
     ou, ov = oracle.displacement_field(cy.astype(np.float64), cx.astype(np.float64), u, v, h, w)
     assert fu.tobytes() == ou.tobytes() and fv.tobytes() == ov.tobytes()
+    du, dv = oracle.displacement_field(cy.astype(np.float64), cx.astype(np.float64), u, v, h, w, precision=64)
+    assert np.abs(fu - du).max() < 1e-5 and np.abs(fv - dv).max() < 1e-5
     # the surface interpolates the tile values at the centres (integer-plus-half centres
     # are not pixels, so check between the 4 surrounding pixels)
     assert np.abs(fu[int(cy[3]), int(cx[5])] - u[3, 5]) < 0.5

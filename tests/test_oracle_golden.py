@@ -180,3 +180,85 @@ def test_piv_pass_matches_single_ia(oracle, rankine_pair):
     assert r["u"] == np.float32(np.float32(pi) - np.float32(31))
     # the vortex field is smooth: most vectors are within a few px
     assert np.median(np.abs(out["u"])) < 8
+
+
+def _akima5_np(x, y, t):
+    d = np.diff(y) / np.diff(x)
+    w = np.r_[0.0, np.abs(np.diff(d))]
+    fd = np.zeros(5)
+    fd[2] = ((w[3] * d[1] + w[1] * d[2]) / (w[3] + w[1]) if w[3] + w[1] > 0
+             else ((x[3] - x[2]) * d[1] + (x[2] - x[1]) * d[2]) / (x[3] - x[1]))
+    for at, (i0, i1, i2) in ((0, (0, 1, 2)), (1, (0, 1, 2)), (3, (2, 3, 4)), (4, (2, 3, 4))):
+        c = np.polyfit(x[[i0, i1, i2]], y[[i0, i1, i2]], 2)
+        fd[at] = 2 * c[0] * x[at] + c[1]
+    k = int(min(max(np.searchsorted(x, t, side="right") - 1, 0), 3))
+    h = x[k + 1] - x[k]
+    s = t - x[k]
+    c2 = (3 * (y[k + 1] - y[k]) / h - 2 * fd[k] - fd[k + 1]) / h
+    c3 = (2 * (y[k] - y[k + 1]) / h + fd[k] + fd[k + 1]) / h ** 2
+    return y[k] + s * (fd[k] + s * (c2 + s * c3))
+
+
+def test_inherit_fp64_matches_independent_akima(oracle):
+    """B-inherit has no reference fixture: the oracle's double Akima (5x5 window) is
+    checked against an independent numpy implementation (parabola derivatives by polyfit)."""
+    rng = np.random.default_rng(5)
+    py = np.arange(9) * 16.0 + 31.5
+    px = np.arange(11) * 16.0 + 31.5
+    pu = rng.standard_normal((9, 11)).astype(np.float32)
+    cy = (np.arange(17) * 8.0 + 15.5).astype(np.float32)
+    cx = (np.arange(21) * 8.0 + 15.5).astype(np.float32)
+    cu, _ = oracle.inherit(py, px, pu, pu, cy, cx, precision=64)
+
+    def window(v, c):
+        lo = np.searchsorted(v, c, side="right")
+        r = (lo - 1) - 2 if lo > 0 and v[lo - 1] == c else lo - 2
+        return min(max(r, 0), len(v) - 5)
+
+    for i in range(len(cy)):
+        for j in range(len(cx)):
+            y = float(np.clip(cy[i], py[0], py[-1]))
+            x = float(np.clip(cx[j], px[0], px[-1]))
+            wi, wj = window(py, y), window(px, x)
+            row = [_akima5_np(py[wi:wi + 5], pu[wi:wi + 5, wj + b].astype(float), y) for b in range(5)]
+            ref = _akima5_np(px[wj:wj + 5], np.array(row), x)
+            assert abs(cu[i, j] - ref) < 2e-6, (i, j)
+
+
+def test_field_fp64_matches_independent_spline(oracle):
+    """B-field: natural cubic splines (scipy) for the knot derivatives and an explicit
+    bicubic Hermite patch, compared with the oracle's double evaluation."""
+    interp = pytest.importorskip("scipy.interpolate")
+    rng = np.random.default_rng(6)
+    ys = np.arange(7) * 8.0 + 7.5
+    xs = np.arange(9) * 8.0 + 7.5
+    f = rng.standard_normal((7, 9)).astype(np.float32)
+    h, w = 64, 80
+    fu, _ = oracle.displacement_field(ys, xs, f, f, h, w, precision=64)
+    fd = f.astype(float)
+    fy = np.stack([interp.CubicSpline(ys, fd[:, j], bc_type="natural")(ys, 1) for j in range(9)], 1)
+    fx = np.stack([interp.CubicSpline(xs, fd[i, :], bc_type="natural")(xs, 1) for i in range(7)], 0)
+    fyx = np.zeros_like(fd)
+    for i in range(7):
+        for j in range(9):
+            ni, pi = min(i + 1, 6), max(i - 1, 0)
+            nj, pj = min(j + 1, 8), max(j - 1, 0)
+            fyx[i, j] = (fd[ni, nj] - fd[ni, pj] - fd[pi, nj] + fd[pi, pj]) / ((ys[ni] - ys[pi]) * (xs[nj] - xs[pj]))
+
+    def basis(t):
+        return np.array([2 * t ** 3 - 3 * t ** 2 + 1, -2 * t ** 3 + 3 * t ** 2]), np.array([t ** 3 - 2 * t ** 2 + t,
+                                                                                           t ** 3 - t ** 2])
+    for (yy, xx) in [(0, 0), (10, 13), (20, 33), (40, 70), (63, 79), (31, 44)]:
+        y = float(np.clip(yy, ys[0], ys[-1]))
+        x = float(np.clip(xx, xs[0], xs[-1]))
+        i = min(int(np.searchsorted(ys, y, side="right") - 1), 5)
+        j = min(int(np.searchsorted(xs, x, side="right") - 1), 7)
+        dy, dx = ys[i + 1] - ys[i], xs[j + 1] - xs[j]
+        a0, a1 = basis((y - ys[i]) / dy)
+        b0, b1 = basis((x - xs[j]) / dx)
+        val = 0.0
+        for a in range(2):
+            for b in range(2):
+                val += (fd[i + a, j + b] * a0[a] * b0[b] + fy[i + a, j + b] * dy * a1[a] * b0[b]
+                        + fx[i + a, j + b] * dx * a0[a] * b1[b] + fyx[i + a, j + b] * dy * dx * a1[a] * b1[b])
+        assert abs(fu[int(yy), int(xx)] - val) < 1e-6, (yy, xx)
