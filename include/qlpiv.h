@@ -260,6 +260,24 @@ qlpiv_status qlpiv_piv_adaptive_device(qlpiv_handle *h, const qlpiv_adaptive_des
                                        int width, int num_pairs, const qlpiv_frame *frames, float *out_u,
                                        float *out_v);
 
+/* Velocity inheritance that allocates nothing (no counterpart in the reference).
+ * For callers that cannot let the library allocate device memory during a call -- a
+ * Java host passing device buffers from its own pool with a fixed memory budget, or an
+ * acquisition loop that must not take cudaMalloc's implicit synchronisation while frames
+ * stream in.  Same result as qlpiv_inherit, but every argument is in device memory (float
+ * centres) and the work is queued on `stream` (NULL: the legacy default stream); the call
+ * returns without waiting.  The stage-1 scratch is a fixed device array of
+ * 2 x QLPIV_NOALLOC_MAX_ROWS floats (4 MiB) that every GPU loading the library holds until
+ * exit; cni x pnj above QLPIV_NOALLOC_MAX_ROWS is rejected with QLPIV_E_SHAPE.  The first
+ * call on a device looks up that array's device address (cudaGetSymbolAddress), so make
+ * the first call on each device before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race.  No entry needs clearing between calls (every
+ * entry read is written earlier in the same call). */
+#define QLPIV_NOALLOC_MAX_ROWS 524288
+qlpiv_status qlpiv_inherit_noalloc(int device, void *stream, int pni, int pnj, const float *p_ci, const float *p_cj,
+                                   const float *pu, const float *pv, int cni, int cnj, const float *c_ci,
+                                   const float *c_cj, int round_int, float *cu, float *cv);
+
 /* Stage timing of the adaptive pipeline (CUDA events around every launch on the
  * handle's stream).  Accumulates while enabled; qlpiv_profile_read synchronises the
  * stream, returns the totals per (stage, level) and clears them. */

@@ -120,6 +120,7 @@ _SIGNATURES = {
     "qlpiv_warp_pair": (_i, [_vp, _i, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "qlpiv_piv_adaptive": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
     "qlpiv_piv_adaptive_device": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
+    "qlpiv_inherit_noalloc": (_i, [_i, _vp, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp]),
     "qlpiv_profile_enable": (_i, [_vp, _i]),
     "qlpiv_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(_i)]),
 }
@@ -180,6 +181,17 @@ def adaptive_levels(desc, height, width):
     grids = (Grid * 16)()
     _check(lib.qlpiv_adaptive_levels(ctypes.byref(desc), height, width, ctypes.byref(n), grids, 16))
     return [{k: getattr(grids[i], k) for k, _ in Grid._fields_} for i in range(n.value)]
+
+
+NOALLOC_MAX_ROWS = 524288
+
+
+def inherit_noalloc(device, stream, p_ci, p_cj, pu, pv, c_ci, c_cj, cu, cv, pni, pnj, cni, cnj, round_int=False):
+    """qlpiv_inherit_noalloc: every array a device buffer (torch tensor or address);
+    queued on `stream` (cudaStream_t as int, 0 = legacy default stream)."""
+    a = [x if isinstance(x, int) else _addr(x) for x in (p_ci, p_cj, pu, pv, c_ci, c_cj, cu, cv)]
+    _check(load_library().qlpiv_inherit_noalloc(device, stream or None, pni, pnj, a[0], a[1], a[2], a[3], cni, cnj,
+                                                a[4], a[5], int(round_int), a[6], a[7]))
 
 
 def measure_fp32_peak(device=0):
