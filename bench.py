@@ -5,8 +5,11 @@ Workload ("adaptive-1024-u12"): 1024x1024 12-bit-in-uint16 synthetic particle pa
 (0.03 ppp, d = 2.5 px, shear 0.005 + Rankine vortex, max 6 px), adaptive PIV with
 IA 64 -> 32 -> 16 at 75 % overlap (61^2 + 125^2 + 253^2 = 83,355 vectors per pair):
 velocity inheritance, bicubic displacement field and BothImages bilinear warp between
-passes, FP32, 3-point Gaussian sub-pixel fit.  A step processes a batch of `pairs`
-pairs resident in HBM (inputs larger than L2) through the whole level loop.
+passes, FP32, 3-point Gaussian sub-pixel fit of every peak, FindMaximumMultiPeaks (3 peaks,
+3x3 cells) and the multi-peak normalised-median validation (threshold 2, epsilon0 0.1,
+secondary-peak then bilinear replacement, at most 2 correction sweeps) after every level.
+A step processes a batch of `pairs` pairs resident in HBM (inputs larger than L2)
+through the whole level loop.
 
   value      frame-pairs/s with inputs resident in HBM (CUDA events on the library's
              stream, max over ranks);
@@ -125,6 +128,15 @@ def make_pairs(pkg, unique):
 
 
 FULL_SCALE = 65535.0   # tiles copied from warped 16-bit images keep the full-scale max
+# VelocityValidationOptionsMultiPeakNormalizedMedianModel settings of the workload
+VALIDATION = dict(num_peaks=3, peak_kernel=3, threshold=2.0, epsilon0=0.1, max_iterations=2, iterate_until=False)
+
+
+def oracle_validation(orc):
+    v = VALIDATION
+    return orc.valid_cfg(num_peaks=v["num_peaks"], kernel_width=v["peak_kernel"], threshold=v["threshold"],
+                         epsilon0=v["epsilon0"], max_iterations=v["max_iterations"],
+                         iterate_until_no_corrections=v["iterate_until"])
 
 
 def cpu_baseline(pkg, pair, threads, reps=1):
@@ -136,14 +148,16 @@ def cpu_baseline(pkg, pair, threads, reps=1):
     for _ in range(reps):
         t0 = time.perf_counter()
         orc.piv_adaptive(a, b, LEVELS[0], LEVELS[-1], OVERLAP_FACTOR, norm_mode=orc.NORM_MAX_A, fixed_max=FULL_SCALE,
-                         precision=32, nthreads=threads)
+                         precision=32, nthreads=threads, validation=oracle_validation(orc))
         times.append(time.perf_counter() - t0)
     return min(times)
 
 
 WORKLOAD = ("adaptive-1024-u12: 1024x1024 12-bit pairs, IA 64 -> 32 -> 16 at 75 % overlap, BothImages bilinear "
             "warp between passes (velocity inheritance + bicubic displacement field), tile A max normalisation, "
-            "3-point Gaussian sub-pixel; vector validation not included")
+            "FindMaximumMultiPeaks (3 peaks, 3x3 cells) + 3-point Gaussian sub-pixel of every peak, multi-peak "
+            "normalised-median validation (threshold 2, eps0 0.1, secondary-peak then bilinear replacement, "
+            "<= 2 sweeps) after every level")
 
 
 def run_reference(args, rank):
@@ -186,7 +200,7 @@ def run_gpu(args, rank, world):
     bpp = 2
     desc = pkg.adaptive_desc(LEVELS[0], LEVELS[-1], OVERLAP_FACTOR, warp_mode=pkg.WARP_BOTH_BILINEAR,
                              norm_mode=pkg.NORM_MAX_A, max_mode=pkg.MAX_FIXED, fixed_max=FULL_SCALE,
-                             subpix_mode=pkg.SUBPIX_GAUSS3)
+                             subpix_mode=pkg.SUBPIX_GAUSS3, validation=VALIDATION)
     # device-resident frames: P slots filled from `unique` distinct synthetic pairs
     imgs = torch.empty((P, 2, H, W), dtype=torch.int16, device=dev)
     for k in range(P):

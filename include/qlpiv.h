@@ -70,6 +70,11 @@ typedef enum {
 #define QLPIV_F_PARABOLIC 4u /* a stencil value was negative: parabolic fallback */
 #define QLPIV_F_EDGE 8u      /* 3-point stencil leaves the plane: integer peak kept */
 #define QLPIV_F_NO_PEAK 16u  /* no non-negative cell: peak left at (0,0) */
+#define QLPIV_F_ABSENT 32u   /* multi-peak slot beyond the peaks found (vector zeroed) */
+
+/* FindMaximumMultiPeaks limits of this library: 1..QLPIV_MAX_PEAKS peaks per IA and a
+ * cell width of at least 2 (the per-cell maxima of one IA are staged on chip). */
+#define QLPIV_MAX_PEAKS 16
 
 /* One IA result (32 bytes): MaxCrossResult main peak after interpolation.
  * u/v are the displacement increments along rows/columns
@@ -93,7 +98,11 @@ typedef struct qlpiv_pass_desc {
     float fixed_max_a;  /* QLPIV_MAX_FIXED: max of every A tile */
     float fixed_max_b;  /* QLPIV_MAX_FIXED: max of every B tile */
     int subpix_mode;    /* qlpiv_subpix */
-    int reserved[6];
+    int num_peaks;      /* 0: FindMaximumFromCenter, one vector per IA.  k >= 1:
+                           FindMaximumMultiPeaks (S/maximum/FindMaximumMultiPeaks.java:42-162),
+                           k vectors per IA, largest peak first, every peak fitted */
+    int peak_kernel;    /* FindMaximumMultiPeaks cell width (kernelWidth), >= 2 */
+    int reserved[4];
 } qlpiv_pass_desc;
 
 /* One image pair of a batch.  Pixels are row-major with `pitch` elements per row; both
@@ -131,8 +140,25 @@ typedef struct qlpiv_adaptive_desc {
     int subpix_mode;       /* qlpiv_subpix */
     int int16_warp_quirk;  /* 1: store warped 16-bit pixels through a signed byte like
                               MatrixInt16.setElement(float) (S/MatrixInt16.java:95-101) */
-    int reserved[8];
+    int validation;        /* qlpiv_validation: vector validation after every level */
+    int num_peaks;         /* QLPIV_VALIDATE_MULTIPEAK_MEDIAN: peaks per IA = strategies */
+    int peak_kernel;       /* FindMaximumMultiPeaks cell width */
+    float median_threshold;   /* NormalizedMedianValidator distance threshold */
+    float median_epsilon0;    /* NormalizedMedianValidator epsilon0 */
+    int max_correction_iterations;      /* VectorValidatorConfiguration */
+    int iterate_until_no_corrections;   /* VectorValidatorConfiguration */
+    int reserved[1];
 } qlpiv_adaptive_desc;
+
+/* Vector validation after each level (VectorValidatorJob, S/jobs/validator/VectorValidatorJob.java:242-405). */
+typedef enum {
+    QLPIV_VALIDATE_NONE = 0,
+    /* VelocityValidationOptionsMultiPeakNormalizedMedianModel: FindMaximumMultiPeaks with
+     * num_peaks peaks, strategies 0..k-2 = normalised median + SecondaryPeakReplacement of
+     * peak s+1, strategy k-1 = normalised median + BilinearReplacement; still-invalid
+     * vectors are set to 0 (PIVConfigurationConverterVisitor.visit, multi-peak model). */
+    QLPIV_VALIDATE_MULTIPEAK_MEDIAN = 1
+} qlpiv_validation;
 
 typedef struct qlpiv_params {
     int device;         /* CUDA device ordinal */
@@ -169,6 +195,14 @@ qlpiv_status qlpiv_xcorr_planes(qlpiv_handle *h, int n, long count, int pixel_ty
 qlpiv_status qlpiv_xcorr_peaks(qlpiv_handle *h, int n, long count, int pixel_type, const void *tiles_a,
                                const void *tiles_b, const float *max_a, const float *max_b, int norm_mode,
                                int subpix_mode, qlpiv_vector *out);
+
+/* Fused xcorr + FindMaximumMultiPeaks.findMaximum (S/maximum/FindMaximumMultiPeaks.java:42-162,
+ * S/util/SimpleFixedLengthFloatLinkedList.java:98-237) + the sub-pixel fit of every peak:
+ * out receives count x num_peaks vectors, largest peak first; slots beyond the peaks
+ * found carry QLPIV_F_ABSENT.  min_floor is the minimum over the whole plane. */
+qlpiv_status qlpiv_xcorr_multipeaks(qlpiv_handle *h, int n, long count, int pixel_type, const void *tiles_a,
+                                    const void *tiles_b, const float *max_a, const float *max_b, int norm_mode,
+                                    int subpix_mode, int num_peaks, int peak_kernel, qlpiv_vector *out);
 
 /* One correlation pass over an image pair in host memory (height x width, row-major):
  * warp/clip (IImageWarpingStrategy.warpAndClipImage, S/images/NoImageWarpingStrategy.java:27-89,
@@ -247,9 +281,9 @@ qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, const void *img_a,
                              const float *v, int int16_quirk, void *out_a, void *out_b);
 
 /* Whole adaptive PIV of num_pairs image pairs of one size (LocalPIVOpenCLGpuJob's level
- * loop, S/jobs/LocalPIVOpenCLGpuJob.java:188-411, SimpleStrategy, no validation):
- * per level grid -> inheritance -> warp/clip -> xcorr + peak + sub-pixel -> accumulate,
- * all on the device.  frames[] are host images (pitch in elements); out_u/out_v receive
+ * loop, S/jobs/LocalPIVOpenCLGpuJob.java:188-411, SimpleStrategy): per level grid ->
+ * inheritance -> warp/clip -> xcorr + peak + sub-pixel -> accumulate -> validation
+ * (desc->validation), all on the device.  frames[] are host images (pitch in elements); out_u/out_v receive
  * num_pairs x (tiles_i x tiles_j) displacements of the last level (rows, columns). */
 qlpiv_status qlpiv_piv_adaptive(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int pixel_type, int height,
                                 int width, int num_pairs, const qlpiv_frame *frames, float *out_u, float *out_v);
@@ -259,6 +293,18 @@ qlpiv_status qlpiv_piv_adaptive(qlpiv_handle *h, const qlpiv_adaptive_desc *desc
 qlpiv_status qlpiv_piv_adaptive_device(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int pixel_type, int height,
                                        int width, int num_pairs, const qlpiv_frame *frames, float *out_u,
                                        float *out_v);
+
+/* VectorValidatorJob.compute (S/jobs/validator/VectorValidatorJob.java:242-405) for one
+ * frame's ni x nj tiles with the multi-peak normalised-median model: u/v (row-major,
+ * main peak already accumulated) are validated and replaced in place; peak_u/peak_v hold
+ * the k = desc->num_peaks displacement increments per tile (peak 0 = main), npeaks the
+ * peaks found per tile; tops/lefts the tile rows' top and columns' left pixels.
+ * invalid_out (may be NULL) receives the final invalid flags.  Host arrays; synchronous.
+ * Uses desc->num_peaks, median_threshold, median_epsilon0, max_correction_iterations,
+ * iterate_until_no_corrections. */
+qlpiv_status qlpiv_validate(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int ni, int nj, const int32_t *tops,
+                            const int32_t *lefts, float *u, float *v, const float *peak_u, const float *peak_v,
+                            const int32_t *npeaks, uint8_t *invalid_out);
 
 /* Velocity inheritance that allocates nothing (no counterpart in the reference).
  * For callers that cannot let the library allocate device memory during a call -- a

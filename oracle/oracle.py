@@ -29,10 +29,23 @@ NORM_MAX_A, NORM_OWN_MAX, NORM_FIXED, NORM_NONE = 0, 1, 2, 3
 _lib = None
 
 
+class ValidCfg(ctypes.Structure):
+    """orc_valid_cfg: multi-peak normalised-median validation settings."""
+    _fields_ = [("enabled", ctypes.c_int), ("num_peaks", ctypes.c_int), ("kernel_width", ctypes.c_int),
+                ("threshold", ctypes.c_float), ("epsilon0", ctypes.c_float), ("max_iterations", ctypes.c_int),
+                ("iterate_until_no_corrections", ctypes.c_int)]
+
+
+def valid_cfg(num_peaks=3, kernel_width=3, threshold=2.0, epsilon0=0.1, max_iterations=2,
+              iterate_until_no_corrections=False):
+    return ValidCfg(1, num_peaks, kernel_width, threshold, epsilon0, max_iterations,
+                    int(iterate_until_no_corrections))
+
+
 def build(force=False):
     """Compile the oracle with its Makefile (gcc only; seconds)."""
-    src = [HERE / "qlpiv_oracle.c", HERE / "qlpiv_oracle_adaptive.c", HERE / "oracle_impl.h", HERE / "oracle_interp_impl.h",
-           HERE / "Makefile"]
+    src = [HERE / "qlpiv_oracle.c", HERE / "qlpiv_oracle_adaptive.c", HERE / "qlpiv_oracle_validate.c",
+           HERE / "oracle_types.h", HERE / "oracle_impl.h", HERE / "oracle_interp_impl.h", HERE / "Makefile"]
     if not force and LIB_PATH.exists() and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in src):
         return LIB_PATH
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
@@ -67,6 +80,14 @@ def lib():
         L.orc_inherit.argtypes = [dp, c_int, dp, c_int, fp, fp, fp, c_int, fp, c_int, c_int, c_int, fp, fp]
         L.orc_piv_adaptive.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_float,
                                        c_int, c_int, c_int, fp, fp, ip, ip, vp]
+        L.orc_piv_pass_multi.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_long, ip, ip, ip, ip, c_int,
+                                         c_float, c_float, c_int, c_int, c_int, c_int, vp, ip, c_int]
+        L.orc_find_max_multipeaks_f32.argtypes = [fp, c_int, c_int, c_int, c_int, ip, ip, fp, fp]
+        L.orc_mp_list_run.argtypes = [c_int, c_int, c_int, fp, ip, ip, fp, ip, ip]
+        L.orc_spiral_order.argtypes = [c_int, c_int, ip]
+        L.orc_validate.argtypes = [c_int, c_int, ip, ip, fp, fp, fp, fp, ip, c_int, ctypes.POINTER(ValidCfg), vp]
+        L.orc_piv_adaptive_ex.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_float,
+                                          c_int, c_int, c_int, ctypes.POINTER(ValidCfg), fp, fp, ip, ip, vp, vp, vp]
         L.orc_vector_size.restype = c_int
         assert L.orc_vector_size() == VECTOR_DTYPE.itemsize
         _lib = L
@@ -240,9 +261,12 @@ def inherit(py, px, pu, pv, cy, cx, round_int=False, precision=32):
 
 
 def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MAX_A, fixed_max=None,
-                 int16_quirk=False, precision=32, nthreads=None, return_levels=False, warp=True):
+                 int16_quirk=False, precision=32, nthreads=None, return_levels=False, warp=True, validation=None):
     """Adaptive multi-pass PIV (BothImages bilinear warping, or none); returns (u, v) of
-    the last level, shaped (tiles_i, tiles_j), and optionally all levels' vectors."""
+    the last level, shaped (tiles_i, tiles_j), and optionally all levels' vectors.
+    validation: a ValidCfg (multi-peak finder + normalised-median validation per level);
+    with return_levels the result also carries every level's validated (u, v) and
+    invalid flags."""
     img_a, img_b = np.ascontiguousarray(img_a), np.ascontiguousarray(img_b)
     h, w = img_a.shape
     cap = 65536 * 16
@@ -257,13 +281,103 @@ def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MA
         n >>= 1
         lv += 1
     vec = np.zeros(total, VECTOR_DTYPE) if return_levels else None
-    rc = lib().orc_piv_adaptive(img_a.ctypes.data, img_b.ctypes.data, h, w, img_a.dtype.itemsize, n_start, n_end,
-                                overlap_factor, int(warp), norm_mode, float(fixed_max or 0.0), int(int16_quirk),
-                                0 if precision == 32 else 1, nthreads or (os.cpu_count() or 1),
-                                _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), ctypes.byref(ni), ctypes.byref(nj),
-                                vec.ctypes.data if vec is not None else None)
+    luv = np.zeros(2 * total, np.float32) if return_levels else None
+    linv = np.zeros(total, np.uint8) if return_levels else None
+    cfg = validation if validation is not None else ValidCfg(0, 0, 0, 0.0, 0.0, 0, 0)
+    rc = lib().orc_piv_adaptive_ex(img_a.ctypes.data, img_b.ctypes.data, h, w, img_a.dtype.itemsize, n_start, n_end,
+                                   overlap_factor, int(warp), norm_mode, float(fixed_max or 0.0), int(int16_quirk),
+                                   0 if precision == 32 else 1, nthreads or (os.cpu_count() or 1), ctypes.byref(cfg),
+                                   _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), ctypes.byref(ni),
+                                   ctypes.byref(nj), vec.ctypes.data if vec is not None else None,
+                                   luv.ctypes.data if luv is not None else None,
+                                   linv.ctypes.data if linv is not None else None)
     if rc != 0:
         raise ValueError("adaptive PIV failed")
     shape = (ni.value, nj.value)
     out = (u[:ni.value * nj.value].reshape(shape).copy(), v[:ni.value * nj.value].reshape(shape).copy())
-    return (out, vec) if return_levels else out
+    if not return_levels:
+        return out
+    if validation is None:
+        return out, vec
+    return out, vec, luv, linv
+
+
+def piv_pass_multi(img_a, img_b, n, a_top, a_left, b_top=None, b_left=None, norm_mode=NORM_MAX_A,
+                   fixed_max=(255.0, 255.0), subpix=True, precision=32, kernel_width=3, num_peaks=3, nthreads=None):
+    """One pass with FindMaximumMultiPeaks: vectors shaped (count, num_peaks), largest
+    peak first, and the number of peaks found per IA."""
+    img_a = np.ascontiguousarray(img_a)
+    img_b = np.ascontiguousarray(img_b)
+    assert img_a.dtype == img_b.dtype and img_a.dtype in (np.uint8, np.uint16)
+    a_top = np.ascontiguousarray(a_top, np.int32)
+    a_left = np.ascontiguousarray(a_left, np.int32)
+    b_top = a_top if b_top is None else np.ascontiguousarray(b_top, np.int32)
+    b_left = a_left if b_left is None else np.ascontiguousarray(b_left, np.int32)
+    count = a_top.shape[0]
+    out = np.zeros((count, num_peaks), VECTOR_DTYPE)
+    npk = np.zeros(count, np.int32)
+    rc = lib().orc_piv_pass_multi(img_a.ctypes.data, img_b.ctypes.data, img_a.shape[0], img_a.shape[1],
+                                  img_a.dtype.itemsize, n, count, _ptr(a_top, ctypes.c_int),
+                                  _ptr(a_left, ctypes.c_int), _ptr(b_top, ctypes.c_int), _ptr(b_left, ctypes.c_int),
+                                  norm_mode, fixed_max[0], fixed_max[1], int(subpix), 0 if precision == 32 else 1,
+                                  kernel_width, num_peaks, out.ctypes.data, _ptr(npk, ctypes.c_int),
+                                  nthreads or (os.cpu_count() or 1))
+    if rc != 0:
+        raise ValueError("bad multi-peak settings")
+    return out, npk
+
+
+def find_max_multipeaks(plane, kernel_width, num_peaks):
+    """FindMaximumMultiPeaks on one plane: [(i, j, value), ...] largest first, minFloor."""
+    p = _f32(plane)
+    oi = np.zeros(64, np.int32)
+    oj = np.zeros(64, np.int32)
+    ov = np.zeros(64, np.float32)
+    mf = np.zeros(1, np.float32)
+    n = lib().orc_find_max_multipeaks_f32(_ptr(p, ctypes.c_float), p.shape[0], p.shape[1], kernel_width, num_peaks,
+                                          _ptr(oi, ctypes.c_int), _ptr(oj, ctypes.c_int), _ptr(ov, ctypes.c_float),
+                                          _ptr(mf, ctypes.c_float))
+    if n < 0:
+        raise ValueError("bad multi-peak settings")
+    return [(int(oi[r]), int(oj[r]), float(ov[r])) for r in range(n)], float(mf[0])
+
+
+def mp_list_run(max_size, kernel_width, entries):
+    """SimpleFixedLengthFloatLinkedList: addInAscendOrder of every (value, i, j); returns the
+    list in ascending order."""
+    v = _f32([e[0] for e in entries])
+    i = np.ascontiguousarray([e[1] for e in entries], np.int32)
+    j = np.ascontiguousarray([e[2] for e in entries], np.int32)
+    ov = np.zeros(65, np.float32)
+    oi = np.zeros(65, np.int32)
+    oj = np.zeros(65, np.int32)
+    n = lib().orc_mp_list_run(max_size, kernel_width, len(entries), _ptr(v, ctypes.c_float), _ptr(i, ctypes.c_int),
+                              _ptr(j, ctypes.c_int), _ptr(ov, ctypes.c_float), _ptr(oi, ctypes.c_int),
+                              _ptr(oj, ctypes.c_int))
+    return [(float(ov[r]), int(oi[r]), int(oj[r])) for r in range(n)]
+
+
+def spiral_order(ni, nj):
+    """VectorValidatorJob.circularVisitor visit order (flat tile indices)."""
+    order = np.zeros(ni * nj, np.int32)
+    n = lib().orc_spiral_order(ni, nj, _ptr(order, ctypes.c_int))
+    return order[:n]
+
+
+def validate(tops, lefts, u, v, peak_u, peak_v, npeaks, cfg):
+    """Multi-peak normalised-median validation of one frame's tiles.  u, v: (ni, nj)
+    accumulated displacements (main peak included); peak_u/peak_v: (ni, nj, k) peak
+    increments; npeaks: (ni, nj).  Returns validated (u, v), invalid flags, sweeps."""
+    u = _f32(u).copy()
+    v = _f32(v).copy()
+    ni, nj = u.shape
+    k = peak_u.shape[-1]
+    tops = np.ascontiguousarray(tops, np.int32)
+    lefts = np.ascontiguousarray(lefts, np.int32)
+    pu, pv = _f32(peak_u), _f32(peak_v)
+    npk = np.ascontiguousarray(npeaks, np.int32)
+    inv = np.zeros((ni, nj), np.uint8)
+    sweeps = lib().orc_validate(ni, nj, _ptr(tops, ctypes.c_int), _ptr(lefts, ctypes.c_int), _ptr(u, ctypes.c_float),
+                                _ptr(v, ctypes.c_float), _ptr(pu, ctypes.c_float), _ptr(pv, ctypes.c_float),
+                                _ptr(npk, ctypes.c_int), k, ctypes.byref(cfg), inv.ctypes.data)
+    return u, v, inv, sweeps

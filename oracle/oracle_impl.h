@@ -306,6 +306,143 @@ static void FN(ia_vector)(const float *ta, const float *tb, int n, float maxA, f
     out->v64 = (double)(pj - half);
 }
 
+
+/* FindMaximumMultiPeaks.findMaximum (S/maximum/FindMaximumMultiPeaks.java:42-162) with the
+ * sorted, adjacency-suppressing list of SimpleFixedLengthFloatLinkedList.addInAscendOrder
+ * (S/util/SimpleFixedLengthFloatLinkedList.java).  The plane is cut into kw x kw cells in four
+ * interleaved quadrant groups; each cell's maximum (strict >, starting from 0, position kept
+ * from the previous slice when nothing beats 0) is inserted in slice order.  The list holds
+ * at most k entries in ascending order; an insertion deletes smaller entries within squared
+ * distance (kw-1)*kw and is refused next to an equal or larger one.  Output peaks are sorted
+ * largest first.  Returns the number of peaks; *ominf = minimum over every visited cell. */
+typedef struct { REAL v; int i, j; } FN(mp_entry);
+
+static int FN(mp_adjacent)(const FN(mp_entry) *e, int i, int j, float kd) {
+    const float d = (float)((double)(i - e->i) * (double)(i - e->i) + (double)(j - e->j) * (double)(j - e->j));
+    return d < kd;
+}
+
+static void FN(mp_add)(FN(mp_entry) *lst, int *size, int maxsize, float kd, REAL v, int i, int j) {
+    if (*size == 0) {
+        lst[0].v = v; lst[0].i = i; lst[0].j = j;
+        *size = 1;
+        return;
+    }
+    int del[64], ndel = 0;
+    int pos = 0;
+    while (pos < *size && lst[pos].v < v) {
+        if (FN(mp_adjacent)(&lst[pos], i, j, kd) && v > lst[pos].v) del[ndel++] = pos;
+        pos++;
+    }
+    if (*size == maxsize && pos == 0) return;
+    for (int q = pos; q < *size; q++)
+        if (FN(mp_adjacent)(&lst[q], i, j, kd) && v <= lst[q].v) return;
+    /* perform the scheduled deletions (all before pos) */
+    if (ndel > 0) {
+        int w = 0, d = 0;
+        for (int r = 0; r < *size; r++) {
+            if (d < ndel && del[d] == r) { d++; continue; }
+            lst[w++] = lst[r];
+        }
+        *size -= ndel;
+        pos -= ndel;
+    }
+    if (pos > 0) {  /* insert after the last smaller survivor */
+        for (int r = *size; r > pos; r--) lst[r] = lst[r - 1];
+        lst[pos].v = v; lst[pos].i = i; lst[pos].j = j;
+        (*size)++;
+        if (*size > maxsize) {  /* drop the smallest */
+            for (int r = 0; r < *size - 1; r++) lst[r] = lst[r + 1];
+            (*size)--;
+        }
+    } else {
+        if (*size == maxsize) return;
+        for (int r = *size; r > 0; r--) lst[r] = lst[r - 1];
+        lst[0].v = v; lst[0].i = i; lst[0].j = j;
+        (*size)++;
+    }
+}
+
+static int FN(find_max_multipeaks)(const REAL *p, int di, int dj, int kw, int k, int *oi, int *oj, REAL *ov,
+                                   REAL *ominf) {
+    int iS = di / kw; if (iS * kw != di) iS += 1;
+    const int iBottom = iS / 2, iTop = iS - iBottom;
+    int jS = dj / kw; if (jS * kw != dj) jS += 1;
+    const int jRight = jS / 2, jLeft = jS - jRight;
+    const float kd = (float)((kw - 1) * kw);
+    FN(mp_entry) lst[65];
+    int size = 0;
+    REAL maxs[4];
+    int mi[4] = {0, 0, 0, 0}, mj[4] = {0, 0, 0, 0};
+    REAL minv = (REAL)FLT_MAX;
+#define P(a, b) p[(size_t)(a) * dj + (b)]
+    for (int sI = 0; sI < iTop; sI++) {
+        for (int sJ = 0; sJ < jLeft; sJ++) {
+            const int top = sI * kw, left = sJ * kw, bottom = sI * kw + iTop * kw, right = sJ * kw + jLeft * kw;
+            for (int q = 0; q < 4; q++) maxs[q] = (REAL)0;
+            for (int a = 0; a < kw; a++) {
+                for (int b = 0; b < kw; b++) {
+                    const int i1 = top + a, j1 = left + b;
+                    { const REAL v = P(i1, j1);
+                      if (v > maxs[0]) { maxs[0] = v; mi[0] = i1; mj[0] = j1; }
+                      if (v < minv) minv = v; }
+                    const int j2 = right + b;
+                    if (j2 < dj) { const REAL v = P(i1, j2);
+                      if (v > maxs[1]) { maxs[1] = v; mi[1] = i1; mj[1] = j2; }
+                      if (v < minv) minv = v; }
+                    const int i3 = bottom + a;
+                    if (i3 < di) { const REAL v = P(i3, j1);
+                      if (v > maxs[2]) { maxs[2] = v; mi[2] = i3; mj[2] = j1; }
+                      if (v < minv) minv = v; }
+                    if (i3 < di && j2 < dj) { const REAL v = P(i3, j2);
+                      if (v > maxs[3]) { maxs[3] = v; mi[3] = i3; mj[3] = j2; }
+                      if (v < minv) minv = v; }
+                }
+            }
+            for (int q = 0; q < 4; q++) FN(mp_add)(lst, &size, k, kd, maxs[q], mi[q], mj[q]);
+        }
+    }
+#undef P
+    for (int r = 0; r < size; r++) {  /* largest first */
+        oi[r] = lst[size - 1 - r].i;
+        oj[r] = lst[size - 1 - r].j;
+        ov[r] = lst[size - 1 - r].v;
+    }
+    *ominf = minv;
+    return size;
+}
+
+/* One IA through the CPU path with FindMaximumMultiPeaks: up to k vectors, peak 0 the
+ * largest, each with the Gaussian 1D-1D sub-pixel fit (the interpolator visits every
+ * peak, Gaussian1DPolynomialInterpolator.java:25-106). */
+static int FN(ia_vectors_multi)(const float *ta, const float *tb, int n, float maxA, float maxB, int normalize,
+                                int subpix, int kw, int k, orc_vector *out, REAL *plane_scratch) {
+    const int d = 2 * n - 1;
+    FN(xcorr_fft)(ta, tb, n, maxA, maxB, normalize, plane_scratch);
+    int pi[64], pj[64];
+    REAL pv[64], minf;
+    const int np = FN(find_max_multipeaks)(plane_scratch, d, d, kw, k, pi, pj, pv, &minf);
+    for (int r = 0; r < np; r++) {
+        REAL si = (REAL)pi[r], sj = (REAL)pj[r];
+        uint32_t flags = 0;
+        if (subpix) FN(subpixel_gauss3)(plane_scratch, d, d, pi[r], pj[r], &si, &sj, &flags);
+        const REAL half = (REAL)(d / 2);
+        orc_vector *o = &out[r];
+        o->u = (float)(si - half);
+        o->v = (float)(sj - half);
+        o->sub_i = (float)si;
+        o->sub_j = (float)sj;
+        o->peak_value = (float)pv[r];
+        o->min_floor = (float)minf;
+        o->peak_i = (int16_t)pi[r];
+        o->peak_j = (int16_t)pj[r];
+        o->flags = flags;
+        o->u64 = (double)(si - half);
+        o->v64 = (double)(sj - half);
+    }
+    return np;
+}
+
 #undef FN
 #undef CAT
 #undef CAT_

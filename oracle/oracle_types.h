@@ -1,0 +1,48 @@
+/*
+ * Types and cross-file prototypes of the qlpiv CPU oracle -- TEST INFRASTRUCTURE ONLY.
+ */
+#ifndef QLPIV_ORACLE_TYPES_H
+#define QLPIV_ORACLE_TYPES_H
+
+#include <stdint.h>
+
+typedef struct {
+    float u, v;
+    float sub_i, sub_j;
+    float peak_value, min_floor;
+    int16_t peak_i, peak_j;
+    uint32_t flags;
+    double u64, v64;
+} orc_vector; /* 48 bytes */
+
+typedef struct {
+    int n, tiles_i, tiles_j, margin_top, margin_left, margin_bottom, margin_right;
+} orc_grid;
+
+/* Multi-peak normalised-median validation (VelocityValidationOptionsMultiPeakNormalizedMedianModel):
+ * num_peaks k >= 1 validation strategies; strategy s < k-1 replaces by peak s+1, the last
+ * one by bilinear interpolation.  enabled == 0: no validation, FindMaximumFromCenter. */
+typedef struct {
+    int enabled;
+    int num_peaks;        /* k: peaks searched per IA and validation strategies */
+    int kernel_width;     /* FindMaximumMultiPeaks cell width */
+    float threshold;      /* normalised-median distance threshold */
+    float epsilon0;
+    int max_iterations;
+    int iterate_until_no_corrections;
+} orc_valid_cfg;
+
+int orc_grid_superposition(int h, int w, int mtop, int mbottom, int mleft, int mright, int n_start, int level,
+                           float overlap_factor, orc_grid *g, int *tops, int *lefts, int cap);
+int orc_piv_pass(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,
+                 const int *a_top, const int *a_left, const int *b_top, const int *b_left, int norm_mode,
+                 float fixed_max_a, float fixed_max_b, int subpix, int precision, orc_vector *out, int nthreads);
+int orc_piv_pass_multi(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,
+                       const int *a_top, const int *a_left, const int *b_top, const int *b_left, int norm_mode,
+                       float fixed_max_a, float fixed_max_b, int subpix, int precision, int kw, int k,
+                       orc_vector *out, int *npeaks, int nthreads);
+int orc_spiral_order(int ni, int nj, int *order);
+int orc_validate(int ni, int nj, const int *tops, const int *lefts, float *u, float *v, const float *pu,
+                 const float *pv, const int *npeaks, int k, const orc_valid_cfg *cfg, unsigned char *invalid_out);
+
+#endif

@@ -38,14 +38,7 @@
 #define ORC_F_EDGE 8u
 #define ORC_F_NO_PEAK 16u
 
-typedef struct {
-    float u, v;
-    float sub_i, sub_j;
-    float peak_value, min_floor;
-    int16_t peak_i, peak_j;
-    uint32_t flags;
-    double u64, v64;
-} orc_vector; /* 48 bytes */
+#include "oracle_types.h"
 
 /* perfectShuffleFFTInput (S/jobs/xcorr/SimpleFFT.java:32-69) produces the
  * bit-reversal permutation; tests/test_oracle_golden.py restates the swap loop and
@@ -161,12 +154,7 @@ static int java_round_f(float x) { return (int)floorf(x + 0.5f); }
 /* ---------------------------------------------------------------------------
  * IA grids
  * ------------------------------------------------------------------------- */
-typedef struct {
-    int n;             /* IA side */
-    int tiles_i, tiles_j;
-    int margin_top, margin_left, margin_bottom, margin_right;
-} orc_grid;
-
+/* orc_grid (oracle_types.h): IA side, tiles per axis, margins */
 /* AdaptiveInterAreaStrategySuperPosition (S/iareas/AdaptiveInterAreaStrategySuperPosition.java:31-197).
  * level 0: tile origin = margin + round(k * f * N); levels > 0: origins accumulate the
  * float increment (:107-116).  Margins of level L are computed from that level's
@@ -240,6 +228,8 @@ typedef struct {
     const int *a_top, *a_left, *b_top, *b_left;
     orc_vector *out;
     long begin, end;
+    int kw, k;        /* k > 0: FindMaximumMultiPeaks with kw x kw cells, k peaks per IA */
+    int *npeaks;      /* multi-peak mode: peaks found per IA; out holds k vectors per IA */
 } orc_job;
 
 static void *orc_worker(void *arg) {
@@ -258,10 +248,17 @@ static void *orc_worker(void *arg) {
             case 2: maxA = j->fixed_max_a; maxB = j->fixed_max_b; break;
             default: normalize = 0; break;
         }
-        if (j->precision == 0)
+        if (j->k > 0) {
+            orc_vector *o = &j->out[k * j->k];
+            memset(o, 0, sizeof(orc_vector) * j->k);
+            j->npeaks[k] = j->precision == 0
+                ? ia_vectors_multi_f32(ta, tb, n, maxA, maxB, normalize, j->subpix, j->kw, j->k, o, (float *)plane)
+                : ia_vectors_multi_f64(ta, tb, n, maxA, maxB, normalize, j->subpix, j->kw, j->k, o, (double *)plane);
+        } else if (j->precision == 0) {
             ia_vector_f32(ta, tb, n, maxA, maxB, normalize, j->subpix, &j->out[k], (float *)plane);
-        else
+        } else {
             ia_vector_f64(ta, tb, n, maxA, maxB, normalize, j->subpix, &j->out[k], (double *)plane);
+        }
     }
     free(ta);
     free(tb);
@@ -269,9 +266,10 @@ static void *orc_worker(void *arg) {
     return NULL;
 }
 
-int orc_piv_pass(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,
-                 const int *a_top, const int *a_left, const int *b_top, const int *b_left, int norm_mode,
-                 float fixed_max_a, float fixed_max_b, int subpix, int precision, orc_vector *out, int nthreads) {
+static int run_pass(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,
+                    const int *a_top, const int *a_left, const int *b_top, const int *b_left, int norm_mode,
+                    float fixed_max_a, float fixed_max_b, int subpix, int precision, orc_vector *out, int nthreads,
+                    int kw, int k, int *npeaks) {
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 256) nthreads = 256;
     if ((long)nthreads > count) nthreads = count > 0 ? (int)count : 1;
@@ -285,11 +283,52 @@ int orc_piv_pass(const void *img_a, const void *img_b, int h, int w, int pix_byt
         j->a_top = a_top; j->a_left = a_left; j->b_top = b_top; j->b_left = b_left; j->out = out;
         j->begin = count * t / nthreads;
         j->end = count * (t + 1) / nthreads;
+        j->kw = kw;
+        j->k = k;
+        j->npeaks = npeaks;
     }
     for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, orc_worker, &jobs[t]);
     orc_worker(&jobs[0]);
     for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
     return 0;
+}
+
+int orc_piv_pass(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,
+                 const int *a_top, const int *a_left, const int *b_top, const int *b_left, int norm_mode,
+                 float fixed_max_a, float fixed_max_b, int subpix, int precision, orc_vector *out, int nthreads) {
+    return run_pass(img_a, img_b, h, w, pix_bytes, n, count, a_top, a_left, b_top, b_left, norm_mode, fixed_max_a,
+                    fixed_max_b, subpix, precision, out, nthreads, 0, 0, NULL);
+}
+
+/* The same pass with FindMaximumMultiPeaks (kw x kw cells, k <= 64 peaks): out holds k
+ * vectors per IA, largest peak first, npeaks[k] the number found. */
+int orc_piv_pass_multi(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,
+                       const int *a_top, const int *a_left, const int *b_top, const int *b_left, int norm_mode,
+                       float fixed_max_a, float fixed_max_b, int subpix, int precision, int kw, int k,
+                       orc_vector *out, int *npeaks, int nthreads) {
+    if (k < 1 || k > 64 || kw < 1) return -1;
+    return run_pass(img_a, img_b, h, w, pix_bytes, n, count, a_top, a_left, b_top, b_left, norm_mode, fixed_max_a,
+                    fixed_max_b, subpix, precision, out, nthreads, kw, k, npeaks);
+}
+
+/* FindMaximumMultiPeaks on one plane (d_i x d_j, row-major). */
+int orc_find_max_multipeaks_f32(const float *p, int di, int dj, int kw, int k, int *oi, int *oj, float *ov,
+                                float *ominf) {
+    if (k < 1 || k > 64 || kw < 1) return -1;
+    return find_max_multipeaks_f32(p, di, dj, kw, k, oi, oj, ov, ominf);
+}
+
+/* SimpleFixedLengthFloatLinkedList(max_size, kernel_width): a sequence of
+ * addInAscendOrder calls; the list is returned in ascending order. */
+int orc_mp_list_run(int max_size, int kernel_width, int count, const float *v, const int *i, const int *j,
+                    float *ov, int *oi, int *oj) {
+    if (max_size < 1 || max_size > 64) return -1;
+    mp_entry_f32 lst[65];
+    int size = 0;
+    const float kd = (float)((kernel_width - 1) * kernel_width);
+    for (int q = 0; q < count; q++) mp_add_f32(lst, &size, max_size, kd, v[q], i[q], j[q]);
+    for (int r = 0; r < size; r++) { ov[r] = lst[r].v; oi[r] = lst[r].i; oj[r] = lst[r].j; }
+    return size;
 }
 
 int orc_vector_size(void) { return (int)sizeof(orc_vector); }

@@ -24,7 +24,8 @@
  *  A-accum   Tile.accumulateDisplacement (S/iareas/Tile.java:103-136), clipping mode
  *            AllowedOutOfBoundClipping (the UI converter's default).
  *  A-loop    LocalPIVOpenCLGpuJob (S/jobs/LocalPIVOpenCLGpuJob.java:188-411) with
- *            SimpleStrategy (one correlation per level), no validation.
+ *            SimpleStrategy (one correlation per level); optionally the multi-peak
+ *            normalised-median validation after every level (qlpiv_oracle_validate.c).
  *
  * The reference evaluates both interpolators in double.  The FP32 pipeline here
  * evaluates them in float (spline knot derivatives still solved in double), the
@@ -38,24 +39,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-typedef struct {
-    float u, v;
-    float sub_i, sub_j;
-    float peak_value, min_floor;
-    int16_t peak_i, peak_j;
-    uint32_t flags;
-    double u64, v64;
-} orc_vector;
-
-/* from qlpiv_oracle.c */
-typedef struct {
-    int n, tiles_i, tiles_j, margin_top, margin_left, margin_bottom, margin_right;
-} orc_grid;
-int orc_grid_superposition(int h, int w, int mtop, int mbottom, int mleft, int mright, int n_start, int level,
-                           float overlap_factor, orc_grid *g, int *tops, int *lefts, int cap);
-int orc_piv_pass(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,
-                 const int *a_top, const int *a_left, const int *b_top, const int *b_left, int norm_mode,
-                 float fixed_max_a, float fixed_max_b, int subpix, int precision, orc_vector *out, int nthreads);
+#include "oracle_types.h"
 
 /* ---------------- natural cubic spline: first derivative at every knot ---------------- */
 static void natural_spline_deriv(const double *x, const double *y, long ys, int n, double *d) {
@@ -266,9 +250,13 @@ void orc_inherit(const double *py, int pni, const double *px, int pnj, const flo
  * fixed_max when > 0 (full-image-warp tiles: 255 / 65535), else the tile max.
  * Outputs the last level's displacement (u rows, v columns) and, optionally, every
  * level's vectors concatenated (level_vectors, sized by the caller). */
-int orc_piv_adaptive(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n_start, int n_end,
-                     float overlap_factor, int warp_mode, int norm_mode, float fixed_max, int int16_quirk, int precision,
-                     int nthreads, float *out_u, float *out_v, int *out_ni, int *out_nj, orc_vector *level_vectors) {
+int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n_start, int n_end,
+                        float overlap_factor, int warp_mode, int norm_mode, float fixed_max, int int16_quirk,
+                        int precision, int nthreads, const orc_valid_cfg *val, float *out_u, float *out_v, int *out_ni,
+                        int *out_nj, orc_vector *level_vectors, float *level_uv, unsigned char *level_invalid) {
+    const int validate = val != NULL && val->enabled;
+    const int kpk = validate ? val->num_peaks : 0;
+    if (validate && (kpk < 1 || kpk > 64 || val->kernel_width < 1)) return -2;
     int levels = 0;
     for (int n = n_start; n >= n_end; n >>= 1) levels++;
     const int cap = 65536;
@@ -318,16 +306,44 @@ int orc_piv_adaptive(const void *img_a, const void *img_b, int h, int w, int pix
                 bt[k] = warp_mode == 0 ? java_round((float)tops[i] + cu[k]) : tops[i];
                 bl[k] = warp_mode == 0 ? java_round((float)lefts[j] + cv[k]) : lefts[j];
             }
-        orc_vector *vec = (orc_vector *)malloc(sizeof(orc_vector) * cnt);
         const float fm = fixed_max > 0.0f ? fixed_max : 0.0f;
-        orc_piv_pass(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, fixed_max > 0.0f ? 2 : norm_mode, fm, fm, 1,
-                     precision, vec, nthreads);
+        const int nm = fixed_max > 0.0f ? 2 : norm_mode;
+        orc_vector *vec = (orc_vector *)malloc(sizeof(orc_vector) * cnt);
+        orc_vector *mvec = NULL;
+        int *npk = NULL;
+        if (validate) {
+            /* FindMaximumMultiPeaks (the finder the multi-peak validation model selects) */
+            mvec = (orc_vector *)malloc(sizeof(orc_vector) * cnt * kpk);
+            npk = (int *)malloc(sizeof(int) * cnt);
+            orc_piv_pass_multi(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, nm, fm, fm, 1, precision,
+                               val->kernel_width, kpk, mvec, npk, nthreads);
+            for (long k = 0; k < cnt; k++) vec[k] = mvec[k * kpk];
+        } else {
+            orc_piv_pass(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, nm, fm, fm, 1, precision, vec, nthreads);
+        }
         if (level_vectors) memcpy(level_vectors + vec_off, vec, sizeof(orc_vector) * cnt);
-        vec_off += cnt;
         for (long k = 0; k < cnt; k++) {
             if (precision == 0) { cu[k] += vec[k].u; cv[k] += vec[k].v; }
             else { cu[k] = (float)((double)cu[k] + vec[k].u64); cv[k] = (float)((double)cv[k] + vec[k].v64); }
         }
+        if (validate) {
+            /* VectorValidatorJob after IterationStepTiles.updateDisplacementsFromMaxCrossResults
+             * (S/jobs/LocalPIVOpenCLGpuJob.java:384-402) */
+            float *pku = (float *)malloc(sizeof(float) * cnt * kpk), *pkv = (float *)malloc(sizeof(float) * cnt * kpk);
+            for (long q = 0; q < cnt * kpk; q++) {
+                pku[q] = precision == 0 ? mvec[q].u : (float)mvec[q].u64;
+                pkv[q] = precision == 0 ? mvec[q].v : (float)mvec[q].v64;
+            }
+            orc_validate(ni, nj, tops, lefts, cu, cv, pku, pkv, npk, kpk, val,
+                         level_invalid ? level_invalid + vec_off : NULL);
+            free(pku); free(pkv);
+        }
+        if (level_uv) {
+            memcpy(level_uv + 2 * vec_off, cu, sizeof(float) * cnt);
+            memcpy(level_uv + 2 * vec_off + cnt, cv, sizeof(float) * cnt);
+        }
+        vec_off += cnt;
+        free(mvec); free(npk);
         free(at); free(al); free(bt); free(bl); free(vec); free(cyd); free(cxd); free(cyf); free(cxf);
         free(pu); free(pv);
         pu = cu; pv = cv;
@@ -343,4 +359,12 @@ int orc_piv_adaptive(const void *img_a, const void *img_b, int h, int w, int pix
     }
     free(pu); free(pv); free(tops); free(lefts); free(ptops); free(plefts); free(wa); free(wb); free(fu); free(fv);
     return rc;
+}
+
+int orc_piv_adaptive(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n_start, int n_end,
+                     float overlap_factor, int warp_mode, int norm_mode, float fixed_max, int int16_quirk, int precision,
+                     int nthreads, float *out_u, float *out_v, int *out_ni, int *out_nj, orc_vector *level_vectors) {
+    return orc_piv_adaptive_ex(img_a, img_b, h, w, pix_bytes, n_start, n_end, overlap_factor, warp_mode, norm_mode,
+                               fixed_max, int16_quirk, precision, nthreads, NULL, out_u, out_v, out_ni, out_nj,
+                               level_vectors, NULL, NULL);
 }

@@ -21,7 +21,9 @@ PIX_U8, PIX_U16, PIX_F32 = 0, 1, 2
 NORM_MAX_A, NORM_OWN_MAX, NORM_NONE = 0, 1, 3
 MAX_COMPUTE, MAX_GIVEN, MAX_FIXED = 0, 1, 2
 SUBPIX_NONE, SUBPIX_GAUSS3 = 0, 1
-F_SUB_I, F_SUB_J, F_PARABOLIC, F_EDGE, F_NO_PEAK = 1, 2, 4, 8, 16
+F_SUB_I, F_SUB_J, F_PARABOLIC, F_EDGE, F_NO_PEAK, F_ABSENT = 1, 2, 4, 8, 16, 32
+MAX_PEAKS = 16
+VALIDATE_NONE, VALIDATE_MULTIPEAK_MEDIAN = 0, 1
 
 VECTOR_DTYPE = np.dtype([
     ("u", "<f4"), ("v", "<f4"), ("sub_i", "<f4"), ("sub_j", "<f4"),
@@ -45,7 +47,7 @@ class QlpivError(RuntimeError):
 class PassDesc(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int), ("norm_mode", ctypes.c_int), ("max_mode", ctypes.c_int),
                 ("fixed_max_a", ctypes.c_float), ("fixed_max_b", ctypes.c_float), ("subpix_mode", ctypes.c_int),
-                ("reserved", ctypes.c_int * 6)]
+                ("num_peaks", ctypes.c_int), ("peak_kernel", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 class Frame(ctypes.Structure):
@@ -69,19 +71,44 @@ class AdaptiveDesc(ctypes.Structure):
     _fields_ = [("ia_start", ctypes.c_int), ("ia_end", ctypes.c_int), ("overlap_factor", ctypes.c_float),
                 ("margins", ctypes.c_int * 4), ("warp_mode", ctypes.c_int), ("norm_mode", ctypes.c_int),
                 ("max_mode", ctypes.c_int), ("fixed_max", ctypes.c_float), ("subpix_mode", ctypes.c_int),
-                ("int16_warp_quirk", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+                ("int16_warp_quirk", ctypes.c_int), ("validation", ctypes.c_int), ("num_peaks", ctypes.c_int),
+                ("peak_kernel", ctypes.c_int), ("median_threshold", ctypes.c_float),
+                ("median_epsilon0", ctypes.c_float), ("max_correction_iterations", ctypes.c_int),
+                ("iterate_until_no_corrections", ctypes.c_int), ("reserved", ctypes.c_int * 1)]
 
 
 def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_mode=WARP_BOTH_BILINEAR,
                   norm_mode=NORM_MAX_A, max_mode=MAX_FIXED, fixed_max=0.0, subpix_mode=SUBPIX_GAUSS3,
-                  int16_warp_quirk=False):
+                  int16_warp_quirk=False, validation=None):
     """Adaptive PIV parameters; the defaults follow the reference's BothImages bilinear
-    warping (tiles copied from the warped image keep the full-scale maximum)."""
+    warping (tiles copied from the warped image keep the full-scale maximum).
+    validation: None, or a dict for the multi-peak normalised-median model with keys
+    num_peaks, peak_kernel, threshold, epsilon0, max_iterations, iterate_until (see
+    multipeak_validation())."""
     d = AdaptiveDesc()
     d.ia_start, d.ia_end, d.overlap_factor = ia_start, ia_end, overlap_factor
     d.margins[:] = list(margins)
     d.warp_mode, d.norm_mode, d.max_mode, d.fixed_max = warp_mode, norm_mode, max_mode, fixed_max
     d.subpix_mode, d.int16_warp_quirk = subpix_mode, int(int16_warp_quirk)
+    if validation is not None:
+        set_validation(d, **validation)
+    return d
+
+
+def multipeak_validation(num_peaks=3, peak_kernel=3, threshold=2.0, epsilon0=0.1, max_iterations=2,
+                         iterate_until=False):
+    """Settings of VelocityValidationOptionsMultiPeakNormalizedMedianModel plus the
+    validator job's iteration settings."""
+    return dict(num_peaks=num_peaks, peak_kernel=peak_kernel, threshold=threshold, epsilon0=epsilon0,
+                max_iterations=max_iterations, iterate_until=iterate_until)
+
+
+def set_validation(d, num_peaks=3, peak_kernel=3, threshold=2.0, epsilon0=0.1, max_iterations=2,
+                   iterate_until=False):
+    d.validation = VALIDATE_MULTIPEAK_MEDIAN
+    d.num_peaks, d.peak_kernel = num_peaks, peak_kernel
+    d.median_threshold, d.median_epsilon0 = threshold, epsilon0
+    d.max_correction_iterations, d.iterate_until_no_corrections = max_iterations, int(iterate_until)
     return d
 
 
@@ -105,6 +132,8 @@ _SIGNATURES = {
     "qlpiv_launch_count": (_l, [_vp]),
     "qlpiv_xcorr_planes": (_i, [_vp, _i, _l, _i, _vp, _vp, _vp, _vp, _i, _vp]),
     "qlpiv_xcorr_peaks": (_i, [_vp, _i, _l, _i, _vp, _vp, _vp, _vp, _i, _i, _vp]),
+    "qlpiv_xcorr_multipeaks": (_i, [_vp, _i, _l, _i, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "qlpiv_validate": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "qlpiv_pass": (_i, [_vp, ctypes.POINTER(PassDesc), _vp, _vp, _i, _i, _i, _l, _vp, _vp, _vp, _vp, _vp]),
     "qlpiv_pass_device": (_i, [_vp, ctypes.POINTER(PassDesc), _vp, _vp, _i, _i, _i, _l, _vp, _vp, _vp, _vp, _vp]),
     "qlpiv_pass_batch": (_i, [_vp, ctypes.POINTER(PassDesc), _i, _i, _vp, _l, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -317,14 +346,35 @@ class Handle:
                                            _addr(ma), _addr(mb), norm_mode, subpix_mode, _addr(out)))
         return out
 
+    def xcorr_multipeaks(self, tiles_a, tiles_b, max_a=None, max_b=None, norm_mode=NORM_MAX_A,
+                         subpix_mode=SUBPIX_GAUSS3, num_peaks=3, peak_kernel=3):
+        """FindMaximumMultiPeaks on every tile pair: vectors shaped (count, num_peaks),
+        largest peak first (absent slots flagged F_ABSENT)."""
+        ta, tb = self._tiles(tiles_a, tiles_b)
+        count, n = ta.shape[0], ta.shape[1]
+        ma, mb = self._maxes(max_a, max_b, count)
+        out = np.empty((count, num_peaks), VECTOR_DTYPE)
+        _check(self._lib.qlpiv_xcorr_multipeaks(self._h, n, count, pixel_type_of(ta.dtype), _addr(ta), _addr(tb),
+                                                _addr(ma), _addr(mb), norm_mode, subpix_mode, num_peaks, peak_kernel,
+                                                _addr(out)))
+        return out
+
     # -- frame API ---------------------------------------------------------------
     @staticmethod
-    def desc(n, norm_mode=NORM_MAX_A, max_mode=MAX_COMPUTE, fixed_max=(255.0, 255.0), subpix_mode=SUBPIX_GAUSS3):
+    def desc(n, norm_mode=NORM_MAX_A, max_mode=MAX_COMPUTE, fixed_max=(255.0, 255.0), subpix_mode=SUBPIX_GAUSS3,
+             num_peaks=0, peak_kernel=3):
+        """Pass descriptor; num_peaks > 0 selects FindMaximumMultiPeaks (num_peaks vectors
+        per IA)."""
         d = PassDesc()
         d.n, d.norm_mode, d.max_mode = n, norm_mode, max_mode
         d.fixed_max_a, d.fixed_max_b = fixed_max
         d.subpix_mode = subpix_mode
+        d.num_peaks, d.peak_kernel = num_peaks, peak_kernel
         return d
+
+    @staticmethod
+    def _out_vectors(count, d):
+        return np.empty(count, VECTOR_DTYPE) if d.num_peaks == 0 else np.empty((count, d.num_peaks), VECTOR_DTYPE)
 
     def piv_pass(self, img_a, img_b, n, a_top, a_left, b_top=None, b_left=None, **kw):
         """One correlation pass over host images; origins per IA (int32)."""
@@ -339,8 +389,8 @@ class Handle:
         count = at.shape[0]
         if not (al.shape[0] == bt.shape[0] == bl.shape[0] == count):
             raise ValueError("origin arrays differ in length")
-        out = np.empty(count, VECTOR_DTYPE)
         d = self.desc(n, **kw)
+        out = self._out_vectors(count, d)
         _check(self._lib.qlpiv_pass(self._h, ctypes.byref(d), _addr(ia), _addr(ib), ia.shape[0], ia.shape[1],
                                     pixel_type_of(ia.dtype), count, _addr(at), _addr(al), _addr(bt), _addr(bl),
                                     _addr(out)))
@@ -372,8 +422,8 @@ class Handle:
         al = np.ascontiguousarray(a_left, np.int32)
         bt = at if b_top is None else np.ascontiguousarray(b_top, np.int32)
         bl = al if b_left is None else np.ascontiguousarray(b_left, np.int32)
-        out = np.empty(len(at), VECTOR_DTYPE)
         d = self.desc(n, **kw)
+        out = self._out_vectors(len(at), d)
         _check(self._lib.qlpiv_pass_batch(self._h, ctypes.byref(d), pixel_type_of(dt), len(fa), table, len(at),
                                           _addr(fi), _addr(at), _addr(al), _addr(bt), _addr(bl), _addr(out)))
         return out
@@ -426,6 +476,25 @@ class Handle:
                                          ia.shape[1], len(ci), len(cj), _addr(ci), _addr(cj), _addr(u), _addr(v),
                                          int(int16_quirk), _addr(oa), _addr(ob)))
         return oa, ob
+
+    def validate(self, tops, lefts, u, v, peak_u, peak_v, npeaks, desc):
+        """Multi-peak normalised-median validation of one frame's tiles (host arrays):
+        u, v (ni, nj) with the main peak accumulated, peak_u/peak_v (ni, nj, k), npeaks
+        (ni, nj).  Returns validated copies of (u, v) and the invalid flags."""
+        u = np.array(u, np.float32, order="C", copy=True)
+        v = np.array(v, np.float32, order="C", copy=True)
+        ni, nj = u.shape
+        pu = np.ascontiguousarray(peak_u, np.float32)
+        pv = np.ascontiguousarray(peak_v, np.float32)
+        if pu.shape != (ni, nj, desc.num_peaks) or pv.shape != pu.shape:
+            raise ValueError("peak arrays must be (ni, nj, num_peaks)")
+        npk = np.ascontiguousarray(npeaks, np.int32)
+        tops = np.ascontiguousarray(tops, np.int32)
+        lefts = np.ascontiguousarray(lefts, np.int32)
+        inv = np.empty((ni, nj), np.uint8)
+        _check(self._lib.qlpiv_validate(self._h, ctypes.byref(desc), ni, nj, _addr(tops), _addr(lefts), _addr(u),
+                                        _addr(v), _addr(pu), _addr(pv), _addr(npk), _addr(inv)))
+        return u, v, inv
 
     def piv_adaptive(self, frames_a, frames_b, desc):
         """Adaptive multi-pass PIV of image pairs of one size; returns (u, v) of the last

@@ -58,8 +58,14 @@ qlpiv_status check_desc(const qlpiv_pass_desc *d) {
         return fail(QLPIV_E_ARG, "fixed tile maxima must be positive");
     if (d->subpix_mode != QLPIV_SUBPIX_NONE && d->subpix_mode != QLPIV_SUBPIX_GAUSS3)
         return fail(QLPIV_E_ARG, "unknown sub-pixel mode %d", d->subpix_mode);
+    if (d->num_peaks != 0 && !qlpiv::multipeak_supported(d->n, d->num_peaks, d->peak_kernel))
+        return fail(QLPIV_E_ARG, "multi-peak search: %d peaks with cell width %d not supported for IA %d "
+                    "(1..%d peaks, cell width >= 2)", d->num_peaks, d->peak_kernel, d->n, QLPIV_MAX_PEAKS);
     return QLPIV_OK;
 }
+
+// vectors written per IA: one, or num_peaks in multi-peak mode
+long vectors_per_ia(const qlpiv_pass_desc *d) { return d->num_peaks > 0 ? d->num_peaks : 1; }
 
 qlpiv_status check_pixel(int pixel_type) {
     if (pixel_type != QLPIV_PIX_U8 && pixel_type != QLPIV_PIX_U16 && pixel_type != QLPIV_PIX_F32)
@@ -78,7 +84,7 @@ qlpiv_status launch(qlpiv_handle *h, const qlpiv::IaJob &job, int n, int pixel_t
 // contiguous per tile, form a virtual image of count*n rows and n columns.
 qlpiv_status tiles_call(qlpiv_handle *h, int n, long count, int pixel_type, const void *ta, const void *tb,
                         const float *max_a, const float *max_b, int norm_mode, int subpix_mode,
-                        qlpiv_vector *vec_out, float *planes_out) {
+                        qlpiv_vector *vec_out, float *planes_out, int num_peaks = 0, int peak_kernel = 0) {
     if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
     if (count < 0) return fail(QLPIV_E_ARG, "count < 0");
     if (count == 0) return QLPIV_OK;
@@ -90,6 +96,10 @@ qlpiv_status tiles_call(qlpiv_handle *h, int n, long count, int pixel_type, cons
     if (norm_mode != QLPIV_NORM_MAX_A && norm_mode != QLPIV_NORM_OWN_MAX && norm_mode != QLPIV_NORM_NONE)
         return fail(QLPIV_E_ARG, "unknown normalisation mode %d", norm_mode);
     if ((long)n * n * count > (1L << 31) - 1) return fail(QLPIV_E_SHAPE, "tile batch too large for one call");
+    if (num_peaks != 0 && !qlpiv::multipeak_supported(n, num_peaks, peak_kernel))
+        return fail(QLPIV_E_ARG, "multi-peak search: %d peaks with cell width %d not supported for IA %d "
+                    "(1..%d peaks, cell width >= 2)", num_peaks, peak_kernel, n, QLPIV_MAX_PEAKS);
+    const long kq = num_peaks > 0 ? num_peaks : 1;
 
     std::lock_guard<std::mutex> lock(h->mu);
     DeviceScope ds(h->device);
@@ -103,7 +113,8 @@ qlpiv_status tiles_call(qlpiv_handle *h, int n, long count, int pixel_type, cons
         if ((e = h->max_a.ensure(sizeof(float) * count)) != cudaSuccess) return cuda_fail(e, "max buffer");
         if ((e = h->max_b.ensure(sizeof(float) * count)) != cudaSuccess) return cuda_fail(e, "max buffer");
     }
-    if ((e = h->vectors.ensure(sizeof(qlpiv_vector) * count)) != cudaSuccess) return cuda_fail(e, "vector buffer");
+    if ((e = h->vectors.ensure(sizeof(qlpiv_vector) * count * kq)) != cudaSuccess)
+        return cuda_fail(e, "vector buffer");
     if (planes_out && (e = h->planes.ensure(sizeof(float) * (size_t)d * d * count)) != cudaSuccess)
         return cuda_fail(e, "plane buffer");
 
@@ -135,10 +146,12 @@ qlpiv_status tiles_call(qlpiv_handle *h, int n, long count, int pixel_type, cons
     job.subpix = subpix_mode == QLPIV_SUBPIX_GAUSS3;
     job.out = (qlpiv_vector *)h->vectors.p;
     job.planes = planes_out ? (float *)h->planes.p : nullptr;
+    job.num_peaks = num_peaks;
+    job.peak_kernel = peak_kernel;
     if ((st = launch(h, job, n, pixel_type)) != QLPIV_OK) return st;
 
-    if (vec_out && (e = cudaMemcpyAsync(vec_out, h->vectors.p, sizeof(qlpiv_vector) * count, cudaMemcpyDeviceToHost,
-                                        h->stream)) != cudaSuccess)
+    if (vec_out && (e = cudaMemcpyAsync(vec_out, h->vectors.p, sizeof(qlpiv_vector) * count * kq,
+                                        cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess)
         return cuda_fail(e, "vector download");
     if (planes_out && (e = cudaMemcpyAsync(planes_out, h->planes.p, sizeof(float) * (size_t)d * d * count,
                                            cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess)
@@ -171,6 +184,8 @@ qlpiv::IaJob frame_job(const qlpiv_pass_desc *desc, const void *img_a, const voi
     job.subpix = desc->subpix_mode == QLPIV_SUBPIX_GAUSS3;
     job.out = out;
     job.planes = nullptr;
+    job.num_peaks = desc->num_peaks;
+    job.peak_kernel = desc->peak_kernel;
     return job;
 }
 
@@ -240,6 +255,13 @@ qlpiv_status qlpiv_create(const qlpiv_params *params, qlpiv_handle **out) {
         return cuda_fail(e, "handle set-up");
     }
     h->stream = h->own_stream;
+    // FFT twiddle tables: uploaded here, before any stream of this handle can be captured
+    const qlpiv::cplx *tw = nullptr;
+    if ((e = qlpiv::ensure_twiddles(dev, &tw)) != cudaSuccess) {
+        cudaStreamDestroy(h->own_stream);
+        delete h;
+        return cuda_fail(e, "twiddle tables");
+    }
     *out = h;
     return QLPIV_OK;
 }
@@ -295,6 +317,17 @@ qlpiv_status qlpiv_xcorr_peaks(qlpiv_handle *h, int n, long count, int pixel_typ
     return tiles_call(h, n, count, pixel_type, tiles_a, tiles_b, max_a, max_b, norm_mode, subpix_mode, out, nullptr);
 }
 
+qlpiv_status qlpiv_xcorr_multipeaks(qlpiv_handle *h, int n, long count, int pixel_type, const void *tiles_a,
+                                    const void *tiles_b, const float *max_a, const float *max_b, int norm_mode,
+                                    int subpix_mode, int num_peaks, int peak_kernel, qlpiv_vector *out) {
+    if (count > 0 && !out) return fail(QLPIV_E_ARG, "output vector array is NULL");
+    if (subpix_mode != QLPIV_SUBPIX_NONE && subpix_mode != QLPIV_SUBPIX_GAUSS3)
+        return fail(QLPIV_E_ARG, "unknown sub-pixel mode %d", subpix_mode);
+    if (num_peaks < 1) return fail(QLPIV_E_ARG, "num_peaks must be >= 1");
+    return tiles_call(h, n, count, pixel_type, tiles_a, tiles_b, max_a, max_b, norm_mode, subpix_mode, out, nullptr,
+                      num_peaks, peak_kernel);
+}
+
 qlpiv_status qlpiv_pass(qlpiv_handle *h, const qlpiv_pass_desc *desc, const void *img_a, const void *img_b,
                         int height, int width, int pixel_type, long count, const int32_t *a_top,
                         const int32_t *a_left, const int32_t *b_top, const int32_t *b_left, qlpiv_vector *out) {
@@ -308,7 +341,7 @@ qlpiv_status qlpiv_pass(qlpiv_handle *h, const qlpiv_pass_desc *desc, const void
     cudaError_t e;
     if ((e = h->tiles_a.ensure(img_bytes)) != cudaSuccess || (e = h->tiles_b.ensure(img_bytes)) != cudaSuccess ||
         (e = h->origins.ensure(sizeof(int32_t) * 4 * count)) != cudaSuccess ||
-        (e = h->vectors.ensure(sizeof(qlpiv_vector) * count)) != cudaSuccess)
+        (e = h->vectors.ensure(sizeof(qlpiv_vector) * count * vectors_per_ia(desc))) != cudaSuccess)
         return cuda_fail(e, "workspace");
     int32_t *org = (int32_t *)h->origins.p;
     if ((e = cudaMemcpyAsync(h->tiles_a.p, img_a, img_bytes, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess ||
@@ -325,8 +358,8 @@ qlpiv_status qlpiv_pass(qlpiv_handle *h, const qlpiv_pass_desc *desc, const void
     qlpiv::IaJob job = frame_job(desc, h->tiles_a.p, h->tiles_b.p, height, width, count, org, org + count,
                                  org + 2 * count, org + 3 * count, (qlpiv_vector *)h->vectors.p);
     if ((st = launch(h, job, desc->n, pixel_type)) != QLPIV_OK) return st;
-    if ((e = cudaMemcpyAsync(out, h->vectors.p, sizeof(qlpiv_vector) * count, cudaMemcpyDeviceToHost, h->stream)) !=
-        cudaSuccess)
+    if ((e = cudaMemcpyAsync(out, h->vectors.p, sizeof(qlpiv_vector) * count * vectors_per_ia(desc),
+                             cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess)
         return cuda_fail(e, "download");
     if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(e, "pass");
     return QLPIV_OK;
@@ -367,7 +400,7 @@ qlpiv_status qlpiv_pass_batch(qlpiv_handle *h, const qlpiv_pass_desc *desc, int 
     cudaError_t e;
     if ((e = h->tiles_a.ensure(total)) != cudaSuccess || (e = h->frames.ensure(sizeof(qlpiv_frame) * num_frames)) !=
         cudaSuccess || (e = h->origins.ensure(sizeof(int32_t) * 5 * count)) != cudaSuccess ||
-        (e = h->vectors.ensure(sizeof(qlpiv_vector) * count)) != cudaSuccess)
+        (e = h->vectors.ensure(sizeof(qlpiv_vector) * count * vectors_per_ia(desc))) != cudaSuccess)
         return cuda_fail(e, "workspace");
     // pack the images densely (pitch = width) and rebuild the frame table for the device
     std::vector<qlpiv_frame> dev_frames(num_frames);
@@ -399,8 +432,8 @@ qlpiv_status qlpiv_pass_batch(qlpiv_handle *h, const qlpiv_pass_desc *desc, int 
     qlpiv::IaJob job = batch_job(desc, (const qlpiv_frame *)h->frames.p, count, org, org + count, org + 2 * count,
                                  org + 3 * count, org + 4 * count, (qlpiv_vector *)h->vectors.p);
     if ((st = launch(h, job, desc->n, pixel_type)) != QLPIV_OK) return st;
-    if ((e = cudaMemcpyAsync(out, h->vectors.p, sizeof(qlpiv_vector) * count, cudaMemcpyDeviceToHost, h->stream)) !=
-        cudaSuccess)
+    if ((e = cudaMemcpyAsync(out, h->vectors.p, sizeof(qlpiv_vector) * count * vectors_per_ia(desc),
+                             cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess)
         return cuda_fail(e, "download");
     // the frame table lives in pageable host memory: wait before it goes out of scope
     if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(e, "batch pass");

@@ -9,6 +9,8 @@
 //                                 origins (no warping)
 //   xcorr + peak + sub-pixel   -> K1, which also accumulates the increment into the
 //                                 level's tile displacements
+//   validation (optional)      -> multi-peak normalised-median validation and replacement
+//                                 (VectorValidatorJob, qlpiv_validate.cu)
 // Everything stays on the device; only the last level's displacements leave it.
 #include <cuda_runtime.h>
 
@@ -18,6 +20,7 @@
 #include "qlpiv_adaptive.h"
 #include "qlpiv_handle.h"
 #include "qlpiv_internal.h"
+#include "qlpiv_validate.h"
 #include "qlpiv_xcorr.cuh"
 
 namespace qlpiv {
@@ -32,6 +35,9 @@ struct LevelPlan {
     DevBuf d_u, d_v;                       // tile displacements, pairs x count
     DevBuf coef;                           // 6 doubles + 2 float4 per tile and pair
     DevBuf d_rows;                         // inheritance stage 1: 2 x pairs x tiles_i x parent tiles_j
+    // validation (allocated only when the descriptor asks for it)
+    DevBuf d_tops, d_lefts, d_order, d_rank;  // grid rows / columns, spiral order and rank
+    DevBuf d_bu, d_bv, d_puv, d_npk, d_state, d_list, d_done, d_sweeps;
     long count() const { return (long)g.tiles_i * g.tiles_j; }
 };
 
@@ -49,7 +55,9 @@ void destroy_plan(AdaptivePlan *p) {
     if (!p) return;
     for (LevelPlan &l : p->levels)
         for (DevBuf *b : {&l.d_cy, &l.d_cx, &l.d_cyf, &l.d_cxf, &l.d_cpy, &l.d_cpx, &l.d_fi, &l.d_at, &l.d_al, &l.d_bt,
-                          &l.d_bl, &l.d_u, &l.d_v, &l.coef, &l.d_rows})
+                          &l.d_bl, &l.d_u, &l.d_v, &l.coef, &l.d_rows, &l.d_tops, &l.d_lefts, &l.d_order,
+                          &l.d_rank, &l.d_bu, &l.d_bv, &l.d_puv, &l.d_npk, &l.d_state, &l.d_list, &l.d_done,
+                          &l.d_sweeps})
             b->release();
     for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table}) b->release();
     delete p;
@@ -87,7 +95,27 @@ static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type,
         return fail(QLPIV_E_ARG, "unknown sub-pixel mode %d", d->subpix_mode);
     if (!(d->overlap_factor >= 0.1f && d->overlap_factor <= 0.9f))
         return fail(QLPIV_E_ARG, "Overlap factor must greater than 1/10 and less than 9/10");
+    if (d->validation != QLPIV_VALIDATE_NONE && d->validation != QLPIV_VALIDATE_MULTIPEAK_MEDIAN)
+        return fail(QLPIV_E_ARG, "unknown validation mode %d", d->validation);
+    if (d->validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN) {
+        for (int n = d->ia_start; n >= d->ia_end; n >>= 1)
+            if (!multipeak_supported(n, d->num_peaks, d->peak_kernel))
+                return fail(QLPIV_E_ARG, "multi-peak search: %d peaks with cell width %d not supported for IA %d "
+                            "(1..%d peaks, cell width >= 2)", d->num_peaks, d->peak_kernel, n, QLPIV_MAX_PEAKS);
+        if (!(d->median_threshold > 0.0f) || !(d->median_epsilon0 >= 0.0f))
+            return fail(QLPIV_E_ARG, "median threshold must be > 0 and epsilon0 >= 0");
+        if (d->max_correction_iterations < 0) return fail(QLPIV_E_ARG, "max correction iterations < 0");
+    }
     return QLPIV_OK;
+}
+
+// Spiral visit order of a grid and the rank of every tile in it.
+static void spiral_rank(int ni, int nj, std::vector<int32_t> &order, std::vector<int32_t> &rank) {
+    const long cnt = (long)ni * nj;
+    order.resize(cnt);
+    rank.resize(cnt);
+    spiral_order(ni, nj, order.data());
+    for (long r = 0; r < cnt; r++) rank[order[r]] = (int32_t)r;
 }
 
 static int level_count(const qlpiv_adaptive_desc *d) {
@@ -174,6 +202,23 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
             (lv > 0 && (e = L.d_rows.ensure(sizeof(float) * 2 * (long)pairs * ni *
                                             p->levels[lv - 1].g.tiles_j)) != cudaSuccess))
             return cuda_fail(e, "adaptive plan");
+        std::vector<int32_t> order, rank;
+        if (d->validation != QLPIV_VALIDATE_NONE) {
+            spiral_rank(ni, nj, order, rank);
+            const long k = d->num_peaks;
+            if ((e = upload(L.d_tops, L.tops.data(), sizeof(int32_t) * ni, s)) != cudaSuccess ||
+                (e = upload(L.d_lefts, L.lefts.data(), sizeof(int32_t) * nj, s)) != cudaSuccess ||
+                (e = upload(L.d_order, order.data(), sizeof(int32_t) * cnt, s)) != cudaSuccess ||
+                (e = upload(L.d_rank, rank.data(), sizeof(int32_t) * cnt, s)) != cudaSuccess ||
+                (e = L.d_bu.ensure(sizeof(float) * total)) != cudaSuccess ||
+                (e = L.d_bv.ensure(sizeof(float) * total)) != cudaSuccess ||
+                (e = L.d_puv.ensure(sizeof(float2) * total * k)) != cudaSuccess ||
+                (e = L.d_npk.ensure(total)) != cudaSuccess || (e = L.d_state.ensure(total)) != cudaSuccess ||
+                (e = L.d_list.ensure(sizeof(int32_t) * total)) != cudaSuccess ||
+                (e = L.d_done.ensure(sizeof(int32_t) * total)) != cudaSuccess ||
+                (e = L.d_sweeps.ensure(sizeof(int32_t) * pairs)) != cudaSuccess)
+                return cuda_fail(e, "validation buffers");
+        }
         // the host vectors above die at scope exit: make the copies complete first
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "adaptive plan upload");
     }
@@ -305,12 +350,31 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
         job.subpix = d.subpix_mode == QLPIV_SUBPIX_GAUSS3;
         job.acc_u = u;
         job.acc_v = v;
+        const bool validate = d.validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN;
+        if (validate) {
+            // the multi-peak model selects FindMaximumMultiPeaks for every level
+            job.num_peaks = d.num_peaks;
+            job.peak_kernel = d.peak_kernel;
+            job.peak_uv = L.d_puv.as<float2>();
+            job.npeaks = L.d_npk.as<uint8_t>();
+        }
         {
             StageScope sc(h, "xcorr", (int)lv, L.g.n, 1, total);
             if ((e = launch_xcorr(job, L.g.n, p->pixel_type, s, h->num_sms)) != cudaSuccess)
                 return cuda_fail(e, "xcorr");
         }
         h->launches++;
+        if (validate) {
+            StageScope sc(h, "validate", (int)lv, L.g.n, 2, total);
+            ValidateParams vp{L.g.tiles_i, L.g.tiles_j, d.num_peaks, d.median_threshold, d.median_epsilon0,
+                              d.max_correction_iterations, d.iterate_until_no_corrections};
+            ValidateBufs vb{u, v, L.d_bu.as<float>(), L.d_bv.as<float>(), L.d_puv.as<float2>(),
+                            L.d_npk.as<uint8_t>(), L.d_state.as<uint8_t>(), L.d_tops.as<int>(), L.d_lefts.as<int>(),
+                            L.d_order.as<int>(), L.d_rank.as<int>(), L.d_list.as<int>(), L.d_done.as<int>(),
+                            L.d_sweeps.as<int>()};
+            if ((e = launch_validate(s, pairs, vp, vb)) != cudaSuccess) return cuda_fail(e, "validation");
+            h->launches += 2;
+        }
     }
     return QLPIV_OK;
 }
@@ -558,6 +622,78 @@ qlpiv_status qlpiv_piv_adaptive(qlpiv_handle *h, const qlpiv_adaptive_desc *desc
         (e = cudaMemcpyAsync(out_v, L.d_v.p, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
         return cuda_fail(e, "adaptive PIV");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_validate(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int ni, int nj, const int32_t *tops,
+                            const int32_t *lefts, float *u, float *v, const float *peak_u, const float *peak_v,
+                            const int32_t *npeaks, uint8_t *invalid_out) {
+    if (!h || !desc || !tops || !lefts || !u || !v || !peak_u || !peak_v || !npeaks)
+        return fail(QLPIV_E_ARG, "NULL argument");
+    if (ni < 1 || nj < 1) return fail(QLPIV_E_SHAPE, "empty grid");
+    const int k = desc->num_peaks;
+    if (k < 1 || k > QLPIV_MAX_PEAKS) return fail(QLPIV_E_ARG, "num_peaks must be in 1..%d", QLPIV_MAX_PEAKS);
+    if (!(desc->median_threshold > 0.0f) || !(desc->median_epsilon0 >= 0.0f))
+        return fail(QLPIV_E_ARG, "median threshold must be > 0 and epsilon0 >= 0");
+    const long cnt = (long)ni * nj;
+    std::vector<float2> puv(cnt * k);
+    std::vector<uint8_t> npk(cnt);
+    for (long t = 0; t < cnt; t++) {
+        if (npeaks[t] < 0 || npeaks[t] > k) return fail(QLPIV_E_ARG, "npeaks[%ld] = %d outside 0..%d", t, npeaks[t], k);
+        npk[t] = (uint8_t)npeaks[t];
+        for (int q = 0; q < k; q++) puv[t * k + q] = make_float2(peak_u[t * k + q], peak_v[t * k + q]);
+    }
+    std::vector<int32_t> order, rank;
+    spiral_rank(ni, nj, order, rank);
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaStream_t s = h->stream;
+    // one scratch buffer carved into the per-tile arrays (256-byte aligned pieces)
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t sz_f = al(sizeof(float) * cnt), sz_i = al(sizeof(int32_t) * cnt), sz_b = al(cnt);
+    const size_t sz_p = al(sizeof(float2) * cnt * k), sz_t = al(sizeof(int32_t) * ni), sz_l = al(sizeof(int32_t) * nj);
+    const size_t total = 4 * sz_f + sz_p + 2 * sz_b + 4 * sz_i + sz_t + sz_l + 256;
+    DevBuf &b = h->scratch[11];
+    cudaError_t e = b.ensure(total);
+    if (e != cudaSuccess) return cuda_fail(e, "validation scratch");
+    char *c = b.as<char>();
+    float *du = (float *)c; c += sz_f;
+    float *dv = (float *)c; c += sz_f;
+    float *dbu = (float *)c; c += sz_f;
+    float *dbv = (float *)c; c += sz_f;
+    float2 *dpuv = (float2 *)c; c += sz_p;
+    uint8_t *dnpk = (uint8_t *)c; c += sz_b;
+    uint8_t *dst = (uint8_t *)c; c += sz_b;
+    int32_t *dorder = (int32_t *)c; c += sz_i;
+    int32_t *drank = (int32_t *)c; c += sz_i;
+    int32_t *dlist = (int32_t *)c; c += sz_i;
+    int32_t *ddone = (int32_t *)c; c += sz_i;
+    int32_t *dtops = (int32_t *)c; c += sz_t;
+    int32_t *dlefts = (int32_t *)c; c += sz_l;
+    int32_t *dsweeps = (int32_t *)c;
+    if ((e = cudaMemcpyAsync(du, u, sizeof(float) * cnt, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dv, v, sizeof(float) * cnt, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dpuv, puv.data(), sizeof(float2) * cnt * k, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dnpk, npk.data(), cnt, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dorder, order.data(), sizeof(int32_t) * cnt, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(drank, rank.data(), sizeof(int32_t) * cnt, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dtops, tops, sizeof(int32_t) * ni, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dlefts, lefts, sizeof(int32_t) * nj, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "validation upload");
+    ValidateParams vp{ni, nj, k, desc->median_threshold, desc->median_epsilon0, desc->max_correction_iterations,
+                      desc->iterate_until_no_corrections};
+    ValidateBufs vb{du, dv, dbu, dbv, dpuv, dnpk, dst, dtops, dlefts, dorder, drank, dlist, ddone, dsweeps};
+    if ((e = launch_validate(s, 1, vp, vb)) != cudaSuccess) return cuda_fail(e, "validation");
+    h->launches += 2;
+    std::vector<uint8_t> state(cnt);
+    if ((e = cudaMemcpyAsync(u, du, sizeof(float) * cnt, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(v, dv, sizeof(float) * cnt, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(state.data(), dst, cnt, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "validation download");
+    if (invalid_out)
+        for (long t = 0; t < cnt; t++) invalid_out[t] = state[t] & 1u;
     return QLPIV_OK;
 }
 

@@ -1,10 +1,40 @@
 // K1 instantiations (IA side x pixel type) and their launcher.
+#include <cmath>
 #include <mutex>
 
 #include "qlpiv_internal.h"
 #include "qlpiv_xcorr.cuh"
 
 namespace qlpiv {
+
+// Twiddle tables exp(-2 pi i e / M) for M = 32, 64, 128 (offsets 0, 32, 96), filled once
+// per device from the host (double precision, rounded to float).
+static __device__ cplx g_twiddles[32 + 64 + 128];
+
+static int twiddle_offset(int m) { return m == 32 ? 0 : (m == 64 ? 32 : 96); }
+
+cudaError_t ensure_twiddles(int dev, const cplx **table) {
+    static std::mutex mu;
+    static const cplx *addr[kMaxDevices] = {nullptr};
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (addr[dev] == nullptr) {
+        cplx host[32 + 64 + 128];
+        for (int m : {32, 64, 128})
+            for (int e = 0; e < m; e++) {
+                const double a = -2.0 * M_PI * (double)e / (double)m;
+                host[twiddle_offset(m) + e] = cplx{(float)std::cos(a), (float)std::sin(a)};
+            }
+        cudaError_t err = cudaMemcpyToSymbol(g_twiddles, host, sizeof(host));
+        if (err != cudaSuccess) return err;
+        void *p = nullptr;
+        err = cudaGetSymbolAddress(&p, g_twiddles);
+        if (err != cudaSuccess) return err;
+        addr[dev] = static_cast<const cplx *>(p);
+    }
+    *table = addr[dev];
+    return cudaSuccess;
+}
 
 template <int N, typename Pix>
 static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms) {
@@ -30,10 +60,16 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
         }
         bps = blocks_per_sm[dev];
     }
-    long grid = (long)num_sms * bps * 8;
+    const cplx *tw = nullptr;
+    if ((e = ensure_twiddles(dev, &tw)) != cudaSuccess) return e;
+    IaJob j = job;
+    j.twiddles = tw + twiddle_offset(S::M);
+    // every CTA loops over IAs; eight waves of CTAs balance the single-peak kernel best,
+    // one resident wave the multi-peak one (its fit queue then fills between flushes)
+    long grid = (long)num_sms * bps * (job.num_peaks > 0 ? 1 : 8);
     if (grid > job.count) grid = job.count;
     if (grid < 1) return cudaSuccess;
-    xcorr_kernel<N, Pix><<<(unsigned)grid, S::T, S::SMEM, stream>>>(job);
+    xcorr_kernel<N, Pix><<<(unsigned)grid, S::T, S::SMEM, stream>>>(j);
     return cudaGetLastError();
 }
 
@@ -57,5 +93,20 @@ cudaError_t launch_xcorr(const IaJob &job, int n, int pixel_type, cudaStream_t s
 }
 
 bool xcorr_size_supported(int n) { return n == 16 || n == 32 || n == 64; }
+
+template <int N>
+static bool multipeak_fits_n(int kw) {
+    return mp_stage_bytes(mp_geom(XcorrShape<N>::D, kw)) <= XcorrShape<N>::SCR_BYTES;
+}
+
+bool multipeak_supported(int n, int num_peaks, int peak_kernel) {
+    if (num_peaks < 1 || num_peaks > QLPIV_MAX_PEAKS || peak_kernel < 2 || peak_kernel > 4096) return false;
+    switch (n) {
+        case 16: return multipeak_fits_n<16>(peak_kernel);
+        case 32: return multipeak_fits_n<32>(peak_kernel);
+        case 64: return multipeak_fits_n<64>(peak_kernel);
+        default: return false;
+    }
+}
 
 }  // namespace qlpiv

@@ -25,6 +25,14 @@
 //      (value desc, distance to (N,N) asc, scan rank asc) and keeps the min floor;
 //   5. CTA reduction of the peak key, then thread 0 fits the 3-point Gaussian from
 //      the plane kept in shared memory and writes one 32-byte vector.
+//   5'. multi-peak mode (FindMaximumMultiPeaks, S/maximum/FindMaximumMultiPeaks.java:42-162):
+//      every thread reduces kw x kw cells of the plane to (max, position) records in
+//      the reference's insertion order, with a per-32-record maximum; warp 0 then
+//      replays the sorted, adjacency-suppressing list insertions
+//      (S/util/SimpleFixedLengthFloatLinkedList.java:98-237), visiting only the records
+//      that can change the list (all while it has room, otherwise those above its
+//      minimum; whole 32-record chunks are skipped on their maximum), and queues one
+//      fit per peak.
 #pragma once
 #include "qlpiv_fft.cuh"
 #include "qlpiv.h"
@@ -41,9 +49,27 @@ struct XcorrShape {
     static constexpr int ROUNDS = N / NG;              // tasks per group per phase
     static constexpr int RP = M + M / 8 + 1;           // region pitch (complex), odd
     static constexpr int MIN_BLOCKS = N == 16 ? 16 : (N == 32 ? 4 : 2);
-    static constexpr size_t SMEM =
-        sizeof(cplx) * (size_t)(M + N * RP + NG * RP) + 64 * sizeof(uint64_t) + 32 * 48;  // + fit queue
+    static constexpr size_t SCR_BYTES = sizeof(cplx) * (size_t)(NG * RP);
+    static constexpr size_t SMEM = sizeof(cplx) * (size_t)(M + N * RP) + SCR_BYTES + 64 * sizeof(uint64_t) +
+                                   32 * 56 /* fit queue */ + 256 /* multi-peak list */;
 };
+
+// FindMaximumMultiPeaks geometry of a d x d plane: slices = ceil(d / kw) per axis, the
+// first `top` of them form the top/left half; records are visited slice by slice
+// (row-major), four interleaved quadrant cells each.
+struct MpGeom {
+    int kw, top, nrec, nchunk;
+};
+__host__ __device__ inline MpGeom mp_geom(int d, int kw) {
+    const int slices = (d + kw - 1) / kw;
+    const int top = slices - slices / 2;
+    const int nrec = 4 * top * top;
+    return MpGeom{kw, top, nrec, (nrec + 31) / 32};
+}
+// Bytes of the per-IA record staging (values, positions, chunk maxima).
+__host__ __device__ inline size_t mp_stage_bytes(const MpGeom &g) {
+    return (size_t)g.nrec * 8 + (size_t)g.nchunk * 4;
+}
 
 template <typename Pix>
 __device__ __forceinline__ float load_pix(const Pix *img, long pitch, int h, int w, int y, int x) {
@@ -87,17 +113,24 @@ struct IaJob {
     long count;
     int norm_mode, max_mode, subpix;
     float fixed_max_a, fixed_max_b;
-    qlpiv_vector *out;           // optional per-IA vectors
+    qlpiv_vector *out;           // optional per-IA vectors (num_peaks per IA in multi-peak mode)
     float *planes;               // optional (2N-1)^2 planes per IA
     float *acc_u, *acc_v;        // optional: tile displacements += (u, v)  (Tile.accumulateDisplacement)
+    int num_peaks;               // 0: FindMaximumFromCenter; k >= 1: FindMaximumMultiPeaks
+    int peak_kernel;             // multi-peak cell width
+    float2 *peak_uv;             // optional [count][k] displacement increments of every peak
+    uint8_t *npeaks;             // optional [count] peaks found
+    const cplx *twiddles;        // exp(-2 pi i e / M), e < M (device table, filled once per device)
 };
 
 // Integer peak and 3-point stencil of one IA, queued for the sub-pixel fit.
 struct FitRec {
     long ia;
-    int pi, pj, kind;   // kind: 0 fit, 1 no peak, 2 stencil off the plane, 3 no sub-pixel
+    int pi, pj, kind;   // kind: 0 fit, 1 no peak, 2 stencil off the plane, 3 no sub-pixel, 4 absent slot
+    int slot, npk;      // multi-peak: peak index (0 = largest) and peaks found
     float pv, mn, c0, yu, yd, xl, xr;
 };
+static_assert(sizeof(FitRec) == 56, "fit queue sizing");
 
 // Gaussian1DPolynomialInterpolator.interpolate (S/interpolators/Gaussian1DPolynomialInterpolator.java:25-106)
 // for q[0..n): lane k handles record k, so the double logarithms of 32 IAs share one
@@ -145,13 +178,397 @@ __device__ void fit_flush(const FitRec *q, int n, int lane, const IaJob &job) {
         o.peak_i = (int16_t)r.pi;
         o.peak_j = (int16_t)r.pj;
         o.flags = flags;
-        if (job.out != nullptr) job.out[r.ia] = o;
-        if (job.acc_u != nullptr) {
+        if (r.kind == 4) {
+            o = qlpiv_vector{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0, 0, QLPIV_F_ABSENT};
+        }
+        if (job.num_peaks == 0) {
+            if (job.out != nullptr) job.out[r.ia] = o;
+        } else {
+            const long slot = r.ia * job.num_peaks + r.slot;
+            if (job.out != nullptr) job.out[slot] = o;
+            if (job.peak_uv != nullptr) job.peak_uv[slot] = make_float2(o.u, o.v);
+            if (r.slot == 0 && job.npeaks != nullptr) job.npeaks[r.ia] = (uint8_t)r.npk;
+        }
+        if (job.acc_u != nullptr && r.slot == 0) {
             job.acc_u[r.ia] += o.u;
             job.acc_v[r.ia] += o.v;
         }
     }
     __syncwarp();
+}
+
+// SimpleFixedLengthFloatLinkedList.addInAscendOrder (S/util/SimpleFixedLengthFloatLinkedList.java:98-237)
+// with the list held by one warp, entry r (ascending order) in lane r's registers.
+// Called by the full warp with a warp-uniform candidate (v, i, j).  Entries smaller than v
+// and adjacent to it are deleted, but only if v is inserted; v is refused next to an
+// equal or larger entry, or when the list is full and v is not above its minimum;
+// when the list overflows its smallest entry leaves.  Adjacent = squared distance below
+// kd = (kw - 1) * kw (exact in float for plane coordinates).
+struct WarpPeakList {
+    float lv = 0.0f;
+    int li = 0, lj = 0;
+    int size = 0;       // warp-uniform
+    __device__ __forceinline__ void insert(int lane, int k, float kd, float v, int i, int j) {
+        const bool valid = lane < size;
+        const bool less = valid && lv < v;
+        const int di = i - li, dj = j - lj;
+        const bool adj = valid && (float)(di * di + dj * dj) < kd;
+        const int pos = __popc(__ballot_sync(0xffffffffu, less));
+        if (size == k && pos == 0) return;
+        if (__ballot_sync(0xffffffffu, valid && !less && adj) != 0u) return;
+        const unsigned del = __ballot_sync(0xffffffffu, less && adj);
+        const unsigned keep = ((1u << size) - 1u) & ~del;   // size <= 16
+        const int ipos = pos - __popc(del);                 // deleted entries all lie below pos
+        int nsize = size - __popc(del) + 1;
+        const int drop = nsize > k ? 1 : 0;                 // only when nothing was deleted, ipos >= 1
+        nsize -= drop;
+        const int d = lane + drop;                          // this lane takes element d of the merged list
+        int src = -1;
+        if (d < ipos) src = (int)__fns(keep, 0, d + 1) ;
+        else if (d > ipos) src = (int)__fns(keep, 0, d);
+        const int sl = src < 0 ? 0 : (src & 31);
+        const float sv = __shfl_sync(0xffffffffu, lv, sl);
+        const int si = __shfl_sync(0xffffffffu, li, sl);
+        const int sj = __shfl_sync(0xffffffffu, lj, sl);
+        if (lane < nsize) {
+            if (src < 0) { lv = v; li = i; lj = j; }
+            else { lv = sv; li = si; lj = sj; }
+        }
+        size = nsize;
+    }
+    __device__ __forceinline__ float lowest() const { return __shfl_sync(0xffffffffu, lv, 0); }
+    __device__ __forceinline__ void store(int lane, float *sv, int *si, int *sj) const {
+        if (lane < size) { sv[lane] = lv; si[lane] = li; sj[lane] = lj; }
+    }
+};
+
+// The same list for k <= KF held whole in every lane's registers (fully unrolled, no
+// shuffles): every lane applies the same insertion to its own copy.
+template <int KF>
+struct RegPeakList {
+    float lv[KF];
+    int li[KF], lj[KF];
+    int size = 0;
+    __device__ __forceinline__ RegPeakList() {
+#pragma unroll
+        for (int r = 0; r < KF; r++) { lv[r] = 0.0f; li[r] = 0; lj[r] = 0; }
+    }
+    // entries [0, n) ascending; v goes to index pos (0 <= pos <= n < KF + drop); drop: the
+    // smallest leaves afterwards
+    __device__ __forceinline__ void place(int pos, int drop, float v, int i, int j) {
+        float nv[KF];
+        int ni[KF], nj[KF];
+#pragma unroll
+        for (int d = 0; d < KF; d++) {
+            // merged element m = d + drop: lv[m] below pos, the new entry at pos, lv[m-1] above
+            const int m = d + drop;
+            const float a_v = (d + 1 < KF) ? lv[d + 1 < KF ? d + 1 : 0] : 0.0f;
+            const int a_i = (d + 1 < KF) ? li[d + 1 < KF ? d + 1 : 0] : 0;
+            const int a_j = (d + 1 < KF) ? lj[d + 1 < KF ? d + 1 : 0] : 0;
+            const float lo_v = drop ? a_v : lv[d];              // lv[m]
+            const int lo_i = drop ? a_i : li[d], lo_j = drop ? a_j : lj[d];
+            const float hi_v = drop ? lv[d] : (d > 0 ? lv[d > 0 ? d - 1 : 0] : 0.0f);   // lv[m - 1]
+            const int hi_i = drop ? li[d] : (d > 0 ? li[d > 0 ? d - 1 : 0] : 0);
+            const int hi_j = drop ? lj[d] : (d > 0 ? lj[d > 0 ? d - 1 : 0] : 0);
+            nv[d] = m < pos ? lo_v : (m == pos ? v : hi_v);
+            ni[d] = m < pos ? lo_i : (m == pos ? i : hi_i);
+            nj[d] = m < pos ? lo_j : (m == pos ? j : hi_j);
+        }
+#pragma unroll
+        for (int d = 0; d < KF; d++) { lv[d] = nv[d]; li[d] = ni[d]; lj[d] = nj[d]; }
+    }
+    __device__ __forceinline__ void insert(int /*lane*/, int k, float kd, float v, int i, int j) {
+        int pos = 0;
+        bool refuse = false;
+        unsigned del = 0u;
+#pragma unroll
+        for (int r = 0; r < KF; r++) {
+            const bool valid = r < size;
+            const bool less = valid && lv[r] < v;
+            const int di = i - li[r], dj = j - lj[r];
+            const bool adj = valid && (float)(di * di + dj * dj) < kd;
+            pos += less ? 1 : 0;
+            refuse = refuse || (valid && !less && adj);
+            if (less && adj) del |= 1u << r;
+        }
+        if (size == k && pos == 0) return;
+        if (refuse) return;
+        if (del == 0u && size == k) {  // common: full, nothing adjacent -> the smallest leaves
+            place(pos, 1, v, i, j);
+            return;
+        }
+        if (del != 0u) {
+            // rare: compact the survivors in place first (all deleted entries lie below pos);
+            // survivor r moves down to slot w <= r
+            int w = 0;
+#pragma unroll
+            for (int r = 0; r < KF; r++) {
+                const bool surv = r < size && !((del >> r) & 1u);
+#pragma unroll
+                for (int q = 0; q <= r; q++) {
+                    if (surv && w == q) {
+                        lv[q] = lv[r];
+                        li[q] = li[r];
+                        lj[q] = lj[r];
+                    }
+                }
+                w += surv ? 1 : 0;
+            }
+            const int nd = __popc(del);
+            size -= nd;
+            pos -= nd;
+        }
+        place(pos, 0, v, i, j);  // room for one more
+        size++;
+    }
+    __device__ __forceinline__ float lowest() const { return lv[0]; }
+    __device__ __forceinline__ void store(int lane, float *sv, int *si, int *sj) const {
+        if (lane == 0) {
+#pragma unroll
+            for (int r = 0; r < KF; r++)
+                if (r < size) { sv[r] = lv[r]; si[r] = li[r]; sj[r] = lj[r]; }
+        }
+    }
+};
+
+// Visits, in order, the records e >= e_begin with value >= floor_v that can change the
+// list (all while it has room, otherwise those above its minimum), skipping whole
+// 32-record chunks on their maximum.  With track set, remembers the list as it was before
+// the last insertion that turned a full list into one with room (e_break = that record).
+template <typename List>
+__device__ void mp_visit(const MpGeom &gm, const float *recv, const int *recp, const float *chmax, int lane, int k,
+                         float kd, int e_begin, float floor_v, List &lst, bool track, List &saved, int &e_break) {
+    float lo = lst.size > 0 ? lst.lowest() : 0.0f;
+    for (int c0 = (e_begin >> 5) & ~31; c0 < gm.nchunk; c0 += 32) {
+        const int c = c0 + lane;
+        const float cmx = c < gm.nchunk ? chmax[c] : 0.0f;
+        unsigned todo = __ballot_sync(0xffffffffu, c < gm.nchunk && c >= (e_begin >> 5) && cmx >= floor_v);
+        while (true) {
+            const unsigned cmask = __ballot_sync(0xffffffffu, ((todo >> lane) & 1u) && (lst.size < k || cmx > lo));
+            if (cmask == 0u) break;
+            const int cl = __ffs(cmask) - 1;
+            todo &= ~((2u << cl) - 1u);
+            const int e = (c0 + cl) * 32 + lane;
+            const bool in = e < gm.nrec && e >= e_begin;
+            const float v = in ? recv[e] : 0.0f;
+            const int pp = in ? recp[e] : 0;
+            unsigned pend = __ballot_sync(0xffffffffu, in && v >= floor_v);
+            while (true) {
+                const unsigned cand = __ballot_sync(0xffffffffu, ((pend >> lane) & 1u) && (lst.size < k || v > lo));
+                if (cand == 0u) break;
+                const int src = __ffs(cand) - 1;
+                pend &= ~((2u << src) - 1u);
+                const float cv = __shfl_sync(0xffffffffu, v, src);
+                int cp = __shfl_sync(0xffffffffu, pp, src);
+                const int ce = (c0 + cl) * 32 + src;
+                if (cp < 0) {  // stale position of the same quadrant, else (0, 0)
+                    cp = 0;
+                    for (int e2 = ce - 4; e2 >= 0; e2 -= 4)
+                        if (recp[e2] >= 0) { cp = recp[e2]; break; }
+                }
+                if (track && lst.size == k) {
+                    const List before = lst;
+                    lst.insert(lane, k, kd, cv, cp >> 16, cp & 0xffff);
+                    if (lst.size < k) {
+                        saved = before;
+                        e_break = ce;
+                    }
+                } else {
+                    lst.insert(lane, k, kd, cv, cp >> 16, cp & 0xffff);
+                }
+                lo = lst.lowest();
+            }
+        }
+    }
+}
+
+// Replays the insertions of the records (values recv, positions recp, -1 = stale) and
+// returns the list size; the list is left in sv/si/sj (ascending).
+//
+// Records below a threshold t cannot change which entries >= t the list holds: run on
+// the records >= t alone, the list always holds exactly the full run's entries >= t
+// (an entry < t only ever leaves room or is evicted first, and is never needed to
+// refuse or delete a record >= t).  So with t = the 4th largest chunk maximum the short
+// run over the records >= t is the answer whenever it ends full; if it ended with room,
+// the full run is resumed from the last point where the short run's list was full
+// (both lists are equal there), or from the start if it never was.
+template <typename List>
+__device__ int mp_replay(const MpGeom &gm, const float *recv, const int *recp, const float *chmax, int lane, int k,
+                         float kd, float *sv, int *si, int *sj) {
+    // t: 4th largest chunk maximum (chunks lane, lane + 32, ... ; nchunk <= 128)
+    float cm[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int c = lane + 32 * q;
+        cm[q] = c < gm.nchunk ? chmax[c] : -1.0f;
+    }
+    float t = 0.0f;
+    const int rounds = gm.nchunk < 4 ? gm.nchunk : 4;
+    for (int r = 0; r < rounds; r++) {
+        float lm = fmaxf(fmaxf(cm[0], cm[1]), fmaxf(cm[2], cm[3]));
+        float wm = lm;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+        const int owner = __ffs(__ballot_sync(0xffffffffu, lm == wm)) - 1;
+        if (lane == owner) {  // drop one occurrence
+            if (cm[0] == wm) cm[0] = -1.0f;
+            else if (cm[1] == wm) cm[1] = -1.0f;
+            else if (cm[2] == wm) cm[2] = -1.0f;
+            else cm[3] = -1.0f;
+        }
+        t = wm;
+    }
+    List lst, saved;
+    int e_break = -1;
+    if (t > 0.0f) {
+        mp_visit<List>(gm, recv, recp, chmax, lane, k, kd, 0, t, lst, true, saved, e_break);
+        if (lst.size < k) {
+            if (e_break >= 0) {
+                lst = saved;
+                mp_visit<List>(gm, recv, recp, chmax, lane, k, kd, e_break, -3.402823466e38f, lst, false, saved,
+                               e_break);
+            } else {
+                lst = List();
+                mp_visit<List>(gm, recv, recp, chmax, lane, k, kd, 0, -3.402823466e38f, lst, false, saved, e_break);
+            }
+        }
+    } else {
+        mp_visit<List>(gm, recv, recp, chmax, lane, k, kd, 0, -3.402823466e38f, lst, false, saved, e_break);
+    }
+    lst.store(lane, sv, si, sj);
+    __syncwarp();
+    return lst.size;
+}
+
+// Cell maxima of the plane in record order (records e = 4 * slice + quadrant): strict >
+// from 0, first in row-major order within the cell; position -1 = no positive value (the
+// reference then reuses the quadrant's previous position).  Also the maximum of every
+// 32 consecutive records.  KW = cell width, 0 = gm.kw at run time.  All threads.
+template <int N, int KW>
+__device__ __forceinline__ void mp_cells(const MpGeom &gm, const float *regf, float *recv, int *recp, float *chmax) {
+    using S = XcorrShape<N>;
+    constexpr int D = S::D, RP = S::RP, T = S::T;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int kw = KW > 0 ? KW : gm.kw;
+    for (int base = warp * 32; base < gm.nrec; base += T) {
+        const int e = base + lane;
+        float bv = 0.0f;
+        if (e < gm.nrec) {
+            int bp = -1;
+            const int sl = e >> 2, q = e & 3;
+            const int ci = sl / gm.top + ((q & 2) ? gm.top : 0);
+            const int cj = sl % gm.top + ((q & 1) ? gm.top : 0);
+            const int i0 = ci * kw, j0 = cj * kw;
+            if (KW > 0) {
+#pragma unroll
+                for (int a = 0; a < (KW > 0 ? KW : 1); a++) {
+                    const int i = i0 + a;
+#pragma unroll
+                    for (int b = 0; b < (KW > 0 ? KW : 1); b++) {
+                        const int j = j0 + b;
+                        if (i < D && j < D) {
+                            const float v = regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)];
+                            if (v > bv) { bv = v; bp = (i << 16) | j; }
+                        }
+                    }
+                }
+            } else {
+                for (int a = 0; a < kw; a++) {
+                    const int i = i0 + a;
+                    if (i >= D) break;
+                    for (int b = 0; b < kw; b++) {
+                        const int j = j0 + b;
+                        if (j >= D) break;
+                        const float v = regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)];
+                        if (v > bv) { bv = v; bp = (i << 16) | j; }
+                    }
+                }
+            }
+            recv[e] = bv;
+            recp[e] = bp;
+        }
+        float cm = bv;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cm = fmaxf(cm, __shfl_xor_sync(0xffffffffu, cm, o));
+        if (lane == 0) chmax[base >> 5] = cm;
+    }
+}
+
+// Step 5' of xcorr_kernel for one IA (kept out of line so that the single-peak path
+// keeps its register allocation): FindMaximumMultiPeaks over the plane in `regf`,
+// queueing `multi` fit records at fitq[qn..).  Called by every thread of the CTA.
+template <int N>
+__device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float minf, const float *regf, cplx *scr,
+                                              uint64_t *red, FitRec *fitq, int qn, float *mp_lv, int *mp_li,
+                                              int *mp_lj) {
+    using S = XcorrShape<N>;
+    constexpr int D = S::D, RP = S::RP, T = S::T, NWARPS = T / 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int multi = job.num_peaks;
+    auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)]; };
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
+    __syncthreads();  // plane complete; the FFT scratch is free for the records
+    float *redf = reinterpret_cast<float *>(red);
+    if (lane == 0) redf[warp] = minf;
+    const MpGeom gm = mp_geom(D, job.peak_kernel);
+    const int kw = gm.kw;
+    float *recv = reinterpret_cast<float *>(scr);
+    int *recp = reinterpret_cast<int *>(recv + gm.nrec);
+    float *chmax = reinterpret_cast<float *>(recp + gm.nrec);
+    // cell maxima: strict > from 0, first in row-major order; -1 = no positive
+    // value (the reference then reuses the quadrant's previous position)
+    if (kw == 3) {
+        mp_cells<N, 3>(gm, regf, recv, recp, chmax);
+    } else {
+        mp_cells<N, 0>(gm, regf, recv, recp, chmax);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        float mn = lane < NWARPS ? redf[lane] : 3.402823466e38f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        const float kd = (float)((kw - 1) * kw);
+        int size;
+        switch (multi) {
+            case 1: size = mp_replay<RegPeakList<1>>(gm, recv, recp, chmax, lane, 1, kd, mp_lv, mp_li, mp_lj); break;
+            case 2: size = mp_replay<RegPeakList<2>>(gm, recv, recp, chmax, lane, 2, kd, mp_lv, mp_li, mp_lj); break;
+            case 3: size = mp_replay<RegPeakList<3>>(gm, recv, recp, chmax, lane, 3, kd, mp_lv, mp_li, mp_lj); break;
+            case 4: size = mp_replay<RegPeakList<4>>(gm, recv, recp, chmax, lane, 4, kd, mp_lv, mp_li, mp_lj); break;
+            default: size = mp_replay<WarpPeakList>(gm, recv, recp, chmax, lane, multi, kd, mp_lv, mp_li, mp_lj);
+        }
+        // one fit record per slot, largest peak first
+        if (lane < multi) {
+            FitRec r;
+            r.ia = ia;
+            r.mn = mn;
+            r.slot = lane;
+            r.npk = size;
+            r.pi = 0;
+            r.pj = 0;
+            r.pv = 0.0f;
+            if (lane < size) {
+                const int idx = size - 1 - lane;
+                r.pi = mp_li[idx];
+                r.pj = mp_lj[idx];
+                r.pv = mp_lv[idx];
+                r.kind = 0;
+                if (!job.subpix) r.kind = 3;
+                else if (r.pi == 0 && r.pj == 0) r.kind = 1;
+                else if (r.pi - 1 < 0 || r.pi + 1 >= D || r.pj - 1 < 0 || r.pj + 1 >= D) r.kind = 2;
+                if (r.kind == 0) {
+                    r.c0 = P(r.pi, r.pj);
+                    r.yu = P(r.pi - 1, r.pj);
+                    r.yd = P(r.pi + 1, r.pj);
+                    r.xl = P(r.pi, r.pj - 1);
+                    r.xr = P(r.pi, r.pj + 1);
+                }
+            } else {
+                r.kind = 4;
+            }
+            fitq[qn + lane] = r;
+        }
+    }
 }
 
 template <int N, typename Pix>
@@ -165,7 +582,12 @@ xcorr_kernel(IaJob job) {
     cplx *scr = reg + N * RP;     // NG scratch buffers of RP complex
     uint64_t *red = reinterpret_cast<uint64_t *>(scr + NG * RP);  // 64 words
     FitRec *fitq = reinterpret_cast<FitRec *>(red + 64);           // 32 queued fits
+    float *mp_lv = reinterpret_cast<float *>(fitq + 32);           // multi-peak list (ascending)
+    int *mp_li = reinterpret_cast<int *>(mp_lv + QLPIV_MAX_PEAKS + 1);
+    int *mp_lj = mp_li + QLPIV_MAX_PEAKS + 1;
     int qn = 0;                                                    // uniform across the CTA
+    const int multi = job.num_peaks;                               // 0: FindMaximumFromCenter
+    const int KQ = multi > 0 ? multi : 1;                          // fit records per IA
 
     const int tid = threadIdx.x;
     const int g = tid % G;
@@ -176,11 +598,7 @@ xcorr_kernel(IaJob job) {
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
     const int gbase = lane & ~(G - 1);
 
-    for (int e = tid; e < M; e += T) {
-        double s, c;
-        sincospi(-2.0 * (double)e / (double)M, &s, &c);
-        tw[e] = {(float)c, (float)s};
-    }
+    for (int e = tid; e < M; e += T) tw[e] = job.twiddles[e];
     __syncthreads();
 
     for (long ia = blockIdx.x; ia < job.count; ia += gridDim.x) {
@@ -372,7 +790,13 @@ xcorr_kernel(IaJob job) {
                 // keep the plane in the row slots this pair has consumed
                 regf[2 * ((n2 >> 1) * RP + pad8(ra_)) + (n2 & 1)] = y[m].x;
                 regf[2 * ((n2 >> 1) * RP + pad8(rb_)) + (n2 & 1)] = y[m].y;
-                if (n2 >= 1 && n2 <= M - 2) {
+                if (multi > 0) {
+                    // FindMaximumMultiPeaks visits every cell of the (2N-1)^2 plane
+                    if (n2 <= M - 2) {
+                        minf = fminf(minf, y[m].x);
+                        if (rb_ <= M - 2) minf = fminf(minf, y[m].y);
+                    }
+                } else if (n2 >= 1 && n2 <= M - 2) {
                     if (ra_ >= 1) {
                         minf = fminf(minf, y[m].x);
                         const uint64_t k = peak_key(y[m].x, ra_, n2, N);
@@ -393,65 +817,71 @@ xcorr_kernel(IaJob job) {
         }
 
         // ---- 5. CTA reduction; the fit is queued and run 32 IAs at a time ----
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const uint64_t ok = __shfl_xor_sync(0xffffffffu, best, o);
-            const uint32_t oij = __shfl_xor_sync(0xffffffffu, best_ij, o);
-            if (ok > best) { best = ok; best_ij = oij; }
-            minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
-        }
-        __syncthreads();  // red[] reuse after the max reduction
-        if (lane == 0) {
-            red[warp] = best;
-            red[32 + warp] = ((uint64_t)best_ij << 32) | (uint64_t)__float_as_uint(minf);
-        }
-        __syncthreads();
-        if (warp == 0) {
-            uint64_t bk = 0ull;
-            uint32_t bij = 0u;
-            float mn = 3.402823466e38f;
-            if (lane < NWARPS) {
-                bk = red[lane];
-                bij = (uint32_t)(red[32 + lane] >> 32);
-                mn = __uint_as_float((uint32_t)red[32 + lane]);
-            }
+        auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)]; };
+        if (multi == 0) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                const uint64_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
-                const uint32_t oij = __shfl_xor_sync(0xffffffffu, bij, o);
-                // ties on the full key cannot occur between distinct cells (the rank is unique)
-                if (ok > bk) { bk = ok; bij = oij; }
-                mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+                const uint64_t ok = __shfl_xor_sync(0xffffffffu, best, o);
+                const uint32_t oij = __shfl_xor_sync(0xffffffffu, best_ij, o);
+                if (ok > best) { best = ok; best_ij = oij; }
+                minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
             }
+            __syncthreads();  // red[] reuse after the max reduction
             if (lane == 0) {
-                FitRec r;
-                r.ia = ia;
-                r.mn = mn;
-                r.pi = 0;
-                r.pj = 0;
-                r.pv = 0.0f;
-                if (bk != 0ull) {
-                    r.pi = (int)(bij >> 16);
-                    r.pj = (int)(bij & 0xffffu);
-                    r.pv = __uint_as_float((uint32_t)(bk >> 32));
-                }
-                auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)]; };
-                r.kind = 0;
-                if (!job.subpix) r.kind = 3;
-                else if (r.pi == 0 && r.pj == 0) r.kind = 1;
-                else if (r.pi - 1 < 0 || r.pi + 1 >= D || r.pj - 1 < 0 || r.pj + 1 >= D) r.kind = 2;
-                if (r.kind == 0) {
-                    r.c0 = P(r.pi, r.pj);
-                    r.yu = P(r.pi - 1, r.pj);
-                    r.yd = P(r.pi + 1, r.pj);
-                    r.xl = P(r.pi, r.pj - 1);
-                    r.xr = P(r.pi, r.pj + 1);
-                }
-                fitq[qn] = r;
+                red[warp] = best;
+                red[32 + warp] = ((uint64_t)best_ij << 32) | (uint64_t)__float_as_uint(minf);
             }
+            __syncthreads();
+            if (warp == 0) {
+                uint64_t bk = 0ull;
+                uint32_t bij = 0u;
+                float mn = 3.402823466e38f;
+                if (lane < NWARPS) {
+                    bk = red[lane];
+                    bij = (uint32_t)(red[32 + lane] >> 32);
+                    mn = __uint_as_float((uint32_t)red[32 + lane]);
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const uint64_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
+                    const uint32_t oij = __shfl_xor_sync(0xffffffffu, bij, o);
+                    // ties on the full key cannot occur between distinct cells (the rank is unique)
+                    if (ok > bk) { bk = ok; bij = oij; }
+                    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+                }
+                if (lane == 0) {
+                    FitRec r;
+                    r.ia = ia;
+                    r.mn = mn;
+                    r.pi = 0;
+                    r.pj = 0;
+                    r.pv = 0.0f;
+                    if (bk != 0ull) {
+                        r.pi = (int)(bij >> 16);
+                        r.pj = (int)(bij & 0xffffu);
+                        r.pv = __uint_as_float((uint32_t)(bk >> 32));
+                    }
+                    r.slot = 0;
+                    r.npk = 1;
+                    r.kind = 0;
+                    if (!job.subpix) r.kind = 3;
+                    else if (r.pi == 0 && r.pj == 0) r.kind = 1;
+                    else if (r.pi - 1 < 0 || r.pi + 1 >= D || r.pj - 1 < 0 || r.pj + 1 >= D) r.kind = 2;
+                    if (r.kind == 0) {
+                        r.c0 = P(r.pi, r.pj);
+                        r.yu = P(r.pi - 1, r.pj);
+                        r.yd = P(r.pi + 1, r.pj);
+                        r.xl = P(r.pi, r.pj - 1);
+                        r.xr = P(r.pi, r.pj + 1);
+                    }
+                    fitq[qn] = r;
+                }
+            }
+        } else {
+            multipeak_select<N>(job, ia, minf, regf, scr, red, fitq, qn, mp_lv, mp_li, mp_lj);
         }
-        qn++;
-        if (qn == 32) {
+        qn += KQ;
+        if (qn + KQ > 32) {
             if (warp == 0) fit_flush<D>(fitq, qn, lane, job);
             qn = 0;
         }
