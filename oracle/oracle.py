@@ -44,7 +44,7 @@ def valid_cfg(num_peaks=3, kernel_width=3, threshold=2.0, epsilon0=0.1, max_iter
 
 def build(force=False):
     """Compile the oracle with its Makefile (gcc only; seconds)."""
-    src = [HERE / "qlpiv_oracle.c", HERE / "qlpiv_oracle_adaptive.c", HERE / "qlpiv_oracle_validate.c",
+    src = [HERE / "qlpiv_oracle.c", HERE / "qlpiv_oracle_adaptive.c", HERE / "qlpiv_oracle_validate.c", HERE / "qlpiv_oracle_dense.c",
            HERE / "oracle_types.h", HERE / "oracle_impl.h", HERE / "oracle_interp_impl.h", HERE / "Makefile"]
     if not force and LIB_PATH.exists() and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in src):
         return LIB_PATH
@@ -88,6 +88,11 @@ def lib():
         L.orc_validate.argtypes = [c_int, c_int, ip, ip, fp, fp, fp, fp, ip, c_int, ctypes.POINTER(ValidCfg), vp]
         L.orc_piv_adaptive_ex.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_float,
                                           c_int, c_int, c_int, ctypes.POINTER(ValidCfg), fp, fp, ip, ip, vp, vp, vp]
+        L.orc_gauss_kernel.argtypes = [c_float, c_int, fp]
+        L.orc_gauss_filter.argtypes = [fp, c_int, c_int, fp, c_int, fp]
+        L.orc_normalize.argtypes = [fp, c_long, fp]
+        L.orc_dense_lk.argtypes = [fp, fp, c_int, c_int, fp, fp, c_int, c_int, c_int]
+        L.orc_liu_shen.argtypes = [fp, fp, c_int, c_int, fp, fp, c_float, c_int, c_int, vp, vp, vp]
         L.orc_vector_size.restype = c_int
         assert L.orc_vector_size() == VECTOR_DTYPE.itemsize
         _lib = L
@@ -381,3 +386,58 @@ def validate(tops, lefts, u, v, peak_u, peak_v, npeaks, cfg):
                                 _ptr(v, ctypes.c_float), _ptr(pu, ctypes.c_float), _ptr(pv, ctypes.c_float),
                                 _ptr(npk, ctypes.c_int), k, ctypes.byref(cfg), inv.ctypes.data)
     return u, v, inv, sweeps
+
+
+# ---------------- dense optical flow stages ----------------
+
+def gauss_kernel(sigma, px):
+    """GaussianFilter2D.createKernel weights (float)."""
+    k = np.zeros(px, np.float32)
+    lib().orc_gauss_kernel(sigma, px, _ptr(k, ctypes.c_float))
+    return k
+
+
+def gauss_filter(img, sigma, px):
+    """GaussianFilter2D.applyFilter of a 2-D image (any numeric dtype) -> float32."""
+    a = _f32(img)
+    k = gauss_kernel(sigma, px)
+    out = np.zeros_like(a)
+    lib().orc_gauss_filter(_ptr(a, ctypes.c_float), a.shape[0], a.shape[1], _ptr(k, ctypes.c_float), px,
+                           _ptr(out, ctypes.c_float))
+    return out
+
+
+def normalize(img):
+    a = _f32(img)
+    out = np.zeros_like(a)
+    lib().orc_normalize(_ptr(a, ctypes.c_float), a.size, _ptr(out, ctypes.c_float))
+    return out
+
+
+def dense_lk(img_a, img_b, us, vs, window, iterations, half_pixel=False):
+    """Dense Lucas-Kanade: returns refined (us, vs) (columns, rows)."""
+    a, b = _f32(img_a), _f32(img_b)
+    u, v = _f32(us).copy(), _f32(vs).copy()
+    lib().orc_dense_lk(_ptr(a, ctypes.c_float), _ptr(b, ctypes.c_float), a.shape[0], a.shape[1],
+                       _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), window, iterations, int(half_pixel))
+    return u, v
+
+
+def liu_shen(ls_a, ls_b, us, vs, lam, iterations, half_pixel=False, intermediates=False):
+    """Liu-Shen passes on (us, vs); with intermediates also the fixed terms (12 planes: w, IIx,
+    IIy, II, Ixt, Iyt, A11, A12, A22, B11, B12, B22) and every pass's (unew, vnew)."""
+    a, b = _f32(ls_a), _f32(ls_b)
+    u, v = _f32(us).copy(), _f32(vs).copy()
+    h, w = a.shape
+    fixed = np.zeros((12, h, w), np.float32) if intermediates else None
+    un = np.zeros((iterations, h, w), np.float32) if intermediates else None
+    vn = np.zeros((iterations, h, w), np.float32) if intermediates else None
+    passes = lib().orc_liu_shen(_ptr(a, ctypes.c_float), _ptr(b, ctypes.c_float), h, w, _ptr(u, ctypes.c_float),
+                                _ptr(v, ctypes.c_float), lam, iterations, int(half_pixel),
+                                fixed.ctypes.data if fixed is not None else None,
+                                un.ctypes.data if un is not None else None,
+                                vn.ctypes.data if vn is not None else None)
+    if intermediates:
+        return u, v, passes, fixed, un, vn
+    return u, v
+

@@ -13,6 +13,11 @@ Fixtures written (all from files shipped in the reference project):
                        IA indices.
   shift_kat.npz        testFiles/img1.png, img2.png: the synthetic pair shifted by
                        10 px used by ImageCrossCorrelationRealFFTParStdJobTests.
+  filter_edges.npz     6-pixel border bands of the Gaussian filter outputs of
+                       testFiles/GaussianFilter2D_*.matFloat (padding rules)
+  dense_golden.npz     testFiles/Python_denseLucasKanade_PyrLvs2_Fs2_0_Iter5_64x64.matFloat (window 27,
+                       1/4/5 iterations) and testFiles/Python_with_JavaLK_denseLiuShen_lambda4_*.matFloat
+                       (Liu-Shen images, Java LK input, fixed terms, 5 passes)
   filter_golden.npz    testFiles/GaussianFilter2D_*.matFloat (Gaussian prefilter
                        outputs) cropped to a 96x96 window.
 """
@@ -172,8 +177,34 @@ def main(ref):
                         names1=np.array(fn1), names2=np.array(fn2),
                         **{f"f1_{k}": m[win] for k, m in enumerate(fm1)},
                         **{f"f2_{k}": m[win] for k, m in enumerate(fm2)})
+    # filter edges: 6-pixel bands along the four image borders (the padding rules); the
+    # filtered sources testFiles/rankine_vortex01_{0,1}.tif equal rankine_pair.npz's a, b
+    src0 = read_tiff_gray(ref / "testFiles/rankine_vortex01_0.tif")
+    src1 = read_tiff_gray(ref / "testFiles/rankine_vortex01_1.tif")
+    assert (src0 == a).all() and (src1 == b).all()
+    bands = {}
+    for tag, mats in (("f1", fm1), ("f2", fm2)):
+        for k, m in enumerate(mats):
+            bands[f"{tag}_{k}_top"] = m[:6]
+            bands[f"{tag}_{k}_bottom"] = m[-6:]
+            bands[f"{tag}_{k}_left"] = m[:, :6]
+            bands[f"{tag}_{k}_right"] = m[:, -6:]
+    np.savez_compressed(HERE / "filter_edges.npz", **bands)
+
+    # dense Lucas-Kanade (window 27, no half-pixel offset) and Liu-Shen (lambda 4) fixtures
+    ln, lm = read_matfloat(ref / "testFiles/Python_denseLucasKanade_PyrLvs2_Fs2_0_Iter5_64x64.matFloat")
+    lk = dict(zip(ln, lm))
+    keep_lk = ["imageA", "imageB"] + [f"{w}LK2nd{k}_{c}" for k in (1, 4, 5) for w in ("before", "after")
+                                      for c in ("u", "v")]
+    sn, sm = read_matfloat(ref / "testFiles/Python_with_JavaLK_denseLiuShen_lambda4_Rankine_vortex_64x64.matFloat")
+    ls = dict(zip(sn, sm))
+    keep_ls = ["Im1LS_Filtered", "Im2LS_Filtered", "uLK", "vLK", "cmtx", "IIx", "IIy", "II", "Ixt", "Iyt",
+               "A11", "A12", "A22", "B11", "B12", "B22"] + [f"unews{k}" for k in range(5)] + \
+              [f"vnews{k}" for k in range(5)]
+    np.savez_compressed(HERE / "dense_golden.npz", **{f"lk_{k}": lk[k] for k in keep_lk},
+                        **{f"ls_{k}": ls[k] for k in keep_ls})
     print("shapes:", a.shape, b.shape, i1.shape, i2.shape, [m.shape for m in fm1], [m.shape for m in fm2],
-          fn1, fn2)
+          fn1, fn2, src0.shape, len(keep_lk), len(keep_ls))
 
 
 if __name__ == "__main__":

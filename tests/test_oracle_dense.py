@@ -1,0 +1,90 @@
+"""Pins the oracle's dense optical-flow stages to the reference's fixtures.
+
+* Gaussian prefilter: testFiles/GaussianFilter2D_3px_2.0f_rankine_vortex01_0.matFloat and
+  ..._5px_0.48f_rankine_vortex01_0_1.matFloat (GaussianFilter2DTest: 4e-5 and 1e-4), on an
+  interior window and on 6-pixel bands along every border (the padding rules).
+* Dense Lucas-Kanade: testFiles/Python_denseLucasKanade_PyrLvs2_Fs2_0_Iter5_64x64.matFloat, window
+  27, 1/4/5 iterations (DenseLucasKanadeGpuJTPPythonTest: 6e-3 on every pixel).
+* Liu-Shen: testFiles/Python_with_JavaLK_denseLiuShen_lambda4_Rankine_vortex_64x64.matFloat, lambda 4,
+  5 passes from the Java Lucas-Kanade field (DenseLiuShenGpuJTPTest: fixed terms 1e-5, new vectors
+  1e-3 per pass).
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+@pytest.fixture(scope="module")
+def dense():
+    return np.load(GOLDEN / "dense_golden.npz")
+
+
+def test_gauss_kernel_normalised(oracle):
+    for sigma, px in [(2.0, 3), (0.48, 5), (1.0, 7)]:
+        k = oracle.gauss_kernel(sigma, px)
+        assert abs(float(k.sum()) - 1.0) < 1e-6
+        assert np.array_equal(k, k[::-1])
+
+
+@pytest.mark.parametrize("sigma,px,tol,which", [(2.0, 3, 4e-5, ("f1_0", "a")), (0.48, 5, 1e-4, ("f2_0", "a")),
+                                                (0.48, 5, 1e-4, ("f2_1", "b"))])
+def test_gauss_filter_matches_reference(oracle, rankine_pair, sigma, px, tol, which):
+    name, src = which
+    img = rankine_pair[0] if src == "a" else rankine_pair[1]
+    out = oracle.gauss_filter(img, sigma, px)
+    win = np.load(GOLDEN / "filter_golden.npz")
+    r0, r1, c0, c1 = win["window"]
+    assert np.abs(out[r0:r1, c0:c1] - win[name]).max() <= tol
+    e = np.load(GOLDEN / "filter_edges.npz")
+    assert np.abs(out[:6] - e[f"{name}_top"]).max() <= tol
+    assert np.abs(out[-6:] - e[f"{name}_bottom"]).max() <= tol
+    assert np.abs(out[:, :6] - e[f"{name}_left"]).max() <= tol
+    assert np.abs(out[:, -6:] - e[f"{name}_right"]).max() <= tol
+
+
+def test_gauss_filter_right_padding_rule(oracle):
+    # the right border is padded with the last values in order, not mirrored: a ramp shows it
+    img = np.tile(np.arange(8, dtype=np.float32) ** 2, (3, 1))
+    out = oracle.gauss_filter(img, 0.8, 5)
+    k = oracle.gauss_kernel(0.8, 5)
+    row = img[0]
+    padded = np.concatenate([row[1::-1], row, row[-2:]])     # left: mirror with edge, right: copy
+    f32 = np.float32
+    exp = []
+    for j in range(8):
+        acc = f32(0)
+        for q in range(5):
+            acc = f32(acc + f32(padded[j + 4 - q] * k[q]))
+        exp.append(acc)
+    # the column pass of a constant column returns the row value (weights sum to 1 within rounding)
+    assert np.abs(out[1] - np.array(exp, np.float32)).max() < 1e-4
+
+
+def test_normalize(oracle):
+    a = np.array([[0.0, 2.0], [4.0, 1.0]], np.float32)
+    assert np.array_equal(oracle.normalize(a), a / np.float32(4.0))
+
+
+@pytest.mark.parametrize("iters", [1, 4, 5])
+def test_dense_lk_matches_python_fixture(oracle, dense, iters):
+    a, b = dense["lk_imageA"], dense["lk_imageB"]
+    u0, v0 = dense[f"lk_beforeLK2nd{iters}_u"], dense[f"lk_beforeLK2nd{iters}_v"]
+    u, v = oracle.dense_lk(a, b, u0, v0, 27, iters, half_pixel=False)
+    assert np.abs(u - dense[f"lk_afterLK2nd{iters}_u"]).max() <= 6e-3
+    assert np.abs(v - dense[f"lk_afterLK2nd{iters}_v"]).max() <= 6e-3
+    assert np.abs(u - u0).max() > 1e-2      # the iterations moved the field
+
+
+def test_liu_shen_matches_python_fixture(oracle, dense):
+    la, lb = dense["ls_Im1LS_Filtered"], dense["ls_Im2LS_Filtered"]
+    us, vs = dense["ls_uLK"], dense["ls_vLK"]
+    u, v, passes, fixed, un, vn = oracle.liu_shen(la, lb, us, vs, 4.0, 5, half_pixel=False, intermediates=True)
+    assert passes == 5
+    for q, name in enumerate(["cmtx", "IIx", "IIy", "II", "Ixt", "Iyt", "A11", "A12", "A22", "B11", "B12", "B22"]):
+        assert np.abs(fixed[q] - dense[f"ls_{name}"]).max() <= 1e-5, name
+    for k in range(5):
+        assert np.abs(un[k] - dense[f"ls_unews{k}"]).max() <= 1e-3, k
+        assert np.abs(vn[k] - dense[f"ls_vnews{k}"]).max() <= 1e-3, k
+    # output orientation: columns <- vnew, rows <- unew of the last pass
+    assert np.array_equal(u, vn[-1]) and np.array_equal(v, un[-1])
