@@ -324,6 +324,30 @@ qlpiv_status qlpiv_inherit_noalloc(int device, void *stream, int pni, int pnj, c
                                    const float *pu, const float *pv, int cni, int cnj, const float *c_ci,
                                    const float *c_cj, int round_int, float *cu, float *cv);
 
+/* ---- Dense optical flow after PIV (LiuShenWithLucasKanade / LucasKanade interpolators) ---- */
+
+/* GaussianFilter2D.applyFilter (S/images/filters/GaussianFilter2D.java:31-128,
+ * GaussianFilter2DInternal.java:49-97): separable Gaussian of `kernel_px` (odd) points and
+ * `sigma`, rows then columns, the reference's border padding; img of pixel_type (height x width,
+ * contiguous rows) -> out float.  sigma < 1e-5 copies the image.  Host arrays; synchronous. */
+qlpiv_status qlpiv_gaussian_filter(qlpiv_handle *h, int pixel_type, const void *img, int height, int width,
+                                   float sigma, int kernel_px, float *out);
+/* ImageFloat.normalize (S/images/ImageFloat.java:571-596): out = img / max.  Host arrays. */
+qlpiv_status qlpiv_normalize(qlpiv_handle *h, const float *img, int height, int width, float *out);
+/* DenseLucasKanadeAparapiJob.compute (S/jobs/interpolators/DenseLucasKanadeAparapiJob.java:56-215,
+ * DenseLucasKanadeGpuKernel.java:203-751): dense Lucas-Kanade on two (filtered) float images;
+ * us (columns) / vs (rows) hold the initial field and receive the result.  window odd 3..31,
+ * iterations >= 1, half_pixel: the 2x2-average sampling (half-pixel offset).  Host arrays. */
+qlpiv_status qlpiv_dense_lk(qlpiv_handle *h, const float *img_a, const float *img_b, int height, int width, float *us,
+                            float *vs, int window, int iterations, int half_pixel);
+/* DenseLiuShenAparapiJob.compute (S/jobs/interpolators/DenseLiuShenAparapiJob.java:64-255,
+ * DenseLiuShenGpuKernel.java:66-588): the Lucas-Kanade pass on lk_a/lk_b (skipped when
+ * iterations_lk == 0) followed by iterations_ls Liu-Shen passes with multiplier lambda on the
+ * (filtered, normalised) images ls_a/ls_b.  us (columns) / vs (rows) in and out.  Host arrays. */
+qlpiv_status qlpiv_liu_shen(qlpiv_handle *h, const float *lk_a, const float *lk_b, const float *ls_a,
+                            const float *ls_b, int height, int width, float *us, float *vs, int window,
+                            int iterations_lk, float lambda, int iterations_ls, int half_pixel);
+
 /* Stage timing of the adaptive pipeline (CUDA events around every launch on the
  * handle's stream).  Accumulates while enabled; qlpiv_profile_read synchronises the
  * stream, returns the totals per (stage, level) and clears them. */

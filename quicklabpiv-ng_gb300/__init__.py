@@ -150,6 +150,10 @@ _SIGNATURES = {
     "qlpiv_piv_adaptive": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
     "qlpiv_piv_adaptive_device": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
     "qlpiv_inherit_noalloc": (_i, [_i, _vp, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp]),
+    "qlpiv_gaussian_filter": (_i, [_vp, _i, _vp, _i, _i, _f, _i, _vp]),
+    "qlpiv_normalize": (_i, [_vp, _vp, _i, _i, _vp]),
+    "qlpiv_dense_lk": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp, _i, _i, _i]),
+    "qlpiv_liu_shen": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _i, _f, _i, _i]),
     "qlpiv_profile_enable": (_i, [_vp, _i]),
     "qlpiv_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(_i)]),
 }
@@ -495,6 +499,45 @@ class Handle:
         _check(self._lib.qlpiv_validate(self._h, ctypes.byref(desc), ni, nj, _addr(tops), _addr(lefts), _addr(u),
                                         _addr(v), _addr(pu), _addr(pv), _addr(npk), _addr(inv)))
         return u, v, inv
+
+    # -- dense optical flow ------------------------------------------------------
+    def gaussian_filter(self, img, sigma, kernel_px):
+        """GaussianFilter2D of a 2-D u8 / u16 / f32 image -> float32."""
+        a = np.ascontiguousarray(img)
+        out = np.empty(a.shape, np.float32)
+        _check(self._lib.qlpiv_gaussian_filter(self._h, pixel_type_of(a.dtype), _addr(a), a.shape[0], a.shape[1],
+                                               float(sigma), int(kernel_px), _addr(out)))
+        return out
+
+    def normalize(self, img):
+        a = np.ascontiguousarray(img, np.float32)
+        out = np.empty_like(a)
+        _check(self._lib.qlpiv_normalize(self._h, _addr(a), a.shape[0], a.shape[1], _addr(out)))
+        return out
+
+    def dense_lk(self, img_a, img_b, us, vs, window, iterations, half_pixel=False):
+        """Dense Lucas-Kanade; returns refined (us, vs) (columns, rows)."""
+        a = np.ascontiguousarray(img_a, np.float32)
+        b = np.ascontiguousarray(img_b, np.float32)
+        u = np.array(us, np.float32, order="C", copy=True)
+        v = np.array(vs, np.float32, order="C", copy=True)
+        _check(self._lib.qlpiv_dense_lk(self._h, _addr(a), _addr(b), a.shape[0], a.shape[1], _addr(u), _addr(v),
+                                        int(window), int(iterations), int(half_pixel)))
+        return u, v
+
+    def liu_shen(self, ls_a, ls_b, us, vs, lam, iterations_ls, lk_a=None, lk_b=None, window=27, iterations_lk=0,
+                 half_pixel=False):
+        """Lucas-Kanade pass (iterations_lk > 0) then Liu-Shen passes; returns (us, vs)."""
+        la = np.ascontiguousarray(ls_a, np.float32)
+        lb = np.ascontiguousarray(ls_b, np.float32)
+        ka = np.ascontiguousarray(lk_a, np.float32) if lk_a is not None else None
+        kb = np.ascontiguousarray(lk_b, np.float32) if lk_b is not None else None
+        u = np.array(us, np.float32, order="C", copy=True)
+        v = np.array(vs, np.float32, order="C", copy=True)
+        _check(self._lib.qlpiv_liu_shen(self._h, _addr(ka), _addr(kb), _addr(la), _addr(lb), la.shape[0], la.shape[1],
+                                        _addr(u), _addr(v), int(window), int(iterations_lk), float(lam),
+                                        int(iterations_ls), int(half_pixel)))
+        return u, v
 
     def piv_adaptive(self, frames_a, frames_b, desc):
         """Adaptive multi-pass PIV of image pairs of one size; returns (u, v) of the last

@@ -22,7 +22,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3,
                      "-I", str(ROOT / "include"), "-I", str(CSRC)]
 # Per-file device flags: the adaptive stages are bit-identical to the CPU oracle only
 # without FMA contraction.
-FILE_FLAGS = {"qlpiv_adaptive.cu": ["--fmad=false"], "qlpiv_validate.cu": ["--fmad=false"]}
+FILE_FLAGS = {"qlpiv_adaptive.cu": ["--fmad=false"], "qlpiv_validate.cu": ["--fmad=false"],
+              "qlpiv_dense.cu": ["--fmad=false"]}
 
 
 def _nvcc():

@@ -377,12 +377,13 @@ __global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, 
 
 // Per-pixel field only (test hook for the field stage): pair 0, outputs h x w floats.
 __global__ void field_kernel(int h, int w, const float *ys, int ni, const float *xs, int nj, const float4 *c4u,
-                             const float4 *c4v, float *fu_out, float *fv_out) {
+                             const float4 *c4v, float off_y, float off_x, float *fu_out, float *fv_out) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= h || j >= w) return;
     const float ymin = ys[0], ymax = ys[ni - 1], xmin = xs[0], xmax = xs[nj - 1];
-    float y = (float)i, x = (float)j;
+    // pixel i is evaluated at off_y + i (the reference steps a float from the offset by 1.0f)
+    float y = off_y + (float)i, x = off_x + (float)j;
     if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
     if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
     fu_out[(long)i * w + j] = field_value(ys, ni, xs, nj, c4u, y, x);
@@ -444,9 +445,9 @@ cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w,
 }
 
 cudaError_t launch_field(cudaStream_t s, int h, int w, const float *ys, int ni, const float *xs, int nj,
-                         SplineCoef coef, float *fu, float *fv) {
+                         SplineCoef coef, float *fu, float *fv, float off_y, float off_x) {
     dim3 blk(32, 8), grd(blocks_for(w, 32), blocks_for(h, 8), 1);
-    field_kernel<<<grd, blk, 0, s>>>(h, w, ys, ni, xs, nj, coef.c4_u, coef.c4_v, fu, fv);
+    field_kernel<<<grd, blk, 0, s>>>(h, w, ys, ni, xs, nj, coef.c4_u, coef.c4_v, off_y, off_x, fu, fv);
     return cudaGetLastError();
 }
 

@@ -26,8 +26,9 @@ cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const dou
 cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
                         const qlpiv_frame *dst, const float *ys, int ni, const float *xs, int nj, SplineCoef coef,
                         int int16_quirk);
+// Per-pixel field; pixel (i, j) is evaluated at (off_y + i, off_x + j), clamped to the knot box.
 cudaError_t launch_field(cudaStream_t s, int h, int w, const float *ys, int ni, const float *xs, int nj,
-                         SplineCoef coef, float *fu, float *fv);
+                         SplineCoef coef, float *fu, float *fv, float off_y = 0.0f, float off_x = 0.0f);
 cudaError_t launch_displaced_origins(cudaStream_t s, long count, const int *a_top, const int *a_left, const float *u,
                                      const float *v, int *b_top, int *b_left);
 

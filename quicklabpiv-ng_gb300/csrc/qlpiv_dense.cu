@@ -1,0 +1,579 @@
+// Dense optical flow after PIV (device code and C ABI).
+//
+//   C-filter  GaussianFilter2D (S/images/filters/GaussianFilter2D.java:31-46,
+//             S/images/filters/GaussianFilter2DInternal.java:49-97, DirectConvolution.java:14-53):
+//             rows, then columns of the row result; a line of n values is padded on the
+//             left with its first h values mirrored (edge repeated) and on the right with its
+//             last h values in order; out[j] accumulates in[j + h - q] * k[q], q = 0..2h.
+//             ImageFloat.normalize (S/images/ImageFloat.java:571-596).
+//   C-LK      DenseLucasKanadeGpuKernel (S/jobs/interpolators/DenseLucasKanadeGpuKernel.java:203-751):
+//             one thread per pixel, a 16 x 16 pixel tile per CTA.  The CTA stages the image-A
+//             region its windows span (clamped; 2x2 averages for the half-pixel offset) and
+//             the derivatives (3, 10, 3) / 32 of every window point once in shared memory;
+//             each thread then sums its W x W A matrix and, per iteration, its b vector from
+//             bilinear samples of image B.
+//   C-LS      DenseLiuShenGpuKernel (S/jobs/interpolators/DenseLiuShenGpuKernel.java:66-588):
+//             fixed-image terms once per pixel, then one Jacobi pass per launch; the pass
+//             reads the previous pass's total error on the device and becomes a copy once
+//             the mean error is below 1e-8.
+// Sums run in window row-major order with IEEE single operations and no contraction
+// (--fmad=false), the order of the CPU oracle's restatement: every stage is bit-identical
+// to it.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "qlpiv_adaptive.h"
+#include "qlpiv_dense.h"
+#include "qlpiv_handle.h"
+#include "qlpiv_internal.h"
+
+namespace qlpiv {
+
+namespace {
+
+int blocks_of(long n, int b) { return (int)((n + b - 1) / b); }
+
+// ---------------- Gaussian prefilter ----------------
+
+__device__ __forceinline__ int filter_index(int x, int n, int h) {
+    if (x < 0) return -1 - x;          // mirrored, edge repeated
+    if (x >= n) return n - h + (x - n);  // the last h values, in order
+    return x;
+}
+
+template <typename Pix>
+__global__ void gauss_rows_kernel(const Pix *in, long pitch, int h, int w, const float *k, int K, float *out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= h || j >= w) return;
+    const int hk = K / 2;
+    const Pix *row = in + (long)i * pitch;
+    float acc = 0.0f;
+    for (int q = 0; q < K; q++) acc = __fadd_rn(acc, __fmul_rn((float)row[filter_index(j + hk - q, w, hk)], k[q]));
+    out[(long)i * w + j] = acc;
+}
+
+__global__ void gauss_cols_kernel(const float *in, int h, int w, const float *k, int K, float *out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= h || j >= w) return;
+    const int hk = K / 2;
+    float acc = 0.0f;
+    for (int q = 0; q < K; q++)
+        acc = __fadd_rn(acc, __fmul_rn(in[(long)filter_index(i + hk - q, h, hk) * w + j], k[q]));
+    out[(long)i * w + j] = acc;
+}
+
+// max of the non-negative values (the reference's running max starts at 0)
+__global__ void max_kernel(const float *in, long n, unsigned *mx) {
+    float m = 0.0f;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        m = fmaxf(m, in[q] > 0.0f ? in[q] : 0.0f);
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(mx, __float_as_uint(m));
+}
+
+__global__ void divide_kernel(const float *in, long n, const unsigned *mx, float *out) {
+    const float m = __uint_as_float(*mx);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        out[q] = __fdiv_rn(in[q], m);
+}
+
+// ---------------- dense Lucas-Kanade ----------------
+
+constexpr int kLkTile = 16;
+
+__device__ __forceinline__ float clamp_read(const float *img, int h, int w, int i, int j) {
+    i = i < 0 ? 0 : (i > h - 1 ? h - 1 : i);
+    j = j < 0 ? 0 : (j > w - 1 ? w - 1 : j);
+    return img[(long)i * w + j];
+}
+
+// readPixelWithWarp: anchor at the floor, bilinear weights, clamped reads
+__device__ __forceinline__ float warp_read(const float *img, int h, int w, float li, float lj) {
+    int i = (int)li, j = (int)lj;
+    float di = __fsub_rn(li, (float)i), dj = __fsub_rn(lj, (float)j);
+    const int si = di < 0.0f ? 1 : 0;
+    i -= si;
+    di = __fadd_rn(di, (float)si);
+    const int sj = dj < 0.0f ? 1 : 0;
+    j -= sj;
+    dj = __fadd_rn(dj, (float)sj);
+    const float omj = __fsub_rn(1.0f, dj), omi = __fsub_rn(1.0f, di);
+    const float top = __fadd_rn(__fmul_rn(omj, clamp_read(img, h, w, i, j)), __fmul_rn(dj, clamp_read(img, h, w, i, j + 1)));
+    const float bot =
+        __fadd_rn(__fmul_rn(omj, clamp_read(img, h, w, i + 1, j)), __fmul_rn(dj, clamp_read(img, h, w, i + 1, j + 1)));
+    return __fadd_rn(__fmul_rn(omi, top), __fmul_rn(di, bot));
+}
+
+__global__ void __launch_bounds__(kLkTile *kLkTile) dense_lk_kernel(const float *A, const float *B, int h, int w,
+                                                                     float *us, float *vs, int W, int iterations,
+                                                                     int half_pixel) {
+    extern __shared__ float sm[];
+    const int hw = W / 2;
+    const int RS = kLkTile + W + 1;  // staged region side: window span + derivative margin
+    const int GS = kLkTile + W - 1;  // window points of the tile
+    float *reg = sm;
+    float *val = reg + RS * RS;
+    float *gdj = val + GS * GS;
+    float *gdi = gdj + GS * GS;
+    const int tid = threadIdx.y * kLkTile + threadIdx.x;
+    const int ti0 = blockIdx.y * kLkTile, tj0 = blockIdx.x * kLkTile;
+    for (int q = tid; q < RS * RS; q += kLkTile * kLkTile) {
+        const int r = q / RS, c = q - r * RS;
+        const int y = ti0 - hw - 1 + r, x = tj0 - hw - 1 + c;
+        if (half_pixel) {
+            const float s = __fadd_rn(__fadd_rn(__fadd_rn(clamp_read(A, h, w, y, x), clamp_read(A, h, w, y, x + 1)),
+                                                clamp_read(A, h, w, y + 1, x)),
+                                      clamp_read(A, h, w, y + 1, x + 1));
+            reg[q] = __fdiv_rn(s, 4.0f);
+        } else {
+            reg[q] = clamp_read(A, h, w, y, x);
+        }
+    }
+    __syncthreads();
+    const float c3 = 3.0f / 32.0f;
+    for (int q = tid; q < GS * GS; q += kLkTile * kLkTile) {
+        const int gy = q / GS, gx = q - gy * GS;
+        const float *r0 = reg + gy * RS + gx, *r1 = r0 + RS, *r2 = r1 + RS;
+        const float TL = r0[0], T = r0[1], TR = r0[2], L = r1[0], C = r1[1], R = r1[2], BL = r2[0], Bt = r2[1],
+                    BR = r2[2];
+        const float dj = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TL, BL), TR), BR), c3),
+                                   __fdiv_rn(__fmul_rn(__fsub_rn(L, R), 10.0f), 32.0f));
+        const float di = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TR, TL), BR), BL), c3),
+                                   __fdiv_rn(__fmul_rn(__fsub_rn(T, Bt), 10.0f), 32.0f));
+        val[q] = C;
+        gdj[q] = dj;
+        gdi[q] = di;
+    }
+    __syncthreads();
+    const int pi = ti0 + threadIdx.y, pj = tj0 + threadIdx.x;
+    if (pi >= h || pj >= w) return;
+    float a00 = 0.0f, a01 = 0.0f, a11 = 0.0f;
+    for (int a = 0; a < W; a++) {
+        const int base = (threadIdx.y + a) * GS + threadIdx.x;
+        for (int b = 0; b < W; b++) {
+            const float dj = gdj[base + b], di = gdi[base + b];
+            a00 = __fadd_rn(__fmul_rn(dj, dj), a00);
+            a01 = __fadd_rn(__fmul_rn(dj, di), a01);
+            a11 = __fadd_rn(__fmul_rn(di, di), a11);
+        }
+    }
+    const long p = (long)pi * w + pj;
+    bool active = true;
+    const float det = __fadd_rn(__fmul_rn(a00, a11), -__fmul_rn(a01, a01));
+    if (det < 1.192092896e-7f) active = false;
+    const float i00 = __fdiv_rn(a11, det), i01 = __fdiv_rn(-a01, det), i11 = __fdiv_rn(a00, det);
+    float locI = __fadd_rn((float)pi, vs[p]), locJ = __fadd_rn((float)pj, us[p]);
+    if (half_pixel) {
+        locI = __fadd_rn(locI, 0.5f);
+        locJ = __fadd_rn(locJ, 0.5f);
+    }
+    for (int it = 0; it < iterations && active; it++) {
+        if (locI < 0.0f || locI >= (float)(h + hw) || locJ < 0.0f || locJ >= (float)(w + hw)) break;
+        float b0 = 0.0f, b1 = 0.0f;
+        const float oi = __fsub_rn(locI, (float)hw), oj = __fsub_rn(locJ, (float)hw);
+        for (int a = 0; a < W; a++) {
+            const int base = (threadIdx.y + a) * GS + threadIdx.x;
+            const float li = __fadd_rn(oi, (float)a);
+            for (int b = 0; b < W; b++) {
+                const float dT = __fsub_rn(warp_read(B, h, w, li, __fadd_rn(oj, (float)b)), val[base + b]);
+                b0 = __fadd_rn(__fmul_rn(dT, gdj[base + b]), b0);
+                b1 = __fadd_rn(__fmul_rn(dT, gdi[base + b]), b1);
+            }
+        }
+        const float incU = __fadd_rn(__fmul_rn(b0, i00), __fmul_rn(b1, i01));
+        const float incV = __fadd_rn(__fmul_rn(b0, i01), __fmul_rn(b1, i11));
+        if (fabsf(incU) < 1e-3f && fabsf(incV) < 1e-3f) break;
+        locI = __fadd_rn(locI, incV);
+        locJ = __fadd_rn(locJ, incU);
+    }
+    float v = __fsub_rn(locI, (float)pi), u = __fsub_rn(locJ, (float)pj);
+    if (half_pixel) {
+        v = __fsub_rn(v, 0.5f);
+        u = __fsub_rn(u, 0.5f);
+    }
+    vs[p] = v;
+    us[p] = u;
+}
+
+size_t lk_smem(int W) {
+    const int RS = kLkTile + W + 1, GS = kLkTile + W - 1;
+    return sizeof(float) * ((size_t)RS * RS + 3 * (size_t)GS * GS);
+}
+
+// ---------------- Liu-Shen ----------------
+
+enum { kTL = 0, kT = 1, kTR = 2, kL = 3, kC = 4, kR = 5, kBL = 6, kB = 7, kBR = 8 };
+
+__device__ __forceinline__ void ls_load(const float *img, int h, int w, int pi, int pj, int half_pixel, float *n9) {
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) {
+            const int y = pi - 1 + a, x = pj - 1 + b;
+            float v;
+            if (half_pixel) {
+                v = 0.0f;
+                for (int i = 0; i < 2; i++)
+                    for (int j = 0; j < 2; j++) v = __fadd_rn(__fmul_rn(clamp_read(img, h, w, y + i, x + j), 0.25f), v);
+            } else {
+                v = clamp_read(img, h, w, y, x);
+            }
+            n9[a * 3 + b] = v;
+        }
+}
+
+__device__ __forceinline__ void ls_weights(int pi, int pj, int h, int w, float *wq) {
+    wq[kTL] = (pi - 1) >= 0 && (pj - 1) >= 0 && (pi - 1) < h && (pj - 1) < w ? 1.0f : 0.0f;
+    wq[kT] = (pi - 1) >= 0 && (pi - 1) < h && pj < w ? 1.0f : 0.0f;
+    wq[kTR] = (pi - 1) >= 0 && (pj + 1) >= 0 && (pi - 1) < h && (pj + 1) < w ? 1.0f : 0.0f;
+    wq[kL] = (pj - 1) >= 0 && pi < h && (pj - 1) < w ? 1.0f : 0.0f;
+    wq[kC] = 0.0f;
+    wq[kR] = pi < h && (pj + 1) < w ? 1.0f : 0.0f;
+    wq[kBL] = (pj - 1) >= 0 && (pi + 1) < h && (pj - 1) < w ? 1.0f : 0.0f;
+    wq[kB] = (pi + 1) < h && pj < w ? 1.0f : 0.0f;
+    wq[kBR] = (pi + 1) < h && (pj + 1) < w ? 1.0f : 0.0f;
+}
+
+// Fixed terms, 8 planes of h x w: IIx, IIy, II, Ixt, Iyt, B11, B12, B22.
+__global__ void ls_fixed_kernel(const float *la, const float *lb, int h, int w, float lambda, int half_pixel,
+                                float *fx) {
+    const int pj = blockIdx.x * blockDim.x + threadIdx.x, pi = blockIdx.y * blockDim.y + threadIdx.y;
+    if (pi >= h || pj >= w) return;
+    float a9[9], b9[9], wq[9];
+    ls_load(la, h, w, pi, pj, half_pixel, a9);
+    ls_load(lb, h, w, pi, pj, half_pixel, b9);
+    ls_weights(pi, pj, h, w, wq);
+    const int ring[8] = {kTL, kT, kTR, kL, kR, kBL, kB, kBR};
+    float ws = 0.0f;
+#pragma unroll
+    for (int t = 0; t < 8; t++) ws = __fadd_rn(ws, wq[ring[t]]);
+    const float c = a9[kC], c2 = __fmul_rn(2.0f, c);
+    const float IIx = __fdiv_rn(__fmul_rn(c, __fsub_rn(a9[kB], a9[kT])), 2.0f);
+    const float IIy = __fdiv_rn(__fmul_rn(c, __fsub_rn(a9[kR], a9[kL])), 2.0f);
+    const float II = __fmul_rn(c, c);
+    const float Ixt =
+        __fdiv_rn(__fmul_rn(c, __fsub_rn(__fsub_rn(b9[kB], a9[kB]), __fsub_rn(b9[kT], a9[kT]))), 2.0f);
+    const float Iyt =
+        __fdiv_rn(__fmul_rn(c, __fsub_rn(__fsub_rn(b9[kR], a9[kR]), __fsub_rn(b9[kL], a9[kL]))), 2.0f);
+    const float lw = -__fmul_rn(lambda, ws);
+    const float A11 = __fadd_rn(__fmul_rn(c, __fsub_rn(__fsub_rn(__fadd_rn(a9[kB], a9[kT]), c2), c2)), lw);
+    const float A22 = __fadd_rn(__fmul_rn(c, __fsub_rn(__fsub_rn(__fadd_rn(a9[kR], a9[kL]), c2), c2)), lw);
+    const float A12 =
+        __fdiv_rn(__fmul_rn(c, __fadd_rn(__fsub_rn(__fsub_rn(a9[kTL], a9[kTR]), a9[kBL]), a9[kBR])), 4.0f);
+    const float det = __fadd_rn(__fmul_rn(A11, A22), -__fmul_rn(A12, A12));
+    const long n = (long)h * w, p = (long)pi * w + pj;
+    fx[0 * n + p] = IIx;
+    fx[1 * n + p] = IIy;
+    fx[2 * n + p] = II;
+    fx[3 * n + p] = Ixt;
+    fx[4 * n + p] = Iyt;
+    fx[5 * n + p] = __fdiv_rn(A22, det);
+    fx[6 * n + p] = __fdiv_rn(-A12, det);
+    fx[7 * n + p] = __fdiv_rn(A11, det);
+}
+
+// One Jacobi pass: (us_in, vs_in) -> (us_out, vs_out); err[pass] accumulates the pass's
+// total error (double).  Once the previous pass's mean error is below 1e-8 the pass copies.
+__global__ void ls_pass_kernel(const float *fx, int h, int w, float lambda, const float *us_in, const float *vs_in,
+                               float *us_out, float *vs_out, double *err, int pass) {
+    const int pj = blockIdx.x * blockDim.x + threadIdx.x, pi = blockIdx.y * blockDim.y + threadIdx.y;
+    const long n = (long)h * w;
+    const bool stop = pass > 0 && err[pass - 1] / (double)n < 1e-8;
+    double e = 0.0;
+    if (pi < h && pj < w) {
+        const long p = (long)pi * w + pj;
+        if (stop) {
+            us_out[p] = us_in[p];
+            vs_out[p] = vs_in[p];
+        } else {
+            float U[9], V[9], wq[9];
+            ls_load(us_in, h, w, pi, pj, 0, U);
+            ls_load(vs_in, h, w, pi, pj, 0, V);
+            ls_weights(pi, pj, h, w, wq);
+            const float IIx = fx[0 * n + p], IIy = fx[1 * n + p], II = fx[2 * n + p];
+            const float Ixt = fx[3 * n + p], Iyt = fx[4 * n + p];
+            const float B11 = fx[5 * n + p], B12 = fx[6 * n + p], B22 = fx[7 * n + p];
+            const int ring[7] = {kT, kTR, kL, kR, kBL, kB, kBR};
+            float sV = __fmul_rn(V[kTL], wq[kTL]), sU = __fmul_rn(U[kTL], wq[kTL]);
+#pragma unroll
+            for (int t = 0; t < 7; t++) {
+                const int q = ring[t];
+                sV = __fadd_rn(sV, __fmul_rn(V[q], wq[q]));
+                sU = __fadd_rn(sU, __fmul_rn(U[q], wq[q]));
+            }
+            const float hu = __fadd_rn(__fmul_rn(lambda, sV), Ixt);
+            const float hv = __fadd_rn(__fmul_rn(lambda, sU), Iyt);
+            const float u_xy = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(U[kTL], U[kTR]), U[kBL]), U[kBR]), 4.0f);
+            const float v_xy = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(V[kTL], V[kTR]), V[kBL]), V[kBR]), 4.0f);
+            const float bu = __fadd_rn(
+                __fmul_rn(__fmul_rn(2.0f, IIx), __fdiv_rn(__fsub_rn(V[kB], V[kT]), 2.0f)),
+                __fadd_rn(__fmul_rn(IIx, __fdiv_rn(__fsub_rn(U[kR], U[kL]), 2.0f)),
+                          __fadd_rn(__fmul_rn(IIy, __fdiv_rn(__fsub_rn(U[kB], U[kT]), 2.0f)),
+                                    __fadd_rn(__fmul_rn(II, __fadd_rn(V[kT], V[kB])), __fadd_rn(__fmul_rn(II, u_xy), hu)))));
+            const float bv = __fadd_rn(
+                __fmul_rn(__fmul_rn(2.0f, IIy), __fdiv_rn(__fsub_rn(U[kR], U[kL]), 2.0f)),
+                __fadd_rn(__fmul_rn(IIx, __fdiv_rn(__fsub_rn(V[kR], V[kL]), 2.0f)),
+                          __fadd_rn(__fmul_rn(IIy, __fdiv_rn(__fsub_rn(V[kB], V[kT]), 2.0f)),
+                                    __fadd_rn(__fmul_rn(II, __fadd_rn(U[kL], U[kR])), __fadd_rn(__fmul_rn(II, v_xy), hv)))));
+            const float unew = -__fadd_rn(__fmul_rn(B11, bu), __fmul_rn(B12, bv));
+            const float vnew = -__fadd_rn(__fmul_rn(B12, bu), __fmul_rn(B22, bv));
+            const float du = __fsub_rn(unew, V[kC]), dv = __fsub_rn(vnew, U[kC]);
+            e = (double)__fsqrt_rn(__fadd_rn(__fmul_rn(du, du), __fmul_rn(dv, dv)));
+            us_out[p] = vnew;  // columns <- vnew, rows <- unew (copyVectors)
+            vs_out[p] = unew;
+        }
+    }
+    if (stop) {
+        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) err[pass] = err[pass - 1];
+        return;
+    }
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if (((threadIdx.y * blockDim.x + threadIdx.x) & 31) == 0 && e != 0.0) atomicAdd(&err[pass], e);
+}
+
+}  // namespace
+
+void gauss_weights(float sigma, int px, float *k) {
+    std::vector<double> kd(px);
+    const int half = px / 2;
+    double sum = 0.0;
+    for (int i = 0; i < px; i++) {
+        const double x = i - half, s = (double)sigma;
+        kd[i] = 1.0 / std::sqrt(2.0 * M_PI * s * s) * std::exp(-x * x / (2.0 * s * s));
+        sum += kd[i];
+    }
+    for (int i = 0; i < px; i++) k[i] = (float)(kd[i] / sum);
+}
+
+cudaError_t launch_gauss(cudaStream_t s, int pixel_type, const void *in, long pitch, int h, int w, const float *k,
+                         int K, float *tmp, float *out) {
+    dim3 blk(32, 8), grd(blocks_of(w, 32), blocks_of(h, 8));
+    switch (pixel_type) {
+        case QLPIV_PIX_U8:
+            gauss_rows_kernel<uint8_t><<<grd, blk, 0, s>>>((const uint8_t *)in, pitch, h, w, k, K, tmp);
+            break;
+        case QLPIV_PIX_U16:
+            gauss_rows_kernel<uint16_t><<<grd, blk, 0, s>>>((const uint16_t *)in, pitch, h, w, k, K, tmp);
+            break;
+        default:
+            gauss_rows_kernel<float><<<grd, blk, 0, s>>>((const float *)in, pitch, h, w, k, K, tmp);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    gauss_cols_kernel<<<grd, blk, 0, s>>>(tmp, h, w, k, K, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_normalize(cudaStream_t s, const float *in, long n, unsigned *mx, float *out) {
+    cudaError_t e = cudaMemsetAsync(mx, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    const int blocks = blocks_of(n, 256) < 1024 ? blocks_of(n, 256) : 1024;
+    max_kernel<<<blocks, 256, 0, s>>>(in, n, mx);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    divide_kernel<<<blocks, 256, 0, s>>>(in, n, mx, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dense_lk(cudaStream_t s, const float *a, const float *b, int h, int w, float *us, float *vs, int W,
+                            int iterations, int half_pixel) {
+    const size_t sm = lk_smem(W);
+    dim3 blk(kLkTile, kLkTile), grd(blocks_of(w, kLkTile), blocks_of(h, kLkTile));
+    dense_lk_kernel<<<grd, blk, sm, s>>>(a, b, h, w, us, vs, W, iterations, half_pixel);
+    return cudaGetLastError();
+}
+
+// Liu-Shen passes on (us, vs) in place; fx: 8 planes, tmp: 2 planes, err: `iterations` doubles.
+cudaError_t launch_liu_shen(cudaStream_t s, const float *la, const float *lb, int h, int w, float *us, float *vs,
+                            float lambda, int iterations, int half_pixel, float *fx, float *tmp, double *err) {
+    dim3 blk(32, 8), grd(blocks_of(w, 32), blocks_of(h, 8));
+    const long n = (long)h * w;
+    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(double) * iterations, s);
+    if (e != cudaSuccess) return e;
+    ls_fixed_kernel<<<grd, blk, 0, s>>>(la, lb, h, w, lambda, half_pixel, fx);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    float *cu = us, *cv = vs, *nu = tmp, *nv = tmp + n;
+    for (int it = 0; it < iterations; it++) {
+        ls_pass_kernel<<<grd, blk, 0, s>>>(fx, h, w, lambda, cu, cv, nu, nv, err, it);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        float *t = cu; cu = nu; nu = t;
+        t = cv; cv = nv; nv = t;
+    }
+    if (cu != us) {  // odd pass count: the result sits in tmp
+        if ((e = cudaMemcpyAsync(us, cu, sizeof(float) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(vs, cv, sizeof(float) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace qlpiv
+
+using namespace qlpiv;
+
+namespace {
+
+qlpiv_status check_image(int pixel_type, int height, int width) {
+    if (pixel_type != QLPIV_PIX_U8 && pixel_type != QLPIV_PIX_U16 && pixel_type != QLPIV_PIX_F32)
+        return fail(QLPIV_E_ARG, "unknown pixel type %d", pixel_type);
+    if (height < 1 || width < 1) return fail(QLPIV_E_SHAPE, "image size %d x %d", height, width);
+    return QLPIV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+qlpiv_status qlpiv_gaussian_filter(qlpiv_handle *h, int pixel_type, const void *img, int height, int width,
+                                   float sigma, int kernel_px, float *out) {
+    if (!h || !img || !out) return fail(QLPIV_E_ARG, "NULL argument");
+    qlpiv_status st = check_image(pixel_type, height, width);
+    if (st != QLPIV_OK) return st;
+    if (kernel_px < 1 || kernel_px % 2 == 0 || kernel_px > 63)
+        return fail(QLPIV_E_ARG, "kernel width %d must be odd, 1..63", kernel_px);
+    if (kernel_px / 2 > height || kernel_px / 2 > width)
+        return fail(QLPIV_E_SHAPE, "image %d x %d smaller than half the kernel", height, width);
+    const long n = (long)height * width;
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaStream_t s = h->stream;
+    if (sigma < 1e-5f) {  // GaussianFilter2D.applyFilter returns the input unchanged
+        std::vector<float> f(n);
+        for (long q = 0; q < n; q++)
+            f[q] = pixel_type == QLPIV_PIX_U8 ? (float)((const uint8_t *)img)[q]
+                   : pixel_type == QLPIV_PIX_U16 ? (float)((const uint16_t *)img)[q]
+                                                 : ((const float *)img)[q];
+        std::copy(f.begin(), f.end(), out);
+        return QLPIV_OK;
+    }
+    std::vector<float> k(kernel_px);
+    gauss_weights(sigma, kernel_px, k.data());
+    DevBuf *b = h->scratch;
+    const size_t ib = (size_t)n * pixel_bytes(pixel_type);
+    cudaError_t e;
+    if ((e = b[0].ensure(ib)) != cudaSuccess || (e = b[1].ensure(sizeof(float) * n)) != cudaSuccess ||
+        (e = b[2].ensure(sizeof(float) * n)) != cudaSuccess || (e = b[3].ensure(sizeof(float) * 64)) != cudaSuccess)
+        return cuda_fail(e, "filter buffers");
+    if ((e = cudaMemcpyAsync(b[0].p, img, ib, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b[3].p, k.data(), sizeof(float) * kernel_px, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "filter upload");
+    if ((e = launch_gauss(s, pixel_type, b[0].p, width, height, width, b[3].as<float>(), kernel_px, b[1].as<float>(),
+                          b[2].as<float>())) != cudaSuccess)
+        return cuda_fail(e, "filter");
+    h->launches += 2;
+    if ((e = cudaMemcpyAsync(out, b[2].p, sizeof(float) * n, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "filter download");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_normalize(qlpiv_handle *h, const float *img, int height, int width, float *out) {
+    if (!h || !img || !out) return fail(QLPIV_E_ARG, "NULL argument");
+    if (height < 1 || width < 1) return fail(QLPIV_E_SHAPE, "image size %d x %d", height, width);
+    const long n = (long)height * width;
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaStream_t s = h->stream;
+    DevBuf *b = h->scratch;
+    cudaError_t e;
+    if ((e = b[0].ensure(sizeof(float) * n)) != cudaSuccess || (e = b[1].ensure(sizeof(float) * n)) != cudaSuccess ||
+        (e = b[3].ensure(256)) != cudaSuccess)
+        return cuda_fail(e, "normalize buffers");
+    if ((e = cudaMemcpyAsync(b[0].p, img, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "normalize upload");
+    if ((e = launch_normalize(s, b[0].as<float>(), n, b[3].as<unsigned>(), b[1].as<float>())) != cudaSuccess)
+        return cuda_fail(e, "normalize");
+    h->launches += 2;
+    if ((e = cudaMemcpyAsync(out, b[1].p, sizeof(float) * n, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "normalize download");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_dense_lk(qlpiv_handle *h, const float *img_a, const float *img_b, int height, int width, float *us,
+                            float *vs, int window, int iterations, int half_pixel) {
+    if (!h || !img_a || !img_b || !us || !vs) return fail(QLPIV_E_ARG, "NULL argument");
+    if (height < 1 || width < 1) return fail(QLPIV_E_SHAPE, "image size %d x %d", height, width);
+    // DenseLucasKanadeAparapiJob.analyze limits
+    if (window < 3) return fail(QLPIV_E_ARG, "dense Lucas-Kanade: Window size too small");
+    if (window > 31) return fail(QLPIV_E_ARG, "dense Lucas-Kanade: Window size too large");
+    if (window % 2 == 0) return fail(QLPIV_E_ARG, "dense Lucas-Kanade: window size must be odd");
+    if (iterations <= 0) return fail(QLPIV_E_ARG, "dense Lucas-Kanade: Number of iterations must greater or equal to 1");
+    const long n = (long)height * width;
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaStream_t s = h->stream;
+    DevBuf *b = h->scratch;
+    cudaError_t e;
+    for (int q = 0; q < 4; q++)
+        if ((e = b[q].ensure(sizeof(float) * n)) != cudaSuccess) return cuda_fail(e, "dense LK buffers");
+    if ((e = cudaMemcpyAsync(b[0].p, img_a, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b[1].p, img_b, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b[2].p, us, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b[3].p, vs, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "dense LK upload");
+    if ((e = launch_dense_lk(s, b[0].as<float>(), b[1].as<float>(), height, width, b[2].as<float>(), b[3].as<float>(),
+                             window, iterations, half_pixel)) != cudaSuccess)
+        return cuda_fail(e, "dense LK");
+    h->launches++;
+    if ((e = cudaMemcpyAsync(us, b[2].p, sizeof(float) * n, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(vs, b[3].p, sizeof(float) * n, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "dense LK download");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_liu_shen(qlpiv_handle *h, const float *lk_a, const float *lk_b, const float *ls_a,
+                            const float *ls_b, int height, int width, float *us, float *vs, int window,
+                            int iterations_lk, float lambda, int iterations_ls, int half_pixel) {
+    if (!h || !ls_a || !ls_b || !us || !vs) return fail(QLPIV_E_ARG, "NULL argument");
+    if (height < 1 || width < 1) return fail(QLPIV_E_SHAPE, "image size %d x %d", height, width);
+    if (iterations_ls <= 0) return fail(QLPIV_E_ARG, "dense Liu-Shen: Number of iterations must greater or equal to 1");
+    if (iterations_lk > 0) {
+        if (!lk_a || !lk_b) return fail(QLPIV_E_ARG, "NULL Lucas-Kanade image");
+        if (window < 3 || window > 31 || window % 2 == 0)
+            return fail(QLPIV_E_ARG, "dense Lucas-Kanade: window size %d must be odd, 3..31", window);
+    }
+    const long n = (long)height * width;
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaStream_t s = h->stream;
+    DevBuf *b = h->scratch;
+    cudaError_t e;
+    for (int q = 0; q < 6; q++)
+        if ((e = b[q].ensure(sizeof(float) * n)) != cudaSuccess) return cuda_fail(e, "Liu-Shen buffers");
+    if ((e = b[6].ensure(sizeof(float) * 10 * n)) != cudaSuccess ||
+        (e = b[7].ensure(sizeof(double) * iterations_ls)) != cudaSuccess)
+        return cuda_fail(e, "Liu-Shen buffers");
+    if ((iterations_lk > 0 &&
+         ((e = cudaMemcpyAsync(b[0].p, lk_a, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(b[1].p, lk_b, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess)) ||
+        (e = cudaMemcpyAsync(b[2].p, ls_a, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b[3].p, ls_b, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b[4].p, us, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b[5].p, vs, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "Liu-Shen upload");
+    if (iterations_lk > 0) {  // pass 0 of DenseLiuShenGpuKernel: Lucas-Kanade
+        if ((e = launch_dense_lk(s, b[0].as<float>(), b[1].as<float>(), height, width, b[4].as<float>(),
+                                 b[5].as<float>(), window, iterations_lk, half_pixel)) != cudaSuccess)
+            return cuda_fail(e, "dense LK");
+        h->launches++;
+    }
+    float *fx = b[6].as<float>();
+    if ((e = launch_liu_shen(s, b[2].as<float>(), b[3].as<float>(), height, width, b[4].as<float>(), b[5].as<float>(),
+                             lambda, iterations_ls, half_pixel, fx, fx + 8 * n, b[7].as<double>())) != cudaSuccess)
+        return cuda_fail(e, "Liu-Shen");
+    h->launches += 1 + iterations_ls;
+    if ((e = cudaMemcpyAsync(us, b[4].p, sizeof(float) * n, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(vs, b[5].p, sizeof(float) * n, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "Liu-Shen download");
+    return QLPIV_OK;
+}
+
+}  // extern "C"
