@@ -348,6 +348,54 @@ qlpiv_status qlpiv_liu_shen(qlpiv_handle *h, const float *lk_a, const float *lk_
                             const float *ls_b, int height, int width, float *us, float *vs, int window,
                             int iterations_lk, float lambda, int iterations_ls, int half_pixel);
 
+/* Optical flow after PIV (IOpticalFlowInterpolator.interpolate(stepTilesA, stepTilesB) of the
+ * LucasKanade and LiuShenWithLucasKanade interpolators,
+ * S/interpolators/DenseLucasKanadeAparapiJobInterpolator.java:247-334,
+ * S/interpolators/DenseLiuShenAparapiJobInterpolator.java:226-341). */
+typedef enum {
+    QLPIV_FLOW_LUCAS_KANADE = 1,  /* dense Lucas-Kanade */
+    QLPIV_FLOW_LIU_SHEN = 2       /* dense Lucas-Kanade followed by Liu-Shen */
+} qlpiv_flow_mode;
+
+typedef struct qlpiv_flow_desc {
+    int mode;               /* qlpiv_flow_mode */
+    float filter_sigma_lk;  /* Lucas-Kanade prefilter (GaussianFilter2D) */
+    int filter_px_lk;
+    float filter_sigma_ls;  /* Liu-Shen prefilter, followed by normalisation */
+    int filter_px_ls;
+    int window_lk;          /* odd, 3..31 */
+    int iterations_lk;
+    float lambda_ls;        /* Liu-Shen Lagrange multiplier */
+    int iterations_ls;
+    int dense_export;       /* denseVectors: whole-pixel field and dense output */
+    int reserved[6];
+} qlpiv_flow_desc;
+
+/* The optical flow after PIV of one frame pair on the last adaptive step's grid (tiles of side
+ * n, rows tops[ni], columns lefts[nj]): images prefiltered (Liu-Shen images normalised), the tile
+ * displacements tile_u/tile_v (rows, columns; ni x nj, updated in place) interpolated per pixel
+ * (bicubic spline at pixel + 0.5, or + 0 with dense export), Lucas-Kanade (+ Liu-Shen) with the
+ * half-pixel offset unless dense export, tiles replaced from the pixel at top + n/2 - 1 (the 2x2
+ * average there with dense export).  dense_u/dense_v (rows, columns; may be NULL) receive the
+ * dense field.  Host arrays; synchronous. */
+qlpiv_status qlpiv_flow_after_piv(qlpiv_handle *h, const qlpiv_flow_desc *desc, int pixel_type, const void *img_a,
+                                  const void *img_b, int height, int width, int n, int ni, int nj,
+                                  const int32_t *tops, const int32_t *lefts, float *tile_u, float *tile_v,
+                                  float *dense_u, float *dense_v);
+
+/* Adaptive PIV of num_pairs host frame pairs (as qlpiv_piv_adaptive) followed on the device by
+ * the optical flow after PIV of every pair (LocalPIVOpenCLGpuJob.java:414).  out_u/out_v:
+ * num_pairs x last-level tiles; dense_u/dense_v (may be NULL): num_pairs x height x width. */
+qlpiv_status qlpiv_piv_flow(qlpiv_handle *h, const qlpiv_adaptive_desc *piv, const qlpiv_flow_desc *flow,
+                            int pixel_type, int height, int width, int num_pairs, const qlpiv_frame *frames,
+                            float *out_u, float *out_v, float *dense_u, float *dense_v);
+
+/* qlpiv_piv_flow on frames and outputs resident on the device; asynchronous on the handle's
+ * stream. */
+qlpiv_status qlpiv_piv_flow_device(qlpiv_handle *h, const qlpiv_adaptive_desc *piv, const qlpiv_flow_desc *flow,
+                                   int pixel_type, int height, int width, int num_pairs, const qlpiv_frame *frames,
+                                   float *out_u, float *out_v, float *dense_u, float *dense_v);
+
 /* Stage timing of the adaptive pipeline (CUDA events around every launch on the
  * handle's stream).  Accumulates while enabled; qlpiv_profile_read synchronises the
  * stream, returns the totals per (stage, level) and clears them. */

@@ -76,6 +76,8 @@ def lib():
         L.orc_piv_pass.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_long, ip, ip, ip, ip, c_int,
                                    c_float, c_float, c_int, c_int, vp, c_int]
         L.orc_displacement_field.argtypes = [dp, c_int, dp, c_int, fp, fp, c_int, c_int, c_int, fp, fp]
+        L.orc_displacement_field_off.argtypes = [dp, c_int, dp, c_int, fp, fp, c_int, c_int, c_int, c_float, c_float,
+                                                 fp, fp]
         L.orc_warp_both.argtypes = [vp, vp, c_int, c_int, c_int, fp, fp, c_int, vp, vp]
         L.orc_inherit.argtypes = [dp, c_int, dp, c_int, fp, fp, fp, c_int, fp, c_int, c_int, c_int, fp, fp]
         L.orc_piv_adaptive.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_float,
@@ -93,6 +95,8 @@ def lib():
         L.orc_normalize.argtypes = [fp, c_long, fp]
         L.orc_dense_lk.argtypes = [fp, fp, c_int, c_int, fp, fp, c_int, c_int, c_int]
         L.orc_liu_shen.argtypes = [fp, fp, c_int, c_int, fp, fp, c_float, c_int, c_int, vp, vp, vp]
+        L.orc_flow_after_piv.argtypes = [fp, fp, c_int, c_int, c_int, c_int, c_int, ip, ip, fp, fp, c_int, c_float,
+                                         c_int, c_float, c_int, c_int, c_int, c_float, c_int, c_int, vp, vp]
         L.orc_vector_size.restype = c_int
         assert L.orc_vector_size() == VECTOR_DTYPE.itemsize
         _lib = L
@@ -229,17 +233,17 @@ def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
-def displacement_field(ys, xs, u, v, h, w, precision=32):
+def displacement_field(ys, xs, u, v, h, w, precision=32, offset=0.0):
     """Per-pixel (u, v) from tile displacements at tile centres (bicubic spline), evaluated
-    in float (precision=32, the CUDA formulation) or double."""
+    in float (precision=32, the CUDA formulation) or double, pixel (i, j) at (i, j) + offset."""
     ys, xs = _f64(ys), _f64(xs)
     u, v = _f32(u), _f32(v)
     fu = np.zeros((h, w), np.float32)
     fv = np.zeros((h, w), np.float32)
-    lib().orc_displacement_field(_ptr(ys, ctypes.c_double), len(ys), _ptr(xs, ctypes.c_double), len(xs),
-                                 _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), h, w, 0 if precision == 32 else 1,
-                                 _ptr(fu, ctypes.c_float),
-                                 _ptr(fv, ctypes.c_float))
+    lib().orc_displacement_field_off(_ptr(ys, ctypes.c_double), len(ys), _ptr(xs, ctypes.c_double), len(xs),
+                                     _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), h, w,
+                                     0 if precision == 32 else 1, offset, offset, _ptr(fu, ctypes.c_float),
+                                     _ptr(fv, ctypes.c_float))
     return fu, fv
 
 
@@ -440,4 +444,23 @@ def liu_shen(ls_a, ls_b, us, vs, lam, iterations, half_pixel=False, intermediate
     if intermediates:
         return u, v, passes, fixed, un, vn
     return u, v
+
+
+def flow_after_piv(img_a, img_b, n, tops, lefts, tu, tv, mode=2, sigma_lk=2.0, px_lk=3, sigma_ls=0.48, px_ls=5,
+                   window=27, iterations_lk=5, lam=4.0, iterations_ls=60, dense_export=True):
+    """Optical flow after PIV on the last step's tile grid: returns updated tile (u, v)
+    (rows, columns) and the dense field (rows, columns)."""
+    a, b = _f32(img_a), _f32(img_b)
+    h, w = a.shape
+    tops = np.ascontiguousarray(tops, np.int32)
+    lefts = np.ascontiguousarray(lefts, np.int32)
+    u = np.array(tu, np.float32, order="C", copy=True)
+    v = np.array(tv, np.float32, order="C", copy=True)
+    du = np.zeros((h, w), np.float32)
+    dv = np.zeros((h, w), np.float32)
+    lib().orc_flow_after_piv(_ptr(a, ctypes.c_float), _ptr(b, ctypes.c_float), h, w, n, len(tops), len(lefts),
+                             _ptr(tops, ctypes.c_int), _ptr(lefts, ctypes.c_int), _ptr(u, ctypes.c_float),
+                             _ptr(v, ctypes.c_float), mode, sigma_lk, px_lk, sigma_ls, px_ls, window, iterations_lk,
+                             lam, iterations_ls, int(dense_export), du.ctypes.data, dv.ctypes.data)
+    return u, v, du, dv
 

@@ -45,4 +45,14 @@ int orc_spiral_order(int ni, int nj, int *order);
 int orc_validate(int ni, int nj, const int *tops, const int *lefts, float *u, float *v, const float *pu,
                  const float *pv, const int *npeaks, int k, const orc_valid_cfg *cfg, unsigned char *invalid_out);
 
+void orc_displacement_field_off(const double *ys, int ni, const double *xs, int nj, const float *u, const float *v,
+                                int h, int w, int precision, float off_y, float off_x, float *fu, float *fv);
+void orc_gauss_kernel(float sigma, int px, float *k);
+void orc_gauss_filter(const float *in, int h, int w, const float *k, int K, float *out);
+void orc_normalize(const float *in, long n, float *out);
+void orc_dense_lk(const float *A, const float *B, int h, int w, float *us, float *vs, int win, int iterations,
+                  int half_pixel);
+int orc_liu_shen(const float *la, const float *lb, int h, int w, float *us, float *vs, float lambda, int iterations,
+                 int half_pixel, float *fixed_out, float *unews, float *vnews);
+
 #endif

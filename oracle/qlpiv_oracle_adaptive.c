@@ -159,8 +159,10 @@ static void store_pix(void *img, int pix_bytes, int w, int y, int x, float v, in
 /* Per-pixel field of one level: tile displacements u, v (ni x nj, row-major) at tile
  * centres ys[ni], xs[nj] -> fu, fv (h x w float).  Coordinates clamped to the centre box.
  * precision 0: the surface is evaluated in float (the CUDA formulation); 1: in double. */
-void orc_displacement_field(const double *ys, int ni, const double *xs, int nj, const float *u, const float *v, int h,
-                            int w, int precision, float *fu, float *fv) {
+/* Pixel (i, j) is evaluated at (off_y + i, off_x + j): interpolateDisplacements(height, width,
+ * offsetY, offsetX) (S/iareas/BiCubicSplineInterpolatorWithBiLinearBackup.java:108-160). */
+void orc_displacement_field_off(const double *ys, int ni, const double *xs, int nj, const float *u, const float *v,
+                                int h, int w, int precision, float off_y, float off_x, float *fu, float *fv) {
     const size_t nn = (size_t)ni * nj;
     double *du = (double *)malloc(nn * sizeof(double)), *dv = (double *)malloc(nn * sizeof(double));
     double *cu = (double *)malloc(4 * nn * sizeof(double)), *cv = (double *)malloc(4 * nn * sizeof(double));
@@ -174,10 +176,10 @@ void orc_displacement_field(const double *ys, int ni, const double *xs, int nj, 
     for (int i = 0; i < ni; i++) fys[i] = (float)ys[i];
     for (int j = 0; j < nj; j++) fxs[j] = (float)xs[j];
     for (int i = 0; i < h; i++) {
-        float y = (float)i;
+        float y = off_y + (float)i;
         if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
         for (int j = 0; j < w; j++) {
-            float x = (float)j;
+            float x = off_x + (float)j;
             if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
             if (precision == 0) {
                 fu[(size_t)i * w + j] = bicubic_value_f32(fys, ni, fxs, nj, fcu, y, x);
@@ -189,6 +191,11 @@ void orc_displacement_field(const double *ys, int ni, const double *xs, int nj, 
         }
     }
     free(du); free(dv); free(cu); free(cv); free(fcu); free(fcv); free(fys); free(fxs);
+}
+
+void orc_displacement_field(const double *ys, int ni, const double *xs, int nj, const float *u, const float *v, int h,
+                            int w, int precision, float *fu, float *fv) {
+    orc_displacement_field_off(ys, ni, xs, nj, u, v, h, w, precision, 0.0f, 0.0f, fu, fv);
 }
 
 /* BothImages bilinear warp of a pair with a per-pixel field (halved inside). */

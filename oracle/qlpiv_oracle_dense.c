@@ -27,6 +27,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "oracle_types.h"
+
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
 #endif
@@ -303,3 +305,67 @@ int orc_liu_shen(const float *la, const float *lb, int h, int w, float *us, floa
     free(vn);
     return passes;
 }
+
+/* IOpticalFlowInterpolator.interpolate(stepTilesA, stepTilesB) of the LucasKanade (mode 1) and
+ * LiuShenWithLucasKanade (mode 2) interpolators
+ * (S/interpolators/DenseLucasKanadeAparapiJobInterpolator.java:247-334,
+ *  S/interpolators/DenseLiuShenAparapiJobInterpolator.java:226-341) for the last adaptive step:
+ * images filtered (LK: sigma_lk/px_lk; LS: sigma_ls/px_ls then normalised), the tile field
+ * interpolated per pixel (offset 0 with dense export, else 0.5), Lucas-Kanade (+ Liu-Shen) with the
+ * half-pixel offset unless dense export, tile displacements replaced from the pixel at
+ * top + N/2 - 1 (average of the 2x2 pixels there with dense export).  img: float copies of the
+ * frames.  tu/tv: tile displacements (rows, columns), ni x nj, updated in place; dense_u/dense_v
+ * (rows, columns) receive the dense field when non-NULL. */
+void orc_flow_after_piv(const float *img_a, const float *img_b, int h, int w, int n, int ni, int nj, const int *tops,
+                        const int *lefts, float *tu, float *tv, int mode, float sigma_lk, int px_lk, float sigma_ls,
+                        int px_ls, int window, int iters_lk, float lambda, int iters_ls, int dense_export,
+                        float *dense_u, float *dense_v) {
+    const long np = (long)h * w;
+    float *lka = (float *)malloc(sizeof(float) * np), *lkb = (float *)malloc(sizeof(float) * np);
+    float *lsa = NULL, *lsb = NULL;
+    float k[64];
+    orc_gauss_kernel(sigma_lk, px_lk, k);
+    if (sigma_lk < 1e-5f) { memcpy(lka, img_a, sizeof(float) * np); memcpy(lkb, img_b, sizeof(float) * np); }
+    else { orc_gauss_filter(img_a, h, w, k, px_lk, lka); orc_gauss_filter(img_b, h, w, k, px_lk, lkb); }
+    if (mode == 2) {
+        lsa = (float *)malloc(sizeof(float) * np);
+        lsb = (float *)malloc(sizeof(float) * np);
+        float *t = (float *)malloc(sizeof(float) * np);
+        orc_gauss_kernel(sigma_ls, px_ls, k);
+        if (sigma_ls < 1e-5f) memcpy(t, img_a, sizeof(float) * np); else orc_gauss_filter(img_a, h, w, k, px_ls, t);
+        orc_normalize(t, np, lsa);
+        if (sigma_ls < 1e-5f) memcpy(t, img_b, sizeof(float) * np); else orc_gauss_filter(img_b, h, w, k, px_ls, t);
+        orc_normalize(t, np, lsb);
+        free(t);
+    }
+    double *ys = (double *)malloc(sizeof(double) * ni), *xs = (double *)malloc(sizeof(double) * nj);
+    for (int i = 0; i < ni; i++) ys[i] = (double)((float)tops[i] + (float)n / 2.0f - 0.5f);
+    for (int j = 0; j < nj; j++) xs[j] = (double)((float)lefts[j] + (float)n / 2.0f - 0.5f);
+    float *fu = (float *)malloc(sizeof(float) * np), *fv = (float *)malloc(sizeof(float) * np);
+    const float off = dense_export ? 0.0f : 0.5f;
+    orc_displacement_field_off(ys, ni, xs, nj, tu, tv, h, w, 0, off, off, fu, fv);
+    /* the flow jobs take columns (us) and rows (vs) */
+    float *us = fv, *vs = fu;
+    const int half = dense_export ? 0 : 1;
+    orc_dense_lk(lka, lkb, h, w, us, vs, window, iters_lk, half);
+    if (mode == 2) orc_liu_shen(lsa, lsb, h, w, us, vs, lambda, iters_ls, half, NULL, NULL, NULL);
+    for (int ti = 0; ti < ni; ti++)
+        for (int tj = 0; tj < nj; tj++) {
+            const int i = tops[ti] + n / 2 - 1, j = lefts[tj] + n / 2 - 1;
+            const long idx = (long)i * w + j, idx2 = (long)(i + 1) * w + j;
+            float u, v;
+            if (!dense_export) {
+                u = us[idx];
+                v = vs[idx];
+            } else {
+                u = (((us[idx] + us[idx + 1]) + us[idx2]) + us[idx2 + 1]) / 4.0f;
+                v = (((vs[idx] + vs[idx + 1]) + vs[idx2]) + vs[idx2 + 1]) / 4.0f;
+            }
+            tu[ti * nj + tj] = v;   /* Tile.replaceDisplacement(v, u): rows, columns */
+            tv[ti * nj + tj] = u;
+        }
+    if (dense_u) memcpy(dense_u, vs, sizeof(float) * np);
+    if (dense_v) memcpy(dense_v, us, sizeof(float) * np);
+    free(lka); free(lkb); free(lsa); free(lsb); free(ys); free(xs); free(fu); free(fv);
+}
+

@@ -112,6 +112,28 @@ def set_validation(d, num_peaks=3, peak_kernel=3, threshold=2.0, epsilon0=0.1, m
     return d
 
 
+FLOW_LUCAS_KANADE, FLOW_LIU_SHEN = 1, 2
+
+
+class FlowDesc(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int), ("filter_sigma_lk", ctypes.c_float), ("filter_px_lk", ctypes.c_int),
+                ("filter_sigma_ls", ctypes.c_float), ("filter_px_ls", ctypes.c_int), ("window_lk", ctypes.c_int),
+                ("iterations_lk", ctypes.c_int), ("lambda_ls", ctypes.c_float), ("iterations_ls", ctypes.c_int),
+                ("dense_export", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+
+
+def flow_desc(mode=FLOW_LUCAS_KANADE, filter_sigma_lk=2.0, filter_px_lk=3, filter_sigma_ls=0.48, filter_px_ls=5,
+              window_lk=27, iterations_lk=5, lambda_ls=4.0, iterations_ls=60, dense_export=False):
+    """Optical flow after PIV (OpticalFlowAfterPIV Lucas-Kanade or Liu-Shen interpolator
+    options); dense_export selects whole-pixel evaluation and the dense field export."""
+    d = FlowDesc()
+    d.mode, d.filter_sigma_lk, d.filter_px_lk = mode, filter_sigma_lk, filter_px_lk
+    d.filter_sigma_ls, d.filter_px_ls, d.window_lk, d.iterations_lk = filter_sigma_ls, filter_px_ls, window_lk, \
+        iterations_lk
+    d.lambda_ls, d.iterations_ls, d.dense_export = lambda_ls, iterations_ls, int(dense_export)
+    return d
+
+
 class StageTime(ctypes.Structure):
     _fields_ = [("stage", ctypes.c_char * 24), ("level", ctypes.c_int), ("ia_side", ctypes.c_int),
                 ("launches", ctypes.c_long), ("items", ctypes.c_long), ("ms", ctypes.c_double)]
@@ -154,6 +176,12 @@ _SIGNATURES = {
     "qlpiv_normalize": (_i, [_vp, _vp, _i, _i, _vp]),
     "qlpiv_dense_lk": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp, _i, _i, _i]),
     "qlpiv_liu_shen": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _i, _f, _i, _i]),
+    "qlpiv_flow_after_piv": (_i, [_vp, ctypes.POINTER(FlowDesc), _i, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp,
+                                  _vp, _vp, _vp]),
+    "qlpiv_piv_flow": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), ctypes.POINTER(FlowDesc), _i, _i, _i, _i, _vp, _vp,
+                            _vp, _vp, _vp]),
+    "qlpiv_piv_flow_device": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), ctypes.POINTER(FlowDesc), _i, _i, _i, _i, _vp,
+                                   _vp, _vp, _vp, _vp]),
     "qlpiv_profile_enable": (_i, [_vp, _i]),
     "qlpiv_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(_i)]),
 }
@@ -538,6 +566,52 @@ class Handle:
                                         _addr(u), _addr(v), int(window), int(iterations_lk), float(lam),
                                         int(iterations_ls), int(half_pixel)))
         return u, v
+
+    def flow_after_piv(self, img_a, img_b, n, tops, lefts, tile_u, tile_v, desc, dense=True):
+        """Optical flow after PIV of one frame pair on a tile grid (side n, rows tops, columns
+        lefts); returns (tile_u, tile_v) and, with dense, the dense field (u, v) (rows, columns)."""
+        a = np.ascontiguousarray(img_a)
+        b = np.ascontiguousarray(img_b, a.dtype)
+        tops = np.ascontiguousarray(tops, np.int32)
+        lefts = np.ascontiguousarray(lefts, np.int32)
+        tu = np.array(tile_u, np.float32, order="C", copy=True)
+        tv = np.array(tile_v, np.float32, order="C", copy=True)
+        if tu.shape != (len(tops), len(lefts)) or tv.shape != tu.shape:
+            raise ValueError("tile displacements must be (len(tops), len(lefts))")
+        du = np.empty(a.shape, np.float32) if dense else None
+        dv = np.empty(a.shape, np.float32) if dense else None
+        _check(self._lib.qlpiv_flow_after_piv(self._h, ctypes.byref(desc), pixel_type_of(a.dtype), _addr(a), _addr(b),
+                                              a.shape[0], a.shape[1], int(n), len(tops), len(lefts), _addr(tops),
+                                              _addr(lefts), _addr(tu), _addr(tv), _addr(du), _addr(dv)))
+        return (tu, tv, du, dv) if dense else (tu, tv)
+
+    def piv_flow(self, frames_a, frames_b, desc, flow, dense=False):
+        """Adaptive PIV followed by the optical flow after PIV of every pair; returns (u, v)
+        shaped (pairs, tiles_i, tiles_j), plus the dense fields (pairs, h, w) with dense."""
+        fa = [np.ascontiguousarray(x) for x in frames_a]
+        fb = [np.ascontiguousarray(x) for x in frames_b]
+        h, w = fa[0].shape
+        dt = fa[0].dtype
+        table = (Frame * len(fa))()
+        for k, (x, y) in enumerate(zip(fa, fb)):
+            if x.shape != (h, w) or y.shape != (h, w) or x.dtype != dt or y.dtype != dt:
+                raise ValueError("all frames must share shape and dtype")
+            table[k] = Frame(x.ctypes.data, y.ctypes.data, h, w, w)
+        last = adaptive_levels(desc, h, w)[-1]
+        u = np.empty((len(fa), last["tiles_i"], last["tiles_j"]), np.float32)
+        v = np.empty_like(u)
+        du = np.empty((len(fa), h, w), np.float32) if dense else None
+        dv = np.empty((len(fa), h, w), np.float32) if dense else None
+        _check(self._lib.qlpiv_piv_flow(self._h, ctypes.byref(desc), ctypes.byref(flow), pixel_type_of(dt), h, w,
+                                        len(fa), table, _addr(u), _addr(v), _addr(du), _addr(dv)))
+        return (u, v, du, dv) if dense else (u, v)
+
+    def piv_flow_device(self, desc, flow, pixel_type, height, width, num_pairs, frames, out_u, out_v, dense_u=None,
+                        dense_v=None):
+        """Queue adaptive PIV plus optical flow over a device frame table into device outputs."""
+        a = [x if isinstance(x, int) or x is None else _addr(x) for x in (frames, out_u, out_v, dense_u, dense_v)]
+        _check(self._lib.qlpiv_piv_flow_device(self._h, ctypes.byref(desc), ctypes.byref(flow), pixel_type, height,
+                                               width, num_pairs, *a))
 
     def piv_adaptive(self, frames_a, frames_b, desc):
         """Adaptive multi-pass PIV of image pairs of one size; returns (u, v) of the last

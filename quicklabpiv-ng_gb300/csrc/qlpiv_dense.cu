@@ -333,7 +333,44 @@ __global__ void ls_pass_kernel(const float *fx, int h, int w, float lambda, cons
     if (((threadIdx.y * blockDim.x + threadIdx.x) & 31) == 0 && e != 0.0) atomicAdd(&err[pass], e);
 }
 
+// Tile displacements from the dense field (rows vs, columns us) at top + n/2 - 1, left + n/2 - 1,
+// or the 2x2 average there with dense export (Tile.replaceDisplacement(v, u)).
+__global__ void tiles_from_dense_kernel(const float *us, const float *vs, int w, int n, int ni, int nj,
+                                        const int *tops, const int *lefts, int dense, float *tile_u, float *tile_v) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ni * nj) return;
+    const int ti = t / nj, tj = t - ti * nj;
+    const int i = tops[ti] + n / 2 - 1, j = lefts[tj] + n / 2 - 1;
+    const long idx = (long)i * w + j, idx2 = (long)(i + 1) * w + j;
+    float u, v;
+    if (!dense) {
+        u = us[idx];
+        v = vs[idx];
+    } else {
+        u = __fdiv_rn(__fadd_rn(__fadd_rn(__fadd_rn(us[idx], us[idx + 1]), us[idx2]), us[idx2 + 1]), 4.0f);
+        v = __fdiv_rn(__fadd_rn(__fadd_rn(__fadd_rn(vs[idx], vs[idx + 1]), vs[idx2]), vs[idx2 + 1]), 4.0f);
+    }
+    tile_u[t] = v;
+    tile_v[t] = u;
+}
+
 }  // namespace
+
+size_t spline_coef_bytes(long tiles) { return (size_t)tiles * (6 * sizeof(double) + 2 * sizeof(float4)); }
+
+const char *check_flow_desc(const qlpiv_flow_desc *d) {
+    if (!d) return "flow descriptor is NULL";
+    if (d->mode != QLPIV_FLOW_LUCAS_KANADE && d->mode != QLPIV_FLOW_LIU_SHEN) return "unknown optical-flow mode";
+    if (d->window_lk < 3 || d->window_lk > 31 || d->window_lk % 2 == 0)
+        return "dense Lucas-Kanade: window size must be odd, 3..31";
+    if (d->iterations_lk <= 0) return "dense Lucas-Kanade: Number of iterations must greater or equal to 1";
+    if (d->filter_px_lk < 1 || d->filter_px_lk % 2 == 0 || d->filter_px_lk > 63) return "Lucas-Kanade filter width";
+    if (d->mode == QLPIV_FLOW_LIU_SHEN) {
+        if (d->iterations_ls <= 0) return "dense Liu-Shen: Number of iterations must greater or equal to 1";
+        if (d->filter_px_ls < 1 || d->filter_px_ls % 2 == 0 || d->filter_px_ls > 63) return "Liu-Shen filter width";
+    }
+    return nullptr;
+}
 
 void gauss_weights(float sigma, int px, float *k) {
     std::vector<double> kd(px);
@@ -406,6 +443,105 @@ cudaError_t launch_liu_shen(cudaStream_t s, const float *la, const float *lb, in
             return e;
     }
     return cudaSuccess;
+}
+
+static SplineCoef coef_view(void *base, long n) {
+    double *c = reinterpret_cast<double *>(base);
+    float4 *q = reinterpret_cast<float4 *>(c + 6 * n);
+    return SplineCoef{c, c + n, c + 2 * n, c + 3 * n, c + 4 * n, c + 5 * n, q, q + n};
+}
+
+// prefilter of a frame; sigma < 1e-5 keeps the frame (converted to float)
+static cudaError_t filter_or_copy(cudaStream_t s, int pixel_type, const void *img, long pitch, int h, int w, float sigma,
+                                  const float *k, int K, float *tmp, float *out, long *launches) {
+    *launches += 2;
+    // sigma < 1e-5: the weights hold a one-point unit kernel, which converts and copies exactly
+    return launch_gauss(s, pixel_type, img, pitch, h, w, k, sigma < 1e-5f ? 1 : K, tmp, out);
+}
+
+cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, const void *img_a, const void *img_b,
+                     long pitch, int h, int w, int n, int ni, int nj, const double *cy, const double *cx,
+                     const float *cyf, const float *cxf, const int *tops, const int *lefts, float *tile_u,
+                     float *tile_v, float *dense_u, float *dense_v, const FlowBufs &b, long *launches) {
+    cudaError_t e;
+    const long np = (long)h * w;
+    if ((e = filter_or_copy(s, pixel_type, img_a, pitch, h, w, d.filter_sigma_lk, b.k_lk, d.filter_px_lk, b.tmp, b.lka,
+                            launches)) != cudaSuccess ||
+        (e = filter_or_copy(s, pixel_type, img_b, pitch, h, w, d.filter_sigma_lk, b.k_lk, d.filter_px_lk, b.tmp, b.lkb,
+                            launches)) != cudaSuccess)
+        return e;
+    if (d.mode == QLPIV_FLOW_LIU_SHEN) {
+        if ((e = filter_or_copy(s, pixel_type, img_a, pitch, h, w, d.filter_sigma_ls, b.k_ls, d.filter_px_ls, b.tmp,
+                                b.fu, launches)) != cudaSuccess ||
+            (e = launch_normalize(s, b.fu, np, b.mx, b.lsa)) != cudaSuccess ||
+            (e = filter_or_copy(s, pixel_type, img_b, pitch, h, w, d.filter_sigma_ls, b.k_ls, d.filter_px_ls, b.tmp,
+                                b.fu, launches)) != cudaSuccess ||
+            (e = launch_normalize(s, b.fu, np, b.mx, b.lsb)) != cudaSuccess)
+            return e;
+        *launches += 4;
+    }
+    // per-pixel field from the tiles (knots at the tile centres), offset 0.5 unless dense export
+    const SplineCoef coef = coef_view(b.coef, (long)ni * nj);
+    if ((e = launch_spline(s, 1, cy, b.cp, ni, cx, b.cp + ni, nj, tile_u, tile_v, coef)) != cudaSuccess) return e;
+    *launches += 4;
+    const float off = d.dense_export ? 0.0f : 0.5f;
+    if ((e = launch_field(s, h, w, cyf, ni, cxf, nj, coef, b.fu, b.fv, off, off)) != cudaSuccess) return e;
+    *launches += 1;
+    float *us = b.fv, *vs = b.fu;  // the flow jobs take columns (us) and rows (vs)
+    const int half = d.dense_export ? 0 : 1;
+    if ((e = launch_dense_lk(s, b.lka, b.lkb, h, w, us, vs, d.window_lk, d.iterations_lk, half)) != cudaSuccess)
+        return e;
+    *launches += 1;
+    if (d.mode == QLPIV_FLOW_LIU_SHEN) {
+        if ((e = launch_liu_shen(s, b.lsa, b.lsb, h, w, us, vs, d.lambda_ls, d.iterations_ls, half, b.fx, b.fx + 8 * np,
+                                 b.err)) != cudaSuccess)
+            return e;
+        *launches += 1 + d.iterations_ls;
+    }
+    tiles_from_dense_kernel<<<blocks_of((long)ni * nj, 128), 128, 0, s>>>(us, vs, w, n, ni, nj, tops, lefts,
+                                                                          d.dense_export, tile_u, tile_v);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    *launches += 1;
+    if (dense_u && (e = cudaMemcpyAsync(dense_u, vs, sizeof(float) * np, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+        return e;
+    if (dense_v && (e = cudaMemcpyAsync(dense_v, us, sizeof(float) * np, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+        return e;
+    return cudaSuccess;
+}
+
+// Carves FlowBufs for an h x w frame and ni x nj tiles out of one device buffer.
+cudaError_t flow_buffers(DevBuf &buf, int h, int w, int ni, int nj, int iterations_ls, FlowBufs *b) {
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t pl = al(sizeof(float) * (size_t)h * w);
+    const size_t total = 7 * pl + 10 * pl + al(sizeof(double) * (iterations_ls > 0 ? iterations_ls : 1)) + 256 +
+                         2 * al(sizeof(float) * 64) + al(sizeof(double) * (ni + nj)) +
+                         al(spline_coef_bytes((long)ni * nj));
+    cudaError_t e = buf.ensure(total);
+    if (e != cudaSuccess) return e;
+    char *c = buf.as<char>();
+    float **planes[7] = {&b->lka, &b->lkb, &b->lsa, &b->lsb, &b->tmp, &b->fu, &b->fv};
+    for (float **p : planes) { *p = (float *)c; c += pl; }
+    b->fx = (float *)c; c += 10 * pl;
+    b->err = (double *)c; c += al(sizeof(double) * (iterations_ls > 0 ? iterations_ls : 1));
+    b->mx = (unsigned *)c; c += 256;
+    b->k_lk = (float *)c; c += al(sizeof(float) * 64);
+    b->k_ls = (float *)c; c += al(sizeof(float) * 64);
+    b->cp = (double *)c; c += al(sizeof(double) * (ni + nj));
+    b->coef = c;
+    return cudaSuccess;
+}
+
+// Uploads both filters' weights (a one-point unit kernel when sigma < 1e-5).
+cudaError_t upload_flow_weights(cudaStream_t s, const qlpiv_flow_desc &d, const FlowBufs &b, std::vector<float> &host) {
+    host.assign(128, 0.0f);
+    if (d.filter_sigma_lk < 1e-5f) host[0] = 1.0f; else gauss_weights(d.filter_sigma_lk, d.filter_px_lk, host.data());
+    if (d.mode == QLPIV_FLOW_LIU_SHEN) {
+        if (d.filter_sigma_ls < 1e-5f) host[64] = 1.0f;
+        else gauss_weights(d.filter_sigma_ls, d.filter_px_ls, host.data() + 64);
+    }
+    cudaError_t e = cudaMemcpyAsync(b.k_lk, host.data(), sizeof(float) * 64, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(b.k_ls, host.data() + 64, sizeof(float) * 64, cudaMemcpyHostToDevice, s);
 }
 
 }  // namespace qlpiv
@@ -576,4 +712,77 @@ qlpiv_status qlpiv_liu_shen(qlpiv_handle *h, const float *lk_a, const float *lk_
     return QLPIV_OK;
 }
 
+qlpiv_status qlpiv_flow_after_piv(qlpiv_handle *h, const qlpiv_flow_desc *desc, int pixel_type, const void *img_a,
+                                  const void *img_b, int height, int width, int n, int ni, int nj,
+                                  const int32_t *tops, const int32_t *lefts, float *tile_u, float *tile_v,
+                                  float *dense_u, float *dense_v) {
+    if (!h || !img_a || !img_b || !tops || !lefts || !tile_u || !tile_v) return fail(QLPIV_E_ARG, "NULL argument");
+    if (const char *m = check_flow_desc(desc)) return fail(QLPIV_E_ARG, "%s", m);
+    qlpiv_status st = check_image(pixel_type, height, width);
+    if (st != QLPIV_OK) return st;
+    if (ni < 3 || nj < 3) return fail(QLPIV_E_SHAPE, "the spline needs at least 3 tiles per axis");
+    for (int i = 0; i < ni; i++)
+        if (tops[i] + n / 2 < 1 || tops[i] + n / 2 >= height) return fail(QLPIV_E_SHAPE, "tile row %d outside the image", i);
+    for (int j = 0; j < nj; j++)
+        if (lefts[j] + n / 2 < 1 || lefts[j] + n / 2 >= width) return fail(QLPIV_E_SHAPE, "tile column %d outside the image", j);
+    const long np = (long)height * width, nt = (long)ni * nj;
+    std::vector<double> knots(ni + nj);
+    std::vector<float> fknots(ni + nj);
+    for (int i = 0; i < ni; i++) {
+        fknots[i] = (float)tops[i] + (float)n / 2.0f - 0.5f;
+        knots[i] = fknots[i];
+    }
+    for (int j = 0; j < nj; j++) {
+        fknots[ni + j] = (float)lefts[j] + (float)n / 2.0f - 0.5f;
+        knots[ni + j] = fknots[ni + j];
+    }
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaStream_t s = h->stream;
+    DevBuf *sb = h->scratch;
+    const size_t ib = (size_t)np * pixel_bytes(pixel_type);
+    cudaError_t e;
+    FlowBufs fb;
+    if ((e = flow_buffers(sb[9], height, width, ni, nj, desc->iterations_ls, &fb)) != cudaSuccess ||
+        (e = sb[0].ensure(2 * ((ib + 255) & ~(size_t)255))) != cudaSuccess ||
+        (e = sb[1].ensure(sizeof(double) * (ni + nj) + sizeof(float) * (ni + nj) + sizeof(int32_t) * (ni + nj) +
+                          sizeof(float) * 2 * nt + 1024)) != cudaSuccess ||
+        (e = sb[2].ensure(sizeof(float) * 2 * np)) != cudaSuccess)
+        return cuda_fail(e, "flow buffers");
+    char *im = sb[0].as<char>();
+    char *ib2 = im + ((ib + 255) & ~(size_t)255);
+    double *dk = sb[1].as<double>();
+    float *dfk = (float *)(dk + ni + nj);
+    int32_t *dtl = (int32_t *)(dfk + ni + nj);
+    float *dtu = (float *)(dtl + ni + nj);
+    float *dtv = dtu + nt;
+    std::vector<int32_t> tl(tops, tops + ni);
+    tl.insert(tl.end(), lefts, lefts + nj);
+    std::vector<float> wts;
+    if ((e = cudaMemcpyAsync(im, img_a, ib, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(ib2, img_b, ib, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dk, knots.data(), sizeof(double) * (ni + nj), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dfk, fknots.data(), sizeof(float) * (ni + nj), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dtl, tl.data(), sizeof(int32_t) * (ni + nj), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dtu, tile_u, sizeof(float) * nt, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dtv, tile_v, sizeof(float) * nt, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = upload_flow_weights(s, *desc, fb, wts)) != cudaSuccess)
+        return cuda_fail(e, "flow upload");
+    float *du = sb[2].as<float>(), *dv = du + np;
+    long launches = 0;
+    if ((e = run_flow(s, *desc, pixel_type, im, ib2, width, height, width, n, ni, nj, dk, dk + ni, dfk, dfk + ni, dtl,
+                      dtl + ni, dtu, dtv, du, dv, fb, &launches)) != cudaSuccess)
+        return cuda_fail(e, "optical flow after PIV");
+    h->launches += launches;
+    if ((e = cudaMemcpyAsync(tile_u, dtu, sizeof(float) * nt, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(tile_v, dtv, sizeof(float) * nt, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (dense_u && (e = cudaMemcpyAsync(dense_u, du, sizeof(float) * np, cudaMemcpyDeviceToHost, s)) != cudaSuccess) ||
+        (dense_v && (e = cudaMemcpyAsync(dense_v, dv, sizeof(float) * np, cudaMemcpyDeviceToHost, s)) != cudaSuccess) ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "flow download");
+    return QLPIV_OK;
+}
+
 }  // extern "C"
+

@@ -2,6 +2,11 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "qlpiv.h"
+#include "qlpiv_adaptive.h"
+
+#include <vector>
+
 namespace qlpiv {
 
 // GaussianFilter2D.createKernel weights (double, normalised, rounded to float).
@@ -18,5 +23,32 @@ cudaError_t launch_dense_lk(cudaStream_t s, const float *a, const float *b, int 
 // Liu-Shen passes in place; fx: 10 x h x w floats of scratch, err: `iterations` doubles.
 cudaError_t launch_liu_shen(cudaStream_t s, const float *la, const float *lb, int h, int w, float *us, float *vs,
                             float lambda, int iterations, int half_pixel, float *fx, float *tmp, double *err);
+
+// Device buffers of one frame pair's optical flow after PIV (h x w floats each unless noted).
+struct FlowBufs {
+    float *lka, *lkb, *lsa, *lsb, *tmp, *fu, *fv;
+    float *fx;        // 10 x h x w (Liu-Shen fixed terms and ping-pong field)
+    double *err;      // iterations_ls
+    unsigned *mx;     // one word
+    float *k_lk, *k_ls;  // filter weights (device)
+    double *cp;       // ni + nj doubles (spline elimination factors)
+    void *coef;       // spline coefficients of ni x nj tiles (spline_coef_bytes)
+};
+size_t spline_coef_bytes(long tiles);
+
+// Optical flow after PIV of one frame pair on the device (see qlpiv_flow_after_piv): frames of
+// pixel_type with `pitch` elements per row; tile grid knots cy/cx (double, ni / nj) and cyf/cxf
+// (float); tops/lefts (device int); tile_u/tile_v (rows, columns) updated in place; dense_u /
+// dense_v (rows, columns) optional.  *launches counts the kernels queued.
+cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, const void *img_a, const void *img_b,
+                     long pitch, int h, int w, int n, int ni, int nj, const double *cy, const double *cx,
+                     const float *cyf, const float *cxf, const int *tops, const int *lefts, float *tile_u,
+                     float *tile_v, float *dense_u, float *dense_v, const FlowBufs &b, long *launches);
+// Carves the buffers of one frame pair's flow out of `buf` (grown on demand).
+cudaError_t flow_buffers(struct DevBuf &buf, int h, int w, int ni, int nj, int iterations_ls, FlowBufs *b);
+// Uploads both prefilters' weights (host staging kept by the caller until the stream syncs).
+cudaError_t upload_flow_weights(cudaStream_t s, const qlpiv_flow_desc &d, const FlowBufs &b, std::vector<float> &host);
+// Checks a flow descriptor; returns a message or nullptr.
+const char *check_flow_desc(const qlpiv_flow_desc *d);
 
 }  // namespace qlpiv

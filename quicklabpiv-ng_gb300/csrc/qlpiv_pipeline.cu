@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "qlpiv_adaptive.h"
+#include "qlpiv_dense.h"
 #include "qlpiv_handle.h"
 #include "qlpiv_internal.h"
 #include "qlpiv_validate.h"
@@ -49,6 +50,8 @@ struct AdaptivePlan {
     DevBuf warped_table;  // pairs qlpiv_frame entries
     DevBuf host_frames;   // images uploaded by qlpiv_piv_adaptive (host variant)
     DevBuf host_table;
+    DevBuf flow;          // optical flow after PIV: one pair's planes (FlowBufs)
+    DevBuf flow_dense;    // dense field of the host variant, 2 x pairs x height x width
 };
 
 void destroy_plan(AdaptivePlan *p) {
@@ -59,7 +62,8 @@ void destroy_plan(AdaptivePlan *p) {
                           &l.d_rank, &l.d_bu, &l.d_bv, &l.d_puv, &l.d_npk, &l.d_state, &l.d_list, &l.d_done,
                           &l.d_sweeps})
             b->release();
-    for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table}) b->release();
+    for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table, &p->flow, &p->flow_dense})
+        b->release();
     delete p;
 }
 
@@ -202,13 +206,14 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
             (lv > 0 && (e = L.d_rows.ensure(sizeof(float) * 2 * (long)pairs * ni *
                                             p->levels[lv - 1].g.tiles_j)) != cudaSuccess))
             return cuda_fail(e, "adaptive plan");
+        if ((e = upload(L.d_tops, L.tops.data(), sizeof(int32_t) * ni, s)) != cudaSuccess ||
+            (e = upload(L.d_lefts, L.lefts.data(), sizeof(int32_t) * nj, s)) != cudaSuccess)
+            return cuda_fail(e, "grid upload");
         std::vector<int32_t> order, rank;
         if (d->validation != QLPIV_VALIDATE_NONE) {
             spiral_rank(ni, nj, order, rank);
             const long k = d->num_peaks;
-            if ((e = upload(L.d_tops, L.tops.data(), sizeof(int32_t) * ni, s)) != cudaSuccess ||
-                (e = upload(L.d_lefts, L.lefts.data(), sizeof(int32_t) * nj, s)) != cudaSuccess ||
-                (e = upload(L.d_order, order.data(), sizeof(int32_t) * cnt, s)) != cudaSuccess ||
+            if ((e = upload(L.d_order, order.data(), sizeof(int32_t) * cnt, s)) != cudaSuccess ||
                 (e = upload(L.d_rank, rank.data(), sizeof(int32_t) * cnt, s)) != cudaSuccess ||
                 (e = L.d_bu.ensure(sizeof(float) * total)) != cudaSuccess ||
                 (e = L.d_bv.ensure(sizeof(float) * total)) != cudaSuccess ||
@@ -577,31 +582,27 @@ qlpiv_status qlpiv_piv_adaptive_device(qlpiv_handle *h, const qlpiv_adaptive_des
     return QLPIV_OK;
 }
 
-qlpiv_status qlpiv_piv_adaptive(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int pixel_type, int height,
-                                int width, int num_pairs, const qlpiv_frame *frames, float *out_u, float *out_v) {
-    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
-    qlpiv_status st = check_adaptive(desc, pixel_type, height, width);
-    if (st != QLPIV_OK) return st;
-    if (num_pairs < 0) return fail(QLPIV_E_ARG, "num_pairs < 0");
-    if (num_pairs == 0) return QLPIV_OK;
-    if (!frames || !out_u || !out_v) return fail(QLPIV_E_ARG, "NULL frame table or output");
+static qlpiv_status check_host_frames(const qlpiv_frame *frames, int num_pairs, int height, int width) {
     for (int q = 0; q < num_pairs; q++)
         if (!frames[q].img_a || !frames[q].img_b || frames[q].height != height || frames[q].width != width ||
             frames[q].pitch < width)
             return fail(QLPIV_E_SHAPE, "frame %d: NULL image or size differs from %d x %d", q, height, width);
-    std::lock_guard<std::mutex> lock(h->mu);
-    DeviceScope ds(h->device);
-    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
-    if ((st = build_plan(h, desc, pixel_type, height, width, num_pairs)) != QLPIV_OK) return st;
+    return QLPIV_OK;
+}
+
+// Copies host frame pairs into the plan's frame buffers (packed rows) and their table; the
+// table's host staging is kept in `t` until the caller synchronises.
+static qlpiv_status upload_host_frames(qlpiv_handle *h, const qlpiv_frame *frames, std::vector<qlpiv_frame> &t) {
     AdaptivePlan *p = h->plan;
     cudaStream_t s = h->stream;
-    const size_t pb = pixel_bytes(pixel_type), row = (size_t)width * pb, img = row * height;
+    const int num_pairs = p->pairs, height = p->height, width = p->width;
+    const size_t pb = pixel_bytes(p->pixel_type), row = (size_t)width * pb, img = row * height;
     const size_t stride = (img + 255) & ~(size_t)255;
     cudaError_t e;
     if ((e = p->host_frames.ensure(2 * stride * num_pairs)) != cudaSuccess ||
         (e = p->host_table.ensure(sizeof(qlpiv_frame) * num_pairs)) != cudaSuccess)
         return cuda_fail(e, "frame buffers");
-    std::vector<qlpiv_frame> t(num_pairs);
+    t.resize(num_pairs);
     char *base = p->host_frames.as<char>();
     for (int q = 0; q < num_pairs; q++) {
         char *da = base + 2 * q * stride, *db = base + (2 * q + 1) * stride;
@@ -615,6 +616,64 @@ qlpiv_status qlpiv_piv_adaptive(qlpiv_handle *h, const qlpiv_adaptive_desc *desc
     if ((e = cudaMemcpyAsync(p->host_table.p, t.data(), sizeof(qlpiv_frame) * num_pairs, cudaMemcpyHostToDevice,
                              s)) != cudaSuccess)
         return cuda_fail(e, "frame table upload");
+    return QLPIV_OK;
+}
+
+// Queues the optical flow after PIV of every pair on the last level's tiles (in place in
+// d_u/d_v).  frames: host-side copy of the device frame table (image pointers per pair).
+// dense_u/dense_v: device, pairs x height x width, or NULL.
+static qlpiv_status queue_flow(qlpiv_handle *h, const qlpiv_flow_desc &fd, const qlpiv_frame *frames,
+                               float *dense_u, float *dense_v, std::vector<float> &weights) {
+    AdaptivePlan *p = h->plan;
+    LevelPlan &L = p->levels.back();
+    cudaStream_t s = h->stream;
+    const int ni = L.g.tiles_i, nj = L.g.tiles_j;
+    const long cnt = L.count(), np = (long)p->height * p->width;
+    FlowBufs fb;
+    cudaError_t e;
+    if ((e = flow_buffers(p->flow, p->height, p->width, ni, nj, fd.iterations_ls, &fb)) != cudaSuccess ||
+        (e = upload_flow_weights(s, fd, fb, weights)) != cudaSuccess)
+        return cuda_fail(e, "flow buffers");
+    for (int q = 0; q < p->pairs; q++) {
+        StageScope sc(h, "flow", (int)p->levels.size() - 1, L.g.n, 0, np);
+        long launches = 0;
+        if ((e = run_flow(s, fd, p->pixel_type, frames[q].img_a, frames[q].img_b, frames[q].pitch, p->height,
+                          p->width, L.g.n, ni, nj, L.d_cy.as<double>(), L.d_cx.as<double>(), L.d_cyf.as<float>(),
+                          L.d_cxf.as<float>(), L.d_tops.as<int>(), L.d_lefts.as<int>(), L.d_u.as<float>() + q * cnt,
+                          L.d_v.as<float>() + q * cnt, dense_u ? dense_u + q * np : nullptr,
+                          dense_v ? dense_v + q * np : nullptr, fb, &launches)) != cudaSuccess)
+            return cuda_fail(e, "optical flow after PIV");
+        h->launches += launches;
+    }
+    return QLPIV_OK;
+}
+
+static qlpiv_status check_flow_grid(qlpiv_handle *h) {
+    LevelPlan &L = h->plan->levels.back();
+    if (L.g.tiles_i < 3 || L.g.tiles_j < 3)
+        return fail(QLPIV_E_SHAPE, "last level has %d x %d tiles: the flow spline needs at least 3 per axis",
+                    L.g.tiles_i, L.g.tiles_j);
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_piv_adaptive(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int pixel_type, int height,
+                                int width, int num_pairs, const qlpiv_frame *frames, float *out_u, float *out_v) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    qlpiv_status st = check_adaptive(desc, pixel_type, height, width);
+    if (st != QLPIV_OK) return st;
+    if (num_pairs < 0) return fail(QLPIV_E_ARG, "num_pairs < 0");
+    if (num_pairs == 0) return QLPIV_OK;
+    if (!frames || !out_u || !out_v) return fail(QLPIV_E_ARG, "NULL frame table or output");
+    if ((st = check_host_frames(frames, num_pairs, height, width)) != QLPIV_OK) return st;
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    if ((st = build_plan(h, desc, pixel_type, height, width, num_pairs)) != QLPIV_OK) return st;
+    AdaptivePlan *p = h->plan;
+    cudaStream_t s = h->stream;
+    cudaError_t e;
+    std::vector<qlpiv_frame> t;
+    if ((st = upload_host_frames(h, frames, t)) != QLPIV_OK) return st;
     if ((st = run_levels(h, p->host_table.as<qlpiv_frame>())) != QLPIV_OK) return st;
     LevelPlan &L = p->levels.back();
     const size_t bytes = sizeof(float) * L.count() * num_pairs;
@@ -622,6 +681,89 @@ qlpiv_status qlpiv_piv_adaptive(qlpiv_handle *h, const qlpiv_adaptive_desc *desc
         (e = cudaMemcpyAsync(out_v, L.d_v.p, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
         return cuda_fail(e, "adaptive PIV");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_piv_flow(qlpiv_handle *h, const qlpiv_adaptive_desc *piv, const qlpiv_flow_desc *flow,
+                            int pixel_type, int height, int width, int num_pairs, const qlpiv_frame *frames,
+                            float *out_u, float *out_v, float *dense_u, float *dense_v) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    qlpiv_status st = check_adaptive(piv, pixel_type, height, width);
+    if (st != QLPIV_OK) return st;
+    if (const char *m = check_flow_desc(flow)) return fail(QLPIV_E_ARG, "%s", m);
+    if (num_pairs < 0) return fail(QLPIV_E_ARG, "num_pairs < 0");
+    if (num_pairs == 0) return QLPIV_OK;
+    if (!frames || !out_u || !out_v) return fail(QLPIV_E_ARG, "NULL frame table or output");
+    if ((st = check_host_frames(frames, num_pairs, height, width)) != QLPIV_OK) return st;
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    if ((st = build_plan(h, piv, pixel_type, height, width, num_pairs)) != QLPIV_OK) return st;
+    if ((st = check_flow_grid(h)) != QLPIV_OK) return st;
+    AdaptivePlan *p = h->plan;
+    cudaStream_t s = h->stream;
+    cudaError_t e;
+    std::vector<qlpiv_frame> t;
+    std::vector<float> weights;
+    if ((st = upload_host_frames(h, frames, t)) != QLPIV_OK) return st;
+    if ((st = run_levels(h, p->host_table.as<qlpiv_frame>())) != QLPIV_OK) return st;
+    const size_t np = (size_t)height * width;
+    float *du = nullptr, *dv = nullptr;
+    if (dense_u || dense_v) {
+        if ((e = p->flow_dense.ensure(sizeof(float) * 2 * np * num_pairs)) != cudaSuccess)
+            return cuda_fail(e, "dense field buffer");
+        du = p->flow_dense.as<float>();
+        dv = du + np * num_pairs;
+    }
+    if ((st = queue_flow(h, *flow, t.data(), du, dv, weights)) != QLPIV_OK) return st;
+    LevelPlan &L = p->levels.back();
+    const size_t bytes = sizeof(float) * L.count() * num_pairs, db = sizeof(float) * np * num_pairs;
+    if ((e = cudaMemcpyAsync(out_u, L.d_u.p, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(out_v, L.d_v.p, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (dense_u && (e = cudaMemcpyAsync(dense_u, du, db, cudaMemcpyDeviceToHost, s)) != cudaSuccess) ||
+        (dense_v && (e = cudaMemcpyAsync(dense_v, dv, db, cudaMemcpyDeviceToHost, s)) != cudaSuccess) ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "PIV with optical flow");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_piv_flow_device(qlpiv_handle *h, const qlpiv_adaptive_desc *piv, const qlpiv_flow_desc *flow,
+                                   int pixel_type, int height, int width, int num_pairs, const qlpiv_frame *frames,
+                                   float *out_u, float *out_v, float *dense_u, float *dense_v) {
+    if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
+    qlpiv_status st = check_adaptive(piv, pixel_type, height, width);
+    if (st != QLPIV_OK) return st;
+    if (const char *m = check_flow_desc(flow)) return fail(QLPIV_E_ARG, "%s", m);
+    if (num_pairs < 0) return fail(QLPIV_E_ARG, "num_pairs < 0");
+    if (num_pairs == 0) return QLPIV_OK;
+    if (!frames || !out_u || !out_v) return fail(QLPIV_E_ARG, "NULL frame table or output");
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    if ((st = build_plan(h, piv, pixel_type, height, width, num_pairs)) != QLPIV_OK) return st;
+    if ((st = check_flow_grid(h)) != QLPIV_OK) return st;
+    AdaptivePlan *p = h->plan;
+    cudaStream_t s = h->stream;
+    cudaError_t e;
+    // the flow stages take image pointers on the host side: read the device table once
+    std::vector<qlpiv_frame> t(num_pairs);
+    std::vector<float> weights;
+    if ((e = cudaMemcpyAsync(t.data(), frames, sizeof(qlpiv_frame) * num_pairs, cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "frame table read");
+    for (int q = 0; q < num_pairs; q++)
+        if (!t[q].img_a || !t[q].img_b || t[q].height != height || t[q].width != width || t[q].pitch < width)
+            return fail(QLPIV_E_SHAPE, "frame %d: NULL image or size differs from %d x %d", q, height, width);
+    if ((st = run_levels(h, frames)) != QLPIV_OK) return st;
+    if ((st = queue_flow(h, *flow, t.data(), dense_u, dense_v, weights)) != QLPIV_OK) return st;
+    LevelPlan &L = p->levels.back();
+    const size_t bytes = sizeof(float) * L.count() * num_pairs;
+    if ((e = cudaMemcpyAsync(out_u, L.d_u.p, bytes, cudaMemcpyDeviceToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(out_v, L.d_v.p, bytes, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "PIV with optical flow output");
+    // the filter weights' host staging must outlive the queued upload
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "PIV with optical flow");
     return QLPIV_OK;
 }
 

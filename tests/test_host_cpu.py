@@ -32,6 +32,38 @@ def test_library_exports_header_symbols(qp):
     assert qp.load_library().qlpiv_abi_version() == 1
 
 
+def test_ctypes_structs_match_header(qp, tmp_path):
+    """Every ctypes / numpy mirror has the size and field offsets the C compiler gives the
+    header's structs."""
+    import ctypes
+    import subprocess
+    mirrors = {"qlpiv_pass_desc": qp.PassDesc, "qlpiv_frame": qp.Frame, "qlpiv_grid": qp.Grid,
+               "qlpiv_adaptive_desc": qp.AdaptiveDesc, "qlpiv_flow_desc": qp.FlowDesc,
+               "qlpiv_stage_time": qp.StageTime, "qlpiv_params": qp.Params}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "qlpiv.h"', "int main(void) {"]
+    for name, cls in mirrors.items():
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{name}.{f} %zu\\n", offsetof({name}, {f}));')
+    lines.append('printf("qlpiv_vector %zu\\n", sizeof(qlpiv_vector));')
+    for f in qp.VECTOR_DTYPE.names:
+        lines.append(f'printf("qlpiv_vector.{f} %zu\\n", offsetof(qlpiv_vector, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                        text=True).stdout.splitlines())
+    for name, cls in mirrors.items():
+        assert int(got[name]) == ctypes.sizeof(cls), name
+        for f, _ in cls._fields_:
+            assert int(got[f"{name}.{f}"]) == getattr(cls, f).offset, (name, f)
+    assert int(got["qlpiv_vector"]) == qp.VECTOR_DTYPE.itemsize
+    for f in qp.VECTOR_DTYPE.names:
+        assert int(got[f"qlpiv_vector.{f}"]) == qp.VECTOR_DTYPE.fields[f][1], f
+
+
 def test_create_without_gpu_reports_no_device(qp):
     torch = pytest.importorskip("torch")
     if torch.cuda.is_available():

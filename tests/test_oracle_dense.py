@@ -88,3 +88,53 @@ def test_liu_shen_matches_python_fixture(oracle, dense):
         assert np.abs(vn[k] - dense[f"ls_vnews{k}"]).max() <= 1e-3, k
     # output orientation: columns <- vnew, rows <- unew of the last pass
     assert np.array_equal(u, vn[-1]) and np.array_equal(v, un[-1])
+
+
+def _flow_case(oracle, h=96, w=112, n=16, seed=0):
+    rng = np.random.default_rng(seed)
+    a = rng.integers(0, 255, (h, w)).astype(np.uint8)
+    b = np.roll(a, (1, 2), axis=(0, 1))
+    _, tops, lefts = oracle.grid(h, w, n, 0, 0.5)
+    tu = rng.normal(1.0, 0.2, (len(tops), len(lefts))).astype(np.float32)
+    tv = rng.normal(2.0, 0.2, (len(tops), len(lefts))).astype(np.float32)
+    return a, b, tops, lefts, tu, tv
+
+
+@pytest.mark.parametrize("mode,dense", [(1, False), (1, True), (2, False), (2, True)])
+def test_flow_after_piv_is_the_stage_composition(oracle, mode, dense):
+    """orc_flow_after_piv equals the pinned stages chained by hand (DenseLucasKanade /
+    DenseLiuShen AparapiJobInterpolator.interpolate(stepTilesA, stepTilesB))."""
+    n = 16
+    a, b, tops, lefts, tu, tv = _flow_case(oracle, n=n)
+    h, w = a.shape
+    u, v, du, dv = oracle.flow_after_piv(a, b, n, tops, lefts, tu, tv, mode=mode, iterations_ls=12,
+                                         dense_export=dense)
+    ys = (tops + n / 2.0 - 0.5).astype(np.float32)
+    xs = (lefts + n / 2.0 - 0.5).astype(np.float32)
+    fu, fv = oracle.displacement_field(ys, xs, tu, tv, h, w, offset=0.0 if dense else 0.5)
+    us, vs = oracle.dense_lk(oracle.gauss_filter(a, 2.0, 3), oracle.gauss_filter(b, 2.0, 3), fv, fu, 27, 5,
+                             half_pixel=not dense)
+    if mode == 2:
+        la = oracle.normalize(oracle.gauss_filter(a, 0.48, 5))
+        lb = oracle.normalize(oracle.gauss_filter(b, 0.48, 5))
+        us, vs = oracle.liu_shen(la, lb, us, vs, 4.0, 12, half_pixel=not dense)
+    np.testing.assert_array_equal(du, vs)
+    np.testing.assert_array_equal(dv, us)
+    ci = tops + n // 2 - 1
+    cj = lefts + n // 2 - 1
+    if dense:
+        def avg(f):
+            return (((f[np.ix_(ci, cj)] + f[np.ix_(ci, cj + 1)]) + f[np.ix_(ci + 1, cj)]) +
+                    f[np.ix_(ci + 1, cj + 1)]) / np.float32(4.0)
+        eu, ev = avg(vs), avg(us)
+    else:
+        eu, ev = vs[np.ix_(ci, cj)], us[np.ix_(ci, cj)]
+    np.testing.assert_array_equal(u, eu)
+    np.testing.assert_array_equal(v, ev)
+
+
+def test_flow_after_piv_still_images_stay_still(oracle):
+    a, _, tops, lefts, tu, tv = _flow_case(oracle, seed=3)
+    z = np.zeros_like(tu)
+    u, v, du, dv = oracle.flow_after_piv(a, a, 16, tops, lefts, z, z, mode=2, iterations_ls=5)
+    assert not u.any() and not v.any() and not du.any() and not dv.any()
