@@ -160,6 +160,109 @@ WORKLOAD = ("adaptive-1024-u12: 1024x1024 12-bit pairs, IA 64 -> 32 -> 16 at 75 
             "<= 2 sweeps) after every level")
 
 
+# Hybrid PIV + dense optical flow (1024x1024 u8, one 32x32 pass at 50 % overlap, then dense
+# Lucas-Kanade (prefilter sigma 2.0, 3 px; window 27; 5 iterations) and Liu-Shen (lambda 4,
+# prefilter sigma 0.48, 5 px; 60 passes), dense field exported).
+HYBRID_PAIRS = 8
+HYBRID_WORKLOAD = ("hybrid-1024-u8: 1024x1024 u8 vortex pairs (0.05 ppp, max 3 px), one 32x32 PIV pass at 50 % "
+                   "overlap, then dense Lucas-Kanade (sigma 2.0, window 27, 5 iterations) and Liu-Shen (lambda 4, "
+                   "sigma 0.48, 60 passes), FP32 dense field")
+
+
+def hybrid_descs(pkg):
+    piv = pkg.adaptive_desc(32, 32, 0.5, warp_mode=pkg.WARP_NONE, norm_mode=pkg.NORM_MAX_A, max_mode=pkg.MAX_COMPUTE)
+    flow = pkg.flow_desc(mode=pkg.FLOW_LIU_SHEN, filter_sigma_lk=2.0, filter_px_lk=3, window_lk=27, iterations_lk=5,
+                         filter_sigma_ls=0.48, filter_px_ls=5, lambda_ls=4.0, iterations_ls=60, dense_export=True)
+    return piv, flow
+
+
+def run_hybrid(pkg, h, dev, stream, steps, warmup):
+    """Config-4 step: PIV + flow of HYBRID_PAIRS pairs resident in HBM, dense field out."""
+    import torch
+    piv, flow = hybrid_descs(pkg)
+    hp = HYBRID_PAIRS
+    pairs = [pkg.synth.config4_pair(pair_id=k) for k in range(4)]
+    imgs = torch.empty((hp, 2, H, W), dtype=torch.uint8, device=dev)
+    for k in range(hp):
+        a, b = pairs[k % len(pairs)]
+        imgs[k, 0].copy_(torch.from_numpy(a))
+        imgs[k, 1].copy_(torch.from_numpy(b))
+    table = np.zeros(hp, pkg.FRAME_DTYPE)
+    for k in range(hp):
+        table[k] = (imgs[k, 0].data_ptr(), imgs[k, 1].data_ptr(), H, W, W)
+    dtable = torch.from_numpy(table.view(np.uint8)).to(dev)
+    last = pkg.adaptive_levels(piv, H, W)[-1]
+    tiles = last["tiles_i"] * last["tiles_j"]
+    ou = torch.empty(hp * tiles, dtype=torch.float32, device=dev)
+    ov = torch.empty_like(ou)
+    du = torch.empty((hp, H, W), dtype=torch.float32, device=dev)
+    dv = torch.empty_like(du)
+
+    def step():
+        h.piv_flow_device(piv, flow, pkg.PIX_U8, H, W, hp, dtable, ou, ov, du, dv)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    launches0 = h.launches
+    t0.record(stream)
+    for _ in range(steps):
+        step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / steps
+    launches = (h.launches - launches0) // steps
+    # per-kernel split from the library's stage events (flow = the whole flow stage of a pair)
+    h.profile(True)
+    h.profile_read()
+    step()
+    stages = h.profile_read()
+    h.profile(False)
+    # e2e: host frames in, tile vectors and dense field out
+    fa = [pairs[k % len(pairs)][0] for k in range(hp)]
+    fb = [pairs[k % len(pairs)][1] for k in range(hp)]
+    h.piv_flow(fa, fb, piv, flow, dense=True)
+    e2e_steps = 2
+    tt = time.perf_counter()
+    for _ in range(e2e_steps):
+        h.piv_flow(fa, fb, piv, flow, dense=True)
+    e2e_s = (time.perf_counter() - tt) / e2e_steps
+    px = float(H * W)
+    return {
+        "workload": HYBRID_WORKLOAD, "pairs_per_step": hp, "ms_per_step": ms, "frame_pairs_per_s": hp / (ms * 1e-3),
+        "dense_mpx_per_s": hp * px / (ms * 1e-3) / 1e6, "gpu_launches_per_step": launches,
+        "stages": [{"stage": st["stage"], "ia_side": st["ia_side"], "ms_per_step": st["ms"]} for st in stages],
+        "e2e": {"value": hp / e2e_s, "unit": "frame-pairs/s", "h2d_bytes_per_step": hp * 2 * H * W,
+                "d2h_bytes_per_step": hp * (2 * tiles + 2 * H * W) * 4},
+    }
+
+
+def run_per_call(pkg, dev, desc, pairs_host, count):
+    """The plain per-call GPU path: one pair at a time, one synchronous library call per stage
+    (inheritance, warp, correlation pass, validation), host arrays in and out."""
+    h2 = pkg.Handle(dev.index)
+    try:
+        a, b = pairs_host[0]
+        pkg.per_call.piv_adaptive_per_call(h2, a, b, desc)
+        t0 = time.perf_counter()
+        for k in range(count):
+            a, b = pairs_host[k % len(pairs_host)]
+            pkg.per_call.piv_adaptive_per_call(h2, a, b, desc)
+        per_call_s = (time.perf_counter() - t0) / count
+        # one pair per call through the fused host API (no per-stage round trips)
+        h2.piv_adaptive([a], [b], desc)
+        t0 = time.perf_counter()
+        for k in range(count):
+            a, b = pairs_host[k % len(pairs_host)]
+            h2.piv_adaptive([a], [b], desc)
+        per_pair_s = (time.perf_counter() - t0) / count
+    finally:
+        h2.close()
+    return 1.0 / per_call_s, 1.0 / per_pair_s
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -314,6 +417,15 @@ def run_gpu(args, rank, world):
         result["compute_roofline"] = {"bound": "fp32", "achieved": alg_flops / t_launch / 1e12, "peak": fp32_peak,
                                       "unit": "TFLOP/s", "frac": alg_flops / t_launch / 1e12 / fp32_peak,
                                       "kernel": kernel, "peak_source": "live FP32 FMA probe (qlpiv_measure_fp32_peak)"}
+    # ---- the plain per-call GPU path on the same workload (denominator of the batching gain) ----
+    pc_value, pp_value = run_per_call(pkg, dev, desc, pairs_host, 4)
+    result["plain_per_call"] = {
+        "value": world * pc_value, "unit": "frame-pairs/s",
+        "sample": "4 pairs, one at a time, one synchronous library call per stage (host arrays in and out)",
+        "value_vs": pairs_per_s / pc_value, "e2e_vs": e2e_val / (world * pc_value),
+        "one_pair_per_call_fused": world * pp_value}
+    if not args.no_hybrid:
+        result["hybrid"] = run_hybrid(pkg, h, dev, stream, max(2, min(args.steps, 5)), max(3, args.warmup))
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         t_cpu = cpu_baseline(pkg, pairs_host[0], threads)
@@ -333,6 +445,7 @@ def main():
     ap.add_argument("--pairs", type=int, default=48)
     ap.add_argument("--unique", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-hybrid", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -357,6 +357,20 @@ typedef enum {
     QLPIV_FLOW_LIU_SHEN = 2       /* dense Lucas-Kanade followed by Liu-Shen */
 } qlpiv_flow_mode;
 
+/* IgnorePIVBaseDisplacementsModeEnum (S/IgnorePIVBaseDisplacementsModeEnum.java): what the flow
+ * stage keeps of the PIV field before Lucas-Kanade (the interpolators' interpolate(stepTilesA,
+ * stepTilesB)).  IGNORE_V / IGNORE_U name the reference's axes: IGNORE_V fills the row
+ * component, IGNORE_U the column component, with 0 (dense export) or 0.5; AUTO / AUTO_SMALL zero
+ * components below 3 / 0.9 px in magnitude. */
+typedef enum {
+    QLPIV_IGNORE_PIV_NONE = 0,
+    QLPIV_IGNORE_PIV_U = 1,
+    QLPIV_IGNORE_PIV_V = 2,
+    QLPIV_IGNORE_PIV_UV = 3,
+    QLPIV_IGNORE_PIV_AUTO = 4,
+    QLPIV_IGNORE_PIV_AUTO_SMALL = 5
+} qlpiv_ignore_piv;
+
 typedef struct qlpiv_flow_desc {
     int mode;               /* qlpiv_flow_mode */
     float filter_sigma_lk;  /* Lucas-Kanade prefilter (GaussianFilter2D) */
@@ -368,7 +382,8 @@ typedef struct qlpiv_flow_desc {
     float lambda_ls;        /* Liu-Shen Lagrange multiplier */
     int iterations_ls;
     int dense_export;       /* denseVectors: whole-pixel field and dense output */
-    int reserved[6];
+    int ignore_piv;         /* qlpiv_ignore_piv: ignorePIVBaseDisplacements(Mode) */
+    int reserved[5];
 } qlpiv_flow_desc;
 
 /* The optical flow after PIV of one frame pair on the last adaptive step's grid (tiles of side

@@ -319,7 +319,7 @@ int orc_liu_shen(const float *la, const float *lb, int h, int w, float *us, floa
 void orc_flow_after_piv(const float *img_a, const float *img_b, int h, int w, int n, int ni, int nj, const int *tops,
                         const int *lefts, float *tu, float *tv, int mode, float sigma_lk, int px_lk, float sigma_ls,
                         int px_ls, int window, int iters_lk, float lambda, int iters_ls, int dense_export,
-                        float *dense_u, float *dense_v) {
+                        int ignore_piv, float *dense_u, float *dense_v) {
     const long np = (long)h * w;
     float *lka = (float *)malloc(sizeof(float) * np), *lkb = (float *)malloc(sizeof(float) * np);
     float *lsa = NULL, *lsb = NULL;
@@ -344,6 +344,18 @@ void orc_flow_after_piv(const float *img_a, const float *img_b, int h, int w, in
     float *fu = (float *)malloc(sizeof(float) * np), *fv = (float *)malloc(sizeof(float) * np);
     const float off = dense_export ? 0.0f : 0.5f;
     orc_displacement_field_off(ys, ni, xs, nj, tu, tv, h, w, 0, off, off, fu, fv);
+    /* ignorePIVBaseDisplacements (DenseLucasKanadeAparapiJobInterpolator.java:233-277) */
+    if (ignore_piv == 4 || ignore_piv == 5) {
+        const float lim = ignore_piv == 4 ? 3.0f : 0.9f;
+        for (long p = 0; p < np; p++) {
+            if (fabsf(fu[p]) < lim) fu[p] = 0.0f;
+            if (fabsf(fv[p]) < lim) fv[p] = 0.0f;
+        }
+    }
+    if (ignore_piv == 2 || ignore_piv == 3)
+        for (long p = 0; p < np; p++) fu[p] = dense_export ? 0.0f : 0.5f;
+    if (ignore_piv == 1 || ignore_piv == 3)
+        for (long p = 0; p < np; p++) fv[p] = dense_export ? 0.0f : 0.5f;
     /* the flow jobs take columns (us) and rows (vs) */
     float *us = fv, *vs = fu;
     const int half = dense_export ? 0 : 1;

@@ -113,17 +113,18 @@ def set_validation(d, num_peaks=3, peak_kernel=3, threshold=2.0, epsilon0=0.1, m
 
 
 FLOW_LUCAS_KANADE, FLOW_LIU_SHEN = 1, 2
+IGNORE_PIV_NONE, IGNORE_PIV_U, IGNORE_PIV_V, IGNORE_PIV_UV, IGNORE_PIV_AUTO, IGNORE_PIV_AUTO_SMALL = range(6)
 
 
 class FlowDesc(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("filter_sigma_lk", ctypes.c_float), ("filter_px_lk", ctypes.c_int),
                 ("filter_sigma_ls", ctypes.c_float), ("filter_px_ls", ctypes.c_int), ("window_lk", ctypes.c_int),
                 ("iterations_lk", ctypes.c_int), ("lambda_ls", ctypes.c_float), ("iterations_ls", ctypes.c_int),
-                ("dense_export", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+                ("dense_export", ctypes.c_int), ("ignore_piv", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
 
 
 def flow_desc(mode=FLOW_LUCAS_KANADE, filter_sigma_lk=2.0, filter_px_lk=3, filter_sigma_ls=0.48, filter_px_ls=5,
-              window_lk=27, iterations_lk=5, lambda_ls=4.0, iterations_ls=60, dense_export=False):
+              window_lk=27, iterations_lk=5, lambda_ls=4.0, iterations_ls=60, dense_export=False, ignore_piv=0):
     """Optical flow after PIV (OpticalFlowAfterPIV Lucas-Kanade or Liu-Shen interpolator
     options); dense_export selects whole-pixel evaluation and the dense field export."""
     d = FlowDesc()
@@ -131,6 +132,7 @@ def flow_desc(mode=FLOW_LUCAS_KANADE, filter_sigma_lk=2.0, filter_px_lk=3, filte
     d.filter_sigma_ls, d.filter_px_ls, d.window_lk, d.iterations_lk = filter_sigma_ls, filter_px_ls, window_lk, \
         iterations_lk
     d.lambda_ls, d.iterations_ls, d.dense_export = lambda_ls, iterations_ls, int(dense_export)
+    d.ignore_piv = ignore_piv
     return d
 
 
@@ -639,4 +641,4 @@ class Handle:
                                                    a[0], a[1], a[2]))
 
 
-from . import grid, jobs, synth  # noqa: E402,F401
+from . import grid, jobs, per_call, synth  # noqa: E402,F401

@@ -108,20 +108,97 @@ __device__ __forceinline__ float warp_read(const float *img, int h, int w, float
     return __fadd_rn(__fmul_rn(omi, top), __fmul_rn(di, bot));
 }
 
-__global__ void __launch_bounds__(kLkTile *kLkTile) dense_lk_kernel(const float *A, const float *B, int h, int w,
-                                                                     float *us, float *vs, int W, int iterations,
+// One axis of a Lucas-Kanade window: sample k (0 <= k < W) sits at fl(o + k) and reads the
+// pixels floor(fl(o + k)) and the next one with the fraction as weight.  For o >= 1 the samples
+// of one binade are exact (o + k needs no rounding); past the next power of two they round to the
+// coarser spacing, by the same amount for every k (k is a multiple of twice that spacing).  So
+// when the window spans at most one boundary and the anchors stay contiguous, anchor(k) = base + k
+// and the fraction is f1 below `split`, f2 from `split` on: exactly the per-sample arithmetic.
+struct LkAxis {
+    int base, split;
+    float f1, f2;
+};
+
+__device__ __forceinline__ bool lk_axis(float o, int W, LkAxis &ax) {
+    if (!(o >= 1.0f) || !(o < 1048576.0f)) return false;
+    const unsigned eo = __float_as_uint(o) >> 23;
+    const unsigned el = __float_as_uint(__fadd_rn(o, (float)(W - 1))) >> 23;
+    ax.base = (int)o;
+    ax.f1 = __fsub_rn(o, (float)ax.base);
+    if (el == eo) {
+        ax.split = W;
+        ax.f2 = ax.f1;
+        return true;
+    }
+    if (el != eo + 1) return false;
+    const float t = __uint_as_float((eo + 1) << 23);   // the boundary 2^(e+1); t - o is exact
+    const int split = (int)ceilf(__fsub_rn(t, o));     // first k with o + k >= t
+    const float ls = __fadd_rn(o, (float)split);
+    const int as = (int)ls;
+    if (as != ax.base + split) return false;           // the rounding moved the anchor
+    ax.split = split;
+    ax.f2 = __fsub_rn(ls, (float)as);
+    return true;
+}
+
+// The window sums b0, b1 of one iteration with the sample rows in registers (window side WT).
+// br: B at (ay.base, ax.base); g: the thread's first window point.  SPLIT: the column fraction
+// changes at ax.split (selected per column from a bit mask), else it is ax.f1 throughout.
+template <int WT, bool SPLIT>
+__device__ __forceinline__ void lk_rows(const float *br, int w, const float4 *g, int GS, const LkAxis &ay,
+                                        const LkAxis &ax, float &b0, float &b1) {
+    const unsigned upper = SPLIT ? ~((1u << ax.split) - 1u) : 0u;  // columns past the boundary
+    const float omj1 = __fsub_rn(1.0f, ax.f1), omj2 = __fsub_rn(1.0f, ax.f2);
+    float hb[WT];
+    float x0 = br[0];
+#pragma unroll
+    for (int b = 0; b < WT; b++) {
+        const bool up = SPLIT && ((upper >> b) & 1u);
+        const float x1 = br[b + 1];
+        hb[b] = __fadd_rn(__fmul_rn(up ? omj2 : omj1, x0), __fmul_rn(up ? ax.f2 : ax.f1, x1));
+        x0 = x1;
+    }
+#pragma unroll 1
+    for (int a = 0; a < WT; a++) {
+        const float di = a < ay.split ? ay.f1 : ay.f2, omi = __fsub_rn(1.0f, di);
+        br += w;
+        x0 = br[0];
+#pragma unroll
+        for (int b = 0; b < WT; b++) {
+            const bool up = SPLIT && ((upper >> b) & 1u);
+            const float x1 = br[b + 1];
+            const float bot = __fadd_rn(__fmul_rn(up ? omj2 : omj1, x0), __fmul_rn(up ? ax.f2 : ax.f1, x1));
+            x0 = x1;
+            const float smp = __fadd_rn(__fmul_rn(omi, hb[b]), __fmul_rn(di, bot));
+            hb[b] = bot;
+            const float4 t = g[b];
+            const float dT = __fsub_rn(smp, t.x);
+            b0 = __fadd_rn(__fmul_rn(dT, t.y), b0);
+            b1 = __fadd_rn(__fmul_rn(dT, t.z), b1);
+        }
+        g += GS;
+    }
+}
+
+// Dense LK over a 16 x 16 pixel tile.  Shared memory: the tile's window points as float4
+// (value of A, dj, di, unused), then a scratch area that first holds the staged A region and
+// later (WT = 0) one row of horizontally interpolated B samples per thread.  WT > 0: the window
+// side is WT and the rows of samples live in registers.
+template <int WT>
+__global__ void __launch_bounds__(kLkTile *kLkTile, WT > 0 ? 3 : 2) dense_lk_kernel(const float *A, const float *B, int h, int w,
+                                                                     float *us, float *vs, int W_, int iterations,
                                                                      int half_pixel) {
-    extern __shared__ float sm[];
+    extern __shared__ float4 sm4[];
+    const int W = WT > 0 ? WT : W_;
     const int hw = W / 2;
     const int RS = kLkTile + W + 1;  // staged region side: window span + derivative margin
     const int GS = kLkTile + W - 1;  // window points of the tile
-    float *reg = sm;
-    float *val = reg + RS * RS;
-    float *gdj = val + GS * GS;
-    float *gdi = gdj + GS * GS;
+    constexpr int kThreads = kLkTile * kLkTile;
+    float4 *vg = sm4;                                   // GS x GS: (A, dj, di, 0)
+    float *reg = reinterpret_cast<float *>(vg + GS * GS);  // RS x RS during set-up
     const int tid = threadIdx.y * kLkTile + threadIdx.x;
     const int ti0 = blockIdx.y * kLkTile, tj0 = blockIdx.x * kLkTile;
-    for (int q = tid; q < RS * RS; q += kLkTile * kLkTile) {
+    for (int q = tid; q < RS * RS; q += kThreads) {
         const int r = q / RS, c = q - r * RS;
         const int y = ti0 - hw - 1 + r, x = tj0 - hw - 1 + c;
         if (half_pixel) {
@@ -135,7 +212,7 @@ __global__ void __launch_bounds__(kLkTile *kLkTile) dense_lk_kernel(const float 
     }
     __syncthreads();
     const float c3 = 3.0f / 32.0f;
-    for (int q = tid; q < GS * GS; q += kLkTile * kLkTile) {
+    for (int q = tid; q < GS * GS; q += kThreads) {
         const int gy = q / GS, gx = q - gy * GS;
         const float *r0 = reg + gy * RS + gx, *r1 = r0 + RS, *r2 = r1 + RS;
         const float TL = r0[0], T = r0[1], TR = r0[2], L = r1[0], C = r1[1], R = r1[2], BL = r2[0], Bt = r2[1],
@@ -144,21 +221,20 @@ __global__ void __launch_bounds__(kLkTile *kLkTile) dense_lk_kernel(const float 
                                    __fdiv_rn(__fmul_rn(__fsub_rn(L, R), 10.0f), 32.0f));
         const float di = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TR, TL), BR), BL), c3),
                                    __fdiv_rn(__fmul_rn(__fsub_rn(T, Bt), 10.0f), 32.0f));
-        val[q] = C;
-        gdj[q] = dj;
-        gdi[q] = di;
+        vg[q] = make_float4(C, dj, di, 0.0f);
     }
-    __syncthreads();
+    __syncthreads();  // reg is dead from here on: its space becomes the per-thread rows
     const int pi = ti0 + threadIdx.y, pj = tj0 + threadIdx.x;
     if (pi >= h || pj >= w) return;
     float a00 = 0.0f, a01 = 0.0f, a11 = 0.0f;
     for (int a = 0; a < W; a++) {
-        const int base = (threadIdx.y + a) * GS + threadIdx.x;
+        const float4 *g = vg + (threadIdx.y + a) * GS + threadIdx.x;
+#pragma unroll(WT > 0 ? WT : 1)
         for (int b = 0; b < W; b++) {
-            const float dj = gdj[base + b], di = gdi[base + b];
-            a00 = __fadd_rn(__fmul_rn(dj, dj), a00);
-            a01 = __fadd_rn(__fmul_rn(dj, di), a01);
-            a11 = __fadd_rn(__fmul_rn(di, di), a11);
+            const float4 t = g[b];
+            a00 = __fadd_rn(__fmul_rn(t.y, t.y), a00);
+            a01 = __fadd_rn(__fmul_rn(t.y, t.z), a01);
+            a11 = __fadd_rn(__fmul_rn(t.z, t.z), a11);
         }
     }
     const long p = (long)pi * w + pj;
@@ -175,13 +251,57 @@ __global__ void __launch_bounds__(kLkTile *kLkTile) dense_lk_kernel(const float 
         if (locI < 0.0f || locI >= (float)(h + hw) || locJ < 0.0f || locJ >= (float)(w + hw)) break;
         float b0 = 0.0f, b1 = 0.0f;
         const float oi = __fsub_rn(locI, (float)hw), oj = __fsub_rn(locJ, (float)hw);
-        for (int a = 0; a < W; a++) {
-            const int base = (threadIdx.y + a) * GS + threadIdx.x;
-            const float li = __fadd_rn(oi, (float)a);
-            for (int b = 0; b < W; b++) {
-                const float dT = __fsub_rn(warp_read(B, h, w, li, __fadd_rn(oj, (float)b)), val[base + b]);
-                b0 = __fadd_rn(__fmul_rn(dT, gdj[base + b]), b0);
-                b1 = __fadd_rn(__fmul_rn(dT, gdi[base + b]), b1);
+        LkAxis ay, ax;
+        const bool fast = lk_axis(oi, W, ay) && lk_axis(oj, W, ax) && ay.base + W <= h - 1 &&
+                          ax.base + W <= w - 1 && (WT > 0 || (ay.split == W && ax.split == W));
+        if (fast) {
+            // Window row a reads B rows base + a (top) and base + a + 1 (bottom) with the row's
+            // weights; the horizontal interpolation of a B row is the bottom of window row a and
+            // the top of window row a + 1, so each is computed once.
+            const float *br = B + (long)ay.base * w + ax.base;
+            if constexpr (WT > 0) {
+                if (ax.split == WT)
+                    lk_rows<WT, false>(br, w, vg + threadIdx.y * GS + threadIdx.x, GS, ay, ax, b0, b1);
+                else
+                    lk_rows<WT, true>(br, w, vg + threadIdx.y * GS + threadIdx.x, GS, ay, ax, b0, b1);
+            } else {
+                float *hb = reinterpret_cast<float *>(vg + GS * GS) + tid;  // stride kThreads (bank = lane)
+                const float dj = ax.f1, omj = __fsub_rn(1.0f, dj);
+                const float di = ay.f1, omi = __fsub_rn(1.0f, di);
+                float x0 = br[0];
+                for (int b = 0; b < W; b++) {
+                    const float x1 = br[b + 1];
+                    hb[b * kThreads] = __fadd_rn(__fmul_rn(omj, x0), __fmul_rn(dj, x1));
+                    x0 = x1;
+                }
+                for (int a = 0; a < W; a++) {
+                    const float4 *g = vg + (threadIdx.y + a) * GS + threadIdx.x;
+                    br += w;
+                    x0 = br[0];
+                    for (int b = 0; b < W; b++) {
+                        const float x1 = br[b + 1];
+                        const float bot = __fadd_rn(__fmul_rn(omj, x0), __fmul_rn(dj, x1));
+                        x0 = x1;
+                        const float top = hb[b * kThreads];
+                        hb[b * kThreads] = bot;
+                        const float smp = __fadd_rn(__fmul_rn(omi, top), __fmul_rn(di, bot));
+                        const float4 t = g[b];
+                        const float dT = __fsub_rn(smp, t.x);
+                        b0 = __fadd_rn(__fmul_rn(dT, t.y), b0);
+                        b1 = __fadd_rn(__fmul_rn(dT, t.z), b1);
+                    }
+                }
+            }
+        } else {
+            for (int a = 0; a < W; a++) {
+                const float4 *g = vg + (threadIdx.y + a) * GS + threadIdx.x;
+                const float li = __fadd_rn(oi, (float)a);
+                for (int b = 0; b < W; b++) {
+                    const float4 t = g[b];
+                    const float dT = __fsub_rn(warp_read(B, h, w, li, __fadd_rn(oj, (float)b)), t.x);
+                    b0 = __fadd_rn(__fmul_rn(dT, t.y), b0);
+                    b1 = __fadd_rn(__fmul_rn(dT, t.z), b1);
+                }
             }
         }
         const float incU = __fadd_rn(__fmul_rn(b0, i00), __fmul_rn(b1, i01));
@@ -199,9 +319,22 @@ __global__ void __launch_bounds__(kLkTile *kLkTile) dense_lk_kernel(const float 
     us[p] = u;
 }
 
-size_t lk_smem(int W) {
-    const int RS = kLkTile + W + 1, GS = kLkTile + W - 1;
-    return sizeof(float) * ((size_t)RS * RS + 3 * (size_t)GS * GS);
+// WT > 0 keeps the sample rows in registers; WT = 0 needs W rows of floats per thread.
+size_t lk_smem(int W, bool rows_in_smem) {
+    const size_t RS = kLkTile + W + 1, GS = kLkTile + W - 1;
+    const size_t rows = rows_in_smem ? (size_t)W * kLkTile * kLkTile : 0;
+    return sizeof(float4) * GS * GS + sizeof(float) * (RS * RS > rows ? RS * RS : rows);
+}
+
+template <int WT>
+static cudaError_t launch_lk_t(cudaStream_t s, const float *a, const float *b, int h, int w, float *us, float *vs,
+                               int W, int iterations, int half_pixel) {
+    const size_t sm = lk_smem(W, WT == 0);
+    cudaError_t e = cudaFuncSetAttribute(dense_lk_kernel<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    dim3 blk(kLkTile, kLkTile), grd(blocks_of(w, kLkTile), blocks_of(h, kLkTile));
+    dense_lk_kernel<WT><<<grd, blk, sm, s>>>(a, b, h, w, us, vs, W, iterations, half_pixel);
+    return cudaGetLastError();
 }
 
 // ---------------- Liu-Shen ----------------
@@ -274,63 +407,127 @@ __global__ void ls_fixed_kernel(const float *la, const float *lb, int h, int w, 
     fx[7 * n + p] = __fdiv_rn(A11, det);
 }
 
-// One Jacobi pass: (us_in, vs_in) -> (us_out, vs_out); err[pass] accumulates the pass's
-// total error (double).  Once the previous pass's mean error is below 1e-8 the pass copies.
-__global__ void ls_pass_kernel(const float *fx, int h, int w, float lambda, const float *us_in, const float *vs_in,
-                               float *us_out, float *vs_out, double *err, int pass) {
-    const int pj = blockIdx.x * blockDim.x + threadIdx.x, pi = blockIdx.y * blockDim.y + threadIdx.y;
+// The Liu-Shen update of one pixel from its 3 x 3 neighbourhoods U (columns field) and V (rows
+// field) and its fixed terms.  INTERIOR: every neighbour exists, all weights are 1 and the
+// weighted sums are plain sums (x * 1.0f == x exactly).
+template <bool INTERIOR>
+__device__ __forceinline__ void ls_update(const float *U, const float *V, const float *wq, const float *fx, long n,
+                                          long p, float lambda, float &unew, float &vnew) {
+    const float IIx = fx[0 * n + p], IIy = fx[1 * n + p], II = fx[2 * n + p];
+    const float Ixt = fx[3 * n + p], Iyt = fx[4 * n + p];
+    const float B11 = fx[5 * n + p], B12 = fx[6 * n + p], B22 = fx[7 * n + p];
+    const int ring[7] = {kT, kTR, kL, kR, kBL, kB, kBR};
+    float sV, sU;
+    if (INTERIOR) {
+        sV = V[kTL];
+        sU = U[kTL];
+    } else {
+        sV = __fmul_rn(V[kTL], wq[kTL]);
+        sU = __fmul_rn(U[kTL], wq[kTL]);
+    }
+#pragma unroll
+    for (int t = 0; t < 7; t++) {
+        const int q = ring[t];
+        sV = __fadd_rn(sV, INTERIOR ? V[q] : __fmul_rn(V[q], wq[q]));
+        sU = __fadd_rn(sU, INTERIOR ? U[q] : __fmul_rn(U[q], wq[q]));
+    }
+    const float hu = __fadd_rn(__fmul_rn(lambda, sV), Ixt);
+    const float hv = __fadd_rn(__fmul_rn(lambda, sU), Iyt);
+    const float u_xy = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(U[kTL], U[kTR]), U[kBL]), U[kBR]), 4.0f);
+    const float v_xy = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(V[kTL], V[kTR]), V[kBL]), V[kBR]), 4.0f);
+    const float bu = __fadd_rn(
+        __fmul_rn(__fmul_rn(2.0f, IIx), __fdiv_rn(__fsub_rn(V[kB], V[kT]), 2.0f)),
+        __fadd_rn(__fmul_rn(IIx, __fdiv_rn(__fsub_rn(U[kR], U[kL]), 2.0f)),
+                  __fadd_rn(__fmul_rn(IIy, __fdiv_rn(__fsub_rn(U[kB], U[kT]), 2.0f)),
+                            __fadd_rn(__fmul_rn(II, __fadd_rn(V[kT], V[kB])), __fadd_rn(__fmul_rn(II, u_xy), hu)))));
+    const float bv = __fadd_rn(
+        __fmul_rn(__fmul_rn(2.0f, IIy), __fdiv_rn(__fsub_rn(U[kR], U[kL]), 2.0f)),
+        __fadd_rn(__fmul_rn(IIx, __fdiv_rn(__fsub_rn(V[kR], V[kL]), 2.0f)),
+                  __fadd_rn(__fmul_rn(IIy, __fdiv_rn(__fsub_rn(V[kB], V[kT]), 2.0f)),
+                            __fadd_rn(__fmul_rn(II, __fadd_rn(U[kL], U[kR])), __fadd_rn(__fmul_rn(II, v_xy), hv)))));
+    unew = -__fadd_rn(__fmul_rn(B11, bu), __fmul_rn(B12, bv));
+    vnew = -__fadd_rn(__fmul_rn(B12, bu), __fmul_rn(B22, bv));
+}
+
+// One Jacobi pass: (us_in, vs_in) -> (us_out, vs_out).  A pass's total error (the sum of the
+// pixels' update lengths, in double) is spread over kLsSlots accumulators err[pass][slot] so
+// that the CTAs' atomics do not queue on one address; once the previous pass's mean error is
+// below 1e-8 the pass copies.  A CTA of 32 x 8 threads covers 32 x (8 kLsRows) pixels.
+constexpr int kLsRows = 4;
+constexpr int kLsSlots = 32;
+
+// s + c += x exactly (TwoSum), so a thread's few errors need one conversion to double.
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float x) {
+    const float t = __fadd_rn(s, x);
+    const float bp = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+    s = t;
+    c = __fadd_rn(c, e);
+}
+
+__global__ void __launch_bounds__(256) ls_pass_kernel(const float *fx, int h, int w, float lambda,
+                                                      const float *us_in, const float *vs_in, float *us_out,
+                                                      float *vs_out, double *err, int pass) {
+    const int pj = blockIdx.x * blockDim.x + threadIdx.x;
     const long n = (long)h * w;
-    const bool stop = pass > 0 && err[pass - 1] / (double)n < 1e-8;
-    double e = 0.0;
-    if (pi < h && pj < w) {
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    __shared__ double wsum[8];
+    __shared__ bool stop_s;
+    if (t < 32) {  // the previous pass's total from its slots
+        double prev = pass > 0 ? err[(pass - 1) * kLsSlots + t] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) prev += __shfl_xor_sync(0xffffffffu, prev, o);
+        if (t == 0) stop_s = pass > 0 && prev / (double)n < 1e-8;
+    }
+    __syncthreads();
+    const bool stop = stop_s;
+    float es = 0.0f, ec = 0.0f;
+#pragma unroll
+    for (int r = 0; r < kLsRows; r++) {
+        const int pi = (blockIdx.y * kLsRows + r) * blockDim.y + threadIdx.y;
+        if (pi >= h || pj >= w) continue;
         const long p = (long)pi * w + pj;
         if (stop) {
             us_out[p] = us_in[p];
             vs_out[p] = vs_in[p];
+            continue;
+        }
+        float U[9], V[9], unew, vnew;
+        if (pi >= 1 && pi <= h - 2 && pj >= 1 && pj <= w - 2) {
+            const float *u0 = us_in + p - w - 1, *v0 = vs_in + p - w - 1;
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int b = 0; b < 3; b++) {
+                    U[a * 3 + b] = u0[(long)a * w + b];
+                    V[a * 3 + b] = v0[(long)a * w + b];
+                }
+            ls_update<true>(U, V, nullptr, fx, n, p, lambda, unew, vnew);
         } else {
-            float U[9], V[9], wq[9];
+            float wq[9];
             ls_load(us_in, h, w, pi, pj, 0, U);
             ls_load(vs_in, h, w, pi, pj, 0, V);
             ls_weights(pi, pj, h, w, wq);
-            const float IIx = fx[0 * n + p], IIy = fx[1 * n + p], II = fx[2 * n + p];
-            const float Ixt = fx[3 * n + p], Iyt = fx[4 * n + p];
-            const float B11 = fx[5 * n + p], B12 = fx[6 * n + p], B22 = fx[7 * n + p];
-            const int ring[7] = {kT, kTR, kL, kR, kBL, kB, kBR};
-            float sV = __fmul_rn(V[kTL], wq[kTL]), sU = __fmul_rn(U[kTL], wq[kTL]);
-#pragma unroll
-            for (int t = 0; t < 7; t++) {
-                const int q = ring[t];
-                sV = __fadd_rn(sV, __fmul_rn(V[q], wq[q]));
-                sU = __fadd_rn(sU, __fmul_rn(U[q], wq[q]));
-            }
-            const float hu = __fadd_rn(__fmul_rn(lambda, sV), Ixt);
-            const float hv = __fadd_rn(__fmul_rn(lambda, sU), Iyt);
-            const float u_xy = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(U[kTL], U[kTR]), U[kBL]), U[kBR]), 4.0f);
-            const float v_xy = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(V[kTL], V[kTR]), V[kBL]), V[kBR]), 4.0f);
-            const float bu = __fadd_rn(
-                __fmul_rn(__fmul_rn(2.0f, IIx), __fdiv_rn(__fsub_rn(V[kB], V[kT]), 2.0f)),
-                __fadd_rn(__fmul_rn(IIx, __fdiv_rn(__fsub_rn(U[kR], U[kL]), 2.0f)),
-                          __fadd_rn(__fmul_rn(IIy, __fdiv_rn(__fsub_rn(U[kB], U[kT]), 2.0f)),
-                                    __fadd_rn(__fmul_rn(II, __fadd_rn(V[kT], V[kB])), __fadd_rn(__fmul_rn(II, u_xy), hu)))));
-            const float bv = __fadd_rn(
-                __fmul_rn(__fmul_rn(2.0f, IIy), __fdiv_rn(__fsub_rn(U[kR], U[kL]), 2.0f)),
-                __fadd_rn(__fmul_rn(IIx, __fdiv_rn(__fsub_rn(V[kR], V[kL]), 2.0f)),
-                          __fadd_rn(__fmul_rn(IIy, __fdiv_rn(__fsub_rn(V[kB], V[kT]), 2.0f)),
-                                    __fadd_rn(__fmul_rn(II, __fadd_rn(U[kL], U[kR])), __fadd_rn(__fmul_rn(II, v_xy), hv)))));
-            const float unew = -__fadd_rn(__fmul_rn(B11, bu), __fmul_rn(B12, bv));
-            const float vnew = -__fadd_rn(__fmul_rn(B12, bu), __fmul_rn(B22, bv));
-            const float du = __fsub_rn(unew, V[kC]), dv = __fsub_rn(vnew, U[kC]);
-            e = (double)__fsqrt_rn(__fadd_rn(__fmul_rn(du, du), __fmul_rn(dv, dv)));
-            us_out[p] = vnew;  // columns <- vnew, rows <- unew (copyVectors)
-            vs_out[p] = unew;
+            ls_update<false>(U, V, wq, fx, n, p, lambda, unew, vnew);
         }
+        const float du = __fsub_rn(unew, V[kC]), dv = __fsub_rn(vnew, U[kC]);
+        two_sum_acc(es, ec, __fsqrt_rn(__fadd_rn(__fmul_rn(du, du), __fmul_rn(dv, dv))));
+        us_out[p] = vnew;  // columns <- vnew, rows <- unew (copyVectors)
+        vs_out[p] = unew;
     }
-    if (stop) {
-        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) err[pass] = err[pass - 1];
+    const unsigned bid = blockIdx.y * gridDim.x + blockIdx.x;
+    if (stop) {  // carry the previous total forward
+        if (bid == 0 && t < kLsSlots) err[pass * kLsSlots + t] = err[(pass - 1) * kLsSlots + t];
         return;
     }
+    double e = (double)es + (double)ec;
     for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
-    if (((threadIdx.y * blockDim.x + threadIdx.x) & 31) == 0 && e != 0.0) atomicAdd(&err[pass], e);
+    if ((t & 31) == 0) wsum[t >> 5] = e;
+    __syncthreads();
+    if (t == 0) {
+        double sum = 0.0;
+        for (int k = 0; k < (int)(blockDim.x * blockDim.y) / 32; k++) sum += wsum[k];
+        if (sum != 0.0) atomicAdd(&err[pass * kLsSlots + (bid % kLsSlots)], sum);
+    }
 }
 
 // Tile displacements from the dense field (rows vs, columns us) at top + n/2 - 1, left + n/2 - 1,
@@ -354,6 +551,23 @@ __global__ void tiles_from_dense_kernel(const float *us, const float *vs, int w,
     tile_v[t] = u;
 }
 
+// ignorePIVBaseDisplacements on the per-pixel PIV field fu (rows) / fv (columns)
+// (DenseLucasKanadeAparapiJobInterpolator.java:233-277).
+__global__ void ignore_piv_kernel(float *fu, float *fv, long n, int mode, float fill) {
+    const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float u = fu[p], v = fv[p];
+    if (mode == QLPIV_IGNORE_PIV_AUTO || mode == QLPIV_IGNORE_PIV_AUTO_SMALL) {
+        const float lim = mode == QLPIV_IGNORE_PIV_AUTO ? 3.0f : 0.9f;
+        if (fabsf(u) < lim) u = 0.0f;
+        if (fabsf(v) < lim) v = 0.0f;
+    }
+    if (mode == QLPIV_IGNORE_PIV_V || mode == QLPIV_IGNORE_PIV_UV) u = fill;
+    if (mode == QLPIV_IGNORE_PIV_U || mode == QLPIV_IGNORE_PIV_UV) v = fill;
+    fu[p] = u;
+    fv[p] = v;
+}
+
 }  // namespace
 
 size_t spline_coef_bytes(long tiles) { return (size_t)tiles * (6 * sizeof(double) + 2 * sizeof(float4)); }
@@ -364,6 +578,8 @@ const char *check_flow_desc(const qlpiv_flow_desc *d) {
     if (d->window_lk < 3 || d->window_lk > 31 || d->window_lk % 2 == 0)
         return "dense Lucas-Kanade: window size must be odd, 3..31";
     if (d->iterations_lk <= 0) return "dense Lucas-Kanade: Number of iterations must greater or equal to 1";
+    if (d->ignore_piv < QLPIV_IGNORE_PIV_NONE || d->ignore_piv > QLPIV_IGNORE_PIV_AUTO_SMALL)
+        return "unknown ignore-PIV mode";
     if (d->filter_px_lk < 1 || d->filter_px_lk % 2 == 0 || d->filter_px_lk > 63) return "Lucas-Kanade filter width";
     if (d->mode == QLPIV_FLOW_LIU_SHEN) {
         if (d->iterations_ls <= 0) return "dense Liu-Shen: Number of iterations must greater or equal to 1";
@@ -415,24 +631,30 @@ cudaError_t launch_normalize(cudaStream_t s, const float *in, long n, unsigned *
 
 cudaError_t launch_dense_lk(cudaStream_t s, const float *a, const float *b, int h, int w, float *us, float *vs, int W,
                             int iterations, int half_pixel) {
-    const size_t sm = lk_smem(W);
-    dim3 blk(kLkTile, kLkTile), grd(blocks_of(w, kLkTile), blocks_of(h, kLkTile));
-    dense_lk_kernel<<<grd, blk, sm, s>>>(a, b, h, w, us, vs, W, iterations, half_pixel);
-    return cudaGetLastError();
+    // the reference's example window (27) runs with its sample rows in registers
+    if (W == 27) return launch_lk_t<27>(s, a, b, h, w, us, vs, W, iterations, half_pixel);
+    return launch_lk_t<0>(s, a, b, h, w, us, vs, W, iterations, half_pixel);
 }
 
-// Liu-Shen passes on (us, vs) in place; fx: 8 planes, tmp: 2 planes, err: `iterations` doubles.
+// Liu-Shen passes on (us, vs) in place; fx: 8 planes, tmp: 2 planes, err: ls_err_bytes.
+size_t ls_err_bytes(int h, int w, int iterations) {
+    (void)h;
+    (void)w;
+    return sizeof(double) * kLsSlots * (size_t)(iterations > 0 ? iterations : 1);
+}
+
 cudaError_t launch_liu_shen(cudaStream_t s, const float *la, const float *lb, int h, int w, float *us, float *vs,
                             float lambda, int iterations, int half_pixel, float *fx, float *tmp, double *err) {
     dim3 blk(32, 8), grd(blocks_of(w, 32), blocks_of(h, 8));
     const long n = (long)h * w;
-    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(double) * iterations, s);
+    const dim3 pgrd(blocks_of(w, 32), blocks_of(h, 8 * kLsRows));
+    cudaError_t e = cudaMemsetAsync(err, 0, ls_err_bytes(h, w, iterations), s);
     if (e != cudaSuccess) return e;
     ls_fixed_kernel<<<grd, blk, 0, s>>>(la, lb, h, w, lambda, half_pixel, fx);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     float *cu = us, *cv = vs, *nu = tmp, *nv = tmp + n;
     for (int it = 0; it < iterations; it++) {
-        ls_pass_kernel<<<grd, blk, 0, s>>>(fx, h, w, lambda, cu, cv, nu, nv, err, it);
+        ls_pass_kernel<<<pgrd, blk, 0, s>>>(fx, h, w, lambda, cu, cv, nu, nv, err, it);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         float *t = cu; cu = nu; nu = t;
         t = cv; cv = nv; nv = t;
@@ -462,9 +684,14 @@ static cudaError_t filter_or_copy(cudaStream_t s, int pixel_type, const void *im
 cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, const void *img_a, const void *img_b,
                      long pitch, int h, int w, int n, int ni, int nj, const double *cy, const double *cx,
                      const float *cyf, const float *cxf, const int *tops, const int *lefts, float *tile_u,
-                     float *tile_v, float *dense_u, float *dense_v, const FlowBufs &b, long *launches) {
+                     float *tile_v, float *dense_u, float *dense_v, const FlowBufs &b, long *launches,
+                     const FlowMarks *marks, const SplineCoef *given) {
     cudaError_t e;
     const long np = (long)h * w;
+    auto mark = [&](const char *stage, bool begin) {
+        if (marks) marks->fn(marks->ctx, stage, begin);
+    };
+    mark("flow:prefilter", true);
     if ((e = filter_or_copy(s, pixel_type, img_a, pitch, h, w, d.filter_sigma_lk, b.k_lk, d.filter_px_lk, b.tmp, b.lka,
                             launches)) != cudaSuccess ||
         (e = filter_or_copy(s, pixel_type, img_b, pitch, h, w, d.filter_sigma_lk, b.k_lk, d.filter_px_lk, b.tmp, b.lkb,
@@ -480,23 +707,41 @@ cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, c
             return e;
         *launches += 4;
     }
+    mark("flow:prefilter", false);
+    mark("flow:field", true);
     // per-pixel field from the tiles (knots at the tile centres), offset 0.5 unless dense export
-    const SplineCoef coef = coef_view(b.coef, (long)ni * nj);
-    if ((e = launch_spline(s, 1, cy, b.cp, ni, cx, b.cp + ni, nj, tile_u, tile_v, coef)) != cudaSuccess) return e;
-    *launches += 4;
+    SplineCoef coef;
+    if (given) {  // solved by the caller (all pairs at once)
+        coef = *given;
+    } else {
+        coef = coef_view(b.coef, (long)ni * nj);
+        if ((e = launch_spline(s, 1, cy, b.cp, ni, cx, b.cp + ni, nj, tile_u, tile_v, coef)) != cudaSuccess) return e;
+        *launches += 4;
+    }
     const float off = d.dense_export ? 0.0f : 0.5f;
     if ((e = launch_field(s, h, w, cyf, ni, cxf, nj, coef, b.fu, b.fv, off, off)) != cudaSuccess) return e;
     *launches += 1;
+    if (d.ignore_piv != QLPIV_IGNORE_PIV_NONE) {
+        ignore_piv_kernel<<<blocks_of(np, 256), 256, 0, s>>>(b.fu, b.fv, np, d.ignore_piv,
+                                                             d.dense_export ? 0.0f : 0.5f);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        *launches += 1;
+    }
+    mark("flow:field", false);
     float *us = b.fv, *vs = b.fu;  // the flow jobs take columns (us) and rows (vs)
     const int half = d.dense_export ? 0 : 1;
+    mark("flow:lucas_kanade", true);
     if ((e = launch_dense_lk(s, b.lka, b.lkb, h, w, us, vs, d.window_lk, d.iterations_lk, half)) != cudaSuccess)
         return e;
     *launches += 1;
+    mark("flow:lucas_kanade", false);
     if (d.mode == QLPIV_FLOW_LIU_SHEN) {
+        mark("flow:liu_shen", true);
         if ((e = launch_liu_shen(s, b.lsa, b.lsb, h, w, us, vs, d.lambda_ls, d.iterations_ls, half, b.fx, b.fx + 8 * np,
                                  b.err)) != cudaSuccess)
             return e;
         *launches += 1 + d.iterations_ls;
+        mark("flow:liu_shen", false);
     }
     tiles_from_dense_kernel<<<blocks_of((long)ni * nj, 128), 128, 0, s>>>(us, vs, w, n, ni, nj, tops, lefts,
                                                                           d.dense_export, tile_u, tile_v);
@@ -513,7 +758,7 @@ cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, c
 cudaError_t flow_buffers(DevBuf &buf, int h, int w, int ni, int nj, int iterations_ls, FlowBufs *b) {
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t pl = al(sizeof(float) * (size_t)h * w);
-    const size_t total = 7 * pl + 10 * pl + al(sizeof(double) * (iterations_ls > 0 ? iterations_ls : 1)) + 256 +
+    const size_t total = 7 * pl + 10 * pl + al(ls_err_bytes(h, w, iterations_ls)) + 256 +
                          2 * al(sizeof(float) * 64) + al(sizeof(double) * (ni + nj)) +
                          al(spline_coef_bytes((long)ni * nj));
     cudaError_t e = buf.ensure(total);
@@ -522,7 +767,7 @@ cudaError_t flow_buffers(DevBuf &buf, int h, int w, int ni, int nj, int iteratio
     float **planes[7] = {&b->lka, &b->lkb, &b->lsa, &b->lsb, &b->tmp, &b->fu, &b->fv};
     for (float **p : planes) { *p = (float *)c; c += pl; }
     b->fx = (float *)c; c += 10 * pl;
-    b->err = (double *)c; c += al(sizeof(double) * (iterations_ls > 0 ? iterations_ls : 1));
+    b->err = (double *)c; c += al(ls_err_bytes(h, w, iterations_ls));
     b->mx = (unsigned *)c; c += 256;
     b->k_lk = (float *)c; c += al(sizeof(float) * 64);
     b->k_ls = (float *)c; c += al(sizeof(float) * 64);
@@ -684,7 +929,7 @@ qlpiv_status qlpiv_liu_shen(qlpiv_handle *h, const float *lk_a, const float *lk_
     for (int q = 0; q < 6; q++)
         if ((e = b[q].ensure(sizeof(float) * n)) != cudaSuccess) return cuda_fail(e, "Liu-Shen buffers");
     if ((e = b[6].ensure(sizeof(float) * 10 * n)) != cudaSuccess ||
-        (e = b[7].ensure(sizeof(double) * iterations_ls)) != cudaSuccess)
+        (e = b[7].ensure(ls_err_bytes(height, width, iterations_ls))) != cudaSuccess)
         return cuda_fail(e, "Liu-Shen buffers");
     if ((iterations_lk > 0 &&
          ((e = cudaMemcpyAsync(b[0].p, lk_a, sizeof(float) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
@@ -772,7 +1017,7 @@ qlpiv_status qlpiv_flow_after_piv(qlpiv_handle *h, const qlpiv_flow_desc *desc, 
     float *du = sb[2].as<float>(), *dv = du + np;
     long launches = 0;
     if ((e = run_flow(s, *desc, pixel_type, im, ib2, width, height, width, n, ni, nj, dk, dk + ni, dfk, dfk + ni, dtl,
-                      dtl + ni, dtu, dtv, du, dv, fb, &launches)) != cudaSuccess)
+                      dtl + ni, dtu, dtv, du, dv, fb, &launches, nullptr)) != cudaSuccess)
         return cuda_fail(e, "optical flow after PIV");
     h->launches += launches;
     if ((e = cudaMemcpyAsync(tile_u, dtu, sizeof(float) * nt, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||

@@ -20,7 +20,9 @@ cudaError_t launch_normalize(cudaStream_t s, const float *in, long n, unsigned *
 // Dense Lucas-Kanade in place on us (columns) / vs (rows).
 cudaError_t launch_dense_lk(cudaStream_t s, const float *a, const float *b, int h, int w, float *us, float *vs, int W,
                             int iterations, int half_pixel);
-// Liu-Shen passes in place; fx: 10 x h x w floats of scratch, err: `iterations` doubles.
+// Liu-Shen passes in place; fx: 10 x h x w floats of scratch, err: ls_err_bytes(h, w, iterations)
+// (every pass's error sum, spread over a few accumulators).
+size_t ls_err_bytes(int h, int w, int iterations);
 cudaError_t launch_liu_shen(cudaStream_t s, const float *la, const float *lb, int h, int w, float *us, float *vs,
                             float lambda, int iterations, int half_pixel, float *fx, float *tmp, double *err);
 
@@ -28,7 +30,7 @@ cudaError_t launch_liu_shen(cudaStream_t s, const float *la, const float *lb, in
 struct FlowBufs {
     float *lka, *lkb, *lsa, *lsb, *tmp, *fu, *fv;
     float *fx;        // 10 x h x w (Liu-Shen fixed terms and ping-pong field)
-    double *err;      // iterations_ls
+    double *err;      // ls_err_bytes(h, w, iterations_ls)
     unsigned *mx;     // one word
     float *k_lk, *k_ls;  // filter weights (device)
     double *cp;       // ni + nj doubles (spline elimination factors)
@@ -36,14 +38,23 @@ struct FlowBufs {
 };
 size_t spline_coef_bytes(long tiles);
 
+// Optional sub-stage hook of run_flow: fn(ctx, stage, true) before a sub-stage's launches are
+// queued, fn(ctx, stage, false) after them (stage timing).
+struct FlowMarks {
+    void (*fn)(void *ctx, const char *stage, bool begin);
+    void *ctx;
+};
+
 // Optical flow after PIV of one frame pair on the device (see qlpiv_flow_after_piv): frames of
 // pixel_type with `pitch` elements per row; tile grid knots cy/cx (double, ni / nj) and cyf/cxf
 // (float); tops/lefts (device int); tile_u/tile_v (rows, columns) updated in place; dense_u /
-// dense_v (rows, columns) optional.  *launches counts the kernels queued.
+// dense_v (rows, columns) optional.  *launches counts the kernels queued.  given: the spline
+// coefficients of this pair's tiles when the caller solved them already (else solved here).
 cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, const void *img_a, const void *img_b,
                      long pitch, int h, int w, int n, int ni, int nj, const double *cy, const double *cx,
                      const float *cyf, const float *cxf, const int *tops, const int *lefts, float *tile_u,
-                     float *tile_v, float *dense_u, float *dense_v, const FlowBufs &b, long *launches);
+                     float *tile_v, float *dense_u, float *dense_v, const FlowBufs &b, long *launches,
+                     const FlowMarks *marks = nullptr, const SplineCoef *given = nullptr);
 // Carves the buffers of one frame pair's flow out of `buf` (grown on demand).
 cudaError_t flow_buffers(struct DevBuf &buf, int h, int w, int ni, int nj, int iterations_ls, FlowBufs *b);
 // Uploads both prefilters' weights (host staging kept by the caller until the stream syncs).

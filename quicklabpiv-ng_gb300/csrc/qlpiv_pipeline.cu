@@ -634,14 +634,45 @@ static qlpiv_status queue_flow(qlpiv_handle *h, const qlpiv_flow_desc &fd, const
     if ((e = flow_buffers(p->flow, p->height, p->width, ni, nj, fd.iterations_ls, &fb)) != cudaSuccess ||
         (e = upload_flow_weights(s, fd, fb, weights)) != cudaSuccess)
         return cuda_fail(e, "flow buffers");
+    struct MarkCtx {
+        qlpiv_handle *h;
+        int level, n;
+        long items;
+        StageEvent ev;
+    } mc{h, (int)p->levels.size() - 1, L.g.n, np, {}};
+    auto on_mark = [](void *c, const char *stage, bool begin) {
+        MarkCtx *m = static_cast<MarkCtx *>(c);
+        if (begin) {
+            m->ev = StageEvent{stage, m->level, m->n, 0, m->items, nullptr, nullptr};
+            if (cudaEventCreate(&m->ev.begin) != cudaSuccess || cudaEventCreate(&m->ev.end) != cudaSuccess) return;
+            cudaEventRecord(m->ev.begin, m->h->stream);
+        } else if (m->ev.end) {
+            cudaEventRecord(m->ev.end, m->h->stream);
+            m->h->prof_pending.push_back(m->ev);
+            m->ev.end = nullptr;
+        }
+    };
+    const FlowMarks marks{on_mark, &mc};
+    // the splines of every pair's final tile displacements in one launch set (the warp of this
+    // level used the inherited displacements; the coefficients are free again)
+    const SplineCoef all = coef_of(L, p->pairs);
+    if (h->profiling) on_mark(&mc, "flow:spline", true);
+    if ((e = launch_spline(s, p->pairs, L.d_cy.as<double>(), L.d_cpy.as<double>(), ni, L.d_cx.as<double>(),
+                           L.d_cpx.as<double>(), nj, L.d_u.as<float>(), L.d_v.as<float>(), all)) != cudaSuccess)
+        return cuda_fail(e, "flow spline");
+    if (h->profiling) on_mark(&mc, "flow:spline", false);
+    h->launches += 4;
     for (int q = 0; q < p->pairs; q++) {
-        StageScope sc(h, "flow", (int)p->levels.size() - 1, L.g.n, 0, np);
         long launches = 0;
+        const long off = (long)q * cnt;
+        const SplineCoef pc{all.fy_u + off, all.fx_u + off, all.fyx_u + off, all.fy_v + off, all.fx_v + off,
+                            all.fyx_v + off, all.c4_u + off, all.c4_v + off};
         if ((e = run_flow(s, fd, p->pixel_type, frames[q].img_a, frames[q].img_b, frames[q].pitch, p->height,
                           p->width, L.g.n, ni, nj, L.d_cy.as<double>(), L.d_cx.as<double>(), L.d_cyf.as<float>(),
                           L.d_cxf.as<float>(), L.d_tops.as<int>(), L.d_lefts.as<int>(), L.d_u.as<float>() + q * cnt,
                           L.d_v.as<float>() + q * cnt, dense_u ? dense_u + q * np : nullptr,
-                          dense_v ? dense_v + q * np : nullptr, fb, &launches)) != cudaSuccess)
+                          dense_v ? dense_v + q * np : nullptr, fb, &launches,
+                          h->profiling ? &marks : nullptr, &pc)) != cudaSuccess)
             return cuda_fail(e, "optical flow after PIV");
         h->launches += launches;
     }

@@ -1,0 +1,70 @@
+"""Plain per-call GPU path: the adaptive PIV loop of one frame pair driven stage by stage from
+the host, every stage one synchronous library call on host arrays (inputs copied in, results
+copied out), no batching across pairs and no device-resident state between stages.
+
+This is how the reference drives its GPU jobs (`LocalPIVOpenCLGpuJob.java:188-411`: per pair and
+per level, the warp, the correlation job and the validator each take host data and return host
+data), and it is the denominator of the batched path's speed-up.  It runs the same kernels as
+`Handle.piv_adaptive` and gives bit-identical displacements.
+"""
+import numpy as np
+
+from . import F_ABSENT, VALIDATE_MULTIPEAK_MEDIAN, WARP_BOTH_BILINEAR, WARP_NONE, adaptive_levels, grid
+
+
+def _java_round(x):
+    return np.floor(x + np.float32(0.5)).astype(np.int32)
+
+
+def piv_adaptive_per_call(handle, img_a, img_b, desc):
+    """Adaptive multi-pass PIV of one pair, one library call per stage; returns (u, v) of the
+    last level shaped (tiles_i, tiles_j)."""
+    a = np.ascontiguousarray(img_a)
+    b = np.ascontiguousarray(img_b)
+    h, w = a.shape
+    levels = adaptive_levels(desc, h, w)
+    fm = desc.fixed_max if desc.fixed_max > 0 else (255.0 if a.dtype == np.uint8 else 65535.0)
+    validate = desc.validation == VALIDATE_MULTIPEAK_MEDIAN
+    pass_kw = dict(norm_mode=desc.norm_mode, max_mode=desc.max_mode, fixed_max=(fm, fm),
+                   subpix_mode=desc.subpix_mode)
+    if validate:
+        pass_kw.update(num_peaks=desc.num_peaks, peak_kernel=desc.peak_kernel)
+    margins = list(desc.margins)
+    prev = None
+    for lv, g in enumerate(levels):
+        n = g["n"]
+        st = grid.superposition(h, w, desc.ia_start, lv, desc.overlap_factor, margins)
+        assert (st.n, st.tiles_i, st.tiles_j) == (n, g["tiles_i"], g["tiles_j"])
+        tops = np.asarray(st.tops, np.int32)
+        lefts = np.asarray(st.lefts, np.int32)
+        cy, cx = st.centres()
+        ni, nj = len(tops), len(lefts)
+        if prev is None:
+            u = np.zeros((ni, nj), np.float32)
+            v = np.zeros((ni, nj), np.float32)
+        else:
+            pcy, pcx, pu, pv = prev
+            u, v = handle.inherit(pcy, pcx, pu, pv, cy, cx, round_int=desc.warp_mode == WARP_NONE)
+        at = np.repeat(tops, nj)
+        al = np.tile(lefts, ni)
+        src_a, src_b = a, b
+        bt, bl = at, al
+        if desc.warp_mode == WARP_BOTH_BILINEAR:
+            if lv > 0:
+                src_a, src_b = handle.warp_pair(a, b, cy.astype(np.float64), cx.astype(np.float64), u, v,
+                                                int16_quirk=bool(desc.int16_warp_quirk))
+        else:
+            bt = _java_round(at.astype(np.float32) + u.ravel())
+            bl = _java_round(al.astype(np.float32) + v.ravel())
+        vec = handle.piv_pass(src_a, src_b, n, at, al, bt, bl, **pass_kw)
+        main = vec[:, 0] if vec.ndim == 2 else vec
+        u = (u.ravel() + main["u"]).reshape(ni, nj).astype(np.float32)
+        v = (v.ravel() + main["v"]).reshape(ni, nj).astype(np.float32)
+        if validate:
+            present = (vec["flags"] & F_ABSENT) == 0
+            npk = present.sum(axis=1).astype(np.int32).reshape(ni, nj)
+            k = desc.num_peaks
+            u, v, _ = handle.validate(tops, lefts, u, v, vec["u"].reshape(ni, nj, k), vec["v"].reshape(ni, nj, k),
+                                      npk, desc)
+        prev = (cy, cx, u, v)
+    return prev[2], prev[3]

@@ -89,3 +89,9 @@ def config2_pair(seed=2, pair_id=0):
     """1024x1024 12-bit in u16, 0.03 ppp, d = 2.5, shear 0.005 + Rankine, max 6 px."""
     return particle_pair((1024, 1024), Flow(vmax=6.0 - 0.005 * 512, rc=96.0, shear=0.005), ppp=0.03, diam=2.5,
                          diam_sd=0.0, noise=3.0, bits=12, seed=seed, pair_id=pair_id)
+
+
+def config4_pair(seed=4, pair_id=0):
+    """1024x1024 u8 vortex pair, 0.05 ppp, max 3 px (hybrid PIV + dense optical flow)."""
+    return particle_pair((1024, 1024), Flow(vmax=3.0, rc=64.0), ppp=0.05, diam=3.0, diam_sd=0.5, noise=3.0, bits=8,
+                         seed=seed, pair_id=pair_id)

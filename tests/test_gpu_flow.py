@@ -47,27 +47,32 @@ def _tiles(oracle, flow, h, w, n, rng):
 
 
 CASES = [
-    # mode, dense export, sigma_lk, px_lk, window, iterations_lk, iterations_ls, bits, (h, w), n
-    (1, False, 2.0, 3, 27, 5, 0, 8, (192, 224), 16),
-    (1, True, 2.0, 3, 27, 5, 0, 8, (192, 224), 16),
-    (1, False, 0.0, 3, 9, 3, 0, 12, (160, 130), 32),
-    (2, False, 2.0, 3, 15, 2, 25, 8, (176, 160), 16),
-    (2, True, 1.3, 5, 27, 3, 40, 16, (128, 192), 16),
+    # mode, dense export, sigma_lk, px_lk, window, iterations_lk, iterations_ls, bits, (h, w), n, ignore_piv
+    (1, False, 2.0, 3, 27, 5, 0, 8, (192, 224), 16, 0),
+    (1, True, 2.0, 3, 27, 5, 0, 8, (192, 224), 16, 0),
+    (1, False, 0.0, 3, 9, 3, 0, 12, (160, 130), 32, 0),
+    (2, False, 2.0, 3, 15, 2, 25, 8, (176, 160), 16, 0),
+    (2, True, 1.3, 5, 27, 3, 40, 16, (128, 192), 16, 0),
+    (1, False, 2.0, 3, 27, 5, 0, 8, (128, 144), 16, 1),
+    (1, True, 2.0, 3, 27, 5, 0, 8, (128, 144), 16, 2),
+    (2, False, 2.0, 3, 15, 3, 10, 8, (128, 144), 16, 3),
+    (1, False, 2.0, 3, 27, 5, 0, 8, (128, 144), 16, 4),
+    (2, True, 2.0, 3, 27, 5, 10, 8, (128, 144), 16, 5),
 ]
 
 
 @pytest.mark.parametrize("case", range(len(CASES)))
 def test_flow_after_piv_bit_exact(qp, handle, oracle, case):
-    mode, dense, sig, px, win, it_lk, it_ls, bits, (h, w), n = CASES[case]
+    mode, dense, sig, px, win, it_lk, it_ls, bits, (h, w), n, ign = CASES[case]
     a, b, flow = _pair(qp, h, w, bits=bits, seed=case + 11)
     rng = np.random.default_rng(case)
     tops, lefts, tu, tv = _tiles(oracle, flow, h, w, n, rng)
     d = qp.flow_desc(mode=mode, filter_sigma_lk=sig, filter_px_lk=px, window_lk=win, iterations_lk=it_lk,
-                     iterations_ls=max(it_ls, 1), dense_export=dense)
+                     iterations_ls=max(it_ls, 1), dense_export=dense, ignore_piv=ign)
     gu, gv, gdu, gdv = handle.flow_after_piv(a, b, n, tops, lefts, tu, tv, d)
     ou, ov, odu, odv = oracle.flow_after_piv(a, b, n, tops, lefts, tu, tv, mode=mode, sigma_lk=sig, px_lk=px,
                                              window=win, iterations_lk=it_lk, iterations_ls=max(it_ls, 1),
-                                             dense_export=dense)
+                                             dense_export=dense, ignore_piv=ign)
     assert not np.array_equal(ou, tu)               # the flow stage changed the tiles
     assert gu.tobytes() == ou.tobytes() and gv.tobytes() == ov.tobytes()
     assert gdu.tobytes() == odu.tobytes() and gdv.tobytes() == odv.tobytes()
@@ -97,7 +102,7 @@ def test_flow_descriptor_rejected(qp, handle, oracle):
     a, b, flow = _pair(qp, 96, 96)
     tops, lefts, tu, tv = _tiles(oracle, flow, 96, 96, 16, np.random.default_rng(0))
     for bad in (dict(mode=3), dict(window_lk=8), dict(window_lk=33), dict(iterations_lk=0),
-                dict(mode=2, iterations_ls=0), dict(filter_px_lk=4)):
+                dict(mode=2, iterations_ls=0), dict(filter_px_lk=4), dict(ignore_piv=6)):
         with pytest.raises(qp.QlpivError) as e:
             handle.flow_after_piv(a, b, 16, tops, lefts, tu, tv, qp.flow_desc(**bad))
         assert e.value.status == qp.E_ARG

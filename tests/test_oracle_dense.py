@@ -138,3 +138,30 @@ def test_flow_after_piv_still_images_stay_still(oracle):
     z = np.zeros_like(tu)
     u, v, du, dv = oracle.flow_after_piv(a, a, 16, tops, lefts, z, z, mode=2, iterations_ls=5)
     assert not u.any() and not v.any() and not du.any() and not dv.any()
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3, 4, 5])
+def test_flow_after_piv_ignore_piv_modes(oracle, mode):
+    """ignorePIVBaseDisplacements: the PIV field handed to Lucas-Kanade, checked through a run
+    with one LK iteration on identical images (no motion: LK keeps the field where it starts)."""
+    n = 16
+    a, _, tops, lefts, tu, tv = _flow_case(oracle, n=n, seed=mode)
+    tu = tu * 3.0
+    h, w = a.shape
+    ys = (tops + n / 2.0 - 0.5).astype(np.float32)
+    xs = (lefts + n / 2.0 - 0.5).astype(np.float32)
+    fu, fv = oracle.displacement_field(ys, xs, tu, tv, h, w, offset=0.5)
+    if mode in (4, 5):
+        lim = np.float32(3.0 if mode == 4 else 0.9)
+        fu = np.where(np.abs(fu) < lim, np.float32(0), fu)
+        fv = np.where(np.abs(fv) < lim, np.float32(0), fv)
+    if mode in (2, 3):
+        fu = np.full_like(fu, 0.5)
+    if mode in (1, 3):
+        fv = np.full_like(fv, 0.5)
+    us, vs = oracle.dense_lk(oracle.gauss_filter(a, 2.0, 3), oracle.gauss_filter(a, 2.0, 3), fv, fu, 27, 1,
+                             half_pixel=True)
+    u, v, du, dv = oracle.flow_after_piv(a, a, n, tops, lefts, tu, tv, mode=1, iterations_lk=1, dense_export=False,
+                                         ignore_piv=mode)
+    np.testing.assert_array_equal(du, vs)
+    np.testing.assert_array_equal(dv, us)
