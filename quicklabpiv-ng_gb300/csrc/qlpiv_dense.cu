@@ -7,11 +7,15 @@
 //             last h values in order; out[j] accumulates in[j + h - q] * k[q], q = 0..2h.
 //             ImageFloat.normalize (S/images/ImageFloat.java:571-596).
 //   C-LK      DenseLucasKanadeGpuKernel (S/jobs/interpolators/DenseLucasKanadeGpuKernel.java:203-751):
-//             one thread per pixel, a 16 x 16 pixel tile per CTA.  The CTA stages the image-A
-//             region its windows span (clamped; 2x2 averages for the half-pixel offset) and
-//             the derivatives (3, 10, 3) / 32 of every window point once in shared memory;
-//             each thread then sums its W x W A matrix and, per iteration, its b vector from
-//             bilinear samples of image B.
+//             a 16 x 16 pixel tile per CTA.  The CTA stages the image-A region its windows
+//             span (clamped; 2x2 averages for the half-pixel offset) and the derivatives
+//             (3, 10, 3) / 32 of every window point once in shared memory; each pixel then
+//             sums its W x W A matrix and, per iteration, its b vector from bilinear samples
+//             of image B.  Where the window's sample positions are exact (or round uniformly
+//             past one power of two) the samples come from horizontal interpolations of B
+//             rows computed once per row; elsewhere every sample is read as the reference
+//             reads it.  Window 27 runs two vertically adjacent pixels per thread with those
+//             rows in registers; other windows one pixel per thread.
 //   C-LS      DenseLiuShenGpuKernel (S/jobs/interpolators/DenseLiuShenGpuKernel.java:66-588):
 //             fixed-image terms once per pixel, then one Jacobi pass per launch; the pass
 //             reads the previous pass's total error on the device and becomes a copy once
@@ -141,64 +145,19 @@ __device__ __forceinline__ bool lk_axis(float o, int W, LkAxis &ax) {
     return true;
 }
 
-// The window sums b0, b1 of one iteration with the sample rows in registers (window side WT).
-// br: B at (ay.base, ax.base); g: the thread's first window point.  SPLIT: the column fraction
-// changes at ax.split (selected per column from a bit mask), else it is ax.f1 throughout.
-template <int WT, bool SPLIT>
-__device__ __forceinline__ void lk_rows(const float *br, int w, const float4 *g, int GS, const LkAxis &ay,
-                                        const LkAxis &ax, float &b0, float &b1) {
-    const unsigned upper = SPLIT ? ~((1u << ax.split) - 1u) : 0u;  // columns past the boundary
-    const float omj1 = __fsub_rn(1.0f, ax.f1), omj2 = __fsub_rn(1.0f, ax.f2);
-    float hb[WT];
-    float x0 = br[0];
-#pragma unroll
-    for (int b = 0; b < WT; b++) {
-        const bool up = SPLIT && ((upper >> b) & 1u);
-        const float x1 = br[b + 1];
-        hb[b] = __fadd_rn(__fmul_rn(up ? omj2 : omj1, x0), __fmul_rn(up ? ax.f2 : ax.f1, x1));
-        x0 = x1;
-    }
-#pragma unroll 1
-    for (int a = 0; a < WT; a++) {
-        const float di = a < ay.split ? ay.f1 : ay.f2, omi = __fsub_rn(1.0f, di);
-        br += w;
-        x0 = br[0];
-#pragma unroll
-        for (int b = 0; b < WT; b++) {
-            const bool up = SPLIT && ((upper >> b) & 1u);
-            const float x1 = br[b + 1];
-            const float bot = __fadd_rn(__fmul_rn(up ? omj2 : omj1, x0), __fmul_rn(up ? ax.f2 : ax.f1, x1));
-            x0 = x1;
-            const float smp = __fadd_rn(__fmul_rn(omi, hb[b]), __fmul_rn(di, bot));
-            hb[b] = bot;
-            const float4 t = g[b];
-            const float dT = __fsub_rn(smp, t.x);
-            b0 = __fadd_rn(__fmul_rn(dT, t.y), b0);
-            b1 = __fadd_rn(__fmul_rn(dT, t.z), b1);
-        }
-        g += GS;
-    }
-}
+// The window points of a CTA's pixel tile: image A and its derivatives dj, di, row-major
+// GS x GS each.
+struct LkWin {
+    const float *a, *dj, *di;
+};
 
-// Dense LK over a 16 x 16 pixel tile.  Shared memory: the tile's window points as float4
-// (value of A, dj, di, unused), then a scratch area that first holds the staged A region and
-// later (WT = 0) one row of horizontally interpolated B samples per thread.  WT > 0: the window
-// side is WT and the rows of samples live in registers.
-template <int WT>
-__global__ void __launch_bounds__(kLkTile *kLkTile, WT > 0 ? 3 : 2) dense_lk_kernel(const float *A, const float *B, int h, int w,
-                                                                     float *us, float *vs, int W_, int iterations,
-                                                                     int half_pixel) {
-    extern __shared__ float4 sm4[];
-    const int W = WT > 0 ? WT : W_;
+// Stages the A region (clamped; 2x2 averages for the half-pixel offset) of a tile with origin
+// (ti0, tj0) in reg (RS x RS) and computes the window points' values and derivatives.
+__device__ __forceinline__ void lk_stage(const float *A, int h, int w, int W, int half_pixel, int ti0, int tj0,
+                                         int tid, int nthr, int tile, float *reg, float *wa, float *wj, float *wi) {
     const int hw = W / 2;
-    const int RS = kLkTile + W + 1;  // staged region side: window span + derivative margin
-    const int GS = kLkTile + W - 1;  // window points of the tile
-    constexpr int kThreads = kLkTile * kLkTile;
-    float4 *vg = sm4;                                   // GS x GS: (A, dj, di, 0)
-    float *reg = reinterpret_cast<float *>(vg + GS * GS);  // RS x RS during set-up
-    const int tid = threadIdx.y * kLkTile + threadIdx.x;
-    const int ti0 = blockIdx.y * kLkTile, tj0 = blockIdx.x * kLkTile;
-    for (int q = tid; q < RS * RS; q += kThreads) {
+    const int RS = tile + W + 1, GS = tile + W - 1;
+    for (int q = tid; q < RS * RS; q += nthr) {
         const int r = q / RS, c = q - r * RS;
         const int y = ti0 - hw - 1 + r, x = tj0 - hw - 1 + c;
         if (half_pixel) {
@@ -212,128 +171,375 @@ __global__ void __launch_bounds__(kLkTile *kLkTile, WT > 0 ? 3 : 2) dense_lk_ker
     }
     __syncthreads();
     const float c3 = 3.0f / 32.0f;
-    for (int q = tid; q < GS * GS; q += kThreads) {
+    for (int q = tid; q < GS * GS; q += nthr) {
         const int gy = q / GS, gx = q - gy * GS;
         const float *r0 = reg + gy * RS + gx, *r1 = r0 + RS, *r2 = r1 + RS;
         const float TL = r0[0], T = r0[1], TR = r0[2], L = r1[0], C = r1[1], R = r1[2], BL = r2[0], Bt = r2[1],
                     BR = r2[2];
-        const float dj = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TL, BL), TR), BR), c3),
-                                   __fdiv_rn(__fmul_rn(__fsub_rn(L, R), 10.0f), 32.0f));
-        const float di = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TR, TL), BR), BL), c3),
-                                   __fdiv_rn(__fmul_rn(__fsub_rn(T, Bt), 10.0f), 32.0f));
-        vg[q] = make_float4(C, dj, di, 0.0f);
+        wj[q] = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TL, BL), TR), BR), c3),
+                          __fdiv_rn(__fmul_rn(__fsub_rn(L, R), 10.0f), 32.0f));
+        wi[q] = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TR, TL), BR), BL), c3),
+                          __fdiv_rn(__fmul_rn(__fsub_rn(T, Bt), 10.0f), 32.0f));
+        wa[q] = C;
     }
-    __syncthreads();  // reg is dead from here on: its space becomes the per-thread rows
-    const int pi = ti0 + threadIdx.y, pj = tj0 + threadIdx.x;
-    if (pi >= h || pj >= w) return;
+    __syncthreads();
+}
+
+// Per-pixel state of the iterations.
+struct LkPix {
+    long p;
+    int pi, pj;
+    bool active;
+    float locI, locJ, i00, i01, i11;
+};
+
+// The A matrix of the pixel whose first window point is g (offset into the window arrays),
+// its inverse and the start location; sets `active`.
+__device__ __forceinline__ void lk_begin(const LkWin &win, int g, int GS, int W, const float *us, const float *vs,
+                                         int half_pixel, LkPix &px) {
     float a00 = 0.0f, a01 = 0.0f, a11 = 0.0f;
     for (int a = 0; a < W; a++) {
-        const float4 *g = vg + (threadIdx.y + a) * GS + threadIdx.x;
-#pragma unroll(WT > 0 ? WT : 1)
+        const float *wj = win.dj + g + a * GS, *wi = win.di + g + a * GS;
         for (int b = 0; b < W; b++) {
-            const float4 t = g[b];
-            a00 = __fadd_rn(__fmul_rn(t.y, t.y), a00);
-            a01 = __fadd_rn(__fmul_rn(t.y, t.z), a01);
-            a11 = __fadd_rn(__fmul_rn(t.z, t.z), a11);
+            const float dj = wj[b], di = wi[b];
+            a00 = __fadd_rn(__fmul_rn(dj, dj), a00);
+            a01 = __fadd_rn(__fmul_rn(dj, di), a01);
+            a11 = __fadd_rn(__fmul_rn(di, di), a11);
         }
     }
-    const long p = (long)pi * w + pj;
-    bool active = true;
     const float det = __fadd_rn(__fmul_rn(a00, a11), -__fmul_rn(a01, a01));
-    if (det < 1.192092896e-7f) active = false;
-    const float i00 = __fdiv_rn(a11, det), i01 = __fdiv_rn(-a01, det), i11 = __fdiv_rn(a00, det);
-    float locI = __fadd_rn((float)pi, vs[p]), locJ = __fadd_rn((float)pj, us[p]);
+    px.active = !(det < 1.192092896e-7f);
+    px.i00 = __fdiv_rn(a11, det);
+    px.i01 = __fdiv_rn(-a01, det);
+    px.i11 = __fdiv_rn(a00, det);
+    px.locI = __fadd_rn((float)px.pi, vs[px.p]);
+    px.locJ = __fadd_rn((float)px.pj, us[px.p]);
     if (half_pixel) {
-        locI = __fadd_rn(locI, 0.5f);
-        locJ = __fadd_rn(locJ, 0.5f);
+        px.locI = __fadd_rn(px.locI, 0.5f);
+        px.locJ = __fadd_rn(px.locJ, 0.5f);
     }
-    for (int it = 0; it < iterations && active; it++) {
-        if (locI < 0.0f || locI >= (float)(h + hw) || locJ < 0.0f || locJ >= (float)(w + hw)) break;
-        float b0 = 0.0f, b1 = 0.0f;
-        const float oi = __fsub_rn(locI, (float)hw), oj = __fsub_rn(locJ, (float)hw);
-        LkAxis ay, ax;
-        const bool fast = lk_axis(oi, W, ay) && lk_axis(oj, W, ax) && ay.base + W <= h - 1 &&
-                          ax.base + W <= w - 1 && (WT > 0 || (ay.split == W && ax.split == W));
-        if (fast) {
-            // Window row a reads B rows base + a (top) and base + a + 1 (bottom) with the row's
-            // weights; the horizontal interpolation of a B row is the bottom of window row a and
-            // the top of window row a + 1, so each is computed once.
-            const float *br = B + (long)ay.base * w + ax.base;
-            if constexpr (WT > 0) {
-                if (ax.split == WT)
-                    lk_rows<WT, false>(br, w, vg + threadIdx.y * GS + threadIdx.x, GS, ay, ax, b0, b1);
-                else
-                    lk_rows<WT, true>(br, w, vg + threadIdx.y * GS + threadIdx.x, GS, ay, ax, b0, b1);
-            } else {
-                float *hb = reinterpret_cast<float *>(vg + GS * GS) + tid;  // stride kThreads (bank = lane)
-                const float dj = ax.f1, omj = __fsub_rn(1.0f, dj);
-                const float di = ay.f1, omi = __fsub_rn(1.0f, di);
-                float x0 = br[0];
-                for (int b = 0; b < W; b++) {
-                    const float x1 = br[b + 1];
-                    hb[b * kThreads] = __fadd_rn(__fmul_rn(omj, x0), __fmul_rn(dj, x1));
-                    x0 = x1;
-                }
-                for (int a = 0; a < W; a++) {
-                    const float4 *g = vg + (threadIdx.y + a) * GS + threadIdx.x;
-                    br += w;
-                    x0 = br[0];
-                    for (int b = 0; b < W; b++) {
-                        const float x1 = br[b + 1];
-                        const float bot = __fadd_rn(__fmul_rn(omj, x0), __fmul_rn(dj, x1));
-                        x0 = x1;
-                        const float top = hb[b * kThreads];
-                        hb[b * kThreads] = bot;
-                        const float smp = __fadd_rn(__fmul_rn(omi, top), __fmul_rn(di, bot));
-                        const float4 t = g[b];
-                        const float dT = __fsub_rn(smp, t.x);
-                        b0 = __fadd_rn(__fmul_rn(dT, t.y), b0);
-                        b1 = __fadd_rn(__fmul_rn(dT, t.z), b1);
-                    }
-                }
-            }
-        } else {
-            for (int a = 0; a < W; a++) {
-                const float4 *g = vg + (threadIdx.y + a) * GS + threadIdx.x;
-                const float li = __fadd_rn(oi, (float)a);
-                for (int b = 0; b < W; b++) {
-                    const float4 t = g[b];
-                    const float dT = __fsub_rn(warp_read(B, h, w, li, __fadd_rn(oj, (float)b)), t.x);
-                    b0 = __fadd_rn(__fmul_rn(dT, t.y), b0);
-                    b1 = __fadd_rn(__fmul_rn(dT, t.z), b1);
-                }
-            }
-        }
-        const float incU = __fadd_rn(__fmul_rn(b0, i00), __fmul_rn(b1, i01));
-        const float incV = __fadd_rn(__fmul_rn(b0, i01), __fmul_rn(b1, i11));
-        if (fabsf(incU) < 1e-3f && fabsf(incV) < 1e-3f) break;
-        locI = __fadd_rn(locI, incV);
-        locJ = __fadd_rn(locJ, incU);
-    }
-    float v = __fsub_rn(locI, (float)pi), u = __fsub_rn(locJ, (float)pj);
+}
+
+// Applies one iteration's window sums; returns false when the pixel stops.
+__device__ __forceinline__ bool lk_update(LkPix &px, float b0, float b1) {
+    const float incU = __fadd_rn(__fmul_rn(b0, px.i00), __fmul_rn(b1, px.i01));
+    const float incV = __fadd_rn(__fmul_rn(b0, px.i01), __fmul_rn(b1, px.i11));
+    if (fabsf(incU) < 1e-3f && fabsf(incV) < 1e-3f) return false;
+    px.locI = __fadd_rn(px.locI, incV);
+    px.locJ = __fadd_rn(px.locJ, incU);
+    return true;
+}
+
+__device__ __forceinline__ void lk_end(const LkPix &px, int half_pixel, float *us, float *vs) {
+    float v = __fsub_rn(px.locI, (float)px.pi), u = __fsub_rn(px.locJ, (float)px.pj);
     if (half_pixel) {
         v = __fsub_rn(v, 0.5f);
         u = __fsub_rn(u, 0.5f);
     }
-    vs[p] = v;
-    us[p] = u;
+    vs[px.p] = v;
+    us[px.p] = u;
 }
 
-// WT > 0 keeps the sample rows in registers; WT = 0 needs W rows of floats per thread.
+// Window sums from per-sample bilinear reads (any location, clamped).
+__device__ __forceinline__ void lk_sums_slow(const float *B, int h, int w, int W, float oi, float oj,
+                                             const LkWin &win, int g, int GS, float &b0, float &b1) {
+    for (int a = 0; a < W; a++) {
+        const int r = g + a * GS;
+        const float li = __fadd_rn(oi, (float)a);
+        for (int b = 0; b < W; b++) {
+            const float dT = __fsub_rn(warp_read(B, h, w, li, __fadd_rn(oj, (float)b)), win.a[r + b]);
+            b0 = __fadd_rn(__fmul_rn(dT, win.dj[r + b]), b0);
+            b1 = __fadd_rn(__fmul_rn(dT, win.di[r + b]), b1);
+        }
+    }
+}
+
+// The register fast path of one pixel (window side WT): window row a reads B rows base + a (top)
+// and base + a + 1 (bottom); the horizontal interpolation of a B row is the bottom of window row
+// a and the top of window row a + 1, so each is computed once and kept in hb.  SPLIT: the column
+// fraction changes at ax.split (selected per column from a bit mask), else it is ax.f1.
+template <int WT, bool SPLIT>
+struct LkRows {
+    float hb[WT];
+    const float *br;
+    unsigned upper;
+    float f1, f2, om1, om2;
+    LkAxis ay;
+    float b0, b1;
+
+    __device__ __forceinline__ float wj(int b) const { return SPLIT && ((upper >> b) & 1u) ? f2 : f1; }
+    __device__ __forceinline__ float womj(int b) const { return SPLIT && ((upper >> b) & 1u) ? om2 : om1; }
+
+    __device__ __forceinline__ void init(const float *B, int w, const LkAxis &ay_, const LkAxis &ax) {
+        ay = ay_;
+        upper = SPLIT ? ~((1u << ax.split) - 1u) : 0u;
+        f1 = ax.f1;
+        f2 = ax.f2;
+        om1 = __fsub_rn(1.0f, f1);
+        om2 = __fsub_rn(1.0f, f2);
+        br = B + (long)ay.base * w + ax.base;
+        b0 = 0.0f;
+        b1 = 0.0f;
+        float x0 = br[0];
+#pragma unroll
+        for (int b = 0; b < WT; b++) {
+            const float x1 = br[b + 1];
+            hb[b] = __fadd_rn(__fmul_rn(womj(b), x0), __fmul_rn(wj(b), x1));
+            x0 = x1;
+        }
+    }
+    // window row a against the window points va/vj/vi of that row
+    __device__ __forceinline__ void row(int a, int w, const float *va, const float *vj, const float *vi) {
+        const float di = a < ay.split ? ay.f1 : ay.f2, omi = __fsub_rn(1.0f, di);
+        br += w;
+        float x0 = br[0];
+#pragma unroll
+        for (int b = 0; b < WT; b++) {
+            const float x1 = br[b + 1];
+            const float bot = __fadd_rn(__fmul_rn(womj(b), x0), __fmul_rn(wj(b), x1));
+            x0 = x1;
+            const float smp = __fadd_rn(__fmul_rn(omi, hb[b]), __fmul_rn(di, bot));
+            hb[b] = bot;
+            const float dT = __fsub_rn(smp, va[b]);
+            b0 = __fadd_rn(__fmul_rn(dT, vj[b]), b0);
+            b1 = __fadd_rn(__fmul_rn(dT, vi[b]), b1);
+        }
+    }
+};
+
+// Two vertically adjacent pixels (rows pi, pi + 1) share all but one window row: window row r of
+// the upper pixel is row r - 1 of the lower one, so both consume each loaded window point.
+template <int WT, bool S0, bool S1>
+__device__ __forceinline__ void lk_pair_sums(const float *B, int w, const LkAxis &ay0, const LkAxis &ax0,
+                                             const LkAxis &ay1, const LkAxis &ax1, const LkWin &win, int g, int GS,
+                                             float &s00, float &s01, float &s10, float &s11) {
+    LkRows<WT, S0> r0;
+    LkRows<WT, S1> r1;
+    r0.init(B, w, ay0, ax0);
+    r1.init(B, w, ay1, ax1);
+    r0.row(0, w, win.a + g, win.dj + g, win.di + g);
+#pragma unroll 1
+    for (int r = 1; r < WT; r++) {
+        const int o = g + r * GS;
+        const float *va = win.a + o, *vj = win.dj + o, *vi = win.di + o;
+        const float di0 = r < ay0.split ? ay0.f1 : ay0.f2, omi0 = __fsub_rn(1.0f, di0);
+        const float di1 = r - 1 < ay1.split ? ay1.f1 : ay1.f2, omi1 = __fsub_rn(1.0f, di1);
+        r0.br += w;
+        r1.br += w;
+        float x00 = r0.br[0], x10 = r1.br[0];
+#pragma unroll
+        for (int b = 0; b < WT; b++) {
+            const float a_ = va[b], j_ = vj[b], i_ = vi[b];
+            const float x01 = r0.br[b + 1], x11 = r1.br[b + 1];
+            const float bot0 = __fadd_rn(__fmul_rn(r0.womj(b), x00), __fmul_rn(r0.wj(b), x01));
+            const float bot1 = __fadd_rn(__fmul_rn(r1.womj(b), x10), __fmul_rn(r1.wj(b), x11));
+            x00 = x01;
+            x10 = x11;
+            const float smp0 = __fadd_rn(__fmul_rn(omi0, r0.hb[b]), __fmul_rn(di0, bot0));
+            const float smp1 = __fadd_rn(__fmul_rn(omi1, r1.hb[b]), __fmul_rn(di1, bot1));
+            r0.hb[b] = bot0;
+            r1.hb[b] = bot1;
+            const float dT0 = __fsub_rn(smp0, a_), dT1 = __fsub_rn(smp1, a_);
+            r0.b0 = __fadd_rn(__fmul_rn(dT0, j_), r0.b0);
+            r0.b1 = __fadd_rn(__fmul_rn(dT0, i_), r0.b1);
+            r1.b0 = __fadd_rn(__fmul_rn(dT1, j_), r1.b0);
+            r1.b1 = __fadd_rn(__fmul_rn(dT1, i_), r1.b1);
+        }
+    }
+    const int o = g + WT * GS;
+    r1.row(WT - 1, w, win.a + o, win.dj + o, win.di + o);
+    s00 = r0.b0;
+    s01 = r0.b1;
+    s10 = r1.b0;
+    s11 = r1.b1;
+}
+
+template <int WT, bool S>
+__device__ __forceinline__ void lk_one_sums(const float *B, int w, const LkAxis &ay, const LkAxis &ax,
+                                            const LkWin &win, int g, int GS, float &b0, float &b1) {
+    LkRows<WT, S> r;
+    r.init(B, w, ay, ax);
+#pragma unroll 1
+    for (int a = 0; a < WT; a++) {
+        const int o = g + a * GS;
+        r.row(a, w, win.a + o, win.dj + o, win.di + o);
+    }
+    b0 = r.b0;
+    b1 = r.b1;
+}
+
+// Whether one iteration of pixel px may take the register fast path; fills the axes.
+__device__ __forceinline__ bool lk_fast(const LkPix &px, int h, int w, int W, float oi, float oj, LkAxis &ay,
+                                        LkAxis &ax) {
+    return lk_axis(oi, W, ay) && lk_axis(oj, W, ax) && ay.base + W <= h - 1 && ax.base + W <= w - 1;
+}
+
+// Window side WT, two vertically adjacent pixels per thread: a CTA of 16 x 8 threads covers
+// 16 x 16 pixels.  Shared memory: the window arrays (3 x GS^2 floats) after the staged region.
+template <int WT, int MB>
+__global__ void __launch_bounds__(128, MB) dense_lk_pair_kernel(const float *A, const float *B, int h, int w,
+                                                                float *us, float *vs, int iterations, int half_pixel) {
+    extern __shared__ float smf[];
+    constexpr int W = WT, hw = WT / 2, GS = kLkTile + WT - 1;
+    float *wa = smf, *wj = wa + GS * GS, *wi = wj + GS * GS, *reg = wi + GS * GS;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int ti0 = blockIdx.y * kLkTile, tj0 = blockIdx.x * kLkTile;
+    lk_stage(A, h, w, W, half_pixel, ti0, tj0, tid, blockDim.x * blockDim.y, kLkTile, reg, wa, wj, wi);
+    const LkWin win{wa, wj, wi};
+    const int pj = tj0 + threadIdx.x, pi0 = ti0 + 2 * threadIdx.y;
+    if (pj >= w || pi0 >= h) return;
+    const bool two = pi0 + 1 < h;
+    const int g0 = 2 * threadIdx.y * GS + threadIdx.x, g1 = g0 + GS;
+    LkPix px[2];
+    px[0].pi = pi0;
+    px[0].pj = pj;
+    px[0].p = (long)pi0 * w + pj;
+    lk_begin(win, g0, GS, W, us, vs, half_pixel, px[0]);
+    px[1].pi = pi0 + 1;
+    px[1].pj = pj;
+    px[1].p = px[0].p + w;
+    if (two) lk_begin(win, g1, GS, W, us, vs, half_pixel, px[1]);
+    else px[1].active = false;
+    for (int it = 0; it < iterations && (px[0].active || px[1].active); it++) {
+        bool run[2], fast[2];
+        LkAxis ay[2], ax[2];
+        float oi[2], oj[2];
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            run[k] = px[k].active;
+            if (run[k] && (px[k].locI < 0.0f || px[k].locI >= (float)(h + hw) || px[k].locJ < 0.0f ||
+                           px[k].locJ >= (float)(w + hw))) {
+                px[k].active = false;
+                run[k] = false;
+            }
+            oi[k] = __fsub_rn(px[k].locI, (float)hw);
+            oj[k] = __fsub_rn(px[k].locJ, (float)hw);
+            fast[k] = run[k] && lk_fast(px[k], h, w, W, oi[k], oj[k], ay[k], ax[k]);
+        }
+        float s[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+        if (fast[0] && fast[1]) {
+            const bool sp0 = ax[0].split != W, sp1 = ax[1].split != W;
+            if (!sp0 && !sp1)
+                lk_pair_sums<WT, false, false>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, GS, s[0][0], s[0][1],
+                                               s[1][0], s[1][1]);
+            else if (sp0 && !sp1)
+                lk_pair_sums<WT, true, false>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, GS, s[0][0], s[0][1],
+                                              s[1][0], s[1][1]);
+            else if (!sp0 && sp1)
+                lk_pair_sums<WT, false, true>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, GS, s[0][0], s[0][1],
+                                              s[1][0], s[1][1]);
+            else
+                lk_pair_sums<WT, true, true>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, GS, s[0][0], s[0][1],
+                                             s[1][0], s[1][1]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                if (!run[k]) continue;
+                const int g = k ? g1 : g0;
+                if (fast[k]) {
+                    if (ax[k].split == W) lk_one_sums<WT, false>(B, w, ay[k], ax[k], win, g, GS, s[k][0], s[k][1]);
+                    else lk_one_sums<WT, true>(B, w, ay[k], ax[k], win, g, GS, s[k][0], s[k][1]);
+                } else {
+                    lk_sums_slow(B, h, w, W, oi[k], oj[k], win, g, GS, s[k][0], s[k][1]);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+            if (run[k] && !lk_update(px[k], s[k][0], s[k][1])) px[k].active = false;
+    }
+    lk_end(px[0], half_pixel, us, vs);
+    if (two) lk_end(px[1], half_pixel, us, vs);
+}
+
+// Any window side, one pixel per thread (16 x 16 threads per tile); the uniform fast path keeps
+// each thread's row of horizontal samples in shared memory (stride = threads, bank = lane).
+__global__ void __launch_bounds__(kLkTile *kLkTile, 2) dense_lk_kernel(const float *A, const float *B, int h, int w,
+                                                                        float *us, float *vs, int W, int iterations,
+                                                                        int half_pixel) {
+    extern __shared__ float smf[];
+    constexpr int kThreads = kLkTile * kLkTile;
+    const int hw = W / 2, GS = kLkTile + W - 1;
+    float *wa = smf, *wj = wa + GS * GS, *wi = wj + GS * GS, *reg = wi + GS * GS;
+    const int tid = threadIdx.y * kLkTile + threadIdx.x;
+    const int ti0 = blockIdx.y * kLkTile, tj0 = blockIdx.x * kLkTile;
+    lk_stage(A, h, w, W, half_pixel, ti0, tj0, tid, kThreads, kLkTile, reg, wa, wj, wi);
+    const LkWin win{wa, wj, wi};
+    const int pi = ti0 + threadIdx.y, pj = tj0 + threadIdx.x;
+    if (pi >= h || pj >= w) return;
+    const int g = threadIdx.y * GS + threadIdx.x;
+    LkPix px;
+    px.pi = pi;
+    px.pj = pj;
+    px.p = (long)pi * w + pj;
+    lk_begin(win, g, GS, W, us, vs, half_pixel, px);
+    float *hb = reg + tid;  // the staged region is dead: per-thread rows, stride kThreads
+    for (int it = 0; it < iterations && px.active; it++) {
+        if (px.locI < 0.0f || px.locI >= (float)(h + hw) || px.locJ < 0.0f || px.locJ >= (float)(w + hw)) break;
+        float b0 = 0.0f, b1 = 0.0f;
+        const float oi = __fsub_rn(px.locI, (float)hw), oj = __fsub_rn(px.locJ, (float)hw);
+        LkAxis ay, ax;
+        if (lk_fast(px, h, w, W, oi, oj, ay, ax) && ay.split == W && ax.split == W) {
+            const float dj = ax.f1, omj = __fsub_rn(1.0f, dj);
+            const float di = ay.f1, omi = __fsub_rn(1.0f, di);
+            const float *br = B + (long)ay.base * w + ax.base;
+            float x0 = br[0];
+            for (int b = 0; b < W; b++) {
+                const float x1 = br[b + 1];
+                hb[b * kThreads] = __fadd_rn(__fmul_rn(omj, x0), __fmul_rn(dj, x1));
+                x0 = x1;
+            }
+            for (int a = 0; a < W; a++) {
+                const int r = g + a * GS;
+                br += w;
+                x0 = br[0];
+                for (int b = 0; b < W; b++) {
+                    const float x1 = br[b + 1];
+                    const float bot = __fadd_rn(__fmul_rn(omj, x0), __fmul_rn(dj, x1));
+                    x0 = x1;
+                    const float top = hb[b * kThreads];
+                    hb[b * kThreads] = bot;
+                    const float smp = __fadd_rn(__fmul_rn(omi, top), __fmul_rn(di, bot));
+                    const float dT = __fsub_rn(smp, wa[r + b]);
+                    b0 = __fadd_rn(__fmul_rn(dT, wj[r + b]), b0);
+                    b1 = __fadd_rn(__fmul_rn(dT, wi[r + b]), b1);
+                }
+            }
+        } else {
+            lk_sums_slow(B, h, w, W, oi, oj, win, g, GS, b0, b1);
+        }
+        if (!lk_update(px, b0, b1)) break;
+    }
+    lk_end(px, half_pixel, us, vs);
+}
+
+// Shared memory: 3 window arrays plus the staged region (which later holds the per-thread rows of
+// the generic kernel).
 size_t lk_smem(int W, bool rows_in_smem) {
     const size_t RS = kLkTile + W + 1, GS = kLkTile + W - 1;
     const size_t rows = rows_in_smem ? (size_t)W * kLkTile * kLkTile : 0;
-    return sizeof(float4) * GS * GS + sizeof(float) * (RS * RS > rows ? RS * RS : rows);
+    return sizeof(float) * (3 * GS * GS + (RS * RS > rows ? RS * RS : rows));
 }
 
-template <int WT>
-static cudaError_t launch_lk_t(cudaStream_t s, const float *a, const float *b, int h, int w, float *us, float *vs,
-                               int W, int iterations, int half_pixel) {
-    const size_t sm = lk_smem(W, WT == 0);
-    cudaError_t e = cudaFuncSetAttribute(dense_lk_kernel<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+template <int WT, int MB>
+static cudaError_t launch_lk_pair(cudaStream_t s, const float *a, const float *b, int h, int w, float *us, float *vs,
+                                  int iterations, int half_pixel) {
+    const size_t sm = lk_smem(WT, false);
+    cudaError_t e =
+        cudaFuncSetAttribute(dense_lk_pair_kernel<WT, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    dim3 blk(kLkTile, kLkTile / 2), grd(blocks_of(w, kLkTile), blocks_of(h, kLkTile));
+    dense_lk_pair_kernel<WT, MB><<<grd, blk, sm, s>>>(a, b, h, w, us, vs, iterations, half_pixel);
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_lk_generic(cudaStream_t s, const float *a, const float *b, int h, int w, float *us,
+                                     float *vs, int W, int iterations, int half_pixel) {
+    const size_t sm = lk_smem(W, true);
+    cudaError_t e = cudaFuncSetAttribute(dense_lk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     dim3 blk(kLkTile, kLkTile), grd(blocks_of(w, kLkTile), blocks_of(h, kLkTile));
-    dense_lk_kernel<WT><<<grd, blk, sm, s>>>(a, b, h, w, us, vs, W, iterations, half_pixel);
+    dense_lk_kernel<<<grd, blk, sm, s>>>(a, b, h, w, us, vs, W, iterations, half_pixel);
     return cudaGetLastError();
 }
 
@@ -632,8 +838,8 @@ cudaError_t launch_normalize(cudaStream_t s, const float *in, long n, unsigned *
 cudaError_t launch_dense_lk(cudaStream_t s, const float *a, const float *b, int h, int w, float *us, float *vs, int W,
                             int iterations, int half_pixel) {
     // the reference's example window (27) runs with its sample rows in registers
-    if (W == 27) return launch_lk_t<27>(s, a, b, h, w, us, vs, W, iterations, half_pixel);
-    return launch_lk_t<0>(s, a, b, h, w, us, vs, W, iterations, half_pixel);
+    if (W == 27) return launch_lk_pair<27, 2>(s, a, b, h, w, us, vs, iterations, half_pixel);
+    return launch_lk_generic(s, a, b, h, w, us, vs, W, iterations, half_pixel);
 }
 
 // Liu-Shen passes on (us, vs) in place; fx: 8 planes, tmp: 2 planes, err: ls_err_bytes.
