@@ -411,6 +411,66 @@ qlpiv_status qlpiv_piv_flow_device(qlpiv_handle *h, const qlpiv_adaptive_desc *p
                                    int pixel_type, int height, int width, int num_pairs, const qlpiv_frame *frames,
                                    float *out_u, float *out_v, float *dense_u, float *dense_v);
 
+/* ---------------- request server (continuous batching) ----------------
+ * The reference runs one job per frame pair and host thread (S/jobs/LocalPIVOpenCLGpuJob.java,
+ * pooled by OpenClGpuManager.java:121-148); it has no server.  A qlpiv_server owns one device
+ * and a device-owner thread: requests (frame pairs of any size, each with its own adaptive
+ * schedule) are copied into pinned staging at submit, admitted while their device memory fits
+ * the HBM budget and a slot (a CUDA stream with its own plan) is free, run concurrently with the
+ * requests already on the device, and complete independently.  A request's displacements are
+ * those qlpiv_piv_adaptive gives for the same pair, whatever else is in flight. */
+typedef struct qlpiv_server qlpiv_server;
+
+typedef struct qlpiv_server_params {
+    int device;
+    int slots;                /* concurrent requests on the device; 0: 16 */
+    int64_t hbm_budget;       /* device bytes for in-flight requests; 0: 80 % of the free memory */
+    int64_t staging_bytes;    /* pinned host bytes for queued inputs and results; 0: 1 GiB */
+    int submit_timeout_ms;    /* how long qlpiv_submit waits for staging space; 0: 10 s */
+    int reserved[7];
+} qlpiv_server_params;
+
+typedef struct qlpiv_request {
+    const qlpiv_adaptive_desc *schedule;  /* copied at submit */
+    int pixel_type;                       /* QLPIV_PIX_U8 or QLPIV_PIX_U16 */
+    int height, width;
+    int64_t pitch;                        /* elements per row, >= width */
+    const void *img_a, *img_b;            /* copied at submit */
+    float *out_u, *out_v;                 /* last-level tiles (rows, columns); written before
+                                             qlpiv_poll reports the request done, so they must stay
+                                             valid until then */
+} qlpiv_request;
+
+typedef struct qlpiv_result {
+    int status;               /* qlpiv_status of the request */
+    int tiles_i, tiles_j;     /* last-level grid */
+    double queue_ms;          /* submit -> admitted to the device */
+    double device_ms;         /* admitted -> results on the host */
+    double total_ms;          /* submit -> results on the host */
+} qlpiv_result;
+
+typedef struct qlpiv_server_stats {
+    int64_t submitted, completed, failed, pending, in_flight;
+    int64_t device_bytes_in_flight, hbm_budget;
+    int64_t reserved[4];
+} qlpiv_server_stats;
+
+qlpiv_status qlpiv_server_create(const qlpiv_server_params *params, qlpiv_server **out);
+/* Cancels the queued requests (their qlpiv_poll reports QLPIV_E_CANCELLED), waits for those on
+ * the device and frees everything. */
+qlpiv_status qlpiv_server_destroy(qlpiv_server *s);
+/* Checks and copies the request; returns a ticket.  QLPIV_E_TIMEOUT when the staging stayed full
+ * for submit_timeout_ms, QLPIV_E_OOM when the request can never fit the budget or the staging. */
+qlpiv_status qlpiv_submit(qlpiv_server *s, const qlpiv_request *req, uint64_t *ticket);
+/* Waits up to timeout_ms (< 0: forever) for the request.  QLPIV_OK: done, *result filled and the
+ * ticket released (check result->status); QLPIV_E_TIMEOUT: not done yet; QLPIV_E_ARG: unknown
+ * ticket. */
+qlpiv_status qlpiv_poll(qlpiv_server *s, uint64_t ticket, qlpiv_result *result, int timeout_ms);
+qlpiv_status qlpiv_server_stats_read(qlpiv_server *s, qlpiv_server_stats *stats);
+/* Device bytes an adaptive plan of `pairs` frame pairs uses (the server's admission estimate). */
+qlpiv_status qlpiv_adaptive_plan_bytes(const qlpiv_adaptive_desc *desc, int pixel_type, int height, int width,
+                                       int pairs, int64_t *bytes);
+
 /* Stage timing of the adaptive pipeline (CUDA events around every launch on the
  * handle's stream).  Accumulates while enabled; qlpiv_profile_read synchronises the
  * stream, returns the totals per (stage, level) and clears them. */

@@ -145,6 +145,28 @@ class Params(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
 
+class ServerParams(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("slots", ctypes.c_int), ("hbm_budget", ctypes.c_int64),
+                ("staging_bytes", ctypes.c_int64), ("submit_timeout_ms", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("schedule", ctypes.POINTER(AdaptiveDesc)), ("pixel_type", ctypes.c_int), ("height", ctypes.c_int),
+                ("width", ctypes.c_int), ("pitch", ctypes.c_int64), ("img_a", ctypes.c_void_p),
+                ("img_b", ctypes.c_void_p), ("out_u", ctypes.c_void_p), ("out_v", ctypes.c_void_p)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("tiles_i", ctypes.c_int), ("tiles_j", ctypes.c_int),
+                ("queue_ms", ctypes.c_double), ("device_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int64) for k in ("submitted", "completed", "failed", "pending", "in_flight",
+                                              "device_bytes_in_flight", "hbm_budget")] + \
+               [("reserved", ctypes.c_int64 * 4)]
+
+
 # C ABI symbol table: name -> (restype, argtypes).  Kept beside include/qlpiv.h.
 _vp, _i, _l, _f = ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_float
 _SIGNATURES = {
@@ -184,6 +206,12 @@ _SIGNATURES = {
                             _vp, _vp, _vp]),
     "qlpiv_piv_flow_device": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), ctypes.POINTER(FlowDesc), _i, _i, _i, _i, _vp,
                                    _vp, _vp, _vp, _vp]),
+    "qlpiv_server_create": (_i, [ctypes.POINTER(ServerParams), ctypes.POINTER(_vp)]),
+    "qlpiv_server_destroy": (_i, [_vp]),
+    "qlpiv_submit": (_i, [_vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+    "qlpiv_poll": (_i, [_vp, ctypes.c_uint64, ctypes.POINTER(Result), _i]),
+    "qlpiv_server_stats_read": (_i, [_vp, ctypes.POINTER(ServerStats)]),
+    "qlpiv_adaptive_plan_bytes": (_i, [ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, ctypes.POINTER(ctypes.c_int64)]),
     "qlpiv_profile_enable": (_i, [_vp, _i]),
     "qlpiv_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(_i)]),
 }
@@ -639,6 +667,85 @@ class Handle:
         a = [x if isinstance(x, int) else _addr(x) for x in (frames, out_u, out_v)]
         _check(self._lib.qlpiv_piv_adaptive_device(self._h, ctypes.byref(desc), pixel_type, height, width, num_pairs,
                                                    a[0], a[1], a[2]))
+
+
+def adaptive_plan_bytes(desc, pixel_type, height, width, pairs=1):
+    """Device bytes of an adaptive plan (the request server's admission estimate)."""
+    b = ctypes.c_int64()
+    _check(load_library().qlpiv_adaptive_plan_bytes(ctypes.byref(desc), pixel_type, height, width, pairs,
+                                                    ctypes.byref(b)))
+    return b.value
+
+
+class Server:
+    """Request server (qlpiv_server_*): submit frame pairs of any size with their own adaptive
+    schedule from any thread, poll for the displacements."""
+
+    def __init__(self, device=0, slots=0, hbm_budget=0, staging_bytes=0, submit_timeout_ms=0):
+        lib = load_library()
+        self._lib = lib
+        p = ServerParams()
+        p.device, p.slots, p.hbm_budget, p.staging_bytes, p.submit_timeout_ms = (device, slots, hbm_budget,
+                                                                                  staging_bytes, submit_timeout_ms)
+        s = ctypes.c_void_p()
+        _check(lib.qlpiv_server_create(ctypes.byref(p), ctypes.byref(s)))
+        self._s = s
+        self._outs = {}
+
+    def close(self):
+        if getattr(self, "_s", None):
+            self._lib.qlpiv_server_destroy(self._s)
+            self._s = None
+            self._outs.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, img_a, img_b, desc):
+        """Queues one pair (2-D u8 / u16 arrays of one shape); returns the ticket."""
+        a = np.ascontiguousarray(img_a)
+        b = np.ascontiguousarray(img_b, a.dtype)
+        h, w = a.shape
+        last = adaptive_levels(desc, h, w)[-1]
+        u = np.empty((last["tiles_i"], last["tiles_j"]), np.float32)
+        v = np.empty_like(u)
+        r = Request()
+        keep_desc = AdaptiveDesc.from_buffer_copy(desc)
+        r.schedule = ctypes.pointer(keep_desc)
+        r.pixel_type, r.height, r.width, r.pitch = pixel_type_of(a.dtype), h, w, w
+        r.img_a, r.img_b, r.out_u, r.out_v = a.ctypes.data, b.ctypes.data, u.ctypes.data, v.ctypes.data
+        t = ctypes.c_uint64()
+        _check(self._lib.qlpiv_submit(self._s, ctypes.byref(r), ctypes.byref(t)))
+        self._outs[t.value] = (u, v)   # the library writes them before poll reports the ticket done
+        return t.value
+
+    def poll(self, ticket, timeout_ms=-1):
+        """None while the request runs (timeout); else (u, v, info); raises on a failed request."""
+        res = Result()
+        st = self._lib.qlpiv_poll(self._s, ctypes.c_uint64(ticket), ctypes.byref(res), int(timeout_ms))
+        if st == E_TIMEOUT:
+            return None
+        _check(st)
+        u, v = self._outs.pop(ticket)
+        info = {"queue_ms": res.queue_ms, "device_ms": res.device_ms, "total_ms": res.total_ms,
+                "tiles": (res.tiles_i, res.tiles_j)}
+        if res.status != OK:
+            raise QlpivError(res.status, self._lib.qlpiv_last_error().decode())
+        return u, v, info
+
+    def stats(self):
+        st = ServerStats()
+        _check(self._lib.qlpiv_server_stats_read(self._s, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_ if k != "reserved"}
 
 
 from . import grid, jobs, per_call, synth  # noqa: E402,F401

@@ -16,10 +16,13 @@
 namespace {
 
 thread_local std::string g_last_error;
+thread_local qlpiv::AsyncAlloc g_async_alloc;
 
 }  // namespace
 
 namespace qlpiv {
+
+AsyncAlloc &async_alloc_tls() { return g_async_alloc; }
 
 qlpiv_status fail(qlpiv_status st, const char *fmt, ...) {
     char buf[512];

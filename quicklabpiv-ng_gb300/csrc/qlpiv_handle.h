@@ -13,24 +13,51 @@ namespace qlpiv {
 qlpiv_status fail(qlpiv_status st, const char *fmt, ...);
 qlpiv_status cuda_fail(cudaError_t e, const char *what);
 
+// Stream-ordered allocation for the buffers a thread creates while an AsyncAllocScope is
+// active (the request server: no device-wide synchronisation from cudaMalloc / cudaFree while
+// other requests run).
+struct AsyncAlloc {
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t stream = nullptr;
+};
+AsyncAlloc &async_alloc_tls();
+struct AsyncAllocScope {
+    AsyncAlloc saved;
+    AsyncAllocScope(cudaMemPool_t pool, cudaStream_t stream) : saved(async_alloc_tls()) {
+        async_alloc_tls() = AsyncAlloc{pool, stream};
+    }
+    ~AsyncAllocScope() { async_alloc_tls() = saved; }
+};
+
 // Device buffer that only grows.
 struct DevBuf {
     void *p = nullptr;
     size_t cap = 0;
+    cudaStream_t astream = nullptr;  // set when allocated from a pool: freed in that stream's order
     cudaError_t ensure(size_t bytes) {
         if (bytes <= cap) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
+        release();
         size_t want = bytes < 256 ? 256 : bytes;
-        cudaError_t e = cudaMalloc(&p, want);
+        const AsyncAlloc &aa = async_alloc_tls();
+        cudaError_t e;
+        if (aa.pool) {
+            e = cudaMallocFromPoolAsync(&p, want, aa.pool, aa.stream);
+            if (e == cudaSuccess) astream = aa.stream;
+        } else {
+            e = cudaMalloc(&p, want);
+        }
         if (e == cudaSuccess) cap = want;
+        else p = nullptr;
         return e;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (astream) cudaFreeAsync(p, astream);
+            else cudaFree(p);
+        }
         p = nullptr;
         cap = 0;
+        astream = nullptr;
     }
     template <typename T>
     T *as() const {

@@ -20,6 +20,14 @@ bool xcorr_size_supported(int n);
 // FindMaximumMultiPeaks settings the kernel supports for IA side n (records fit on chip).
 bool multipeak_supported(int n, int num_peaks, int peak_kernel);
 
+// Request-server helpers (qlpiv_pipeline.cu): admission estimate of an adaptive plan's device
+// memory; the adaptive loop of one pinned host pair queued without waiting; dropping a plan.
+size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int height, int width, int pairs);
+qlpiv_status queue_adaptive_pinned(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int pixel_type, int height,
+                                   int width, const void *img_a, const void *img_b, long pitch, float *out_u,
+                                   float *out_v);
+void drop_plan(qlpiv_handle *h);
+
 inline size_t pixel_bytes(int pixel_type) {
     return pixel_type == QLPIV_PIX_U8 ? 1 : (pixel_type == QLPIV_PIX_U16 ? 2 : 4);
 }

@@ -384,6 +384,104 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
     return QLPIV_OK;
 }
 
+static qlpiv_status check_host_frames(const qlpiv_frame *frames, int num_pairs, int height, int width) {
+    for (int q = 0; q < num_pairs; q++)
+        if (!frames[q].img_a || !frames[q].img_b || frames[q].height != height || frames[q].width != width ||
+            frames[q].pitch < width)
+            return fail(QLPIV_E_SHAPE, "frame %d: NULL image or size differs from %d x %d", q, height, width);
+    return QLPIV_OK;
+}
+
+// Copies host frame pairs into the plan's frame buffers (packed rows) and their table; the
+// table's host staging is kept in `t` until the caller synchronises.
+static qlpiv_status upload_host_frames(qlpiv_handle *h, const qlpiv_frame *frames, std::vector<qlpiv_frame> &t) {
+    AdaptivePlan *p = h->plan;
+    cudaStream_t s = h->stream;
+    const int num_pairs = p->pairs, height = p->height, width = p->width;
+    const size_t pb = pixel_bytes(p->pixel_type), row = (size_t)width * pb, img = row * height;
+    const size_t stride = (img + 255) & ~(size_t)255;
+    cudaError_t e;
+    if ((e = p->host_frames.ensure(2 * stride * num_pairs)) != cudaSuccess ||
+        (e = p->host_table.ensure(sizeof(qlpiv_frame) * num_pairs)) != cudaSuccess)
+        return cuda_fail(e, "frame buffers");
+    t.resize(num_pairs);
+    char *base = p->host_frames.as<char>();
+    for (int q = 0; q < num_pairs; q++) {
+        char *da = base + 2 * q * stride, *db = base + (2 * q + 1) * stride;
+        if ((e = cudaMemcpy2DAsync(da, row, frames[q].img_a, (size_t)frames[q].pitch * pb, row, height,
+                                   cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpy2DAsync(db, row, frames[q].img_b, (size_t)frames[q].pitch * pb, row, height,
+                                   cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return cuda_fail(e, "frame upload");
+        t[q] = {da, db, height, width, (int64_t)width};
+    }
+    if ((e = cudaMemcpyAsync(p->host_table.p, t.data(), sizeof(qlpiv_frame) * num_pairs, cudaMemcpyHostToDevice,
+                             s)) != cudaSuccess)
+        return cuda_fail(e, "frame table upload");
+    return QLPIV_OK;
+}
+
+// Device bytes the adaptive plan of `pairs` pairs allocates (the buffers of build_plan_inner, each
+// rounded to 256 B) plus the device copies of host frames: the request server's admission estimate.
+size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int height, int width, int pairs) {
+    auto al = [](size_t x) { return ((x < 256 ? 256 : x) + 255) & ~(size_t)255; };
+    size_t total = 0;
+    const int nlev = level_count(d);
+    int prev_nj = 0;
+    for (int lv = 0; lv < nlev; lv++) {
+        qlpiv_grid g{};
+        if (grid_superposition(height, width, d->margins, d->ia_start, lv, d->overlap_factor, &g, nullptr, nullptr,
+                               0) < -1)
+            return 0;
+        const size_t ni = g.tiles_i, nj = g.tiles_j, cnt = ni * nj, tot = cnt * pairs;
+        total += al(8 * ni) + al(8 * nj) + al(4 * ni) + al(4 * nj) + al(8 * ni) + al(8 * nj);
+        total += 5 * al(4 * tot) + 2 * al(4 * tot) + al(coef_bytes((long)tot));
+        if (lv > 0) total += al(8 * (size_t)pairs * ni * prev_nj);
+        total += al(4 * ni) + al(4 * nj);
+        if (d->validation != QLPIV_VALIDATE_NONE) {
+            const size_t k = d->num_peaks;
+            total += 2 * al(4 * cnt) + 2 * al(4 * tot) + al(8 * tot * k) + 2 * al(tot) + 2 * al(4 * tot) +
+                     al(4 * (size_t)pairs);
+        }
+        prev_nj = (int)nj;
+    }
+    const size_t img = (size_t)height * width * pixel_bytes(pixel_type);
+    const size_t stride = (img + 255) & ~(size_t)255;
+    total += al(2 * stride * pairs) + al(sizeof(qlpiv_frame) * pairs);  // frames copied from the host
+    if (d->warp_mode == QLPIV_WARP_BOTH_BILINEAR) total += al(2 * stride * pairs) + al(sizeof(qlpiv_frame) * pairs);
+    return total;
+}
+
+// Queues one host frame pair (pinned memory, rows of `pitch` elements) through the adaptive loop
+// on the handle's stream and the last level's displacements into pinned out_u / out_v; does not
+// wait.  The frames and the results stay valid until the stream passes this point.
+qlpiv_status queue_adaptive_pinned(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int pixel_type, int height,
+                                   int width, const void *img_a, const void *img_b, long pitch, float *out_u,
+                                   float *out_v) {
+    qlpiv_status st = check_adaptive(desc, pixel_type, height, width);
+    if (st != QLPIV_OK) return st;
+    if ((st = build_plan(h, desc, pixel_type, height, width, 1)) != QLPIV_OK) return st;
+    qlpiv_frame f{img_a, img_b, height, width, (int64_t)pitch};
+    std::vector<qlpiv_frame> t;
+    if ((st = upload_host_frames(h, &f, t)) != QLPIV_OK) return st;
+    if ((st = run_levels(h, h->plan->host_table.as<qlpiv_frame>())) != QLPIV_OK) return st;
+    LevelPlan &L = h->plan->levels.back();
+    const size_t bytes = sizeof(float) * L.count();
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(out_u, L.d_u.p, bytes, cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(out_v, L.d_v.p, bytes, cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess)
+        return cuda_fail(e, "result download");
+    return QLPIV_OK;
+}
+
+// Releases the handle's cached adaptive plan (its device memory) after the stream drains.
+void drop_plan(qlpiv_handle *h) {
+    if (!h->plan) return;
+    cudaStreamSynchronize(h->stream);
+    destroy_plan(h->plan);
+    h->plan = nullptr;
+}
+
 }  // namespace qlpiv
 
 using namespace qlpiv;
@@ -579,43 +677,6 @@ qlpiv_status qlpiv_piv_adaptive_device(qlpiv_handle *h, const qlpiv_adaptive_des
     if ((e = cudaMemcpyAsync(out_u, L.d_u.p, bytes, cudaMemcpyDeviceToDevice, h->stream)) != cudaSuccess ||
         (e = cudaMemcpyAsync(out_v, L.d_v.p, bytes, cudaMemcpyDeviceToDevice, h->stream)) != cudaSuccess)
         return cuda_fail(e, "adaptive output");
-    return QLPIV_OK;
-}
-
-static qlpiv_status check_host_frames(const qlpiv_frame *frames, int num_pairs, int height, int width) {
-    for (int q = 0; q < num_pairs; q++)
-        if (!frames[q].img_a || !frames[q].img_b || frames[q].height != height || frames[q].width != width ||
-            frames[q].pitch < width)
-            return fail(QLPIV_E_SHAPE, "frame %d: NULL image or size differs from %d x %d", q, height, width);
-    return QLPIV_OK;
-}
-
-// Copies host frame pairs into the plan's frame buffers (packed rows) and their table; the
-// table's host staging is kept in `t` until the caller synchronises.
-static qlpiv_status upload_host_frames(qlpiv_handle *h, const qlpiv_frame *frames, std::vector<qlpiv_frame> &t) {
-    AdaptivePlan *p = h->plan;
-    cudaStream_t s = h->stream;
-    const int num_pairs = p->pairs, height = p->height, width = p->width;
-    const size_t pb = pixel_bytes(p->pixel_type), row = (size_t)width * pb, img = row * height;
-    const size_t stride = (img + 255) & ~(size_t)255;
-    cudaError_t e;
-    if ((e = p->host_frames.ensure(2 * stride * num_pairs)) != cudaSuccess ||
-        (e = p->host_table.ensure(sizeof(qlpiv_frame) * num_pairs)) != cudaSuccess)
-        return cuda_fail(e, "frame buffers");
-    t.resize(num_pairs);
-    char *base = p->host_frames.as<char>();
-    for (int q = 0; q < num_pairs; q++) {
-        char *da = base + 2 * q * stride, *db = base + (2 * q + 1) * stride;
-        if ((e = cudaMemcpy2DAsync(da, row, frames[q].img_a, (size_t)frames[q].pitch * pb, row, height,
-                                   cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-            (e = cudaMemcpy2DAsync(db, row, frames[q].img_b, (size_t)frames[q].pitch * pb, row, height,
-                                   cudaMemcpyHostToDevice, s)) != cudaSuccess)
-            return cuda_fail(e, "frame upload");
-        t[q] = {da, db, height, width, (int64_t)width};
-    }
-    if ((e = cudaMemcpyAsync(p->host_table.p, t.data(), sizeof(qlpiv_frame) * num_pairs, cudaMemcpyHostToDevice,
-                             s)) != cudaSuccess)
-        return cuda_fail(e, "frame table upload");
     return QLPIV_OK;
 }
 

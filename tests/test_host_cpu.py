@@ -39,7 +39,9 @@ def test_ctypes_structs_match_header(qp, tmp_path):
     import subprocess
     mirrors = {"qlpiv_pass_desc": qp.PassDesc, "qlpiv_frame": qp.Frame, "qlpiv_grid": qp.Grid,
                "qlpiv_adaptive_desc": qp.AdaptiveDesc, "qlpiv_flow_desc": qp.FlowDesc,
-               "qlpiv_stage_time": qp.StageTime, "qlpiv_params": qp.Params}
+               "qlpiv_stage_time": qp.StageTime, "qlpiv_params": qp.Params,
+               "qlpiv_server_params": qp.ServerParams, "qlpiv_request": qp.Request, "qlpiv_result": qp.Result,
+               "qlpiv_server_stats": qp.ServerStats}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "qlpiv.h"', "int main(void) {"]
     for name, cls in mirrors.items():
         lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
@@ -181,3 +183,31 @@ def test_adaptive_levels_config2(qp):
         qp.adaptive_levels(qp.adaptive_desc(64, 24, 0.25), 1024, 1024)
     with pytest.raises(qp.QlpivError):
         qp.adaptive_levels(qp.adaptive_desc(128, 16, 0.25), 1024, 1024)   # IA 128 not built yet
+
+
+def test_adaptive_plan_bytes_properties(qp):
+    """The request server's admission estimate: grows with the frame size and the pair count,
+    and by the warped frames and the validation buffers when those are configured."""
+    d = qp.adaptive_desc(64, 16, 0.25, warp_mode=qp.WARP_NONE)
+    b1 = qp.adaptive_plan_bytes(d, qp.PIX_U8, 512, 512)
+    b2 = qp.adaptive_plan_bytes(d, qp.PIX_U8, 512, 512, pairs=2)
+    assert 2 * 512 * 512 < b1 < b2 <= 2 * b1
+    assert qp.adaptive_plan_bytes(d, qp.PIX_U16, 512, 512) - b1 >= 2 * 512 * 512   # 2 bytes per pixel
+    assert qp.adaptive_plan_bytes(d, qp.PIX_U8, 1024, 1024) > 3 * b1
+    dw = qp.adaptive_desc(64, 16, 0.25, warp_mode=qp.WARP_BOTH_BILINEAR)
+    assert qp.adaptive_plan_bytes(dw, qp.PIX_U8, 512, 512) - b1 >= 2 * 512 * 512   # warped copies
+    dv = qp.adaptive_desc(64, 16, 0.25, warp_mode=qp.WARP_NONE, validation=qp.multipeak_validation(num_peaks=3))
+    assert qp.adaptive_plan_bytes(dv, qp.PIX_U8, 512, 512) > b1 + 3 * 8 * 253 * 253 // 4
+    with pytest.raises(qp.QlpivError):
+        qp.adaptive_plan_bytes(d, qp.PIX_F32, 512, 512)
+    with pytest.raises(qp.QlpivError):
+        qp.adaptive_plan_bytes(d, qp.PIX_U8, 40, 40)
+
+
+def test_server_without_gpu_reports_no_device(qp):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(qp.QlpivError) as e:
+        qp.Server(0)
+    assert e.value.status == qp.E_NO_DEVICE
