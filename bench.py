@@ -263,6 +263,108 @@ def run_per_call(pkg, dev, desc, pairs_host, count):
     return 1.0 / per_call_s, 1.0 / per_pair_s
 
 
+# Served stream: requests of log-uniform sizes 256^2..4096^2 (u8 / 12-bit u16 mixed), each with
+# one of three schedules (single 32; 64 -> 32; 64 -> 32 -> 16 with BothImages warp), 50 % overlap.
+SERVING_WORKLOAD = ("served-mixed: Poisson arrivals of frame pairs, sides log-uniform 256..4096 (multiples of 32), "
+                    "u8 / 12-bit u16 mixed, schedules single 32 | 64->32 | 64->32->16 + BothImages warp, 50 % "
+                    "overlap")
+
+
+def serving_requests(pkg, count, seed=5):
+    """Frames cropped from one synthetic 4096x4096 mosaic (a 2048x2048 vortex pair tiled 2 x 2)."""
+    a0, b0 = pkg.synth.particle_pair((2048, 2048), pkg.synth.Flow(vmax=5.0, rc=200.0, shear=0.003), ppp=0.02,
+                                     diam=2.8, bits=8, seed=seed)
+    ma, mb = np.tile(a0, (2, 2)), np.tile(b0, (2, 2))
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        side = lambda: int(np.clip(round(np.exp(rng.uniform(np.log(256), np.log(4096))) / 32) * 32, 256, 4096))
+        h, w = side(), side()
+        y, x = int(rng.integers(0, 4096 - h + 1)), int(rng.integers(0, 4096 - w + 1))
+        a, b = ma[y:y + h, x:x + w], mb[y:y + h, x:x + w]
+        if rng.random() < 0.5:   # 12-bit in u16
+            a, b = a.astype(np.uint16) * 16, b.astype(np.uint16) * 16
+        out.append((np.ascontiguousarray(a), np.ascontiguousarray(b), int(rng.integers(3))))
+    return out
+
+
+def serving_schedules(pkg):
+    return [pkg.adaptive_desc(32, 32, 0.5, warp_mode=pkg.WARP_NONE),
+            pkg.adaptive_desc(64, 32, 0.5, warp_mode=pkg.WARP_NONE),
+            pkg.adaptive_desc(64, 16, 0.5, warp_mode=pkg.WARP_BOTH_BILINEAR)]
+
+
+def run_serving(pkg, dev, count=48, loads=(0.25, 0.5, 0.75, 0.9, 1.1), per_load=48):
+    """Saturation throughput of the request server, the plain per-call paths on the same requests,
+    and p50 / p99 latency (submit -> results on the host) under Poisson arrivals at fractions of
+    the saturation rate."""
+    reqs = serving_requests(pkg, count)
+    sch = serving_schedules(pkg)
+    px = sum(a.size for a, _, _ in reqs)
+    # plain per-call: one synchronous library call per request (fused adaptive loop), and one
+    # synchronous call per stage (the reference's job pattern)
+    h = pkg.Handle(dev.index)
+    for a, b, k in reqs[:3]:
+        h.piv_adaptive([a], [b], sch[k])
+    t0 = time.perf_counter()
+    for a, b, k in reqs:
+        h.piv_adaptive([a], [b], sch[k])
+    per_call = count / (time.perf_counter() - t0)
+    sample = reqs[:8]
+    t0 = time.perf_counter()
+    for a, b, k in sample:
+        pkg.per_call.piv_adaptive_per_call(h, a, b, sch[k])
+    per_stage = len(sample) / (time.perf_counter() - t0)
+    h.close()
+
+    srv = pkg.Server(dev.index, slots=16, staging_bytes=4 << 30)
+    try:
+        def closed_loop():
+            t = time.perf_counter()
+            tickets = [srv.submit(a, b, sch[k]) for a, b, k in reqs]
+            for tk in tickets:
+                srv.poll(tk)
+            return count / (time.perf_counter() - t)
+
+        closed_loop()                       # warm-up: plans, pools
+        saturation = closed_loop()
+        sweep = []
+        rng = np.random.default_rng(9)
+        for load in loads:
+            rate = load * saturation
+            gaps = rng.exponential(1.0 / rate, per_load)
+            order = rng.integers(0, count, per_load)
+            lat = []
+            start = time.perf_counter()
+            due = start
+            pend = []
+            for g, idx in zip(gaps, order):
+                due += g
+                while time.perf_counter() < due:
+                    time.sleep(min(0.0005, max(0.0, due - time.perf_counter())))
+                a, b, k = reqs[idx]
+                pend.append(srv.submit(a, b, sch[k]))
+                # collect whatever finished meanwhile
+                while pend:
+                    r = srv.poll(pend[0], timeout_ms=0)
+                    if r is None:
+                        break
+                    lat.append(r[2]["total_ms"])
+                    pend.pop(0)
+            for tk in pend:
+                lat.append(srv.poll(tk)[2]["total_ms"])
+            elapsed = time.perf_counter() - start
+            sweep.append({"offered_pairs_per_s": rate, "achieved_pairs_per_s": per_load / elapsed,
+                          "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))})
+    finally:
+        srv.close()
+    return {"workload": SERVING_WORKLOAD, "requests": count, "megapixels_per_request": px / count / 1e6,
+            "saturation_pairs_per_s": saturation, "plain_per_call_pairs_per_s": per_call,
+            "plain_per_stage_pairs_per_s": per_stage, "vs_per_call": saturation / per_call,
+            "vs_per_stage": saturation / per_stage, "sweep": sweep,
+            "latency": "submit -> displacements on the host (qlpiv_poll), Poisson arrivals"}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -426,6 +528,8 @@ def run_gpu(args, rank, world):
         "one_pair_per_call_fused": world * pp_value}
     if not args.no_hybrid:
         result["hybrid"] = run_hybrid(pkg, h, dev, stream, max(2, min(args.steps, 5)), max(3, args.warmup))
+    if not args.no_serving and world == 1:
+        result["serving"] = run_serving(pkg, dev)
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         t_cpu = cpu_baseline(pkg, pairs_host[0], threads)
@@ -446,6 +550,7 @@ def main():
     ap.add_argument("--unique", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-hybrid", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
