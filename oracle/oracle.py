@@ -68,6 +68,13 @@ def lib():
         L.orc_find_max_from_center_f32.argtypes = [fp, c_int, c_int, ip, ip, fp, fp]
         L.orc_find_max_from_center_f64.argtypes = [dp, c_int, c_int, ip, ip, dp, dp]
         L.orc_subpixel_gauss3_f32.argtypes = [fp, c_int, c_int, c_int, c_int, fp, fp, ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_gauss_lm_fit.argtypes = [dp, dp, c_int, dp]
+        L.orc_gauss_lm_fit.restype = c_int
+        L.orc_hongwei_guo_fit.argtypes = [fp, fp, c_int, c_int, fp, fp]
+        L.orc_hongwei_guo_fit.restype = c_int
+        L.orc_subpixel_lm.argtypes = [fp, c_int, c_int, c_int, c_int, c_float, fp, fp, ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_subpixel_hg.argtypes = [fp, c_int, c_int, c_int, c_int, c_int, c_float, fp, fp, fp,
+                                      ctypes.POINTER(ctypes.c_uint32)]
         L.orc_subpixel_gauss3_f64.argtypes = [dp, c_int, c_int, c_int, c_int, dp, dp, ctypes.POINTER(ctypes.c_uint32)]
         L.orc_clip_tile.argtypes = [vp, c_int, c_int, c_int, c_int, c_int, c_int, fp]
         L.orc_clip_tile.restype = c_float
@@ -150,6 +157,50 @@ def find_max_from_center(plane):
         lib().orc_find_max_from_center_f64(_ptr(plane, ctypes.c_double), di, dj, ctypes.byref(oi),
                                            ctypes.byref(oj), ctypes.byref(ov), ctypes.byref(om))
     return oi.value, oj.value, ov.value, om.value
+
+
+SUBPIX_NONE, SUBPIX_GAUSS3, SUBPIX_GAUSS_LM, SUBPIX_HONGWEI_GUO = 0, 1, 2, 3
+
+
+def subpix_code(mode, pixels=3, iterations=20):
+    """The packed sub-pixel argument of the oracle's passes."""
+    return int(mode) | (int(pixels) << 8) | (int(iterations) << 16)
+
+
+def gauss_lm_fit(x, y):
+    """Least-squares Gaussian mean of (x, y) (Levenberg-Marquardt), or None."""
+    x, y = _f64(x), _f64(y)
+    m = ctypes.c_double()
+    ok = lib().orc_gauss_lm_fit(_ptr(x, ctypes.c_double), _ptr(y, ctypes.c_double), len(x), ctypes.byref(m))
+    return m.value if ok else None
+
+
+def hongwei_guo_fit(xs, ys, iterations):
+    """Hongwei Guo weighted log fit: (mean, amplitude) or None when singular."""
+    xs, ys = _f32(xs), _f32(ys)
+    m, a = ctypes.c_float(), ctypes.c_float()
+    ok = lib().orc_hongwei_guo_fit(_ptr(xs, ctypes.c_float), _ptr(ys, ctypes.c_float), len(xs), iterations,
+                                   ctypes.byref(m), ctypes.byref(a))
+    return (m.value, a.value) if ok else None
+
+
+def subpixel_lm(plane, mi, mj, pixels, min_floor=0.0):
+    """Gaussian1DInterpolator on a float plane: (sub_i, sub_j, flags)."""
+    plane = _f32(plane)
+    si, sj, fl = ctypes.c_float(), ctypes.c_float(), ctypes.c_uint32()
+    lib().orc_subpixel_lm(_ptr(plane, ctypes.c_float), plane.shape[0], mi, mj, pixels, min_floor, ctypes.byref(si),
+                          ctypes.byref(sj), ctypes.byref(fl))
+    return si.value, sj.value, fl.value
+
+
+def subpixel_hg(plane, mi, mj, pixels, iterations, peak_value, min_floor=0.0):
+    """Gaussian1DHongweiGuoInterpolator on a float plane: (sub_i, sub_j, peak_value, flags)."""
+    plane = _f32(plane)
+    si, sj, fl = ctypes.c_float(), ctypes.c_float(), ctypes.c_uint32()
+    pv = ctypes.c_float(peak_value)
+    lib().orc_subpixel_hg(_ptr(plane, ctypes.c_float), plane.shape[0], mi, mj, pixels, iterations, min_floor,
+                          ctypes.byref(si), ctypes.byref(sj), ctypes.byref(pv), ctypes.byref(fl))
+    return si.value, sj.value, pv.value, fl.value
 
 
 def subpixel_gauss3(plane, mi, mj):

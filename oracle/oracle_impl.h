@@ -279,6 +279,29 @@ static void FN(subpixel_gauss3)(const REAL *p, int di, int dj, int mi, int mj, R
     *pi = peakI; *pj = peakJ; *flags = f;
 }
 
+/* The pass's sub-pixel mode (packed: mode | pixels << 8 | iterations << 16) on peak (mi, mj);
+ * the P-point interpolators fit the plane values as floats, like the reference's MatrixFloat. */
+static void FN(subpixel_any)(const REAL *p, int d, int mi, int mj, int subpix, REAL minf, REAL *pi, REAL *pj,
+                             REAL *pv, uint32_t *flags) {
+    const int mode = subpix & 0xff, P = (subpix >> 8) & 0xff, iters = (subpix >> 16) & 0xff;
+    *pi = (REAL)mi;
+    *pj = (REAL)mj;
+    *flags = 0;
+    if (mode == 1) {
+        FN(subpixel_gauss3)(p, d, d, mi, mj, pi, pj, flags);
+    } else if (mode == 2 || mode == 3) {
+        float *pf = (float *)malloc(sizeof(float) * (size_t)d * d);
+        for (size_t k = 0; k < (size_t)d * d; k++) pf[k] = (float)p[k];
+        float si, sj, v = (float)*pv;
+        if (mode == 2) orc_subpixel_lm(pf, d, mi, mj, P, (float)minf, &si, &sj, flags);
+        else orc_subpixel_hg(pf, d, mi, mj, P, iters, (float)minf, &si, &sj, &v, flags);
+        *pi = (REAL)si;
+        *pj = (REAL)sj;
+        *pv = (REAL)v;
+        free(pf);
+    }
+}
+
 /* One IA through the whole CPU path: xcorr plane -> FindMaximumFromCenter ->
  * Gaussian 1D-1D sub-pixel -> displacement (u rows, v columns). */
 static void FN(ia_vector)(const float *ta, const float *tb, int n, float maxA, float maxB, int normalize,
@@ -290,7 +313,7 @@ static void FN(ia_vector)(const float *ta, const float *tb, int n, float maxA, f
     FN(find_max_from_center)(plane_scratch, d, d, &mi, &mj, &mv, &minf);
     REAL pi = (REAL)mi, pj = (REAL)mj;
     uint32_t flags = 0;
-    if (subpix) FN(subpixel_gauss3)(plane_scratch, d, d, mi, mj, &pi, &pj, &flags);
+    FN(subpixel_any)(plane_scratch, d, mi, mj, subpix, minf, &pi, &pj, &mv, &flags);
     const REAL half = (REAL)(d / 2);
     out->u = (float)(pi - half);
     out->v = (float)(pj - half);
@@ -425,7 +448,7 @@ static int FN(ia_vectors_multi)(const float *ta, const float *tb, int n, float m
     for (int r = 0; r < np; r++) {
         REAL si = (REAL)pi[r], sj = (REAL)pj[r];
         uint32_t flags = 0;
-        if (subpix) FN(subpixel_gauss3)(plane_scratch, d, d, pi[r], pj[r], &si, &sj, &flags);
+        FN(subpixel_any)(plane_scratch, d, pi[r], pj[r], subpix, minf, &si, &sj, &pv[r], &flags);
         const REAL half = (REAL)(d / 2);
         orc_vector *o = &out[r];
         o->u = (float)(si - half);

@@ -32,6 +32,16 @@ typedef struct {
     int iterate_until_no_corrections;
 } orc_valid_cfg;
 
+/* Sub-pixel interpolators of qlpiv_oracle_subpix.c.  A pass's `subpix` argument packs the mode
+ * (bits 0-7: 0 none, 1 Gaussian 3-point, 2 Gaussian least squares, 3 Hongwei Guo), the stencil
+ * pixels (bits 8-15) and the Hongwei Guo iterations (bits 16-23). */
+int orc_gauss_lm_fit(const double *x, const double *y, int n, double *mean_out);
+int orc_hongwei_guo_fit(const float *xs, const float *ys, int n, int iterations, float *mean, float *amplitude);
+void orc_subpixel_lm(const float *plane, int d, int mi, int mj, int P, float min_floor, float *si, float *sj,
+                     uint32_t *flags);
+void orc_subpixel_hg(const float *plane, int d, int mi, int mj, int P, int iterations, float min_floor, float *si,
+                     float *sj, float *pv, uint32_t *flags);
+
 int orc_grid_superposition(int h, int w, int mtop, int mbottom, int mleft, int mright, int n_start, int level,
                            float overlap_factor, orc_grid *g, int *tops, int *lefts, int cap);
 int orc_piv_pass(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,

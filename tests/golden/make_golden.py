@@ -20,6 +20,11 @@ Fixtures written (all from files shipped in the reference project):
                        (Liu-Shen images, Java LK input, fixed terms, 5 passes)
   filter_golden.npz    testFiles/GaussianFilter2D_*.matFloat (Gaussian prefilter
                        outputs) cropped to a 96x96 window.
+  gauss_kat.npz        the known-answer cases of tests/pt/quickLabPIV/interpolators/
+                       Gaussian1DInterpolatorAdvanced{3,5,7}Pixels{Symmetric,Assymmetric,HongWeiGuo}
+                       Test.java: per case the window side, the interpolator (0 Gaussian1D least
+                       squares, 1 Hongwei Guo with 20 iterations), the centre (uX, uY) and widths
+                       (sigmaX, sigmaY) of the analytic peak and the tolerance (8e-3 px).
 """
 import struct
 import sys
@@ -154,6 +159,37 @@ def read_png_gray(path):
     return out[:, ::ch].copy()
 
 
+def gauss_kat_cases(ref):
+    """(dim, kind, uX, uY, sigmaX, sigmaY, tol) of every @Test of the Gaussian 1D KAT files."""
+    import re
+    rows = []
+    d = Path(ref) / "tests/pt/quickLabPIV/interpolators"
+
+    def fexpr(e):
+        # Java float literal expressions of the tests: a, +a, -a, a*b, a/b (float arithmetic)
+        m = re.fullmatch(r"([+-]?[0-9.]+)f(?:([*/])([0-9.]+)f)?", e.strip())
+        a = np.float32(float(m.group(1)))
+        if m.group(2) == "*":
+            a = np.float32(a * np.float32(float(m.group(3))))
+        elif m.group(2) == "/":
+            a = np.float32(a / np.float32(float(m.group(3))))
+        return float(a)
+
+    for f in sorted(d.glob("Gaussian1DInterpolatorAdvanced*Test.java")):
+        text = f.read_text()
+        dim = int(re.search(r"int DIM = (\d+);", text).group(1))
+        kind = 1 if "HongWeiGuo" in f.name else 0
+        for body in text.split("@Test")[1:]:
+            vals = {k: fexpr(re.search(rf"float {k} = ([^;]+);", body).group(1))
+                    for k in ("uX", "uY", "sigmaX", "sigmaY")}
+            assert "createMatrixWithGaussian2DAssymmetric(DIM, DIM, uX, sigmaX, uY, sigmaY)" in body
+            assert ("setupPIVContextHongWeiGuo1D" in body) == (kind == 1)
+            tols = re.findall(r"getMainPeak[IJ]\(\), ([0-9.e-]+)f\);", body)
+            assert len(tols) == 2 and tols[0] == tols[1]
+            rows.append((dim, kind, vals["uX"], vals["uY"], vals["sigmaX"], vals["sigmaY"], float(tols[0])))
+    return np.array(rows, dtype=np.float64)
+
+
 def main(ref):
     ref = Path(ref)
     a = read_tiff_gray(ref / "resources/fftBenchmark/rankine_vortex01_0.tif")
@@ -203,9 +239,13 @@ def main(ref):
               [f"vnews{k}" for k in range(5)]
     np.savez_compressed(HERE / "dense_golden.npz", **{f"lk_{k}": lk[k] for k in keep_lk},
                         **{f"ls_{k}": ls[k] for k in keep_ls})
+    np.savez_compressed(HERE / "gauss_kat.npz", cases=gauss_kat_cases(ref))
     print("shapes:", a.shape, b.shape, i1.shape, i2.shape, [m.shape for m in fm1], [m.shape for m in fm2],
           fn1, fn2, src0.shape, len(keep_lk), len(keep_ls))
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 2 and sys.argv[2] == "--gauss-kat-only":
+        np.savez_compressed(HERE / "gauss_kat.npz", cases=gauss_kat_cases(sys.argv[1]))
+        sys.exit(0)
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
