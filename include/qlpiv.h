@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define QLPIV_ABI_VERSION 1
+#define QLPIV_ABI_VERSION 2
 
 /* Status codes.  The Java shim maps QLPIV_E_SHAPE/QLPIV_E_ARG to JobAnalyzeException
  * (S/jobs/xcorr/CrossCorrelationFFTTemplate.java:594-642 shape checks) and the others
@@ -61,8 +61,17 @@ typedef enum {
 
 typedef enum {
     QLPIV_SUBPIX_NONE = 0,
-    QLPIV_SUBPIX_GAUSS3 = 1 /* Gaussian1DPolynomialInterpolator (3-point, 1D-1D) */
+    QLPIV_SUBPIX_GAUSS3 = 1,      /* Gaussian1DPolynomialInterpolator (3-point, 1D-1D) */
+    QLPIV_SUBPIX_GAUSS_LM = 2,    /* Gaussian1DInterpolator: least-squares Gaussian through
+                                     subpix_pixels points per axis
+                                     (S/interpolators/Gaussian1DInterpolator.java:36-115) */
+    QLPIV_SUBPIX_HONGWEI_GUO = 3  /* Gaussian1DHongweiGuoInterpolator: y^2-weighted log fit,
+                                     subpix_iterations re-weightings
+                                     (S/interpolators/Gaussian1DHongweiGuoInterpolator.java:47-250) */
 } qlpiv_subpix;
+
+/* Stencil pixels of the P-point interpolators: odd, 3..QLPIV_MAX_SUBPIX_PIXELS. */
+#define QLPIV_MAX_SUBPIX_PIXELS 15
 
 /* qlpiv_vector.flags */
 #define QLPIV_F_SUB_I 1u     /* sub-pixel fit accepted along I (rows) */
@@ -71,6 +80,9 @@ typedef enum {
 #define QLPIV_F_EDGE 8u      /* 3-point stencil leaves the plane: integer peak kept */
 #define QLPIV_F_NO_PEAK 16u  /* no non-negative cell: peak left at (0,0) */
 #define QLPIV_F_ABSENT 32u   /* multi-peak slot beyond the peaks found (vector zeroed) */
+#define QLPIV_F_FLOOR 64u    /* min floor below the P-point interpolator's limit (-3.15 least
+                                squares, -5.15 Hongwei Guo; the reference throws
+                                InterpolateException): integer peak kept */
 
 /* FindMaximumMultiPeaks limits of this library: 1..QLPIV_MAX_PEAKS peaks per IA and a
  * cell width of at least 2 (the per-cell maxima of one IA are staged on chip). */
@@ -102,7 +114,9 @@ typedef struct qlpiv_pass_desc {
                            FindMaximumMultiPeaks (S/maximum/FindMaximumMultiPeaks.java:42-162),
                            k vectors per IA, largest peak first, every peak fitted */
     int peak_kernel;    /* FindMaximumMultiPeaks cell width (kernelWidth), >= 2 */
-    int reserved[4];
+    int subpix_pixels;  /* QLPIV_SUBPIX_GAUSS_LM / HONGWEI_GUO: stencil pixels (odd) */
+    int subpix_iterations; /* QLPIV_SUBPIX_HONGWEI_GUO: re-weightings, 6..50 */
+    int reserved[2];
 } qlpiv_pass_desc;
 
 /* One image pair of a batch.  Pixels are row-major with `pitch` elements per row; both
@@ -147,7 +161,9 @@ typedef struct qlpiv_adaptive_desc {
     float median_epsilon0;    /* NormalizedMedianValidator epsilon0 */
     int max_correction_iterations;      /* VectorValidatorConfiguration */
     int iterate_until_no_corrections;   /* VectorValidatorConfiguration */
-    int reserved[1];
+    int subpix_pixels;     /* as qlpiv_pass_desc */
+    int subpix_iterations; /* as qlpiv_pass_desc */
+    int reserved[3];
 } qlpiv_adaptive_desc;
 
 /* Vector validation after each level (VectorValidatorJob, S/jobs/validator/VectorValidatorJob.java:242-405). */

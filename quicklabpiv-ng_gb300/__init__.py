@@ -20,8 +20,9 @@ OK, E_ARG, E_SHAPE, E_OOM, E_CUDA, E_TIMEOUT, E_CANCELLED, E_UNSUPPORTED, E_NO_D
 PIX_U8, PIX_U16, PIX_F32 = 0, 1, 2
 NORM_MAX_A, NORM_OWN_MAX, NORM_NONE = 0, 1, 3
 MAX_COMPUTE, MAX_GIVEN, MAX_FIXED = 0, 1, 2
-SUBPIX_NONE, SUBPIX_GAUSS3 = 0, 1
-F_SUB_I, F_SUB_J, F_PARABOLIC, F_EDGE, F_NO_PEAK, F_ABSENT = 1, 2, 4, 8, 16, 32
+SUBPIX_NONE, SUBPIX_GAUSS3, SUBPIX_GAUSS_LM, SUBPIX_HONGWEI_GUO = 0, 1, 2, 3
+MAX_SUBPIX_PIXELS = 15
+F_SUB_I, F_SUB_J, F_PARABOLIC, F_EDGE, F_NO_PEAK, F_ABSENT, F_FLOOR = 1, 2, 4, 8, 16, 32, 64
 MAX_PEAKS = 16
 VALIDATE_NONE, VALIDATE_MULTIPEAK_MEDIAN = 0, 1
 
@@ -47,7 +48,8 @@ class QlpivError(RuntimeError):
 class PassDesc(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int), ("norm_mode", ctypes.c_int), ("max_mode", ctypes.c_int),
                 ("fixed_max_a", ctypes.c_float), ("fixed_max_b", ctypes.c_float), ("subpix_mode", ctypes.c_int),
-                ("num_peaks", ctypes.c_int), ("peak_kernel", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+                ("num_peaks", ctypes.c_int), ("peak_kernel", ctypes.c_int), ("subpix_pixels", ctypes.c_int),
+                ("subpix_iterations", ctypes.c_int), ("reserved", ctypes.c_int * 2)]
 
 
 class Frame(ctypes.Structure):
@@ -74,12 +76,13 @@ class AdaptiveDesc(ctypes.Structure):
                 ("int16_warp_quirk", ctypes.c_int), ("validation", ctypes.c_int), ("num_peaks", ctypes.c_int),
                 ("peak_kernel", ctypes.c_int), ("median_threshold", ctypes.c_float),
                 ("median_epsilon0", ctypes.c_float), ("max_correction_iterations", ctypes.c_int),
-                ("iterate_until_no_corrections", ctypes.c_int), ("reserved", ctypes.c_int * 1)]
+                ("iterate_until_no_corrections", ctypes.c_int), ("subpix_pixels", ctypes.c_int),
+                ("subpix_iterations", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_mode=WARP_BOTH_BILINEAR,
                   norm_mode=NORM_MAX_A, max_mode=MAX_FIXED, fixed_max=0.0, subpix_mode=SUBPIX_GAUSS3,
-                  int16_warp_quirk=False, validation=None):
+                  int16_warp_quirk=False, validation=None, subpix_pixels=3, subpix_iterations=20):
     """Adaptive PIV parameters; the defaults follow the reference's BothImages bilinear
     warping (tiles copied from the warped image keep the full-scale maximum).
     validation: None, or a dict for the multi-peak normalised-median model with keys
@@ -90,6 +93,7 @@ def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_m
     d.margins[:] = list(margins)
     d.warp_mode, d.norm_mode, d.max_mode, d.fixed_max = warp_mode, norm_mode, max_mode, fixed_max
     d.subpix_mode, d.int16_warp_quirk = subpix_mode, int(int16_warp_quirk)
+    d.subpix_pixels, d.subpix_iterations = subpix_pixels, subpix_iterations
     if validation is not None:
         set_validation(d, **validation)
     return d
@@ -233,7 +237,7 @@ def load_library(path=None):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.qlpiv_abi_version() != 1:
+    if lib.qlpiv_abi_version() != 2:
         raise RuntimeError("libqlpiv_gpu.so ABI version mismatch")
     if path is None:
         _lib = lib
@@ -424,14 +428,15 @@ class Handle:
     # -- frame API ---------------------------------------------------------------
     @staticmethod
     def desc(n, norm_mode=NORM_MAX_A, max_mode=MAX_COMPUTE, fixed_max=(255.0, 255.0), subpix_mode=SUBPIX_GAUSS3,
-             num_peaks=0, peak_kernel=3):
+             num_peaks=0, peak_kernel=3, subpix_pixels=3, subpix_iterations=20):
         """Pass descriptor; num_peaks > 0 selects FindMaximumMultiPeaks (num_peaks vectors
-        per IA)."""
+        per IA); subpix_pixels / subpix_iterations configure the P-point interpolators."""
         d = PassDesc()
         d.n, d.norm_mode, d.max_mode = n, norm_mode, max_mode
         d.fixed_max_a, d.fixed_max_b = fixed_max
         d.subpix_mode = subpix_mode
         d.num_peaks, d.peak_kernel = num_peaks, peak_kernel
+        d.subpix_pixels, d.subpix_iterations = subpix_pixels, subpix_iterations
         return d
 
     @staticmethod

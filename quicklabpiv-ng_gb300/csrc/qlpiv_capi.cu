@@ -39,6 +39,18 @@ qlpiv_status cuda_fail(cudaError_t e, const char *what) {
     return fail(QLPIV_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+qlpiv_status check_subpix(int mode, int pixels, int iterations) {
+    if (mode == QLPIV_SUBPIX_NONE || mode == QLPIV_SUBPIX_GAUSS3) return QLPIV_OK;
+    if (mode != QLPIV_SUBPIX_GAUSS_LM && mode != QLPIV_SUBPIX_HONGWEI_GUO)
+        return fail(QLPIV_E_ARG, "unknown sub-pixel mode %d", mode);
+    if (pixels < 3 || pixels > QLPIV_MAX_SUBPIX_PIXELS || pixels % 2 != 1)
+        return fail(QLPIV_E_ARG, "Number of interpolation pixels must be an odd number (3..%d), got %d",
+                    QLPIV_MAX_SUBPIX_PIXELS, pixels);
+    if (mode == QLPIV_SUBPIX_HONGWEI_GUO && (iterations < 6 || iterations > 50))
+        return fail(QLPIV_E_ARG, "Invalid number of interpolations: should be >= 6 and <= 50, got %d", iterations);
+    return QLPIV_OK;
+}
+
 }  // namespace qlpiv
 
 using qlpiv::cuda_fail;
@@ -59,8 +71,7 @@ qlpiv_status check_desc(const qlpiv_pass_desc *d) {
         return fail(QLPIV_E_ARG, "max mode %d not valid for a frame pass", d->max_mode);
     if (d->max_mode == QLPIV_MAX_FIXED && !(d->fixed_max_a > 0.0f && d->fixed_max_b > 0.0f))
         return fail(QLPIV_E_ARG, "fixed tile maxima must be positive");
-    if (d->subpix_mode != QLPIV_SUBPIX_NONE && d->subpix_mode != QLPIV_SUBPIX_GAUSS3)
-        return fail(QLPIV_E_ARG, "unknown sub-pixel mode %d", d->subpix_mode);
+    if (qlpiv_status st = qlpiv::check_subpix(d->subpix_mode, d->subpix_pixels, d->subpix_iterations)) return st;
     if (d->num_peaks != 0 && !qlpiv::multipeak_supported(d->n, d->num_peaks, d->peak_kernel))
         return fail(QLPIV_E_ARG, "multi-peak search: %d peaks with cell width %d not supported for IA %d "
                     "(1..%d peaks, cell width >= 2)", d->num_peaks, d->peak_kernel, d->n, QLPIV_MAX_PEAKS);
@@ -146,7 +157,7 @@ qlpiv_status tiles_call(qlpiv_handle *h, int n, long count, int pixel_type, cons
     job.count = count;
     job.norm_mode = norm_mode;
     job.max_mode = max_a ? QLPIV_MAX_GIVEN : QLPIV_MAX_COMPUTE;
-    job.subpix = subpix_mode == QLPIV_SUBPIX_GAUSS3;
+    job.subpix = subpix_mode;  // tile entry points: none or 3-point
     job.out = (qlpiv_vector *)h->vectors.p;
     job.planes = planes_out ? (float *)h->planes.p : nullptr;
     job.num_peaks = num_peaks;
@@ -184,7 +195,9 @@ qlpiv::IaJob frame_job(const qlpiv_pass_desc *desc, const void *img_a, const voi
     job.max_mode = desc->max_mode;
     job.fixed_max_a = desc->fixed_max_a;
     job.fixed_max_b = desc->fixed_max_b;
-    job.subpix = desc->subpix_mode == QLPIV_SUBPIX_GAUSS3;
+    job.subpix = desc->subpix_mode;
+    job.subpix_pixels = desc->subpix_mode >= QLPIV_SUBPIX_GAUSS_LM ? desc->subpix_pixels : 0;
+    job.subpix_iters = desc->subpix_iterations;
     job.out = out;
     job.planes = nullptr;
     job.num_peaks = desc->num_peaks;

@@ -28,6 +28,9 @@ qlpiv_status queue_adaptive_pinned(qlpiv_handle *h, const qlpiv_adaptive_desc *d
                                    float *out_v);
 void drop_plan(qlpiv_handle *h);
 
+// Sub-pixel mode settings (qlpiv_capi.cu): QLPIV_OK or QLPIV_E_ARG with the message set.
+qlpiv_status check_subpix(int mode, int pixels, int iterations);
+
 inline size_t pixel_bytes(int pixel_type) {
     return pixel_type == QLPIV_PIX_U8 ? 1 : (pixel_type == QLPIV_PIX_U16 ? 2 : 4);
 }

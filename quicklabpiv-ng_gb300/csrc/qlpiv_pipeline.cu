@@ -95,8 +95,7 @@ static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type,
         return fail(QLPIV_E_ARG, "unknown normalisation mode %d", d->norm_mode);
     if (d->max_mode != QLPIV_MAX_COMPUTE && d->max_mode != QLPIV_MAX_FIXED)
         return fail(QLPIV_E_ARG, "max mode %d not valid for adaptive PIV", d->max_mode);
-    if (d->subpix_mode != QLPIV_SUBPIX_NONE && d->subpix_mode != QLPIV_SUBPIX_GAUSS3)
-        return fail(QLPIV_E_ARG, "unknown sub-pixel mode %d", d->subpix_mode);
+    if (qlpiv_status st = check_subpix(d->subpix_mode, d->subpix_pixels, d->subpix_iterations)) return st;
     if (!(d->overlap_factor >= 0.1f && d->overlap_factor <= 0.9f))
         return fail(QLPIV_E_ARG, "Overlap factor must greater than 1/10 and less than 9/10");
     if (d->validation != QLPIV_VALIDATE_NONE && d->validation != QLPIV_VALIDATE_MULTIPEAK_MEDIAN)
@@ -352,7 +351,9 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
         job.norm_mode = d.norm_mode;
         job.max_mode = d.max_mode;
         job.fixed_max_a = job.fixed_max_b = fm;
-        job.subpix = d.subpix_mode == QLPIV_SUBPIX_GAUSS3;
+        job.subpix = d.subpix_mode;
+        job.subpix_pixels = d.subpix_mode >= QLPIV_SUBPIX_GAUSS_LM ? d.subpix_pixels : 0;
+        job.subpix_iters = d.subpix_iterations;
         job.acc_u = u;
         job.acc_v = v;
         const bool validate = d.validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN;

@@ -36,7 +36,9 @@ cudaError_t ensure_twiddles(int dev, const cplx **table) {
     return cudaSuccess;
 }
 
-template <int N, typename Pix>
+constexpr size_t kSubpixSmem = sizeof(float) * 32 * 2 * kMaxSubpixPixels;
+
+template <int N, typename Pix, bool PP>
 static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms) {
     using S = XcorrShape<N>;
     // The shared-memory opt-in is a per-device attribute of the function: set it once
@@ -51,10 +53,11 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
     {
         std::lock_guard<std::mutex> lock(mu);
         if (blocks_per_sm[dev] == 0) {
-            e = cudaFuncSetAttribute(xcorr_kernel<N, Pix>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+            e = cudaFuncSetAttribute(xcorr_kernel<N, Pix, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(S::SMEM + kSubpixSmem));
             if (e != cudaSuccess) return e;
             int b = 0;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, xcorr_kernel<N, Pix>, S::T, S::SMEM);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, xcorr_kernel<N, Pix, PP>, S::T, S::SMEM);
             if (e != cudaSuccess) return e;
             blocks_per_sm[dev] = b < 1 ? 1 : b;
         }
@@ -69,18 +72,26 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
     long grid = (long)num_sms * bps * (job.num_peaks > 0 ? 1 : 8);
     if (grid > job.count) grid = job.count;
     if (grid < 1) return cudaSuccess;
-    xcorr_kernel<N, Pix><<<(unsigned)grid, S::T, S::SMEM, stream>>>(j);
+    // P-point sub-pixel stencils: 2 P floats per queued fit after the fixed layout
+    const size_t smem = S::SMEM + (j.subpix_pixels > 0 ? sizeof(float) * 32 * 2 * j.subpix_pixels : 0);
+    xcorr_kernel<N, Pix, PP><<<(unsigned)grid, S::T, smem, stream>>>(j);
     return cudaGetLastError();
+}
+
+template <typename Pix, bool PP>
+static cudaError_t launch_pix(const IaJob &job, int n, cudaStream_t stream, int num_sms) {
+    switch (n) {
+        case 16: return launch_one<16, Pix, PP>(job, stream, num_sms);
+        case 32: return launch_one<32, Pix, PP>(job, stream, num_sms);
+        case 64: return launch_one<64, Pix, PP>(job, stream, num_sms);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 template <typename Pix>
 static cudaError_t launch_pix(const IaJob &job, int n, cudaStream_t stream, int num_sms) {
-    switch (n) {
-        case 16: return launch_one<16, Pix>(job, stream, num_sms);
-        case 32: return launch_one<32, Pix>(job, stream, num_sms);
-        case 64: return launch_one<64, Pix>(job, stream, num_sms);
-        default: return cudaErrorInvalidValue;
-    }
+    return job.subpix_pixels > 0 ? launch_pix<Pix, true>(job, n, stream, num_sms)
+                                 : launch_pix<Pix, false>(job, n, stream, num_sms);
 }
 
 cudaError_t launch_xcorr(const IaJob &job, int n, int pixel_type, cudaStream_t stream, int num_sms) {

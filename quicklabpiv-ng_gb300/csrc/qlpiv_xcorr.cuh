@@ -36,6 +36,7 @@
 #pragma once
 #include "qlpiv_fft.cuh"
 #include "qlpiv.h"
+#include "qlpiv_subpix.cuh"
 
 namespace qlpiv {
 
@@ -111,7 +112,8 @@ struct IaJob {
     const int *a_top, *a_left, *b_top, *b_left;  // per IA origins
     const float *max_a, *max_b;  // per IA maxima (max_mode == QLPIV_MAX_GIVEN)
     long count;
-    int norm_mode, max_mode, subpix;
+    int norm_mode, max_mode, subpix;  // subpix: qlpiv_subpix
+    int subpix_pixels, subpix_iters;  // P-point interpolators: stencil pixels, Hongwei Guo iterations
     float fixed_max_a, fixed_max_b;
     qlpiv_vector *out;           // optional per-IA vectors (num_peaks per IA in multi-peak mode)
     float *planes;               // optional (2N-1)^2 planes per IA
@@ -126,26 +128,70 @@ struct IaJob {
 // Integer peak and 3-point stencil of one IA, queued for the sub-pixel fit.
 struct FitRec {
     long ia;
-    int pi, pj, kind;   // kind: 0 fit, 1 no peak, 2 stencil off the plane, 3 no sub-pixel, 4 absent slot
+    int pi, pj, kind;   // kind: 0 fit, 1 no peak, 2 stencil off the plane, 3 no sub-pixel, 4 absent slot,
+                        //       5 floor below the interpolator's limit
     int slot, npk;      // multi-peak: peak index (0 = largest) and peaks found
     float pv, mn, c0, yu, yd, xl, xr;
 };
 static_assert(sizeof(FitRec) == 56, "fit queue sizing");
 
+// P-point interpolators on the stencils v (P values along I through the peak, then P along J):
+// sub-pixel position, flags and (Hongwei Guo) peak value.  Out of line: the fits' double-precision
+// working set stays out of K1's register allocation.
+static __device__ __noinline__ void fit_ppoint(int mode, int P, int iters, int pi, int pj, const float *v, float *si,
+                                        float *sj, float *pv, uint32_t *flags) {
+    const float *vi = v, *vj = v + P;
+    if (mode == QLPIV_SUBPIX_GAUSS_LM) {
+        double m;
+        if (sp_gauss_lm(vi, P, (double)pi, &m) && fabs(m - (double)pi) < 2.0) {
+            *si = (float)m;
+            *flags |= QLPIV_F_SUB_I;
+        }
+        if (sp_gauss_lm(vj, P, (double)pj, &m) && fabs(m - (double)pj) < 2.0) {
+            *sj = (float)m;
+            *flags |= QLPIV_F_SUB_J;
+        }
+        return;
+    }
+    float xs[kMaxSubpixPixels];
+    float ym, ya, xm, xa;
+    for (int k = 0; k < P; k++) xs[k] = (float)(pi - P / 2 + k);
+    sp_hongwei_guo(xs, vi, P, iters, &ym, &ya);
+    for (int k = 0; k < P; k++) xs[k] = (float)(pj - P / 2 + k);
+    sp_hongwei_guo(xs, vj, P, iters, &xm, &xa);
+    const bool yv = !(fabsf(__fsub_rn(ym, (float)pi)) > (float)P / 2.0f);
+    const bool xv = !(fabsf(__fsub_rn(xm, (float)pj)) > (float)P / 2.0f);
+    if (yv) { *si = ym; *flags |= QLPIV_F_SUB_I; }
+    if (xv) { *sj = xm; *flags |= QLPIV_F_SUB_J; }
+    if (yv) {
+        *pv = ya;
+        if (xv && xa > *pv) *pv = xa;
+    } else if (xv) {
+        *pv = xa;
+    }
+}
+
 // Gaussian1DPolynomialInterpolator.interpolate (S/interpolators/Gaussian1DPolynomialInterpolator.java:25-106)
 // for q[0..n): lane k handles record k, so the double logarithms of 32 IAs share one
 // warp instruction.  Called by one full warp.
-template <int D>
-__device__ void fit_flush(const FitRec *q, int n, int lane, const IaJob &job) {
+template <int D, bool PP>
+__device__ void fit_flush(const FitRec *q, const float *fitv, int n, int lane, const IaJob &job) {
     __syncwarp();
     if (lane < n) {
         const FitRec r = q[lane];
         float si = (float)r.pi, sj = (float)r.pj;
+        float pv = r.pv;
         uint32_t flags = 0;
         if (r.kind == 1) {
             flags |= QLPIV_F_NO_PEAK;
         } else if (r.kind == 2) {
             flags |= QLPIV_F_EDGE;
+        } else if (r.kind == 5) {
+            flags |= QLPIV_F_FLOOR;
+        } else if (PP && r.kind == 0 && job.subpix >= QLPIV_SUBPIX_GAUSS_LM) {
+            if constexpr (PP)
+                fit_ppoint(job.subpix, job.subpix_pixels, job.subpix_iters, r.pi, r.pj,
+                           fitv + lane * 2 * job.subpix_pixels, &si, &sj, &pv, &flags);
         } else if (r.kind == 0) {
             const bool neg = r.c0 < 0.0f || r.yu < 0.0f || r.yd < 0.0f || r.xl < 0.0f || r.xr < 0.0f;
             const float y0 = r.yu + 1e-8f, y1 = r.c0 + 1e-8f, y2 = r.yd + 1e-8f;
@@ -173,7 +219,7 @@ __device__ void fit_flush(const FitRec *q, int n, int lane, const IaJob &job) {
         o.v = sj - (float)(D / 2);
         o.sub_i = si;
         o.sub_j = sj;
-        o.peak_value = r.pv;
+        o.peak_value = pv;
         o.min_floor = r.mn;
         o.peak_i = (int16_t)r.pi;
         o.peak_j = (int16_t)r.pj;
@@ -497,10 +543,47 @@ __device__ __forceinline__ void mp_cells(const MpGeom &gm, const float *regf, fl
 // Step 5' of xcorr_kernel for one IA (kept out of line so that the single-peak path
 // keeps its register allocation): FindMaximumMultiPeaks over the plane in `regf`,
 // queueing `multi` fit records at fitq[qn..).  Called by every thread of the CTA.
+// Sub-pixel stencil of record r (peak r.pi, r.pj already set): the kind, and the stencil values
+// (3-point: in the record; P-point: 2P floats at fv, column then row, floor-lifted).
+template <int D, typename Plane>
+__device__ __forceinline__ void fit_stencil(FitRec &r, const IaJob &job, const Plane &P, float *fv) {
+    r.kind = 0;
+    if (!job.subpix) {
+        r.kind = 3;
+    } else if (r.pi == 0 && r.pj == 0) {
+        r.kind = 1;
+    } else if (job.subpix == QLPIV_SUBPIX_GAUSS3) {
+        if (r.pi - 1 < 0 || r.pi + 1 >= D || r.pj - 1 < 0 || r.pj + 1 >= D) {
+            r.kind = 2;
+        } else {
+            r.c0 = P(r.pi, r.pj);
+            r.yu = P(r.pi - 1, r.pj);
+            r.yd = P(r.pi + 1, r.pj);
+            r.xl = P(r.pi, r.pj - 1);
+            r.xr = P(r.pi, r.pj + 1);
+        }
+    } else {
+        const int h = job.subpix_pixels / 2;
+        const float lim = job.subpix == QLPIV_SUBPIX_GAUSS_LM ? -3.15f : -5.15f;
+        if (r.pi - h < 0 || r.pi + h >= D || r.pj - h < 0 || r.pj + h >= D) {
+            r.kind = 2;
+        } else if (r.mn < lim) {
+            r.kind = 5;  // the reference throws InterpolateException here
+        } else {
+            const float add = r.mn < 0.0f ? __fadd_rn(-r.mn, 1e-8f) : 0.0f;
+            const int Pn = job.subpix_pixels;
+            for (int k = 0; k < Pn; k++) {
+                fv[k] = __fadd_rn(P(r.pi - h + k, r.pj), add);
+                fv[Pn + k] = __fadd_rn(P(r.pi, r.pj - h + k), add);
+            }
+        }
+    }
+}
+
 template <int N>
 __device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float minf, const float *regf, cplx *scr,
-                                              uint64_t *red, FitRec *fitq, int qn, float *mp_lv, int *mp_li,
-                                              int *mp_lj) {
+                                              uint64_t *red, FitRec *fitq, float *fitv, int qn, float *mp_lv,
+                                              int *mp_li, int *mp_lj) {
     using S = XcorrShape<N>;
     constexpr int D = S::D, RP = S::RP, T = S::T, NWARPS = T / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -552,17 +635,7 @@ __device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float m
                 r.pi = mp_li[idx];
                 r.pj = mp_lj[idx];
                 r.pv = mp_lv[idx];
-                r.kind = 0;
-                if (!job.subpix) r.kind = 3;
-                else if (r.pi == 0 && r.pj == 0) r.kind = 1;
-                else if (r.pi - 1 < 0 || r.pi + 1 >= D || r.pj - 1 < 0 || r.pj + 1 >= D) r.kind = 2;
-                if (r.kind == 0) {
-                    r.c0 = P(r.pi, r.pj);
-                    r.yu = P(r.pi - 1, r.pj);
-                    r.yd = P(r.pi + 1, r.pj);
-                    r.xl = P(r.pi, r.pj - 1);
-                    r.xr = P(r.pi, r.pj + 1);
-                }
+                fit_stencil<D>(r, job, P, fitv + (qn + lane) * 2 * job.subpix_pixels);
             } else {
                 r.kind = 4;
             }
@@ -571,7 +644,9 @@ __device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float m
     }
 }
 
-template <int N, typename Pix>
+// PP: the P-point sub-pixel interpolators are compiled in (their out-of-line double-precision
+// fits cost the common instantiation registers even when unused).
+template <int N, typename Pix, bool PP>
 __global__ void __launch_bounds__(XcorrShape<N>::T, XcorrShape<N>::MIN_BLOCKS)
 xcorr_kernel(IaJob job) {
     using S = XcorrShape<N>;
@@ -585,6 +660,7 @@ xcorr_kernel(IaJob job) {
     float *mp_lv = reinterpret_cast<float *>(fitq + 32);           // multi-peak list (ascending)
     int *mp_li = reinterpret_cast<int *>(mp_lv + QLPIV_MAX_PEAKS + 1);
     int *mp_lj = mp_li + QLPIV_MAX_PEAKS + 1;
+    float *fitv = reinterpret_cast<float *>(mp_lj + QLPIV_MAX_PEAKS + 1);  // P-point stencils
     int qn = 0;                                                    // uniform across the CTA
     const int multi = job.num_peaks;                               // 0: FindMaximumFromCenter
     const int KQ = multi > 0 ? multi : 1;                          // fit records per IA
@@ -863,31 +939,21 @@ xcorr_kernel(IaJob job) {
                     }
                     r.slot = 0;
                     r.npk = 1;
-                    r.kind = 0;
-                    if (!job.subpix) r.kind = 3;
-                    else if (r.pi == 0 && r.pj == 0) r.kind = 1;
-                    else if (r.pi - 1 < 0 || r.pi + 1 >= D || r.pj - 1 < 0 || r.pj + 1 >= D) r.kind = 2;
-                    if (r.kind == 0) {
-                        r.c0 = P(r.pi, r.pj);
-                        r.yu = P(r.pi - 1, r.pj);
-                        r.yd = P(r.pi + 1, r.pj);
-                        r.xl = P(r.pi, r.pj - 1);
-                        r.xr = P(r.pi, r.pj + 1);
-                    }
+                    fit_stencil<D>(r, job, P, fitv + qn * 2 * job.subpix_pixels);
                     fitq[qn] = r;
                 }
             }
         } else {
-            multipeak_select<N>(job, ia, minf, regf, scr, red, fitq, qn, mp_lv, mp_li, mp_lj);
+            multipeak_select<N>(job, ia, minf, regf, scr, red, fitq, fitv, qn, mp_lv, mp_li, mp_lj);
         }
         qn += KQ;
         if (qn + KQ > 32) {
-            if (warp == 0) fit_flush<D>(fitq, qn, lane, job);
+            if (warp == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
             qn = 0;
         }
         __syncthreads();  // regions are rewritten by the next IA
     }
-    if (qn > 0 && warp == 0) fit_flush<D>(fitq, qn, lane, job);
+    if (qn > 0 && warp == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
 }
 
 }  // namespace qlpiv
