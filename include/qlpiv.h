@@ -138,7 +138,17 @@ typedef struct qlpiv_grid {
 
 typedef enum {
     QLPIV_WARP_NONE = 0,          /* NoImageWarping: B tiles at round(origin + displacement) */
-    QLPIV_WARP_BOTH_BILINEAR = 1  /* BothImagesBiLinearWarping (BiLinearImageWarpingStrategy) */
+    QLPIV_WARP_BOTH_BILINEAR = 1, /* BothImagesBiLinearWarping (BiLinearImageWarpingStrategy) */
+    /* BiLinearImageMicroAndMiniWarpingStrategy (S/images/BiLinearImageMicroAndMiniWarpingStrategy.java):
+     * every tile warped on its own; micro: by its fractional displacement, mini: by a bicubic
+     * spline over its up to 7 x 7 neighbour tiles.  Warped tiles keep the full-scale maximum,
+     * clipped ones their own; level 0 clips both tiles. */
+    QLPIV_WARP_FIRST_MICRO = 4,
+    QLPIV_WARP_SECOND_MICRO = 5,
+    QLPIV_WARP_BOTH_MICRO = 6,
+    QLPIV_WARP_FIRST_MINI = 7,
+    QLPIV_WARP_SECOND_MINI = 8,
+    QLPIV_WARP_BOTH_MINI = 9
 } qlpiv_warp_mode;
 
 /* Adaptive multi-pass PIV parameters (PIVInputParameters fields of the path). */
@@ -295,6 +305,17 @@ qlpiv_status qlpiv_displacement_field(qlpiv_handle *h, int height, int width, in
 qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, const void *img_a, const void *img_b, int height,
                              int width, int ni, int nj, const double *ci, const double *cj, const float *u,
                              const float *v, int int16_quirk, void *out_a, void *out_b);
+
+/* Micro / mini per-tile warping of one pair's tiles (BiLinearImageMicroAndMiniWarpingStrategy
+ * .warpAndClipImage, S/images/BiLinearImageMicroAndMiniWarpingStrategy.java:39-407): grid rows
+ * tops[ni], columns lefts[nj], side n, tile displacements u / v (ni x nj, rows / columns);
+ * warp_mode one of QLPIV_WARP_{FIRST,SECOND,BOTH}_{MICRO,MINI}.  tiles_a / tiles_b receive
+ * ni x nj x n x n pixels of the image type, max_a / max_b the tiles' maxima (warped: full_max,
+ * clipped: own, floor 16).  Host arrays. */
+qlpiv_status qlpiv_tile_warp(qlpiv_handle *h, int pixel_type, const void *img_a, const void *img_b, int height,
+                             int width, int n, int ni, int nj, const int32_t *tops, const int32_t *lefts,
+                             const float *u, const float *v, int warp_mode, float full_max, void *tiles_a,
+                             void *tiles_b, float *max_a, float *max_b);
 
 /* Whole adaptive PIV of num_pairs image pairs of one size (LocalPIVOpenCLGpuJob's level
  * loop, S/jobs/LocalPIVOpenCLGpuJob.java:188-411, SimpleStrategy): per level grid ->

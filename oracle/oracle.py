@@ -83,6 +83,8 @@ def lib():
         L.orc_piv_pass.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_long, ip, ip, ip, ip, c_int,
                                    c_float, c_float, c_int, c_int, vp, c_int]
         L.orc_displacement_field.argtypes = [dp, c_int, dp, c_int, fp, fp, c_int, c_int, c_int, fp, fp]
+        L.orc_tile_warp.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_int, ip, ip, fp, fp, c_int, c_int,
+                                    c_float, vp, vp, vp, vp]
         L.orc_displacement_field_off.argtypes = [dp, c_int, dp, c_int, fp, fp, c_int, c_int, c_int, c_float, c_float,
                                                  fp, fp]
         L.orc_warp_both.argtypes = [vp, vp, c_int, c_int, c_int, fp, fp, c_int, vp, vp]
@@ -284,6 +286,28 @@ def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+WARP_FIRST_MICRO, WARP_SECOND_MICRO, WARP_BOTH_MICRO, WARP_FIRST_MINI, WARP_SECOND_MINI, WARP_BOTH_MINI = range(4, 10)
+
+
+def tile_warp(img_a, img_b, n, tops, lefts, u, v, warp_mode, full_max):
+    """Micro / mini per-tile warping: (tiles_a, tiles_b, max_a, max_b), float tiles."""
+    img_a, img_b = np.ascontiguousarray(img_a), np.ascontiguousarray(img_b)
+    tops = np.ascontiguousarray(tops, np.int32)
+    lefts = np.ascontiguousarray(lefts, np.int32)
+    u, v = _f32(u), _f32(v)
+    cnt = len(tops) * len(lefts)
+    ta = np.zeros((cnt, n, n), np.float32)
+    tb = np.zeros_like(ta)
+    ma = np.zeros(cnt, np.float32)
+    mb = np.zeros(cnt, np.float32)
+    lib().orc_tile_warp(img_a.ctypes.data, img_b.ctypes.data, img_a.shape[0], img_a.shape[1], img_a.dtype.itemsize, n,
+                        len(tops), len(lefts), _ptr(tops, ctypes.c_int), _ptr(lefts, ctypes.c_int),
+                        _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), (warp_mode - 4) % 3 + 1,
+                        int(warp_mode >= 7), float(full_max), ta.ctypes.data, tb.ctypes.data, ma.ctypes.data,
+                        mb.ctypes.data)
+    return ta, tb, ma, mb
+
+
 def displacement_field(ys, xs, u, v, h, w, precision=32, offset=0.0):
     """Per-pixel (u, v) from tile displacements at tile centres (bicubic spline), evaluated
     in float (precision=32, the CUDA formulation) or double, pixel (i, j) at (i, j) + offset."""
@@ -322,7 +346,8 @@ def inherit(py, px, pu, pv, cy, cx, round_int=False, precision=32):
 
 def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MAX_A, fixed_max=None,
                  int16_quirk=False, precision=32, nthreads=None, return_levels=False, warp=True, validation=None):
-    """Adaptive multi-pass PIV (BothImages bilinear warping, or none); returns (u, v) of
+    """Adaptive multi-pass PIV (warp: False none, True BothImages bilinear, or a micro / mini mode
+    4..9 as WARP_*); returns (u, v) of
     the last level, shaped (tiles_i, tiles_j), and optionally all levels' vectors.
     validation: a ValidCfg (multi-peak finder + normalised-median validation per level);
     with return_levels the result also carries every level's validated (u, v) and

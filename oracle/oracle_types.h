@@ -42,6 +42,13 @@ void orc_subpixel_lm(const float *plane, int d, int mi, int mj, int P, float min
 void orc_subpixel_hg(const float *plane, int d, int mi, int mj, int P, int iterations, float min_floor, float *si,
                      float *sj, float *pv, uint32_t *flags);
 
+int orc_tiles_pass(const float *tiles_a, const float *tiles_b, const float *max_a, const float *max_b, long count,
+                   int n, int norm_mode, int subpix, int precision, int kw, int k, orc_vector *out, int *npeaks);
+void orc_tile_warp(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, int ni, int nj,
+                   const int *tops, const int *lefts, const float *cu, const float *cv, int image_mode, int mini,
+                   float full_max, float *tiles_a, float *tiles_b, float *max_a, float *max_b);
+float orc_clip_tile(const void *img, int h, int w, int pix_bytes, int top, int left, int n, float *tile);
+
 int orc_grid_superposition(int h, int w, int mtop, int mbottom, int mleft, int mright, int n_start, int level,
                            float overlap_factor, orc_grid *g, int *tops, int *lefts, int cap);
 int orc_piv_pass(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,

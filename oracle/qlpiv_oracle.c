@@ -331,4 +331,33 @@ int orc_mp_list_run(int max_size, int kernel_width, int count, const float *v, c
     return size;
 }
 
+/* One pass over ready tiles (count x n x n floats) with given per-tile maxima: the CPU path from
+ * the correlation on.  norm_mode as orc_piv_pass (0: both by A's max, 1: own, 3: raw); k > 0:
+ * FindMaximumMultiPeaks with k peaks (out holds k vectors per tile, npeaks the peaks found). */
+int orc_tiles_pass(const float *tiles_a, const float *tiles_b, const float *max_a, const float *max_b, long count,
+                   int n, int norm_mode, int subpix, int precision, int kw, int k, orc_vector *out, int *npeaks) {
+    const int d = 2 * n - 1;
+    void *plane = malloc(sizeof(double) * d * d);
+    for (long q = 0; q < count; q++) {
+        const float *ta = tiles_a + q * n * n, *tb = tiles_b + q * n * n;
+        float maxA = max_a[q], maxB = max_b[q];
+        int normalize = 1;
+        if (norm_mode == 0) maxB = maxA;
+        else if (norm_mode != 1) normalize = 0;
+        if (k > 0) {
+            orc_vector *o = out + q * k;
+            const int np = precision == 0
+                ? ia_vectors_multi_f32(ta, tb, n, maxA, maxB, normalize, subpix, kw, k, o, (float *)plane)
+                : ia_vectors_multi_f64(ta, tb, n, maxA, maxB, normalize, subpix, kw, k, o, (double *)plane);
+            if (npeaks) npeaks[q] = np;
+        } else if (precision == 0) {
+            ia_vector_f32(ta, tb, n, maxA, maxB, normalize, subpix, &out[q], (float *)plane);
+        } else {
+            ia_vector_f64(ta, tb, n, maxA, maxB, normalize, subpix, &out[q], (double *)plane);
+        }
+    }
+    free(plane);
+    return 0;
+}
+
 int orc_vector_size(void) { return (int)sizeof(orc_vector); }

@@ -209,6 +209,115 @@ void orc_warp_both(const void *img_a, const void *img_b, int h, int w, int pix_b
         }
 }
 
+/* Micro / mini per-tile warping (BiLinearImageMicroAndMiniWarpingStrategy.warpAndClipImage,
+ * S/images/BiLinearImageMicroAndMiniWarpingStrategy.java:39-186, createMicroDisplacements :188-202,
+ * createMiniDisplacements :204-290, doBiLinearWarp :292-336, warpPixelOnImage :338-407) of the
+ * tiles of one level (grid tops[ni] x lefts[nj], side n, tile displacements cu/cv row-major).
+ * image_mode: 1 first image, 2 second image, 3 both; mini: 0 micro (the tile's fractional
+ * displacement everywhere), 1 mini (bicubic spline over the tile's up to 7 x 7 neighbours, values
+ * relative to floor of the tile's displacement, evaluated over the tile region of the displaced B
+ * tile).  Warped tiles keep the full-scale maximum `full_max`; clipped tiles their own maximum
+ * (floor 16).  Outputs: count x n x n float tiles and per-tile maxima. */
+static void mini_field(const int *tops, const int *lefts, int ni, int nj, int n, const float *cu, const float *cv,
+                       int ti, int tj, int eval_top, int eval_left, float *fu, float *fv) {
+    const int R = 7, r2 = R / 2;
+    const int i0 = ti - r2 < 0 ? 0 : ti - r2, i1 = ti + r2 > ni - 1 ? ni - 1 : ti + r2;
+    const int j0 = tj - r2 < 0 ? 0 : tj - r2, j1 = tj + r2 > nj - 1 ? nj - 1 : tj + r2;
+    const int di = i1 - i0 + 1, dj = j1 - j0 + 1;
+    double ys[7], xs[7];
+    float us[49], vs[49];
+    const long kc = (long)ti * nj + tj;
+    const double fu0 = floor((double)cu[kc]), fv0 = floor((double)cv[kc]);
+    for (int i = 0; i < di; i++) ys[i] = (double)((float)tops[i0 + i] + (float)n / 2.0f - 0.5f);
+    for (int j = 0; j < dj; j++) xs[j] = (double)((float)lefts[j0 + j] + (float)n / 2.0f - 0.5f);
+    for (int i = 0; i < di; i++)
+        for (int j = 0; j < dj; j++) {
+            const long k = (long)(i0 + i) * nj + (j0 + j);
+            us[i * dj + j] = (float)((double)cu[k] - fu0);
+            vs[i * dj + j] = (float)((double)cv[k] - fv0);
+        }
+    orc_displacement_field_off(ys, di, xs, dj, us, vs, n, n, 0, (float)eval_top, (float)eval_left, fu, fv);
+}
+
+void orc_tile_warp(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, int ni, int nj,
+                   const int *tops, const int *lefts, const float *cu, const float *cv, int image_mode, int mini,
+                   float full_max, float *tiles_a, float *tiles_b, float *max_a, float *max_b) {
+    float *fu = (float *)malloc(sizeof(float) * n * n), *fv = (float *)malloc(sizeof(float) * n * n);
+    for (int ti = 0; ti < ni; ti++)
+        for (int tj = 0; tj < nj; tj++) {
+            const long k = (long)ti * nj + tj;
+            float *ta = tiles_a + k * n * n, *tb = tiles_b + k * n * n;
+            const int top = tops[ti], left = lefts[tj];
+            const float du = cu[k], dv = cv[k];
+            const double flu = floor((double)du), flv = floor((double)dv);
+            const double flu2 = floor((double)(du / 2.0f)), flv2 = floor((double)(dv / 2.0f));
+            const int topRefB = (int)(short)((double)top + flu), leftRefB = (int)(short)((double)left + flv);
+            /* the pixel displacements of the tile region */
+            if (mini) {
+                mini_field(tops, lefts, ni, nj, n, cu, cv, ti, tj, topRefB, leftRefB, fu, fv);
+            } else {
+                const float mu = du - (float)flu, mv = dv - (float)flv;
+                for (int q = 0; q < n * n; q++) { fu[q] = mu; fv[q] = mv; }
+            }
+            /* image A */
+            if (image_mode == 2) {
+                max_a[k] = orc_clip_tile(img_a, h, w, pix_bytes, top, left, n, ta);
+            } else {
+                int topA, leftA;
+                float uo = 0.0f, vo = 0.0f;
+                if (image_mode == 1) {
+                    topA = (int)(short)((double)top - flu);
+                    leftA = (int)(short)((double)left - flv);
+                } else {
+                    topA = (int)(short)((double)top - flu2);
+                    leftA = (int)(short)((double)left - flv2);
+                    uo = (float)((double)(du / 2.0f) - flu2) - (float)((double)du - flu);
+                    vo = (float)((double)(dv / 2.0f) - flv2) - (float)((double)dv - flv);
+                }
+                for (int i = 0; i < n; i++)
+                    for (int j = 0; j < n; j++) {
+                        float u = fu[i * n + j], v = fv[i * n + j];
+                        if (image_mode == 3) {
+                            u = u / 2.0f + uo;
+                            v = v / 2.0f + vo;
+                        }
+                        ta[i * n + j] = warp_pixel(img_a, pix_bytes, h, w, u, v, (int)(short)(i + topA),
+                                                   (int)(short)(j + leftA), 1);
+                    }
+                max_a[k] = full_max;
+            }
+            /* image B */
+            if (image_mode == 1) {
+                max_b[k] = orc_clip_tile(img_b, h, w, pix_bytes, top, left, n, tb);
+            } else {
+                int topB, leftB;
+                float uo = 0.0f, vo = 0.0f;
+                if (image_mode == 2) {
+                    topB = topRefB;
+                    leftB = leftRefB;
+                } else {
+                    topB = (int)(short)((double)top + flu2);
+                    leftB = (int)(short)((double)left + flv2);
+                    uo = (float)((double)(du / 2.0f) - flu2);
+                    vo = (float)((double)(dv / 2.0f) - flv2);
+                }
+                for (int i = 0; i < n; i++)
+                    for (int j = 0; j < n; j++) {
+                        float u = fu[i * n + j], v = fv[i * n + j];
+                        if (image_mode == 3) {
+                            u = u / 2.0f + uo;
+                            v = v / 2.0f + vo;
+                        }
+                        tb[i * n + j] = warp_pixel(img_b, pix_bytes, h, w, u, v, (int)(short)(i + topB),
+                                                   (int)(short)(j + leftB), 0);
+                    }
+                max_b[k] = full_max;
+            }
+        }
+    free(fu);
+    free(fv);
+}
+
 /* Inherited displacement of child tiles at centres (cy[ci], cx[cj]) from parent tiles
  * (pu, pv at centres py[pi], px[pj]), clamped to the parent box; needs >= 5 parent
  * tiles per axis, otherwise nothing is inherited (the reference computes a bilinear
@@ -290,12 +399,25 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
         for (int i = 0; i < ni; i++) { cyf[i] = (float)tops[i] + (float)n / 2.0f - 0.5f; cyd[i] = cyf[i]; }
         for (int j = 0; j < nj; j++) { cxf[j] = (float)lefts[j] + (float)n / 2.0f - 0.5f; cxd[j] = cxf[j]; }
         const void *sa = img_a, *sb = img_b;
+        /* warp_mode: 0 none, 1 BothImages full-image bilinear, 4/5/6 First/Second/Both micro,
+         * 7/8/9 First/Second/Both mini */
+        const int per_tile = warp_mode >= 4 && warp_mode <= 9;
+        float *wta = NULL, *wtb = NULL, *wma = NULL, *wmb = NULL;
         if (lv > 0) {
             double *pyd = (double *)malloc(sizeof(double) * pni), *pxd = (double *)malloc(sizeof(double) * pnj);
             for (int i = 0; i < pni; i++) pyd[i] = (double)((float)ptops[i] + (float)pn / 2.0f - 0.5f);
             for (int j = 0; j < pnj; j++) pxd[j] = (double)((float)plefts[j] + (float)pn / 2.0f - 0.5f);
             orc_inherit(pyd, pni, pxd, pnj, pu, pv, cyf, ni, cxf, nj, warp_mode == 0, precision, cu, cv);
             free(pyd); free(pxd);
+            if (per_tile) {
+                wta = (float *)malloc(sizeof(float) * cnt * n * n);
+                wtb = (float *)malloc(sizeof(float) * cnt * n * n);
+                wma = (float *)malloc(sizeof(float) * cnt);
+                wmb = (float *)malloc(sizeof(float) * cnt);
+                const float full = fixed_max > 0.0f ? fixed_max : (pix_bytes == 1 ? 255.0f : 65535.0f);
+                orc_tile_warp(img_a, img_b, h, w, pix_bytes, n, ni, nj, tops, lefts, cu, cv, (warp_mode - 4) % 3 + 1,
+                              warp_mode >= 7, full, wta, wtb, wma, wmb);
+            }
             if (warp_mode == 1) {
                 orc_displacement_field(cyd, ni, cxd, nj, cu, cv, h, w, precision, fu, fv);
                 orc_warp_both(img_a, img_b, h, w, pix_bytes, fu, fv, int16_quirk, wa, wb);
@@ -313,8 +435,8 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
                 bt[k] = warp_mode == 0 ? java_round((float)tops[i] + cu[k]) : tops[i];
                 bl[k] = warp_mode == 0 ? java_round((float)lefts[j] + cv[k]) : lefts[j];
             }
-        const float fm = fixed_max > 0.0f ? fixed_max : 0.0f;
-        const int nm = fixed_max > 0.0f ? 2 : norm_mode;
+        const float fm = fixed_max > 0.0f && !per_tile ? fixed_max : 0.0f;
+        const int nm = fixed_max > 0.0f && !per_tile ? 2 : norm_mode;
         orc_vector *vec = (orc_vector *)malloc(sizeof(orc_vector) * cnt);
         orc_vector *mvec = NULL;
         int *npk = NULL;
@@ -322,12 +444,18 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
             /* FindMaximumMultiPeaks (the finder the multi-peak validation model selects) */
             mvec = (orc_vector *)malloc(sizeof(orc_vector) * cnt * kpk);
             npk = (int *)malloc(sizeof(int) * cnt);
-            orc_piv_pass_multi(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, nm, fm, fm, 1, precision,
-                               val->kernel_width, kpk, mvec, npk, nthreads);
+            if (wta)
+                orc_tiles_pass(wta, wtb, wma, wmb, cnt, n, norm_mode, 1, precision, val->kernel_width, kpk, mvec, npk);
+            else
+                orc_piv_pass_multi(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, nm, fm, fm, 1, precision,
+                                   val->kernel_width, kpk, mvec, npk, nthreads);
             for (long k = 0; k < cnt; k++) vec[k] = mvec[k * kpk];
+        } else if (wta) {
+            orc_tiles_pass(wta, wtb, wma, wmb, cnt, n, norm_mode, 1, precision, 0, 0, vec, NULL);
         } else {
             orc_piv_pass(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, nm, fm, fm, 1, precision, vec, nthreads);
         }
+        free(wta); free(wtb); free(wma); free(wmb);
         if (level_vectors) memcpy(level_vectors + vec_off, vec, sizeof(orc_vector) * cnt);
         for (long k = 0; k < cnt; k++) {
             if (precision == 0) { cu[k] += vec[k].u; cv[k] += vec[k].v; }

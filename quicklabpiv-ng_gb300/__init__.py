@@ -67,6 +67,7 @@ class Grid(ctypes.Structure):
 
 
 WARP_NONE, WARP_BOTH_BILINEAR = 0, 1
+WARP_FIRST_MICRO, WARP_SECOND_MICRO, WARP_BOTH_MICRO, WARP_FIRST_MINI, WARP_SECOND_MINI, WARP_BOTH_MINI = range(4, 10)
 
 
 class AdaptiveDesc(ctypes.Structure):
@@ -197,6 +198,7 @@ _SIGNATURES = {
     "qlpiv_inherit": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp]),
     "qlpiv_displacement_field": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "qlpiv_warp_pair": (_i, [_vp, _i, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
+    "qlpiv_tile_warp": (_i, [_vp, _i, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _f, _vp, _vp, _vp, _vp]),
     "qlpiv_piv_adaptive": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
     "qlpiv_piv_adaptive_device": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
     "qlpiv_inherit_noalloc": (_i, [_i, _vp, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp]),
@@ -543,6 +545,26 @@ class Handle:
                                          ia.shape[1], len(ci), len(cj), _addr(ci), _addr(cj), _addr(u), _addr(v),
                                          int(int16_quirk), _addr(oa), _addr(ob)))
         return oa, ob
+
+    def tile_warp(self, img_a, img_b, n, tops, lefts, u, v, warp_mode, full_max):
+        """Micro / mini per-tile warping of one pair: (tiles_a, tiles_b, max_a, max_b), tiles
+        shaped (len(tops) * len(lefts), n, n) in the image's dtype."""
+        ia = np.ascontiguousarray(img_a)
+        ib = np.ascontiguousarray(img_b, ia.dtype)
+        tops = np.ascontiguousarray(tops, np.int32)
+        lefts = np.ascontiguousarray(lefts, np.int32)
+        u = np.ascontiguousarray(u, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        cnt = len(tops) * len(lefts)
+        ta = np.empty((cnt, n, n), ia.dtype)
+        tb = np.empty_like(ta)
+        ma = np.empty(cnt, np.float32)
+        mb = np.empty(cnt, np.float32)
+        _check(self._lib.qlpiv_tile_warp(self._h, pixel_type_of(ia.dtype), _addr(ia), _addr(ib), ia.shape[0],
+                                         ia.shape[1], n, len(tops), len(lefts), _addr(tops), _addr(lefts), _addr(u),
+                                         _addr(v), int(warp_mode), float(full_max), _addr(ta), _addr(tb), _addr(ma),
+                                         _addr(mb)))
+        return ta, tb, ma, mb
 
     def validate(self, tops, lefts, u, v, peak_u, peak_v, npeaks, desc):
         """Multi-peak normalised-median validation of one frame's tiles (host arrays):

@@ -278,12 +278,15 @@ __global__ void spline_cross_kernel(int pairs, const double *ys, int ni, const d
 // ---------------- B-field evaluation + B-warp ----------------
 
 template <typename Pix>
-__host__ __device__ __forceinline__ float warp_read(const Pix *img, int w, int y, int x) {
-    return (float)img[(long)y * w + x];
+__host__ __device__ __forceinline__ float warp_read(const Pix *img, long pitch, int y, int x) {
+    return (float)img[(long)y * pitch + x];
 }
 
+// warpPixelOnImage (S/images/BiLinearImageWarpingStrategy.java:185-265) on an h x w image with
+// `pitch` elements per row.
 template <typename Pix>
-__host__ __device__ float warp_pixel(const Pix *img, int h, int w, float u, float v, int i, int j, bool first) {
+__host__ __device__ float warp_pixel(const Pix *img, int h, int w, long pitch, float u, float v, int i, int j,
+                                     bool first) {
     float sI = first ? (float)i - u : (float)i + u;
     float sJ = first ? (float)j - v : (float)j + v;
     int pI = (int)(short)java_round(sI), pJ = (int)(short)java_round(sJ);
@@ -296,10 +299,10 @@ __host__ __device__ float warp_pixel(const Pix *img, int h, int w, float u, floa
     if (oI + pI < 0 || oI + pI >= h) oI = 0;
     if (oJ + pJ < 0 || oJ + pJ >= w) oJ = 0;
     const float wU = fabsf(dU), wV = fabsf(dV);
-    const float tl = warp_read(img, w, pI, pJ);
-    const float tr = warp_read(img, w, pI, pJ + oJ);
-    const float bl = warp_read(img, w, pI + oI, pJ);
-    const float br = warp_read(img, w, pI + oI, pJ + oJ);
+    const float tl = warp_read(img, pitch, pI, pJ);
+    const float tr = warp_read(img, pitch, pI, pJ + oJ);
+    const float bl = warp_read(img, pitch, pI + oI, pJ);
+    const float br = warp_read(img, pitch, pI + oI, pJ + oJ);
     const float a = (1.0f - wU) * (1.0f - wV) * tl;
     const float b = (1.0f - wU) * wV * tr;
     const float c = wU * (1.0f - wV) * bl;
@@ -360,8 +363,8 @@ __host__ __device__ __forceinline__ void warp_one(int pair, int i, int j, const 
     const Pix *ib = reinterpret_cast<const Pix *>(fs.img_b);
     Pix *oa = reinterpret_cast<Pix *>(const_cast<void *>(fd.img_a));
     Pix *ob = reinterpret_cast<Pix *>(const_cast<void *>(fd.img_b));
-    oa[(long)i * fd.pitch + j] = warp_store<Pix>(warp_pixel(ia, h, w, hu, hv, i, j, true), int16_quirk);
-    ob[(long)i * fd.pitch + j] = warp_store<Pix>(warp_pixel(ib, h, w, hu, hv, i, j, false), int16_quirk);
+    oa[(long)i * fd.pitch + j] = warp_store<Pix>(warp_pixel(ia, h, w, fs.pitch, hu, hv, i, j, true), int16_quirk);
+    ob[(long)i * fd.pitch + j] = warp_store<Pix>(warp_pixel(ib, h, w, fs.pitch, hu, hv, i, j, false), int16_quirk);
 }
 
 // One thread per pixel of one pair (blockIdx.z = pair).  src/dst frame tables hold the
@@ -373,6 +376,170 @@ __global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, 
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     warp_one<Pix>(blockIdx.z, i, j, src, dst, ys, ni, xs, nj, c4u, c4v, int16_quirk);
+}
+
+// ---------------- micro / mini per-tile warping ----------------
+// BiLinearImageMicroAndMiniWarpingStrategy.warpAndClipImage
+// (S/images/BiLinearImageMicroAndMiniWarpingStrategy.java:39-186): one CTA per tile of one pair.
+// The pixel displacements of the tile region are the tile's fractional displacement (micro) or a
+// bicubic spline over its up to 7 x 7 neighbour tiles, relative to floor of its displacement and
+// evaluated over the displaced B tile's region (mini, :204-290); the warped side(s) are sampled
+// with the full-image rule, the other side is clipped.  Tiles are written pair-major as
+// [pairs][tiles][n][n] pixels with their maxima (warped: full scale; clipped: own, floor 16).
+constexpr int kMiniR = 7;
+
+template <typename Pix>
+__global__ void __launch_bounds__(256) tile_warp_kernel(const qlpiv_frame *frames, int n, int ni, int nj,
+                                                        const int *tops, const int *lefts, const float *cu,
+                                                        const float *cv, int image_mode, int mini, float full_max,
+                                                        Pix *tiles_a, Pix *tiles_b, float *max_a, float *max_b) {
+    const long cnt = (long)ni * nj;
+    const int pair = blockIdx.y;
+    const long k = blockIdx.x;
+    const int ti = (int)(k / nj), tj = (int)(k - (long)ti * nj);
+    const qlpiv_frame fr = frames[pair];
+    const Pix *ia = (const Pix *)fr.img_a, *ib = (const Pix *)fr.img_b;
+    const int h = fr.height, w = fr.width;
+    const long pitch = fr.pitch;
+    const float *pu = cu + (long)pair * cnt, *pv = cv + (long)pair * cnt;
+    const float du = pu[k], dv = pv[k];
+    const double flu = floor((double)du), flv = floor((double)dv);
+    const double flu2 = floor((double)(du / 2.0f)), flv2 = floor((double)(dv / 2.0f));
+    const int top = tops[ti], left = lefts[tj];
+    const int topRefB = (int)(short)((double)top + flu), leftRefB = (int)(short)((double)left + flv);
+    const int tid = threadIdx.x, nt = blockDim.x;
+
+    // mini: the neighbourhood spline in shared memory
+    __shared__ double s_ys[kMiniR], s_xs[kMiniR], s_cpy[kMiniR], s_cpx[kMiniR];
+    __shared__ float s_fys[kMiniR], s_fxs[kMiniR], s_f[2][kMiniR * kMiniR];
+    __shared__ double s_fy[2][kMiniR * kMiniR], s_fx[2][kMiniR * kMiniR];
+    __shared__ float4 s_c4[2][kMiniR * kMiniR];
+    __shared__ int s_max[2];
+    const int r2 = kMiniR / 2;
+    const int i0 = ti - r2 < 0 ? 0 : ti - r2, i1 = ti + r2 > ni - 1 ? ni - 1 : ti + r2;
+    const int j0 = tj - r2 < 0 ? 0 : tj - r2, j1 = tj + r2 > nj - 1 ? nj - 1 : tj + r2;
+    const int di = i1 - i0 + 1, dj = j1 - j0 + 1;
+    if (tid < 2) s_max[tid] = 0;
+    if (mini) {
+        for (int q = tid; q < di * dj; q += nt) {
+            const int a = q / dj, b = q - a * dj;
+            const long kk = (long)(i0 + a) * nj + (j0 + b);
+            s_f[0][q] = (float)((double)pu[kk] - flu);
+            s_f[1][q] = (float)((double)pv[kk] - flv);
+        }
+        if (tid < di) {
+            s_fys[tid] = (float)tops[i0 + tid] + (float)n / 2.0f - 0.5f;
+            s_ys[tid] = (double)s_fys[tid];
+        }
+        if (tid >= 32 && tid < 32 + dj) {
+            const int j = tid - 32;
+            s_fxs[j] = (float)lefts[j0 + j] + (float)n / 2.0f - 0.5f;
+            s_xs[j] = (double)s_fxs[j];
+        }
+        __syncthreads();
+        if (tid == 0) spline_factor(s_ys, di, s_cpy);
+        if (tid == 1) spline_factor(s_xs, dj, s_cpx);
+        __syncthreads();
+        // knot derivatives: column lines (along y) and row lines (along x) of both components
+        for (int q = tid; q < 2 * (dj + di); q += nt) {
+            const int comp = q / (dj + di), line = q - comp * (dj + di);
+            if (line < dj)
+                spline_line(s_ys, s_cpy, di, s_f[comp] + line, dj, s_fy[comp] + line, dj);
+            else
+                spline_line(s_xs, s_cpx, dj, s_f[comp] + (long)(line - dj) * dj, 1, s_fx[comp] + (long)(line - dj) * dj, 1);
+        }
+        __syncthreads();
+        // cross derivatives (central differences, one-sided at the border) and float nodes
+        for (int q = tid; q < 2 * di * dj; q += nt) {
+            const int comp = q / (di * dj), kk = q - comp * di * dj;
+            const int i = kk / dj, j = kk - i * dj;
+            const int in = i + 1 < di ? i + 1 : di - 1, ip = i - 1 >= 0 ? i - 1 : 0;
+            const int jn = j + 1 < dj ? j + 1 : dj - 1, jp = j - 1 >= 0 ? j - 1 : 0;
+            const double den = (s_ys[in] - s_ys[ip]) * (s_xs[jn] - s_xs[jp]);
+            const float *f = s_f[comp];
+            const double a = (double)f[in * dj + jn], b = (double)f[in * dj + jp];
+            const double c = (double)f[ip * dj + jn], d = (double)f[ip * dj + jp];
+            const double fyx = (a - b - c + d) / den;
+            s_c4[comp][kk] = make_float4(f[kk], (float)s_fy[comp][kk], (float)s_fx[comp][kk], (float)fyx);
+        }
+        __syncthreads();
+    }
+    // offsets and origins of the warped sides
+    int topA = top, leftA = left, topB = top, leftB = left;
+    float uoA = 0.0f, voA = 0.0f, uoB = 0.0f, voB = 0.0f;
+    if (image_mode == 1) {
+        topA = (int)(short)((double)top - flu);
+        leftA = (int)(short)((double)left - flv);
+    } else if (image_mode == 2) {
+        topB = topRefB;
+        leftB = leftRefB;
+    } else {
+        topA = (int)(short)((double)top - flu2);
+        leftA = (int)(short)((double)left - flv2);
+        uoA = (float)((double)(du / 2.0f) - flu2) - (float)((double)du - flu);
+        voA = (float)((double)(dv / 2.0f) - flv2) - (float)((double)dv - flv);
+        topB = (int)(short)((double)top + flu2);
+        leftB = (int)(short)((double)left + flv2);
+        uoB = (float)((double)(du / 2.0f) - flu2);
+        voB = (float)((double)(dv / 2.0f) - flv2);
+    }
+    const float mu = du - (float)flu, mv = dv - (float)flv;
+    const long base = ((long)pair * cnt + k) * n * n;
+    int lmax[2] = {0, 0};
+    for (int q = tid; q < n * n; q += nt) {
+        const int i = q / n, j = q - i * n;
+        float u = mu, v = mv;
+        if (mini) {
+            float y = (float)topRefB + (float)i, x = (float)leftRefB + (float)j;
+            const float ymin = s_fys[0], ymax = s_fys[di - 1], xmin = s_fxs[0], xmax = s_fxs[dj - 1];
+            if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
+            if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
+            u = field_value(s_fys, di, s_fxs, dj, s_c4[0], y, x);
+            v = field_value(s_fys, di, s_fxs, dj, s_c4[1], y, x);
+        }
+        // image A
+        if (image_mode == 2) {
+            const int y = top + i, x = left + j;
+            const int val = (y >= 0 && y < h && x >= 0 && x < w) ? (int)ia[(long)y * pitch + x] : 0;
+            tiles_a[base + q] = (Pix)val;
+            lmax[0] = val > lmax[0] ? val : lmax[0];
+        } else {
+            float ua = u, va = v;
+            if (image_mode == 3) {
+                ua = u / 2.0f + uoA;
+                va = v / 2.0f + voA;
+            }
+            const float val =
+                warp_pixel(ia, h, w, pitch, ua, va, (int)(short)(i + topA), (int)(short)(j + leftA), true);
+            tiles_a[base + q] = (Pix)(int)val;
+        }
+        // image B
+        if (image_mode == 1) {
+            const int y = top + i, x = left + j;
+            const int val = (y >= 0 && y < h && x >= 0 && x < w) ? (int)ib[(long)y * pitch + x] : 0;
+            tiles_b[base + q] = (Pix)val;
+            lmax[1] = val > lmax[1] ? val : lmax[1];
+        } else {
+            float ub = u, vb = v;
+            if (image_mode == 3) {
+                ub = u / 2.0f + uoB;
+                vb = v / 2.0f + voB;
+            }
+            const float val =
+                warp_pixel(ib, h, w, pitch, ub, vb, (int)(short)(i + topB), (int)(short)(j + leftB), false);
+            tiles_b[base + q] = (Pix)(int)val;
+        }
+    }
+    if (image_mode != 3) {
+        atomicMax(&s_max[0], lmax[0]);
+        atomicMax(&s_max[1], lmax[1]);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const long o = (long)pair * cnt + k;
+        max_a[o] = image_mode == 2 ? (float)(s_max[0] < 16 ? 16 : s_max[0]) : full_max;
+        max_b[o] = image_mode == 1 ? (float)(s_max[1] < 16 ? 16 : s_max[1]) : full_max;
+    }
 }
 
 // Per-pixel field only (test hook for the field stage): pair 0, outputs h x w floats.
@@ -439,6 +606,23 @@ cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w,
         warp_both_kernel<uint8_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk);
     else if (pixel_type == QLPIV_PIX_U16)
         warp_both_kernel<uint16_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk);
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile_warp(cudaStream_t s, int pixel_type, int pairs, const qlpiv_frame *frames, int n, int ni,
+                             int nj, const int *tops, const int *lefts, const float *cu, const float *cv,
+                             int image_mode, int mini, float full_max, void *tiles_a, void *tiles_b, float *max_a,
+                             float *max_b) {
+    const dim3 grd((unsigned)((long)ni * nj), pairs);
+    if (pixel_type == QLPIV_PIX_U8)
+        tile_warp_kernel<uint8_t><<<grd, 256, 0, s>>>(frames, n, ni, nj, tops, lefts, cu, cv, image_mode, mini,
+                                                      full_max, (uint8_t *)tiles_a, (uint8_t *)tiles_b, max_a, max_b);
+    else if (pixel_type == QLPIV_PIX_U16)
+        tile_warp_kernel<uint16_t><<<grd, 256, 0, s>>>(frames, n, ni, nj, tops, lefts, cu, cv, image_mode, mini,
+                                                       full_max, (uint16_t *)tiles_a, (uint16_t *)tiles_b, max_a,
+                                                       max_b);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();

@@ -26,6 +26,13 @@ cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const dou
 cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
                         const qlpiv_frame *dst, const float *ys, int ni, const float *xs, int nj, SplineCoef coef,
                         int int16_quirk);
+// Micro / mini per-tile warping of every pair's tiles (grid tops[ni] x lefts[nj], side n; tile
+// displacements cu / cv [pairs][ni*nj]); image_mode 1 first, 2 second, 3 both.  Writes
+// [pairs][tiles][n][n] pixels of pixel_type and per-tile maxima.
+cudaError_t launch_tile_warp(cudaStream_t s, int pixel_type, int pairs, const qlpiv_frame *frames, int n, int ni,
+                             int nj, const int *tops, const int *lefts, const float *cu, const float *cv,
+                             int image_mode, int mini, float full_max, void *tiles_a, void *tiles_b, float *max_a,
+                             float *max_b);
 // Per-pixel field; pixel (i, j) is evaluated at (off_y + i, off_x + j), clamped to the knot box.
 cudaError_t launch_field(cudaStream_t s, int h, int w, const float *ys, int ni, const float *xs, int nj,
                          SplineCoef coef, float *fu, float *fv, float off_y = 0.0f, float off_x = 0.0f);

@@ -39,6 +39,7 @@ struct LevelPlan {
     // validation (allocated only when the descriptor asks for it)
     DevBuf d_tops, d_lefts, d_order, d_rank;  // grid rows / columns, spiral order and rank
     DevBuf d_bu, d_bv, d_puv, d_npk, d_state, d_list, d_done, d_sweeps;
+    DevBuf d_tiles, d_tmax;  // micro / mini warping: warped tiles (A then B) and their maxima
     long count() const { return (long)g.tiles_i * g.tiles_j; }
 };
 
@@ -60,7 +61,7 @@ void destroy_plan(AdaptivePlan *p) {
         for (DevBuf *b : {&l.d_cy, &l.d_cx, &l.d_cyf, &l.d_cxf, &l.d_cpy, &l.d_cpx, &l.d_fi, &l.d_at, &l.d_al, &l.d_bt,
                           &l.d_bl, &l.d_u, &l.d_v, &l.coef, &l.d_rows, &l.d_tops, &l.d_lefts, &l.d_order,
                           &l.d_rank, &l.d_bu, &l.d_bv, &l.d_puv, &l.d_npk, &l.d_state, &l.d_list, &l.d_done,
-                          &l.d_sweeps})
+                          &l.d_sweeps, &l.d_tiles, &l.d_tmax})
             b->release();
     for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table, &p->flow, &p->flow_dense})
         b->release();
@@ -78,6 +79,11 @@ static SplineCoef coef_at(void *base, long n) {
 
 static float full_scale(int pixel_type) { return pixel_type == QLPIV_PIX_U8 ? 255.0f : 65535.0f; }
 
+// Micro / mini per-tile warping modes: image mode (1 first, 2 second, 3 both) and mini flag.
+static bool per_tile_warp(int m) { return m >= QLPIV_WARP_FIRST_MICRO && m <= QLPIV_WARP_BOTH_MINI; }
+static int tile_image_mode(int m) { return (m - QLPIV_WARP_FIRST_MICRO) % 3 + 1; }
+static bool tile_mini(int m) { return m >= QLPIV_WARP_FIRST_MINI; }
+
 static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type, int height, int width) {
     if (!d) return fail(QLPIV_E_ARG, "adaptive descriptor is NULL");
     if (pixel_type != QLPIV_PIX_U8 && pixel_type != QLPIV_PIX_U16)
@@ -89,7 +95,7 @@ static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type,
     if ((r & (r - 1)) != 0) return fail(QLPIV_E_ARG, "IA start / end ratio is not a power of two");
     for (int n = d->ia_start; n >= d->ia_end; n >>= 1)
         if (!xcorr_size_supported(n)) return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64)", n);
-    if (d->warp_mode != QLPIV_WARP_NONE && d->warp_mode != QLPIV_WARP_BOTH_BILINEAR)
+    if (d->warp_mode != QLPIV_WARP_NONE && d->warp_mode != QLPIV_WARP_BOTH_BILINEAR && !per_tile_warp(d->warp_mode))
         return fail(QLPIV_E_ARG, "unknown warp mode %d", d->warp_mode);
     if (d->norm_mode != QLPIV_NORM_MAX_A && d->norm_mode != QLPIV_NORM_OWN_MAX && d->norm_mode != QLPIV_NORM_NONE)
         return fail(QLPIV_E_ARG, "unknown normalisation mode %d", d->norm_mode);
@@ -157,7 +163,8 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
         if (grid_superposition(height, width, d->margins, d->ia_start, lv, d->overlap_factor, &L.g, nullptr, nullptr,
                                0) < -1)
             return fail(QLPIV_E_SHAPE, "image too small for IA %d at level %d", d->ia_start >> lv, lv);
-        if (d->warp_mode == QLPIV_WARP_BOTH_BILINEAR && lv > 0 && (L.g.tiles_i < 3 || L.g.tiles_j < 3))
+        if ((d->warp_mode == QLPIV_WARP_BOTH_BILINEAR || per_tile_warp(d->warp_mode)) && lv > 0 &&
+            (L.g.tiles_i < 3 || L.g.tiles_j < 3))
             return fail(QLPIV_E_SHAPE, "level %d has %d x %d tiles: the warp spline needs at least 3 per axis", lv,
                         L.g.tiles_i, L.g.tiles_j);
         L.tops.resize(L.g.tiles_i);
@@ -222,6 +229,12 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
                 (e = L.d_done.ensure(sizeof(int32_t) * total)) != cudaSuccess ||
                 (e = L.d_sweeps.ensure(sizeof(int32_t) * pairs)) != cudaSuccess)
                 return cuda_fail(e, "validation buffers");
+        }
+        if (per_tile_warp(d->warp_mode) && lv > 0) {
+            const size_t tb = (size_t)total * n * n * pixel_bytes(pixel_type);
+            if ((e = L.d_tiles.ensure(2 * tb)) != cudaSuccess ||
+                (e = L.d_tmax.ensure(sizeof(float) * 2 * total)) != cudaSuccess)
+                return cuda_fail(e, "warped tile buffers");
         }
         // the host vectors above die at scope exit: make the copies complete first
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "adaptive plan upload");
@@ -311,7 +324,20 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
         }
         const qlpiv_frame *src = frames_dev;
         const int *bt = L.d_at.as<int>(), *bl = L.d_al.as<int>();
-        if (d.warp_mode == QLPIV_WARP_BOTH_BILINEAR) {
+        const bool tiles = per_tile_warp(d.warp_mode) && lv > 0;
+        if (tiles) {
+            StageScope sc(h, "tile-warp", (int)lv, L.g.n, 1, total);
+            const size_t tb = (size_t)total * L.g.n * L.g.n * pixel_bytes(p->pixel_type);
+            char *ta = L.d_tiles.as<char>();
+            float *mx = L.d_tmax.as<float>();
+            if ((e = launch_tile_warp(s, p->pixel_type, pairs, frames_dev, L.g.n, L.g.tiles_i, L.g.tiles_j,
+                                      L.d_tops.as<int>(), L.d_lefts.as<int>(), u, v, tile_image_mode(d.warp_mode),
+                                      tile_mini(d.warp_mode), fm, ta, ta + tb, mx, mx + total)) != cudaSuccess)
+                return cuda_fail(e, "tile warp");
+            h->launches++;
+        } else if (per_tile_warp(d.warp_mode)) {
+            // level 0: both tiles clipped at the grid (the displacements are zero)
+        } else if (d.warp_mode == QLPIV_WARP_BOTH_BILINEAR) {
             if (lv > 0) {  // no warping at the first level: displacements are all zero
                 SplineCoef c = coef_of(L, pairs);
                 {
@@ -351,6 +377,23 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
         job.norm_mode = d.norm_mode;
         job.max_mode = d.max_mode;
         job.fixed_max_a = job.fixed_max_b = fm;
+        if (per_tile_warp(d.warp_mode)) {
+            job.max_mode = QLPIV_MAX_COMPUTE;  // level 0: clipped tiles
+            if (tiles) {  // the warped tiles, contiguous, with their maxima
+                const size_t tb = (size_t)total * L.g.n * L.g.n * pixel_bytes(p->pixel_type);
+                job.frames = nullptr;
+                job.frame_idx = nullptr;
+                job.img_a = L.d_tiles.p;
+                job.img_b = L.d_tiles.as<char>() + tb;
+                job.pitch_a = job.pitch_b = L.g.n;
+                job.h = (int)(total * L.g.n);
+                job.w = L.g.n;
+                job.a_top = job.a_left = job.b_top = job.b_left = nullptr;
+                job.max_mode = QLPIV_MAX_GIVEN;
+                job.max_a = L.d_tmax.as<float>();
+                job.max_b = L.d_tmax.as<float>() + total;
+            }
+        }
         job.subpix = d.subpix_mode;
         job.subpix_pixels = d.subpix_mode >= QLPIV_SUBPIX_GAUSS_LM ? d.subpix_pixels : 0;
         job.subpix_iters = d.subpix_iterations;
@@ -439,6 +482,8 @@ size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int heigh
         total += 5 * al(4 * tot) + 2 * al(4 * tot) + al(coef_bytes((long)tot));
         if (lv > 0) total += al(8 * (size_t)pairs * ni * prev_nj);
         total += al(4 * ni) + al(4 * nj);
+        if (per_tile_warp(d->warp_mode) && lv > 0)
+            total += al(2 * tot * g.n * g.n * pixel_bytes(pixel_type)) + al(8 * tot);
         if (d->validation != QLPIV_VALIDATE_NONE) {
             const size_t k = d->num_peaks;
             total += 2 * al(4 * cnt) + 2 * al(4 * tot) + al(8 * tot * k) + 2 * al(tot) + 2 * al(4 * tot) +
@@ -655,6 +700,62 @@ qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, const void *img_a,
         (e = cudaMemcpyAsync(out_b, base + 3 * stride, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
         return cuda_fail(e, "warp download");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_tile_warp(qlpiv_handle *h, int pixel_type, const void *img_a, const void *img_b, int height,
+                             int width, int n, int ni, int nj, const int32_t *tops, const int32_t *lefts,
+                             const float *u, const float *v, int warp_mode, float full_max, void *tiles_a,
+                             void *tiles_b, float *max_a, float *max_b) {
+    if (!h || !img_a || !img_b || !tops || !lefts || !u || !v || !tiles_a || !tiles_b || !max_a || !max_b)
+        return fail(QLPIV_E_ARG, "NULL argument");
+    if (pixel_type != QLPIV_PIX_U8 && pixel_type != QLPIV_PIX_U16) return fail(QLPIV_E_ARG, "u8 or u16 images only");
+    if (!per_tile_warp(warp_mode)) return fail(QLPIV_E_ARG, "warp mode %d is not a micro / mini mode", warp_mode);
+    if (ni < 3 || nj < 3) return fail(QLPIV_E_SHAPE, "the spline needs at least 3 tiles per axis");
+    if (height <= 0 || width <= 0 || n <= 0 || n > 64) return fail(QLPIV_E_SHAPE, "image %d x %d, tile %d", height, width, n);
+    for (int i = 0; i < ni; i++)
+        if (tops[i] < 0 || tops[i] + n > height) return fail(QLPIV_E_SHAPE, "tile row %d leaves the image", i);
+    for (int j = 0; j < nj; j++)
+        if (lefts[j] < 0 || lefts[j] + n > width) return fail(QLPIV_E_SHAPE, "tile column %d leaves the image", j);
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaStream_t s = h->stream;
+    const size_t pb = pixel_bytes(pixel_type), bytes = (size_t)height * width * pb;
+    const size_t stride = (bytes + 255) & ~(size_t)255;
+    const long cnt = (long)ni * nj;
+    const size_t tb = (size_t)cnt * n * n * pb;
+    DevBuf *b = h->scratch;
+    cudaError_t e;
+    if ((e = h->tiles_a.ensure(2 * stride)) != cudaSuccess || (e = h->frames.ensure(sizeof(qlpiv_frame))) != cudaSuccess ||
+        (e = b[0].ensure(sizeof(int32_t) * (ni + nj))) != cudaSuccess ||
+        (e = b[1].ensure(sizeof(float) * 2 * cnt)) != cudaSuccess || (e = b[2].ensure(2 * tb)) != cudaSuccess ||
+        (e = b[3].ensure(sizeof(float) * 2 * cnt)) != cudaSuccess)
+        return cuda_fail(e, "tile warp buffers");
+    char *base = h->tiles_a.as<char>();
+    const qlpiv_frame t{base, base + stride, height, width, (int64_t)width};
+    int32_t *dtl = b[0].as<int32_t>();
+    float *duv = b[1].as<float>(), *dmx = b[3].as<float>();
+    char *dtiles = b[2].as<char>();
+    if ((e = cudaMemcpyAsync(base, img_a, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(base + stride, img_b, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(h->frames.p, &t, sizeof(t), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dtl, tops, sizeof(int32_t) * ni, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dtl + ni, lefts, sizeof(int32_t) * nj, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(duv, u, sizeof(float) * cnt, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(duv + cnt, v, sizeof(float) * cnt, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "tile warp upload");
+    if ((e = launch_tile_warp(s, pixel_type, 1, h->frames.as<qlpiv_frame>(), n, ni, nj, dtl, dtl + ni, duv, duv + cnt,
+                              tile_image_mode(warp_mode), tile_mini(warp_mode), full_max, dtiles, dtiles + tb, dmx,
+                              dmx + cnt)) != cudaSuccess)
+        return cuda_fail(e, "tile warp");
+    h->launches++;
+    if ((e = cudaMemcpyAsync(tiles_a, dtiles, tb, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(tiles_b, dtiles + tb, tb, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(max_a, dmx, sizeof(float) * cnt, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(max_b, dmx + cnt, sizeof(float) * cnt, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "tile warp download");
     return QLPIV_OK;
 }
 

@@ -9,7 +9,8 @@ data), and it is the denominator of the batched path's speed-up.  It runs the sa
 """
 import numpy as np
 
-from . import F_ABSENT, VALIDATE_MULTIPEAK_MEDIAN, WARP_BOTH_BILINEAR, WARP_NONE, adaptive_levels, grid
+from . import (F_ABSENT, MAX_COMPUTE, VALIDATE_MULTIPEAK_MEDIAN, WARP_BOTH_BILINEAR, WARP_BOTH_MINI,
+               WARP_FIRST_MICRO, WARP_NONE, adaptive_levels, grid)
 
 
 def _java_round(x):
@@ -49,14 +50,24 @@ def piv_adaptive_per_call(handle, img_a, img_b, desc):
         al = np.tile(lefts, ni)
         src_a, src_b = a, b
         bt, bl = at, al
-        if desc.warp_mode == WARP_BOTH_BILINEAR:
+        per_tile = WARP_FIRST_MICRO <= desc.warp_mode <= WARP_BOTH_MINI
+        if per_tile:
+            if lv > 0:   # warped tiles with their maxima, through the tile entry points
+                ta, tb, ma, mb = handle.tile_warp(a, b, n, tops, lefts, u, v, desc.warp_mode, fm)
+                tkw = dict(norm_mode=desc.norm_mode, subpix_mode=desc.subpix_mode)
+                vec = handle.xcorr_multipeaks(ta, tb, ma, mb, num_peaks=desc.num_peaks, peak_kernel=desc.peak_kernel,
+                                              **tkw) if validate else handle.xcorr_peaks(ta, tb, ma, mb, **tkw)
+            else:        # level 0: both tiles clipped with their own maxima
+                vec = handle.piv_pass(a, b, n, at, al, **dict(pass_kw, max_mode=MAX_COMPUTE))
+        elif desc.warp_mode == WARP_BOTH_BILINEAR:
             if lv > 0:
                 src_a, src_b = handle.warp_pair(a, b, cy.astype(np.float64), cx.astype(np.float64), u, v,
                                                 int16_quirk=bool(desc.int16_warp_quirk))
         else:
             bt = _java_round(at.astype(np.float32) + u.ravel())
             bl = _java_round(al.astype(np.float32) + v.ravel())
-        vec = handle.piv_pass(src_a, src_b, n, at, al, bt, bl, **pass_kw)
+        if not per_tile:
+            vec = handle.piv_pass(src_a, src_b, n, at, al, bt, bl, **pass_kw)
         main = vec[:, 0] if vec.ndim == 2 else vec
         u = (u.ravel() + main["u"]).reshape(ni, nj).astype(np.float32)
         v = (v.ravel() + main["v"]).reshape(ni, nj).astype(np.float32)

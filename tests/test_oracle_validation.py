@@ -175,3 +175,60 @@ def test_validation_zeroes_what_it_cannot_repair(oracle):
     np.testing.assert_array_equal(inv, einv)
     np.testing.assert_array_equal(gu, eu)
     assert (gu[inv == 1] == 0).all()
+
+
+def _tile_grid(oracle, h, w, n):
+    _, tops, lefts = oracle.grid(h, w, n, 0, 0.5)
+    return tops, lefts
+
+
+def test_micro_warp_integer_displacement_is_a_shift(oracle):
+    """Micro warping by a whole-pixel displacement cuts the tiles at the displaced origins
+    (BiLinearImageMicroAndMiniWarpingStrategy: floor(u) moves the tile, the fraction warps)."""
+    rng = np.random.default_rng(4)
+    a = rng.integers(0, 255, (96, 112)).astype(np.uint8)
+    b = rng.integers(0, 255, (96, 112)).astype(np.uint8)
+    n = 16
+    tops, lefts = _tile_grid(oracle, 96, 112, n)
+    cnt = len(tops) * len(lefts)
+    u = np.full(cnt, 4.0, np.float32)
+    v = np.full(cnt, -2.0, np.float32)
+    for mode in (oracle.WARP_FIRST_MICRO, oracle.WARP_SECOND_MICRO, oracle.WARP_BOTH_MICRO):
+        ta, tb, ma, mb = oracle.tile_warp(a, b, n, tops, lefts, u, v, mode, 255.0)
+        for k in range(cnt):
+            t, l = tops[k // len(lefts)], lefts[k % len(lefts)]
+            da, db = {oracle.WARP_FIRST_MICRO: ((-4, 2), (0, 0)), oracle.WARP_SECOND_MICRO: ((0, 0), (4, -2)),
+                      oracle.WARP_BOTH_MICRO: ((-2, 1), (2, -1))}[mode]
+
+            def cut(img, dy, dx):
+                y0, x0 = t + dy, l + dx
+                out = np.zeros((n, n), np.float32)
+                for i in range(n):
+                    for j in range(n):
+                        yy = min(max(y0 + i, 0), 95)
+                        xx = min(max(x0 + j, 0), 111)
+                        out[i, j] = img[yy, xx]
+                return out
+            np.testing.assert_array_equal(ta[k], cut(a, *da))
+            np.testing.assert_array_equal(tb[k], cut(b, *db))
+            assert ma[k] == (max(16, a[t:t + n, l:l + n].max()) if mode == oracle.WARP_SECOND_MICRO else 255.0)
+            assert mb[k] == (max(16, b[t:t + n, l:l + n].max()) if mode == oracle.WARP_FIRST_MICRO else 255.0)
+
+
+def test_mini_warp_of_a_uniform_field_equals_micro(oracle):
+    """With every tile displaced alike the mini spline is flat: mini == micro."""
+    rng = np.random.default_rng(5)
+    a = rng.integers(0, 4095, (128, 128)).astype(np.uint16)
+    b = rng.integers(0, 4095, (128, 128)).astype(np.uint16)
+    n = 32
+    tops, lefts = _tile_grid(oracle, 128, 128, n)
+    cnt = len(tops) * len(lefts)
+    u = np.full(cnt, 1.375, np.float32)
+    v = np.full(cnt, -0.625, np.float32)
+    for micro, mini in ((oracle.WARP_FIRST_MICRO, oracle.WARP_FIRST_MINI),
+                        (oracle.WARP_SECOND_MICRO, oracle.WARP_SECOND_MINI),
+                        (oracle.WARP_BOTH_MICRO, oracle.WARP_BOTH_MINI)):
+        r1 = oracle.tile_warp(a, b, n, tops, lefts, u, v, micro, 4095.0)
+        r2 = oracle.tile_warp(a, b, n, tops, lefts, u, v, mini, 4095.0)
+        for x, y in zip(r1, r2):
+            np.testing.assert_array_equal(x, y)
