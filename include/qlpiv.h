@@ -448,6 +448,29 @@ qlpiv_status qlpiv_piv_flow_device(qlpiv_handle *h, const qlpiv_adaptive_desc *p
                                    int pixel_type, int height, int width, int num_pairs, const qlpiv_frame *frames,
                                    float *out_u, float *out_v, float *dense_u, float *dense_v);
 
+/* ---------------- mixed batches ----------------
+ * Many frame pairs of uneven sizes, each with its own IA size (16, 32, 64) and overlap factor,
+ * correlated as one flattened work list per IA size (the pair's level-0 SuperPosition grid),
+ * launched from one captured CUDA graph whose branches run the sizes concurrently.  `frames`
+ * is a host table of device images; the plan keeps a device copy and the output.  With
+ * autotune the grid of each size's launch is chosen by timing 1, 2, 4 and 8 waves of resident
+ * CTAs on its work list.  Output vectors are size-major and pair-contiguous: pair q's
+ * tiles_i x tiles_j tiles (row-major) start at pair_offset[q]. */
+typedef struct qlpiv_mixed_plan qlpiv_mixed_plan;
+qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmpl, int pixel_type, int num_pairs,
+                                     const qlpiv_frame *frames, const int32_t *ia_size, const float *overlap_factor,
+                                     int autotune, qlpiv_mixed_plan **plan);
+/* total_vectors; pair_offset[num_pairs + 1] (the last entry = total); tiles_ij[2 num_pairs]
+ * (tiles_i, tiles_j); waves[3]
+ * chosen for sizes 16, 32, 64 (0: default).  Any output may be NULL. */
+qlpiv_status qlpiv_mixed_plan_info(const qlpiv_mixed_plan *plan, int64_t *total_vectors, int64_t *pair_offset,
+                                   int32_t *tiles_ij, int32_t *waves);
+/* Queues the plan's graph on the handle's stream; *device_out receives the device vectors. */
+qlpiv_status qlpiv_mixed_plan_run(qlpiv_handle *h, qlpiv_mixed_plan *plan, qlpiv_vector **device_out);
+/* Waits for the handle's stream and copies the plan's vectors to the host. */
+qlpiv_status qlpiv_mixed_plan_download(qlpiv_handle *h, qlpiv_mixed_plan *plan, qlpiv_vector *host_out);
+qlpiv_status qlpiv_mixed_plan_destroy(qlpiv_mixed_plan *plan);
+
 /* ---------------- request server (continuous batching) ----------------
  * The reference runs one job per frame pair and host thread (S/jobs/LocalPIVOpenCLGpuJob.java,
  * pooled by OpenClGpuManager.java:121-148); it has no server.  A qlpiv_server owns one device

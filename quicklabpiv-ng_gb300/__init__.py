@@ -212,6 +212,11 @@ _SIGNATURES = {
                             _vp, _vp, _vp]),
     "qlpiv_piv_flow_device": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), ctypes.POINTER(FlowDesc), _i, _i, _i, _i, _vp,
                                    _vp, _vp, _vp, _vp]),
+    "qlpiv_mixed_plan_create": (_i, [_vp, ctypes.POINTER(PassDesc), _i, _i, _vp, _vp, _vp, _i, ctypes.POINTER(_vp)]),
+    "qlpiv_mixed_plan_info": (_i, [_vp, ctypes.POINTER(ctypes.c_int64), _vp, _vp, _vp]),
+    "qlpiv_mixed_plan_run": (_i, [_vp, _vp, ctypes.POINTER(_vp)]),
+    "qlpiv_mixed_plan_download": (_i, [_vp, _vp, _vp]),
+    "qlpiv_mixed_plan_destroy": (_i, [_vp]),
     "qlpiv_server_create": (_i, [ctypes.POINTER(ServerParams), ctypes.POINTER(_vp)]),
     "qlpiv_server_destroy": (_i, [_vp]),
     "qlpiv_submit": (_i, [_vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
@@ -702,6 +707,59 @@ def adaptive_plan_bytes(desc, pixel_type, height, width, pairs=1):
     _check(load_library().qlpiv_adaptive_plan_bytes(ctypes.byref(desc), pixel_type, height, width, pairs,
                                                     ctypes.byref(b)))
     return b.value
+
+
+class MixedPlan:
+    """Mixed batch plan (qlpiv_mixed_plan_*): pairs of uneven sizes, each with its own IA size
+    and overlap, one graph launch per batch.  frames: FRAME_DTYPE table of device images."""
+
+    def __init__(self, handle, frames, ia_sizes, overlap_factors, pixel_type, autotune=True, **desc_kw):
+        self._h = handle
+        self._lib = handle._lib
+        table = np.ascontiguousarray(frames, FRAME_DTYPE)
+        sizes = np.ascontiguousarray(ia_sizes, np.int32)
+        ofac = np.ascontiguousarray(overlap_factors, np.float32)
+        self.num_pairs = len(table)
+        d = Handle.desc(16, **desc_kw)
+        p = ctypes.c_void_p()
+        _check(self._lib.qlpiv_mixed_plan_create(handle._h, ctypes.byref(d), pixel_type, self.num_pairs,
+                                                 table.ctypes.data, _addr(sizes), _addr(ofac), int(autotune),
+                                                 ctypes.byref(p)))
+        self._p = p
+        tot = ctypes.c_int64()
+        self.pair_offset = np.empty(self.num_pairs + 1, np.int64)
+        self.tiles = np.empty((self.num_pairs, 2), np.int32)
+        self.waves = np.empty(3, np.int32)
+        _check(self._lib.qlpiv_mixed_plan_info(p, ctypes.byref(tot), _addr(self.pair_offset), _addr(self.tiles),
+                                               _addr(self.waves)))
+        self.total = tot.value
+
+    def run(self):
+        """Queues the batch on the handle's stream; returns the device address of the vectors."""
+        out = ctypes.c_void_p()
+        _check(self._lib.qlpiv_mixed_plan_run(self._h._h, self._p, ctypes.byref(out)))
+        return out.value
+
+    def vectors(self):
+        out = np.empty(self.total, VECTOR_DTYPE)
+        _check(self._lib.qlpiv_mixed_plan_download(self._h._h, self._p, _addr(out)))
+        return out
+
+    def pair_vectors(self, vec, q):
+        ti, tj = int(self.tiles[q][0]), int(self.tiles[q][1])
+        o = int(self.pair_offset[q])
+        return vec[o:o + ti * tj].reshape(ti, tj)
+
+    def close(self):
+        if getattr(self, "_p", None):
+            self._lib.qlpiv_mixed_plan_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Server:

@@ -69,7 +69,7 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
     j.twiddles = tw + twiddle_offset(S::M);
     // every CTA loops over IAs; eight waves of CTAs balance the single-peak kernel best,
     // one resident wave the multi-peak one (its fit queue then fills between flushes)
-    long grid = (long)num_sms * bps * (job.num_peaks > 0 ? 1 : 8);
+    long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? 1 : 8));
     if (grid > job.count) grid = job.count;
     if (grid < 1) return cudaSuccess;
     // P-point sub-pixel stencils: 2 P floats per queued fit after the fixed layout

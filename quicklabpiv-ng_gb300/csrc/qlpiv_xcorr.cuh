@@ -123,6 +123,7 @@ struct IaJob {
     float2 *peak_uv;             // optional [count][k] displacement increments of every peak
     uint8_t *npeaks;             // optional [count] peaks found
     const cplx *twiddles;        // exp(-2 pi i e / M), e < M (device table, filled once per device)
+    int waves;                   // grid = SMs x resident CTAs x waves; 0: the default per mode
 };
 
 // Integer peak and 3-point stencil of one IA, queued for the sub-pixel fit.
