@@ -365,6 +365,82 @@ def run_serving(pkg, dev, count=48, loads=(0.25, 0.5, 0.75, 0.9, 1.1), per_load=
             "latency": "submit -> displacements on the host (qlpiv_poll), Poisson arrivals"}
 
 
+# Batched launch: 256 pairs of sizes from {256^2, 512^2, 1024^2, 2048^2} u8, each with its own IA
+# size from {16, 32, 64} at 50 % overlap, one graph launch per batch (IA 128 is not supported).
+BATCH_WORKLOAD = ("batched-mixed: 256 u8 pairs, sides from {256, 512, 1024, 2048} (uniform), IA size per pair from "
+                  "{16, 32, 64} (uniform; 128 not supported), 50 % overlap, FindMaximumFromCenter + 3-point Gaussian, "
+                  "frames cropped at random positions from a 2048x2048 vortex + shear pair tiled 2x2, one captured "
+                  "graph per batch with autotuned launches")
+
+
+def run_batched(pkg, dev, stream, steps, warmup, count=256):
+    import torch
+    rng = np.random.default_rng(3)
+    a0, b0 = pkg.synth.particle_pair((2048, 2048), pkg.synth.Flow(vmax=8.0 - 0.003 * 1024, rc=180.0, shear=0.003),
+                                     ppp=0.02, diam=3.0, bits=8, seed=33)
+    ma, mb = np.tile(a0, (2, 2)), np.tile(b0, (2, 2))
+    sides = rng.choice([256, 512, 1024, 2048], count)
+    sizes = rng.choice([16, 32, 64], count).astype(np.int32)
+    ofac = np.full(count, 0.5, np.float32)
+    keep, host, table = [], [], np.zeros(count, pkg.FRAME_DTYPE)
+    for k in range(count):
+        s_ = int(sides[k])
+        y, x = int(rng.integers(0, 4096 - s_ + 1)), int(rng.integers(0, 4096 - s_ + 1))
+        a = np.ascontiguousarray(ma[y:y + s_, x:x + s_])
+        b = np.ascontiguousarray(mb[y:y + s_, x:x + s_])
+        ta, tb = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+        keep.append((ta, tb))
+        host.append((a, b))
+        table[k] = (ta.data_ptr(), tb.data_ptr(), s_, s_, s_)
+    h = pkg.Handle(dev.index)
+    hs = torch.cuda.ExternalStream(h.stream, device=dev)
+    t0 = time.perf_counter()
+    plan = pkg.MixedPlan(h, table, sizes, ofac, pkg.PIX_U8, autotune=True)
+    plan_s = time.perf_counter() - t0
+    for _ in range(warmup):
+        plan.run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(hs)
+    for _ in range(steps):
+        plan.run()
+    e1.record(hs)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    total = plan.total
+    ia_by_n = {n: int(sum(plan.tiles[q][0] * plan.tiles[q][1] for q in range(count) if sizes[q] == n))
+               for n in (16, 32, 64)}
+    flops = sum(flops_per_ia(n) * c for n, c in ia_by_n.items())
+    bytes_ = sum(bytes_per_ia(n, 1) * c for n, c in ia_by_n.items())
+    # plain per-call: one synchronous frame pass per pair through the host API (sampled)
+    sample = list(range(0, count, 8))
+    for q in sample[:2]:
+        a, b = host[q]
+        g = pkg.grid.superposition(a.shape[0], a.shape[1], int(sizes[q]), 0, 0.5)
+        at, al = g.origins()
+        h.piv_pass(a, b, int(sizes[q]), at, al)
+    tt = time.perf_counter()
+    sample_ias = 0
+    for q in sample:
+        a, b = host[q]
+        g = pkg.grid.superposition(a.shape[0], a.shape[1], int(sizes[q]), 0, 0.5)
+        at, al = g.origins()
+        h.piv_pass(a, b, int(sizes[q]), at, al)
+        sample_ias += g.count
+    per_call_s = time.perf_counter() - tt
+    per_call_pairs = len(sample) / per_call_s
+    plan.close()
+    h.close()
+    return {"workload": BATCH_WORKLOAD, "pairs_per_step": count, "ia_vectors_per_step": total,
+            "ia_vectors_by_size": ia_by_n, "ms_per_step": ms, "frame_pairs_per_s": count / (ms * 1e-3),
+            "ia_vectors_per_s": total / (ms * 1e-3), "fp32_tflops": flops / (ms * 1e-3) / 1e12,
+            "algorithmic_gbs": bytes_ / (ms * 1e-3) / 1e9, "plan_seconds": plan_s,
+            "autotuned_waves": {"16": int(plan.waves[0]), "32": int(plan.waves[1]), "64": int(plan.waves[2])},
+            "plain_per_call": {"frame_pairs_per_s": per_call_pairs, "ia_vectors_per_s": sample_ias / per_call_s,
+                               "sample": f"{len(sample)} pairs, one synchronous qlpiv_pass per pair (host images)"},
+            "vs_per_call_pairs": (count / (ms * 1e-3)) / per_call_pairs}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -528,6 +604,8 @@ def run_gpu(args, rank, world):
         "one_pair_per_call_fused": world * pp_value}
     if not args.no_hybrid:
         result["hybrid"] = run_hybrid(pkg, h, dev, stream, max(2, min(args.steps, 5)), max(3, args.warmup))
+    if not args.no_batched:
+        result["batched"] = run_batched(pkg, dev, stream, max(3, min(args.steps, 10)), max(3, args.warmup))
     if not args.no_serving and world == 1:
         result["serving"] = run_serving(pkg, dev)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -551,6 +629,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-hybrid", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
