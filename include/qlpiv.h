@@ -531,6 +531,48 @@ qlpiv_status qlpiv_server_stats_read(qlpiv_server *s, qlpiv_server_stats *stats)
 qlpiv_status qlpiv_adaptive_plan_bytes(const qlpiv_adaptive_desc *desc, int pixel_type, int height, int width,
                                        int pairs, int64_t *bytes);
 
+/* ---------------- Host data formats either side of the path (no device use) ----------------
+ *
+ * Image ingest replaces S/jobs/ImageReaderJob.java:81-115 (ImageIO read of the frame files) for
+ * baseline greyscale TIFF: one sample per pixel, 8 or 16 bits, strips, uncompressed, LZW or PackBits,
+ * either byte order.  Other TIFFs are rejected with QLPIV_E_UNSUPPORTED, malformed ones with
+ * QLPIV_E_SHAPE.  16-bit samples are returned in host order (12-bit cameras store 0..4095). */
+qlpiv_status qlpiv_tiff_info(const char *path, int *height, int *width, int *bits_per_sample);
+/* Decodes the image row-major into `pixels` (uint8 or uint16 per bits_per_sample). */
+qlpiv_status qlpiv_tiff_read(const char *path, void *pixels, int64_t capacity_bytes);
+
+/* MATLAB level-5 export of the vector maps, the variable layout of
+ * S/exporter/StructMultiFrameFloatVelocityExporter.java:54-181 (one map per IA size):
+ *   exportDate                      char
+ *   parameters                      struct: imageWidth, imageHeight, iaStartI, iaEndI, iaStartJ,
+ *                                   iaEndJ (int32), overlapFactor (single), hasSwappedUVVectors,
+ *                                   markInvalidAsNaN, totalNumberOfVelocityMaps, multiVolumeExport,
+ *                                   multiVolumeLastVolume (int32)
+ *   velocities<iaHeight>x<iaWidth>  struct: iaHeight, iaWidth, adaptiveStep (int32),
+ *                                   margins (struct top, left, bottom, right), u, v (single,
+ *                                   tiles_i x tiles_j x frames). */
+typedef struct qlpiv_mat_export_params {
+    int image_width, image_height;
+    int ia_start, ia_end;       /* first and last adaptive IA side (square IAs) */
+    float overlap_factor;
+    int frames;                 /* velocity maps per IA size */
+    int swap_uv;                /* recorded as hasSwappedUVVectors */
+    int mark_invalid_as_nan;    /* invalid vectors written as NaN */
+    const char *export_date;    /* NULL: the current UTC time */
+    int reserved[4];
+} qlpiv_mat_export_params;
+
+typedef struct qlpiv_mat_velocity_map {
+    int ia_height, ia_width, adaptive_step;
+    int tiles_i, tiles_j;
+    int margins[4];             /* top, left, bottom, right */
+    const float *u, *v;         /* frames x tiles_i x tiles_j, row-major */
+    const uint8_t *invalid;     /* same shape, nonzero = invalid; may be NULL */
+} qlpiv_mat_velocity_map;
+
+qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *params, int num_maps,
+                              const qlpiv_mat_velocity_map *maps);
+
 /* Stage timing of the adaptive pipeline (CUDA events around every launch on the
  * handle's stream).  Accumulates while enabled; qlpiv_profile_read synchronises the
  * stream, returns the totals per (stage, level) and clears them. */

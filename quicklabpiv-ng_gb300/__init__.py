@@ -6,6 +6,7 @@ binding (`Handle`) and mirrors of the reference's stage plugins (`jobs`, `grid`)
 There is no CPU fallback: without the built library every entry point raises.
 """
 import ctypes
+import os
 from pathlib import Path
 
 import numpy as np
@@ -172,6 +173,19 @@ class ServerStats(ctypes.Structure):
                [("reserved", ctypes.c_int64 * 4)]
 
 
+class MatExportParams(ctypes.Structure):
+    _fields_ = [("image_width", ctypes.c_int), ("image_height", ctypes.c_int), ("ia_start", ctypes.c_int),
+                ("ia_end", ctypes.c_int), ("overlap_factor", ctypes.c_float), ("frames", ctypes.c_int),
+                ("swap_uv", ctypes.c_int), ("mark_invalid_as_nan", ctypes.c_int),
+                ("export_date", ctypes.c_char_p), ("reserved", ctypes.c_int * 4)]
+
+
+class MatVelocityMap(ctypes.Structure):
+    _fields_ = [("ia_height", ctypes.c_int), ("ia_width", ctypes.c_int), ("adaptive_step", ctypes.c_int),
+                ("tiles_i", ctypes.c_int), ("tiles_j", ctypes.c_int), ("margins", ctypes.c_int * 4),
+                ("u", ctypes.c_void_p), ("v", ctypes.c_void_p), ("invalid", ctypes.c_void_p)]
+
+
 # C ABI symbol table: name -> (restype, argtypes).  Kept beside include/qlpiv.h.
 _vp, _i, _l, _f = ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_float
 _SIGNATURES = {
@@ -223,6 +237,9 @@ _SIGNATURES = {
     "qlpiv_poll": (_i, [_vp, ctypes.c_uint64, ctypes.POINTER(Result), _i]),
     "qlpiv_server_stats_read": (_i, [_vp, ctypes.POINTER(ServerStats)]),
     "qlpiv_adaptive_plan_bytes": (_i, [ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, ctypes.POINTER(ctypes.c_int64)]),
+    "qlpiv_tiff_info": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    "qlpiv_tiff_read": (_i, [ctypes.c_char_p, _vp, ctypes.c_int64]),
+    "qlpiv_mat_export": (_i, [ctypes.c_char_p, ctypes.POINTER(MatExportParams), _i, ctypes.POINTER(MatVelocityMap)]),
     "qlpiv_profile_enable": (_i, [_vp, _i]),
     "qlpiv_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(_i)]),
 }
@@ -707,6 +724,68 @@ def adaptive_plan_bytes(desc, pixel_type, height, width, pairs=1):
     _check(load_library().qlpiv_adaptive_plan_bytes(ctypes.byref(desc), pixel_type, height, width, pairs,
                                                     ctypes.byref(b)))
     return b.value
+
+
+def tiff_info(path):
+    """(height, width, bits_per_sample) of a baseline greyscale TIFF."""
+    h, w, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _check(load_library().qlpiv_tiff_info(os.fsencode(path), ctypes.byref(h), ctypes.byref(w), ctypes.byref(b)))
+    return h.value, w.value, b.value
+
+
+def read_tiff(path):
+    """Decode a baseline greyscale TIFF (8 or 16 bits, uncompressed or PackBits) to a uint8 /
+    uint16 array, the frame reader of S/jobs/ImageReaderJob.java:81-115."""
+    h, w, b = tiff_info(path)
+    out = np.empty((h, w), np.uint8 if b == 8 else np.uint16)
+    _check(load_library().qlpiv_tiff_read(os.fsencode(path), out.ctypes.data, out.nbytes))
+    return out
+
+
+def export_mat(path, maps, image_height, image_width, ia_start, ia_end, overlap_factor, swap_uv=False,
+               mark_invalid_as_nan=False, export_date=None):
+    """Write the vector maps as a MATLAB level-5 file with the variables of
+    S/exporter/StructMultiFrameFloatVelocityExporter.java.
+
+    maps: one dict per IA size with u, v (frames x tiles_i x tiles_j float32), ia (height, width),
+    adaptive_step, margins (top, left, bottom, right) and optionally invalid (same shape, bool)."""
+    keep, table = [], (MatVelocityMap * max(1, len(maps)))()
+    frames = None
+    for k, m in enumerate(maps):
+        u = np.ascontiguousarray(m["u"], np.float32)
+        v = np.ascontiguousarray(m["v"], np.float32)
+        if u.ndim == 2:
+            u, v = u[None], v[None]
+        if u.shape != v.shape or u.ndim != 3:
+            raise ValueError("u and v must be frames x tiles_i x tiles_j")
+        if frames is not None and u.shape[0] != frames:
+            raise ValueError("every map needs the same number of frames")
+        frames = u.shape[0]
+        inv = m.get("invalid")
+        inv = None if inv is None else np.ascontiguousarray(np.asarray(inv).reshape(u.shape), np.uint8)
+        keep += [u, v, inv]
+        e = table[k]
+        e.ia_height, e.ia_width = (int(x) for x in m["ia"])
+        e.adaptive_step = int(m.get("adaptive_step", 0))
+        e.tiles_i, e.tiles_j = u.shape[1], u.shape[2]
+        e.margins[:] = [int(x) for x in m.get("margins", (0, 0, 0, 0))]
+        e.u, e.v = u.ctypes.data, v.ctypes.data
+        e.invalid = None if inv is None else inv.ctypes.data
+    p = MatExportParams(image_width=image_width, image_height=image_height, ia_start=ia_start, ia_end=ia_end,
+                        overlap_factor=overlap_factor, frames=1 if frames is None else frames, swap_uv=int(bool(swap_uv)),
+                        mark_invalid_as_nan=int(bool(mark_invalid_as_nan)),
+                        export_date=None if export_date is None else export_date.encode())
+    _check(load_library().qlpiv_mat_export(os.fsencode(path), ctypes.byref(p), len(maps), table))
+
+
+def export_adaptive_mat(path, desc, height, width, u, v, invalid=None, **kw):
+    """Export piv_adaptive's final vector maps (pairs x tiles_i x tiles_j) with the last level's
+    IA size, margins and adaptive step, as the reference exports a PIV run's result map."""
+    levels = adaptive_levels(desc, height, width)
+    g = levels[-1]
+    m = dict(u=u, v=v, ia=(g["n"], g["n"]), adaptive_step=len(levels) - 1, invalid=invalid,
+             margins=(g["margin_top"], g["margin_left"], g["margin_bottom"], g["margin_right"]))
+    export_mat(path, [m], height, width, desc.ia_start, desc.ia_end, desc.overlap_factor, **kw)
 
 
 class MixedPlan:

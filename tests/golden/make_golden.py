@@ -25,6 +25,11 @@ Fixtures written (all from files shipped in the reference project):
                        Test.java: per case the window side, the interpolator (0 Gaussian1D least
                        squares, 1 Hongwei Guo with 20 iterations), the centre (uX, uY) and widths
                        (sigmaX, sigmaY) of the analytic peak and the tolerance (8e-3 px).
+  tiff_packbits_rankine.tif  the first four PackBits strips (64 rows) of
+                       testFiles/rankine_vortex01_0.tif, compressed bytes kept verbatim under a
+                       minimal directory; decodes to rankine_pair.npz's a[:64].
+  tiff_lzw_chess.tif   the LZW strip of testFiles/coordTestChessA.tif (128x128 u8, four 64x64
+                       constant quadrants), compressed bytes kept verbatim.
 """
 import struct
 import sys
@@ -105,6 +110,77 @@ def read_tiff_gray(path):
             raise ValueError(f"TIFF compression {comp} not supported")
     dt = np.uint8 if bps == 8 else np.dtype(e + "u2")
     return np.frombuffer(bytes(data), dtype=dt)[: w * h].reshape(h, w).copy()
+
+
+def tiff_strips(path, first_strips=None):
+    """(width, height, bits, compression, rows_per_strip, [strip bytes]) of a TIFF's first page."""
+    b = Path(path).read_bytes()
+    e = "<" if b[:2] == b"II" else ">"
+    (off,) = struct.unpack(e + "I", b[4:8])
+    (n,) = struct.unpack(e + "H", b[off:off + 2])
+    tags = {}
+    for k in range(n):
+        ent = b[off + 2 + 12 * k: off + 14 + 12 * k]
+        t, typ, cnt = struct.unpack(e + "HHI", ent[:8])
+        if typ not in (3, 4):
+            continue
+        size = 2 if typ == 3 else 4
+        fmt = e + ("H" if typ == 3 else "I") * cnt
+        if cnt * size <= 4:
+            tags[t] = list(struct.unpack(fmt, ent[8:8 + cnt * size]))
+        else:
+            (ptr,) = struct.unpack(e + "I", ent[8:12])
+            tags[t] = list(struct.unpack(fmt, b[ptr:ptr + cnt * size]))
+    offs, counts = tags[273], tags[279]
+    if first_strips is not None:
+        offs, counts = offs[:first_strips], counts[:first_strips]
+    rps = tags.get(278, [tags[257][0]])[0]
+    return tags[256][0], tags[257][0], tags[258][0], tags[259][0], rps, [b[o:o + c] for o, c in zip(offs, counts)]
+
+
+def write_min_tiff(dst, width, height, bits, compression, rows_per_strip, strips):
+    """Little-endian TIFF with one directory (size, bits, compression, BlackIsZero, strips)."""
+    ns = len(strips)
+    entries = 9
+    ifd = 8
+    arrays = ifd + 2 + 12 * entries + 4
+    data = arrays + 8 * ns
+    offs, pos = [], data
+    for s in strips:
+        offs.append(pos)
+        pos += len(s)
+    out = bytearray(b"II" + struct.pack("<HI", 42, ifd))
+    out += struct.pack("<H", entries)
+
+    def tag(t, typ, cnt, value):
+        return struct.pack("<HHI", t, typ, cnt) + value
+
+    strip_off = struct.pack("<I", offs[0]) if ns == 1 else struct.pack("<I", arrays)
+    strip_cnt = struct.pack("<I", len(strips[0])) if ns == 1 else struct.pack("<I", arrays + 4 * ns)
+    out += tag(256, 4, 1, struct.pack("<I", width))
+    out += tag(257, 4, 1, struct.pack("<I", height))
+    out += tag(258, 3, 1, struct.pack("<HH", bits, 0))
+    out += tag(259, 3, 1, struct.pack("<HH", compression, 0))
+    out += tag(262, 3, 1, struct.pack("<HH", 1, 0))
+    out += tag(273, 4, ns, strip_off)
+    out += tag(277, 3, 1, struct.pack("<HH", 1, 0))
+    out += tag(278, 4, 1, struct.pack("<I", rows_per_strip))
+    out += tag(279, 4, ns, strip_cnt)
+    out += struct.pack("<I", 0)
+    out += struct.pack(f"<{ns}I", *offs) + struct.pack(f"<{ns}I", *[len(s) for s in strips])
+    for s in strips:
+        out += s
+    Path(dst).write_bytes(bytes(out))
+
+
+def tiff_fixtures(ref):
+    ref = Path(ref)
+    w, h, bits, comp, rps, strips = tiff_strips(ref / "testFiles/rankine_vortex01_0.tif", first_strips=4)
+    assert comp == 32773 and rps == 16
+    write_min_tiff(HERE / "tiff_packbits_rankine.tif", w, 4 * rps, bits, comp, rps, strips)
+    w, h, bits, comp, rps, strips = tiff_strips(ref / "testFiles/coordTestChessA.tif")
+    assert comp == 5 and len(strips) == 1
+    write_min_tiff(HERE / "tiff_lzw_chess.tif", w, h, bits, comp, rps, strips)
 
 
 def read_png_gray(path):
@@ -240,6 +316,7 @@ def main(ref):
     np.savez_compressed(HERE / "dense_golden.npz", **{f"lk_{k}": lk[k] for k in keep_lk},
                         **{f"ls_{k}": ls[k] for k in keep_ls})
     np.savez_compressed(HERE / "gauss_kat.npz", cases=gauss_kat_cases(ref))
+    tiff_fixtures(ref)
     print("shapes:", a.shape, b.shape, i1.shape, i2.shape, [m.shape for m in fm1], [m.shape for m in fm2],
           fn1, fn2, src0.shape, len(keep_lk), len(keep_ls))
 
@@ -247,5 +324,8 @@ def main(ref):
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "--gauss-kat-only":
         np.savez_compressed(HERE / "gauss_kat.npz", cases=gauss_kat_cases(sys.argv[1]))
+        sys.exit(0)
+    if len(sys.argv) > 2 and sys.argv[2] == "--tiff-only":
+        tiff_fixtures(sys.argv[1])
         sys.exit(0)
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

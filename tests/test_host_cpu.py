@@ -41,7 +41,8 @@ def test_ctypes_structs_match_header(qp, tmp_path):
                "qlpiv_adaptive_desc": qp.AdaptiveDesc, "qlpiv_flow_desc": qp.FlowDesc,
                "qlpiv_stage_time": qp.StageTime, "qlpiv_params": qp.Params,
                "qlpiv_server_params": qp.ServerParams, "qlpiv_request": qp.Request, "qlpiv_result": qp.Result,
-               "qlpiv_server_stats": qp.ServerStats}
+               "qlpiv_server_stats": qp.ServerStats, "qlpiv_mat_export_params": qp.MatExportParams,
+               "qlpiv_mat_velocity_map": qp.MatVelocityMap}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "qlpiv.h"', "int main(void) {"]
     for name, cls in mirrors.items():
         lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
