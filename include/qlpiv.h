@@ -151,6 +151,16 @@ typedef enum {
     QLPIV_WARP_BOTH_MINI = 9
 } qlpiv_warp_mode;
 
+/* Velocity inheritance between adaptive levels (InterAreaVelocityStrategiesFactoryEnum,
+ * S/iareas/InterAreaVelocityStrategiesFactoryEnum.java:12-29). */
+typedef enum {
+    QLPIV_INHERIT_BICUBIC_SPLINE = 0, /* AdaptiveInterVelocityInheritanceStrategyBiCubicSpline */
+    QLPIV_INHERIT_DIRECT = 1,         /* ...StrategyDirect: child (2i + a, 2j + b) <- parent (i, j) */
+    QLPIV_INHERIT_AREA = 2,           /* ...StrategyArea: overlap-area weighted parents */
+    QLPIV_INHERIT_DISTANCE = 3        /* ...StrategyDistanceGeneric: inverse-distance weighted
+                                         surrounding parents */
+} qlpiv_inherit_mode;
+
 /* Adaptive multi-pass PIV parameters (PIVInputParameters fields of the path). */
 typedef struct qlpiv_adaptive_desc {
     int ia_start;          /* IA side of the first level (getInterrogationAreaStartIPixels) */
@@ -173,7 +183,8 @@ typedef struct qlpiv_adaptive_desc {
     int iterate_until_no_corrections;   /* VectorValidatorConfiguration */
     int subpix_pixels;     /* as qlpiv_pass_desc */
     int subpix_iterations; /* as qlpiv_pass_desc */
-    int reserved[3];
+    int inherit_mode;      /* qlpiv_inherit_mode (getVelocityInheritanceStrategy) */
+    int reserved[2];
 } qlpiv_adaptive_desc;
 
 /* Vector validation after each level (VectorValidatorJob, S/jobs/validator/VectorValidatorJob.java:242-405). */
@@ -291,6 +302,15 @@ qlpiv_status qlpiv_adaptive_levels(const qlpiv_adaptive_desc *desc, int height, 
 qlpiv_status qlpiv_inherit(qlpiv_handle *h, int pni, int pnj, const double *p_ci, const double *p_cj, const float *pu,
                            const float *pv, int cni, int cnj, const float *c_ci, const float *c_cj, int round_int,
                            float *cu, float *cv);
+
+/* Velocity inheritance with the Direct, Area or Distance strategy
+ * (S/iareas/AdaptiveInterVelocityInheritanceStrategy{Direct,Area,DistanceGeneric}.java): parent
+ * grid (side pn, rows p_tops[pni], columns p_lefts[pnj]) with displacements pu/pv, child grid
+ * (side cn, c_tops[cni], c_lefts[cnj]); round_int for non-warping modes.  Geometries on which
+ * the reference's walk throws are rejected with QLPIV_E_SHAPE.  Host arrays. */
+qlpiv_status qlpiv_inherit_tiles(qlpiv_handle *h, int mode, int pn, int pni, int pnj, const int32_t *p_tops,
+                                 const int32_t *p_lefts, const float *pu, const float *pv, int cn, int cni, int cnj,
+                                 const int32_t *c_tops, const int32_t *c_lefts, int round_int, float *cu, float *cv);
 
 /* Per-pixel displacement field of a level (BiCubicSplineInterpolatorWithBiLinearBackup.
  * interpolateDisplacements, S/iareas/BiCubicSplineInterpolatorWithBiLinearBackup.java:57-107):

@@ -97,8 +97,13 @@ def lib():
         L.orc_mp_list_run.argtypes = [c_int, c_int, c_int, fp, ip, ip, fp, ip, ip]
         L.orc_spiral_order.argtypes = [c_int, c_int, ip]
         L.orc_validate.argtypes = [c_int, c_int, ip, ip, fp, fp, fp, fp, ip, c_int, ctypes.POINTER(ValidCfg), vp]
-        L.orc_piv_adaptive_ex.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_float,
+        L.orc_piv_adaptive_ex.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_int,
+                                          c_float,
                                           c_int, c_int, c_int, ctypes.POINTER(ValidCfg), fp, fp, ip, ip, vp, vp, vp]
+        L.orc_inherit_tiles.argtypes = [c_int, c_int, c_int, c_int, ip, ip, fp, fp, c_int, c_int, c_int, ip, ip, c_int,
+                                        fp, fp]
+        L.orc_area_overlap.argtypes = [c_int, c_int, c_int, c_int, c_int, c_int, ip]
+        L.orc_area_overlap.restype = c_float
         L.orc_gauss_kernel.argtypes = [c_float, c_int, fp]
         L.orc_gauss_filter.argtypes = [fp, c_int, c_int, fp, c_int, fp]
         L.orc_normalize.argtypes = [fp, c_long, fp]
@@ -344,8 +349,38 @@ def inherit(py, px, pu, pv, cy, cx, round_int=False, precision=32):
     return cu, cv
 
 
+INHERIT_BICUBIC_SPLINE, INHERIT_DIRECT, INHERIT_AREA, INHERIT_DISTANCE = range(4)
+
+
+def inherit_tiles(mode, pn, p_tops, p_lefts, pu, pv, cn, c_tops, c_lefts, round_int=False):
+    """Direct / Area / Distance inheritance by the reference's serial walk; raises ValueError
+    where the reference throws."""
+    p_tops = np.ascontiguousarray(p_tops, np.int32)
+    p_lefts = np.ascontiguousarray(p_lefts, np.int32)
+    c_tops = np.ascontiguousarray(c_tops, np.int32)
+    c_lefts = np.ascontiguousarray(c_lefts, np.int32)
+    pu, pv = _f32(pu), _f32(pv)
+    cu = np.zeros((len(c_tops), len(c_lefts)), np.float32)
+    cv = np.zeros_like(cu)
+    rc = lib().orc_inherit_tiles(mode, pn, len(p_tops), len(p_lefts), _ptr(p_tops, ctypes.c_int),
+                                 _ptr(p_lefts, ctypes.c_int), _ptr(pu, ctypes.c_float), _ptr(pv, ctypes.c_float), cn,
+                                 len(c_tops), len(c_lefts), _ptr(c_tops, ctypes.c_int), _ptr(c_lefts, ctypes.c_int),
+                                 int(round_int), _ptr(cu, ctypes.c_float), _ptr(cv, ctypes.c_float))
+    if rc != 0:
+        raise ValueError(f"the reference's inheritance walk throws here (code {rc})")
+    return cu, cv
+
+
+def area_overlap(parent_top, parent_left, pn, top, left, n):
+    """checkOverlappingFactor: (factor, up, down, left, right)."""
+    fl = ctypes.c_int()
+    f = lib().orc_area_overlap(parent_top, parent_left, pn, top, left, n, ctypes.byref(fl))
+    return float(f), bool(fl.value & 1), bool(fl.value & 2), bool(fl.value & 4), bool(fl.value & 8)
+
+
 def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MAX_A, fixed_max=None,
-                 int16_quirk=False, precision=32, nthreads=None, return_levels=False, warp=True, validation=None):
+                 int16_quirk=False, precision=32, nthreads=None, return_levels=False, warp=True, validation=None,
+                 inherit=INHERIT_BICUBIC_SPLINE):
     """Adaptive multi-pass PIV (warp: False none, True BothImages bilinear, or a micro / mini mode
     4..9 as WARP_*); returns (u, v) of
     the last level, shaped (tiles_i, tiles_j), and optionally all levels' vectors.
@@ -370,7 +405,8 @@ def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MA
     linv = np.zeros(total, np.uint8) if return_levels else None
     cfg = validation if validation is not None else ValidCfg(0, 0, 0, 0.0, 0.0, 0, 0)
     rc = lib().orc_piv_adaptive_ex(img_a.ctypes.data, img_b.ctypes.data, h, w, img_a.dtype.itemsize, n_start, n_end,
-                                   overlap_factor, int(warp), norm_mode, float(fixed_max or 0.0), int(int16_quirk),
+                                   overlap_factor, int(warp), int(inherit), norm_mode, float(fixed_max or 0.0),
+                                   int(int16_quirk),
                                    0 if precision == 32 else 1, nthreads or (os.cpu_count() or 1), ctypes.byref(cfg),
                                    _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), ctypes.byref(ni),
                                    ctypes.byref(nj), vec.ctypes.data if vec is not None else None,

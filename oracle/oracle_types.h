@@ -59,6 +59,10 @@ int orc_piv_pass_multi(const void *img_a, const void *img_b, int h, int w, int p
                        float fixed_max_a, float fixed_max_b, int subpix, int precision, int kw, int k,
                        orc_vector *out, int *npeaks, int nthreads);
 int orc_spiral_order(int ni, int nj, int *order);
+float orc_area_overlap(int pt, int pl, int pn, int ct, int cl, int cn, int *flags);
+int orc_inherit_tiles(int mode, int pn, int pni, int pnj, const int *ptops, const int *plefts, const float *pu,
+                      const float *pv, int cn, int cni, int cnj, const int *ctops, const int *clefts, int round_int,
+                      float *cu, float *cv);
 int orc_validate(int ni, int nj, const int *tops, const int *lefts, float *u, float *v, const float *pu,
                  const float *pv, const int *npeaks, int k, const orc_valid_cfg *cfg, unsigned char *invalid_out);
 

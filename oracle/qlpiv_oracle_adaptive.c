@@ -18,6 +18,7 @@
  *            5x5 knot window around the point, Akima splines (Akima 1970) along the first
  *            coordinate for each of the 5 second-coordinate knots, then one along the
  *            second coordinate; end derivatives from the parabola through 3 knots.
+ *            The Direct / Area / Distance strategies are in qlpiv_oracle_inherit.c.
  *  B-warp    BiLinearImageWarpingStrategy.doBiLinearWarp / warpPixelOnImage
  *            (S/images/BiLinearImageWarpingStrategy.java:143-265), BothImages mode: the
  *            field is halved, image A sampled at (i-u, j-v), image B at (i+u, j+v).
@@ -367,7 +368,8 @@ void orc_inherit(const double *py, int pni, const double *px, int pnj, const flo
  * Outputs the last level's displacement (u rows, v columns) and, optionally, every
  * level's vectors concatenated (level_vectors, sized by the caller). */
 int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n_start, int n_end,
-                        float overlap_factor, int warp_mode, int norm_mode, float fixed_max, int int16_quirk,
+                        float overlap_factor, int warp_mode, int inherit_mode, int norm_mode, float fixed_max,
+                        int int16_quirk,
                         int precision, int nthreads, const orc_valid_cfg *val, float *out_u, float *out_v, int *out_ni,
                         int *out_nj, orc_vector *level_vectors, float *level_uv, unsigned char *level_invalid) {
     const int validate = val != NULL && val->enabled;
@@ -407,7 +409,14 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
             double *pyd = (double *)malloc(sizeof(double) * pni), *pxd = (double *)malloc(sizeof(double) * pnj);
             for (int i = 0; i < pni; i++) pyd[i] = (double)((float)ptops[i] + (float)pn / 2.0f - 0.5f);
             for (int j = 0; j < pnj; j++) pxd[j] = (double)((float)plefts[j] + (float)pn / 2.0f - 0.5f);
-            orc_inherit(pyd, pni, pxd, pnj, pu, pv, cyf, ni, cxf, nj, warp_mode == 0, precision, cu, cv);
+            if (inherit_mode == 0) {
+                orc_inherit(pyd, pni, pxd, pnj, pu, pv, cyf, ni, cxf, nj, warp_mode == 0, precision, cu, cv);
+            } else if (orc_inherit_tiles(inherit_mode, pn, pni, pnj, ptops, plefts, pu, pv, n, ni, nj, tops, lefts,
+                                         warp_mode == 0, cu, cv) != 0) {
+                free(pyd); free(pxd); free(cu); free(cv); free(cyd); free(cxd); free(cyf); free(cxf);
+                rc = -3;
+                break;
+            }
             free(pyd); free(pxd);
             if (per_tile) {
                 wta = (float *)malloc(sizeof(float) * cnt * n * n);
@@ -499,7 +508,7 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
 int orc_piv_adaptive(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n_start, int n_end,
                      float overlap_factor, int warp_mode, int norm_mode, float fixed_max, int int16_quirk, int precision,
                      int nthreads, float *out_u, float *out_v, int *out_ni, int *out_nj, orc_vector *level_vectors) {
-    return orc_piv_adaptive_ex(img_a, img_b, h, w, pix_bytes, n_start, n_end, overlap_factor, warp_mode, norm_mode,
+    return orc_piv_adaptive_ex(img_a, img_b, h, w, pix_bytes, n_start, n_end, overlap_factor, warp_mode, 0, norm_mode,
                                fixed_max, int16_quirk, precision, nthreads, NULL, out_u, out_v, out_ni, out_nj,
                                level_vectors, NULL, NULL);
 }

@@ -79,12 +79,13 @@ class AdaptiveDesc(ctypes.Structure):
                 ("peak_kernel", ctypes.c_int), ("median_threshold", ctypes.c_float),
                 ("median_epsilon0", ctypes.c_float), ("max_correction_iterations", ctypes.c_int),
                 ("iterate_until_no_corrections", ctypes.c_int), ("subpix_pixels", ctypes.c_int),
-                ("subpix_iterations", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("subpix_iterations", ctypes.c_int), ("inherit_mode", ctypes.c_int), ("reserved", ctypes.c_int * 2)]
 
 
 def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_mode=WARP_BOTH_BILINEAR,
                   norm_mode=NORM_MAX_A, max_mode=MAX_FIXED, fixed_max=0.0, subpix_mode=SUBPIX_GAUSS3,
-                  int16_warp_quirk=False, validation=None, subpix_pixels=3, subpix_iterations=20):
+                  int16_warp_quirk=False, validation=None, subpix_pixels=3, subpix_iterations=20,
+                  inherit_mode=0):
     """Adaptive PIV parameters; the defaults follow the reference's BothImages bilinear
     warping (tiles copied from the warped image keep the full-scale maximum).
     validation: None, or a dict for the multi-peak normalised-median model with keys
@@ -96,6 +97,7 @@ def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_m
     d.warp_mode, d.norm_mode, d.max_mode, d.fixed_max = warp_mode, norm_mode, max_mode, fixed_max
     d.subpix_mode, d.int16_warp_quirk = subpix_mode, int(int16_warp_quirk)
     d.subpix_pixels, d.subpix_iterations = subpix_pixels, subpix_iterations
+    d.inherit_mode = inherit_mode
     if validation is not None:
         set_validation(d, **validation)
     return d
@@ -119,6 +121,7 @@ def set_validation(d, num_peaks=3, peak_kernel=3, threshold=2.0, epsilon0=0.1, m
 
 
 FLOW_LUCAS_KANADE, FLOW_LIU_SHEN = 1, 2
+INHERIT_BICUBIC_SPLINE, INHERIT_DIRECT, INHERIT_AREA, INHERIT_DISTANCE = range(4)
 IGNORE_PIV_NONE, IGNORE_PIV_U, IGNORE_PIV_V, IGNORE_PIV_UV, IGNORE_PIV_AUTO, IGNORE_PIV_AUTO_SMALL = range(6)
 
 
@@ -210,6 +213,7 @@ _SIGNATURES = {
     "qlpiv_grid_nosuperposition": (_i, [_i, _i, _vp, _i, _i, ctypes.POINTER(Grid), _vp, _vp, _i]),
     "qlpiv_adaptive_levels": (_i, [ctypes.POINTER(AdaptiveDesc), _i, _i, ctypes.POINTER(_i), _vp, _i]),
     "qlpiv_inherit": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp]),
+    "qlpiv_inherit_tiles": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),
     "qlpiv_displacement_field": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "qlpiv_warp_pair": (_i, [_vp, _i, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "qlpiv_tile_warp": (_i, [_vp, _i, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _f, _vp, _vp, _vp, _vp]),
@@ -541,6 +545,21 @@ class Handle:
         _check(self._lib.qlpiv_inherit(self._h, len(p_ci), len(p_cj), _addr(p_ci), _addr(p_cj), _addr(pu), _addr(pv),
                                        len(c_ci), len(c_cj), _addr(c_ci), _addr(c_cj), int(round_int), _addr(cu),
                                        _addr(cv)))
+        return cu, cv
+
+    def inherit_tiles(self, mode, pn, p_tops, p_lefts, pu, pv, cn, c_tops, c_lefts, round_int=False):
+        """Direct / Area / Distance velocity inheritance between two grids (host arrays)."""
+        p_tops = np.ascontiguousarray(p_tops, np.int32)
+        p_lefts = np.ascontiguousarray(p_lefts, np.int32)
+        c_tops = np.ascontiguousarray(c_tops, np.int32)
+        c_lefts = np.ascontiguousarray(c_lefts, np.int32)
+        pu = np.ascontiguousarray(pu, np.float32)
+        pv = np.ascontiguousarray(pv, np.float32)
+        cu = np.empty((len(c_tops), len(c_lefts)), np.float32)
+        cv = np.empty_like(cu)
+        _check(self._lib.qlpiv_inherit_tiles(self._h, mode, pn, len(p_tops), len(p_lefts), _addr(p_tops),
+                                             _addr(p_lefts), _addr(pu), _addr(pv), cn, len(c_tops), len(c_lefts),
+                                             _addr(c_tops), _addr(c_lefts), int(round_int), _addr(cu), _addr(cv)))
         return cu, cv
 
     def displacement_field(self, ci, cj, u, v, height, width):

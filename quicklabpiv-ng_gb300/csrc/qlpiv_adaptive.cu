@@ -160,6 +160,90 @@ __global__ void inherit_cols_kernel(int pairs, const float *px, int pnj, const f
     inherit_cols_one(gid, px, pnj, cx, cni, cnj, ru, rv, round_int, cu, cv);
 }
 
+// ---------------- B-inherit: Direct, Area, Distance ----------------
+//
+// The reference walks the child tiles serially, carrying a parent "reference tile" from tile
+// to tile (S/iareas/AdaptiveInterVelocityInheritanceStrategy{Direct,Area,DistanceGeneric}.java).
+// On the regular separable grids of the adaptive levels that walk resolves, per child row and
+// per child column independently, to a parent index range (Area) or a parent index and a side
+// flag (Distance); inherit_tables computes those on the host, rejecting the geometries where
+// the walk throws, and inherit_tiles_kernel evaluates every child tile on its own with the
+// reference's float operations in the walk's order.
+
+__global__ void inherit_tiles_kernel(int pairs, int mode, int pn, int pni, int pnj, const int *ptops,
+                                     const int *plefts, const float *pu, const float *pv, int cn, int cni, int cnj,
+                                     const int *ctops, const int *clefts, const int2 *rows, const int2 *cols,
+                                     int round_int, float *cu, float *cv) {
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long cnt = (long)cni * cnj;
+    if (gid >= (long)pairs * cnt) return;
+    const int pair = (int)(gid / cnt);
+    const long k = gid - (long)pair * cnt;
+    const int i = (int)(k / cnj), j = (int)(k - (long)i * cnj);
+    const float *fu = pu + (long)pair * pni * pnj, *fv = pv + (long)pair * pni * pnj;
+    float du = 0.0f, dv = 0.0f;
+    if (mode == QLPIV_INHERIT_DIRECT) {
+        const int qi = i >> 1, qj = j >> 1;
+        if (qi < pni && qj < pnj) {
+            du = fu[(long)qi * pnj + qj];
+            dv = fv[(long)qi * pnj + qj];
+        }
+    } else if (mode == QLPIV_INHERIT_AREA) {
+        const int2 R = rows[i], C = cols[j];
+        const int ct = ctops[i], cl = clefts[j];
+        float acc = 0.0f;
+        for (int r = R.x; r <= R.y; r++) {
+            const int vo = span_overlap(ptops[r], pn, ct, cn);
+            for (int c = C.x; c <= C.y; c++) acc += (float)(vo * span_overlap(plefts[c], pn, cl, cn));
+        }
+        for (int r = R.x; r <= R.y; r++) {
+            const int vo = span_overlap(ptops[r], pn, ct, cn);
+            for (int c = C.x; c <= C.y; c++) {
+                const float w = (float)(vo * span_overlap(plefts[c], pn, cl, cn)) / acc;
+                du += w * fu[(long)r * pnj + c];
+                dv += w * fv[(long)r * pnj + c];
+            }
+        }
+    } else {  // Distance: parents (p, q), (p, q + 1), (p + 1, q), (p + 1, q + 1) in that order
+        const int2 R = rows[i], C = cols[j];
+        const float ccy = (float)ctops[i] + (float)cn / 2.0f, ccx = (float)clefts[j] + (float)cn / 2.0f;
+        const bool has_r = C.x + 1 < pnj && !C.y, has_d = R.x + 1 < pni && !R.y;
+        int qi[4], qj[4];
+        float dist[4];
+        bool ok[4] = {true, has_r, has_d, has_r && has_d};
+        int zero = -1;
+        float total = 0.0f;
+        for (int a = 0; a < 4; a++) {
+            qi[a] = R.x + (a >> 1);
+            qj[a] = C.x + (a & 1);
+            if (!ok[a]) continue;
+            const float py = (float)ptops[qi[a]] + (float)pn / 2.0f, px = (float)plefts[qj[a]] + (float)pn / 2.0f;
+            const double dx = (double)(ccx - px), dy = (double)(ccy - py);
+            dist[a] = (float)sqrt(dx * dx + dy * dy);
+            if (zero < 0 && dist[a] == 0.0f) zero = a;
+        }
+        if (zero >= 0) {
+            du = fu[(long)qi[zero] * pnj + qj[zero]];
+            dv = fv[(long)qi[zero] * pnj + qj[zero]];
+        } else {
+            for (int a = 0; a < 4; a++)
+                if (ok[a]) total += 1.0f / dist[a];
+            for (int a = 0; a < 4; a++) {
+                if (!ok[a]) continue;
+                const float w = (1.0f / dist[a]) / total;
+                du += w * fu[(long)qi[a] * pnj + qj[a]];
+                dv += w * fv[(long)qi[a] * pnj + qj[a]];
+            }
+        }
+    }
+    if (round_int) {
+        du = (float)java_round(du);
+        dv = (float)java_round(dv);
+    }
+    cu[gid] = 0.0f + du;
+    cv[gid] = 0.0f + dv;
+}
+
 // ---------------- B-field spline set-up ----------------
 
 // cp[i] of the natural-spline tridiagonal elimination for knots v[n].
@@ -584,6 +668,18 @@ cudaError_t launch_inherit(cudaStream_t s, int pairs, const float *py, int pni, 
     const long nr = (long)pairs * cni * pnj;
     inherit_rows_kernel<<<blocks_for(nr, 128), 128, 0, s>>>(pairs, py, pni, pnj, pu, pv, cy, cni, ru, rv);
     inherit_cols_kernel<<<blocks_for(n, 128), 128, 0, s>>>(pairs, px, pnj, cx, cni, cnj, ru, rv, round_int, cu, cv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_inherit_tiles(cudaStream_t s, int pairs, int mode, int pn, int pni, int pnj, const int *ptops,
+                                 const int *plefts, const float *pu, const float *pv, int cn, int cni, int cnj,
+                                 const int *ctops, const int *clefts, const int2 *tables, int round_int, float *cu,
+                                 float *cv) {
+    const long n = (long)pairs * cni * cnj;
+    if (n == 0) return cudaSuccess;
+    inherit_tiles_kernel<<<blocks_for(n, 128), 128, 0, s>>>(pairs, mode, pn, pni, pnj, ptops, plefts, pu, pv, cn, cni,
+                                                              cnj, ctops, clefts, tables, tables + cni, round_int, cu,
+                                                              cv);
     return cudaGetLastError();
 }
 

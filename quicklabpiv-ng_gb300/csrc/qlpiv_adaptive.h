@@ -20,6 +20,26 @@ struct SplineCoef {
 cudaError_t launch_inherit(cudaStream_t s, int pairs, const float *py, int pni, const float *px, int pnj,
                            const float *pu, const float *pv, const float *cy, int cni, const float *cx, int cnj,
                            int round_int, float *ru, float *rv, float *cu, float *cv);
+// Vertical (or horizontal) overlap in pixels of the child span [c, c + cn) with the parent span
+// [p, p + pn), in checkOverlappingFactor's branch form (Area.java:222-299).
+__host__ __device__ __forceinline__ int span_overlap(int p, int pn, int c, int cn) {
+    if (p <= c) {
+        if (p + pn > c) {
+            int end = c + cn;
+            if (end - 1 >= p + pn) end = p + pn;
+            return end - c;
+        }
+        return 0;
+    }
+    return c + cn > p ? c + cn - p : 0;
+}
+
+// Direct / Area / Distance inheritance (mode: qlpiv_inherit_mode); tables: cni row entries then
+// cnj column entries built by inherit_tables (qlpiv_pipeline.cu).
+cudaError_t launch_inherit_tiles(cudaStream_t s, int pairs, int mode, int pn, int pni, int pnj, const int *ptops,
+                                 const int *plefts, const float *pu, const float *pv, int cn, int cni, int cnj,
+                                 const int *ctops, const int *clefts, const int2 *tables, int round_int, float *cu,
+                                 float *cv);
 // cpy/cpx: scratch of ni/nj doubles for the elimination factors.
 cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const double *cpy, int ni, const double *xs,
                           const double *cpx, int nj, const float *u, const float *v, SplineCoef coef);

@@ -36,6 +36,7 @@ struct LevelPlan {
     DevBuf d_u, d_v;                       // tile displacements, pairs x count
     DevBuf coef;                           // 6 doubles + 2 float4 per tile and pair
     DevBuf d_rows;                         // inheritance stage 1: 2 x pairs x tiles_i x parent tiles_j
+    DevBuf d_inh;                          // Direct / Area / Distance tables: tiles_i + tiles_j int2
     // validation (allocated only when the descriptor asks for it)
     DevBuf d_tops, d_lefts, d_order, d_rank;  // grid rows / columns, spiral order and rank
     DevBuf d_bu, d_bv, d_puv, d_npk, d_state, d_list, d_done, d_sweeps;
@@ -59,7 +60,7 @@ void destroy_plan(AdaptivePlan *p) {
     if (!p) return;
     for (LevelPlan &l : p->levels)
         for (DevBuf *b : {&l.d_cy, &l.d_cx, &l.d_cyf, &l.d_cxf, &l.d_cpy, &l.d_cpx, &l.d_fi, &l.d_at, &l.d_al, &l.d_bt,
-                          &l.d_bl, &l.d_u, &l.d_v, &l.coef, &l.d_rows, &l.d_tops, &l.d_lefts, &l.d_order,
+                          &l.d_bl, &l.d_u, &l.d_v, &l.coef, &l.d_rows, &l.d_inh, &l.d_tops, &l.d_lefts, &l.d_order,
                           &l.d_rank, &l.d_bu, &l.d_bv, &l.d_puv, &l.d_npk, &l.d_state, &l.d_list, &l.d_done,
                           &l.d_sweeps, &l.d_tiles, &l.d_tmax})
             b->release();
@@ -102,6 +103,8 @@ static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type,
     if (d->max_mode != QLPIV_MAX_COMPUTE && d->max_mode != QLPIV_MAX_FIXED)
         return fail(QLPIV_E_ARG, "max mode %d not valid for adaptive PIV", d->max_mode);
     if (qlpiv_status st = check_subpix(d->subpix_mode, d->subpix_pixels, d->subpix_iterations)) return st;
+    if (d->inherit_mode < QLPIV_INHERIT_BICUBIC_SPLINE || d->inherit_mode > QLPIV_INHERIT_DISTANCE)
+        return fail(QLPIV_E_ARG, "unknown velocity inheritance mode %d", d->inherit_mode);
     if (!(d->overlap_factor >= 0.1f && d->overlap_factor <= 0.9f))
         return fail(QLPIV_E_ARG, "Overlap factor must greater than 1/10 and less than 9/10");
     if (d->validation != QLPIV_VALIDATE_NONE && d->validation != QLPIV_VALIDATE_MULTIPEAK_MEDIAN)
@@ -116,6 +119,73 @@ static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type,
         if (d->max_correction_iterations < 0) return fail(QLPIV_E_ARG, "max correction iterations < 0");
     }
     return QLPIV_OK;
+}
+
+// Per child row and per child column tables of the Direct / Area / Distance inheritance
+// (cni row entries, then cnj column entries; Direct needs none).  The reference's serial walk
+// keeps a parent reference row across child rows and a reference column that restarts at 0 on
+// every child row; on separable grids both advance independently:
+//   Area      (first, last) parent index overlapping the child span.  The walk moves the
+//             reference by one parent per child tile before scanning, and throws when one move
+//             is not enough, when the child lies before the reference, or when a row move and a
+//             column move fall on the same tile (Area.java:76-104, 121-131).
+//   Distance  (p, past): p the last parent whose centre is at or before the child centre (0
+//             when none is, the last parent at most), past = the centre of parent p lies after
+//             the child centre (DistanceGeneric.java:77-166, 168-176).
+static qlpiv_status inherit_tables(int mode, int pn, int pni, int pnj, const int32_t *ptops, const int32_t *plefts,
+                                   int cn, int cni, int cnj, const int32_t *ctops, const int32_t *clefts,
+                                   std::vector<int2> &tab) {
+    tab.assign((size_t)cni + cnj, make_int2(0, 0));
+    if (mode == QLPIV_INHERIT_DIRECT) {
+        if (cni < 2 * pni || cnj < 2 * pnj)
+            return fail(QLPIV_E_SHAPE, "Direct inheritance needs at least 2 x %d by 2 x %d child tiles, got %d x %d",
+                        pni, pnj, cni, cnj);
+        return QLPIV_OK;
+    }
+    if (mode == QLPIV_INHERIT_AREA) {
+        // relation of a parent span to a child span: 0 overlap, +1 parent before, -1 parent after
+        auto rel = [&](int p, int c) { return span_overlap(p, pn, c, cn) > 0 ? 0 : (p <= c ? 1 : -1); };
+        bool row_moved = false, col0_moved = false;
+        for (int axis = 0; axis < 2; axis++) {
+            const int np = axis == 0 ? pni : pnj, nc = axis == 0 ? cni : cnj;
+            const int32_t *ps = axis == 0 ? ptops : plefts, *cs = axis == 0 ? ctops : clefts;
+            int ref = 0;
+            for (int k = 0; k < nc; k++) {
+                int r = rel(ps[ref], cs[k]);
+                if (r < 0) return fail(QLPIV_E_SHAPE, "Area inheritance: child tile %d lies before its parent", k);
+                if (r > 0) {
+                    if (ref + 1 == np) return fail(QLPIV_E_SHAPE, "Area inheritance: no parent tile past child %d", k);
+                    ref++;
+                    if (axis == 0) row_moved = true;
+                    else if (k == 0) col0_moved = true;
+                    if (rel(ps[ref], cs[k]) != 0)
+                        return fail(QLPIV_E_SHAPE, "Area inheritance: child %d skips a parent tile", k);
+                }
+                int last = ref;
+                while (last + 1 < np && rel(ps[last + 1], cs[k]) == 0) last++;
+                tab[(size_t)(axis == 0 ? k : cni + k)] = make_int2(ref, last);
+            }
+        }
+        if (row_moved && col0_moved)
+            return fail(QLPIV_E_SHAPE, "Area inheritance: reference tile moves right and down at once");
+        return QLPIV_OK;
+    }
+    if (mode == QLPIV_INHERIT_DISTANCE) {
+        const float half_p = (float)pn / 2.0f, half_c = (float)cn / 2.0f;
+        for (int axis = 0; axis < 2; axis++) {
+            const int np = axis == 0 ? pni : pnj, nc = axis == 0 ? cni : cnj;
+            const int32_t *ps = axis == 0 ? ptops : plefts, *cs = axis == 0 ? ctops : clefts;
+            int ref = 0;
+            for (int k = 0; k < nc; k++) {
+                const float c = (float)cs[k] + half_c;
+                while (ref + 1 < np && (float)ps[ref + 1] + half_p <= c) ref++;
+                const int past = (float)ps[ref] + half_p > c ? 1 : 0;
+                tab[(size_t)(axis == 0 ? k : cni + k)] = make_int2(ref, past);
+            }
+        }
+        return QLPIV_OK;
+    }
+    return fail(QLPIV_E_ARG, "inheritance mode %d has no tables", mode);
 }
 
 // Spiral visit order of a grid and the rank of every tile in it.
@@ -215,6 +285,15 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
         if ((e = upload(L.d_tops, L.tops.data(), sizeof(int32_t) * ni, s)) != cudaSuccess ||
             (e = upload(L.d_lefts, L.lefts.data(), sizeof(int32_t) * nj, s)) != cudaSuccess)
             return cuda_fail(e, "grid upload");
+        std::vector<int2> inh;
+        if (lv > 0 && d->inherit_mode != QLPIV_INHERIT_BICUBIC_SPLINE) {
+            const LevelPlan &P = p->levels[lv - 1];
+            if (qlpiv_status st = inherit_tables(d->inherit_mode, P.g.n, P.g.tiles_i, P.g.tiles_j, P.tops.data(),
+                                                 P.lefts.data(), n, ni, nj, L.tops.data(), L.lefts.data(), inh))
+                return st;
+            if ((e = upload(L.d_inh, inh.data(), sizeof(int2) * inh.size(), s)) != cudaSuccess)
+                return cuda_fail(e, "inheritance tables");
+        }
         std::vector<int32_t> order, rank;
         if (d->validation != QLPIV_VALIDATE_NONE) {
             spiral_rank(ni, nj, order, rank);
@@ -313,14 +392,20 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
                 return cuda_fail(e, "level 0 reset");
         } else {
             LevelPlan &P = p->levels[lv - 1];
-            StageScope sc(h, "inherit", (int)lv, L.g.n, 2, total);
+            const bool spline = d.inherit_mode == QLPIV_INHERIT_BICUBIC_SPLINE;
+            StageScope sc(h, "inherit", (int)lv, L.g.n, spline ? 2 : 1, total);
             float *ru = L.d_rows.as<float>(), *rv = ru + (long)pairs * L.g.tiles_i * P.g.tiles_j;
-            if ((e = launch_inherit(s, pairs, P.d_cyf.as<float>(), P.g.tiles_i, P.d_cxf.as<float>(), P.g.tiles_j,
-                                    P.d_u.as<float>(), P.d_v.as<float>(), L.d_cyf.as<float>(), L.g.tiles_i,
-                                    L.d_cxf.as<float>(), L.g.tiles_j, d.warp_mode == QLPIV_WARP_NONE, ru, rv, u,
-                                    v)) != cudaSuccess)
-                return cuda_fail(e, "inheritance");
-            h->launches += 2;
+            if (spline)
+                e = launch_inherit(s, pairs, P.d_cyf.as<float>(), P.g.tiles_i, P.d_cxf.as<float>(), P.g.tiles_j,
+                                   P.d_u.as<float>(), P.d_v.as<float>(), L.d_cyf.as<float>(), L.g.tiles_i,
+                                   L.d_cxf.as<float>(), L.g.tiles_j, d.warp_mode == QLPIV_WARP_NONE, ru, rv, u, v);
+            else
+                e = launch_inherit_tiles(s, pairs, d.inherit_mode, P.g.n, P.g.tiles_i, P.g.tiles_j, P.d_tops.as<int>(),
+                                         P.d_lefts.as<int>(), P.d_u.as<float>(), P.d_v.as<float>(), L.g.n,
+                                         L.g.tiles_i, L.g.tiles_j, L.d_tops.as<int>(), L.d_lefts.as<int>(),
+                                         L.d_inh.as<int2>(), d.warp_mode == QLPIV_WARP_NONE, u, v);
+            if (e != cudaSuccess) return cuda_fail(e, "inheritance");
+            h->launches += spline ? 2 : 1;
         }
         const qlpiv_frame *src = frames_dev;
         const int *bt = L.d_at.as<int>(), *bl = L.d_al.as<int>();
@@ -481,6 +566,7 @@ size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int heigh
         total += al(8 * ni) + al(8 * nj) + al(4 * ni) + al(4 * nj) + al(8 * ni) + al(8 * nj);
         total += 5 * al(4 * tot) + 2 * al(4 * tot) + al(coef_bytes((long)tot));
         if (lv > 0) total += al(8 * (size_t)pairs * ni * prev_nj);
+        if (lv > 0 && d->inherit_mode != QLPIV_INHERIT_BICUBIC_SPLINE) total += al(8 * (ni + nj));
         total += al(4 * ni) + al(4 * nj);
         if (per_tile_warp(d->warp_mode) && lv > 0)
             total += al(2 * tot * g.n * g.n * pixel_bytes(pixel_type)) + al(8 * tot);
@@ -598,6 +684,46 @@ qlpiv_status qlpiv_inherit(qlpiv_handle *h, int pni, int pnj, const double *p_ci
                             out, out + cc)) != cudaSuccess)
         return cuda_fail(e, "inherit");
     h->launches += 2;
+    if ((e = cudaMemcpyAsync(cu, out, sizeof(float) * cc, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(cv, out + cc, sizeof(float) * cc, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "inherit download");
+    return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_inherit_tiles(qlpiv_handle *h, int mode, int pn, int pni, int pnj, const int32_t *p_tops,
+                                 const int32_t *p_lefts, const float *pu, const float *pv, int cn, int cni, int cnj,
+                                 const int32_t *c_tops, const int32_t *c_lefts, int round_int, float *cu, float *cv) {
+    if (!h || !p_tops || !p_lefts || !pu || !pv || !c_tops || !c_lefts || !cu || !cv)
+        return fail(QLPIV_E_ARG, "NULL argument");
+    if (mode < QLPIV_INHERIT_DIRECT || mode > QLPIV_INHERIT_DISTANCE)
+        return fail(QLPIV_E_ARG, "inheritance mode %d (Direct, Area or Distance)", mode);
+    if (pni < 1 || pnj < 1 || cni < 1 || cnj < 1 || pn < 1 || cn < 1) return fail(QLPIV_E_SHAPE, "empty grid");
+    std::vector<int2> tab;
+    if (qlpiv_status st = inherit_tables(mode, pn, pni, pnj, p_tops, p_lefts, cn, cni, cnj, c_tops, c_lefts, tab))
+        return st;
+    std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope ds(h->device);
+    if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
+    cudaStream_t s = h->stream;
+    const long pc = (long)pni * pnj, cc = (long)cni * cnj;
+    DevBuf *b = h->scratch;
+    cudaError_t e;
+    if ((e = upload(b[0], p_tops, sizeof(int32_t) * pni, s)) != cudaSuccess ||
+        (e = upload(b[1], p_lefts, sizeof(int32_t) * pnj, s)) != cudaSuccess ||
+        (e = upload(b[2], pu, sizeof(float) * pc, s)) != cudaSuccess ||
+        (e = upload(b[3], pv, sizeof(float) * pc, s)) != cudaSuccess ||
+        (e = upload(b[4], c_tops, sizeof(int32_t) * cni, s)) != cudaSuccess ||
+        (e = upload(b[5], c_lefts, sizeof(int32_t) * cnj, s)) != cudaSuccess ||
+        (e = upload(b[7], tab.data(), sizeof(int2) * tab.size(), s)) != cudaSuccess ||
+        (e = b[6].ensure(sizeof(float) * 2 * cc)) != cudaSuccess)
+        return cuda_fail(e, "inherit upload");
+    float *out = b[6].as<float>();
+    if ((e = launch_inherit_tiles(s, 1, mode, pn, pni, pnj, b[0].as<int>(), b[1].as<int>(), b[2].as<float>(),
+                                  b[3].as<float>(), cn, cni, cnj, b[4].as<int>(), b[5].as<int>(), b[7].as<int2>(),
+                                  round_int, out, out + cc)) != cudaSuccess)
+        return cuda_fail(e, "inherit");
+    h->launches += 1;
     if ((e = cudaMemcpyAsync(cu, out, sizeof(float) * cc, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(cv, out + cc, sizeof(float) * cc, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)

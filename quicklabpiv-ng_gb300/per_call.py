@@ -44,8 +44,13 @@ def piv_adaptive_per_call(handle, img_a, img_b, desc):
             u = np.zeros((ni, nj), np.float32)
             v = np.zeros((ni, nj), np.float32)
         else:
-            pcy, pcx, pu, pv = prev
-            u, v = handle.inherit(pcy, pcx, pu, pv, cy, cx, round_int=desc.warp_mode == WARP_NONE)
+            pcy, pcx, pu, pv, pn, ptops, plefts = prev
+            rnd = desc.warp_mode == WARP_NONE
+            if desc.inherit_mode == 0:
+                u, v = handle.inherit(pcy, pcx, pu, pv, cy, cx, round_int=rnd)
+            else:
+                u, v = handle.inherit_tiles(desc.inherit_mode, pn, ptops, plefts, pu, pv, n, tops, lefts,
+                                            round_int=rnd)
         at = np.repeat(tops, nj)
         al = np.tile(lefts, ni)
         src_a, src_b = a, b
@@ -77,5 +82,5 @@ def piv_adaptive_per_call(handle, img_a, img_b, desc):
             k = desc.num_peaks
             u, v, _ = handle.validate(tops, lefts, u, v, vec["u"].reshape(ni, nj, k), vec["v"].reshape(ni, nj, k),
                                       npk, desc)
-        prev = (cy, cx, u, v)
+        prev = (cy, cx, u, v, n, tops, lefts)
     return prev[2], prev[3]
