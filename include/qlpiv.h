@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define QLPIV_ABI_VERSION 2
+#define QLPIV_ABI_VERSION 3
 
 /* Status codes.  The Java shim maps QLPIV_E_SHAPE/QLPIV_E_ARG to JobAnalyzeException
  * (S/jobs/xcorr/CrossCorrelationFFTTemplate.java:594-642 shape checks) and the others
@@ -104,7 +104,7 @@ typedef struct qlpiv_vector {
 
 /* One correlation pass: IA side and tile/peak semantics. */
 typedef struct qlpiv_pass_desc {
-    int n;              /* IA side: 16, 32 or 64 */
+    int n;              /* IA side: 16, 32, 64 or 128 (128: num_peaks 0 only) */
     int norm_mode;      /* qlpiv_norm */
     int max_mode;       /* qlpiv_max_mode */
     float fixed_max_a;  /* QLPIV_MAX_FIXED: max of every A tile */
@@ -481,8 +481,8 @@ qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmp
                                      const qlpiv_frame *frames, const int32_t *ia_size, const float *overlap_factor,
                                      int autotune, qlpiv_mixed_plan **plan);
 /* total_vectors; pair_offset[num_pairs + 1] (the last entry = total); tiles_ij[2 num_pairs]
- * (tiles_i, tiles_j); waves[3]
- * chosen for sizes 16, 32, 64 (0: default).  Any output may be NULL. */
+ * (tiles_i, tiles_j); waves[4]
+ * chosen for sizes 16, 32, 64, 128 (0: default).  Any output may be NULL. */
 qlpiv_status qlpiv_mixed_plan_info(const qlpiv_mixed_plan *plan, int64_t *total_vectors, int64_t *pair_offset,
                                    int32_t *tiles_ij, int32_t *waves);
 /* Queues the plan's graph on the handle's stream; *device_out receives the device vectors. */

@@ -33,7 +33,7 @@ VECTOR_DTYPE = np.dtype([
 ])
 assert VECTOR_DTYPE.itemsize == 32
 
-SUPPORTED_IA = (16, 32, 64)
+SUPPORTED_IA = (16, 32, 64, 128)
 
 _STATUS_NAMES = {OK: "OK", E_ARG: "E_ARG", E_SHAPE: "E_SHAPE", E_OOM: "E_OOM", E_CUDA: "E_CUDA",
                  E_TIMEOUT: "E_TIMEOUT", E_CANCELLED: "E_CANCELLED", E_UNSUPPORTED: "E_UNSUPPORTED",
@@ -265,7 +265,7 @@ def load_library(path=None):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.qlpiv_abi_version() != 2:
+    if lib.qlpiv_abi_version() != 3:
         raise RuntimeError("libqlpiv_gpu.so ABI version mismatch")
     if path is None:
         _lib = lib
@@ -827,7 +827,7 @@ class MixedPlan:
         tot = ctypes.c_int64()
         self.pair_offset = np.empty(self.num_pairs + 1, np.int64)
         self.tiles = np.empty((self.num_pairs, 2), np.int32)
-        self.waves = np.empty(3, np.int32)
+        self.waves = np.empty(4, np.int32)
         _check(self._lib.qlpiv_mixed_plan_info(p, ctypes.byref(tot), _addr(self.pair_offset), _addr(self.tiles),
                                                _addr(self.waves)))
         self.total = tot.value

@@ -8,7 +8,7 @@
 // list of its IA size; the plan launches K1 once per size, each launch on its own branch of the
 // graph so the sizes run concurrently, and the graph is replayed per batch.  The autotuner times
 // each size's launch over its real work list with 1, 2, 4 and 8 waves of resident CTAs and keeps
-// the fastest.  Vectors come out size-major (16, 32, 64) and pair-contiguous inside a size.
+// the fastest.  Vectors come out size-major (16, 32, 64, 128) and pair-contiguous inside a size.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -23,7 +23,8 @@ using namespace qlpiv;
 
 namespace {
 
-constexpr int kSizes[3] = {16, 32, 64};
+constexpr int kNumSizes = 4;
+constexpr int kSizes[kNumSizes] = {16, 32, 64, 128};
 
 struct Group {
     int n = 0;
@@ -40,7 +41,7 @@ struct qlpiv_mixed_plan {
     int device = 0, pixel_type = 0, num_pairs = 0;
     qlpiv_pass_desc tmpl{};
     DevBuf frames, out;
-    Group groups[3];
+    Group groups[kNumSizes];
     std::vector<int64_t> pair_offset;
     std::vector<int32_t> tiles_ij;
     int64_t total = 0;
@@ -107,7 +108,7 @@ qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmp
     p->num_pairs = num_pairs;
     p->tmpl = *tmpl;
     // per size: the flattened work lists (pairs in order, tiles row-major)
-    std::vector<int32_t> lists[3][3];
+    std::vector<int32_t> lists[kNumSizes][3];
     std::vector<int> pair_group(num_pairs);
     std::vector<long> pair_first(num_pairs);
     p->tiles_ij.resize(2 * (size_t)num_pairs);
@@ -115,11 +116,11 @@ qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmp
     for (int q = 0; q < num_pairs; q++) {
         const qlpiv_frame &f = frames[q];
         int gi = -1;
-        for (int k = 0; k < 3; k++)
+        for (int k = 0; k < kNumSizes; k++)
             if (ia_size[q] == kSizes[k]) gi = k;
         if (gi < 0) {
             release(p);
-            return fail(QLPIV_E_SHAPE, "pair %d: IA size %d is not supported (16, 32, 64)", q, ia_size[q]);
+            return fail(QLPIV_E_SHAPE, "pair %d: IA size %d is not supported (16, 32, 64, 128)", q, ia_size[q]);
         }
         if (!f.img_a || !f.img_b || f.height <= 0 || f.width <= 0 || f.pitch < f.width) {
             release(p);
@@ -151,7 +152,7 @@ qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmp
     cudaStream_t s = h->stream;
     cudaError_t e;
     long off = 0;
-    for (int k = 0; k < 3; k++) {
+    for (int k = 0; k < kNumSizes; k++) {
         Group &g = p->groups[k];
         g.n = kSizes[k];
         g.count = (long)lists[k][0].size();
@@ -255,7 +256,7 @@ qlpiv_status qlpiv_mixed_plan_info(const qlpiv_mixed_plan *p, int64_t *total_vec
     if (pair_offset) std::memcpy(pair_offset, p->pair_offset.data(), sizeof(int64_t) * (p->num_pairs + 1));
     if (tiles_ij) std::memcpy(tiles_ij, p->tiles_ij.data(), sizeof(int32_t) * 2 * p->num_pairs);
     if (waves)
-        for (int k = 0; k < 3; k++) waves[k] = p->groups[k].waves;
+        for (int k = 0; k < kNumSizes; k++) waves[k] = p->groups[k].waves;
     return QLPIV_OK;
 }
 

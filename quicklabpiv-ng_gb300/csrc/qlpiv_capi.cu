@@ -64,7 +64,7 @@ namespace {
 qlpiv_status check_desc(const qlpiv_pass_desc *d) {
     if (!d) return fail(QLPIV_E_ARG, "pass descriptor is NULL");
     if (!qlpiv::xcorr_size_supported(d->n))
-        return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64)", d->n);
+        return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64, 128)", d->n);
     if (d->norm_mode != QLPIV_NORM_MAX_A && d->norm_mode != QLPIV_NORM_OWN_MAX && d->norm_mode != QLPIV_NORM_NONE)
         return fail(QLPIV_E_ARG, "unknown normalisation mode %d", d->norm_mode);
     if (d->max_mode != QLPIV_MAX_COMPUTE && d->max_mode != QLPIV_MAX_FIXED)
@@ -104,7 +104,7 @@ qlpiv_status tiles_call(qlpiv_handle *h, int n, long count, int pixel_type, cons
     if (count == 0) return QLPIV_OK;
     if (!ta || !tb) return fail(QLPIV_E_ARG, "tile arrays are NULL");
     if ((max_a == nullptr) != (max_b == nullptr)) return fail(QLPIV_E_ARG, "give both tile max arrays or none");
-    if (!qlpiv::xcorr_size_supported(n)) return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64)", n);
+    if (!qlpiv::xcorr_size_supported(n)) return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64, 128)", n);
     qlpiv_status st = check_pixel(pixel_type);
     if (st != QLPIV_OK) return st;
     if (norm_mode != QLPIV_NORM_MAX_A && norm_mode != QLPIV_NORM_OWN_MAX && norm_mode != QLPIV_NORM_NONE)

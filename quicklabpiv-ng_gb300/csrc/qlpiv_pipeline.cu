@@ -95,7 +95,7 @@ static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type,
     int r = d->ia_start / d->ia_end;
     if ((r & (r - 1)) != 0) return fail(QLPIV_E_ARG, "IA start / end ratio is not a power of two");
     for (int n = d->ia_start; n >= d->ia_end; n >>= 1)
-        if (!xcorr_size_supported(n)) return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64)", n);
+        if (!xcorr_size_supported(n)) return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64, 128)", n);
     if (d->warp_mode != QLPIV_WARP_NONE && d->warp_mode != QLPIV_WARP_BOTH_BILINEAR && !per_tile_warp(d->warp_mode))
         return fail(QLPIV_E_ARG, "unknown warp mode %d", d->warp_mode);
     if (d->norm_mode != QLPIV_NORM_MAX_A && d->norm_mode != QLPIV_NORM_OWN_MAX && d->norm_mode != QLPIV_NORM_NONE)

@@ -7,11 +7,11 @@
 
 namespace qlpiv {
 
-// Twiddle tables exp(-2 pi i e / M) for M = 32, 64, 128 (offsets 0, 32, 96), filled once
-// per device from the host (double precision, rounded to float).
-static __device__ cplx g_twiddles[32 + 64 + 128];
+// Twiddle tables exp(-2 pi i e / M) for M = 32, 64, 128, 256 (offsets 0, 32, 96, 224), filled
+// once per device from the host (double precision, rounded to float).
+static __device__ cplx g_twiddles[32 + 64 + 128 + 256];
 
-static int twiddle_offset(int m) { return m == 32 ? 0 : (m == 64 ? 32 : 96); }
+static int twiddle_offset(int m) { return m == 32 ? 0 : (m == 64 ? 32 : (m == 128 ? 96 : 224)); }
 
 cudaError_t ensure_twiddles(int dev, const cplx **table) {
     static std::mutex mu;
@@ -19,8 +19,8 @@ cudaError_t ensure_twiddles(int dev, const cplx **table) {
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(mu);
     if (addr[dev] == nullptr) {
-        cplx host[32 + 64 + 128];
-        for (int m : {32, 64, 128})
+        cplx host[32 + 64 + 128 + 256];
+        for (int m : {32, 64, 128, 256})
             for (int e = 0; e < m; e++) {
                 const double a = -2.0 * M_PI * (double)e / (double)m;
                 host[twiddle_offset(m) + e] = cplx{(float)std::cos(a), (float)std::sin(a)};
@@ -70,11 +70,31 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
     // every CTA loops over IAs; eight waves of CTAs balance the single-peak kernel best,
     // one resident wave the multi-peak one (its fit queue then fills between flushes)
     long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? 1 : 8));
-    if (grid > job.count) grid = job.count;
+    if (grid > job.count * S::CL) grid = job.count * S::CL;
     if (grid < 1) return cudaSuccess;
     // P-point sub-pixel stencils: 2 P floats per queued fit after the fixed layout
     const size_t smem = S::SMEM + (j.subpix_pixels > 0 ? sizeof(float) * 32 * 2 * j.subpix_pixels : 0);
-    xcorr_kernel<N, Pix, PP><<<(unsigned)grid, S::T, smem, stream>>>(j);
+    if constexpr (S::CL == 1) {
+        xcorr_kernel<N, Pix, PP><<<(unsigned)grid, S::T, smem, stream>>>(j);
+    } else {
+        // one cluster of CL CTAs per IA: the grid is a whole number of clusters
+        grid = (grid + S::CL - 1) / S::CL * S::CL;
+        if (grid > (long)S::CL * job.count) grid = (long)S::CL * job.count;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3(S::T);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = S::CL;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, xcorr_kernel<N, Pix, PP>, j);
+        if (e != cudaSuccess) return e;
+    }
     return cudaGetLastError();
 }
 
@@ -84,6 +104,7 @@ static cudaError_t launch_pix(const IaJob &job, int n, cudaStream_t stream, int 
         case 16: return launch_one<16, Pix, PP>(job, stream, num_sms);
         case 32: return launch_one<32, Pix, PP>(job, stream, num_sms);
         case 64: return launch_one<64, Pix, PP>(job, stream, num_sms);
+        case 128: return launch_one<128, Pix, PP>(job, stream, num_sms);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -103,7 +124,7 @@ cudaError_t launch_xcorr(const IaJob &job, int n, int pixel_type, cudaStream_t s
     }
 }
 
-bool xcorr_size_supported(int n) { return n == 16 || n == 32 || n == 64; }
+bool xcorr_size_supported(int n) { return n == 16 || n == 32 || n == 64 || n == 128; }
 
 template <int N>
 static bool multipeak_fits_n(int kw) {
@@ -116,7 +137,7 @@ bool multipeak_supported(int n, int num_peaks, int peak_kernel) {
         case 16: return multipeak_fits_n<16>(peak_kernel);
         case 32: return multipeak_fits_n<32>(peak_kernel);
         case 64: return multipeak_fits_n<64>(peak_kernel);
-        default: return false;
+        default: return false;  // N = 128 (the cluster variant): FindMaximumFromCenter only
     }
 }
 

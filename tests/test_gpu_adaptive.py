@@ -144,3 +144,19 @@ def test_adaptive_device_variant_and_repeatability(qp, handle):
     handle.piv_adaptive_device(desc, qp.PIX_U16, h, w, 2, ttab, ou, ov)
     handle.synchronize()
     assert ou.cpu().numpy().tobytes() == u1.tobytes() and ov.cpu().numpy().tobytes() == v1.tobytes()
+
+
+@pytest.mark.parametrize("warp", [True, False])
+def test_adaptive_from_ia128(qp, handle, oracle, warp):
+    """IA 128 -> 32 (the first level on the two-CTA cluster kernel) against the FP64 oracle."""
+    h, w = 512, 448
+    flow = qp.synth.Flow(vmax=6.0, rc=100.0, shear=0.004)
+    pairs = [qp.synth.particle_pair((h, w), flow, ppp=0.03, diam=2.5, diam_sd=0.0, bits=8, seed=70 + k)
+             for k in range(2)]
+    desc = qp.adaptive_desc(128, 32, 0.5, warp_mode=qp.WARP_BOTH_BILINEAR if warp else qp.WARP_NONE,
+                            max_mode=qp.MAX_FIXED if warp else qp.MAX_COMPUTE, fixed_max=255.0 if warp else 0.0)
+    u, v = handle.piv_adaptive([p[0] for p in pairs], [p[1] for p in pairs], desc)
+    for k, (a, b) in enumerate(pairs):
+        ou, ov = oracle.piv_adaptive(a, b, 128, 32, 0.5, fixed_max=255.0 if warp else None, precision=64, warp=warp)
+        err = np.maximum(np.abs(u[k] - ou), np.abs(v[k] - ov))
+        assert np.mean(err <= 1e-3) >= 0.99, (k, float(np.mean(err <= 1e-3)), float(err.max()))

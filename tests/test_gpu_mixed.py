@@ -25,11 +25,13 @@ def handle(qp):
 
 def _batch(qp, bits, count, seed):
     rng = np.random.default_rng(seed)
-    shapes = [(96, 96), (128, 160), (256, 256), (200, 296), (160, 128)]
+    shapes = [(96, 96), (128, 160), (256, 256), (200, 296), (160, 128), (384, 320)]
     pairs, sizes, ofac = [], [], []
     for k in range(count):
         h, w = shapes[rng.integers(len(shapes))]
-        n = int([16, 32, 64][rng.integers(3)])
+        n = int([16, 32, 64, 128][rng.integers(4)])
+        if k == 0:   # at least one IA-128 pair (the two-CTA cluster kernel)
+            (h, w), n = (384, 320), 128
         if min(h, w) < 2 * n:
             n = 16
         flow = qp.synth.Flow(vmax=float(rng.uniform(1, 4)), rc=min(h, w) / 4.0)
@@ -62,6 +64,7 @@ def test_mixed_plan_equals_single_passes(qp, handle, bits, autotune):
     assert plan.total == plan.pair_offset[-1]
     if autotune:
         assert all(w in (0, 1, 2, 4, 8) for w in plan.waves)
+    assert 128 in sizes
     plan.run()
     vec = plan.vectors()
     for q, (a, b) in enumerate(pairs):
@@ -91,7 +94,7 @@ def test_mixed_plan_rejects(qp, handle):
     pairs, sizes, ofac = _batch(qp, 8, 3, seed=3)
     keep, table = _device_table(qp, pairs)
     with pytest.raises(qp.QlpivError) as e:
-        qp.MixedPlan(handle, table, [128, 16, 16], ofac, qp.PIX_U8)
+        qp.MixedPlan(handle, table, [256, 16, 16], ofac, qp.PIX_U8)
     assert e.value.status == qp.E_SHAPE
     with pytest.raises(qp.QlpivError) as e:
         qp.MixedPlan(handle, table, sizes, ofac, qp.PIX_U8, num_peaks=3)

@@ -46,7 +46,7 @@ def _close(x, y, tol):
     return both_nan | (np.abs(x - y) <= tol)
 
 
-@pytest.mark.parametrize("n", [16, 32, 64])
+@pytest.mark.parametrize("n", [16, 32, 64, 128])
 @pytest.mark.parametrize("mode,pixels,iters", MODES)
 def test_ppoint_fit_matches_oracle_on_kernel_planes(qp, handle, oracle, n, mode, pixels, iters):
     a, b, tops, lefts = _frames(qp, n, seed=n + 7 * pixels + mode)

@@ -41,7 +41,7 @@ def _random_tiles(rng, count, n, dtype):
             rng.uniform(0, 200, (count, n, n)).astype(np.float32))
 
 
-@pytest.mark.parametrize("n", [16, 32, 64])
+@pytest.mark.parametrize("n", [16, 32, 64, 128])
 @pytest.mark.parametrize("dtype", [np.uint8, np.uint16, np.float32])
 @pytest.mark.parametrize("norm", ["max_a", "own"])
 def test_planes_match_fp64(qp, handle, oracle, n, dtype, norm):
@@ -122,7 +122,7 @@ def test_rankine_reference_pair_parity(qp, handle, oracle, rankine_pair):
     assert same.mean() > 0.99, st
 
 
-@pytest.mark.parametrize("n", [16, 32, 64])
+@pytest.mark.parametrize("n", [16, 32, 64, 128])
 def test_synthetic_config1_parity(qp, handle, oracle, n):
     a, b = qp.synth.config1_pair(seed=11)
     g = qp.grid.superposition(512, 512, n, 0, 0.5)
@@ -165,10 +165,34 @@ def test_empty_and_errors(qp, handle):
         handle.piv_pass(a, a, 24, [0], [0])
     assert ei.value.status == qp.E_SHAPE
     with pytest.raises(qp.QlpivError) as ei:
-        handle.xcorr_planes(np.zeros((2, 128, 128), np.uint8), np.zeros((2, 128, 128), np.uint8))
+        handle.xcorr_planes(np.zeros((2, 256, 256), np.uint8), np.zeros((2, 256, 256), np.uint8))
     assert ei.value.status == qp.E_SHAPE
+    with pytest.raises(qp.QlpivError) as ei:   # the two-CTA IA 128 kernel runs FindMaximumFromCenter only
+        handle.piv_pass(np.zeros((256, 256), np.uint8), np.zeros((256, 256), np.uint8), 128, [0], [0], num_peaks=2,
+                        peak_kernel=3)
+    assert ei.value.status == qp.E_ARG
     with pytest.raises(ValueError):
         handle.piv_pass(a, a.astype(np.uint16), 32, [0], [0])
+
+
+def test_ia128_shift_and_clipping(qp, handle, oracle):
+    """IA 128 (two-CTA cluster kernel): known shifts, partly clipped B tiles, u8 and 12-bit,
+    against the FP64 oracle; repeated runs are bit-identical."""
+    rng = np.random.default_rng(128)
+    for bits in (8, 12):
+        a, b = qp.synth.particle_pair((400, 448), qp.synth.Flow(vmax=6.0, rc=90.0, shear=0.01), ppp=0.02, diam=2.6,
+                                      diam_sd=0.3, bits=bits, seed=bits)
+        count = 40
+        at = rng.integers(0, 400 - 128, count).astype(np.int32)
+        al = rng.integers(0, 448 - 128, count).astype(np.int32)
+        bt = (at + rng.integers(-20, 21, count)).astype(np.int32)
+        bl = (al + rng.integers(-20, 21, count)).astype(np.int32)
+        bt[:3] = [-30, 300, 5]
+        bl[:3] = [0, 330, -40]
+        _pass_and_check(qp, handle, oracle, a, b, 128, at, al, bt, bl, oracle.NORM_MAX_A)
+        r1 = handle.piv_pass(a, b, 128, at, al, bt, bl)
+        r2 = handle.piv_pass(a, b, 128, at, al, bt, bl)
+        assert r1.tobytes() == r2.tobytes()
 
 
 def test_flat_tiles_and_determinism(qp, handle, oracle):

@@ -29,7 +29,7 @@ def test_library_exports_header_symbols(qp):
     for s in syms:
         assert hasattr(lib, s), s
     assert sorted(qp.exported_symbols()) == syms
-    assert qp.load_library().qlpiv_abi_version() == 2
+    assert qp.load_library().qlpiv_abi_version() == 3
 
 
 def test_ctypes_structs_match_header(qp, tmp_path):
@@ -182,8 +182,10 @@ def test_adaptive_levels_config2(qp):
     assert [(g["n"], g["tiles_i"], g["tiles_j"]) for g in lv] == [(64, 61, 61), (32, 125, 125), (16, 253, 253)]
     with pytest.raises(qp.QlpivError):
         qp.adaptive_levels(qp.adaptive_desc(64, 24, 0.25), 1024, 1024)
+    lv = qp.adaptive_levels(qp.adaptive_desc(128, 16, 0.25), 1024, 1024)
+    assert [g["n"] for g in lv] == [128, 64, 32, 16]
     with pytest.raises(qp.QlpivError):
-        qp.adaptive_levels(qp.adaptive_desc(128, 16, 0.25), 1024, 1024)   # IA 128 not built yet
+        qp.adaptive_levels(qp.adaptive_desc(256, 16, 0.25), 1024, 1024)   # IA 256: no kernel
 
 
 def test_adaptive_plan_bytes_properties(qp):
