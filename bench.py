@@ -366,9 +366,9 @@ def run_serving(pkg, dev, count=48, loads=(0.25, 0.5, 0.75, 0.9, 1.1), per_load=
 
 
 # Batched launch: 256 pairs of sizes from {256^2, 512^2, 1024^2, 2048^2} u8, each with its own IA
-# size from {16, 32, 64} at 50 % overlap, one graph launch per batch (IA 128 is not supported).
+# size from {16, 32, 64, 128} at 50 % overlap, one graph launch per batch.
 BATCH_WORKLOAD = ("batched-mixed: 256 u8 pairs, sides from {256, 512, 1024, 2048} (uniform), IA size per pair from "
-                  "{16, 32, 64} (uniform; 128 not supported), 50 % overlap, FindMaximumFromCenter + 3-point Gaussian, "
+                  "{16, 32, 64, 128} (uniform), 50 % overlap, FindMaximumFromCenter + 3-point Gaussian, "
                   "frames cropped at random positions from a 2048x2048 vortex + shear pair tiled 2x2, one captured "
                   "graph per batch with autotuned launches")
 
@@ -380,7 +380,7 @@ def run_batched(pkg, dev, stream, steps, warmup, count=256):
                                      ppp=0.02, diam=3.0, bits=8, seed=33)
     ma, mb = np.tile(a0, (2, 2)), np.tile(b0, (2, 2))
     sides = rng.choice([256, 512, 1024, 2048], count)
-    sizes = rng.choice([16, 32, 64], count).astype(np.int32)
+    sizes = rng.choice([16, 32, 64, 128], count).astype(np.int32)
     ofac = np.full(count, 0.5, np.float32)
     keep, host, table = [], [], np.zeros(count, pkg.FRAME_DTYPE)
     for k in range(count):
@@ -409,7 +409,7 @@ def run_batched(pkg, dev, stream, steps, warmup, count=256):
     ms = e0.elapsed_time(e1) / steps
     total = plan.total
     ia_by_n = {n: int(sum(plan.tiles[q][0] * plan.tiles[q][1] for q in range(count) if sizes[q] == n))
-               for n in (16, 32, 64)}
+               for n in (16, 32, 64, 128)}
     flops = sum(flops_per_ia(n) * c for n, c in ia_by_n.items())
     bytes_ = sum(bytes_per_ia(n, 1) * c for n, c in ia_by_n.items())
     # plain per-call: one synchronous frame pass per pair through the host API (sampled)
@@ -435,7 +435,7 @@ def run_batched(pkg, dev, stream, steps, warmup, count=256):
             "ia_vectors_by_size": ia_by_n, "ms_per_step": ms, "frame_pairs_per_s": count / (ms * 1e-3),
             "ia_vectors_per_s": total / (ms * 1e-3), "fp32_tflops": flops / (ms * 1e-3) / 1e12,
             "algorithmic_gbs": bytes_ / (ms * 1e-3) / 1e9, "plan_seconds": plan_s,
-            "autotuned_waves": {"16": int(plan.waves[0]), "32": int(plan.waves[1]), "64": int(plan.waves[2])},
+            "autotuned_waves": {str(n): int(plan.waves[k]) for k, n in enumerate((16, 32, 64, 128))},
             "plain_per_call": {"frame_pairs_per_s": per_call_pairs, "ia_vectors_per_s": sample_ias / per_call_s,
                                "sample": f"{len(sample)} pairs, one synchronous qlpiv_pass per pair (host images)"},
             "vs_per_call_pairs": (count / (ms * 1e-3)) / per_call_pairs}

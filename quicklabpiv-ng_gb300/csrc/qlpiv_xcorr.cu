@@ -1,9 +1,11 @@
-// K1 instantiations (IA side x pixel type) and their launcher.
+// K1 instantiations (IA side x pixel type) and their launcher; IA 128 runs the two-CTA cluster
+// variant (qlpiv_xcorr_pair.cuh).
 #include <cmath>
 #include <mutex>
 
 #include "qlpiv_internal.h"
 #include "qlpiv_xcorr.cuh"
+#include "qlpiv_xcorr_pair.cuh"
 
 namespace qlpiv {
 
@@ -70,31 +72,42 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
     // every CTA loops over IAs; eight waves of CTAs balance the single-peak kernel best,
     // one resident wave the multi-peak one (its fit queue then fills between flushes)
     long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? 1 : 8));
-    if (grid > job.count * S::CL) grid = job.count * S::CL;
+    if (grid > job.count) grid = job.count;
     if (grid < 1) return cudaSuccess;
     // P-point sub-pixel stencils: 2 P floats per queued fit after the fixed layout
     const size_t smem = S::SMEM + (j.subpix_pixels > 0 ? sizeof(float) * 32 * 2 * j.subpix_pixels : 0);
-    if constexpr (S::CL == 1) {
-        xcorr_kernel<N, Pix, PP><<<(unsigned)grid, S::T, smem, stream>>>(j);
-    } else {
-        // one cluster of CL CTAs per IA: the grid is a whole number of clusters
-        grid = (grid + S::CL - 1) / S::CL * S::CL;
-        if (grid > (long)S::CL * job.count) grid = (long)S::CL * job.count;
-        cudaLaunchConfig_t cfg{};
-        cfg.gridDim = dim3((unsigned)grid);
-        cfg.blockDim = dim3(S::T);
-        cfg.dynamicSmemBytes = smem;
-        cfg.stream = stream;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = S::CL;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        e = cudaLaunchKernelEx(&cfg, xcorr_kernel<N, Pix, PP>, j);
-        if (e != cudaSuccess) return e;
+    xcorr_kernel<N, Pix, PP><<<(unsigned)grid, S::T, smem, stream>>>(j);
+    return cudaGetLastError();
+}
+
+// IA 128: one cluster of two CTAs per IA, one CTA per SM; `waves` clusters per SM pair.
+template <typename Pix, bool PP>
+static cudaError_t launch_pair(const IaJob &job, cudaStream_t stream, int num_sms) {
+    static std::mutex mu;
+    static bool ready[kMaxDevices] = {false};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!ready[dev]) {
+            e = cudaFuncSetAttribute(xcorr_pair_kernel<Pix, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(PairShape::SMEM + kSubpixSmem));
+            if (e != cudaSuccess) return e;
+            ready[dev] = true;
+        }
     }
+    if (job.num_peaks != 0) return cudaErrorInvalidValue;  // FindMaximumFromCenter only
+    const cplx *tw = nullptr;
+    if ((e = ensure_twiddles(dev, &tw)) != cudaSuccess) return e;
+    IaJob j = job;
+    j.twiddles = tw + twiddle_offset(256);
+    long grid = (long)(num_sms & ~1) * (job.waves > 0 ? job.waves : 4);
+    if (grid > 2 * job.count) grid = 2 * job.count;
+    if (grid < 2) return cudaSuccess;
+    const size_t smem = PairShape::SMEM + (j.subpix_pixels > 0 ? sizeof(float) * 32 * 2 * j.subpix_pixels : 0);
+    xcorr_pair_kernel<Pix, PP><<<(unsigned)grid, PairShape::T, smem, stream>>>(j);
     return cudaGetLastError();
 }
 
@@ -104,7 +117,7 @@ static cudaError_t launch_pix(const IaJob &job, int n, cudaStream_t stream, int 
         case 16: return launch_one<16, Pix, PP>(job, stream, num_sms);
         case 32: return launch_one<32, Pix, PP>(job, stream, num_sms);
         case 64: return launch_one<64, Pix, PP>(job, stream, num_sms);
-        case 128: return launch_one<128, Pix, PP>(job, stream, num_sms);
+        case 128: return launch_pair<Pix, PP>(job, stream, num_sms);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -137,7 +150,7 @@ bool multipeak_supported(int n, int num_peaks, int peak_kernel) {
         case 16: return multipeak_fits_n<16>(peak_kernel);
         case 32: return multipeak_fits_n<32>(peak_kernel);
         case 64: return multipeak_fits_n<64>(peak_kernel);
-        default: return false;  // N = 128 (the cluster variant): FindMaximumFromCenter only
+        default: return false;  // IA 128 (the cluster kernel): FindMaximumFromCenter only
     }
 }
 

@@ -1,8 +1,5 @@
 // K1: fused FFT cross-correlation + integer peak + 3-point Gaussian sub-pixel fit,
-// one CTA per interrogation area (IA) at a time, IA side N in {16, 32, 64}; for N = 128 a
-// cluster of two CTAs per IA (the 128 column-pair regions of the 256 x 256 spectrum, 296 KB,
-// exceed one SM's shared memory: each CTA holds 64 regions and reaches the peer's through
-// distributed shared memory).
+// one CTA per interrogation area (IA) at a time, IA side N in {16, 32, 64}.
 //
 // Reference semantics (QuickLabPIV-ng, S/ = src/main/java/pt/quickLabPIV/):
 //   tile max floored at 16         S/MatrixByte.java:16-33, S/MatrixInt16.java:21-38
@@ -37,8 +34,6 @@
 //      minimum; whole 32-record chunks are skipped on their maximum), and queues one
 //      fit per peak.
 #pragma once
-#include <cooperative_groups.h>
-
 #include "qlpiv_fft.cuh"
 #include "qlpiv.h"
 #include "qlpiv_subpix.cuh"
@@ -50,15 +45,13 @@ struct XcorrShape {
     static constexpr int M = 2 * N;
     static constexpr int D = M - 1;
     static constexpr int G = N / 4;                    // lanes per transform
-    static constexpr int CL = N == 128 ? 2 : 1;        // CTAs per IA (a thread-block cluster)
-    static constexpr int NR = N / CL;                  // column-pair regions held per CTA
     static constexpr int T = N == 16 ? 64 : (N == 32 ? 256 : 512);  // threads per CTA
     static constexpr int NG = T / G;                   // concurrent transforms
-    static constexpr int ROUNDS = N / (NG * CL);       // tasks per group per phase
+    static constexpr int ROUNDS = N / NG;              // tasks per group per phase
     static constexpr int RP = M + M / 8 + 1;           // region pitch (complex), odd
-    static constexpr int MIN_BLOCKS = N == 16 ? 16 : (N == 32 ? 4 : (N == 64 ? 2 : 1));
+    static constexpr int MIN_BLOCKS = N == 16 ? 16 : (N == 32 ? 4 : 2);
     static constexpr size_t SCR_BYTES = sizeof(cplx) * (size_t)(NG * RP);
-    static constexpr size_t SMEM = sizeof(cplx) * (size_t)(M + NR * RP) + SCR_BYTES + 64 * sizeof(uint64_t) +
+    static constexpr size_t SMEM = sizeof(cplx) * (size_t)(M + N * RP) + SCR_BYTES + 64 * sizeof(uint64_t) +
                                    32 * 56 /* fit queue */ + 256 /* multi-peak list */;
 };
 
@@ -654,23 +647,15 @@ __device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float m
 
 // PP: the P-point sub-pixel interpolators are compiled in (their out-of-line double-precision
 // fits cost the common instantiation registers even when unused).
-//
-// N = 128 (CL = 2): the two CTAs of a cluster work on the same IA.  CTA q transforms rows,
-// owns column-pair regions and inverts row pairs [64q, 64q + 64); row-pass outputs and the
-// row-pair reads / plane writes that fall in the peer's regions go through distributed shared
-// memory, and cluster barriers replace the CTA barriers between the phases.  Tile maxima, the
-// peak key and the min floor are exchanged through a few words of each CTA's reduction area;
-// rank 0 queues and runs the fits.
 template <int N, typename Pix, bool PP>
 __global__ void __launch_bounds__(XcorrShape<N>::T, XcorrShape<N>::MIN_BLOCKS)
 xcorr_kernel(IaJob job) {
     using S = XcorrShape<N>;
     constexpr int M = S::M, D = S::D, G = S::G, NG = S::NG, ROUNDS = S::ROUNDS, RP = S::RP, T = S::T;
-    constexpr int CL = S::CL, NR = S::NR;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx *tw = reinterpret_cast<cplx *>(smem_raw);
-    cplx *reg = tw + M;           // NR regions of RP complex
-    cplx *scr = reg + NR * RP;    // NG scratch buffers of RP complex
+    cplx *reg = tw + M;           // N regions of RP complex
+    cplx *scr = reg + N * RP;     // NG scratch buffers of RP complex
     uint64_t *red = reinterpret_cast<uint64_t *>(scr + NG * RP);  // 64 words
     FitRec *fitq = reinterpret_cast<FitRec *>(red + 64);           // 32 queued fits
     float *mp_lv = reinterpret_cast<float *>(fitq + 32);           // multi-peak list (ascending)
@@ -678,8 +663,7 @@ xcorr_kernel(IaJob job) {
     int *mp_lj = mp_li + QLPIV_MAX_PEAKS + 1;
     float *fitv = reinterpret_cast<float *>(mp_lj + QLPIV_MAX_PEAKS + 1);  // P-point stencils
     int qn = 0;                                                    // uniform across the CTA
-    // 0: FindMaximumFromCenter (the only search of the cluster variant; the host rejects others)
-    const int multi = S::CL > 1 ? 0 : job.num_peaks;
+    const int multi = job.num_peaks;                               // 0: FindMaximumFromCenter
     const int KQ = multi > 0 ? multi : 1;                          // fit records per IA
 
     const int tid = threadIdx.x;
@@ -691,32 +675,10 @@ xcorr_kernel(IaJob job) {
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
     const int gbase = lane & ~(G - 1);
 
-    // cluster geometry: rank, the peer's regions and exchange words (red[48..64))
-    int rank = 0;
-    cplx *reg_lo = reg, *reg_hi = reg;  // regions [0, NR) and [NR, 2 NR) as seen from this CTA
-    uint64_t *xch = red + 48, *xch_peer = red + 48;
-    if constexpr (CL > 1) {
-        cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
-        rank = (int)cl.block_rank();
-        cplx *peer = cl.map_shared_rank(reg, (unsigned)(rank ^ 1));
-        reg_lo = rank == 0 ? reg : peer;
-        reg_hi = rank == 0 ? peer : reg;
-        xch_peer = cl.map_shared_rank(xch, (unsigned)(rank ^ 1));
-    }
-    auto region = [&](int c) -> cplx * {
-        if constexpr (CL == 1) return reg + c * RP;
-        else return c < NR ? reg_lo + c * RP : reg_hi + (c - NR) * RP;
-    };
-    auto sync_all = [&]() {
-        if constexpr (CL == 1) __syncthreads();
-        else cooperative_groups::this_cluster().sync();
-    };
-    const int first = CL == 1 ? 0 : rank * NR;  // this CTA's rows, regions and row pairs start here
-
     for (int e = tid; e < M; e += T) tw[e] = job.twiddles[e];
     __syncthreads();
 
-    for (long ia = blockIdx.x / CL; ia < job.count; ia += gridDim.x / CL) {
+    for (long ia = blockIdx.x; ia < job.count; ia += gridDim.x) {
         const Pix *imgA, *imgB;
         long pitch_a, pitch_b;
         int img_h, img_w;
@@ -749,7 +711,7 @@ xcorr_kernel(IaJob job) {
         float mxa = 0.0f, mxb = 0.0f;
 #pragma unroll
         for (int r = 0; r < ROUNDS; r++) {
-            const int n1 = first + grp + NG * r;
+            const int n1 = grp + NG * r;
 #pragma unroll
             for (int m = 0; m < 4; m++) {
                 const int n2 = g + G * m;
@@ -772,17 +734,6 @@ xcorr_kernel(IaJob job) {
             mxa = 0.0f; mxb = 0.0f;
 #pragma unroll
             for (int k = 0; k < NWARPS; k++) { mxa = fmaxf(mxa, redf[k]); mxb = fmaxf(mxb, redf[32 + k]); }
-            if constexpr (CL > 1) {  // the other half of the tiles' rows is in the peer CTA
-                if (tid == 0) {
-                    const uint64_t w = ((uint64_t)__float_as_uint(mxa) << 32) | __float_as_uint(mxb);
-                    xch[rank] = w;
-                    xch_peer[rank] = w;
-                }
-                cooperative_groups::this_cluster().sync();
-                const uint64_t w = xch[rank ^ 1];
-                mxa = fmaxf(mxa, __uint_as_float((uint32_t)(w >> 32)));
-                mxb = fmaxf(mxb, __uint_as_float((uint32_t)w));
-            }
             maxA = fmaxf(mxa, 16.0f);
             maxB = fmaxf(mxb, 16.0f);
         } else if (job.max_mode == QLPIV_MAX_GIVEN) {
@@ -798,7 +749,7 @@ xcorr_kernel(IaJob job) {
         // ---- 2. row pass ----
 #pragma unroll
         for (int r = 0; r < ROUNDS; r++) {
-            const int n1 = first + grp + NG * r;
+            const int n1 = grp + NG * r;
             cplx v[8];
 #pragma unroll
             for (int m = 0; m < 4; m++) {
@@ -815,21 +766,21 @@ xcorr_kernel(IaJob job) {
 #pragma unroll
             for (int m = 0; m < 8; m++) {
                 const int k2 = g + G * m;
-                int rgn, slot;
-                if (k2 == 0) { rgn = 0; slot = n1; }
-                else if (k2 == N) { rgn = 0; slot = N + n1; }
-                else if (k2 < N) { rgn = k2; slot = n1; }
-                else { rgn = M - k2; slot = N + n1; }
-                region(rgn)[pad8(slot)] = v[m];
+                int region, slot;
+                if (k2 == 0) { region = 0; slot = n1; }
+                else if (k2 == N) { region = 0; slot = N + n1; }
+                else if (k2 < N) { region = k2; slot = n1; }
+                else { region = M - k2; slot = N + n1; }
+                reg[region * RP + pad8(slot)] = v[m];
             }
         }
-        sync_all();
+        __syncthreads();
 
-        // ---- 3. column tasks (this CTA's regions) ----
+        // ---- 3. column tasks ----
 #pragma unroll
         for (int r = 0; r < ROUNDS; r++) {
-            const int c = first + grp + NG * r;
-            cplx *rg = reg + (c - first) * RP;
+            const int c = grp + NG * r;
+            cplx *rg = reg + c * RP;
             cplx z1[8], z2[8];
 #pragma unroll
             for (int m = 0; m < 4; m++) {
@@ -881,31 +832,30 @@ xcorr_kernel(IaJob job) {
 #pragma unroll
             for (int m = 0; m < 8; m++) rg[pad8(g + G * m)] = p[m];
         }
-        sync_all();
+        __syncthreads();
 
         // ---- 4. row-pair pass + per-lane peak scoring ----
         uint64_t best = 0ull;
         uint32_t best_ij = 0u;
         float minf = 3.402823466e38f;
+        float *regf = reinterpret_cast<float *>(reg);
 #pragma unroll
         for (int r = 0; r < ROUNDS; r++) {
-            const int pr = first + grp + NG * r;
+            const int pr = grp + NG * r;
             const int ra_ = 2 * pr, rb_ = 2 * pr + 1;
             cplx y[8];
 #pragma unroll
             for (int m = 0; m < 8; m++) {
                 const int k2 = g + G * m;
                 if (k2 == 0 || k2 == N) {
-                    const cplx *r0 = region(0);
-                    const cplx qa = r0[pad8(ra_)], qb = r0[pad8(rb_)];
+                    const cplx qa = reg[pad8(ra_)], qb = reg[pad8(rb_)];
                     y[m] = (k2 == 0) ? cplx{qa.x, qb.x} : cplx{qa.y, qb.y};
                 } else if (k2 < N) {
-                    const cplx *rk = region(k2);
-                    const cplx qa = rk[pad8(ra_)], qb = rk[pad8(rb_)];
+                    const cplx qa = reg[k2 * RP + pad8(ra_)], qb = reg[k2 * RP + pad8(rb_)];
                     y[m] = {qa.x - qb.y, qa.y + qb.x};
                 } else {
-                    const cplx *rk = region(M - k2);
-                    const cplx qa = rk[pad8(ra_)], qb = rk[pad8(rb_)];
+                    const int cc = M - k2;
+                    const cplx qa = reg[cc * RP + pad8(ra_)], qb = reg[cc * RP + pad8(rb_)];
                     y[m] = {qa.x + qb.y, qb.x - qa.y};
                 }
             }
@@ -915,15 +865,8 @@ xcorr_kernel(IaJob job) {
             for (int m = 0; m < 8; m++) {
                 const int n2 = g + G * m;
                 // keep the plane in the row slots this pair has consumed
-                if constexpr (CL == 1) {
-                    float *regf = reinterpret_cast<float *>(reg);
-                    regf[2 * ((n2 >> 1) * RP + pad8(ra_)) + (n2 & 1)] = y[m].x;
-                    regf[2 * ((n2 >> 1) * RP + pad8(rb_)) + (n2 & 1)] = y[m].y;
-                } else {
-                    float *rf = reinterpret_cast<float *>(region(n2 >> 1));
-                    rf[2 * pad8(ra_) + (n2 & 1)] = y[m].x;
-                    rf[2 * pad8(rb_) + (n2 & 1)] = y[m].y;
-                }
+                regf[2 * ((n2 >> 1) * RP + pad8(ra_)) + (n2 & 1)] = y[m].x;
+                regf[2 * ((n2 >> 1) * RP + pad8(rb_)) + (n2 & 1)] = y[m].y;
                 if (multi > 0) {
                     // FindMaximumMultiPeaks visits every cell of the (2N-1)^2 plane
                     if (n2 <= M - 2) {
@@ -950,13 +893,8 @@ xcorr_kernel(IaJob job) {
             }
         }
 
-        // ---- 5. CTA (and cluster) reduction; the fit is queued and run 32 IAs at a time ----
-        auto P = [&](int i, int j) -> float {
-            if constexpr (CL == 1)
-                return reinterpret_cast<const float *>(reg)[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)];
-            else
-                return reinterpret_cast<const float *>(region(j >> 1))[2 * pad8(i) + (j & 1)];
-        };
+        // ---- 5. CTA reduction; the fit is queued and run 32 IAs at a time ----
+        auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)]; };
         if (multi == 0) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -971,12 +909,10 @@ xcorr_kernel(IaJob job) {
                 red[32 + warp] = ((uint64_t)best_ij << 32) | (uint64_t)__float_as_uint(minf);
             }
             __syncthreads();
-            // warp 0 reduces the per-warp candidates; the cluster variant then hands rank 1's
-            // to rank 0 (the barrier also publishes the peer's plane rows)
-            auto reduce_warps = [&](uint64_t &bk, uint32_t &bij, float &mn) {
-                bk = 0ull;
-                bij = 0u;
-                mn = 3.402823466e38f;
+            if (warp == 0) {
+                uint64_t bk = 0ull;
+                uint32_t bij = 0u;
+                float mn = 3.402823466e38f;
                 if (lane < NWARPS) {
                     bk = red[lane];
                     bij = (uint32_t)(red[32 + lane] >> 32);
@@ -990,63 +926,35 @@ xcorr_kernel(IaJob job) {
                     if (ok > bk) { bk = ok; bij = oij; }
                     mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
                 }
-            };
-            auto queue_fit = [&](uint64_t bk, uint32_t bij, float mn) {
-                FitRec r;
-                r.ia = ia;
-                r.mn = mn;
-                r.pi = 0;
-                r.pj = 0;
-                r.pv = 0.0f;
-                if (bk != 0ull) {
-                    r.pi = (int)(bij >> 16);
-                    r.pj = (int)(bij & 0xffffu);
-                    r.pv = __uint_as_float((uint32_t)(bk >> 32));
-                }
-                r.slot = 0;
-                r.npk = 1;
-                fit_stencil<D>(r, job, P, fitv + qn * 2 * job.subpix_pixels);
-                fitq[qn] = r;
-            };
-            if constexpr (CL == 1) {
-                if (warp == 0) {
-                    uint64_t bk;
-                    uint32_t bij;
-                    float mn;
-                    reduce_warps(bk, bij, mn);
-                    if (lane == 0) queue_fit(bk, bij, mn);
-                }
-            } else {
-                uint64_t bk = 0ull;
-                uint32_t bij = 0u;
-                float mn = 3.402823466e38f;
-                if (warp == 0) reduce_warps(bk, bij, mn);
-                if (rank == 1 && tid == 0) {
-                    xch_peer[2] = bk;
-                    xch_peer[3] = ((uint64_t)bij << 32) | (uint64_t)__float_as_uint(mn);
-                }
-                cooperative_groups::this_cluster().sync();
-                if (rank == 0 && tid == 0) {
-                    const uint64_t ok = xch[2];
-                    const uint32_t oij = (uint32_t)(xch[3] >> 32);
-                    if (ok > bk) { bk = ok; bij = oij; }
-                    mn = fminf(mn, __uint_as_float((uint32_t)xch[3]));
-                    queue_fit(bk, bij, mn);
+                if (lane == 0) {
+                    FitRec r;
+                    r.ia = ia;
+                    r.mn = mn;
+                    r.pi = 0;
+                    r.pj = 0;
+                    r.pv = 0.0f;
+                    if (bk != 0ull) {
+                        r.pi = (int)(bij >> 16);
+                        r.pj = (int)(bij & 0xffffu);
+                        r.pv = __uint_as_float((uint32_t)(bk >> 32));
+                    }
+                    r.slot = 0;
+                    r.npk = 1;
+                    fit_stencil<D>(r, job, P, fitv + qn * 2 * job.subpix_pixels);
+                    fitq[qn] = r;
                 }
             }
         } else {
-            if constexpr (CL == 1)
-                multipeak_select<N>(job, ia, minf, reinterpret_cast<float *>(reg), scr, red, fitq, fitv, qn, mp_lv,
-                                    mp_li, mp_lj);
+            multipeak_select<N>(job, ia, minf, regf, scr, red, fitq, fitv, qn, mp_lv, mp_li, mp_lj);
         }
         qn += KQ;
         if (qn + KQ > 32) {
-            if (warp == 0 && rank == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
+            if (warp == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
             qn = 0;
         }
-        sync_all();  // regions are rewritten by the next IA
+        __syncthreads();  // regions are rewritten by the next IA
     }
-    if (qn > 0 && warp == 0 && rank == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
+    if (qn > 0 && warp == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
 }
 
 }  // namespace qlpiv
