@@ -561,32 +561,43 @@ qlpiv_status qlpiv_tiff_info(const char *path, int *height, int *width, int *bit
 /* Decodes the image row-major into `pixels` (uint8 or uint16 per bits_per_sample). */
 qlpiv_status qlpiv_tiff_read(const char *path, void *pixels, int64_t capacity_bytes);
 
-/* MATLAB level-5 export of the vector maps, the variable layout of
- * S/exporter/StructMultiFrameFloatVelocityExporter.java:54-181 (one map per IA size):
+/* MATLAB level-5 export of the vector maps with the variables of
+ * S/exporter/StructMultiFrameFloatVelocityExporter.java (one struct per IA size):
  *   exportDate                      char
  *   parameters                      struct: imageWidth, imageHeight, iaStartI, iaEndI, iaStartJ,
  *                                   iaEndJ (int32), overlapFactor (single), hasSwappedUVVectors,
  *                                   markInvalidAsNaN, totalNumberOfVelocityMaps, multiVolumeExport,
- *                                   multiVolumeLastVolume (int32)
- *   velocities<iaHeight>x<iaWidth>  struct: iaHeight, iaWidth, adaptiveStep (int32),
+ *                                   multiVolumeLastVolume (int32)                      (:80-115)
+ *   velocities<iaHeight>x<iaWidth>  QLPIV_MAT_RUN (the end-of-run export, exportDataToFile(PIVResults),
+ *                                   :185-238): iaHeight, iaWidth, multiVolumeExport (int32),
  *                                   margins (struct top, left, bottom, right), u, v (single,
- *                                   tiles_i x tiles_j x frames). */
+ *                                   tiles_i x tiles_j x frames) taken through PIVMap
+ *                                   (S/PIVMap.java:119-133): u = column displacement and v = row
+ *                                   displacement unless swap_uv;
+ *                                   QLPIV_MAT_STEP (exportDataToFile(frame, IterationStepTiles),
+ *                                   :132-181): iaHeight, iaWidth, adaptiveStep, margins, u = row and
+ *                                   v = column displacement.
+ * Invalid vectors are written as NaN when mark_invalid_as_nan is set. */
+typedef enum { QLPIV_MAT_RUN = 0, QLPIV_MAT_STEP = 1 } qlpiv_mat_layout;
+
 typedef struct qlpiv_mat_export_params {
     int image_width, image_height;
     int ia_start, ia_end;       /* first and last adaptive IA side (square IAs) */
     float overlap_factor;
     int frames;                 /* velocity maps per IA size */
-    int swap_uv;                /* recorded as hasSwappedUVVectors */
+    int swap_uv;                /* PIVMap swapUVOrder, recorded as hasSwappedUVVectors */
     int mark_invalid_as_nan;    /* invalid vectors written as NaN */
     const char *export_date;    /* NULL: the current UTC time */
-    int reserved[4];
+    int layout;                 /* qlpiv_mat_layout */
+    int reserved[3];
 } qlpiv_mat_export_params;
 
 typedef struct qlpiv_mat_velocity_map {
     int ia_height, ia_width, adaptive_step;
     int tiles_i, tiles_j;
     int margins[4];             /* top, left, bottom, right */
-    const float *u, *v;         /* frames x tiles_i x tiles_j, row-major */
+    const float *u, *v;         /* tile displacements along rows (u) and columns (v),
+                                   frames x tiles_i x tiles_j, row-major */
     const uint8_t *invalid;     /* same shape, nonzero = invalid; may be NULL */
 } qlpiv_mat_velocity_map;
 

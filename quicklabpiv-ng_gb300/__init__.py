@@ -180,7 +180,7 @@ class MatExportParams(ctypes.Structure):
     _fields_ = [("image_width", ctypes.c_int), ("image_height", ctypes.c_int), ("ia_start", ctypes.c_int),
                 ("ia_end", ctypes.c_int), ("overlap_factor", ctypes.c_float), ("frames", ctypes.c_int),
                 ("swap_uv", ctypes.c_int), ("mark_invalid_as_nan", ctypes.c_int),
-                ("export_date", ctypes.c_char_p), ("reserved", ctypes.c_int * 4)]
+                ("export_date", ctypes.c_char_p), ("layout", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class MatVelocityMap(ctypes.Structure):
@@ -761,13 +761,18 @@ def read_tiff(path):
     return out
 
 
+MAT_RUN, MAT_STEP = 0, 1
+
+
 def export_mat(path, maps, image_height, image_width, ia_start, ia_end, overlap_factor, swap_uv=False,
-               mark_invalid_as_nan=False, export_date=None):
+               mark_invalid_as_nan=False, export_date=None, layout=MAT_RUN):
     """Write the vector maps as a MATLAB level-5 file with the variables of
     S/exporter/StructMultiFrameFloatVelocityExporter.java.
 
-    maps: one dict per IA size with u, v (frames x tiles_i x tiles_j float32), ia (height, width),
-    adaptive_step, margins (top, left, bottom, right) and optionally invalid (same shape, bool)."""
+    maps: one dict per IA size with u (row displacements) and v (column displacements), frames x
+    tiles_i x tiles_j float32, ia (height, width), margins (top, left, bottom, right), optionally
+    adaptive_step (MAT_STEP layout) and invalid (same shape, bool).  MAT_RUN (the end-of-run
+    export) stores the column displacement as `u` unless swap_uv, as PIVMap does."""
     keep, table = [], (MatVelocityMap * max(1, len(maps)))()
     frames = None
     for k, m in enumerate(maps):
@@ -792,7 +797,7 @@ def export_mat(path, maps, image_height, image_width, ia_start, ia_end, overlap_
         e.invalid = None if inv is None else inv.ctypes.data
     p = MatExportParams(image_width=image_width, image_height=image_height, ia_start=ia_start, ia_end=ia_end,
                         overlap_factor=overlap_factor, frames=1 if frames is None else frames, swap_uv=int(bool(swap_uv)),
-                        mark_invalid_as_nan=int(bool(mark_invalid_as_nan)),
+                        mark_invalid_as_nan=int(bool(mark_invalid_as_nan)), layout=layout,
                         export_date=None if export_date is None else export_date.encode())
     _check(load_library().qlpiv_mat_export(os.fsencode(path), ctypes.byref(p), len(maps), table))
 

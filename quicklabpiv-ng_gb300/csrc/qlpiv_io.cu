@@ -7,9 +7,10 @@
 //         either byte order ("II" / "MM"); the first image of the file.
 //   MAT   StructMultiFrameFloatVelocityExporter (S/exporter/StructMultiFrameFloatVelocityExporter.java):
 //         a 128-byte level-5 header, `exportDate` (char), `parameters` (struct of int32 / single
-//         scalars) and per velocity map a struct `velocities<H>x<W>` with iaHeight, iaWidth,
-//         adaptiveStep (int32), margins (struct top, left, bottom, right) and u, v (single,
-//         tiles_i x tiles_j x frames, MATLAB column-major order), uncompressed elements.
+//         scalars) and per velocity map a struct `velocities<H>x<W>`: iaHeight, iaWidth, then
+//         multiVolumeExport (end-of-run layout, :185-238) or adaptiveStep (per-step layout,
+//         :132-181), margins (struct top, left, bottom, right) and u, v (single,
+//         tiles_i x tiles_j x frames, MATLAB column-major order); uncompressed elements.
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
@@ -331,6 +332,7 @@ qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *p
                               const qlpiv_mat_velocity_map *maps) {
     if (!path || !p || (num_maps > 0 && !maps)) return fail(QLPIV_E_ARG, "NULL argument");
     if (num_maps < 0 || p->frames <= 0) return fail(QLPIV_E_ARG, "num_maps < 0 or frames <= 0");
+    if (p->layout != QLPIV_MAT_RUN && p->layout != QLPIV_MAT_STEP) return fail(QLPIV_E_ARG, "layout %d", p->layout);
     for (int m = 0; m < num_maps; m++)
         if (!maps[m].u || !maps[m].v || maps[m].tiles_i <= 0 || maps[m].tiles_j <= 0)
             return fail(QLPIV_E_ARG, "velocity map %d: NULL data or empty grid", m);
@@ -378,9 +380,10 @@ qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *p
     for (int m = 0; m < num_maps; m++) {
         const qlpiv_mat_velocity_map &mp = maps[m];
         Buf v;
+        const bool run = p->layout == QLPIV_MAT_RUN;
         int32_scalar(v, "", mp.ia_height);
         int32_scalar(v, "", mp.ia_width);
-        int32_scalar(v, "", mp.adaptive_step);
+        int32_scalar(v, "", run ? 0 : mp.adaptive_step);  // multiVolumeExport: one volume
         {
             Buf mv;
             int32_scalar(mv, "", mp.margins[0]);
@@ -391,7 +394,9 @@ qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *p
         }
         const size_t per = (size_t)mp.tiles_i * mp.tiles_j;
         for (int comp = 0; comp < 2; comp++) {
-            const float *src = comp == 0 ? mp.u : mp.v;
+            // end-of-run maps go through PIVMap: u is the column displacement unless swapped
+            const bool rows = run ? (comp == 0) == (p->swap_uv != 0) : comp == 0;
+            const float *src = rows ? mp.u : mp.v;
             // MATLAB order: i fastest, then j, then the frame
             std::vector<float> col(per * p->frames);
             size_t k = 0;
@@ -407,7 +412,8 @@ qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *p
             matrix(v, mxSINGLE, {mp.tiles_i, mp.tiles_j, p->frames}, "", body);
         }
         const std::string name = "velocities" + std::to_string(mp.ia_height) + "x" + std::to_string(mp.ia_width);
-        structure(out, name, {"iaHeight", "iaWidth", "adaptiveStep", "margins", "u", "v"}, v);
+        structure(out, name, {"iaHeight", "iaWidth", run ? "multiVolumeExport" : "adaptiveStep", "margins", "u", "v"},
+                  v);
     }
     FILE *f = std::fopen(path, "wb");
     if (!f) return fail(QLPIV_E_ARG, "cannot create %s", path);

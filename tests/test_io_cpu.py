@@ -225,13 +225,14 @@ def _maps(rng, frames):
 
 
 @pytest.mark.parametrize("nan", [False, True])
-def test_mat_export_reads_back(qp, tmp_path, nan):
+@pytest.mark.parametrize("layout,swap", [(0, False), (0, True), (1, False)])
+def test_mat_export_reads_back(qp, tmp_path, nan, layout, swap):
     sio = pytest.importorskip("scipy.io")
-    rng = np.random.default_rng(int(nan))
+    rng = np.random.default_rng(int(nan) + 2 * layout + 4 * swap)
     maps = _maps(rng, frames=3)
     p = tmp_path / "v.mat"
     qp.export_mat(p, maps, image_height=300, image_width=340, ia_start=32, ia_end=16, overlap_factor=0.5,
-                  swap_uv=True, mark_invalid_as_nan=nan, export_date="Thu Dec 03 12:00:00 UTC 2026")
+                  swap_uv=swap, mark_invalid_as_nan=nan, export_date="Thu Dec 03 12:00:00 UTC 2026", layout=layout)
     head = p.read_bytes()[:128]
     assert head.startswith(b"MATLAB 5.0 - QuickLabPIV-ng Velocities exported on: Thu Dec 03")
     assert head[124:128] == b"\x00\x01IM"
@@ -245,21 +246,25 @@ def test_mat_export_reads_back(qp, tmp_path, nan):
     assert vals["imageWidth"] == 340 and vals["imageHeight"] == 300
     assert (vals["iaStartI"], vals["iaEndI"], vals["iaStartJ"], vals["iaEndJ"]) == (32, 16, 32, 16)
     assert par["imageWidth"].dtype == np.int32 and par["overlapFactor"].dtype == np.float32
-    assert vals["overlapFactor"] == np.float32(0.5) and vals["hasSwappedUVVectors"] == 1
+    assert vals["overlapFactor"] == np.float32(0.5) and vals["hasSwappedUVVectors"] == int(swap)
     assert vals["markInvalidAsNaN"] == int(nan) and vals["totalNumberOfVelocityMaps"] == 3
     assert vals["multiVolumeExport"] == 0 and vals["multiVolumeLastVolume"] == 1
+    third = "multiVolumeExport" if layout == qp.MAT_RUN else "adaptiveStep"
     for mp in maps:
         name = f"velocities{mp['ia'][0]}x{mp['ia'][1]}"
         s = m[name][0, 0]
-        assert s.dtype.names == ("iaHeight", "iaWidth", "adaptiveStep", "margins", "u", "v")
-        assert s["iaHeight"][0, 0] == mp["ia"][0] and s["adaptiveStep"][0, 0] == mp["adaptive_step"]
+        assert s.dtype.names == ("iaHeight", "iaWidth", third, "margins", "u", "v")
+        assert s["iaHeight"][0, 0] == mp["ia"][0]
+        assert s[third][0, 0] == (0 if layout == qp.MAT_RUN else mp["adaptive_step"])
         mg = s["margins"][0, 0]
         assert mg.dtype.names == ("top", "left", "bottom", "right")
         assert [int(mg[k][0, 0]) for k in mg.dtype.names] == [3, 4, 5, 6]
-        for comp in ("u", "v"):
+        # end-of-run maps go through PIVMap: u holds the column displacement unless swapped
+        rows_first = layout == qp.MAT_STEP or swap
+        for comp, src in (("u", "u" if rows_first else "v"), ("v", "v" if rows_first else "u")):
             arr = s[comp]
             assert arr.dtype == np.float32
-            expect = np.moveaxis(mp[comp], 0, -1)              # tiles_i x tiles_j x frames
+            expect = np.moveaxis(mp[src], 0, -1)              # tiles_i x tiles_j x frames
             if nan:
                 expect = np.where(np.moveaxis(mp["invalid"], 0, -1), np.float32(np.nan), expect)
             np.testing.assert_array_equal(arr, expect)
@@ -277,11 +282,17 @@ def test_mat_export_of_an_adaptive_result(qp, tmp_path):
     qp.export_adaptive_mat(p, desc, 256, 320, u, -u)
     s = sio.loadmat(p)["velocities16x16"][0, 0]
     assert s["u"].shape == (last["tiles_i"], last["tiles_j"], 2)
-    assert s["adaptiveStep"][0, 0] == len(levels) - 1
+    assert s["multiVolumeExport"][0, 0] == 0
     mg = s["margins"][0, 0]
     assert [int(mg[k][0, 0]) for k in ("top", "left", "bottom", "right")] == \
         [last["margin_top"], last["margin_left"], last["margin_bottom"], last["margin_right"]]
-    np.testing.assert_array_equal(s["v"][:, :, 1], -u[1])
+    np.testing.assert_array_equal(s["u"][:, :, 1], -u[1])    # column displacements first (PIVMap)
+    np.testing.assert_array_equal(s["v"][:, :, 1], u[1])
+    q = tmp_path / "s.mat"
+    qp.export_adaptive_mat(q, desc, 256, 320, u, -u, layout=qp.MAT_STEP)
+    t = sio.loadmat(q)["velocities16x16"][0, 0]
+    assert t["adaptiveStep"][0, 0] == len(levels) - 1
+    np.testing.assert_array_equal(t["u"][:, :, 1], u[1])
 
 
 def test_mat_export_rejects(qp, tmp_path):
