@@ -56,7 +56,10 @@ typedef enum {
 typedef enum {
     QLPIV_MAX_COMPUTE = 0, /* max of the clipped tile, floored at 16 (MatrixByte.java:16-33) */
     QLPIV_MAX_GIVEN = 1,   /* per-IA arrays supplied by the caller (Matrix.getMaxValue()) */
-    QLPIV_MAX_FIXED = 2    /* one constant per image (full-image warp tiles, MatrixByte.java:366-384) */
+    QLPIV_MAX_FIXED = 2,   /* one constant per image (full-image warp tiles, MatrixByte.java:366-384) */
+    QLPIV_MAX_FIXED_A = 3, /* A tiles fixed_max_a, B tiles computed (FirstImage warping: A cut from the
+                              warped frame, B clipped from the original) */
+    QLPIV_MAX_FIXED_B = 4  /* A tiles computed, B tiles fixed_max_b (SecondImage warping) */
 } qlpiv_max_mode;
 
 typedef enum {
@@ -138,7 +141,11 @@ typedef struct qlpiv_grid {
 
 typedef enum {
     QLPIV_WARP_NONE = 0,          /* NoImageWarping: B tiles at round(origin + displacement) */
-    QLPIV_WARP_BOTH_BILINEAR = 1, /* BothImagesBiLinearWarping (BiLinearImageWarpingStrategy) */
+    QLPIV_WARP_BOTH_BILINEAR = 1, /* BothImagesBiLinearWarping (BiLinearImageWarpingStrategy): both
+                                     frames warped by half the field */
+    QLPIV_WARP_FIRST_BILINEAR = 2,  /* FirstImageBiLinearWarping: A warped by the whole field, B tiles
+                                       clipped from the original frame */
+    QLPIV_WARP_SECOND_BILINEAR = 3, /* SecondImageBiLinearWarping: B warped, A tiles clipped */
     /* BiLinearImageMicroAndMiniWarpingStrategy (S/images/BiLinearImageMicroAndMiniWarpingStrategy.java):
      * every tile warped on its own; micro: by its fractional displacement, mini: by a bicubic
      * spline over its up to 7 x 7 neighbour tiles.  Warped tiles keep the full-scale maximum,
@@ -318,12 +325,14 @@ qlpiv_status qlpiv_inherit_tiles(qlpiv_handle *h, int mode, int pn, int pni, int
 qlpiv_status qlpiv_displacement_field(qlpiv_handle *h, int height, int width, int ni, int nj, const double *ci,
                                       const double *cj, const float *u, const float *v, float *fu, float *fv);
 
-/* IImageWarpingStrategy.warpAndClipImage for BothImages bilinear warping
- * (S/images/BiLinearImageWarpingStrategy.java:38-265): both images warped by half the
- * field through the level's tile displacements.  Host arrays, out_a/out_b as the input
- * pixel type (u8 or u16). */
-qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, const void *img_a, const void *img_b, int height,
-                             int width, int ni, int nj, const double *ci, const double *cj, const float *u,
+/* IImageWarpingStrategy.warpAndClipImage for full-image bilinear warping
+ * (S/images/BiLinearImageWarpingStrategy.java:38-265) through the level's tile displacements:
+ * warp_mode QLPIV_WARP_BOTH_BILINEAR warps both images by half the field, FIRST warps image A
+ * (sampled at (i - u, j - v)) and SECOND image B (at (i + u, j + v)) by the whole field; the
+ * image that is not warped is copied unchanged.  Host arrays, out_a/out_b as the input pixel type
+ * (u8 or u16). */
+qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, int warp_mode, const void *img_a, const void *img_b,
+                             int height, int width, int ni, int nj, const double *ci, const double *cj, const float *u,
                              const float *v, int int16_quirk, void *out_a, void *out_b);
 
 /* Micro / mini per-tile warping of one pair's tiles (BiLinearImageMicroAndMiniWarpingStrategy

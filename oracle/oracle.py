@@ -88,6 +88,7 @@ def lib():
         L.orc_displacement_field_off.argtypes = [dp, c_int, dp, c_int, fp, fp, c_int, c_int, c_int, c_float, c_float,
                                                  fp, fp]
         L.orc_warp_both.argtypes = [vp, vp, c_int, c_int, c_int, fp, fp, c_int, vp, vp]
+        L.orc_warp_full.argtypes = [vp, vp, c_int, c_int, c_int, fp, fp, c_int, c_int, vp, vp]
         L.orc_inherit.argtypes = [dp, c_int, dp, c_int, fp, fp, fp, c_int, fp, c_int, c_int, c_int, fp, fp]
         L.orc_piv_adaptive.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_float,
                                        c_int, c_int, c_int, fp, fp, ip, ip, vp]
@@ -291,6 +292,7 @@ def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+WARP_FIRST_BILINEAR, WARP_SECOND_BILINEAR = 2, 3
 WARP_FIRST_MICRO, WARP_SECOND_MICRO, WARP_BOTH_MICRO, WARP_FIRST_MINI, WARP_SECOND_MINI, WARP_BOTH_MINI = range(4, 10)
 
 
@@ -327,13 +329,15 @@ def displacement_field(ys, xs, u, v, h, w, precision=32, offset=0.0):
     return fu, fv
 
 
-def warp_both(img_a, img_b, fu, fv, int16_quirk=False):
+def warp_both(img_a, img_b, fu, fv, int16_quirk=False, image_mode=3):
+    """Full-image warp: image_mode 3 both frames by half the field, 1 frame A, 2 frame B by the
+    whole field (the other frame copied)."""
     img_a, img_b = np.ascontiguousarray(img_a), np.ascontiguousarray(img_b)
     fu, fv = _f32(fu), _f32(fv)
     oa, ob = np.zeros_like(img_a), np.zeros_like(img_b)
-    lib().orc_warp_both(img_a.ctypes.data, img_b.ctypes.data, img_a.shape[0], img_a.shape[1], img_a.dtype.itemsize,
-                        _ptr(fu, ctypes.c_float), _ptr(fv, ctypes.c_float), int(int16_quirk), oa.ctypes.data,
-                        ob.ctypes.data)
+    lib().orc_warp_full(img_a.ctypes.data, img_b.ctypes.data, img_a.shape[0], img_a.shape[1], img_a.dtype.itemsize,
+                        _ptr(fu, ctypes.c_float), _ptr(fv, ctypes.c_float), int(int16_quirk), int(image_mode),
+                        oa.ctypes.data, ob.ctypes.data)
     return oa, ob
 
 

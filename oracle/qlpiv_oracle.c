@@ -217,7 +217,9 @@ int orc_grid_nosuperposition(int h, int w, int mtop, int mbottom, int mleft, int
  * norm_mode: 0 = both tiles by tile A's max (reference CPU path),
  *            1 = each tile by its own max (reference OpenCL path),
  *            2 = fixed maxima fixed_max_a / fixed_max_b (full-image warp tiles),
- *            3 = raw values (no normalisation).
+ *            3 = raw values (no normalisation);
+ *            | 8: first replace the tile maxima by fixed_max_a / fixed_max_b where those are > 0
+ *            (FirstImage / SecondImage warping: only the warped side keeps a fixed maximum).
  * precision: 0 = FP32 restatement, 1 = FP64 twin.
  * Work is split over nthreads POSIX threads by IA index.
  * ------------------------------------------------------------------------- */
@@ -242,7 +244,11 @@ static void *orc_worker(void *arg) {
         float maxA = orc_clip_tile(j->img_a, j->h, j->w, j->pix_bytes, j->a_top[k], j->a_left[k], n, ta);
         float maxB = orc_clip_tile(j->img_b, j->h, j->w, j->pix_bytes, j->b_top[k], j->b_left[k], n, tb);
         int normalize = 1;
-        switch (j->norm_mode) {
+        if (j->norm_mode & 8) {
+            if (j->fixed_max_a > 0.0f) maxA = j->fixed_max_a;
+            if (j->fixed_max_b > 0.0f) maxB = j->fixed_max_b;
+        }
+        switch (j->norm_mode & 7) {
             case 0: maxB = maxA; break;
             case 1: break;
             case 2: maxA = j->fixed_max_a; maxB = j->fixed_max_b; break;

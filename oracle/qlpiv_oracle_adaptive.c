@@ -200,14 +200,33 @@ void orc_displacement_field(const double *ys, int ni, const double *xs, int nj, 
 }
 
 /* BothImages bilinear warp of a pair with a per-pixel field (halved inside). */
-void orc_warp_both(const void *img_a, const void *img_b, int h, int w, int pix_bytes, const float *fu, const float *fv,
-                   int int16_quirk, void *out_a, void *out_b) {
+/* image_mode: 3 BothImages (both frames, half the field), 1 FirstImage (frame A, whole field),
+ * 2 SecondImage (frame B, whole field) -- BiLinearImageWarpingStrategy.doBiLinearWarp
+ * (S/images/BiLinearImageWarpingStrategy.java:143-183).  The frame that is not warped is copied. */
+void orc_warp_full(const void *img_a, const void *img_b, int h, int w, int pix_bytes, const float *fu, const float *fv,
+                   int int16_quirk, int image_mode, void *out_a, void *out_b) {
     for (int i = 0; i < h; i++)
         for (int j = 0; j < w; j++) {
-            const float u = fu[(size_t)i * w + j] / 2.0f, v = fv[(size_t)i * w + j] / 2.0f;
-            store_pix(out_a, pix_bytes, w, i, j, warp_pixel(img_a, pix_bytes, h, w, u, v, i, j, 1), int16_quirk);
-            store_pix(out_b, pix_bytes, w, i, j, warp_pixel(img_b, pix_bytes, h, w, u, v, i, j, 0), int16_quirk);
+            float u = fu[(size_t)i * w + j], v = fv[(size_t)i * w + j];
+            if (image_mode == 3) {
+                u /= 2.0f;
+                v /= 2.0f;
+            }
+            const size_t off = ((size_t)i * w + j) * pix_bytes;
+            if (image_mode & 1)
+                store_pix(out_a, pix_bytes, w, i, j, warp_pixel(img_a, pix_bytes, h, w, u, v, i, j, 1), int16_quirk);
+            else
+                memcpy((char *)out_a + off, (const char *)img_a + off, pix_bytes);
+            if (image_mode & 2)
+                store_pix(out_b, pix_bytes, w, i, j, warp_pixel(img_b, pix_bytes, h, w, u, v, i, j, 0), int16_quirk);
+            else
+                memcpy((char *)out_b + off, (const char *)img_b + off, pix_bytes);
         }
+}
+
+void orc_warp_both(const void *img_a, const void *img_b, int h, int w, int pix_bytes, const float *fu, const float *fv,
+                   int int16_quirk, void *out_a, void *out_b) {
+    orc_warp_full(img_a, img_b, h, w, pix_bytes, fu, fv, int16_quirk, 3, out_a, out_b);
 }
 
 /* Micro / mini per-tile warping (BiLinearImageMicroAndMiniWarpingStrategy.warpAndClipImage,
@@ -427,9 +446,10 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
                 orc_tile_warp(img_a, img_b, h, w, pix_bytes, n, ni, nj, tops, lefts, cu, cv, (warp_mode - 4) % 3 + 1,
                               warp_mode >= 7, full, wta, wtb, wma, wmb);
             }
-            if (warp_mode == 1) {
+            if (warp_mode >= 1 && warp_mode <= 3) {
                 orc_displacement_field(cyd, ni, cxd, nj, cu, cv, h, w, precision, fu, fv);
-                orc_warp_both(img_a, img_b, h, w, pix_bytes, fu, fv, int16_quirk, wa, wb);
+                orc_warp_full(img_a, img_b, h, w, pix_bytes, fu, fv, int16_quirk,
+                              warp_mode == 1 ? 3 : (warp_mode == 2 ? 1 : 2), wa, wb);
                 sa = wa; sb = wb;
             }
         }
@@ -444,8 +464,15 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
                 bt[k] = warp_mode == 0 ? java_round((float)tops[i] + cu[k]) : tops[i];
                 bl[k] = warp_mode == 0 ? java_round((float)lefts[j] + cv[k]) : lefts[j];
             }
-        const float fm = fixed_max > 0.0f && !per_tile ? fixed_max : 0.0f;
-        const int nm = fixed_max > 0.0f && !per_tile ? 2 : norm_mode;
+        float fm = fixed_max > 0.0f && !per_tile ? fixed_max : 0.0f, fma = fm, fmb = fm;
+        int nm = fixed_max > 0.0f && !per_tile ? 2 : norm_mode;
+        if (fm > 0.0f && (warp_mode == 2 || warp_mode == 3)) {
+            /* FirstImage / SecondImage: the tiles cut from the warped (level 0: whole) frame keep the
+             * fixed maximum, the tiles clipped from the other frame their own (Image.clipImageMatrix) */
+            nm = norm_mode | 8;
+            fma = warp_mode == 2 ? fm : 0.0f;
+            fmb = warp_mode == 3 ? fm : 0.0f;
+        }
         orc_vector *vec = (orc_vector *)malloc(sizeof(orc_vector) * cnt);
         orc_vector *mvec = NULL;
         int *npk = NULL;
@@ -456,13 +483,13 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
             if (wta)
                 orc_tiles_pass(wta, wtb, wma, wmb, cnt, n, norm_mode, 1, precision, val->kernel_width, kpk, mvec, npk);
             else
-                orc_piv_pass_multi(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, nm, fm, fm, 1, precision,
+                orc_piv_pass_multi(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, nm, fma, fmb, 1, precision,
                                    val->kernel_width, kpk, mvec, npk, nthreads);
             for (long k = 0; k < cnt; k++) vec[k] = mvec[k * kpk];
         } else if (wta) {
             orc_tiles_pass(wta, wtb, wma, wmb, cnt, n, norm_mode, 1, precision, 0, 0, vec, NULL);
         } else {
-            orc_piv_pass(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, nm, fm, fm, 1, precision, vec, nthreads);
+            orc_piv_pass(sa, sb, h, w, pix_bytes, n, cnt, at, al, bt, bl, nm, fma, fmb, 1, precision, vec, nthreads);
         }
         free(wta); free(wtb); free(wma); free(wmb);
         if (level_vectors) memcpy(level_vectors + vec_off, vec, sizeof(orc_vector) * cnt);

@@ -20,7 +20,7 @@ LIB_PATH = _build.LIB
 OK, E_ARG, E_SHAPE, E_OOM, E_CUDA, E_TIMEOUT, E_CANCELLED, E_UNSUPPORTED, E_NO_DEVICE = range(9)
 PIX_U8, PIX_U16, PIX_F32 = 0, 1, 2
 NORM_MAX_A, NORM_OWN_MAX, NORM_NONE = 0, 1, 3
-MAX_COMPUTE, MAX_GIVEN, MAX_FIXED = 0, 1, 2
+MAX_COMPUTE, MAX_GIVEN, MAX_FIXED, MAX_FIXED_A, MAX_FIXED_B = 0, 1, 2, 3, 4
 SUBPIX_NONE, SUBPIX_GAUSS3, SUBPIX_GAUSS_LM, SUBPIX_HONGWEI_GUO = 0, 1, 2, 3
 MAX_SUBPIX_PIXELS = 15
 F_SUB_I, F_SUB_J, F_PARABOLIC, F_EDGE, F_NO_PEAK, F_ABSENT, F_FLOOR = 1, 2, 4, 8, 16, 32, 64
@@ -67,7 +67,7 @@ class Grid(ctypes.Structure):
                 ("n", "tiles_i", "tiles_j", "margin_top", "margin_left", "margin_bottom", "margin_right")]
 
 
-WARP_NONE, WARP_BOTH_BILINEAR = 0, 1
+WARP_NONE, WARP_BOTH_BILINEAR, WARP_FIRST_BILINEAR, WARP_SECOND_BILINEAR = 0, 1, 2, 3
 WARP_FIRST_MICRO, WARP_SECOND_MICRO, WARP_BOTH_MICRO, WARP_FIRST_MINI, WARP_SECOND_MINI, WARP_BOTH_MINI = range(4, 10)
 
 
@@ -215,7 +215,7 @@ _SIGNATURES = {
     "qlpiv_inherit": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp]),
     "qlpiv_inherit_tiles": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),
     "qlpiv_displacement_field": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
-    "qlpiv_warp_pair": (_i, [_vp, _i, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
+    "qlpiv_warp_pair": (_i, [_vp, _i, _i, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "qlpiv_tile_warp": (_i, [_vp, _i, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _f, _vp, _vp, _vp, _vp]),
     "qlpiv_piv_adaptive": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
     "qlpiv_piv_adaptive_device": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _vp, _vp, _vp]),
@@ -573,7 +573,9 @@ class Handle:
                                                   _addr(u), _addr(v), _addr(fu), _addr(fv)))
         return fu, fv
 
-    def warp_pair(self, img_a, img_b, ci, cj, u, v, int16_quirk=False):
+    def warp_pair(self, img_a, img_b, ci, cj, u, v, int16_quirk=False, warp_mode=None):
+        """Full-image bilinear warp of one pair (BothImages by default, or WARP_FIRST_BILINEAR /
+        WARP_SECOND_BILINEAR); the frame that is not warped comes back unchanged."""
         ia = np.ascontiguousarray(img_a)
         ib = np.ascontiguousarray(img_b)
         ci = np.ascontiguousarray(ci, np.float64)
@@ -582,7 +584,8 @@ class Handle:
         v = np.ascontiguousarray(v, np.float32)
         oa = np.empty_like(ia)
         ob = np.empty_like(ib)
-        _check(self._lib.qlpiv_warp_pair(self._h, pixel_type_of(ia.dtype), _addr(ia), _addr(ib), ia.shape[0],
+        mode = WARP_BOTH_BILINEAR if warp_mode is None else warp_mode
+        _check(self._lib.qlpiv_warp_pair(self._h, pixel_type_of(ia.dtype), mode, _addr(ia), _addr(ib), ia.shape[0],
                                          ia.shape[1], len(ci), len(cj), _addr(ci), _addr(cj), _addr(u), _addr(v),
                                          int(int16_quirk), _addr(oa), _addr(ob)))
         return oa, ob

@@ -426,11 +426,14 @@ __host__ __device__ __forceinline__ float field_value(const float *ys, int ni, c
     return w[0] * Y0 + w[1] * Y1 + w[2] * Y2 + w[3] * Y3;
 }
 
-// Pixel (i, j) of pair `pair`: field, then both warped pixels.
+// Pixel (i, j) of pair `pair`: field, then the warped pixels.  image_mode 3 (BothImages) warps
+// both frames by half the field, 1 (FirstImage) frame A and 2 (SecondImage) frame B by the whole
+// field (BiLinearImageWarpingStrategy.doBiLinearWarp, :162-181); the other frame is copied as is.
 template <typename Pix>
 __host__ __device__ __forceinline__ void warp_one(int pair, int i, int j, const qlpiv_frame *src,
                                                   const qlpiv_frame *dst, const float *ys, int ni, const float *xs,
-                                                  int nj, const float4 *c4u, const float4 *c4v, int int16_quirk) {
+                                                  int nj, const float4 *c4u, const float4 *c4v, int int16_quirk,
+                                                  int image_mode) {
     const qlpiv_frame fs = src[pair];
     const int h = fs.height, w = fs.width;
     if (i >= h || j >= w) return;
@@ -442,13 +445,18 @@ __host__ __device__ __forceinline__ void warp_one(int pair, int i, int j, const 
     if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
     const float fu = field_value(ys, ni, xs, nj, c4u + base, y, x);
     const float fv = field_value(ys, ni, xs, nj, c4v + base, y, x);
-    const float hu = fu / 2.0f, hv = fv / 2.0f;
+    const bool both = image_mode == 3;
+    const float hu = both ? fu / 2.0f : fu, hv = both ? fv / 2.0f : fv;
     const Pix *ia = reinterpret_cast<const Pix *>(fs.img_a);
     const Pix *ib = reinterpret_cast<const Pix *>(fs.img_b);
     Pix *oa = reinterpret_cast<Pix *>(const_cast<void *>(fd.img_a));
     Pix *ob = reinterpret_cast<Pix *>(const_cast<void *>(fd.img_b));
-    oa[(long)i * fd.pitch + j] = warp_store<Pix>(warp_pixel(ia, h, w, fs.pitch, hu, hv, i, j, true), int16_quirk);
-    ob[(long)i * fd.pitch + j] = warp_store<Pix>(warp_pixel(ib, h, w, fs.pitch, hu, hv, i, j, false), int16_quirk);
+    oa[(long)i * fd.pitch + j] = image_mode & 1
+        ? warp_store<Pix>(warp_pixel(ia, h, w, fs.pitch, hu, hv, i, j, true), int16_quirk)
+        : ia[(long)i * fs.pitch + j];
+    ob[(long)i * fd.pitch + j] = image_mode & 2
+        ? warp_store<Pix>(warp_pixel(ib, h, w, fs.pitch, hu, hv, i, j, false), int16_quirk)
+        : ib[(long)i * fs.pitch + j];
 }
 
 // One thread per pixel of one pair (blockIdx.z = pair).  src/dst frame tables hold the
@@ -456,10 +464,11 @@ __host__ __device__ __forceinline__ void warp_one(int pair, int i, int j, const 
 template <typename Pix>
 __global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, const qlpiv_frame *dst,
                                                         const float *ys, int ni, const float *xs, int nj,
-                                                        const float4 *c4u, const float4 *c4v, int int16_quirk) {
+                                                        const float4 *c4u, const float4 *c4v, int int16_quirk,
+                                                        int image_mode) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    warp_one<Pix>(blockIdx.z, i, j, src, dst, ys, ni, xs, nj, c4u, c4v, int16_quirk);
+    warp_one<Pix>(blockIdx.z, i, j, src, dst, ys, ni, xs, nj, c4u, c4v, int16_quirk, image_mode);
 }
 
 // ---------------- micro / mini per-tile warping ----------------
@@ -696,12 +705,15 @@ cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const dou
 
 cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
                         const qlpiv_frame *dst, const float *ys, int ni, const float *xs, int nj, SplineCoef coef,
-                        int int16_quirk) {
+                        int int16_quirk, int image_mode) {
+    if (image_mode < 1 || image_mode > 3) return cudaErrorInvalidValue;
     dim3 blk(32, 8), grd(blocks_for(w, 32), blocks_for(h, 8), pairs);
     if (pixel_type == QLPIV_PIX_U8)
-        warp_both_kernel<uint8_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk);
+        warp_both_kernel<uint8_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk,
+                                                      image_mode);
     else if (pixel_type == QLPIV_PIX_U16)
-        warp_both_kernel<uint16_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk);
+        warp_both_kernel<uint16_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk,
+                                                       image_mode);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();

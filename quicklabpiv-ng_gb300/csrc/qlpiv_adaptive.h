@@ -45,7 +45,7 @@ cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const dou
                           const double *cpx, int nj, const float *u, const float *v, SplineCoef coef);
 cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
                         const qlpiv_frame *dst, const float *ys, int ni, const float *xs, int nj, SplineCoef coef,
-                        int int16_quirk);
+                        int int16_quirk, int image_mode);
 // Micro / mini per-tile warping of every pair's tiles (grid tops[ni] x lefts[nj], side n; tile
 // displacements cu / cv [pairs][ni*nj]); image_mode 1 first, 2 second, 3 both.  Writes
 // [pairs][tiles][n][n] pixels of pixel_type and per-tile maxima.

@@ -67,9 +67,12 @@ qlpiv_status check_desc(const qlpiv_pass_desc *d) {
         return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64, 128)", d->n);
     if (d->norm_mode != QLPIV_NORM_MAX_A && d->norm_mode != QLPIV_NORM_OWN_MAX && d->norm_mode != QLPIV_NORM_NONE)
         return fail(QLPIV_E_ARG, "unknown normalisation mode %d", d->norm_mode);
-    if (d->max_mode != QLPIV_MAX_COMPUTE && d->max_mode != QLPIV_MAX_FIXED)
+    if (d->max_mode != QLPIV_MAX_COMPUTE && d->max_mode != QLPIV_MAX_FIXED && d->max_mode != QLPIV_MAX_FIXED_A &&
+        d->max_mode != QLPIV_MAX_FIXED_B)
         return fail(QLPIV_E_ARG, "max mode %d not valid for a frame pass", d->max_mode);
-    if (d->max_mode == QLPIV_MAX_FIXED && !(d->fixed_max_a > 0.0f && d->fixed_max_b > 0.0f))
+    if ((d->max_mode == QLPIV_MAX_FIXED || d->max_mode == QLPIV_MAX_FIXED_A) && !(d->fixed_max_a > 0.0f))
+        return fail(QLPIV_E_ARG, "fixed tile maxima must be positive");
+    if ((d->max_mode == QLPIV_MAX_FIXED || d->max_mode == QLPIV_MAX_FIXED_B) && !(d->fixed_max_b > 0.0f))
         return fail(QLPIV_E_ARG, "fixed tile maxima must be positive");
     if (qlpiv_status st = qlpiv::check_subpix(d->subpix_mode, d->subpix_pixels, d->subpix_iterations)) return st;
     if (d->num_peaks != 0 && !qlpiv::multipeak_supported(d->n, d->num_peaks, d->peak_kernel))

@@ -82,6 +82,11 @@ static float full_scale(int pixel_type) { return pixel_type == QLPIV_PIX_U8 ? 25
 
 // Micro / mini per-tile warping modes: image mode (1 first, 2 second, 3 both) and mini flag.
 static bool per_tile_warp(int m) { return m >= QLPIV_WARP_FIRST_MICRO && m <= QLPIV_WARP_BOTH_MINI; }
+// Full-image bilinear warping (BiLinearImageWarpingStrategy): image mode 1 first, 2 second, 3 both.
+static bool full_warp(int m) { return m >= QLPIV_WARP_BOTH_BILINEAR && m <= QLPIV_WARP_SECOND_BILINEAR; }
+static int full_image_mode(int m) {
+    return m == QLPIV_WARP_BOTH_BILINEAR ? 3 : (m == QLPIV_WARP_FIRST_BILINEAR ? 1 : 2);
+}
 static int tile_image_mode(int m) { return (m - QLPIV_WARP_FIRST_MICRO) % 3 + 1; }
 static bool tile_mini(int m) { return m >= QLPIV_WARP_FIRST_MINI; }
 
@@ -96,7 +101,7 @@ static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type,
     if ((r & (r - 1)) != 0) return fail(QLPIV_E_ARG, "IA start / end ratio is not a power of two");
     for (int n = d->ia_start; n >= d->ia_end; n >>= 1)
         if (!xcorr_size_supported(n)) return fail(QLPIV_E_SHAPE, "IA size %d is not supported (16, 32, 64, 128)", n);
-    if (d->warp_mode != QLPIV_WARP_NONE && d->warp_mode != QLPIV_WARP_BOTH_BILINEAR && !per_tile_warp(d->warp_mode))
+    if (d->warp_mode != QLPIV_WARP_NONE && !full_warp(d->warp_mode) && !per_tile_warp(d->warp_mode))
         return fail(QLPIV_E_ARG, "unknown warp mode %d", d->warp_mode);
     if (d->norm_mode != QLPIV_NORM_MAX_A && d->norm_mode != QLPIV_NORM_OWN_MAX && d->norm_mode != QLPIV_NORM_NONE)
         return fail(QLPIV_E_ARG, "unknown normalisation mode %d", d->norm_mode);
@@ -233,7 +238,7 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
         if (grid_superposition(height, width, d->margins, d->ia_start, lv, d->overlap_factor, &L.g, nullptr, nullptr,
                                0) < -1)
             return fail(QLPIV_E_SHAPE, "image too small for IA %d at level %d", d->ia_start >> lv, lv);
-        if ((d->warp_mode == QLPIV_WARP_BOTH_BILINEAR || per_tile_warp(d->warp_mode)) && lv > 0 &&
+        if ((full_warp(d->warp_mode) || per_tile_warp(d->warp_mode)) && lv > 0 &&
             (L.g.tiles_i < 3 || L.g.tiles_j < 3))
             return fail(QLPIV_E_SHAPE, "level %d has %d x %d tiles: the warp spline needs at least 3 per axis", lv,
                         L.g.tiles_i, L.g.tiles_j);
@@ -318,7 +323,7 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
         // the host vectors above die at scope exit: make the copies complete first
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "adaptive plan upload");
     }
-    if (d->warp_mode == QLPIV_WARP_BOTH_BILINEAR) {
+    if (full_warp(d->warp_mode)) {
         const size_t img = (size_t)height * width * pixel_bytes(pixel_type);
         const size_t stride = (img + 255) & ~(size_t)255;
         if ((e = p->warped.ensure(2 * stride * pairs)) != cudaSuccess ||
@@ -422,7 +427,7 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
             h->launches++;
         } else if (per_tile_warp(d.warp_mode)) {
             // level 0: both tiles clipped at the grid (the displacements are zero)
-        } else if (d.warp_mode == QLPIV_WARP_BOTH_BILINEAR) {
+        } else if (full_warp(d.warp_mode)) {
             if (lv > 0) {  // no warping at the first level: displacements are all zero
                 SplineCoef c = coef_of(L, pairs);
                 {
@@ -436,7 +441,8 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
                     StageScope sc(h, "warp", (int)lv, L.g.n, 1, (long)pairs * p->height * p->width);
                     if ((e = launch_warp(s, p->pixel_type, pairs, p->height, p->width, frames_dev,
                                          p->warped_table.as<qlpiv_frame>(), L.d_cyf.as<float>(), L.g.tiles_i,
-                                         L.d_cxf.as<float>(), L.g.tiles_j, c, d.int16_warp_quirk)) != cudaSuccess)
+                                         L.d_cxf.as<float>(), L.g.tiles_j, c, d.int16_warp_quirk,
+                                         full_image_mode(d.warp_mode))) != cudaSuccess)
                         return cuda_fail(e, "warp");
                 }
                 h->launches += 5;
@@ -462,6 +468,10 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
         job.norm_mode = d.norm_mode;
         job.max_mode = d.max_mode;
         job.fixed_max_a = job.fixed_max_b = fm;
+        // FirstImage / SecondImage: tiles cut from the warped (or, at level 0, the whole) frame keep
+        // the fixed maximum, tiles clipped from the other frame their own (Image.clipImageMatrix)
+        if (d.max_mode == QLPIV_MAX_FIXED && d.warp_mode == QLPIV_WARP_FIRST_BILINEAR) job.max_mode = QLPIV_MAX_FIXED_A;
+        if (d.max_mode == QLPIV_MAX_FIXED && d.warp_mode == QLPIV_WARP_SECOND_BILINEAR) job.max_mode = QLPIV_MAX_FIXED_B;
         if (per_tile_warp(d.warp_mode)) {
             job.max_mode = QLPIV_MAX_COMPUTE;  // level 0: clipped tiles
             if (tiles) {  // the warped tiles, contiguous, with their maxima
@@ -580,7 +590,7 @@ size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int heigh
     const size_t img = (size_t)height * width * pixel_bytes(pixel_type);
     const size_t stride = (img + 255) & ~(size_t)255;
     total += al(2 * stride * pairs) + al(sizeof(qlpiv_frame) * pairs);  // frames copied from the host
-    if (d->warp_mode == QLPIV_WARP_BOTH_BILINEAR) total += al(2 * stride * pairs) + al(sizeof(qlpiv_frame) * pairs);
+    if (full_warp(d->warp_mode)) total += al(2 * stride * pairs) + al(sizeof(qlpiv_frame) * pairs);
     return total;
 }
 
@@ -789,10 +799,11 @@ qlpiv_status qlpiv_displacement_field(qlpiv_handle *h, int height, int width, in
     return QLPIV_OK;
 }
 
-qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, const void *img_a, const void *img_b, int height,
-                             int width, int ni, int nj, const double *ci, const double *cj, const float *u,
+qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, int warp_mode, const void *img_a, const void *img_b,
+                             int height, int width, int ni, int nj, const double *ci, const double *cj, const float *u,
                              const float *v, int int16_quirk, void *out_a, void *out_b) {
     if (!h || !img_a || !img_b || !ci || !cj || !u || !v || !out_a || !out_b) return fail(QLPIV_E_ARG, "NULL argument");
+    if (!full_warp(warp_mode)) return fail(QLPIV_E_ARG, "warp mode %d is not a full-image bilinear warp", warp_mode);
     if (pixel_type != QLPIV_PIX_U8 && pixel_type != QLPIV_PIX_U16) return fail(QLPIV_E_ARG, "u8 or u16 images only");
     if (ni < 3 || nj < 3) return fail(QLPIV_E_SHAPE, "the spline needs at least 3 tiles per axis");
     if (height <= 0 || width <= 0) return fail(QLPIV_E_SHAPE, "image size %d x %d", height, width);
@@ -819,7 +830,7 @@ qlpiv_status qlpiv_warp_pair(qlpiv_handle *h, int pixel_type, const void *img_a,
     const qlpiv_frame *dt = h->frames.as<qlpiv_frame>();
     DevBuf *b = h->scratch;
     if ((e = launch_warp(s, pixel_type, 1, height, width, dt, dt + 1, b[8].as<float>(), ni, b[8].as<float>() + ni, nj,
-                         coef, int16_quirk)) != cudaSuccess)
+                         coef, int16_quirk, full_image_mode(warp_mode))) != cudaSuccess)
         return cuda_fail(e, "warp");
     h->launches++;
     if ((e = cudaMemcpyAsync(out_a, base + 2 * stride, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||

@@ -722,7 +722,8 @@ xcorr_kernel(IaJob job) {
             }
         }
         float maxA, maxB;
-        if (job.max_mode == QLPIV_MAX_COMPUTE) {
+        if (job.max_mode == QLPIV_MAX_COMPUTE || job.max_mode == QLPIV_MAX_FIXED_A ||
+            job.max_mode == QLPIV_MAX_FIXED_B) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 mxa = fmaxf(mxa, __shfl_xor_sync(0xffffffffu, mxa, o));
@@ -734,8 +735,8 @@ xcorr_kernel(IaJob job) {
             mxa = 0.0f; mxb = 0.0f;
 #pragma unroll
             for (int k = 0; k < NWARPS; k++) { mxa = fmaxf(mxa, redf[k]); mxb = fmaxf(mxb, redf[32 + k]); }
-            maxA = fmaxf(mxa, 16.0f);
-            maxB = fmaxf(mxb, 16.0f);
+            maxA = job.max_mode == QLPIV_MAX_FIXED_A ? job.fixed_max_a : fmaxf(mxa, 16.0f);
+            maxB = job.max_mode == QLPIV_MAX_FIXED_B ? job.fixed_max_b : fmaxf(mxb, 16.0f);
         } else if (job.max_mode == QLPIV_MAX_GIVEN) {
             maxA = job.max_a[ia];
             maxB = job.max_b[ia];

@@ -134,7 +134,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
 
         // ---- 1. tile maxima (each CTA reads both whole tiles) ----
         float maxA, maxB;
-        if (job.max_mode == QLPIV_MAX_COMPUTE) {
+        if (job.max_mode == QLPIV_MAX_COMPUTE || job.max_mode == QLPIV_MAX_FIXED_A ||
+            job.max_mode == QLPIV_MAX_FIXED_B) {
             float mxa = 0.0f, mxb = 0.0f;
             for (int k = tid; k < N * N; k += T) {
                 const int y = k / N, x = k % N;
@@ -152,8 +153,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
             mxa = 0.0f; mxb = 0.0f;
 #pragma unroll
             for (int k = 0; k < NWARPS; k++) { mxa = fmaxf(mxa, redf[k]); mxb = fmaxf(mxb, redf[32 + k]); }
-            maxA = fmaxf(mxa, 16.0f);
-            maxB = fmaxf(mxb, 16.0f);
+            maxA = job.max_mode == QLPIV_MAX_FIXED_A ? job.fixed_max_a : fmaxf(mxa, 16.0f);
+            maxB = job.max_mode == QLPIV_MAX_FIXED_B ? job.fixed_max_b : fmaxf(mxb, 16.0f);
         } else if (job.max_mode == QLPIV_MAX_GIVEN) {
             maxA = job.max_a[ia];
             maxB = job.max_b[ia];

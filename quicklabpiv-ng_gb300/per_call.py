@@ -9,8 +9,9 @@ data), and it is the denominator of the batched path's speed-up.  It runs the sa
 """
 import numpy as np
 
-from . import (F_ABSENT, MAX_COMPUTE, VALIDATE_MULTIPEAK_MEDIAN, WARP_BOTH_BILINEAR, WARP_BOTH_MINI,
-               WARP_FIRST_MICRO, WARP_NONE, adaptive_levels, grid)
+from . import (F_ABSENT, MAX_COMPUTE, MAX_FIXED, MAX_FIXED_A, MAX_FIXED_B, VALIDATE_MULTIPEAK_MEDIAN,
+               WARP_BOTH_BILINEAR, WARP_BOTH_MINI, WARP_FIRST_BILINEAR, WARP_FIRST_MICRO, WARP_NONE,
+               WARP_SECOND_BILINEAR, adaptive_levels, grid)
 
 
 def _java_round(x):
@@ -26,7 +27,12 @@ def piv_adaptive_per_call(handle, img_a, img_b, desc):
     levels = adaptive_levels(desc, h, w)
     fm = desc.fixed_max if desc.fixed_max > 0 else (255.0 if a.dtype == np.uint8 else 65535.0)
     validate = desc.validation == VALIDATE_MULTIPEAK_MEDIAN
-    pass_kw = dict(norm_mode=desc.norm_mode, max_mode=desc.max_mode, fixed_max=(fm, fm),
+    max_mode = desc.max_mode
+    if max_mode == MAX_FIXED and desc.warp_mode == WARP_FIRST_BILINEAR:
+        max_mode = MAX_FIXED_A     # tiles of the warped first frame keep the fixed maximum
+    if max_mode == MAX_FIXED and desc.warp_mode == WARP_SECOND_BILINEAR:
+        max_mode = MAX_FIXED_B
+    pass_kw = dict(norm_mode=desc.norm_mode, max_mode=max_mode, fixed_max=(fm, fm),
                    subpix_mode=desc.subpix_mode)
     if validate:
         pass_kw.update(num_peaks=desc.num_peaks, peak_kernel=desc.peak_kernel)
@@ -64,10 +70,10 @@ def piv_adaptive_per_call(handle, img_a, img_b, desc):
                                               **tkw) if validate else handle.xcorr_peaks(ta, tb, ma, mb, **tkw)
             else:        # level 0: both tiles clipped with their own maxima
                 vec = handle.piv_pass(a, b, n, at, al, **dict(pass_kw, max_mode=MAX_COMPUTE))
-        elif desc.warp_mode == WARP_BOTH_BILINEAR:
+        elif desc.warp_mode in (WARP_BOTH_BILINEAR, WARP_FIRST_BILINEAR, WARP_SECOND_BILINEAR):
             if lv > 0:
                 src_a, src_b = handle.warp_pair(a, b, cy.astype(np.float64), cx.astype(np.float64), u, v,
-                                                int16_quirk=bool(desc.int16_warp_quirk))
+                                                int16_quirk=bool(desc.int16_warp_quirk), warp_mode=desc.warp_mode)
         else:
             bt = _java_round(at.astype(np.float32) + u.ravel())
             bl = _java_round(al.astype(np.float32) + v.ravel())

@@ -90,6 +90,34 @@ def test_warp_pair_bit_exact(qp, handle, oracle, bits, quirk):
     oa, ob = oracle.warp_both(a, b, fu, fv, int16_quirk=quirk)
     assert wa.dtype == a.dtype and wa.tobytes() == oa.tobytes() and wb.tobytes() == ob.tobytes()
     assert not np.array_equal(wa, a)
+    # FirstImage / SecondImage: one frame warped by the whole field, the other unchanged
+    for mode, image_mode in ((qp.WARP_FIRST_BILINEAR, 1), (qp.WARP_SECOND_BILINEAR, 2)):
+        wa, wb = handle.warp_pair(a, b, cy.astype(np.float64), cx.astype(np.float64), u, v, int16_quirk=quirk,
+                                  warp_mode=mode)
+        oa, ob = oracle.warp_both(a, b, fu, fv, int16_quirk=quirk, image_mode=image_mode)
+        assert wa.tobytes() == oa.tobytes() and wb.tobytes() == ob.tobytes()
+        assert np.array_equal(wb if image_mode == 1 else wa, b if image_mode == 1 else a)
+
+
+@pytest.mark.parametrize("mode,bits", [(2, 8), (3, 8), (2, 12), (3, 12)])
+def test_adaptive_first_second_image_warping(qp, handle, oracle, mode, bits):
+    """FirstImage / SecondImage full-image warping: the warped frame's tiles keep the full-scale
+    maximum, the other frame's tiles their own; against the FP32 and FP64 oracle and the per-call
+    path."""
+    h, w = 288, 320
+    flow = qp.synth.Flow(vmax=5.0, rc=56.0, shear=0.004)
+    pairs = [qp.synth.particle_pair((h, w), flow, ppp=0.03, diam=2.5, diam_sd=0.0, bits=bits, seed=90 + k + mode)
+             for k in range(2)]
+    fm = 255.0 if bits == 8 else 4095.0
+    desc = qp.adaptive_desc(64, 16, 0.5, warp_mode=mode, fixed_max=fm)
+    u, v = handle.piv_adaptive([p[0] for p in pairs], [p[1] for p in pairs], desc)
+    for k, (a, b) in enumerate(pairs):
+        for prec in (32, 64):
+            ou, ov = oracle.piv_adaptive(a, b, 64, 16, 0.5, fixed_max=fm, precision=prec, warp=mode)
+            err = np.maximum(np.abs(u[k] - ou), np.abs(v[k] - ov))
+            assert np.mean(err <= 1e-3) >= 0.97, (k, prec, float(np.mean(err <= 1e-3)))
+    pu, pv = qp.per_call.piv_adaptive_per_call(handle, pairs[0][0], pairs[0][1], desc)
+    assert pu.tobytes() == u[0].tobytes() and pv.tobytes() == v[0].tobytes()
 
 
 def _true_flow(qp, flow, g, shape):
