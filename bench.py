@@ -373,14 +373,14 @@ BATCH_WORKLOAD = ("batched-mixed: 256 u8 pairs, sides from {256, 512, 1024, 2048
                   "graph per batch with autotuned launches")
 
 
-def run_batched(pkg, dev, stream, steps, warmup, count=256):
+def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64, 128)):
     import torch
     rng = np.random.default_rng(3)
     a0, b0 = pkg.synth.particle_pair((2048, 2048), pkg.synth.Flow(vmax=8.0 - 0.003 * 1024, rc=180.0, shear=0.003),
                                      ppp=0.02, diam=3.0, bits=8, seed=33)
     ma, mb = np.tile(a0, (2, 2)), np.tile(b0, (2, 2))
     sides = rng.choice([256, 512, 1024, 2048], count)
-    sizes = rng.choice([16, 32, 64, 128], count).astype(np.int32)
+    sizes = rng.choice(list(ia_sizes), count).astype(np.int32)
     ofac = np.full(count, 0.5, np.float32)
     keep, host, table = [], [], np.zeros(count, pkg.FRAME_DTYPE)
     for k in range(count):
@@ -630,7 +630,21 @@ def main():
     ap.add_argument("--no-hybrid", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    # profiling aid: only the batched mixed-size leg (its own JSON line), optionally with fewer
+    # pairs and a subset of the IA sizes, so that one kernel can be captured on a small case
+    ap.add_argument("--only-batched", action="store_true")
+    ap.add_argument("--batched-pairs", type=int, default=256)
+    ap.add_argument("--batched-sizes", default="16,32,64,128")
     args = ap.parse_args()
+    if args.only_batched:
+        import torch
+        pkg = load_pkg()
+        pkg.build.build()
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        sizes = tuple(int(x) for x in args.batched_sizes.split(","))
+        print(json.dumps(run_batched(pkg, dev, None, args.steps, args.warmup, args.batched_pairs, sizes)), flush=True)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
