@@ -98,14 +98,32 @@ static cudaError_t launch_pair(const IaJob &job, cudaStream_t stream, int num_sm
             ready[dev] = true;
         }
     }
-    if (job.num_peaks != 0) return cudaErrorInvalidValue;  // FindMaximumFromCenter only
     const cplx *tw = nullptr;
     if ((e = ensure_twiddles(dev, &tw)) != cudaSuccess) return e;
     IaJob j = job;
     j.twiddles = tw + twiddle_offset(256);
-    long grid = (long)(num_sms & ~1) * (job.waves > 0 ? job.waves : 4);
+    // multi-peak mode: one resident wave (the fit queue fills between flushes), as K1
+    long grid = (long)(num_sms & ~1) * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? 1 : 4));
     if (grid > 2 * job.count) grid = 2 * job.count;
     if (grid < 2) return cudaSuccess;
+    if (job.num_peaks > 0) {
+        // one (2N-1)^2 plane per cluster, kept per device and grown on demand
+        static float *planes[kMaxDevices] = {nullptr};
+        static long capacity[kMaxDevices] = {0};
+        std::lock_guard<std::mutex> lock(mu);
+        const long need = grid / 2 * (long)PairShape::D * PairShape::D;
+        if (capacity[dev] < need) {
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            if ((e = cudaStreamIsCapturing(stream, &cs)) != cudaSuccess) return e;
+            if (cs != cudaStreamCaptureStatusNone) return cudaErrorStreamCaptureUnsupported;
+            if (planes[dev] != nullptr && (e = cudaFree(planes[dev])) != cudaSuccess) return e;
+            planes[dev] = nullptr;
+            capacity[dev] = 0;
+            if ((e = cudaMalloc(&planes[dev], sizeof(float) * need)) != cudaSuccess) return e;
+            capacity[dev] = need;
+        }
+        j.mp_planes = planes[dev];
+    }
     const size_t smem = PairShape::SMEM + (j.subpix_pixels > 0 ? sizeof(float) * 32 * 2 * j.subpix_pixels : 0);
     xcorr_pair_kernel<Pix, PP><<<(unsigned)grid, PairShape::T, smem, stream>>>(j);
     return cudaGetLastError();
@@ -150,7 +168,10 @@ bool multipeak_supported(int n, int num_peaks, int peak_kernel) {
         case 16: return multipeak_fits_n<16>(peak_kernel);
         case 32: return multipeak_fits_n<32>(peak_kernel);
         case 64: return multipeak_fits_n<64>(peak_kernel);
-        default: return false;  // IA 128 (the cluster kernel): FindMaximumFromCenter only
+        // IA 128: the records are staged in rank 0's 64 column-pair regions
+        case 128: return mp_stage_bytes(mp_geom(PairShape::D, peak_kernel)) <=
+                         sizeof(cplx) * (size_t)PairShape::NR * PairShape::RP;
+        default: return false;
     }
 }
 

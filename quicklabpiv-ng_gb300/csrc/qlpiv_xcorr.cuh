@@ -124,6 +124,7 @@ struct IaJob {
     uint8_t *npeaks;             // optional [count] peaks found
     const cplx *twiddles;        // exp(-2 pi i e / M), e < M (device table, filled once per device)
     int waves;                   // grid = SMs x resident CTAs x waves; 0: the default per mode
+    float *mp_planes;            // IA 128 multi-peak mode: one (2N-1)^2 plane per cluster (set by the launcher)
 };
 
 // Integer peak and 3-point stencil of one IA, queued for the sub-pixel fit.
@@ -491,10 +492,8 @@ __device__ int mp_replay(const MpGeom &gm, const float *recv, const int *recp, c
 // from 0, first in row-major order within the cell; position -1 = no positive value (the
 // reference then reuses the quadrant's previous position).  Also the maximum of every
 // 32 consecutive records.  KW = cell width, 0 = gm.kw at run time.  All threads.
-template <int N, int KW>
-__device__ __forceinline__ void mp_cells(const MpGeom &gm, const float *regf, float *recv, int *recp, float *chmax) {
-    using S = XcorrShape<N>;
-    constexpr int D = S::D, RP = S::RP, T = S::T;
+template <int D, int T, int KW, typename Plane>
+__device__ __forceinline__ void mp_cells(const MpGeom &gm, const Plane &P, float *recv, int *recp, float *chmax) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int kw = KW > 0 ? KW : gm.kw;
     for (int base = warp * 32; base < gm.nrec; base += T) {
@@ -514,7 +513,7 @@ __device__ __forceinline__ void mp_cells(const MpGeom &gm, const float *regf, fl
                     for (int b = 0; b < (KW > 0 ? KW : 1); b++) {
                         const int j = j0 + b;
                         if (i < D && j < D) {
-                            const float v = regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)];
+                            const float v = P(i, j);
                             if (v > bv) { bv = v; bp = (i << 16) | j; }
                         }
                     }
@@ -526,7 +525,7 @@ __device__ __forceinline__ void mp_cells(const MpGeom &gm, const float *regf, fl
                     for (int b = 0; b < kw; b++) {
                         const int j = j0 + b;
                         if (j >= D) break;
-                        const float v = regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)];
+                        const float v = P(i, j);
                         if (v > bv) { bv = v; bp = (i << 16) | j; }
                     }
                 }
@@ -541,9 +540,6 @@ __device__ __forceinline__ void mp_cells(const MpGeom &gm, const float *regf, fl
     }
 }
 
-// Step 5' of xcorr_kernel for one IA (kept out of line so that the single-peak path
-// keeps its register allocation): FindMaximumMultiPeaks over the plane in `regf`,
-// queueing `multi` fit records at fitq[qn..).  Called by every thread of the CTA.
 // Sub-pixel stencil of record r (peak r.pi, r.pj already set): the kind, and the stencil values
 // (3-point: in the record; P-point: 2P floats at fv, column then row, floor-lifted).
 template <int D, typename Plane>
@@ -581,15 +577,16 @@ __device__ __forceinline__ void fit_stencil(FitRec &r, const IaJob &job, const P
     }
 }
 
-template <int N>
-__device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float minf, const float *regf, cplx *scr,
-                                              uint64_t *red, FitRec *fitq, float *fitv, int qn, float *mp_lv,
-                                              int *mp_li, int *mp_lj) {
-    using S = XcorrShape<N>;
-    constexpr int D = S::D, RP = S::RP, T = S::T, NWARPS = T / 32;
+// FindMaximumMultiPeaks over a D x D plane read through P(i, j), by a CTA of T threads: the
+// records are staged at `stage` (mp_stage_bytes), the list replayed by warp 0, one fit record
+// queued per slot.
+template <int D, int T, typename Plane>
+__device__ __forceinline__ void multipeak_core(const IaJob &job, long ia, float minf, const Plane &P, void *stage,
+                                               uint64_t *red, FitRec *fitq, float *fitv, int qn, float *mp_lv,
+                                               int *mp_li, int *mp_lj) {
+    constexpr int NWARPS = T / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int multi = job.num_peaks;
-    auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)]; };
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
     __syncthreads();  // plane complete; the FFT scratch is free for the records
@@ -597,15 +594,15 @@ __device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float m
     if (lane == 0) redf[warp] = minf;
     const MpGeom gm = mp_geom(D, job.peak_kernel);
     const int kw = gm.kw;
-    float *recv = reinterpret_cast<float *>(scr);
+    float *recv = reinterpret_cast<float *>(stage);
     int *recp = reinterpret_cast<int *>(recv + gm.nrec);
     float *chmax = reinterpret_cast<float *>(recp + gm.nrec);
     // cell maxima: strict > from 0, first in row-major order; -1 = no positive
     // value (the reference then reuses the quadrant's previous position)
     if (kw == 3) {
-        mp_cells<N, 3>(gm, regf, recv, recp, chmax);
+        mp_cells<D, T, 3>(gm, P, recv, recp, chmax);
     } else {
-        mp_cells<N, 0>(gm, regf, recv, recp, chmax);
+        mp_cells<D, T, 0>(gm, P, recv, recp, chmax);
     }
     __syncthreads();
     if (warp == 0) {
@@ -643,6 +640,19 @@ __device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float m
             fitq[qn + lane] = r;
         }
     }
+}
+
+// Step 5' of xcorr_kernel for one IA (kept out of line so that the single-peak path keeps its
+// register allocation): the plane is in the column-pair regions, the records go to the FFT
+// scratch, `multi` fit records are queued at fitq[qn..).  Called by every thread of the CTA.
+template <int N>
+__device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float minf, const float *regf, cplx *scr,
+                                              uint64_t *red, FitRec *fitq, float *fitv, int qn, float *mp_lv,
+                                              int *mp_li, int *mp_lj) {
+    using S = XcorrShape<N>;
+    constexpr int RP = S::RP;
+    auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)]; };
+    multipeak_core<S::D, S::T>(job, ia, minf, P, scr, red, fitq, fitv, qn, mp_lv, mp_li, mp_lj);
 }
 
 // PP: the P-point sub-pixel interpolators are compiled in (their out-of-line double-precision

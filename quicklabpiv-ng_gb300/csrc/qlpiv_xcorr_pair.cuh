@@ -23,7 +23,8 @@
 //
 // Reference semantics are K1's (qlpiv_xcorr.cuh): normalisation, Hermitian split and product,
 // FindMaximumFromCenter order and the sub-pixel interpolators.  FindMaximumMultiPeaks needs the
-// whole plane and is not offered for IA 128 (the host rejects num_peaks > 0).
+// whole plane: in that mode the combine writes the plane to a per-cluster scratch in global memory
+// (L2-resident, 254 KB) and rank 0 runs K1's multi-peak search over it (pair_multipeak).
 #pragma once
 #include <cooperative_groups.h>
 
@@ -40,7 +41,7 @@ struct PairShape {
     static constexpr int G2 = 32, NG2 = T / G2;  // 256-point column transforms: a warp each
     static constexpr int RP1 = 128 + 16 + 1;     // scratch pitch of a 128-point transform
     static constexpr size_t SMEM = sizeof(cplx) * (size_t)(M + M / 2 + NR * RP + NG1 * RP1) +
-                                   64 * sizeof(uint64_t) + 32 * sizeof(FitRec);
+                                   64 * sizeof(uint64_t) + 32 * sizeof(FitRec) + 256 /* multi-peak list */;
 };
 
 __device__ __forceinline__ uint32_t cluster_addr(const void *p, unsigned rank) {
@@ -75,6 +76,36 @@ __device__ __forceinline__ int pair_slot(int p, int np) {
     return (np >> 1) * PairShape::RP + pad8(2 * p + (np & 1));
 }
 
+// Multi-peak mode of step 5 (out of line: the single-peak path keeps its registers).  Both CTAs
+// have written their row pairs of the plane to the cluster's global scratch `mp`; rank 1 hands its
+// min floor to rank 0, and rank 0 runs FindMaximumMultiPeaks over the plane (L2 reads), staging the
+// cell records in its regions (the partials are no longer needed) and queueing one fit per peak.
+// Called by every thread of both CTAs.
+static __device__ __noinline__ void pair_multipeak(const IaJob &job, long ia, float minf, const float *mp, cplx *reg,
+                                                   uint64_t *red, FitRec *fitq, float *fitv, int qn, float *mp_lv,
+                                                   int *mp_li, int *mp_lj, int q, uint32_t xch0) {
+    constexpr int D = PairShape::D, T = PairShape::T, NWARPS = T / 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
+    float *redf = reinterpret_cast<float *>(red);
+    __syncthreads();
+    if (lane == 0) redf[warp] = minf;
+    __syncthreads();
+    if (q == 1 && tid == 0) {
+        float m = redf[0];
+        for (int k = 1; k < NWARPS; k++) m = fminf(m, redf[k]);
+        cluster_st_u64(xch0 + 16u, (uint64_t)__float_as_uint(m));
+    }
+    __threadfence();  // the plane rows written to global memory, before the barrier
+    cooperative_groups::this_cluster().sync();
+    if (q == 0) {
+        if (tid == 0) minf = fminf(minf, __uint_as_float((uint32_t)red[50]));
+        auto P = [&](int i, int j) -> float { return __ldcg(mp + i * D + j); };
+        multipeak_core<D, T>(job, ia, minf, P, reg, red, fitq, fitv, qn, mp_lv, mp_li, mp_lj);
+    }
+}
+
 template <typename Pix, bool PP>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xcorr_pair_kernel(IaJob job) {
     using S = PairShape;
@@ -88,7 +119,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
     cplx *scr = reg + S::NR * RP;                    // 32 scratch buffers of the 128-point transforms
     uint64_t *red = reinterpret_cast<uint64_t *>(scr + NG1 * RP1);  // 64 words
     FitRec *fitq = reinterpret_cast<FitRec *>(red + 64);           // 32 queued fits
-    float *fitv = reinterpret_cast<float *>(fitq + 32);            // P-point stencils
+    float *mp_lv = reinterpret_cast<float *>(fitq + 32);           // multi-peak list (ascending)
+    int *mp_li = reinterpret_cast<int *>(mp_lv + QLPIV_MAX_PEAKS + 1);
+    int *mp_lj = mp_li + QLPIV_MAX_PEAKS + 1;
+    float *fitv = reinterpret_cast<float *>(mp_lj + QLPIV_MAX_PEAKS + 1);  // P-point stencils
     cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
     const int q = (int)cl.block_rank();
     const uint32_t peer_reg = cluster_addr(reg, (unsigned)(q ^ 1));
@@ -98,6 +132,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
     const int g1 = tid % G1, grp1 = tid / G1;
     const int g2 = lane, grp2 = warp;
     int qn = 0;
+    const int multi = job.num_peaks;  // 0: FindMaximumFromCenter; k: FindMaximumMultiPeaks
+    const int KQ = multi > 0 ? multi : 1;
 
     for (int e = tid; e < M; e += T) tw[e] = job.twiddles[e];
     for (int e = tid; e < M / 2; e += T) tw1[e] = job.twiddles[2 * e];
@@ -280,6 +316,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
         cl.sync();  // both parities' partials are complete
 
         // ---- 5. combine row pairs [64q, 64q + 64) and score the peak ----
+        // (multi-peak mode: write the plane to this cluster's global scratch instead)
+        float *mp = multi > 0 ? job.mp_planes + (long)(blockIdx.x / 2) * (D * D) : nullptr;
         uint64_t best = 0ull;
         uint32_t best_ij = 0u;
         float minf = 3.402823466e38f;
@@ -298,7 +336,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
                 for (int h = 0; h < 2; h++) {
                     const int n2 = np + h * (M / 2);
                     const cplx yv = h ? yhi : ylo;
-                    if (n2 >= 1 && n2 <= M - 2) {
+                    if (multi > 0) {
+                        // FindMaximumMultiPeaks visits every cell of the (2N-1)^2 plane
+                        if (n2 <= M - 2) {
+                            minf = fminf(minf, yv.x);
+                            if (rb_ <= M - 2) minf = fminf(minf, yv.y);
+                        }
+                        if (n2 < D) {
+                            mp[ra_ * D + n2] = yv.x;
+                            if (rb_ < D) mp[rb_ * D + n2] = yv.y;
+                        }
+                    } else if (n2 >= 1 && n2 <= M - 2) {
                         if (ra_ >= 1) {
                             minf = fminf(minf, yv.x);
                             const uint64_t kk = peak_key(yv.x, ra_, n2, N);
@@ -318,74 +366,78 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
                 }
             }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const uint64_t ok = __shfl_xor_sync(0xffffffffu, best, o);
-            const uint32_t oij = __shfl_xor_sync(0xffffffffu, best_ij, o);
-            if (ok > best) { best = ok; best_ij = oij; }
-            minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
-        }
-        __syncthreads();  // red[] reuse after the max reduction
-        if (lane == 0) {
-            red[warp] = best;
-            red[32 + warp] = ((uint64_t)best_ij << 32) | (uint64_t)__float_as_uint(minf);
-        }
-        __syncthreads();
-        uint64_t bk = 0ull;
-        uint32_t bij = 0u;
-        float mn = 3.402823466e38f;
-        if (warp == 0) {
-            if (lane < NWARPS) {
-                bk = red[lane];
-                bij = (uint32_t)(red[32 + lane] >> 32);
-                mn = __uint_as_float((uint32_t)red[32 + lane]);
-            }
-#pragma unroll
+        if (multi > 0) {
+            pair_multipeak(job, ia, minf, mp, reg, red, fitq, fitv, qn, mp_lv, mp_li, mp_lj, q, xch0);
+        } else {
+    #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                const uint64_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
-                const uint32_t oij = __shfl_xor_sync(0xffffffffu, bij, o);
+                const uint64_t ok = __shfl_xor_sync(0xffffffffu, best, o);
+                const uint32_t oij = __shfl_xor_sync(0xffffffffu, best_ij, o);
+                if (ok > best) { best = ok; best_ij = oij; }
+                minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
+            }
+            __syncthreads();  // red[] reuse after the max reduction
+            if (lane == 0) {
+                red[warp] = best;
+                red[32 + warp] = ((uint64_t)best_ij << 32) | (uint64_t)__float_as_uint(minf);
+            }
+            __syncthreads();
+            uint64_t bk = 0ull;
+            uint32_t bij = 0u;
+            float mn = 3.402823466e38f;
+            if (warp == 0) {
+                if (lane < NWARPS) {
+                    bk = red[lane];
+                    bij = (uint32_t)(red[32 + lane] >> 32);
+                    mn = __uint_as_float((uint32_t)red[32 + lane]);
+                }
+    #pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const uint64_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
+                    const uint32_t oij = __shfl_xor_sync(0xffffffffu, bij, o);
+                    if (ok > bk) { bk = ok; bij = oij; }
+                    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+                }
+            }
+            if (q == 1 && tid == 0) {
+                cluster_st_u64(xch0, bk);
+                cluster_st_u64(xch0 + 8u, ((uint64_t)bij << 32) | (uint64_t)__float_as_uint(mn));
+            }
+            cl.sync();  // rank 1's candidate has arrived
+            if (q == 0 && tid == 0) {
+                const uint64_t ok = red[48];
+                const uint32_t oij = (uint32_t)(red[49] >> 32);
                 if (ok > bk) { bk = ok; bij = oij; }
-                mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+                mn = fminf(mn, __uint_as_float((uint32_t)red[49]));
+                // plane value (i, j) recomputed from the partials: E here, O in rank 1
+                auto P = [&](int i, int j) -> float {
+                    const int np = j & (M / 2 - 1);
+                    const int off = pair_slot(i >> 1, np);
+                    const cplx w = {tw[np].x, -tw[np].y};
+                    cplx ylo, yhi;
+                    pair_combine(reg[off], cluster_ld(peer_reg + 8u * (uint32_t)off), w, ylo, yhi);
+                    const cplx yv = (j >> 7) ? yhi : ylo;
+                    return (i & 1) ? yv.y : yv.x;
+                };
+                FitRec rec;
+                rec.ia = ia;
+                rec.mn = mn;
+                rec.pi = 0;
+                rec.pj = 0;
+                rec.pv = 0.0f;
+                if (bk != 0ull) {
+                    rec.pi = (int)(bij >> 16);
+                    rec.pj = (int)(bij & 0xffffu);
+                    rec.pv = __uint_as_float((uint32_t)(bk >> 32));
+                }
+                rec.slot = 0;
+                rec.npk = 1;
+                fit_stencil<D>(rec, job, P, fitv + qn * 2 * job.subpix_pixels);
+                fitq[qn] = rec;
             }
         }
-        if (q == 1 && tid == 0) {
-            cluster_st_u64(xch0, bk);
-            cluster_st_u64(xch0 + 8u, ((uint64_t)bij << 32) | (uint64_t)__float_as_uint(mn));
-        }
-        cl.sync();  // rank 1's candidate has arrived
-        if (q == 0 && tid == 0) {
-            const uint64_t ok = red[48];
-            const uint32_t oij = (uint32_t)(red[49] >> 32);
-            if (ok > bk) { bk = ok; bij = oij; }
-            mn = fminf(mn, __uint_as_float((uint32_t)red[49]));
-            // plane value (i, j) recomputed from the partials: E here, O in rank 1
-            auto P = [&](int i, int j) -> float {
-                const int np = j & (M / 2 - 1);
-                const int off = pair_slot(i >> 1, np);
-                const cplx w = {tw[np].x, -tw[np].y};
-                cplx ylo, yhi;
-                pair_combine(reg[off], cluster_ld(peer_reg + 8u * (uint32_t)off), w, ylo, yhi);
-                const cplx yv = (j >> 7) ? yhi : ylo;
-                return (i & 1) ? yv.y : yv.x;
-            };
-            FitRec rec;
-            rec.ia = ia;
-            rec.mn = mn;
-            rec.pi = 0;
-            rec.pj = 0;
-            rec.pv = 0.0f;
-            if (bk != 0ull) {
-                rec.pi = (int)(bij >> 16);
-                rec.pj = (int)(bij & 0xffffu);
-                rec.pv = __uint_as_float((uint32_t)(bk >> 32));
-            }
-            rec.slot = 0;
-            rec.npk = 1;
-            fit_stencil<D>(rec, job, P, fitv + qn * 2 * job.subpix_pixels);
-            fitq[qn] = rec;
-        }
-        qn += 1;
-        if (qn + 1 > 32) {
+        qn += KQ;
+        if (qn + KQ > 32) {
             if (warp == 0 && q == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
             qn = 0;
         }

@@ -59,7 +59,9 @@ def _tiles(qp, n, count, bits=8, seed=0, sparse=False):
                                                 (32, 2, 4, 1, False), (64, 5, 1, 0, False), (16, 7, 16, 1, False),
                                                 (32, 3, 3, 3, True), (16, 2, 5, 3, True), (16, 3, 4, 1, False),
                                                 (32, 3, 3, 1, False), (64, 2, 4, 0, False), (64, 3, 8, 1, False),
-                                                (32, 4, 2, 0, False), (16, 3, 3, 3, True)])
+                                                (32, 4, 2, 0, False), (16, 3, 3, 3, True),
+                                                (128, 3, 3, 0, False), (128, 2, 4, 1, False),
+                                                (128, 3, 2, 3, True)])
 def test_multipeaks_match_oracle_on_kernel_planes(qp, handle, oracle, n, kw, k, norm, sparse):
     ta, tb = _tiles(qp, n, 160, seed=n + kw + k, sparse=sparse)
     planes = handle.xcorr_planes(ta, tb, norm_mode=norm)
@@ -178,6 +180,24 @@ def test_adaptive_pipeline_with_validation(qp, handle, oracle):
         assert np.mean(err32 <= 1e-3) >= 0.97
     u2, v2 = handle.piv_adaptive([p[0] for p in pairs], [p[1] for p in pairs], desc)
     assert u2.tobytes() == u.tobytes() and v2.tobytes() == v.tobytes()
+
+
+def test_adaptive_validation_from_ia128(qp, handle, oracle):
+    """Validation at an IA-128 level: the cluster kernel's multi-peak search over its plane in
+    global scratch, against the FP64 and FP32 oracle."""
+    h, w = 512, 448
+    pairs = [_outlier_pair(qp, h, w, 21 + k) for k in range(2)]
+    vd = qp.multipeak_validation(num_peaks=3, peak_kernel=3, threshold=2.0, epsilon0=0.1, max_iterations=2)
+    desc = qp.adaptive_desc(128, 32, 0.5, fixed_max=255.0, validation=vd)
+    u, v = handle.piv_adaptive([p[0] for p in pairs], [p[1] for p in pairs], desc)
+    cfg = oracle.valid_cfg(num_peaks=3, kernel_width=3, threshold=2.0, epsilon0=0.1, max_iterations=2)
+    for k, (a, b, flow) in enumerate(pairs):
+        for prec in (64, 32):
+            ou, ov = oracle.piv_adaptive(a, b, 128, 32, 0.5, fixed_max=255.0, precision=prec, validation=cfg)
+            err = np.maximum(np.abs(u[k] - ou), np.abs(v[k] - ov))
+            assert np.mean(err <= 1e-3) >= 0.97, (k, prec, float(np.mean(err <= 1e-3)))
+    pu, pv = qp.per_call.piv_adaptive_per_call(handle, pairs[0][0], pairs[0][1], desc)
+    assert pu.tobytes() == u[0].tobytes() and pv.tobytes() == v[0].tobytes()
 
 
 def test_adaptive_validation_settings_rejected(qp, handle):

@@ -167,9 +167,9 @@ def test_empty_and_errors(qp, handle):
     with pytest.raises(qp.QlpivError) as ei:
         handle.xcorr_planes(np.zeros((2, 256, 256), np.uint8), np.zeros((2, 256, 256), np.uint8))
     assert ei.value.status == qp.E_SHAPE
-    with pytest.raises(qp.QlpivError) as ei:   # the two-CTA IA 128 kernel runs FindMaximumFromCenter only
+    with pytest.raises(qp.QlpivError) as ei:   # IA 128 multi-peak: cell width 1 is invalid
         handle.piv_pass(np.zeros((256, 256), np.uint8), np.zeros((256, 256), np.uint8), 128, [0], [0], num_peaks=2,
-                        peak_kernel=3)
+                        peak_kernel=1)
     assert ei.value.status == qp.E_ARG
     with pytest.raises(ValueError):
         handle.piv_pass(a, a.astype(np.uint16), 32, [0], [0])
