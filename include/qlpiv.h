@@ -632,6 +632,10 @@ qlpiv_status qlpiv_profile_read(qlpiv_handle *h, qlpiv_stage_time *out, int cap,
  * (TFLOP/s, best of three), the compute roofline denominator of the FFT kernels. */
 qlpiv_status qlpiv_measure_fp32_peak(int device, double *tflops);
 
+/* Instrumentation: the sub-pixel fit's float-pair logarithm beside CUDA's double log for n
+ * positive normal floats (host arrays), to check its error bound on the device. */
+qlpiv_status qlpiv_probe_log(int device, const float *x, long n, double *mine, double *ref);
+
 /* Number of kernel launches issued by this handle since creation (instrumentation). */
 long qlpiv_launch_count(qlpiv_handle *h);
 

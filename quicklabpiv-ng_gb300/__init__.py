@@ -244,6 +244,7 @@ _SIGNATURES = {
     "qlpiv_tiff_info": (_i, [ctypes.c_char_p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "qlpiv_tiff_read": (_i, [ctypes.c_char_p, _vp, ctypes.c_int64]),
     "qlpiv_mat_export": (_i, [ctypes.c_char_p, ctypes.POINTER(MatExportParams), _i, ctypes.POINTER(MatVelocityMap)]),
+    "qlpiv_probe_log": (_i, [_i, _vp, _l, _vp, _vp]),
     "qlpiv_profile_enable": (_i, [_vp, _i]),
     "qlpiv_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(_i)]),
 }
@@ -315,6 +316,15 @@ def inherit_noalloc(device, stream, p_ci, p_cj, pu, pv, c_ci, c_cj, cu, cv, pni,
     a = [x if isinstance(x, int) else _addr(x) for x in (p_ci, p_cj, pu, pv, c_ci, c_cj, cu, cv)]
     _check(load_library().qlpiv_inherit_noalloc(device, stream or None, pni, pnj, a[0], a[1], a[2], a[3], cni, cnj,
                                                 a[4], a[5], int(round_int), a[6], a[7]))
+
+
+def probe_log(x, device=0):
+    """(fit logarithm, CUDA double log) of positive floats x, evaluated on the device."""
+    x = np.ascontiguousarray(x, np.float32)
+    mine = np.empty(x.size, np.float64)
+    ref = np.empty(x.size, np.float64)
+    _check(load_library().qlpiv_probe_log(device, _addr(x), x.size, _addr(mine), _addr(ref)))
+    return mine, ref
 
 
 def measure_fp32_peak(device=0):

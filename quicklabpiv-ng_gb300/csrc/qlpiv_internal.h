@@ -13,6 +13,8 @@ constexpr int kMaxDevices = 64;
 
 // Uploads the FFT twiddle tables to device `dev` (the current device) once.
 cudaError_t ensure_twiddles(int dev, const cplx **table);
+// log_fpair table of `dev` (valid after ensure_twiddles on that device).
+const float4 *log_table(int dev);
 
 // K1 fused FFT-PIV over job.count IAs of side n on `stream`.
 cudaError_t launch_xcorr(const IaJob &job, int n, int pixel_type, cudaStream_t stream, int num_sms);

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include "qlpiv.h"
+#include "qlpiv_internal.h"
+#include "qlpiv_logdf.cuh"
 
 namespace {
 
@@ -59,5 +61,46 @@ extern "C" qlpiv_status qlpiv_measure_fp32_peak(int device, double *tflops) {
     if (e1) cudaEventDestroy(e1);
     if (out) cudaFree(out);
     cudaSetDevice(prev);
+    return st;
+}
+
+// Instrumentation: the fit's float-pair logarithm (qlpiv_logdf.cuh) beside CUDA's double log for
+// n host floats, so that its error bound can be checked on the device.
+namespace {
+__global__ void log_probe(const float *x, long n, const float4 *tab, double *mine, double *ref) {
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const qlpiv::fpair p = qlpiv::log_fpair(x[k], tab);
+    mine[k] = (double)p.hi + (double)p.lo;
+    ref[k] = log((double)x[k]);
+}
+}  // namespace
+
+extern "C" qlpiv_status qlpiv_probe_log(int device, const float *x, long n, double *mine, double *ref) {
+    if (!x || !mine || !ref || n < 0) return QLPIV_E_ARG;
+    for (long k = 0; k < n; k++)
+        if (!(x[k] >= 1.17549435e-38f && x[k] < 3.4e38f)) return QLPIV_E_ARG;  // positive normal floats
+    if (n == 0) return QLPIV_OK;
+    if (cudaSetDevice(device) != cudaSuccess) return QLPIV_E_NO_DEVICE;
+    const qlpiv::cplx *tw = nullptr;
+    if (qlpiv::ensure_twiddles(device, &tw) != cudaSuccess) return QLPIV_E_CUDA;
+    float *dx = nullptr;
+    double *dm = nullptr, *dr = nullptr;
+    qlpiv_status st = QLPIV_OK;
+    if (cudaMalloc(&dx, sizeof(float) * n) != cudaSuccess || cudaMalloc(&dm, sizeof(double) * n) != cudaSuccess ||
+        cudaMalloc(&dr, sizeof(double) * n) != cudaSuccess) {
+        st = QLPIV_E_OOM;
+    } else if (cudaMemcpy(dx, x, sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+        st = QLPIV_E_CUDA;
+    } else {
+        log_probe<<<(unsigned)((n + 255) / 256), 256>>>(dx, n, qlpiv::log_table(device), dm, dr);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(mine, dm, sizeof(double) * n, cudaMemcpyDeviceToHost) !=
+                                                     cudaSuccess ||
+            cudaMemcpy(ref, dr, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = QLPIV_E_CUDA;
+    }
+    cudaFree(dx);
+    cudaFree(dm);
+    cudaFree(dr);
     return st;
 }

@@ -15,6 +15,13 @@ static __device__ cplx g_twiddles[32 + 64 + 128 + 256];
 
 static int twiddle_offset(int m) { return m == 32 ? 0 : (m == 64 ? 32 : (m == 128 ? 96 : 224)); }
 
+// log_fpair table (qlpiv_logdf.cuh): {inv_k, -ln(inv_k) hi, -ln(inv_k) lo, 0}, inv_k = 1/(1 + k/64)
+// rounded to float, k = 0..64; the logarithm of the float inv_k is taken in double.
+static __device__ float4 g_logtab[65];
+static const float4 *g_logtab_addr[kMaxDevices] = {nullptr};
+
+const float4 *log_table(int dev) { return dev >= 0 && dev < kMaxDevices ? g_logtab_addr[dev] : nullptr; }
+
 cudaError_t ensure_twiddles(int dev, const cplx **table) {
     static std::mutex mu;
     static const cplx *addr[kMaxDevices] = {nullptr};
@@ -29,6 +36,17 @@ cudaError_t ensure_twiddles(int dev, const cplx **table) {
             }
         cudaError_t err = cudaMemcpyToSymbol(g_twiddles, host, sizeof(host));
         if (err != cudaSuccess) return err;
+        float4 lt[65];
+        for (int k = 0; k <= 64; k++) {
+            const float inv = (float)(1.0 / (1.0 + k / 64.0));
+            const double v = -std::log((double)inv);
+            const float hi = (float)v;
+            lt[k] = make_float4(inv, hi, (float)(v - (double)hi), 0.0f);
+        }
+        if ((err = cudaMemcpyToSymbol(g_logtab, lt, sizeof(lt))) != cudaSuccess) return err;
+        void *lp = nullptr;
+        if ((err = cudaGetSymbolAddress(&lp, g_logtab)) != cudaSuccess) return err;
+        g_logtab_addr[dev] = static_cast<const float4 *>(lp);
         void *p = nullptr;
         err = cudaGetSymbolAddress(&p, g_twiddles);
         if (err != cudaSuccess) return err;
@@ -69,6 +87,7 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
     if ((e = ensure_twiddles(dev, &tw)) != cudaSuccess) return e;
     IaJob j = job;
     j.twiddles = tw + twiddle_offset(S::M);
+    j.log_tab = log_table(dev);
     // every CTA loops over IAs; eight waves of CTAs balance the single-peak kernel best,
     // one resident wave the multi-peak one (its fit queue then fills between flushes)
     long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? 1 : 8));
@@ -102,6 +121,7 @@ static cudaError_t launch_pair(const IaJob &job, cudaStream_t stream, int num_sm
     if ((e = ensure_twiddles(dev, &tw)) != cudaSuccess) return e;
     IaJob j = job;
     j.twiddles = tw + twiddle_offset(256);
+    j.log_tab = log_table(dev);
     // multi-peak mode: one resident wave (the fit queue fills between flushes), as K1
     long grid = (long)(num_sms & ~1) * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? 1 : 4));
     if (grid > 2 * job.count) grid = 2 * job.count;

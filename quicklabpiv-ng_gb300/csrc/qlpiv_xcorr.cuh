@@ -35,6 +35,7 @@
 //      fit per peak.
 #pragma once
 #include "qlpiv_fft.cuh"
+#include "qlpiv_logdf.cuh"
 #include "qlpiv.h"
 #include "qlpiv_subpix.cuh"
 
@@ -125,6 +126,7 @@ struct IaJob {
     const cplx *twiddles;        // exp(-2 pi i e / M), e < M (device table, filled once per device)
     int waves;                   // grid = SMs x resident CTAs x waves; 0: the default per mode
     float *mp_planes;            // IA 128 multi-peak mode: one (2N-1)^2 plane per cluster (set by the launcher)
+    const float4 *log_tab;       // log_fpair table (device, filled once per device with the twiddles)
 };
 
 // Integer peak and 3-point stencil of one IA, queued for the sub-pixel fit.
@@ -200,12 +202,16 @@ __device__ void fit_flush(const FitRec *q, const float *fitv, int n, int lane, c
             const float x0 = r.xl + 1e-8f, x1 = r.c0 + 1e-8f, x2 = r.xr + 1e-8f;
             float ti, tj;
             if (!neg) {
-                const double ly0 = log((double)y0), ly1 = log((double)y1), ly2 = log((double)y2);
-                const double lx0 = log((double)x0), lx1 = log((double)x1), lx2 = log((double)x2);
-                const double di = __dadd_rn(__dadd_rn(__dmul_rn(2.0, ly0), -__dmul_rn(4.0, ly1)), __dmul_rn(2.0, ly2));
-                const double dj = __dadd_rn(__dadd_rn(__dmul_rn(2.0, lx0), -__dmul_rn(4.0, lx1)), __dmul_rn(2.0, lx2));
-                ti = __fadd_rn((float)r.pi, __fdiv_rn((float)(ly0 - ly2), (float)di));
-                tj = __fadd_rn((float)r.pj, __fdiv_rn((float)(lx0 - lx2), (float)dj));
+                // the reference's double logarithms, carried as float pairs (error < 1e-11)
+                const fpair ly0 = log_fpair(y0, job.log_tab), ly1 = log_fpair(y1, job.log_tab),
+                            ly2 = log_fpair(y2, job.log_tab);
+                const fpair lx0 = log_fpair(x0, job.log_tab), lx1 = log_fpair(x1, job.log_tab),
+                            lx2 = log_fpair(x2, job.log_tab);
+                const fpair di = fp_add(fp_add(fp_scale2(ly0, 2.0f), fp_scale2(ly1, -4.0f)), fp_scale2(ly2, 2.0f));
+                const fpair dj = fp_add(fp_add(fp_scale2(lx0, 2.0f), fp_scale2(lx1, -4.0f)), fp_scale2(lx2, 2.0f));
+                const fpair ni = fp_add(ly0, fp_scale2(ly2, -1.0f)), nj = fp_add(lx0, fp_scale2(lx2, -1.0f));
+                ti = __fadd_rn((float)r.pi, __fdiv_rn(fp_round(ni), fp_round(di)));
+                tj = __fadd_rn((float)r.pj, __fdiv_rn(fp_round(nj), fp_round(dj)));
             } else {
                 flags |= QLPIV_F_PARABOLIC;
                 const float dy = __fadd_rn(__fadd_rn(__fmul_rn(2.0f, y0), -__fmul_rn(4.0f, y1)), __fmul_rn(2.0f, y2));

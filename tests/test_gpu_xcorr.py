@@ -279,3 +279,17 @@ def test_batched_frames_equal_single_passes(qp, handle):
     handle.piv_pass_batch_device(qp.PIX_U8, len(pairs), ttab, 32, len(at), wl[0], wl[1], wl[2], wl[1], wl[2], out)
     handle.synchronize()
     assert out.cpu().numpy().tobytes() == batch.tobytes()
+
+
+def test_fit_logarithm_error_bound(qp):
+    """The 3-point fit's float-pair logarithm stays within 1e-11 of CUDA's double log over the
+    range of fit samples (plane values + 1e-8) and around every table and binade boundary."""
+    rng = np.random.default_rng(17)
+    x = np.exp(rng.uniform(np.log(1e-8), np.log(1e7), 200000)).astype(np.float32)
+    k = np.arange(65, dtype=np.float64)
+    edges = np.concatenate([(1.0 + (k + 0.5) / 64.0) * s for s in (1.0, 2.0 ** -20, 2.0 ** 10)])
+    x = np.concatenate([x, edges.astype(np.float32), np.nextafter(edges.astype(np.float32), np.float32(0)),
+                        np.float32([1e-8, 1.0, 2.0, 0.5, 16.0, 17.0, 255.0, 4095.0, 65535.0])])
+    mine, ref = qp.probe_log(x)
+    err = np.abs(mine - ref)
+    assert err.max() < 1e-11, (float(err.max()), float(x[err.argmax()]))
