@@ -176,7 +176,7 @@ static __device__ __noinline__ void fit_ppoint(int mode, int P, int iters, int p
 }
 
 // Gaussian1DPolynomialInterpolator.interpolate (S/interpolators/Gaussian1DPolynomialInterpolator.java:25-106)
-// for q[0..n): lane k handles record k, so the double logarithms of 32 IAs share one
+// for q[0..n): lane k handles record k, so the logarithms of 32 IAs share one
 // warp instruction.  Called by one full warp.
 template <int D, bool PP>
 __device__ void fit_flush(const FitRec *q, const float *fitv, int n, int lane, const IaJob &job) {
