@@ -107,7 +107,7 @@ typedef struct qlpiv_vector {
 
 /* One correlation pass: IA side and tile/peak semantics. */
 typedef struct qlpiv_pass_desc {
-    int n;              /* IA side: 16, 32, 64 or 128 (128: num_peaks 0 only) */
+    int n;              /* IA side: 16, 32, 64 or 128 (128: a two-CTA cluster per IA) */
     int norm_mode;      /* qlpiv_norm */
     int max_mode;       /* qlpiv_max_mode */
     float fixed_max_a;  /* QLPIV_MAX_FIXED: max of every A tile */
