@@ -36,7 +36,7 @@ struct PairShape {
     static constexpr int N = 128, M = 256, D = 255;
     static constexpr int NR = 64;                // regions per CTA
     static constexpr int RP = M + M / 8 + 1;     // region pitch (complex), odd
-    static constexpr int T = 512;
+    static constexpr int T = 768;                // 24 warps: 32 groups do not divide the phases
     static constexpr int G1 = 16, NG1 = T / G1;  // 128-point transforms: 16 lanes, 32 groups
     static constexpr int G2 = 32, NG2 = T / G2;  // 256-point column transforms: a warp each
     static constexpr int RP1 = 128 + 16 + 1;     // scratch pitch of a 128-point transform
@@ -100,7 +100,7 @@ static __device__ __noinline__ void pair_multipeak(const IaJob &job, long ia, fl
     __threadfence();  // the plane rows written to global memory, before the barrier
     cooperative_groups::this_cluster().sync();
     if (q == 0) {
-        if (tid == 0) minf = fminf(minf, __uint_as_float((uint32_t)red[50]));
+        if (tid == 0) minf = fminf(minf, __uint_as_float((uint32_t)red[62]));
         auto P = [&](int i, int j) -> float { return __ldcg(mp + i * D + j); };
         multipeak_core<D, T>(job, ia, minf, P, reg, red, fitq, fitv, qn, mp_lv, mp_li, mp_lj);
     }
@@ -126,7 +126,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
     cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
     const int q = (int)cl.block_rank();
     const uint32_t peer_reg = cluster_addr(reg, (unsigned)(q ^ 1));
-    const uint32_t xch0 = cluster_addr(red + 48, 0u);  // rank 0's exchange words
+    const uint32_t xch0 = cluster_addr(red + 60, 0u);  // rank 0's exchange words red[60..62]
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g1 = tid % G1, grp1 = tid / G1;
@@ -203,8 +203,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
 
         // ---- 2. row pass: frequencies of parity q of every row ----
 #pragma unroll 1
-        for (int r = 0; r < N / NG1; r++) {
+        for (int r = 0; r < (N + NG1 - 1) / NG1; r++) {
             const int n1 = grp1 + NG1 * r;
+            if (n1 >= N) break;  // whole warps (N - NG1 * r is even)
             cplx v[8];
 #pragma unroll
             for (int m = 0; m < 8; m++) {
@@ -234,8 +235,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
 
         // ---- 3. column tasks on this CTA's regions (as in K1) ----
 #pragma unroll 1
-        for (int r = 0; r < S::NR / NG2; r++) {
+        for (int r = 0; r < (S::NR + NG2 - 1) / NG2; r++) {
             const int lc = grp2 + NG2 * r;
+            if (lc >= S::NR) break;  // one warp per region
             const int c = 2 * lc + q;
             cplx *rg = reg + lc * RP;
             cplx z1[8], z2[8];
@@ -288,8 +290,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
 
         // ---- 4. partial inverse row-pair transforms (frequencies of parity q), in place ----
 #pragma unroll 1
-        for (int r = 0; r < (M / 2) / NG1; r++) {
+        for (int r = 0; r < (M / 2 + NG1 - 1) / NG1; r++) {
             const int pr = grp1 + NG1 * r;
+            if (pr >= M / 2) break;
             const int ra_ = 2 * pr, rb_ = 2 * pr + 1;
             cplx y[8];
 #pragma unroll
@@ -325,8 +328,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
             const int np = tid & (M / 2 - 1);
             const cplx w = {tw[np].x, -tw[np].y};  // w256^-n'
 #pragma unroll 4
-            for (int k = 0; k < (M / 4) / (T / (M / 2)); k++) {
-                const int pr = (M / 4) * q + (tid >> 7) + (T / (M / 2)) * k;
+            for (int k = 0; k < (M / 4 + T / (M / 2) - 1) / (T / (M / 2)); k++) {
+                const int pl = (tid >> 7) + (T / (M / 2)) * k;  // this CTA's row pair index
+                if (pl >= M / 4) break;
+                const int pr = (M / 4) * q + pl;
                 const int off = pair_slot(pr, np);
                 const cplx own = reg[off], other = cluster_ld(peer_reg + 8u * (uint32_t)off);
                 cplx ylo, yhi;
@@ -405,10 +410,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
             }
             cl.sync();  // rank 1's candidate has arrived
             if (q == 0 && tid == 0) {
-                const uint64_t ok = red[48];
-                const uint32_t oij = (uint32_t)(red[49] >> 32);
+                const uint64_t ok = red[60];
+                const uint32_t oij = (uint32_t)(red[61] >> 32);
                 if (ok > bk) { bk = ok; bij = oij; }
-                mn = fminf(mn, __uint_as_float((uint32_t)red[49]));
+                mn = fminf(mn, __uint_as_float((uint32_t)red[61]));
                 // plane value (i, j) recomputed from the partials: E here, O in rank 1
                 auto P = [&](int i, int j) -> float {
                     const int np = j & (M / 2 - 1);
