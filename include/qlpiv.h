@@ -587,7 +587,11 @@ qlpiv_status qlpiv_tiff_read(const char *path, void *pixels, int64_t capacity_by
  *                                   :132-181): iaHeight, iaWidth, adaptiveStep, margins, u = row and
  *                                   v = column displacement.
  * Invalid vectors are written as NaN when mark_invalid_as_nan is set. */
-typedef enum { QLPIV_MAT_RUN = 0, QLPIV_MAT_STEP = 1 } qlpiv_mat_layout;
+/* QLPIV_MAT_DENSE (exportDenseDataToFile, :240-290, the optical-flow dense export): one struct
+ * `velocities` with the same fields as QLPIV_MAT_RUN; the map's tiles_i x tiles_j is the whole
+ * frame (the dense field of qlpiv_flow_after_piv) and u, v are written for the pixels inside the
+ * margins, (H - top - bottom) x (W - left - right) x frames, in PIVMap's U/V order. */
+typedef enum { QLPIV_MAT_RUN = 0, QLPIV_MAT_STEP = 1, QLPIV_MAT_DENSE = 2 } qlpiv_mat_layout;
 
 typedef struct qlpiv_mat_export_params {
     int image_width, image_height;

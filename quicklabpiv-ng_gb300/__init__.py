@@ -774,7 +774,7 @@ def read_tiff(path):
     return out
 
 
-MAT_RUN, MAT_STEP = 0, 1
+MAT_RUN, MAT_STEP, MAT_DENSE = 0, 1, 2
 
 
 def export_mat(path, maps, image_height, image_width, ia_start, ia_end, overlap_factor, swap_uv=False,
@@ -823,6 +823,16 @@ def export_adaptive_mat(path, desc, height, width, u, v, invalid=None, **kw):
     m = dict(u=u, v=v, ia=(g["n"], g["n"]), adaptive_step=len(levels) - 1, invalid=invalid,
              margins=(g["margin_top"], g["margin_left"], g["margin_bottom"], g["margin_right"]))
     export_mat(path, [m], height, width, desc.ia_start, desc.ia_end, desc.overlap_factor, **kw)
+
+
+def export_dense_mat(path, desc, height, width, dense_u, dense_v, **kw):
+    """Export a dense flow field (pairs x height x width, rows / columns as qlpiv_flow_after_piv
+    returns it) in the reference's dense layout: one `velocities` struct over the pixels inside
+    the last level's margins."""
+    g = adaptive_levels(desc, height, width)[-1]
+    m = dict(u=dense_u, v=dense_v, ia=(g["n"], g["n"]),
+             margins=(g["margin_top"], g["margin_left"], g["margin_bottom"], g["margin_right"]))
+    export_mat(path, [m], height, width, desc.ia_start, desc.ia_end, desc.overlap_factor, layout=MAT_DENSE, **kw)
 
 
 class MixedPlan:

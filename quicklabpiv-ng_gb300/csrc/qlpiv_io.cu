@@ -332,7 +332,15 @@ qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *p
                               const qlpiv_mat_velocity_map *maps) {
     if (!path || !p || (num_maps > 0 && !maps)) return fail(QLPIV_E_ARG, "NULL argument");
     if (num_maps < 0 || p->frames <= 0) return fail(QLPIV_E_ARG, "num_maps < 0 or frames <= 0");
-    if (p->layout != QLPIV_MAT_RUN && p->layout != QLPIV_MAT_STEP) return fail(QLPIV_E_ARG, "layout %d", p->layout);
+    if (p->layout != QLPIV_MAT_RUN && p->layout != QLPIV_MAT_STEP && p->layout != QLPIV_MAT_DENSE)
+        return fail(QLPIV_E_ARG, "layout %d", p->layout);
+    if (p->layout == QLPIV_MAT_DENSE && num_maps != 1) return fail(QLPIV_E_ARG, "the dense layout holds one map");
+    for (int m = 0; m < num_maps && p->layout == QLPIV_MAT_DENSE; m++) {
+        const int *g = maps[m].margins;
+        if (g[0] < 0 || g[1] < 0 || g[2] < 0 || g[3] < 0 || g[0] + g[2] >= maps[m].tiles_i ||
+            g[1] + g[3] >= maps[m].tiles_j)
+            return fail(QLPIV_E_ARG, "dense map: margins leave no pixels");
+    }
     for (int m = 0; m < num_maps; m++)
         if (!maps[m].u || !maps[m].v || maps[m].tiles_i <= 0 || maps[m].tiles_j <= 0)
             return fail(QLPIV_E_ARG, "velocity map %d: NULL data or empty grid", m);
@@ -380,7 +388,11 @@ qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *p
     for (int m = 0; m < num_maps; m++) {
         const qlpiv_mat_velocity_map &mp = maps[m];
         Buf v;
-        const bool run = p->layout == QLPIV_MAT_RUN;
+        const bool run = p->layout != QLPIV_MAT_STEP, dense = p->layout == QLPIV_MAT_DENSE;
+        // dense maps (exportDenseDataToFile, :240-290) cover the image inside the margins
+        const int r0 = dense ? mp.margins[0] : 0, c0 = dense ? mp.margins[1] : 0;
+        const int rows_out = dense ? mp.tiles_i - mp.margins[0] - mp.margins[2] : mp.tiles_i;
+        const int cols_out = dense ? mp.tiles_j - mp.margins[1] - mp.margins[3] : mp.tiles_j;
         int32_scalar(v, "", mp.ia_height);
         int32_scalar(v, "", mp.ia_width);
         int32_scalar(v, "", run ? 0 : mp.adaptive_step);  // multiVolumeExport: one volume
@@ -398,20 +410,21 @@ qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *p
             const bool rows = run ? (comp == 0) == (p->swap_uv != 0) : comp == 0;
             const float *src = rows ? mp.u : mp.v;
             // MATLAB order: i fastest, then j, then the frame
-            std::vector<float> col(per * p->frames);
+            std::vector<float> col((size_t)rows_out * cols_out * p->frames);
             size_t k = 0;
             for (int f = 0; f < p->frames; f++)
-                for (int j = 0; j < mp.tiles_j; j++)
-                    for (int i = 0; i < mp.tiles_i; i++) {
-                        const size_t s = f * per + (size_t)i * mp.tiles_j + j;
-                        const bool bad = p->mark_invalid_as_nan && mp.invalid && mp.invalid[s];
+                for (int j = 0; j < cols_out; j++)
+                    for (int i = 0; i < rows_out; i++) {
+                        const size_t s = f * per + (size_t)(i + r0) * mp.tiles_j + (j + c0);
+                        const bool bad = !dense && p->mark_invalid_as_nan && mp.invalid && mp.invalid[s];
                         col[k++] = bad ? std::numeric_limits<float>::quiet_NaN() : src[s];
                     }
             Buf body;
             body.element(miSINGLE, col.data(), sizeof(float) * col.size());
-            matrix(v, mxSINGLE, {mp.tiles_i, mp.tiles_j, p->frames}, "", body);
+            matrix(v, mxSINGLE, {rows_out, cols_out, p->frames}, "", body);
         }
-        const std::string name = "velocities" + std::to_string(mp.ia_height) + "x" + std::to_string(mp.ia_width);
+        const std::string name = dense ? std::string("velocities")
+                                       : "velocities" + std::to_string(mp.ia_height) + "x" + std::to_string(mp.ia_width);
         structure(out, name, {"iaHeight", "iaWidth", run ? "multiVolumeExport" : "adaptiveStep", "margins", "u", "v"},
                   v);
     }

@@ -302,3 +302,28 @@ def test_mat_export_rejects(qp, tmp_path):
     with pytest.raises(qp.QlpivError) as e:
         qp.export_mat(tmp_path / "nodir" / "x.mat", [], 64, 64, 16, 16, 0.5)
     assert e.value.status == qp.E_ARG
+
+
+def test_mat_dense_export(qp, tmp_path):
+    """The optical-flow dense layout: one `velocities` struct, u / v over the pixels inside the
+    margins, column displacement first (PIVMap), no NaN marking."""
+    sio = pytest.importorskip("scipy.io")
+    desc = qp.adaptive_desc(64, 32, 0.5, margins=(3, 4, 5, 6))
+    h, w = 200, 230
+    rng = np.random.default_rng(4)
+    du = rng.normal(0, 1, (2, h, w)).astype(np.float32)
+    dv = rng.normal(0, 1, (2, h, w)).astype(np.float32)
+    p = tmp_path / "d.mat"
+    qp.export_dense_mat(p, desc, h, w, du, dv)
+    m = sio.loadmat(p)
+    assert "velocities" in m and not any(k.startswith("velocities3") for k in m)
+    s = m["velocities"][0, 0]
+    assert s.dtype.names == ("iaHeight", "iaWidth", "multiVolumeExport", "margins", "u", "v")
+    g = qp.adaptive_levels(desc, h, w)[-1]
+    t, l, b, r = g["margin_top"], g["margin_left"], g["margin_bottom"], g["margin_right"]
+    assert s["u"].shape == (h - t - b, w - l - r, 2)
+    np.testing.assert_array_equal(s["u"][:, :, 1], dv[1, t:h - b, l:w - r])
+    np.testing.assert_array_equal(s["v"][:, :, 0], du[0, t:h - b, l:w - r])
+    with pytest.raises(qp.QlpivError):
+        qp.export_mat(tmp_path / "x.mat", [dict(u=du, v=dv, ia=(32, 32), margins=(0, 0, 0, 0))] * 2, h, w, 64, 32,
+                      0.5, layout=qp.MAT_DENSE)
