@@ -465,6 +465,21 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def job_time_ms(ms_local, world, device=None):
+    """Whole-job time of a replicated run: the slowest rank's time (MAX over the process group)."""
+    if world <= 1:
+        return float(ms_local)
+    import torch
+    t = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world, ms):
+    """Units processed by all ranks per second (weak scaling: every rank runs the same work)."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def run_gpu(args, rank, world):
     import torch
     pkg = load_pkg()
@@ -516,13 +531,9 @@ def run_gpu(args, rank, world):
         t_end.record(stream)
         torch.cuda.synchronize()
     launches = h.launches - launches0
-    ms = t_start.elapsed_time(t_end)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = job_time_ms(t_start.elapsed_time(t_end), world, dev)
     ms_per_step = ms / args.steps
-    pairs_per_s = world * P * args.steps / (ms * 1e-3)
+    pairs_per_s = job_throughput(P * args.steps, world, ms)
 
     # ---- per-stage device time (events around every launch), two extra steps ----
     h.profile(True)
