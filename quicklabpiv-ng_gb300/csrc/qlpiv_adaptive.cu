@@ -405,46 +405,78 @@ __host__ __device__ __forceinline__ Pix warp_store(float value, int int16_quirk)
 // Canonical field evaluation order shared with the oracle's float path: column basis
 // X = (h00, h01, dx*h10, dx*h11)(tx), row basis Y likewise; the four column sums w
 // first, then ((w0*Y0 + w1*Y1) + w2*Y2) + w3*Y3.
-__host__ __device__ __forceinline__ float field_value(const float *ys, int ni, const float *xs, int nj,
-                                                      const float4 *c4, float y, float x) {
-    const int i = knot_interval(ys, ni, y), j = knot_interval(xs, nj, x);
-    const float dy = ys[i + 1] - ys[i], dx = xs[j + 1] - xs[j];
-    const float ty = (y - ys[i]) / dy, tx = (x - xs[j]) / dx;
-    float ay0[2], ay1[2], ax0[2], ax1[2];
-    hermite_basis(ty, ay0, ay1);
-    hermite_basis(tx, ax0, ax1);
-    const float X0 = ax0[0], X1 = ax0[1], X2 = dx * ax1[0], X3 = dx * ax1[1];
-    const float Y0 = ay0[0], Y1 = ay0[1], Y2 = dy * ay1[0], Y3 = dy * ay1[1];
+// Knot interval k of coordinate c and its Hermite basis (h00, h01, d*h10, d*h11)(t).
+__host__ __device__ __forceinline__ int field_basis(const float *v, int n, float c, float B[4]) {
+    const int k = knot_interval(v, n, c);
+    const float d = v[k + 1] - v[k];
+    const float t = (c - v[k]) / d;
+    float a0[2], a1[2];
+    hermite_basis(t, a0, a1);
+    B[0] = a0[0];
+    B[1] = a0[1];
+    B[2] = d * a1[0];
+    B[3] = d * a1[1];
+    return k;
+}
+
+// Patch (i, j) of the node quadruples evaluated with row basis Y and column basis X.
+__host__ __device__ __forceinline__ float field_combine(const float4 *c4, int nj, int i, int j, const float X[4],
+                                                        const float Y[4]) {
     float w[4];
 #pragma unroll
     for (int a = 0; a < 2; a++) {
         const long k0 = (long)(i + a) * nj + j;
         const float4 n0 = c4[k0], n1 = c4[k0 + 1];
-        w[a] = n0.x * X0 + n1.x * X1 + n0.z * X2 + n1.z * X3;
-        w[2 + a] = n0.y * X0 + n1.y * X1 + n0.w * X2 + n1.w * X3;
+        w[a] = n0.x * X[0] + n1.x * X[1] + n0.z * X[2] + n1.z * X[3];
+        w[2 + a] = n0.y * X[0] + n1.y * X[1] + n0.w * X[2] + n1.w * X[3];
     }
-    return w[0] * Y0 + w[1] * Y1 + w[2] * Y2 + w[3] * Y3;
+    return w[0] * Y[0] + w[1] * Y[1] + w[2] * Y[2] + w[3] * Y[3];
 }
 
-// Pixel (i, j) of pair `pair`: field, then the warped pixels.  image_mode 3 (BothImages) warps
-// both frames by half the field, 1 (FirstImage) frame A and 2 (SecondImage) frame B by the whole
-// field (BiLinearImageWarpingStrategy.doBiLinearWarp, :162-181); the other frame is copied as is.
+__host__ __device__ __forceinline__ float field_value(const float *ys, int ni, const float *xs, int nj,
+                                                      const float4 *c4, float y, float x) {
+    float X[4], Y[4];
+    const int i = field_basis(ys, ni, y, Y), j = field_basis(xs, nj, x, X);
+    return field_combine(c4, nj, i, j, X, Y);
+}
+
+// One thread per pixel of one pair (blockIdx.z = pair), 32 x 8 pixels per block; src/dst frame
+// tables hold the original and the warped images.  The knot search and Hermite basis of the
+// block's 32 columns and 8 rows are computed once in shared memory (the same operations
+// field_value performs per pixel, so the field is bit-identical).
 template <typename Pix>
-__host__ __device__ __forceinline__ void warp_one(int pair, int i, int j, const qlpiv_frame *src,
-                                                  const qlpiv_frame *dst, const float *ys, int ni, const float *xs,
-                                                  int nj, const float4 *c4u, const float4 *c4v, int int16_quirk,
-                                                  int image_mode) {
+__global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, const qlpiv_frame *dst,
+                                                        const float *ys, int ni, const float *xs, int nj,
+                                                        const float4 *c4u, const float4 *c4v, int int16_quirk,
+                                                        int image_mode) {
+    __shared__ float sx[32][4], sy[8][4];
+    __shared__ int sj[32], si[8];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int j = blockIdx.x * 32 + tx, i = blockIdx.y * 8 + ty;
+    const int pair = blockIdx.z;
+    if (ty == 0) {
+        float x = (float)j;
+        if (x < xs[0]) x = xs[0]; else if (x > xs[nj - 1]) x = xs[nj - 1];
+        sj[tx] = field_basis(xs, nj, x, sx[tx]);
+    } else if (ty == 1 && tx < 8) {
+        float y = (float)(blockIdx.y * 8 + tx);
+        if (y < ys[0]) y = ys[0]; else if (y > ys[ni - 1]) y = ys[ni - 1];
+        si[tx] = field_basis(ys, ni, y, sy[tx]);
+    }
+    __syncthreads();
     const qlpiv_frame fs = src[pair];
     const int h = fs.height, w = fs.width;
     if (i >= h || j >= w) return;
     const qlpiv_frame fd = dst[pair];
     const long base = (long)pair * ni * nj;
-    const float ymin = ys[0], ymax = ys[ni - 1], xmin = xs[0], xmax = xs[nj - 1];
-    float y = (float)i, x = (float)j;
-    if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
-    if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
-    const float fu = field_value(ys, ni, xs, nj, c4u + base, y, x);
-    const float fv = field_value(ys, ni, xs, nj, c4v + base, y, x);
+    float X[4], Y[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        X[k] = sx[tx][k];
+        Y[k] = sy[ty][k];
+    }
+    const float fu = field_combine(c4u + base, nj, si[ty], sj[tx], X, Y);
+    const float fv = field_combine(c4v + base, nj, si[ty], sj[tx], X, Y);
     const bool both = image_mode == 3;
     const float hu = both ? fu / 2.0f : fu, hv = both ? fv / 2.0f : fv;
     const Pix *ia = reinterpret_cast<const Pix *>(fs.img_a);
@@ -457,18 +489,6 @@ __host__ __device__ __forceinline__ void warp_one(int pair, int i, int j, const 
     ob[(long)i * fd.pitch + j] = image_mode & 2
         ? warp_store<Pix>(warp_pixel(ib, h, w, fs.pitch, hu, hv, i, j, false), int16_quirk)
         : ib[(long)i * fs.pitch + j];
-}
-
-// One thread per pixel of one pair (blockIdx.z = pair).  src/dst frame tables hold the
-// original and the warped images.
-template <typename Pix>
-__global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, const qlpiv_frame *dst,
-                                                        const float *ys, int ni, const float *xs, int nj,
-                                                        const float4 *c4u, const float4 *c4v, int int16_quirk,
-                                                        int image_mode) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    warp_one<Pix>(blockIdx.z, i, j, src, dst, ys, ni, xs, nj, c4u, c4v, int16_quirk, image_mode);
 }
 
 // ---------------- micro / mini per-tile warping ----------------
