@@ -656,18 +656,34 @@ __global__ void __launch_bounds__(256) tile_warp_kernel(const qlpiv_frame *frame
 }
 
 // Per-pixel field only (test hook for the field stage): pair 0, outputs h x w floats.
-__global__ void field_kernel(int h, int w, const float *ys, int ni, const float *xs, int nj, const float4 *c4u,
-                             const float4 *c4v, float off_y, float off_x, float *fu_out, float *fv_out) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= h || j >= w) return;
-    const float ymin = ys[0], ymax = ys[ni - 1], xmin = xs[0], xmax = xs[nj - 1];
+// 32 x 8 pixels per block, the column and row bases shared as in warp_both_kernel.
+__global__ void __launch_bounds__(256) field_kernel(int h, int w, const float *ys, int ni, const float *xs, int nj,
+                                                    const float4 *c4u, const float4 *c4v, float off_y, float off_x,
+                                                    float *fu_out, float *fv_out) {
+    __shared__ float sx[32][4], sy[8][4];
+    __shared__ int sj[32], si[8];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int j = blockIdx.x * 32 + tx, i = blockIdx.y * 8 + ty;
     // pixel i is evaluated at off_y + i (the reference steps a float from the offset by 1.0f)
-    float y = off_y + (float)i, x = off_x + (float)j;
-    if (y < ymin) y = ymin; else if (y > ymax) y = ymax;
-    if (x < xmin) x = xmin; else if (x > xmax) x = xmax;
-    fu_out[(long)i * w + j] = field_value(ys, ni, xs, nj, c4u, y, x);
-    fv_out[(long)i * w + j] = field_value(ys, ni, xs, nj, c4v, y, x);
+    if (ty == 0) {
+        float x = off_x + (float)j;
+        if (x < xs[0]) x = xs[0]; else if (x > xs[nj - 1]) x = xs[nj - 1];
+        sj[tx] = field_basis(xs, nj, x, sx[tx]);
+    } else if (ty == 1 && tx < 8) {
+        float y = off_y + (float)(blockIdx.y * 8 + tx);
+        if (y < ys[0]) y = ys[0]; else if (y > ys[ni - 1]) y = ys[ni - 1];
+        si[tx] = field_basis(ys, ni, y, sy[tx]);
+    }
+    __syncthreads();
+    if (i >= h || j >= w) return;
+    float X[4], Y[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        X[k] = sx[tx][k];
+        Y[k] = sy[ty][k];
+    }
+    fu_out[(long)i * w + j] = field_combine(c4u, nj, si[ty], sj[tx], X, Y);
+    fv_out[(long)i * w + j] = field_combine(c4v, nj, si[ty], sj[tx], X, Y);
 }
 
 // B tile origins for non-warping modes: round(top + u), round(left + v)
