@@ -482,8 +482,8 @@ qlpiv_status qlpiv_piv_flow_device(qlpiv_handle *h, const qlpiv_adaptive_desc *p
  * correlated as one flattened work list per IA size (the pair's level-0 SuperPosition grid),
  * launched from one captured CUDA graph whose branches run the sizes concurrently.  `frames`
  * is a host table of device images; the plan keeps a device copy and the output.  With
- * autotune the grid of each size's launch is chosen by timing 1, 2, 4 and 8 waves of resident
- * CTAs on its work list.  Output vectors are size-major and pair-contiguous: pair q's
+ * autotune the grid of each size's launch is chosen by timing 1, 2, 4, 8, 16 and 32 waves of
+ * resident CTAs on its work list.  Output vectors are size-major and pair-contiguous: pair q's
  * tiles_i x tiles_j tiles (row-major) start at pair_offset[q]. */
 typedef struct qlpiv_mixed_plan qlpiv_mixed_plan;
 qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmpl, int pixel_type, int num_pairs,

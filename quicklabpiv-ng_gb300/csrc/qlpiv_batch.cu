@@ -7,8 +7,9 @@
 // (AdaptiveInterAreaStrategySuperPosition, as qlpiv_grid_superposition) is appended to the work
 // list of its IA size; the plan launches K1 once per size, each launch on its own branch of the
 // graph so the sizes run concurrently, and the graph is replayed per batch.  The autotuner times
-// each size's launch over its real work list with 1, 2, 4 and 8 waves of resident CTAs and keeps
-// the fastest.  Vectors come out size-major (16, 32, 64, 128) and pair-contiguous inside a size.
+// each size's launch over its real work list with 1, 2, 4, 8, 16 and 32 waves of resident CTAs
+// and keeps the fastest.  Vectors come out size-major (16, 32, 64, 128) and pair-contiguous
+// inside a size.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -198,10 +199,10 @@ qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmp
     cudaEventCreate(&t1);
     for (Group &g : p->groups) {
         if (g.count == 0) continue;
-        const int cands[4] = {1, 2, 4, 8};
+        const int cands[6] = {1, 2, 4, 8, 16, 32};
         float best = 1e30f;
         int best_w = 8;
-        for (int c = 0; c < (autotune ? 4 : 1); c++) {
+        for (int c = 0; c < (autotune ? 6 : 1); c++) {
             g.waves = autotune ? cands[c] : 0;
             IaJob job = group_job(p, g);
             if ((e = launch_xcorr(job, g.n, pixel_type, s, h->num_sms)) != cudaSuccess) break;  // warm-up

@@ -56,6 +56,10 @@ cudaError_t ensure_twiddles(int dev, const cplx **table) {
     return cudaSuccess;
 }
 
+// Default waves of resident CTAs per launch in multi-peak mode.  Measured on the headline adaptive
+// workload (three multi-peak passes): 1 wave 558 frame-pairs/s, 4: 568, 16: 582, 32: 585, 64: 586.
+constexpr int kMultiWaves = 32;
+
 constexpr size_t kSubpixSmem = sizeof(float) * 32 * 2 * kMaxSubpixPixels;
 
 template <int N, typename Pix, bool PP>
@@ -88,9 +92,9 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
     IaJob j = job;
     j.twiddles = tw + twiddle_offset(S::M);
     j.log_tab = log_table(dev);
-    // every CTA loops over IAs; eight waves of CTAs balance the single-peak kernel best,
-    // one resident wave the multi-peak one (its fit queue then fills between flushes)
-    long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? 1 : 8));
+    // every CTA loops over IAs; eight waves of CTAs balance the single-peak kernel best, 32 the
+    // multi-peak one
+    long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? kMultiWaves : 8));
     if (grid > job.count) grid = job.count;
     if (grid < 1) return cudaSuccess;
     // P-point sub-pixel stencils: 2 P floats per queued fit after the fixed layout

@@ -63,7 +63,7 @@ def test_mixed_plan_equals_single_passes(qp, handle, bits, autotune):
     plan = qp.MixedPlan(handle, table, sizes, ofac, pt, autotune=autotune)
     assert plan.total == plan.pair_offset[-1]
     if autotune:
-        assert all(w in (0, 1, 2, 4, 8) for w in plan.waves)
+        assert all(w in (0, 1, 2, 4, 8, 16, 32) for w in plan.waves)
     assert 128 in sizes
     plan.run()
     vec = plan.vectors()
