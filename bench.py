@@ -161,18 +161,20 @@ WORKLOAD = ("adaptive-1024-u12: 1024x1024 12-bit pairs, IA 64 -> 32 -> 16 at 75 
 
 
 # Hybrid PIV + dense optical flow (1024x1024 u8, one 32x32 pass at 50 % overlap, then dense
-# Lucas-Kanade (prefilter sigma 2.0, 3 px; window 27; 5 iterations) and Liu-Shen (lambda 4,
-# prefilter sigma 0.48, 5 px; 60 passes), dense field exported).
+# Lucas-Kanade over a 2-level pyramid (prefilter sigma 2.0, 3 px; window 27; 5 iterations per
+# level) and Liu-Shen (lambda 4, prefilter sigma 0.48, 5 px; 60 passes), dense field exported).
 HYBRID_PAIRS = 8
 HYBRID_WORKLOAD = ("hybrid-1024-u8: 1024x1024 u8 vortex pairs (0.05 ppp, max 3 px), one 32x32 PIV pass at 50 % "
-                   "overlap, then dense Lucas-Kanade (sigma 2.0, window 27, 5 iterations) and Liu-Shen (lambda 4, "
+                   "overlap, then dense Lucas-Kanade over a 2-level pyramid (sigma 2.0, window 27, 5 iterations per "
+                   "level) and Liu-Shen (lambda 4, "
                    "sigma 0.48, 60 passes), FP32 dense field")
 
 
 def hybrid_descs(pkg):
     piv = pkg.adaptive_desc(32, 32, 0.5, warp_mode=pkg.WARP_NONE, norm_mode=pkg.NORM_MAX_A, max_mode=pkg.MAX_COMPUTE)
     flow = pkg.flow_desc(mode=pkg.FLOW_LIU_SHEN, filter_sigma_lk=2.0, filter_px_lk=3, window_lk=27, iterations_lk=5,
-                         filter_sigma_ls=0.48, filter_px_ls=5, lambda_ls=4.0, iterations_ls=60, dense_export=True)
+                         filter_sigma_ls=0.48, filter_px_ls=5, lambda_ls=4.0, iterations_ls=60, dense_export=True,
+                         pyramid_levels=2)
     return piv, flow
 
 

@@ -449,7 +449,12 @@ typedef struct qlpiv_flow_desc {
     int iterations_ls;
     int dense_export;       /* denseVectors: whole-pixel field and dense output */
     int ignore_piv;         /* qlpiv_ignore_piv: ignorePIVBaseDisplacements(Mode) */
-    int reserved[5];
+    int pyramid_levels;     /* Lucas-Kanade coarse to fine over 1..4 levels (0 or 1: full resolution
+                               only, as the reference): 2 x 2 box down-sampling of the prefiltered
+                               images and of the field (halved), each level's result up-sampled
+                               (nearest, doubled) as the next finer level's start.  This library's
+                               own design; the reference's dense LK has no pyramid */
+    int reserved[4];
 } qlpiv_flow_desc;
 
 /* The optical flow after PIV of one frame pair on the last adaptive step's grid (tiles of side

@@ -111,7 +111,9 @@ def lib():
         L.orc_dense_lk.argtypes = [fp, fp, c_int, c_int, fp, fp, c_int, c_int, c_int]
         L.orc_liu_shen.argtypes = [fp, fp, c_int, c_int, fp, fp, c_float, c_int, c_int, vp, vp, vp]
         L.orc_flow_after_piv.argtypes = [fp, fp, c_int, c_int, c_int, c_int, c_int, ip, ip, fp, fp, c_int, c_float,
-                                         c_int, c_float, c_int, c_int, c_int, c_float, c_int, c_int, c_int, vp, vp]
+                                         c_int, c_float, c_int, c_int, c_int, c_float, c_int, c_int, c_int, c_int,
+                                         vp, vp]
+        L.orc_dense_lk_pyramid.argtypes = [fp, fp, c_int, c_int, fp, fp, c_int, c_int, c_int, c_int]
         L.orc_vector_size.restype = c_int
         assert L.orc_vector_size() == VECTOR_DTYPE.itemsize
         _lib = L
@@ -543,6 +545,17 @@ def dense_lk(img_a, img_b, us, vs, window, iterations, half_pixel=False):
     return u, v
 
 
+def dense_lk_pyramid(img_a, img_b, us, vs, window, iterations, half_pixel=False, levels=2):
+    """Dense Lucas-Kanade coarse to fine over `levels` 2 x 2 box-averaged levels (this library's own
+    design): returns refined (us, vs) (columns, rows)."""
+    a, b = _f32(img_a), _f32(img_b)
+    u, v = _f32(us).copy(), _f32(vs).copy()
+    lib().orc_dense_lk_pyramid(_ptr(a, ctypes.c_float), _ptr(b, ctypes.c_float), a.shape[0], a.shape[1],
+                               _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), window, iterations, int(half_pixel),
+                               levels)
+    return u, v
+
+
 def liu_shen(ls_a, ls_b, us, vs, lam, iterations, half_pixel=False, intermediates=False):
     """Liu-Shen passes on (us, vs); with intermediates also the fixed terms (12 planes: w, IIx,
     IIy, II, Ixt, Iyt, A11, A12, A22, B11, B12, B22) and every pass's (unew, vnew)."""
@@ -563,7 +576,8 @@ def liu_shen(ls_a, ls_b, us, vs, lam, iterations, half_pixel=False, intermediate
 
 
 def flow_after_piv(img_a, img_b, n, tops, lefts, tu, tv, mode=2, sigma_lk=2.0, px_lk=3, sigma_ls=0.48, px_ls=5,
-                   window=27, iterations_lk=5, lam=4.0, iterations_ls=60, dense_export=True, ignore_piv=0):
+                   window=27, iterations_lk=5, lam=4.0, iterations_ls=60, dense_export=True, ignore_piv=0,
+                   pyramid_levels=0):
     """Optical flow after PIV on the last step's tile grid: returns updated tile (u, v)
     (rows, columns) and the dense field (rows, columns).  ignore_piv: 0 none, 1 IgnoreU,
     2 IgnoreV, 3 IgnoreUV, 4 Auto, 5 AutoSmall."""
@@ -578,6 +592,7 @@ def flow_after_piv(img_a, img_b, n, tops, lefts, tu, tv, mode=2, sigma_lk=2.0, p
     lib().orc_flow_after_piv(_ptr(a, ctypes.c_float), _ptr(b, ctypes.c_float), h, w, n, len(tops), len(lefts),
                              _ptr(tops, ctypes.c_int), _ptr(lefts, ctypes.c_int), _ptr(u, ctypes.c_float),
                              _ptr(v, ctypes.c_float), mode, sigma_lk, px_lk, sigma_ls, px_ls, window, iterations_lk,
-                             lam, iterations_ls, int(dense_export), int(ignore_piv), du.ctypes.data, dv.ctypes.data)
+                             lam, iterations_ls, int(dense_export), int(ignore_piv), int(pyramid_levels),
+                             du.ctypes.data, dv.ctypes.data)
     return u, v, du, dv
 

@@ -73,6 +73,8 @@ void orc_gauss_filter(const float *in, int h, int w, const float *k, int K, floa
 void orc_normalize(const float *in, long n, float *out);
 void orc_dense_lk(const float *A, const float *B, int h, int w, float *us, float *vs, int win, int iterations,
                   int half_pixel);
+void orc_dense_lk_pyramid(const float *A, const float *B, int h, int w, float *us, float *vs, int win, int iterations,
+                          int half_pixel, int levels);
 int orc_liu_shen(const float *la, const float *lb, int h, int w, float *us, float *vs, float lambda, int iterations,
                  int half_pixel, float *fixed_out, float *unews, float *vnews);
 

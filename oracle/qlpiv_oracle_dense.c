@@ -306,6 +306,68 @@ int orc_liu_shen(const float *la, const float *lb, int h, int w, float *us, floa
     return passes;
 }
 
+/* Lucas-Kanade pyramid (coarse to fine): this library's own design, not the reference's (its
+ * DenseLucasKanade runs at full resolution only).  A level halves both sides (floor) by 2 x 2 box
+ * averaging, ((a + b) + (c + d)) * 0.25 * scale, scale 0.5 for the displacement field; a coarser
+ * level's result starts the next finer level through nearest up-sampling, doubled, with the
+ * source index clamped to the coarser level. */
+static void pyr_down(const float *s, int h, int w, float *d, float scale) {
+    const int h2 = h / 2, w2 = w / 2;
+    for (int i = 0; i < h2; i++)
+        for (int j = 0; j < w2; j++) {
+            const float *r0 = s + (long)(2 * i) * w + 2 * j, *r1 = r0 + w;
+            const float t = (r0[0] + r0[1]) + (r1[0] + r1[1]);
+            d[(long)i * w2 + j] = (t * 0.25f) * scale;
+        }
+}
+
+static void pyr_up(const float *s, int hs, int ws, float *d, int h, int w) {
+    for (int i = 0; i < h; i++)
+        for (int j = 0; j < w; j++) {
+            const int si = (i >> 1) < hs - 1 ? (i >> 1) : hs - 1, sj = (j >> 1) < ws - 1 ? (j >> 1) : ws - 1;
+            d[(long)i * w + j] = 2.0f * s[(long)si * ws + sj];
+        }
+}
+
+void orc_dense_lk_pyramid(const float *A, const float *B, int h, int w, float *us, float *vs, int win, int iterations,
+                          int half_pixel, int levels) {
+    if (levels <= 1) {
+        orc_dense_lk(A, B, h, w, us, vs, win, iterations, half_pixel);
+        return;
+    }
+    const float *la[4] = {A}, *lb[4] = {B};
+    float *lu[4] = {us}, *lv[4] = {vs};
+    int lh[4] = {h}, lw[4] = {w};
+    for (int l = 1; l < levels; l++) {
+        lh[l] = lh[l - 1] / 2;
+        lw[l] = lw[l - 1] / 2;
+        const long n = (long)lh[l] * lw[l];
+        float *na = (float *)malloc(sizeof(float) * n), *nb = (float *)malloc(sizeof(float) * n);
+        float *nu = (float *)malloc(sizeof(float) * n), *nv = (float *)malloc(sizeof(float) * n);
+        pyr_down(la[l - 1], lh[l - 1], lw[l - 1], na, 1.0f);
+        pyr_down(lb[l - 1], lh[l - 1], lw[l - 1], nb, 1.0f);
+        pyr_down(lu[l - 1], lh[l - 1], lw[l - 1], nu, 0.5f);
+        pyr_down(lv[l - 1], lh[l - 1], lw[l - 1], nv, 0.5f);
+        la[l] = na;
+        lb[l] = nb;
+        lu[l] = nu;
+        lv[l] = nv;
+    }
+    for (int l = levels - 1; l >= 0; l--) {
+        if (l < levels - 1) {
+            pyr_up(lu[l + 1], lh[l + 1], lw[l + 1], lu[l], lh[l], lw[l]);
+            pyr_up(lv[l + 1], lh[l + 1], lw[l + 1], lv[l], lh[l], lw[l]);
+        }
+        orc_dense_lk(la[l], lb[l], lh[l], lw[l], lu[l], lv[l], win, iterations, half_pixel);
+    }
+    for (int l = 1; l < levels; l++) {
+        free((void *)la[l]);
+        free((void *)lb[l]);
+        free(lu[l]);
+        free(lv[l]);
+    }
+}
+
 /* IOpticalFlowInterpolator.interpolate(stepTilesA, stepTilesB) of the LucasKanade (mode 1) and
  * LiuShenWithLucasKanade (mode 2) interpolators
  * (S/interpolators/DenseLucasKanadeAparapiJobInterpolator.java:247-334,
@@ -319,7 +381,7 @@ int orc_liu_shen(const float *la, const float *lb, int h, int w, float *us, floa
 void orc_flow_after_piv(const float *img_a, const float *img_b, int h, int w, int n, int ni, int nj, const int *tops,
                         const int *lefts, float *tu, float *tv, int mode, float sigma_lk, int px_lk, float sigma_ls,
                         int px_ls, int window, int iters_lk, float lambda, int iters_ls, int dense_export,
-                        int ignore_piv, float *dense_u, float *dense_v) {
+                        int ignore_piv, int pyramid_levels, float *dense_u, float *dense_v) {
     const long np = (long)h * w;
     float *lka = (float *)malloc(sizeof(float) * np), *lkb = (float *)malloc(sizeof(float) * np);
     float *lsa = NULL, *lsb = NULL;
@@ -359,7 +421,7 @@ void orc_flow_after_piv(const float *img_a, const float *img_b, int h, int w, in
     /* the flow jobs take columns (us) and rows (vs) */
     float *us = fv, *vs = fu;
     const int half = dense_export ? 0 : 1;
-    orc_dense_lk(lka, lkb, h, w, us, vs, window, iters_lk, half);
+    orc_dense_lk_pyramid(lka, lkb, h, w, us, vs, window, iters_lk, half, pyramid_levels);
     if (mode == 2) orc_liu_shen(lsa, lsb, h, w, us, vs, lambda, iters_ls, half, NULL, NULL, NULL);
     for (int ti = 0; ti < ni; ti++)
         for (int tj = 0; tj < nj; tj++) {

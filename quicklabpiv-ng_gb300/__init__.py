@@ -129,19 +129,23 @@ class FlowDesc(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("filter_sigma_lk", ctypes.c_float), ("filter_px_lk", ctypes.c_int),
                 ("filter_sigma_ls", ctypes.c_float), ("filter_px_ls", ctypes.c_int), ("window_lk", ctypes.c_int),
                 ("iterations_lk", ctypes.c_int), ("lambda_ls", ctypes.c_float), ("iterations_ls", ctypes.c_int),
-                ("dense_export", ctypes.c_int), ("ignore_piv", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("dense_export", ctypes.c_int), ("ignore_piv", ctypes.c_int), ("pyramid_levels", ctypes.c_int),
+                ("reserved", ctypes.c_int * 4)]
 
 
 def flow_desc(mode=FLOW_LUCAS_KANADE, filter_sigma_lk=2.0, filter_px_lk=3, filter_sigma_ls=0.48, filter_px_ls=5,
-              window_lk=27, iterations_lk=5, lambda_ls=4.0, iterations_ls=60, dense_export=False, ignore_piv=0):
+              window_lk=27, iterations_lk=5, lambda_ls=4.0, iterations_ls=60, dense_export=False, ignore_piv=0,
+              pyramid_levels=0):
     """Optical flow after PIV (OpticalFlowAfterPIV Lucas-Kanade or Liu-Shen interpolator
-    options); dense_export selects whole-pixel evaluation and the dense field export."""
+    options); dense_export selects whole-pixel evaluation and the dense field export.
+    pyramid_levels > 1 runs the Lucas-Kanade stage coarse to fine over that many 2 x 2
+    box-averaged levels (an extension: the reference runs it at full resolution only)."""
     d = FlowDesc()
     d.mode, d.filter_sigma_lk, d.filter_px_lk = mode, filter_sigma_lk, filter_px_lk
     d.filter_sigma_ls, d.filter_px_ls, d.window_lk, d.iterations_lk = filter_sigma_ls, filter_px_ls, window_lk, \
         iterations_lk
     d.lambda_ls, d.iterations_ls, d.dense_export = lambda_ls, iterations_ls, int(dense_export)
-    d.ignore_piv = ignore_piv
+    d.ignore_piv, d.pyramid_levels = ignore_piv, pyramid_levels
     return d
 
 

@@ -778,8 +778,11 @@ __global__ void ignore_piv_kernel(float *fu, float *fv, long n, int mode, float 
 
 size_t spline_coef_bytes(long tiles) { return (size_t)tiles * (6 * sizeof(double) + 2 * sizeof(float4)); }
 
-const char *check_flow_desc(const qlpiv_flow_desc *d) {
+const char *check_flow_desc(const qlpiv_flow_desc *d, int h, int w) {
     if (!d) return "flow descriptor is NULL";
+    if (d->pyramid_levels < 0 || d->pyramid_levels > 4) return "Lucas-Kanade pyramid: 0..4 levels";
+    if (d->pyramid_levels > 1 && ((h >> (d->pyramid_levels - 1)) < 8 || (w >> (d->pyramid_levels - 1)) < 8))
+        return "Lucas-Kanade pyramid: the coarsest level must keep at least 8 x 8 pixels";
     if (d->mode != QLPIV_FLOW_LUCAS_KANADE && d->mode != QLPIV_FLOW_LIU_SHEN) return "unknown optical-flow mode";
     if (d->window_lk < 3 || d->window_lk > 31 || d->window_lk % 2 == 0)
         return "dense Lucas-Kanade: window size must be odd, 3..31";
@@ -879,6 +882,78 @@ static SplineCoef coef_view(void *base, long n) {
     return SplineCoef{c, c + n, c + 2 * n, c + 3 * n, c + 4 * n, c + 5 * n, q, q + n};
 }
 
+// ---------------- Lucas-Kanade pyramid (coarse to fine) ----------------
+// This library's own design (the reference's dense LK runs at full resolution only): 2 x 2 box
+// down-sampling, ((a + b) + (c + d)) * 0.25 * scale with rounded single operations (scale 0.5 for
+// the displacement field), and nearest up-sampling of a level's result, doubled.
+
+__global__ void pyr_down_kernel(const float *s, int h, int w, float *d, float scale) {
+    const int h2 = h / 2, w2 = w / 2;
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (long)h2 * w2) return;
+    const int i = (int)(k / w2), j = (int)(k - (long)i * w2);
+    const float *r0 = s + (long)(2 * i) * w + 2 * j, *r1 = r0 + w;
+    const float t = __fadd_rn(__fadd_rn(r0[0], r0[1]), __fadd_rn(r1[0], r1[1]));
+    d[k] = __fmul_rn(__fmul_rn(t, 0.25f), scale);
+}
+
+__global__ void pyr_up_kernel(const float *s, int hs, int ws, float *d, int h, int w) {
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (long)h * w) return;
+    const int i = (int)(k / w), j = (int)(k - (long)i * w);
+    const int si = min(i >> 1, hs - 1), sj = min(j >> 1, ws - 1);
+    d[k] = __fmul_rn(2.0f, s[(long)si * ws + sj]);
+}
+
+// Dense LK over `levels` pyramid levels on the prefiltered frames a, b (h x w) and the start field
+// us / vs (columns, rows), which receives the finest level's result.  pyr: scratch of at least
+// 4 x h x w / 3 floats plus alignment (FlowBufs::pyr).
+static cudaError_t lk_pyramid(cudaStream_t s, const float *a, const float *b, int h, int w, float *us, float *vs,
+                              int window, int iterations, int half, int levels, float *pyr, long *launches) {
+    if (levels <= 1) {
+        *launches += 1;
+        return launch_dense_lk(s, a, b, h, w, us, vs, window, iterations, half);
+    }
+    const float *la[4] = {a}, *lb[4] = {b};
+    float *lu[4] = {us}, *lv[4] = {vs};
+    int lh[4] = {h}, lw[4] = {w};
+    float *c = pyr;
+    cudaError_t e;
+    for (int l = 1; l < levels; l++) {
+        lh[l] = lh[l - 1] / 2;
+        lw[l] = lw[l - 1] / 2;
+        const long n = (long)lh[l] * lw[l], step = (n + 63) & ~63L;
+        float *na = c, *nb = c + step, *nu = c + 2 * step, *nv = c + 3 * step;
+        c += 4 * step;
+        const unsigned g = (unsigned)((n + 255) / 256);
+        pyr_down_kernel<<<g, 256, 0, s>>>(la[l - 1], lh[l - 1], lw[l - 1], na, 1.0f);
+        pyr_down_kernel<<<g, 256, 0, s>>>(lb[l - 1], lh[l - 1], lw[l - 1], nb, 1.0f);
+        pyr_down_kernel<<<g, 256, 0, s>>>(lu[l - 1], lh[l - 1], lw[l - 1], nu, 0.5f);
+        pyr_down_kernel<<<g, 256, 0, s>>>(lv[l - 1], lh[l - 1], lw[l - 1], nv, 0.5f);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        *launches += 4;
+        la[l] = na;
+        lb[l] = nb;
+        lu[l] = nu;
+        lv[l] = nv;
+    }
+    for (int l = levels - 1; l >= 0; l--) {
+        if (l < levels - 1) {  // start from the coarser level's result
+            const long n = (long)lh[l] * lw[l];
+            const unsigned g = (unsigned)((n + 255) / 256);
+            pyr_up_kernel<<<g, 256, 0, s>>>(lu[l + 1], lh[l + 1], lw[l + 1], lu[l], lh[l], lw[l]);
+            pyr_up_kernel<<<g, 256, 0, s>>>(lv[l + 1], lh[l + 1], lw[l + 1], lv[l], lh[l], lw[l]);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            *launches += 2;
+        }
+        if ((e = launch_dense_lk(s, la[l], lb[l], lh[l], lw[l], lu[l], lv[l], window, iterations, half)) !=
+            cudaSuccess)
+            return e;
+        *launches += 1;
+    }
+    return cudaSuccess;
+}
+
 // prefilter of a frame; sigma < 1e-5 keeps the frame (converted to float)
 static cudaError_t filter_or_copy(cudaStream_t s, int pixel_type, const void *img, long pitch, int h, int w, float sigma,
                                   const float *k, int K, float *tmp, float *out, long *launches) {
@@ -937,9 +1012,9 @@ cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, c
     float *us = b.fv, *vs = b.fu;  // the flow jobs take columns (us) and rows (vs)
     const int half = d.dense_export ? 0 : 1;
     mark("flow:lucas_kanade", true);
-    if ((e = launch_dense_lk(s, b.lka, b.lkb, h, w, us, vs, d.window_lk, d.iterations_lk, half)) != cudaSuccess)
+    if ((e = lk_pyramid(s, b.lka, b.lkb, h, w, us, vs, d.window_lk, d.iterations_lk, half, d.pyramid_levels, b.pyr,
+                        launches)) != cudaSuccess)
         return e;
-    *launches += 1;
     mark("flow:lucas_kanade", false);
     if (d.mode == QLPIV_FLOW_LIU_SHEN) {
         mark("flow:liu_shen", true);
@@ -964,7 +1039,7 @@ cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, c
 cudaError_t flow_buffers(DevBuf &buf, int h, int w, int ni, int nj, int iterations_ls, FlowBufs *b) {
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t pl = al(sizeof(float) * (size_t)h * w);
-    const size_t total = 7 * pl + 10 * pl + al(ls_err_bytes(h, w, iterations_ls)) + 256 +
+    const size_t total = 7 * pl + 10 * pl + 2 * pl + al(ls_err_bytes(h, w, iterations_ls)) + 256 +
                          2 * al(sizeof(float) * 64) + al(sizeof(double) * (ni + nj)) +
                          al(spline_coef_bytes((long)ni * nj));
     cudaError_t e = buf.ensure(total);
@@ -973,6 +1048,7 @@ cudaError_t flow_buffers(DevBuf &buf, int h, int w, int ni, int nj, int iteratio
     float **planes[7] = {&b->lka, &b->lkb, &b->lsa, &b->lsb, &b->tmp, &b->fu, &b->fv};
     for (float **p : planes) { *p = (float *)c; c += pl; }
     b->fx = (float *)c; c += 10 * pl;
+    b->pyr = (float *)c; c += 2 * pl;
     b->err = (double *)c; c += al(ls_err_bytes(h, w, iterations_ls));
     b->mx = (unsigned *)c; c += 256;
     b->k_lk = (float *)c; c += al(sizeof(float) * 64);
@@ -1168,7 +1244,7 @@ qlpiv_status qlpiv_flow_after_piv(qlpiv_handle *h, const qlpiv_flow_desc *desc, 
                                   const int32_t *tops, const int32_t *lefts, float *tile_u, float *tile_v,
                                   float *dense_u, float *dense_v) {
     if (!h || !img_a || !img_b || !tops || !lefts || !tile_u || !tile_v) return fail(QLPIV_E_ARG, "NULL argument");
-    if (const char *m = check_flow_desc(desc)) return fail(QLPIV_E_ARG, "%s", m);
+    if (const char *m = check_flow_desc(desc, height, width)) return fail(QLPIV_E_ARG, "%s", m);
     qlpiv_status st = check_image(pixel_type, height, width);
     if (st != QLPIV_OK) return st;
     if (ni < 3 || nj < 3) return fail(QLPIV_E_SHAPE, "the spline needs at least 3 tiles per axis");

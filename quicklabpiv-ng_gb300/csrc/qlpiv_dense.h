@@ -30,6 +30,7 @@ cudaError_t launch_liu_shen(cudaStream_t s, const float *la, const float *lb, in
 struct FlowBufs {
     float *lka, *lkb, *lsa, *lsb, *tmp, *fu, *fv;
     float *fx;        // 10 x h x w (Liu-Shen fixed terms and ping-pong field)
+    float *pyr;       // 2 x h x w: the coarser Lucas-Kanade pyramid levels (images and field)
     double *err;      // ls_err_bytes(h, w, iterations_ls)
     unsigned *mx;     // one word
     float *k_lk, *k_ls;  // filter weights (device)
@@ -60,6 +61,6 @@ cudaError_t flow_buffers(struct DevBuf &buf, int h, int w, int ni, int nj, int i
 // Uploads both prefilters' weights (host staging kept by the caller until the stream syncs).
 cudaError_t upload_flow_weights(cudaStream_t s, const qlpiv_flow_desc &d, const FlowBufs &b, std::vector<float> &host);
 // Checks a flow descriptor; returns a message or nullptr.
-const char *check_flow_desc(const qlpiv_flow_desc *d);
+const char *check_flow_desc(const qlpiv_flow_desc *d, int h, int w);
 
 }  // namespace qlpiv

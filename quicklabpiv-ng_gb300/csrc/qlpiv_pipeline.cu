@@ -1021,7 +1021,7 @@ qlpiv_status qlpiv_piv_flow(qlpiv_handle *h, const qlpiv_adaptive_desc *piv, con
     if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
     qlpiv_status st = check_adaptive(piv, pixel_type, height, width);
     if (st != QLPIV_OK) return st;
-    if (const char *m = check_flow_desc(flow)) return fail(QLPIV_E_ARG, "%s", m);
+    if (const char *m = check_flow_desc(flow, height, width)) return fail(QLPIV_E_ARG, "%s", m);
     if (num_pairs < 0) return fail(QLPIV_E_ARG, "num_pairs < 0");
     if (num_pairs == 0) return QLPIV_OK;
     if (!frames || !out_u || !out_v) return fail(QLPIV_E_ARG, "NULL frame table or output");
@@ -1064,7 +1064,7 @@ qlpiv_status qlpiv_piv_flow_device(qlpiv_handle *h, const qlpiv_adaptive_desc *p
     if (!h) return fail(QLPIV_E_ARG, "handle is NULL");
     qlpiv_status st = check_adaptive(piv, pixel_type, height, width);
     if (st != QLPIV_OK) return st;
-    if (const char *m = check_flow_desc(flow)) return fail(QLPIV_E_ARG, "%s", m);
+    if (const char *m = check_flow_desc(flow, height, width)) return fail(QLPIV_E_ARG, "%s", m);
     if (num_pairs < 0) return fail(QLPIV_E_ARG, "num_pairs < 0");
     if (num_pairs == 0) return QLPIV_OK;
     if (!frames || !out_u || !out_v) return fail(QLPIV_E_ARG, "NULL frame table or output");

@@ -80,6 +80,36 @@ def test_flow_after_piv_bit_exact(qp, handle, oracle, case):
     assert tu2.tobytes() == gu.tobytes() and tv2.tobytes() == gv.tobytes()
 
 
+PYRAMID_CASES = [
+    # mode, dense export, window, iterations_lk, iterations_ls, (h, w), n, pyramid levels
+    (1, False, 27, 5, 0, (192, 224), 16, 2),
+    (1, True, 15, 3, 0, (160, 130), 32, 3),
+    (2, False, 15, 2, 10, (176, 160), 16, 2),
+    (1, False, 9, 4, 0, (256, 200), 16, 4),
+]
+
+
+@pytest.mark.parametrize("case", range(len(PYRAMID_CASES)))
+def test_flow_after_piv_pyramid_bit_exact(qp, handle, oracle, case):
+    """Lucas-Kanade coarse to fine (an extension of the reference's full-resolution stage) equals
+    the oracle's pyramid bit for bit, odd level sides included."""
+    mode, dense, win, it_lk, it_ls, (h, w), n, levels = PYRAMID_CASES[case]
+    a, b, flow = _pair(qp, h, w, seed=case + 31)
+    rng = np.random.default_rng(case + 7)
+    tops, lefts, tu, tv = _tiles(oracle, flow, h, w, n, rng)
+    d = qp.flow_desc(mode=mode, window_lk=win, iterations_lk=it_lk, iterations_ls=max(it_ls, 1), dense_export=dense,
+                     pyramid_levels=levels)
+    gu, gv, gdu, gdv = handle.flow_after_piv(a, b, n, tops, lefts, tu, tv, d)
+    ou, ov, odu, odv = oracle.flow_after_piv(a, b, n, tops, lefts, tu, tv, mode=mode, window=win,
+                                             iterations_lk=it_lk, iterations_ls=max(it_ls, 1), dense_export=dense,
+                                             pyramid_levels=levels)
+    assert gdu.tobytes() == odu.tobytes() and gdv.tobytes() == odv.tobytes()
+    assert gu.tobytes() == ou.tobytes() and gv.tobytes() == ov.tobytes()
+    fu, fv, fdu, _ = oracle.flow_after_piv(a, b, n, tops, lefts, tu, tv, mode=mode, window=win, iterations_lk=it_lk,
+                                           iterations_ls=max(it_ls, 1), dense_export=dense)
+    assert not np.array_equal(fdu, odu)             # the pyramid changed the result
+
+
 def test_flow_after_piv_tracks_the_flow(qp, handle, oracle):
     """Lucas-Kanade after PIV brings noisy tile displacements closer to the true flow."""
     h, w, n = 256, 256, 16
@@ -102,12 +132,19 @@ def test_flow_descriptor_rejected(qp, handle, oracle):
     a, b, flow = _pair(qp, 96, 96)
     tops, lefts, tu, tv = _tiles(oracle, flow, 96, 96, 16, np.random.default_rng(0))
     for bad in (dict(mode=3), dict(window_lk=8), dict(window_lk=33), dict(iterations_lk=0),
-                dict(mode=2, iterations_ls=0), dict(filter_px_lk=4), dict(ignore_piv=6)):
+                dict(mode=2, iterations_ls=0), dict(filter_px_lk=4), dict(ignore_piv=6), dict(pyramid_levels=5),
+                dict(pyramid_levels=-1)):
         with pytest.raises(qp.QlpivError) as e:
             handle.flow_after_piv(a, b, 16, tops, lefts, tu, tv, qp.flow_desc(**bad))
         assert e.value.status == qp.E_ARG
     with pytest.raises(qp.QlpivError):   # tiles outside the image
         handle.flow_after_piv(a, b, 16, tops + 90, lefts, tu, tv, qp.flow_desc())
+    a2, b2 = a[:56], b[:56]              # 56 >> 3 = 7 rows at the fourth level: below 8
+    t2 = tops[tops + 16 <= 56]
+    with pytest.raises(qp.QlpivError) as e:
+        handle.flow_after_piv(a2, b2, 16, t2, lefts, tu[:len(t2)], tv[:len(t2)], qp.flow_desc(pyramid_levels=4))
+    assert e.value.status == qp.E_ARG
+    handle.flow_after_piv(a2, b2, 16, t2, lefts, tu[:len(t2)], tv[:len(t2)], qp.flow_desc(pyramid_levels=3))
 
 
 @pytest.mark.parametrize("mode,dense", [(1, False), (2, True)])

@@ -165,3 +165,75 @@ def test_flow_after_piv_ignore_piv_modes(oracle, mode):
                                          ignore_piv=mode)
     np.testing.assert_array_equal(du, vs)
     np.testing.assert_array_equal(dv, us)
+
+
+def _pyr_down(f, scale):
+    """2 x 2 box average, ((a + b) + (c + d)) * 0.25 * scale in float32."""
+    h2, w2 = f.shape[0] // 2, f.shape[1] // 2
+    g = f[:2 * h2, :2 * w2]
+    t = (g[0::2, 0::2] + g[0::2, 1::2]) + (g[1::2, 0::2] + g[1::2, 1::2])
+    return ((t * np.float32(0.25)) * np.float32(scale)).astype(np.float32)
+
+
+def _pyr_up(f, h, w):
+    si = np.minimum(np.arange(h) >> 1, f.shape[0] - 1)
+    sj = np.minimum(np.arange(w) >> 1, f.shape[1] - 1)
+    return (np.float32(2.0) * f[np.ix_(si, sj)]).astype(np.float32)
+
+
+@pytest.mark.parametrize("levels,shape,half", [(2, (64, 72), False), (3, (67, 81), True), (2, (45, 38), True)])
+def test_lk_pyramid_is_the_level_composition(oracle, levels, shape, half):
+    """orc_dense_lk_pyramid equals down-sampling, coarse LK, nearest up-sampling and finer LK
+    chained by hand (odd sides drop their last row / column)."""
+    rng = np.random.default_rng(levels)
+    h, w = shape
+    a = oracle.gauss_filter(rng.integers(0, 255, (h, w)).astype(np.float32), 1.5, 3)
+    b = np.roll(a, (2, -3), axis=(0, 1))
+    us = rng.normal(0.0, 0.5, (h, w)).astype(np.float32)
+    vs = rng.normal(0.0, 0.5, (h, w)).astype(np.float32)
+    la, lb, lu, lv = [a], [b], [us], [vs]
+    for _ in range(1, levels):
+        la.append(_pyr_down(la[-1], 1.0))
+        lb.append(_pyr_down(lb[-1], 1.0))
+        lu.append(_pyr_down(lu[-1], 0.5))
+        lv.append(_pyr_down(lv[-1], 0.5))
+    u, v = lu[-1], lv[-1]
+    for lev in range(levels - 1, -1, -1):
+        if lev < levels - 1:
+            u = _pyr_up(u, *la[lev].shape)
+            v = _pyr_up(v, *la[lev].shape)
+        u, v = oracle.dense_lk(la[lev], lb[lev], u, v, 9, 3, half_pixel=half)
+    pu, pv = oracle.dense_lk_pyramid(a, b, us, vs, 9, 3, half_pixel=half, levels=levels)
+    np.testing.assert_array_equal(pu, u)
+    np.testing.assert_array_equal(pv, v)
+    one = oracle.dense_lk_pyramid(a, b, us, vs, 9, 3, half_pixel=half, levels=1)
+    np.testing.assert_array_equal(one[0], oracle.dense_lk(a, b, us, vs, 9, 3, half_pixel=half)[0])
+
+
+def test_lk_pyramid_recovers_a_larger_shift(oracle):
+    """From a zero start, a 6-pixel shift of smooth particles is beyond a 9-pixel window at full
+    resolution but within reach at the coarser levels."""
+    rng = np.random.default_rng(5)
+    h, w = 96, 96
+    a = oracle.gauss_filter((rng.random((h, w)) < 0.05).astype(np.float32) * 200.0, 2.0, 5)
+    b = np.roll(a, (0, 6), axis=(0, 1))
+    z = np.zeros((h, w), np.float32)
+    inner = (slice(24, 72), slice(24, 72))
+    u1, _ = oracle.dense_lk_pyramid(a, b, z, z, 9, 5, levels=1)
+    u3, v3 = oracle.dense_lk_pyramid(a, b, z, z, 9, 5, levels=3)
+    e1 = np.median(np.abs(u1[inner] - 6.0))
+    e3 = np.median(np.abs(u3[inner] - 6.0))
+    assert e3 < 0.5 and e3 < e1
+    assert np.median(np.abs(v3[inner])) < 0.5
+
+
+def test_flow_after_piv_pyramid_levels(oracle):
+    """pyramid_levels 0 and 1 are the reference's full-resolution flow; 2 differs."""
+    n = 16
+    a, b, tops, lefts, tu, tv = _flow_case(oracle, n=n)
+    r0 = oracle.flow_after_piv(a, b, n, tops, lefts, tu, tv, mode=1)
+    r1 = oracle.flow_after_piv(a, b, n, tops, lefts, tu, tv, mode=1, pyramid_levels=1)
+    r2 = oracle.flow_after_piv(a, b, n, tops, lefts, tu, tv, mode=1, pyramid_levels=2)
+    for x, y in zip(r0, r1):
+        np.testing.assert_array_equal(x, y)
+    assert not np.array_equal(r0[2], r2[2])
