@@ -648,7 +648,22 @@ def main():
     ap.add_argument("--only-batched", action="store_true")
     ap.add_argument("--batched-pairs", type=int, default=256)
     ap.add_argument("--batched-sizes", default="16,32,64,128")
+    # profiling aid: only the hybrid PIV + dense flow leg (its own JSON line)
+    ap.add_argument("--only-hybrid", action="store_true")
     args = ap.parse_args()
+    if args.only_hybrid:
+        import torch
+        pkg = load_pkg()
+        pkg.build.build()
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        h = pkg.Handle(dev.index)
+        try:
+            stream = torch.cuda.ExternalStream(h.stream, device=dev)
+            print(json.dumps(run_hybrid(pkg, h, dev, stream, max(1, args.steps), max(1, args.warmup))), flush=True)
+        finally:
+            h.close()
+        return
     if args.only_batched:
         import torch
         pkg = load_pkg()
