@@ -145,8 +145,15 @@ __device__ __forceinline__ bool lk_axis(float o, int W, LkAxis &ax) {
     return true;
 }
 
-// The window points of a CTA's pixel tile: image A and its derivatives dj, di, row-major
-// GS x GS each.
+// The window points of a CTA's pixel tile: image A and its derivatives dj, di, GS x GS each,
+// rows `ws` floats apart.  A warp reads one window point per thread from two groups of 16
+// lanes (two thread rows); the row stride is padded so that the groups land 16 banks apart:
+// ws = 8 (mod 16) when the groups are two rows of pixel pairs (2 ws apart), ws = 16 (mod 32)
+// when they are two pixel rows.  GS = 42 (window 27) read at stride 42 put the groups 20 banks
+// apart and half of the kernel's shared wavefronts were conflict replays.
+__host__ __device__ constexpr int lk_pair_stride(int GS) { return GS + (24 - GS % 16) % 16; }
+__host__ __device__ constexpr int lk_row_stride(int GS) { return GS + (48 - GS % 32) % 32; }
+
 struct LkWin {
     const float *a, *dj, *di;
 };
@@ -154,7 +161,8 @@ struct LkWin {
 // Stages the A region (clamped; 2x2 averages for the half-pixel offset) of a tile with origin
 // (ti0, tj0) in reg (RS x RS) and computes the window points' values and derivatives.
 __device__ __forceinline__ void lk_stage(const float *A, int h, int w, int W, int half_pixel, int ti0, int tj0,
-                                         int tid, int nthr, int tile, float *reg, float *wa, float *wj, float *wi) {
+                                         int tid, int nthr, int tile, int ws, float *reg, float *wa, float *wj,
+                                         float *wi) {
     const int hw = W / 2;
     const int RS = tile + W + 1, GS = tile + W - 1;
     for (int q = tid; q < RS * RS; q += nthr) {
@@ -176,11 +184,12 @@ __device__ __forceinline__ void lk_stage(const float *A, int h, int w, int W, in
         const float *r0 = reg + gy * RS + gx, *r1 = r0 + RS, *r2 = r1 + RS;
         const float TL = r0[0], T = r0[1], TR = r0[2], L = r1[0], C = r1[1], R = r1[2], BL = r2[0], Bt = r2[1],
                     BR = r2[2];
-        wj[q] = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TL, BL), TR), BR), c3),
+        const int o = gy * ws + gx;
+        wj[o] = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TL, BL), TR), BR), c3),
                           __fdiv_rn(__fmul_rn(__fsub_rn(L, R), 10.0f), 32.0f));
-        wi[q] = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TR, TL), BR), BL), c3),
+        wi[o] = __fadd_rn(__fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(TR, TL), BR), BL), c3),
                           __fdiv_rn(__fmul_rn(__fsub_rn(T, Bt), 10.0f), 32.0f));
-        wa[q] = C;
+        wa[o] = C;
     }
     __syncthreads();
 }
@@ -375,30 +384,31 @@ __device__ __forceinline__ bool lk_fast(const LkPix &px, int h, int w, int W, fl
 }
 
 // Window side WT, two vertically adjacent pixels per thread: a CTA of 16 x 8 threads covers
-// 16 x 16 pixels.  Shared memory: the window arrays (3 x GS^2 floats) after the staged region.
+// 16 x 16 pixels.  Shared memory: the window arrays (3 x GS rows of SS floats), then the staged
+// region.
 template <int WT, int MB>
 __global__ void __launch_bounds__(128, MB) dense_lk_pair_kernel(const float *A, const float *B, int h, int w,
                                                                 float *us, float *vs, int iterations, int half_pixel) {
     extern __shared__ float smf[];
-    constexpr int W = WT, hw = WT / 2, GS = kLkTile + WT - 1;
-    float *wa = smf, *wj = wa + GS * GS, *wi = wj + GS * GS, *reg = wi + GS * GS;
+    constexpr int W = WT, hw = WT / 2, GS = kLkTile + WT - 1, SS = lk_pair_stride(GS);
+    float *wa = smf, *wj = wa + GS * SS, *wi = wj + GS * SS, *reg = wi + GS * SS;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int ti0 = blockIdx.y * kLkTile, tj0 = blockIdx.x * kLkTile;
-    lk_stage(A, h, w, W, half_pixel, ti0, tj0, tid, blockDim.x * blockDim.y, kLkTile, reg, wa, wj, wi);
+    lk_stage(A, h, w, W, half_pixel, ti0, tj0, tid, blockDim.x * blockDim.y, kLkTile, SS, reg, wa, wj, wi);
     const LkWin win{wa, wj, wi};
     const int pj = tj0 + threadIdx.x, pi0 = ti0 + 2 * threadIdx.y;
     if (pj >= w || pi0 >= h) return;
     const bool two = pi0 + 1 < h;
-    const int g0 = 2 * threadIdx.y * GS + threadIdx.x, g1 = g0 + GS;
+    const int g0 = 2 * threadIdx.y * SS + threadIdx.x, g1 = g0 + SS;
     LkPix px[2];
     px[0].pi = pi0;
     px[0].pj = pj;
     px[0].p = (long)pi0 * w + pj;
-    lk_begin(win, g0, GS, W, us, vs, half_pixel, px[0]);
+    lk_begin(win, g0, SS, W, us, vs, half_pixel, px[0]);
     px[1].pi = pi0 + 1;
     px[1].pj = pj;
     px[1].p = px[0].p + w;
-    if (two) lk_begin(win, g1, GS, W, us, vs, half_pixel, px[1]);
+    if (two) lk_begin(win, g1, SS, W, us, vs, half_pixel, px[1]);
     else px[1].active = false;
     for (int it = 0; it < iterations && (px[0].active || px[1].active); it++) {
         bool run[2], fast[2];
@@ -420,16 +430,16 @@ __global__ void __launch_bounds__(128, MB) dense_lk_pair_kernel(const float *A, 
         if (fast[0] && fast[1]) {
             const bool sp0 = ax[0].split != W, sp1 = ax[1].split != W;
             if (!sp0 && !sp1)
-                lk_pair_sums<WT, false, false>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, GS, s[0][0], s[0][1],
+                lk_pair_sums<WT, false, false>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, SS, s[0][0], s[0][1],
                                                s[1][0], s[1][1]);
             else if (sp0 && !sp1)
-                lk_pair_sums<WT, true, false>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, GS, s[0][0], s[0][1],
+                lk_pair_sums<WT, true, false>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, SS, s[0][0], s[0][1],
                                               s[1][0], s[1][1]);
             else if (!sp0 && sp1)
-                lk_pair_sums<WT, false, true>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, GS, s[0][0], s[0][1],
+                lk_pair_sums<WT, false, true>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, SS, s[0][0], s[0][1],
                                               s[1][0], s[1][1]);
             else
-                lk_pair_sums<WT, true, true>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, GS, s[0][0], s[0][1],
+                lk_pair_sums<WT, true, true>(B, w, ay[0], ax[0], ay[1], ax[1], win, g0, SS, s[0][0], s[0][1],
                                              s[1][0], s[1][1]);
         } else {
 #pragma unroll
@@ -437,10 +447,10 @@ __global__ void __launch_bounds__(128, MB) dense_lk_pair_kernel(const float *A, 
                 if (!run[k]) continue;
                 const int g = k ? g1 : g0;
                 if (fast[k]) {
-                    if (ax[k].split == W) lk_one_sums<WT, false>(B, w, ay[k], ax[k], win, g, GS, s[k][0], s[k][1]);
-                    else lk_one_sums<WT, true>(B, w, ay[k], ax[k], win, g, GS, s[k][0], s[k][1]);
+                    if (ax[k].split == W) lk_one_sums<WT, false>(B, w, ay[k], ax[k], win, g, SS, s[k][0], s[k][1]);
+                    else lk_one_sums<WT, true>(B, w, ay[k], ax[k], win, g, SS, s[k][0], s[k][1]);
                 } else {
-                    lk_sums_slow(B, h, w, W, oi[k], oj[k], win, g, GS, s[k][0], s[k][1]);
+                    lk_sums_slow(B, h, w, W, oi[k], oj[k], win, g, SS, s[k][0], s[k][1]);
                 }
             }
         }
@@ -459,20 +469,20 @@ __global__ void __launch_bounds__(kLkTile *kLkTile, 2) dense_lk_kernel(const flo
                                                                         int half_pixel) {
     extern __shared__ float smf[];
     constexpr int kThreads = kLkTile * kLkTile;
-    const int hw = W / 2, GS = kLkTile + W - 1;
-    float *wa = smf, *wj = wa + GS * GS, *wi = wj + GS * GS, *reg = wi + GS * GS;
+    const int hw = W / 2, GS = kLkTile + W - 1, SS = lk_row_stride(GS);
+    float *wa = smf, *wj = wa + GS * SS, *wi = wj + GS * SS, *reg = wi + GS * SS;
     const int tid = threadIdx.y * kLkTile + threadIdx.x;
     const int ti0 = blockIdx.y * kLkTile, tj0 = blockIdx.x * kLkTile;
-    lk_stage(A, h, w, W, half_pixel, ti0, tj0, tid, kThreads, kLkTile, reg, wa, wj, wi);
+    lk_stage(A, h, w, W, half_pixel, ti0, tj0, tid, kThreads, kLkTile, SS, reg, wa, wj, wi);
     const LkWin win{wa, wj, wi};
     const int pi = ti0 + threadIdx.y, pj = tj0 + threadIdx.x;
     if (pi >= h || pj >= w) return;
-    const int g = threadIdx.y * GS + threadIdx.x;
+    const int g = threadIdx.y * SS + threadIdx.x;
     LkPix px;
     px.pi = pi;
     px.pj = pj;
     px.p = (long)pi * w + pj;
-    lk_begin(win, g, GS, W, us, vs, half_pixel, px);
+    lk_begin(win, g, SS, W, us, vs, half_pixel, px);
     float *hb = reg + tid;  // the staged region is dead: per-thread rows, stride kThreads
     for (int it = 0; it < iterations && px.active; it++) {
         if (px.locI < 0.0f || px.locI >= (float)(h + hw) || px.locJ < 0.0f || px.locJ >= (float)(w + hw)) break;
@@ -490,7 +500,7 @@ __global__ void __launch_bounds__(kLkTile *kLkTile, 2) dense_lk_kernel(const flo
                 x0 = x1;
             }
             for (int a = 0; a < W; a++) {
-                const int r = g + a * GS;
+                const int r = g + a * SS;
                 br += w;
                 x0 = br[0];
                 for (int b = 0; b < W; b++) {
@@ -506,7 +516,7 @@ __global__ void __launch_bounds__(kLkTile *kLkTile, 2) dense_lk_kernel(const flo
                 }
             }
         } else {
-            lk_sums_slow(B, h, w, W, oi, oj, win, g, GS, b0, b1);
+            lk_sums_slow(B, h, w, W, oi, oj, win, g, SS, b0, b1);
         }
         if (!lk_update(px, b0, b1)) break;
     }
@@ -517,8 +527,9 @@ __global__ void __launch_bounds__(kLkTile *kLkTile, 2) dense_lk_kernel(const flo
 // the generic kernel).
 size_t lk_smem(int W, bool rows_in_smem) {
     const size_t RS = kLkTile + W + 1, GS = kLkTile + W - 1;
+    const size_t SS = rows_in_smem ? lk_row_stride((int)GS) : lk_pair_stride((int)GS);
     const size_t rows = rows_in_smem ? (size_t)W * kLkTile * kLkTile : 0;
-    return sizeof(float) * (3 * GS * GS + (RS * RS > rows ? RS * RS : rows));
+    return sizeof(float) * (3 * GS * SS + (RS * RS > rows ? RS * RS : rows));
 }
 
 template <int WT, int MB>
