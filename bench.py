@@ -139,18 +139,35 @@ def oracle_validation(orc):
                          iterate_until_no_corrections=v["iterate_until"])
 
 
-def cpu_baseline(pkg, pair, threads, reps=1):
+def c2_accuracy(pairs_host, u_host, v_host):
+    """Last-level displacements of the timed workload against the FP64 oracle pipeline, per
+    distinct pair: max and 99th-percentile |error| and the fraction within 1e-3 px."""
+    orc = load_oracle()
+    errs = []
+    for k, (a, b) in enumerate(pairs_host):
+        ou, ov = orc.piv_adaptive(a, b, LEVELS[0], LEVELS[-1], OVERLAP_FACTOR, norm_mode=orc.NORM_MAX_A,
+                                  fixed_max=FULL_SCALE, precision=64, validation=oracle_validation(orc))
+        errs.append(np.maximum(np.abs(u_host[k] - ou), np.abs(v_host[k] - ov)).ravel())
+    e = np.concatenate(errs)
+    return {"reference": "FP64 oracle pipeline (same algorithm in double)", "pairs": len(pairs_host),
+            "vectors": int(e.size), "max_px": float(e.max()), "p99_px": float(np.quantile(e, 0.99)),
+            "frac_within_1e-3": float(np.mean(e <= 1e-3))}
+
+
+def cpu_baseline(pkg, pair, threads, reps=5, warmup=1):
     """Oracle FP32 restatement of the reference CPU path on one pair: the same adaptive
-    loop (inheritance, bicubic field, bilinear warp, three correlation passes)."""
+    loop (inheritance, bicubic field, bilinear warp, three correlation passes).  `warmup`
+    untimed runs, then the median of `reps` timed repetitions (seconds per pair)."""
     orc = load_oracle()
     a, b = pair
     times = []
-    for _ in range(reps):
+    for r in range(reps + warmup):
         t0 = time.perf_counter()
         orc.piv_adaptive(a, b, LEVELS[0], LEVELS[-1], OVERLAP_FACTOR, norm_mode=orc.NORM_MAX_A, fixed_max=FULL_SCALE,
                          precision=32, nthreads=threads, validation=oracle_validation(orc))
-        times.append(time.perf_counter() - t0)
-    return min(times)
+        if r >= warmup:
+            times.append(time.perf_counter() - t0)
+    return statistics.median(times)
 
 
 WORKLOAD = ("adaptive-1024-u12: 1024x1024 12-bit pairs, IA 64 -> 32 -> 16 at 75 % overlap, BothImages bilinear "
@@ -178,7 +195,25 @@ def hybrid_descs(pkg):
     return piv, flow
 
 
-def run_hybrid(pkg, h, dev, stream, steps, warmup):
+def hybrid_accuracy(pkg, h, pair, dense_u, dense_v):
+    """Dense field of one hybrid pair against the FP64 twin of the flow stage, fed the GPU's own PIV
+    tiles (RMS and max over every pixel, px)."""
+    orc = load_oracle()
+    piv, _ = hybrid_descs(pkg)
+    a, b = pair
+    pu, pv = h.piv_adaptive([a], [b], piv)
+    _, tops, lefts = orc.grid(H, W, 32, 0, 0.5)
+    _, _, du64, dv64 = orc.flow_after_piv(a, b, 32, tops, lefts, pu[0], pv[0], mode=2, sigma_lk=2.0, px_lk=3,
+                                          sigma_ls=0.48, px_ls=5, window=27, iterations_lk=5, lam=4.0,
+                                          iterations_ls=60, dense_export=True, pyramid_levels=2, precision=64)
+    eu = dense_u.astype(np.float64) - du64
+    ev = dense_v.astype(np.float64) - dv64
+    return {"reference": "FP64 twin of the flow stage on the GPU's PIV tiles", "pairs": 1,
+            "pixels": int(eu.size), "rms_px": float(np.sqrt(np.mean(eu * eu + ev * ev))),
+            "max_px": float(max(np.abs(eu).max(), np.abs(ev).max()))}
+
+
+def run_hybrid(pkg, h, dev, stream, steps, warmup, accuracy=False):
     """Config-4 step: PIV + flow of HYBRID_PAIRS pairs resident in HBM, dense field out."""
     import torch
     piv, flow = hybrid_descs(pkg)
@@ -225,20 +260,90 @@ def run_hybrid(pkg, h, dev, stream, steps, warmup):
     # e2e: host frames in, tile vectors and dense field out
     fa = [pairs[k % len(pairs)][0] for k in range(hp)]
     fb = [pairs[k % len(pairs)][1] for k in range(hp)]
-    h.piv_flow(fa, fb, piv, flow, dense=True)
+    res = h.piv_flow(fa, fb, piv, flow, dense=True)
+    acc = hybrid_accuracy(pkg, h, pairs[0], res[2][0], res[3][0]) if accuracy else None
     e2e_steps = 2
     tt = time.perf_counter()
     for _ in range(e2e_steps):
         h.piv_flow(fa, fb, piv, flow, dense=True)
     e2e_s = (time.perf_counter() - tt) / e2e_steps
     px = float(H * W)
-    return {
+    out = {
         "workload": HYBRID_WORKLOAD, "pairs_per_step": hp, "ms_per_step": ms, "frame_pairs_per_s": hp / (ms * 1e-3),
         "dense_mpx_per_s": hp * px / (ms * 1e-3) / 1e6, "gpu_launches_per_step": launches,
         "stages": [{"stage": st["stage"], "ia_side": st["ia_side"], "ms_per_step": st["ms"]} for st in stages],
         "e2e": {"value": hp / e2e_s, "unit": "frame-pairs/s", "h2d_bytes_per_step": hp * 2 * H * W,
                 "d2h_bytes_per_step": hp * (2 * tiles + 2 * H * W) * 4},
     }
+    if acc is not None:
+        out["accuracy"] = acc
+    return out
+
+
+C1_WORKLOAD = ("single-512-u8: 512x512 u8 Rankine pairs (0.02 ppp, d = 3 +- 0.5 px, max 4 px), one 32x32 pass at "
+               "50 % overlap (961 vectors), FindMaximumFromCenter + 3-point Gaussian")
+
+
+def run_config1(pkg, h, dev, stream, steps, warmup, cpu=True, pairs=256):
+    """The plain single-pass workload three ways: a device-resident batch of `pairs` pairs through
+    the fused adaptive entry point (one level), one synchronous qlpiv_pass per pair on host
+    images, and the oracle's FP32 pass on the host cores; plus the error against the FP64 oracle."""
+    import torch
+    desc = pkg.adaptive_desc(32, 32, 0.5, warp_mode=pkg.WARP_NONE, norm_mode=pkg.NORM_MAX_A,
+                             max_mode=pkg.MAX_COMPUTE)
+    uniq = [pkg.synth.config1_pair(seed=1, pair_id=k) for k in range(8)]
+    imgs = torch.empty((pairs, 2, 512, 512), dtype=torch.uint8, device=dev)
+    table = np.zeros(pairs, pkg.FRAME_DTYPE)
+    for k in range(pairs):
+        imgs[k, 0].copy_(torch.from_numpy(uniq[k % 8][0]))
+        imgs[k, 1].copy_(torch.from_numpy(uniq[k % 8][1]))
+        table[k] = (imgs[k, 0].data_ptr(), imgs[k, 1].data_ptr(), 512, 512, 512)
+    dtable = torch.from_numpy(table.view(np.uint8)).to(dev)
+    ou = torch.empty(pairs * 961, dtype=torch.float32, device=dev)
+    ov = torch.empty_like(ou)
+    for _ in range(warmup):
+        h.piv_adaptive_device(desc, pkg.PIX_U8, 512, 512, pairs, dtable, ou, ov)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        h.piv_adaptive_device(desc, pkg.PIX_U8, 512, 512, pairs, dtable, ou, ov)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    g = pkg.grid.superposition(512, 512, 32, 0, 0.5)
+    at, al = g.origins()
+    for k in range(3):
+        vec = h.piv_pass(uniq[k][0], uniq[k][1], 32, at, al)
+    reps = 32
+    t0 = time.perf_counter()
+    for k in range(reps):
+        h.piv_pass(uniq[k % 8][0], uniq[k % 8][1], 32, at, al)
+    per_call_s = (time.perf_counter() - t0) / reps
+    out = {"workload": C1_WORKLOAD, "pairs_per_step": pairs, "ms_per_step": ms,
+           "frame_pairs_per_s": pairs / (ms * 1e-3), "ia_vectors_per_s": pairs * 961 / (ms * 1e-3),
+           "plain_per_call": {"frame_pairs_per_s": 1.0 / per_call_s,
+                              "sample": f"{reps} pairs, one synchronous qlpiv_pass per pair (host images)"},
+           "vs_per_call": (pairs / (ms * 1e-3)) * per_call_s}
+    if cpu:
+        orc = load_oracle()
+        a, b = uniq[0]
+        threads = os.cpu_count() or 1
+        orc.piv_pass(a, b, 32, at, al, precision=32, nthreads=threads)
+        times = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            orc.piv_pass(a, b, 32, at, al, precision=32, nthreads=threads)
+            times.append(time.perf_counter() - t0)
+        out["cpu_baseline"] = {"value": 1.0 / statistics.median(times), "unit": "frame-pairs/s", "cores": threads,
+                               "kind": "port", "sample": "one pair, median of 5 after 1 warm-up (FP32 oracle pass)"}
+        gu = ou[:961].cpu().numpy()
+        gv = ov[:961].cpu().numpy()
+        o64 = orc.piv_pass(a, b, 32, at, al, precision=64, nthreads=threads)
+        e = np.maximum(np.abs(gu - o64["u64"]), np.abs(gv - o64["v64"]))
+        out["accuracy"] = {"reference": "FP64 oracle pass", "vectors": 961, "max_px": float(e.max()),
+                           "p99_px": float(np.quantile(e, 0.99)), "frac_within_1e-3": float(np.mean(e <= 1e-3))}
+    return out
 
 
 def run_per_call(pkg, dev, desc, pairs_host, count):
@@ -450,8 +555,8 @@ def run_reference(args, rank):
     threads = os.cpu_count() or 1
     pair = make_pairs(pkg, 1)[0]
     for _ in range(args.warmup):
-        cpu_baseline(pkg, pair, threads)
-    times = [cpu_baseline(pkg, pair, threads) for _ in range(args.steps)]
+        cpu_baseline(pkg, pair, threads, reps=1, warmup=0)
+    times = [cpu_baseline(pkg, pair, threads, reps=1, warmup=0) for _ in range(args.steps)]
     t = sum(times) / len(times)
     v = 1.0 / t
     line = {
@@ -564,6 +669,11 @@ def run_gpu(args, rank, world):
     h2d = P * 2 * H * W * bpp
     d2h = 2 * P * last.count * 4
 
+    # ---- accuracy of the timed workload: the e2e run's displacements against the FP64 oracle ----
+    accuracy = None
+    if rank == 0 and not args.no_cpu:
+        accuracy = c2_accuracy(pairs_host, u_host, v_host)
+
     # ---- roofline of the dominant kernel ----
     dom = max(stages, key=lambda s_: s_["ms"])
     t_launch = dom["ms"] / dom["launches"] * 1e-3
@@ -599,15 +709,26 @@ def run_gpu(args, rank, world):
         "stages": [{k: st[k] for k in ("stage", "level", "ia_side", "ms_per_step")} for st in stages],
         "e2e": {"value": e2e_val, "unit": "frame-pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "achieved": alg_bytes / t_launch / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": alg_bytes / t_launch / 1e9 / hbm_peak, "traffic": traffic, "kernel": kernel,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "clocks": sampler.summary(),
     }
+    hbm_view = {"bound": "hbm", "achieved": alg_bytes / t_launch / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": alg_bytes / t_launch / 1e9 / hbm_peak, "traffic": traffic, "kernel": kernel,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
     if alg_flops:
-        result["compute_roofline"] = {"bound": "fp32", "achieved": alg_flops / t_launch / 1e12, "peak": fp32_peak,
-                                      "unit": "TFLOP/s", "frac": alg_flops / t_launch / 1e12 / fp32_peak,
-                                      "kernel": kernel, "peak_source": "live FP32 FMA probe (qlpiv_measure_fp32_peak)"}
+        # the correlation kernel is FP32 (CUDA-core) bound: its roofline is the FP32 FMA peak
+        # measured live on this GPU; the HBM view is kept beside it
+        result["roofline"] = {"bound": "fp32", "achieved": alg_flops / t_launch / 1e12, "peak": fp32_peak,
+                              "unit": "TFLOP/s", "frac": alg_flops / t_launch / 1e12 / fp32_peak,
+                              "traffic": traffic, "kernel": kernel,
+                              "peak_source": "live FP32 FMA probe on this GPU (qlpiv_measure_fp32_peak, best of 3); "
+                                             "nominal 152 SMs x 128 lanes x 2 flop x 2.07 GHz = 80.5 TFLOP/s",
+                              "flops_per_ia": flops_per_ia(dom["ia_side"]),
+                              "ias_per_launch": items_per_launch}
+        result["roofline_hbm"] = hbm_view
+    else:
+        result["roofline"] = hbm_view
+    if accuracy is not None:
+        result["accuracy"] = {"adaptive-1024-u12": accuracy}
     # ---- the plain per-call GPU path on the same workload (denominator of the batching gain) ----
     pc_value, pp_value = run_per_call(pkg, dev, desc, pairs_host, 4)
     result["plain_per_call"] = {
@@ -615,8 +736,11 @@ def run_gpu(args, rank, world):
         "sample": "4 pairs, one at a time, one synchronous library call per stage (host arrays in and out)",
         "value_vs": pairs_per_s / pc_value, "e2e_vs": e2e_val / (world * pc_value),
         "one_pair_per_call_fused": world * pp_value}
+    result["single_pass"] = run_config1(pkg, h, dev, stream, max(3, min(args.steps, 10)), max(3, args.warmup),
+                                        cpu=rank == 0 and not args.no_cpu)
     if not args.no_hybrid:
-        result["hybrid"] = run_hybrid(pkg, h, dev, stream, max(2, min(args.steps, 5)), max(3, args.warmup))
+        result["hybrid"] = run_hybrid(pkg, h, dev, stream, max(2, min(args.steps, 5)), max(3, args.warmup),
+                                      accuracy=rank == 0 and not args.no_cpu)
     if not args.no_batched:
         result["batched"] = run_batched(pkg, dev, stream, max(3, min(args.steps, 10)), max(3, args.warmup))
     if not args.no_serving and world == 1:
@@ -625,7 +749,8 @@ def run_gpu(args, rank, world):
         threads = os.cpu_count() or 1
         t_cpu = cpu_baseline(pkg, pairs_host[0], threads)
         result["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "frame-pairs/s", "cores": threads, "kind": "port",
-                                  "sample": "one 1024x1024 pair through the whole adaptive loop (FP32 oracle)"}
+                                  "sample": "one 1024x1024 pair through the whole adaptive loop (FP32 oracle), "
+                                            "median of 5 runs after 1 warm-up"}
     h.close()
     if rank == 0:
         print(json.dumps(result), flush=True)

@@ -45,7 +45,8 @@ def valid_cfg(num_peaks=3, kernel_width=3, threshold=2.0, epsilon0=0.1, max_iter
 def build(force=False):
     """Compile the oracle with its Makefile (gcc only; seconds)."""
     src = [HERE / "qlpiv_oracle.c", HERE / "qlpiv_oracle_adaptive.c", HERE / "qlpiv_oracle_validate.c", HERE / "qlpiv_oracle_dense.c",
-           HERE / "oracle_types.h", HERE / "oracle_impl.h", HERE / "oracle_interp_impl.h", HERE / "Makefile"]
+           HERE / "oracle_types.h", HERE / "oracle_impl.h", HERE / "oracle_interp_impl.h", HERE / "oracle_dense_impl.h",
+           HERE / "Makefile"]
     if not force and LIB_PATH.exists() and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in src):
         return LIB_PATH
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
@@ -105,15 +106,18 @@ def lib():
                                         fp, fp]
         L.orc_area_overlap.argtypes = [c_int, c_int, c_int, c_int, c_int, c_int, ip]
         L.orc_area_overlap.restype = c_float
-        L.orc_gauss_kernel.argtypes = [c_float, c_int, fp]
-        L.orc_gauss_filter.argtypes = [fp, c_int, c_int, fp, c_int, fp]
-        L.orc_normalize.argtypes = [fp, c_long, fp]
-        L.orc_dense_lk.argtypes = [fp, fp, c_int, c_int, fp, fp, c_int, c_int, c_int]
-        L.orc_liu_shen.argtypes = [fp, fp, c_int, c_int, fp, fp, c_float, c_int, c_int, vp, vp, vp]
-        L.orc_flow_after_piv.argtypes = [fp, fp, c_int, c_int, c_int, c_int, c_int, ip, ip, fp, fp, c_int, c_float,
-                                         c_int, c_float, c_int, c_int, c_int, c_float, c_int, c_int, c_int, c_int,
-                                         vp, vp]
-        L.orc_dense_lk_pyramid.argtypes = [fp, fp, c_int, c_int, fp, fp, c_int, c_int, c_int, c_int]
+        for sfx, real in (("", c_float), ("_f64", ctypes.c_double)):
+            getattr(L, "orc_gauss_kernel" + sfx).argtypes = [c_float, c_int, vp]
+            getattr(L, "orc_gauss_filter" + sfx).argtypes = [vp, c_int, c_int, vp, c_int, vp]
+            getattr(L, "orc_normalize" + sfx).argtypes = [vp, c_long, vp]
+            getattr(L, "orc_dense_lk" + sfx).argtypes = [vp, vp, c_int, c_int, vp, vp, c_int, c_int, c_int]
+            getattr(L, "orc_liu_shen" + sfx).argtypes = [vp, vp, c_int, c_int, vp, vp, real, c_int, c_int, vp, vp,
+                                                         vp]
+            getattr(L, "orc_flow_after_piv" + sfx).argtypes = [fp, fp, c_int, c_int, c_int, c_int, c_int, ip, ip, fp,
+                                                               fp, c_int, c_float, c_int, c_float, c_int, c_int, c_int,
+                                                               c_float, c_int, c_int, c_int, c_int, vp, vp]
+            getattr(L, "orc_dense_lk_pyramid" + sfx).argtypes = [vp, vp, c_int, c_int, vp, vp, c_int, c_int, c_int,
+                                                                 c_int]
         L.orc_vector_size.restype = c_int
         assert L.orc_vector_size() == VECTOR_DTYPE.itemsize
         _lib = L
@@ -512,64 +516,76 @@ def validate(tops, lefts, u, v, peak_u, peak_v, npeaks, cfg):
 
 # ---------------- dense optical flow stages ----------------
 
-def gauss_kernel(sigma, px):
-    """GaussianFilter2D.createKernel weights (float)."""
-    k = np.zeros(px, np.float32)
-    lib().orc_gauss_kernel(sigma, px, _ptr(k, ctypes.c_float))
+def _real(a, precision):
+    return np.ascontiguousarray(a, np.float32 if precision == 32 else np.float64)
+
+
+def _rptr(a):
+    return a.ctypes.data
+
+
+def _fn(name, precision):
+    return getattr(lib(), name if precision == 32 else name + "_f64")
+
+
+def gauss_kernel(sigma, px, precision=32):
+    """GaussianFilter2D.createKernel weights (float, or unrounded double for precision=64)."""
+    k = np.zeros(px, np.float32 if precision == 32 else np.float64)
+    _fn("orc_gauss_kernel", precision)(ctypes.c_float(sigma), px, _rptr(k))
     return k
 
 
-def gauss_filter(img, sigma, px):
-    """GaussianFilter2D.applyFilter of a 2-D image (any numeric dtype) -> float32."""
-    a = _f32(img)
-    k = gauss_kernel(sigma, px)
+def gauss_filter(img, sigma, px, precision=32):
+    """GaussianFilter2D.applyFilter of a 2-D image (any numeric dtype) -> float32 (float64 for the
+    FP64 twin)."""
+    a = _real(img, precision)
+    k = gauss_kernel(sigma, px, precision)
     out = np.zeros_like(a)
-    lib().orc_gauss_filter(_ptr(a, ctypes.c_float), a.shape[0], a.shape[1], _ptr(k, ctypes.c_float), px,
-                           _ptr(out, ctypes.c_float))
+    _fn("orc_gauss_filter", precision)(_rptr(a), a.shape[0], a.shape[1], _rptr(k), px, _rptr(out))
     return out
 
 
-def normalize(img):
-    a = _f32(img)
+def normalize(img, precision=32):
+    a = _real(img, precision)
     out = np.zeros_like(a)
-    lib().orc_normalize(_ptr(a, ctypes.c_float), a.size, _ptr(out, ctypes.c_float))
+    _fn("orc_normalize", precision)(_rptr(a), ctypes.c_long(a.size), _rptr(out))
     return out
 
 
-def dense_lk(img_a, img_b, us, vs, window, iterations, half_pixel=False):
+def dense_lk(img_a, img_b, us, vs, window, iterations, half_pixel=False, precision=32):
     """Dense Lucas-Kanade: returns refined (us, vs) (columns, rows)."""
-    a, b = _f32(img_a), _f32(img_b)
-    u, v = _f32(us).copy(), _f32(vs).copy()
-    lib().orc_dense_lk(_ptr(a, ctypes.c_float), _ptr(b, ctypes.c_float), a.shape[0], a.shape[1],
-                       _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), window, iterations, int(half_pixel))
+    a, b = _real(img_a, precision), _real(img_b, precision)
+    u, v = _real(us, precision).copy(), _real(vs, precision).copy()
+    _fn("orc_dense_lk", precision)(_rptr(a), _rptr(b), a.shape[0], a.shape[1], _rptr(u), _rptr(v), window,
+                                   iterations, int(half_pixel))
     return u, v
 
 
-def dense_lk_pyramid(img_a, img_b, us, vs, window, iterations, half_pixel=False, levels=2):
+def dense_lk_pyramid(img_a, img_b, us, vs, window, iterations, half_pixel=False, levels=2, precision=32):
     """Dense Lucas-Kanade coarse to fine over `levels` 2 x 2 box-averaged levels (this library's own
     design): returns refined (us, vs) (columns, rows)."""
-    a, b = _f32(img_a), _f32(img_b)
-    u, v = _f32(us).copy(), _f32(vs).copy()
-    lib().orc_dense_lk_pyramid(_ptr(a, ctypes.c_float), _ptr(b, ctypes.c_float), a.shape[0], a.shape[1],
-                               _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), window, iterations, int(half_pixel),
-                               levels)
+    a, b = _real(img_a, precision), _real(img_b, precision)
+    u, v = _real(us, precision).copy(), _real(vs, precision).copy()
+    _fn("orc_dense_lk_pyramid", precision)(_rptr(a), _rptr(b), a.shape[0], a.shape[1], _rptr(u), _rptr(v), window,
+                                           iterations, int(half_pixel), levels)
     return u, v
 
 
-def liu_shen(ls_a, ls_b, us, vs, lam, iterations, half_pixel=False, intermediates=False):
+def liu_shen(ls_a, ls_b, us, vs, lam, iterations, half_pixel=False, intermediates=False, precision=32):
     """Liu-Shen passes on (us, vs); with intermediates also the fixed terms (12 planes: w, IIx,
     IIy, II, Ixt, Iyt, A11, A12, A22, B11, B12, B22) and every pass's (unew, vnew)."""
-    a, b = _f32(ls_a), _f32(ls_b)
-    u, v = _f32(us).copy(), _f32(vs).copy()
+    a, b = _real(ls_a, precision), _real(ls_b, precision)
+    u, v = _real(us, precision).copy(), _real(vs, precision).copy()
     h, w = a.shape
-    fixed = np.zeros((12, h, w), np.float32) if intermediates else None
-    un = np.zeros((iterations, h, w), np.float32) if intermediates else None
-    vn = np.zeros((iterations, h, w), np.float32) if intermediates else None
-    passes = lib().orc_liu_shen(_ptr(a, ctypes.c_float), _ptr(b, ctypes.c_float), h, w, _ptr(u, ctypes.c_float),
-                                _ptr(v, ctypes.c_float), lam, iterations, int(half_pixel),
-                                fixed.ctypes.data if fixed is not None else None,
-                                un.ctypes.data if un is not None else None,
-                                vn.ctypes.data if vn is not None else None)
+    dt = a.dtype
+    fixed = np.zeros((12, h, w), dt) if intermediates else None
+    un = np.zeros((iterations, h, w), dt) if intermediates else None
+    vn = np.zeros((iterations, h, w), dt) if intermediates else None
+    lam_c = ctypes.c_float(lam) if precision == 32 else ctypes.c_double(lam)
+    passes = _fn("orc_liu_shen", precision)(_rptr(a), _rptr(b), h, w, _rptr(u), _rptr(v), lam_c, iterations,
+                                            int(half_pixel), fixed.ctypes.data if fixed is not None else None,
+                                            un.ctypes.data if un is not None else None,
+                                            vn.ctypes.data if vn is not None else None)
     if intermediates:
         return u, v, passes, fixed, un, vn
     return u, v
@@ -577,22 +593,24 @@ def liu_shen(ls_a, ls_b, us, vs, lam, iterations, half_pixel=False, intermediate
 
 def flow_after_piv(img_a, img_b, n, tops, lefts, tu, tv, mode=2, sigma_lk=2.0, px_lk=3, sigma_ls=0.48, px_ls=5,
                    window=27, iterations_lk=5, lam=4.0, iterations_ls=60, dense_export=True, ignore_piv=0,
-                   pyramid_levels=0):
+                   pyramid_levels=0, precision=32):
     """Optical flow after PIV on the last step's tile grid: returns updated tile (u, v)
-    (rows, columns) and the dense field (rows, columns).  ignore_piv: 0 none, 1 IgnoreU,
-    2 IgnoreV, 3 IgnoreUV, 4 Auto, 5 AutoSmall."""
+    (rows, columns) and the dense field (rows, columns; float64 for precision=64, the FP64
+    twin).  ignore_piv: 0 none, 1 IgnoreU, 2 IgnoreV, 3 IgnoreUV, 4 Auto, 5 AutoSmall."""
     a, b = _f32(img_a), _f32(img_b)
     h, w = a.shape
     tops = np.ascontiguousarray(tops, np.int32)
     lefts = np.ascontiguousarray(lefts, np.int32)
     u = np.array(tu, np.float32, order="C", copy=True)
     v = np.array(tv, np.float32, order="C", copy=True)
-    du = np.zeros((h, w), np.float32)
-    dv = np.zeros((h, w), np.float32)
-    lib().orc_flow_after_piv(_ptr(a, ctypes.c_float), _ptr(b, ctypes.c_float), h, w, n, len(tops), len(lefts),
-                             _ptr(tops, ctypes.c_int), _ptr(lefts, ctypes.c_int), _ptr(u, ctypes.c_float),
-                             _ptr(v, ctypes.c_float), mode, sigma_lk, px_lk, sigma_ls, px_ls, window, iterations_lk,
-                             lam, iterations_ls, int(dense_export), int(ignore_piv), int(pyramid_levels),
-                             du.ctypes.data, dv.ctypes.data)
+    dt = np.float32 if precision == 32 else np.float64
+    du = np.zeros((h, w), dt)
+    dv = np.zeros((h, w), dt)
+    _fn("orc_flow_after_piv", precision)(_ptr(a, ctypes.c_float), _ptr(b, ctypes.c_float), h, w, n, len(tops),
+                                         len(lefts), _ptr(tops, ctypes.c_int), _ptr(lefts, ctypes.c_int),
+                                         _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), mode, sigma_lk, px_lk,
+                                         sigma_ls, px_ls, window, iterations_lk, lam, iterations_ls,
+                                         int(dense_export), int(ignore_piv), int(pyramid_levels), du.ctypes.data,
+                                         dv.ctypes.data)
     return u, v, du, dv
 

@@ -316,8 +316,22 @@ NOALLOC_MAX_ROWS = 524288
 
 def inherit_noalloc(device, stream, p_ci, p_cj, pu, pv, c_ci, c_cj, cu, cv, pni, pnj, cni, cnj, round_int=False):
     """qlpiv_inherit_noalloc: every array a device buffer (torch tensor or address);
-    queued on `stream` (cudaStream_t as int, 0 = legacy default stream)."""
-    a = [x if isinstance(x, int) else _addr(x) for x in (p_ci, p_cj, pu, pv, c_ci, c_cj, cu, cv)]
+    queued on `stream` (cudaStream_t as int, 0 = legacy default stream).  Tensors are checked
+    (CUDA, on `device`, float32, contiguous, sized for the grids) before the call; raw
+    addresses are the caller's responsibility."""
+    args = (p_ci, p_cj, pu, pv, c_ci, c_cj, cu, cv)
+    sizes = (pni, pnj, pni * pnj, pni * pnj, cni, cnj, cni * cnj, cni * cnj)
+    names = ("p_ci", "p_cj", "pu", "pv", "c_ci", "c_cj", "cu", "cv")
+    for x, size, name in zip(args, sizes, names):
+        if isinstance(x, int):
+            continue
+        if not getattr(x, "is_cuda", False) or x.device.index != device:
+            raise ValueError(f"{name} must be a CUDA tensor on device {device}")
+        if str(x.dtype) != "torch.float32" or not x.is_contiguous():
+            raise ValueError(f"{name} must be a contiguous float32 tensor")
+        if x.numel() != size:
+            raise ValueError(f"{name} has {x.numel()} elements, the grids need {size}")
+    a = [x if isinstance(x, int) else _addr(x) for x in args]
     _check(load_library().qlpiv_inherit_noalloc(device, stream or None, pni, pnj, a[0], a[1], a[2], a[3], cni, cnj,
                                                 a[4], a[5], int(round_int), a[6], a[7]))
 

@@ -58,6 +58,7 @@ IaJob group_job(const qlpiv_mixed_plan *p, const Group &g) {
     const int32_t *w = g.work.as<int32_t>();
     job.frames = p->frames.as<qlpiv_frame>();
     job.frame_idx = w;
+    job.num_frames = p->num_pairs;
     job.a_top = job.b_top = w + g.count;
     job.a_left = job.b_left = w + 2 * g.count;
     job.count = g.count;

@@ -236,12 +236,13 @@ qlpiv_status check_batch(qlpiv_handle *h, const qlpiv_pass_desc *desc, int pixel
     return QLPIV_OK;
 }
 
-qlpiv::IaJob batch_job(const qlpiv_pass_desc *desc, const qlpiv_frame *frames_dev, long count, const int32_t *fi,
-                       const int32_t *at, const int32_t *al, const int32_t *bt, const int32_t *bl,
+qlpiv::IaJob batch_job(const qlpiv_pass_desc *desc, const qlpiv_frame *frames_dev, int num_frames, long count,
+                       const int32_t *fi, const int32_t *at, const int32_t *al, const int32_t *bt, const int32_t *bl,
                        qlpiv_vector *out) {
     qlpiv::IaJob job = frame_job(desc, nullptr, nullptr, 0, 0, count, at, al, bt, bl, out);
     job.frames = frames_dev;
     job.frame_idx = fi;
+    job.num_frames = num_frames;
     return job;
 }
 
@@ -405,6 +406,9 @@ qlpiv_status qlpiv_pass_batch(qlpiv_handle *h, const qlpiv_pass_desc *desc, int 
     qlpiv_status st = check_batch(h, desc, pixel_type, num_frames, frames, count, frame_of_ia, a_top, a_left, b_top,
                                   b_left, out);
     if (st != QLPIV_OK || count == 0) return st;
+    for (long k = 0; k < count; k++)
+        if (frame_of_ia[k] < 0 || frame_of_ia[k] >= num_frames)
+            return fail(QLPIV_E_ARG, "frame_of_ia[%ld] = %d is outside [0, %d)", k, frame_of_ia[k], num_frames);
     const size_t pb = qlpiv::pixel_bytes(pixel_type);
     size_t total = 0;
     for (int f = 0; f < num_frames; f++) {
@@ -448,7 +452,8 @@ qlpiv_status qlpiv_pass_batch(qlpiv_handle *h, const qlpiv_pass_desc *desc, int 
     if ((e = cudaMemcpyAsync(h->frames.p, dev_frames.data(), sizeof(qlpiv_frame) * num_frames,
                              cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
         return cuda_fail(e, "frame table upload");
-    qlpiv::IaJob job = batch_job(desc, (const qlpiv_frame *)h->frames.p, count, org, org + count, org + 2 * count,
+    qlpiv::IaJob job = batch_job(desc, (const qlpiv_frame *)h->frames.p, num_frames, count, org, org + count,
+                                 org + 2 * count,
                                  org + 3 * count, org + 4 * count, (qlpiv_vector *)h->vectors.p);
     if ((st = launch(h, job, desc->n, pixel_type)) != QLPIV_OK) return st;
     if ((e = cudaMemcpyAsync(out, h->vectors.p, sizeof(qlpiv_vector) * count * vectors_per_ia(desc),
@@ -469,7 +474,7 @@ qlpiv_status qlpiv_pass_batch_device(qlpiv_handle *h, const qlpiv_pass_desc *des
     std::lock_guard<std::mutex> lock(h->mu);
     DeviceScope ds(h->device);
     if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
-    qlpiv::IaJob job = batch_job(desc, frames, count, frame_of_ia, a_top, a_left, b_top, b_left, out);
+    qlpiv::IaJob job = batch_job(desc, frames, num_frames, count, frame_of_ia, a_top, a_left, b_top, b_left, out);
     return launch(h, job, desc->n, pixel_type);
 }
 

@@ -12,6 +12,7 @@
 //         :132-181), margins (struct top, left, bottom, right) and u, v (single,
 //         tiles_i x tiles_j x frames, MATLAB column-major order); uncompressed elements.
 #include <algorithm>
+#include <new>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -306,30 +307,46 @@ extern "C" {
 
 qlpiv_status qlpiv_tiff_info(const char *path, int *height, int *width, int *bits_per_sample) {
     if (!path || !height || !width || !bits_per_sample) return fail(QLPIV_E_ARG, "NULL argument");
-    std::vector<uint8_t> b;
-    if (!read_file(path, b)) return fail(QLPIV_E_ARG, "cannot read %s", path);
-    Tiff t;
-    if (qlpiv_status st = parse_tiff(b, t)) return st;
-    *height = t.height;
-    *width = t.width;
-    *bits_per_sample = t.bps;
-    return QLPIV_OK;
+    try {
+        std::vector<uint8_t> b;
+        if (!read_file(path, b)) return fail(QLPIV_E_ARG, "cannot read %s", path);
+        Tiff t;
+        if (qlpiv_status st = parse_tiff(b, t)) return st;
+        *height = t.height;
+        *width = t.width;
+        *bits_per_sample = t.bps;
+        return QLPIV_OK;
+    } catch (const std::bad_alloc &) {
+        return fail(QLPIV_E_OOM, "host memory exhausted while reading %s", path);
+    }
 }
 
 qlpiv_status qlpiv_tiff_read(const char *path, void *pixels, int64_t capacity_bytes) {
     if (!path || !pixels) return fail(QLPIV_E_ARG, "NULL argument");
-    std::vector<uint8_t> b;
-    if (!read_file(path, b)) return fail(QLPIV_E_ARG, "cannot read %s", path);
-    Tiff t;
-    if (qlpiv_status st = parse_tiff(b, t)) return st;
-    const int64_t need = (int64_t)t.width * t.height * (t.bps / 8);
-    if (capacity_bytes < need) return fail(QLPIV_E_ARG, "buffer of %lld bytes, image needs %lld",
-                                          (long long)capacity_bytes, (long long)need);
-    return decode_tiff(b, t, static_cast<uint8_t *>(pixels));
+    // host allocations (file bytes, decoded strips) can fail on a hostile header: report
+    // QLPIV_E_OOM instead of letting std::bad_alloc leave an extern "C" function
+    try {
+        std::vector<uint8_t> b;
+        if (!read_file(path, b)) return fail(QLPIV_E_ARG, "cannot read %s", path);
+        Tiff t;
+        if (qlpiv_status st = parse_tiff(b, t)) return st;
+        const int64_t need = (int64_t)t.width * t.height * (t.bps / 8);
+        if (capacity_bytes < need) return fail(QLPIV_E_ARG, "buffer of %lld bytes, image needs %lld",
+                                              (long long)capacity_bytes, (long long)need);
+        // no strip can expand more than an LZW stream (at most 4096 bytes per 9-bit code)
+        int64_t strip_bytes = 0;
+        for (size_t s = 0; s < t.counts.size(); s++) strip_bytes += (int64_t)t.counts[s];
+        if (need > strip_bytes * 4096 + 4096)
+            return fail(QLPIV_E_SHAPE, "image of %lld bytes cannot come from %lld bytes of strips", (long long)need,
+                        (long long)strip_bytes);
+        return decode_tiff(b, t, static_cast<uint8_t *>(pixels));
+    } catch (const std::bad_alloc &) {
+        return fail(QLPIV_E_OOM, "host memory exhausted while decoding %s", path);
+    }
 }
 
-qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *p, int num_maps,
-                              const qlpiv_mat_velocity_map *maps) {
+static qlpiv_status mat_export_body(const char *path, const qlpiv_mat_export_params *p, int num_maps,
+                                    const qlpiv_mat_velocity_map *maps) {
     if (!path || !p || (num_maps > 0 && !maps)) return fail(QLPIV_E_ARG, "NULL argument");
     if (num_maps < 0 || p->frames <= 0) return fail(QLPIV_E_ARG, "num_maps < 0 or frames <= 0");
     if (p->layout != QLPIV_MAT_RUN && p->layout != QLPIV_MAT_STEP && p->layout != QLPIV_MAT_DENSE)
@@ -434,6 +451,15 @@ qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *p
     const int closed = std::fclose(f);
     if (wrote != out.b.size() || closed != 0) return fail(QLPIV_E_ARG, "short write to %s", path);
     return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_mat_export(const char *path, const qlpiv_mat_export_params *p, int num_maps,
+                              const qlpiv_mat_velocity_map *maps) {
+    try {
+        return mat_export_body(path, p, num_maps, maps);
+    } catch (const std::bad_alloc &) {
+        return fail(QLPIV_E_OOM, "host memory exhausted while building the MAT file");
+    }
 }
 
 }  // extern "C"

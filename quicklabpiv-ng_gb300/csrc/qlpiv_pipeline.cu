@@ -460,6 +460,7 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
         IaJob job{};
         job.frames = src;
         job.frame_idx = L.d_fi.as<int>();
+        job.num_frames = pairs;
         job.a_top = L.d_at.as<int>();
         job.a_left = L.d_al.as<int>();
         job.b_top = bt;

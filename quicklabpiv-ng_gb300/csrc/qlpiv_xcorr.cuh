@@ -110,6 +110,8 @@ struct IaJob {
     int h, w;
     const qlpiv_frame *frames;   // batched: per-IA frame table entry (NULL: img_a/img_b)
     const int *frame_idx;
+    int num_frames;              // entries of `frames`: an IA whose index is outside [0, num_frames)
+                                 // correlates two empty tiles instead of reading past the table
     const int *a_top, *a_left, *b_top, *b_left;  // per IA origins
     const float *max_a, *max_b;  // per IA maxima (max_mode == QLPIV_MAX_GIVEN)
     long count;
@@ -699,7 +701,8 @@ xcorr_kernel(IaJob job) {
         long pitch_a, pitch_b;
         int img_h, img_w;
         if (job.frames != nullptr) {
-            const qlpiv_frame fr = job.frames[job.frame_idx[ia]];
+            const int fi = job.frame_idx[ia];
+            const qlpiv_frame fr = (unsigned)fi < (unsigned)job.num_frames ? job.frames[fi] : qlpiv_frame{};
             imgA = reinterpret_cast<const Pix *>(fr.img_a);
             imgB = reinterpret_cast<const Pix *>(fr.img_b);
             pitch_a = pitch_b = (long)fr.pitch;

@@ -145,7 +145,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
         long pitch_a, pitch_b;
         int img_h, img_w;
         if (job.frames != nullptr) {
-            const qlpiv_frame fr = job.frames[job.frame_idx[ia]];
+            const int fi = job.frame_idx[ia];
+            const qlpiv_frame fr = (unsigned)fi < (unsigned)job.num_frames ? job.frames[fi] : qlpiv_frame{};
             imgA = reinterpret_cast<const Pix *>(fr.img_a);
             imgB = reinterpret_cast<const Pix *>(fr.img_b);
             pitch_a = pitch_b = (long)fr.pitch;

@@ -79,15 +79,20 @@ def particle_pair(shape, flow, ppp=0.02, diam=3.0, diam_sd=0.5, noise=3.0, bits=
     return out[0], out[1]
 
 
-def config1_pair(seed=1):
+def config1_pair(seed=1, pair_id=0):
     """512x512 u8, 0.02 ppp, d = 3 +- 0.5, Rankine r_c = 64 max 4 px, noise 3."""
     return particle_pair((512, 512), Flow(vmax=4.0, rc=64.0), ppp=0.02, diam=3.0, diam_sd=0.5, noise=3.0, bits=8,
-                         seed=seed)
+                         seed=seed, pair_id=pair_id)
+
+
+def config2_flow():
+    """Shear 0.005 px/px plus a Rankine vortex, at most 6 px over a 1024x1024 frame."""
+    return Flow(vmax=6.0 - 0.005 * 512, rc=96.0, shear=0.005)
 
 
 def config2_pair(seed=2, pair_id=0):
     """1024x1024 12-bit in u16, 0.03 ppp, d = 2.5, shear 0.005 + Rankine, max 6 px."""
-    return particle_pair((1024, 1024), Flow(vmax=6.0 - 0.005 * 512, rc=96.0, shear=0.005), ppp=0.03, diam=2.5,
+    return particle_pair((1024, 1024), config2_flow(), ppp=0.03, diam=2.5,
                          diam_sd=0.0, noise=3.0, bits=12, seed=seed, pair_id=pair_id)
 
 

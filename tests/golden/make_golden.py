@@ -32,6 +32,7 @@ Fixtures written (all from files shipped in the reference project):
                        constant quadrants), compressed bytes kept verbatim.
 """
 import struct
+import os
 import sys
 import zlib
 from pathlib import Path
@@ -328,4 +329,8 @@ if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "--tiff-only":
         tiff_fixtures(sys.argv[1])
         sys.exit(0)
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("QLPIV_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <QuickLabPIV-ng checkout> [--gauss-kat-only | --tiff-only] "
+                 "(or set QLPIV_REFERENCE)")
+    main(ref)

@@ -11,6 +11,8 @@ import pytest
 
 from conftest import load_package
 
+import adaptive_trace
+
 pytestmark = pytest.mark.gpu
 
 
@@ -115,7 +117,8 @@ def test_adaptive_first_second_image_warping(qp, handle, oracle, mode, bits):
         for prec in (32, 64):
             ou, ov = oracle.piv_adaptive(a, b, 64, 16, 0.5, fixed_max=fm, precision=prec, warp=mode)
             err = np.maximum(np.abs(u[k] - ou), np.abs(v[k] - ov))
-            assert np.mean(err <= 1e-3) >= 0.97, (k, prec, float(np.mean(err <= 1e-3)))
+            assert np.mean(err <= 1e-3) >= 0.995 and err.max() <= 5e-3, (k, prec, float(np.mean(err <= 1e-3)),
+                                                                          float(err.max()))
     pu, pv = qp.per_call.piv_adaptive_per_call(handle, pairs[0][0], pairs[0][1], desc)
     assert pu.tobytes() == u[0].tobytes() and pv.tobytes() == v[0].tobytes()
 
@@ -144,10 +147,19 @@ def test_adaptive_pipeline_matches_fp64_oracle(qp, handle, oracle, bits, warp, t
     g = qp.grid.superposition(h, w, 64, 2, 0.25)
     assert u.shape == (3, g.tiles_i, g.tiles_j)
     for k, (a, b) in enumerate(pairs):
-        ou, ov = oracle.piv_adaptive(a, b, 64, 16, 0.25, fixed_max=fixed or None, precision=64, warp=warp)
-        err = np.maximum(np.abs(u[k] - ou), np.abs(v[k] - ov))
-        # tiles downstream of a tie or a rounding-boundary pixel may differ; they must be rare
-        assert np.mean(err <= 1e-3) >= 0.99, (k, float(np.mean(err <= 1e-3)), float(err.max()))
+        # every stage, fed the GPU's own inputs, within the criteria (ties excepted)
+        recs = adaptive_trace.gpu_trace(qp, handle, a, b, desc)
+        assert recs[-1]["u"].tobytes() == u[k].tobytes() and recs[-1]["v"].tobytes() == v[k].tobytes()
+        adaptive_trace.check_stages(qp, oracle, recs, desc)
+        # end to end against the FP64 pipeline run from the raw frames: every vector beyond
+        # 1e-3 px has a cause upstream of its last correlation (its inherited value or a pixel
+        # of its warped tiles differs, or an exact tie); the stages' in-tolerance differences
+        # add up over the levels (the reference's own FP32 path drifts the same way)
+        olv = adaptive_trace.oracle_levels(oracle, a, b, recs, desc, (64, 16, 0.25), fixed_max=fixed or None,
+                                           warp=warp)
+        rep = adaptive_trace.cascade_report(recs, olv, desc)
+        assert all(r["causes"]["unexplained"] == 0 for r in rep), rep
+        assert rep[-1]["over_tol"] <= 0.005 * rep[-1]["vectors"], rep
         if bits == 8 or tile_max == "tile":
             tr, tc = _true_flow(qp, flow, g, (h, w))
             assert np.median(np.hypot(u[k] - tr, v[k] - tc)) < 0.15
@@ -185,6 +197,11 @@ def test_adaptive_from_ia128(qp, handle, oracle, warp):
                             max_mode=qp.MAX_FIXED if warp else qp.MAX_COMPUTE, fixed_max=255.0 if warp else 0.0)
     u, v = handle.piv_adaptive([p[0] for p in pairs], [p[1] for p in pairs], desc)
     for k, (a, b) in enumerate(pairs):
-        ou, ov = oracle.piv_adaptive(a, b, 128, 32, 0.5, fixed_max=255.0 if warp else None, precision=64, warp=warp)
-        err = np.maximum(np.abs(u[k] - ou), np.abs(v[k] - ov))
-        assert np.mean(err <= 1e-3) >= 0.99, (k, float(np.mean(err <= 1e-3)), float(err.max()))
+        recs = adaptive_trace.gpu_trace(qp, handle, a, b, desc)
+        assert recs[-1]["u"].tobytes() == u[k].tobytes() and recs[-1]["v"].tobytes() == v[k].tobytes()
+        adaptive_trace.check_stages(qp, oracle, recs, desc)
+        olv = adaptive_trace.oracle_levels(oracle, a, b, recs, desc, (128, 32, 0.5),
+                                           fixed_max=255.0 if warp else None, warp=warp)
+        rep = adaptive_trace.cascade_report(recs, olv, desc)
+        assert all(r["causes"]["unexplained"] == 0 for r in rep), rep
+        assert rep[-1]["over_tol"] <= 0.005 * rep[-1]["vectors"], rep

@@ -105,7 +105,8 @@ def test_adaptive_pipeline_with_inheritance_mode(qp, handle, oracle, mode, warp,
         ou, ov = oracle.piv_adaptive(a, b, 64, 16, 0.5 if warp else 0.25, fixed_max=fm if warp else None,
                                      precision=32, warp=warp, inherit=mode)
         err = np.maximum(np.abs(u[k] - ou), np.abs(v[k] - ov))
-        assert np.mean(err <= 1e-3) >= 0.97, (k, float(np.mean(err <= 1e-3)))
+        assert np.mean(err <= 1e-3) >= 0.995 and err.max() <= 5e-3, (k, float(np.mean(err <= 1e-3)),
+                                                                      float(err.max()))
     pu, pv = qp.per_call.piv_adaptive_per_call(handle, pairs[0][0], pairs[0][1], desc)
     assert pu.tobytes() == u[0].tobytes() and pv.tobytes() == v[0].tobytes()
 

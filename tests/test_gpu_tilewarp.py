@@ -75,10 +75,11 @@ def test_adaptive_pipeline_micro_mini(qp, handle, oracle, mode, bits):
     for k, (a, b) in enumerate(pairs):
         ou, ov = oracle.piv_adaptive(a, b, 64, 16, 0.5, fixed_max=fm, precision=32, warp=mode)
         err = np.maximum(np.abs(u[k] - ou), np.abs(v[k] - ov))
-        assert np.mean(err <= 1e-3) >= 0.97, (k, float(np.mean(err <= 1e-3)))
+        assert np.mean(err <= 1e-3) >= 0.995 and err.max() <= 5e-3, (k, float(np.mean(err <= 1e-3)),
+                                                                      float(err.max()))
         o64u, o64v = oracle.piv_adaptive(a, b, 64, 16, 0.5, fixed_max=fm, precision=64, warp=mode)
         err64 = np.maximum(np.abs(u[k] - o64u), np.abs(v[k] - o64v))
-        assert np.mean(err64 <= 1e-3) >= 0.97
+        assert np.mean(err64 <= 1e-3) >= 0.995 and err64.max() <= 5e-3
     # the per-call path drives the same stages one call at a time
     pu, pv = qp.per_call.piv_adaptive_per_call(handle, pairs[0][0], pairs[0][1], desc)
     assert pu.tobytes() == u[0].tobytes() and pv.tobytes() == v[0].tobytes()

@@ -214,3 +214,34 @@ def test_server_without_gpu_reports_no_device(qp):
     with pytest.raises(qp.QlpivError) as e:
         qp.Server(0)
     assert e.value.status == qp.E_NO_DEVICE
+
+
+@pytest.mark.parametrize("bad", [-1, 2])
+def test_batch_pass_rejects_frame_index_outside_table(qp, bad):
+    """qlpiv_pass_batch checks every IA's frame index against the frame table before it touches
+    the handle or the device (a bad index would otherwise make the kernel read past the
+    table).  The handle here is an opaque placeholder: the call returns before using it."""
+    import ctypes
+    lib = qp.load_library()
+    a = np.zeros((64, 64), np.uint8)
+    table = (qp.Frame * 2)(qp.Frame(a.ctypes.data, a.ctypes.data, 64, 64, 64),
+                           qp.Frame(a.ctypes.data, a.ctypes.data, 64, 64, 64))
+    fi = np.array([0, 1, bad, 0], np.int32)
+    org = np.zeros(4, np.int32)
+    out = np.empty(4, qp.VECTOR_DTYPE)
+    placeholder = ctypes.create_string_buffer(64)
+    d = qp.Handle.desc(32)
+    st = lib.qlpiv_pass_batch(ctypes.cast(placeholder, ctypes.c_void_p), ctypes.byref(d), qp.PIX_U8, 2, table, 4,
+                              fi.ctypes.data, org.ctypes.data, org.ctypes.data, org.ctypes.data, org.ctypes.data,
+                              out.ctypes.data)
+    assert st == 1   # QLPIV_E_ARG
+    assert b"frame_of_ia[2]" in lib.qlpiv_last_error()
+
+
+def test_inherit_noalloc_checks_tensors_before_the_call(qp):
+    """The Python wrapper of the allocation-free inheritance refuses host tensors and
+    mis-sized or non-float32 tensors before anything reaches the library."""
+    torch = pytest.importorskip("torch")
+    t = torch.zeros(16, dtype=torch.float32)
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        qp.inherit_noalloc(0, 0, t, t, t, t, t, t, t, t, 4, 4, 4, 4)

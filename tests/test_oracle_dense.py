@@ -237,3 +237,58 @@ def test_flow_after_piv_pyramid_levels(oracle):
     for x, y in zip(r0, r1):
         np.testing.assert_array_equal(x, y)
     assert not np.array_equal(r0[2], r2[2])
+
+
+# ---- the FP64 twin of the dense stages (error reference of the CUDA dense flow) ----
+
+@pytest.mark.parametrize("sigma,px,tol,which", [(2.0, 3, 4e-5, ("f1_0", "a")), (0.48, 5, 1e-4, ("f2_0", "a"))])
+def test_gauss_filter_fp64_twin_matches_reference(oracle, rankine_pair, sigma, px, tol, which):
+    name, src = which
+    img = rankine_pair[0] if src == "a" else rankine_pair[1]
+    out64 = oracle.gauss_filter(img, sigma, px, precision=64)
+    assert out64.dtype == np.float64
+    win = np.load(GOLDEN / "filter_golden.npz")
+    r0, r1, c0, c1 = win["window"]
+    assert np.abs(out64[r0:r1, c0:c1] - win[name]).max() <= tol
+    out32 = oracle.gauss_filter(img, sigma, px)
+    assert np.abs(out32 - out64).max() <= 1e-4 * max(1.0, float(np.abs(out64).max()))
+    k64 = oracle.gauss_kernel(sigma, px, precision=64)
+    assert abs(float(k64.sum()) - 1.0) < 1e-14
+
+
+@pytest.mark.parametrize("iters", [1, 5])
+def test_dense_lk_fp64_twin_matches_python_fixture(oracle, dense, iters):
+    a, b = dense["lk_imageA"], dense["lk_imageB"]
+    u0, v0 = dense[f"lk_beforeLK2nd{iters}_u"], dense[f"lk_beforeLK2nd{iters}_v"]
+    u, v = oracle.dense_lk(a, b, u0, v0, 27, iters, half_pixel=False, precision=64)
+    assert u.dtype == np.float64
+    assert np.abs(u - dense[f"lk_afterLK2nd{iters}_u"]).max() <= 6e-3
+    assert np.abs(v - dense[f"lk_afterLK2nd{iters}_v"]).max() <= 6e-3
+    u32, v32 = oracle.dense_lk(a, b, u0, v0, 27, iters, half_pixel=False)
+    assert np.sqrt(np.mean((u32 - u) ** 2 + (v32 - v) ** 2)) <= 1e-4
+
+
+def test_liu_shen_fp64_twin_matches_python_fixture(oracle, dense):
+    la, lb = dense["ls_Im1LS_Filtered"], dense["ls_Im2LS_Filtered"]
+    us, vs = dense["ls_uLK"], dense["ls_vLK"]
+    u, v, passes, fixed, un, vn = oracle.liu_shen(la, lb, us, vs, 4.0, 5, half_pixel=False, intermediates=True,
+                                                  precision=64)
+    assert passes == 5 and fixed.dtype == np.float64
+    for q, name in enumerate(["cmtx", "IIx", "IIy", "II", "Ixt", "Iyt", "A11", "A12", "A22", "B11", "B12", "B22"]):
+        assert np.abs(fixed[q] - dense[f"ls_{name}"]).max() <= 1e-5, name
+    for k in range(5):
+        assert np.abs(un[k] - dense[f"ls_unews{k}"]).max() <= 1e-3, k
+        assert np.abs(vn[k] - dense[f"ls_vnews{k}"]).max() <= 1e-3, k
+
+
+@pytest.mark.parametrize("mode,dense_export,levels", [(1, False, 0), (2, True, 2)])
+def test_flow_after_piv_fp64_twin_close_to_float(oracle, mode, dense_export, levels):
+    """The float path (the reference's arithmetic) stays within 1e-4 px RMS of its FP64 twin."""
+    n = 16
+    a, b, tops, lefts, tu, tv = _flow_case(oracle, n=n)
+    kw = dict(mode=mode, iterations_ls=12, dense_export=dense_export, pyramid_levels=levels)
+    u, v, du, dv = oracle.flow_after_piv(a, b, n, tops, lefts, tu, tv, **kw)
+    u64, v64, du64, dv64 = oracle.flow_after_piv(a, b, n, tops, lefts, tu, tv, precision=64, **kw)
+    assert du64.dtype == np.float64 and u64.dtype == np.float32
+    assert np.sqrt(np.mean((du - du64) ** 2 + (dv - dv64) ** 2)) <= 1e-4
+    assert np.abs(du - du64).max() > 0.0      # a separate double-precision run, not the float path
