@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define QLPIV_ABI_VERSION 3
+#define QLPIV_ABI_VERSION 4
 
 /* Status codes.  The Java shim maps QLPIV_E_SHAPE/QLPIV_E_ARG to JobAnalyzeException
  * (S/jobs/xcorr/CrossCorrelationFFTTemplate.java:594-642 shape checks) and the others
@@ -184,24 +184,55 @@ typedef struct qlpiv_adaptive_desc {
     int validation;        /* qlpiv_validation: vector validation after every level */
     int num_peaks;         /* QLPIV_VALIDATE_MULTIPEAK_MEDIAN: peaks per IA = strategies */
     int peak_kernel;       /* FindMaximumMultiPeaks cell width */
-    float median_threshold;   /* NormalizedMedianValidator distance threshold */
+    float median_threshold;   /* NormalizedMedianValidator / DifferenceValidator distance threshold */
     float median_epsilon0;    /* NormalizedMedianValidator epsilon0 */
     int max_correction_iterations;      /* VectorValidatorConfiguration */
     int iterate_until_no_corrections;   /* VectorValidatorConfiguration */
     int subpix_pixels;     /* as qlpiv_pass_desc */
     int subpix_iterations; /* as qlpiv_pass_desc */
     int inherit_mode;      /* qlpiv_inherit_mode (getVelocityInheritanceStrategy) */
-    int reserved[2];
+    int clipping_mode;     /* qlpiv_clipping (PIVInputParameters.getClippingMode) */
+    int reserved[1];
 } qlpiv_adaptive_desc;
 
-/* Vector validation after each level (VectorValidatorJob, S/jobs/validator/VectorValidatorJob.java:242-405). */
+/* ClippingModeEnum (S/ClippingModeEnum.java:9-13).  Under QLPIV_CLIP_NO_OUT_OF_BOUND every
+ * displacement update of a tile -- inheritance, the correlation increment, a validation
+ * replacement, the zeroing of still-invalid vectors, the optical-flow tile replacement -- is
+ * refused when the tile of side n at (top, left), moved by the rounded displacement
+ * (FastMath.round), would leave the image by the reference's test: top + round(u) < 0,
+ * top + n + round(u) >= height, or the same for columns (Tile.accumulateDisplacement /
+ * replaceDisplacement, S/iareas/Tile.java:103-136,156-189).  A refused correlation increment is
+ * dropped; a refused replacement leaves the displacement as it is.  The reference's throw for
+ * NoImageWarping B tiles that need clipping (S/images/NoImageWarpingStrategy.java:48-70) cannot
+ * trigger then: the refusals keep every displaced tile inside the image.  LOGGED behaves as
+ * ALLOWED (the reference only logs). */
+typedef enum {
+    QLPIV_CLIP_ALLOWED = 0,           /* AllowedOutOfBoundClipping (the converter's default) */
+    QLPIV_CLIP_LOGGED = 1,            /* LoggedOutOfBoundClipping */
+    QLPIV_CLIP_NO_OUT_OF_BOUND = 2    /* NoOutOfBoundClipping */
+} qlpiv_clipping;
+
+/* Vector validation after each level (VectorValidatorJob, S/jobs/validator/VectorValidatorJob.java:242-405),
+ * the five models the converter builds (PIVConfigurationConverterVisitor.visit,
+ * ui/src/main/java/pt/quickLabPIV/business/transfer/PIVConfigurationConverterVisitor.java:546-641).
+ * Still-invalid vectors are set to 0 in every model. */
 typedef enum {
     QLPIV_VALIDATE_NONE = 0,
     /* VelocityValidationOptionsMultiPeakNormalizedMedianModel: FindMaximumMultiPeaks with
      * num_peaks peaks, strategies 0..k-2 = normalised median + SecondaryPeakReplacement of
-     * peak s+1, strategy k-1 = normalised median + BilinearReplacement; still-invalid
-     * vectors are set to 0 (PIVConfigurationConverterVisitor.visit, multi-peak model). */
-    QLPIV_VALIDATE_MULTIPEAK_MEDIAN = 1
+     * peak s+1, strategy k-1 = normalised median + BilinearReplacement. */
+    QLPIV_VALIDATE_MULTIPEAK_MEDIAN = 1,
+    /* The four single-strategy models, all with FindMaximumFromCenter peaks:
+     * DifferenceValidator (S/iareas/validation/DifferenceValidator.java:30-60; distance
+     * threshold median_threshold px) without / with BilinearReplacement, and
+     * NormalizedMedianValidator without / with BilinearReplacement.  The difference validator
+     * compares a tile only with its valid top-left, top and left neighbours, and every tile
+     * starts invalid, so in the reference it never validates a vector: these two models set
+     * every vector to 0 (subject to the clipping mode), and so does this library. */
+    QLPIV_VALIDATE_DIFFERENCE_ONLY = 2,
+    QLPIV_VALIDATE_DIFFERENCE = 3,
+    QLPIV_VALIDATE_MEDIAN_ONLY = 4,
+    QLPIV_VALIDATE_MEDIAN = 5
 } qlpiv_validation;
 
 typedef struct qlpiv_params {
@@ -372,6 +403,16 @@ qlpiv_status qlpiv_validate(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, in
                             const int32_t *lefts, float *u, float *v, const float *peak_u, const float *peak_v,
                             const int32_t *npeaks, uint8_t *invalid_out);
 
+/* qlpiv_validate for any desc->validation model, with the tile side n and the image size the
+ * clipping mode needs (desc->clipping_mode; qlpiv_validate itself refuses
+ * QLPIV_CLIP_NO_OUT_OF_BOUND).  peak_u / peak_v / npeaks are read by the multi-peak model only
+ * and may be NULL for the others (k = 1 strategy).  VectorValidatorJob.compute with the
+ * replacements' Tile.replaceDisplacement bounds (S/iareas/Tile.java:156-189). */
+qlpiv_status qlpiv_validate_tiles(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int n, int height, int width,
+                                  int ni, int nj, const int32_t *tops, const int32_t *lefts, float *u, float *v,
+                                  const float *peak_u, const float *peak_v, const int32_t *npeaks,
+                                  uint8_t *invalid_out);
+
 /* Velocity inheritance that allocates nothing (no counterpart in the reference).
  * For callers that cannot let the library allocate device memory during a call -- a
  * Java host passing device buffers from its own pool with a fixed memory budget, or an
@@ -454,7 +495,9 @@ typedef struct qlpiv_flow_desc {
                                images and of the field (halved), each level's result up-sampled
                                (nearest, doubled) as the next finer level's start.  This library's
                                own design; the reference's dense LK has no pyramid */
-    int reserved[4];
+    int clipping_mode;      /* qlpiv_clipping of the tile replacement (qlpiv_flow_after_piv; the
+                               PIV + flow entry points take the PIV descriptor's) */
+    int reserved[3];
 } qlpiv_flow_desc;
 
 /* The optical flow after PIV of one frame pair on the last adaptive step's grid (tiles of side
@@ -644,6 +687,12 @@ qlpiv_status qlpiv_measure_fp32_peak(int device, double *tflops);
 /* Instrumentation: the sub-pixel fit's float-pair logarithm beside CUDA's double log for n
  * positive normal floats (host arrays), to check its error bound on the device. */
 qlpiv_status qlpiv_probe_log(int device, const float *x, long n, double *mine, double *ref);
+
+/* Instrumentation: the IA-16 kernel's tile normalisation divides integer pixels by integer
+ * maxima with a reciprocal and one exact correction step instead of the general division; this
+ * runs it against IEEE division for every v in [0, 65535] and divisor in [1, 65535] and returns
+ * the number of quotients that differ (0 expected). */
+qlpiv_status qlpiv_probe_division(int device, int64_t *mismatches);
 
 /* Number of kernel launches issued by this handle since creation (instrumentation). */
 long qlpiv_launch_count(qlpiv_handle *h);

@@ -30,16 +30,26 @@ _lib = None
 
 
 class ValidCfg(ctypes.Structure):
-    """orc_valid_cfg: multi-peak normalised-median validation settings."""
+    """orc_valid_cfg: validation model and settings.  model 1: multi-peak normalised median
+    (num_peaks strategies); 2 / 3: difference validator without / with bilinear replacement;
+    4 / 5: normalised median without / with bilinear replacement.  clip_n / clip_h / clip_w:
+    NoOutOfBoundClipping bounds of the replacements (clip_n 0: clipping allowed)."""
     _fields_ = [("enabled", ctypes.c_int), ("num_peaks", ctypes.c_int), ("kernel_width", ctypes.c_int),
                 ("threshold", ctypes.c_float), ("epsilon0", ctypes.c_float), ("max_iterations", ctypes.c_int),
-                ("iterate_until_no_corrections", ctypes.c_int)]
+                ("iterate_until_no_corrections", ctypes.c_int), ("model", ctypes.c_int), ("clip_n", ctypes.c_int),
+                ("clip_h", ctypes.c_int), ("clip_w", ctypes.c_int)]
+
+
+MODEL_MULTIPEAK_MEDIAN, MODEL_DIFFERENCE_ONLY, MODEL_DIFFERENCE, MODEL_MEDIAN_ONLY, MODEL_MEDIAN = 1, 2, 3, 4, 5
 
 
 def valid_cfg(num_peaks=3, kernel_width=3, threshold=2.0, epsilon0=0.1, max_iterations=2,
-              iterate_until_no_corrections=False):
-    return ValidCfg(1, num_peaks, kernel_width, threshold, epsilon0, max_iterations,
-                    int(iterate_until_no_corrections))
+              iterate_until_no_corrections=False, model=MODEL_MULTIPEAK_MEDIAN, clip=None):
+    """clip: None (clipping allowed) or (tile side, image height, image width) for
+    NoOutOfBoundClipping."""
+    cn, ch, cw = clip if clip is not None else (0, 0, 0)
+    return ValidCfg(1, num_peaks if model == MODEL_MULTIPEAK_MEDIAN else 1, kernel_width, threshold, epsilon0,
+                    max_iterations, int(iterate_until_no_corrections), model, cn, ch, cw)
 
 
 def build(force=False):
@@ -100,8 +110,8 @@ def lib():
         L.orc_spiral_order.argtypes = [c_int, c_int, ip]
         L.orc_validate.argtypes = [c_int, c_int, ip, ip, fp, fp, fp, fp, ip, c_int, ctypes.POINTER(ValidCfg), vp]
         L.orc_piv_adaptive_ex.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_int,
-                                          c_float,
-                                          c_int, c_int, c_int, ctypes.POINTER(ValidCfg), fp, fp, ip, ip, vp, vp, vp]
+                                          c_int, c_float, c_int, c_int, c_int, ctypes.POINTER(ValidCfg), fp, fp, ip,
+                                          ip, vp, vp, vp]
         L.orc_inherit_tiles.argtypes = [c_int, c_int, c_int, c_int, ip, ip, fp, fp, c_int, c_int, c_int, ip, ip, c_int,
                                         fp, fp]
         L.orc_area_overlap.argtypes = [c_int, c_int, c_int, c_int, c_int, c_int, ip]
@@ -115,7 +125,7 @@ def lib():
                                                          vp]
             getattr(L, "orc_flow_after_piv" + sfx).argtypes = [fp, fp, c_int, c_int, c_int, c_int, c_int, ip, ip, fp,
                                                                fp, c_int, c_float, c_int, c_float, c_int, c_int, c_int,
-                                                               c_float, c_int, c_int, c_int, c_int, vp, vp]
+                                                               c_float, c_int, c_int, c_int, c_int, c_int, vp, vp]
             getattr(L, "orc_dense_lk_pyramid" + sfx).argtypes = [vp, vp, c_int, c_int, vp, vp, c_int, c_int, c_int,
                                                                  c_int]
         L.orc_vector_size.restype = c_int
@@ -388,9 +398,12 @@ def area_overlap(parent_top, parent_left, pn, top, left, n):
     return float(f), bool(fl.value & 1), bool(fl.value & 2), bool(fl.value & 4), bool(fl.value & 8)
 
 
+CLIP_ALLOWED, CLIP_LOGGED, CLIP_NO_OUT_OF_BOUND = 0, 1, 2
+
+
 def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MAX_A, fixed_max=None,
                  int16_quirk=False, precision=32, nthreads=None, return_levels=False, warp=True, validation=None,
-                 inherit=INHERIT_BICUBIC_SPLINE):
+                 inherit=INHERIT_BICUBIC_SPLINE, clip_mode=CLIP_ALLOWED):
     """Adaptive multi-pass PIV (warp: False none, True BothImages bilinear, or a micro / mini mode
     4..9 as WARP_*); returns (u, v) of
     the last level, shaped (tiles_i, tiles_j), and optionally all levels' vectors.
@@ -413,9 +426,10 @@ def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MA
     vec = np.zeros(total, VECTOR_DTYPE) if return_levels else None
     luv = np.zeros(2 * total, np.float32) if return_levels else None
     linv = np.zeros(total, np.uint8) if return_levels else None
-    cfg = validation if validation is not None else ValidCfg(0, 0, 0, 0.0, 0.0, 0, 0)
+    cfg = validation if validation is not None else ValidCfg(0, 0, 0, 0.0, 0.0, 0, 0, 0, 0, 0, 0)
     rc = lib().orc_piv_adaptive_ex(img_a.ctypes.data, img_b.ctypes.data, h, w, img_a.dtype.itemsize, n_start, n_end,
-                                   overlap_factor, int(warp), int(inherit), norm_mode, float(fixed_max or 0.0),
+                                   overlap_factor, int(warp), int(inherit), int(clip_mode), norm_mode,
+                                   float(fixed_max or 0.0),
                                    int(int16_quirk),
                                    0 if precision == 32 else 1, nthreads or (os.cpu_count() or 1), ctypes.byref(cfg),
                                    _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), ctypes.byref(ni),
@@ -593,7 +607,7 @@ def liu_shen(ls_a, ls_b, us, vs, lam, iterations, half_pixel=False, intermediate
 
 def flow_after_piv(img_a, img_b, n, tops, lefts, tu, tv, mode=2, sigma_lk=2.0, px_lk=3, sigma_ls=0.48, px_ls=5,
                    window=27, iterations_lk=5, lam=4.0, iterations_ls=60, dense_export=True, ignore_piv=0,
-                   pyramid_levels=0, precision=32):
+                   pyramid_levels=0, precision=32, clip_mode=CLIP_ALLOWED):
     """Optical flow after PIV on the last step's tile grid: returns updated tile (u, v)
     (rows, columns) and the dense field (rows, columns; float64 for precision=64, the FP64
     twin).  ignore_piv: 0 none, 1 IgnoreU, 2 IgnoreV, 3 IgnoreUV, 4 Auto, 5 AutoSmall."""
@@ -610,7 +624,7 @@ def flow_after_piv(img_a, img_b, n, tops, lefts, tu, tv, mode=2, sigma_lk=2.0, p
                                          len(lefts), _ptr(tops, ctypes.c_int), _ptr(lefts, ctypes.c_int),
                                          _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), mode, sigma_lk, px_lk,
                                          sigma_ls, px_ls, window, iterations_lk, lam, iterations_ls,
-                                         int(dense_export), int(ignore_piv), int(pyramid_levels), du.ctypes.data,
-                                         dv.ctypes.data)
+                                         int(dense_export), int(ignore_piv), int(pyramid_levels), int(clip_mode),
+                                         du.ctypes.data, dv.ctypes.data)
     return u, v, du, dv
 

@@ -394,11 +394,13 @@ void DFN(dense_lk_pyramid)(const REAL *A, const REAL *B, int h, int w, REAL *us,
  * top + N/2 - 1 (average of the 2x2 pixels there with dense export).  img: float copies of the
  * frames.  tu/tv: tile displacements (rows, columns), ni x nj, updated in place (rounded to float
  * in the FP64 twin); dense_u/dense_v (rows, columns) receive the dense field when non-NULL.  The
- * FP64 twin takes the filter weights unrounded and the per-pixel field in double. */
+ * FP64 twin takes the filter weights unrounded and the per-pixel field in double.  clip_mode 2:
+ * NoOutOfBoundClipping of the tile replacement (S/iareas/Tile.java:156-189). */
 void DFN(flow_after_piv)(const float *img_a, const float *img_b, int h, int w, int n, int ni, int nj,
                          const int *tops, const int *lefts, float *tu, float *tv, int mode, float sigma_lk, int px_lk,
                          float sigma_ls, int px_ls, int window, int iters_lk, float lambda, int iters_ls,
-                         int dense_export, int ignore_piv, int pyramid_levels, REAL *dense_u, REAL *dense_v) {
+                         int dense_export, int ignore_piv, int pyramid_levels, int clip_mode, REAL *dense_u,
+                         REAL *dense_v) {
     const long np = (long)h * w;
     REAL *ia = (REAL *)malloc(sizeof(REAL) * np), *ib = (REAL *)malloc(sizeof(REAL) * np);
     for (long p = 0; p < np; p++) { ia[p] = (REAL)img_a[p]; ib[p] = (REAL)img_b[p]; }
@@ -458,7 +460,10 @@ void DFN(flow_after_piv)(const float *img_a, const float *img_b, int h, int w, i
                 u = (((us[idx] + us[idx + 1]) + us[idx2]) + us[idx2 + 1]) / RC(4.0);
                 v = (((vs[idx] + vs[idx + 1]) + vs[idx2]) + vs[idx2 + 1]) / RC(4.0);
             }
-            tu[ti * nj + tj] = (float)v;   /* Tile.replaceDisplacement(v, u): rows, columns */
+            /* Tile.replaceDisplacement(v, u): rows, columns; under NoOutOfBoundClipping (clip_mode 2)
+             * refused when it moves the tile out of the image */
+            if (clip_mode == 2 && !orc_clip_ok(n, h, w, tops[ti], lefts[tj], (float)v, (float)u)) continue;
+            tu[ti * nj + tj] = (float)v;
             tv[ti * nj + tj] = (float)u;
         }
     if (dense_u) memcpy(dense_u, vs, sizeof(REAL) * np);

@@ -4,6 +4,7 @@
 #ifndef QLPIV_ORACLE_TYPES_H
 #define QLPIV_ORACLE_TYPES_H
 
+#include <math.h>
 #include <stdint.h>
 
 typedef struct {
@@ -19,18 +20,37 @@ typedef struct {
     int n, tiles_i, tiles_j, margin_top, margin_left, margin_bottom, margin_right;
 } orc_grid;
 
-/* Multi-peak normalised-median validation (VelocityValidationOptionsMultiPeakNormalizedMedianModel):
- * num_peaks k >= 1 validation strategies; strategy s < k-1 replaces by peak s+1, the last
- * one by bilinear interpolation.  enabled == 0: no validation, FindMaximumFromCenter. */
+/* Vector validation as the converter configures it (PIVConfigurationConverterVisitor.visit of the
+ * five VelocityValidationOptions models, ui/.../PIVConfigurationConverterVisitor.java:546-641):
+ *   model 0 or 1  multi-peak normalised median: num_peaks k >= 1 strategies, strategy s < k-1
+ *                 replaces by peak s+1, the last one by bilinear interpolation (FindMaximumMultiPeaks)
+ *   model 2 / 3   DifferenceValidator, no replacement / bilinear (FindMaximumFromCenter)
+ *   model 4 / 5   NormalizedMedianValidator, no replacement / bilinear (FindMaximumFromCenter)
+ * enabled == 0: no validation, FindMaximumFromCenter.  clip_n / clip_h / clip_w: tile side and
+ * image size when replacements follow NoOutOfBoundClipping (clip_n == 0: clipping allowed). */
 typedef struct {
     int enabled;
-    int num_peaks;        /* k: peaks searched per IA and validation strategies */
+    int num_peaks;        /* k: peaks searched per IA and validation strategies (model 0/1) */
     int kernel_width;     /* FindMaximumMultiPeaks cell width */
-    float threshold;      /* normalised-median distance threshold */
+    float threshold;      /* distance threshold (pixels for the difference validator) */
     float epsilon0;
     int max_iterations;
     int iterate_until_no_corrections;
+    int model;
+    int clip_n, clip_h, clip_w;
 } orc_valid_cfg;
+
+/* Tile.accumulateDisplacement / replaceDisplacement under NoOutOfBoundClipping
+ * (S/iareas/Tile.java:103-136, 156-189): a displacement (u, v) is refused when the tile of side n at
+ * (top, left), moved by the rounded displacement (FastMath.round: floor(x + 0.5f)), fails the
+ * reference's test top + ru < 0, top + n + ru >= h, left + rv < 0, left + n + rv >= w.  n == 0:
+ * clipping allowed (AllowedOutOfBoundClipping, LoggedOutOfBoundClipping), nothing refused. */
+static inline int orc_clip_ok(int n, int h, int w, int top, int left, float u, float v) {
+    if (n == 0) return 1;
+    const float ru = floorf(u + 0.5f), rv = floorf(v + 0.5f);
+    return !((float)top + ru < 0.0f || (float)(top + n) + ru >= (float)h || (float)left + rv < 0.0f ||
+             (float)(left + n) + rv >= (float)w);
+}
 
 /* Sub-pixel interpolators of qlpiv_oracle_subpix.c.  A pass's `subpix` argument packs the mode
  * (bits 0-7: 0 none, 1 Gaussian 3-point, 2 Gaussian least squares, 3 Hongwei Guo), the stencil

@@ -387,13 +387,19 @@ void orc_inherit(const double *py, int pni, const double *px, int pnj, const flo
  * Outputs the last level's displacement (u rows, v columns) and, optionally, every
  * level's vectors concatenated (level_vectors, sized by the caller). */
 int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n_start, int n_end,
-                        float overlap_factor, int warp_mode, int inherit_mode, int norm_mode, float fixed_max,
-                        int int16_quirk,
-                        int precision, int nthreads, const orc_valid_cfg *val, float *out_u, float *out_v, int *out_ni,
-                        int *out_nj, orc_vector *level_vectors, float *level_uv, unsigned char *level_invalid) {
+                        float overlap_factor, int warp_mode, int inherit_mode, int clip_mode, int norm_mode,
+                        float fixed_max, int int16_quirk, int precision, int nthreads, const orc_valid_cfg *val,
+                        float *out_u, float *out_v, int *out_ni, int *out_nj, orc_vector *level_vectors,
+                        float *level_uv, unsigned char *level_invalid) {
     const int validate = val != NULL && val->enabled;
-    const int kpk = validate ? val->num_peaks : 0;
-    if (validate && (kpk < 1 || kpk > 64 || val->kernel_width < 1)) return -2;
+    /* the multi-peak model searches num_peaks peaks (FindMaximumMultiPeaks); the other models keep
+     * FindMaximumFromCenter and one validation strategy */
+    const int multi = validate && val->model <= 1;
+    const int kpk = validate ? (multi ? val->num_peaks : 1) : 0;
+    /* ClippingModeEnum: 2 = NoOutOfBoundClipping (Tile.accumulateDisplacement / replaceDisplacement
+     * refuse displacements that move a tile out of the image) */
+    const int clip = clip_mode == 2;
+    if (validate && (kpk < 1 || kpk > 64 || (multi && val->kernel_width < 1))) return -2;
     int levels = 0;
     for (int n = n_start; n >= n_end; n >>= 1) levels++;
     const int cap = 65536;
@@ -437,6 +443,15 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
                 break;
             }
             free(pyd); free(pxd);
+            if (clip)  /* the new tiles take the inherited value through accumulateDisplacement */
+                for (int i = 0; i < ni; i++)
+                    for (int j = 0; j < nj; j++) {
+                        const size_t k = (size_t)i * nj + j;
+                        const float nu = 0.0f + cu[k], nv = 0.0f + cv[k];
+                        const int ok = orc_clip_ok(n, h, w, tops[i], lefts[j], nu, nv);
+                        cu[k] = ok ? nu : 0.0f;
+                        cv[k] = ok ? nv : 0.0f;
+                    }
             if (per_tile) {
                 wta = (float *)malloc(sizeof(float) * cnt * n * n);
                 wtb = (float *)malloc(sizeof(float) * cnt * n * n);
@@ -476,7 +491,7 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
         orc_vector *vec = (orc_vector *)malloc(sizeof(orc_vector) * cnt);
         orc_vector *mvec = NULL;
         int *npk = NULL;
-        if (validate) {
+        if (multi) {
             /* FindMaximumMultiPeaks (the finder the multi-peak validation model selects) */
             mvec = (orc_vector *)malloc(sizeof(orc_vector) * cnt * kpk);
             npk = (int *)malloc(sizeof(int) * cnt);
@@ -494,20 +509,33 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
         free(wta); free(wtb); free(wma); free(wmb);
         if (level_vectors) memcpy(level_vectors + vec_off, vec, sizeof(orc_vector) * cnt);
         for (long k = 0; k < cnt; k++) {
-            if (precision == 0) { cu[k] += vec[k].u; cv[k] += vec[k].v; }
-            else { cu[k] = (float)((double)cu[k] + vec[k].u64); cv[k] = (float)((double)cv[k] + vec[k].v64); }
+            float nu, nv;
+            if (precision == 0) { nu = cu[k] + vec[k].u; nv = cv[k] + vec[k].v; }
+            else { nu = (float)((double)cu[k] + vec[k].u64); nv = (float)((double)cv[k] + vec[k].v64); }
+            /* Tile.accumulateDisplacement drops an increment that moves the tile out of the image */
+            if (!clip || orc_clip_ok(n, h, w, tops[k / nj], lefts[k % nj], nu, nv)) { cu[k] = nu; cv[k] = nv; }
         }
         if (validate) {
             /* VectorValidatorJob after IterationStepTiles.updateDisplacementsFromMaxCrossResults
              * (S/jobs/LocalPIVOpenCLGpuJob.java:384-402) */
             float *pku = (float *)malloc(sizeof(float) * cnt * kpk), *pkv = (float *)malloc(sizeof(float) * cnt * kpk);
+            int *npk1 = NULL;
             for (long q = 0; q < cnt * kpk; q++) {
-                pku[q] = precision == 0 ? mvec[q].u : (float)mvec[q].u64;
-                pkv[q] = precision == 0 ? mvec[q].v : (float)mvec[q].v64;
+                const orc_vector *src = multi ? &mvec[q] : &vec[q];
+                pku[q] = precision == 0 ? src->u : (float)src->u64;
+                pkv[q] = precision == 0 ? src->v : (float)src->v64;
             }
-            orc_validate(ni, nj, tops, lefts, cu, cv, pku, pkv, npk, kpk, val,
+            if (!multi) {
+                npk1 = (int *)malloc(sizeof(int) * cnt);
+                for (long q = 0; q < cnt; q++) npk1[q] = 1;
+            }
+            orc_valid_cfg vc = *val;
+            vc.clip_n = clip ? n : 0;
+            vc.clip_h = clip ? h : 0;
+            vc.clip_w = clip ? w : 0;
+            orc_validate(ni, nj, tops, lefts, cu, cv, pku, pkv, multi ? npk : npk1, kpk, &vc,
                          level_invalid ? level_invalid + vec_off : NULL);
-            free(pku); free(pkv);
+            free(pku); free(pkv); free(npk1);
         }
         if (level_uv) {
             memcpy(level_uv + 2 * vec_off, cu, sizeof(float) * cnt);
@@ -535,7 +563,7 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
 int orc_piv_adaptive(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n_start, int n_end,
                      float overlap_factor, int warp_mode, int norm_mode, float fixed_max, int int16_quirk, int precision,
                      int nthreads, float *out_u, float *out_v, int *out_ni, int *out_nj, orc_vector *level_vectors) {
-    return orc_piv_adaptive_ex(img_a, img_b, h, w, pix_bytes, n_start, n_end, overlap_factor, warp_mode, 0, norm_mode,
-                               fixed_max, int16_quirk, precision, nthreads, NULL, out_u, out_v, out_ni, out_nj,
-                               level_vectors, NULL, NULL);
+    return orc_piv_adaptive_ex(img_a, img_b, h, w, pix_bytes, n_start, n_end, overlap_factor, warp_mode, 0, 0,
+                               norm_mode, fixed_max, int16_quirk, precision, nthreads, NULL, out_u, out_v, out_ni,
+                               out_nj, level_vectors, NULL, NULL);
 }

@@ -7,10 +7,14 @@
  *   SecondaryPeakReplacement.replaceVector         S/iareas/replacement/SecondaryPeakReplacement.java:41-76
  *   BilinearReplacement.replaceVector              S/iareas/replacement/BilinearReplacement.java
  *   Tile lock / backup / restore                   S/iareas/Tile.java:140-215
- * as configured by the multi-peak normalised-median model
- * (PIVConfigurationConverterVisitor.visit(VelocityValidationOptionsMultiPeakNormalizedMedianModel)):
- * strategies 0..k-2 = median validation + replacement by peak 1..k-1, strategy k-1 = median
- * validation + bilinear replacement.  No masks, AllowedOutOfBoundClipping.
+ *   DifferenceValidator.validateVector             S/iareas/validation/DifferenceValidator.java:30-60
+ * as the converter configures the five validation models
+ * (PIVConfigurationConverterVisitor.visit, ui/.../PIVConfigurationConverterVisitor.java:546-641):
+ * multi-peak normalised median (strategies 0..k-2 = median validation + replacement by peak
+ * 1..k-1, strategy k-1 = median validation + bilinear replacement), and one strategy of
+ * difference or normalised-median validation with no replacement or bilinear replacement.
+ * Every tile starts invalid (the Tile constructors, S/iareas/Tile.java:51-67).  No masks.
+ * Replacements follow the clipping mode (Tile.replaceDisplacement, S/iareas/Tile.java:156-189).
  */
 #include <float.h>
 #include <math.h>
@@ -69,7 +73,14 @@ typedef struct {
     const int *tops, *lefts;
     float *u, *v, *bu, *bv;
     unsigned char *invalid, *locked;
+    int clip_n, clip_h, clip_w;
 } vstate;
+
+/* Tile.replaceDisplacement: refused under NoOutOfBoundClipping when the rounded displacement
+ * moves the tile out of the image */
+static int replace_ok(const vstate *s, int k, float u, float v) {
+    return orc_clip_ok(s->clip_n, s->clip_h, s->clip_w, s->tops[k / s->nj], s->lefts[k % s->nj], u, v);
+}
 
 static int java_round_v(float x) { return (int)floorf(x + 0.5f); }
 
@@ -130,6 +141,25 @@ static void validate_median(vstate *s, int k, float threshold, float eps0) {
     const float du = mu - s->u[k], dv = mv - s->v[k];
     const float dist = (float)sqrt((double)(du * du + dv * dv)) / (rmed + eps0);
     set_invalid(s, k, !(dist < threshold));
+}
+
+/* DifferenceValidator.validateVector: adjacents[i][j] for i, j in {0, 1} except (1, 1) -- the
+ * top-left, top and left neighbours -- each valid one overwriting the tile's flag with the test
+ * |d|^2 < threshold^2; with no valid one among them the flag is left as it is. */
+static void validate_difference(vstate *s, int k, float threshold) {
+    const float t2 = threshold * threshold;
+    const int ti = k / s->nj, tj = k % s->nj;
+    for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++) {
+            if (a == 1 && b == 1) continue;
+            const int i = ti + a - 1, j = tj + b - 1;
+            if (i < 0 || i >= s->ni || j < 0 || j >= s->nj) continue;
+            const int q = i * s->nj + j;
+            if (s->invalid[q]) continue;
+            const float du = s->u[q] - s->u[k], dv = s->v[q] - s->v[k];
+            const float dist = du * du + dv * dv;
+            set_invalid(s, k, !(dist < t2));
+        }
 }
 
 /* BilinearReplacement.interpV / interpU: linear interpolation between two tiles along
@@ -217,7 +247,7 @@ static void replace_bilinear(vstate *s, int k) {
             }
         if (count == 0) {
             set_invalid(s, k, 1);
-        } else {
+        } else if (replace_ok(s, k, uU[0], uV[0])) {
             s->u[k] = uU[0];
             s->v[k] = uV[0];
             set_invalid(s, k, 0);
@@ -233,9 +263,11 @@ static void replace_bilinear(vstate *s, int k) {
         }
         aV /= (float)wV;
         aU /= (float)wU;
-        s->u[k] = aU;
-        s->v[k] = aV;
-        set_invalid(s, k, 0);
+        if (replace_ok(s, k, aU, aV)) {
+            s->u[k] = aU;
+            s->v[k] = aV;
+        }
+        set_invalid(s, k, 0);  /* the reference clears the flag whether or not the value was taken */
     }
 #undef OK
 #undef TOP
@@ -244,23 +276,32 @@ static void replace_bilinear(vstate *s, int k) {
 
 /* VectorValidatorJob.compute for one frame's tiles (in place on u, v).
  * pu/pv: [ni*nj][k] displacement increments of peaks 0..k-1 (0 = main peak, already
- * accumulated into u, v); npeaks: peaks found per tile.  invalid_out: final flags.
- * Returns the number of correction sweeps made. */
+ * accumulated into u, v); npeaks: peaks found per tile (multi-peak model only; may be NULL
+ * otherwise).  invalid_out: final flags.  Returns the number of correction sweeps made. */
 int orc_validate(int ni, int nj, const int *tops, const int *lefts, float *u, float *v, const float *pu,
                  const float *pv, const int *npeaks, int k, const orc_valid_cfg *cfg, unsigned char *invalid_out) {
     const int total = ni * nj;
+    const int model = cfg->model <= 1 ? 1 : cfg->model;
+    const int difference = model == 2 || model == 3;
+    /* strategies: multi-peak k (secondary peaks then bilinear); otherwise one */
+    const int nstrat = model == 1 ? cfg->num_peaks : 1;
+    const int last_bilinear = model == 1 || model == 3 || model == 5;
     vstate s;
     s.ni = ni; s.nj = nj; s.tops = tops; s.lefts = lefts; s.u = u; s.v = v;
+    s.clip_n = cfg->clip_n; s.clip_h = cfg->clip_h; s.clip_w = cfg->clip_w;
     s.bu = (float *)malloc(sizeof(float) * total);
     s.bv = (float *)malloc(sizeof(float) * total);
-    s.invalid = (unsigned char *)calloc((size_t)total, 1);
+    s.invalid = (unsigned char *)malloc((size_t)total);
+    memset(s.invalid, 1, (size_t)total);   /* new tiles are invalid until validated */
     s.locked = (unsigned char *)calloc((size_t)total, 1);
     int *order = (int *)malloc(sizeof(int) * total);
     orc_spiral_order(ni, nj, order);
     for (int t = 0; t < total; t++) { s.bu[t] = u[t]; s.bv[t] = v[t]; }
+#define VALIDATE(t) (difference ? validate_difference(&s, (t), cfg->threshold) \
+                                : validate_median(&s, (t), cfg->threshold, cfg->epsilon0))
     for (int q = 0; q < total; q++) {
         const int t = order[q];
-        validate_median(&s, t, cfg->threshold, cfg->epsilon0);
+        VALIDATE(t);
         if (!s.invalid[t]) s.locked[t] = 1;
     }
     int attempt = 0;
@@ -268,12 +309,16 @@ int orc_validate(int ni, int nj, const int *tops, const int *lefts, float *u, fl
         int corrected = 0;
         for (int q = 0; q < total; q++) {
             const int t = order[q];
-            validate_median(&s, t, cfg->threshold, cfg->epsilon0);
-            for (int idx = 0; idx < cfg->num_peaks && s.invalid[t]; idx++) {
-                /* restore the main-peak displacement, then replace */
-                s.u[t] = s.bu[t];
-                s.v[t] = s.bv[t];
-                if (idx < cfg->num_peaks - 1) {
+            VALIDATE(t);
+            for (int idx = 0; idx < nstrat && s.invalid[t]; idx++) {
+                const int bilinear = idx == nstrat - 1 && last_bilinear;
+                const int secondary = model == 1 && idx < nstrat - 1;
+                if (bilinear || secondary) {
+                    /* restore the main-peak displacement, then replace */
+                    s.u[t] = s.bu[t];
+                    s.v[t] = s.bv[t];
+                }
+                if (secondary) {
                     const int peak = idx + 1;
                     if (npeaks[t] > peak && s.invalid[t]) {
                         float nu = s.u[t], nv = s.v[t];
@@ -281,14 +326,16 @@ int orc_validate(int ni, int nj, const int *tops, const int *lefts, float *u, fl
                         nv -= pv[(size_t)t * k];
                         nu += pu[(size_t)t * k + peak];
                         nv += pv[(size_t)t * k + peak];
-                        s.u[t] = nu;
-                        s.v[t] = nv;
-                        set_invalid(&s, t, 0);
+                        if (replace_ok(&s, t, nu, nv)) {
+                            s.u[t] = nu;
+                            s.v[t] = nv;
+                            set_invalid(&s, t, 0);
+                        }
                     }
-                } else {
+                } else if (bilinear) {
                     replace_bilinear(&s, t);
                 }
-                validate_median(&s, t, cfg->threshold, cfg->epsilon0);
+                VALIDATE(t);
                 if (!s.invalid[t]) { corrected++; break; }
             }
         }
@@ -297,8 +344,10 @@ int orc_validate(int ni, int nj, const int *tops, const int *lefts, float *u, fl
         if (!cfg->iterate_until_no_corrections && attempt >= cfg->max_iterations) break;
         if (attempt >= ORC_MAX_SWEEPS) break;  /* same bound as the CUDA path */
     }
+#undef VALIDATE
     for (int t = 0; t < total; t++) {
-        if (s.invalid[t]) { s.u[t] = 0.0f; s.v[t] = 0.0f; }
+        /* still-invalid vectors are set to 0 (Tile.replaceDisplacement(0, 0)) */
+        if (s.invalid[t] && replace_ok(&s, t, 0.0f, 0.0f)) { s.u[t] = 0.0f; s.v[t] = 0.0f; }
         if (invalid_out) invalid_out[t] = s.invalid[t];
     }
     free(s.bu); free(s.bv); free(s.invalid); free(s.locked); free(order);

@@ -26,6 +26,7 @@ MAX_SUBPIX_PIXELS = 15
 F_SUB_I, F_SUB_J, F_PARABOLIC, F_EDGE, F_NO_PEAK, F_ABSENT, F_FLOOR = 1, 2, 4, 8, 16, 32, 64
 MAX_PEAKS = 16
 VALIDATE_NONE, VALIDATE_MULTIPEAK_MEDIAN = 0, 1
+VALIDATE_DIFFERENCE_ONLY, VALIDATE_DIFFERENCE, VALIDATE_MEDIAN_ONLY, VALIDATE_MEDIAN = 2, 3, 4, 5
 
 VECTOR_DTYPE = np.dtype([
     ("u", "<f4"), ("v", "<f4"), ("sub_i", "<f4"), ("sub_j", "<f4"),
@@ -79,18 +80,23 @@ class AdaptiveDesc(ctypes.Structure):
                 ("peak_kernel", ctypes.c_int), ("median_threshold", ctypes.c_float),
                 ("median_epsilon0", ctypes.c_float), ("max_correction_iterations", ctypes.c_int),
                 ("iterate_until_no_corrections", ctypes.c_int), ("subpix_pixels", ctypes.c_int),
-                ("subpix_iterations", ctypes.c_int), ("inherit_mode", ctypes.c_int), ("reserved", ctypes.c_int * 2)]
+                ("subpix_iterations", ctypes.c_int), ("inherit_mode", ctypes.c_int), ("clipping_mode", ctypes.c_int),
+                ("reserved", ctypes.c_int * 1)]
+
+
+CLIP_ALLOWED, CLIP_LOGGED, CLIP_NO_OUT_OF_BOUND = 0, 1, 2
 
 
 def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_mode=WARP_BOTH_BILINEAR,
                   norm_mode=NORM_MAX_A, max_mode=MAX_FIXED, fixed_max=0.0, subpix_mode=SUBPIX_GAUSS3,
                   int16_warp_quirk=False, validation=None, subpix_pixels=3, subpix_iterations=20,
-                  inherit_mode=0):
+                  inherit_mode=0, clipping_mode=CLIP_ALLOWED):
     """Adaptive PIV parameters; the defaults follow the reference's BothImages bilinear
     warping (tiles copied from the warped image keep the full-scale maximum).
-    validation: None, or a dict for the multi-peak normalised-median model with keys
-    num_peaks, peak_kernel, threshold, epsilon0, max_iterations, iterate_until (see
-    multipeak_validation())."""
+    validation: None, or a dict with keys model (VALIDATE_*; default the multi-peak
+    normalised-median model), num_peaks, peak_kernel, threshold, epsilon0, max_iterations,
+    iterate_until (see multipeak_validation() and validation_model()).  clipping_mode:
+    CLIP_ALLOWED, CLIP_LOGGED or CLIP_NO_OUT_OF_BOUND (ClippingModeEnum)."""
     d = AdaptiveDesc()
     d.ia_start, d.ia_end, d.overlap_factor = ia_start, ia_end, overlap_factor
     d.margins[:] = list(margins)
@@ -98,6 +104,7 @@ def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_m
     d.subpix_mode, d.int16_warp_quirk = subpix_mode, int(int16_warp_quirk)
     d.subpix_pixels, d.subpix_iterations = subpix_pixels, subpix_iterations
     d.inherit_mode = inherit_mode
+    d.clipping_mode = clipping_mode
     if validation is not None:
         set_validation(d, **validation)
     return d
@@ -111,9 +118,16 @@ def multipeak_validation(num_peaks=3, peak_kernel=3, threshold=2.0, epsilon0=0.1
                 max_iterations=max_iterations, iterate_until=iterate_until)
 
 
+def validation_model(model, threshold=2.0, epsilon0=0.1, max_iterations=2, iterate_until=False):
+    """Settings of the four single-strategy models (VALIDATE_DIFFERENCE_ONLY, VALIDATE_DIFFERENCE,
+    VALIDATE_MEDIAN_ONLY, VALIDATE_MEDIAN; FindMaximumFromCenter peaks)."""
+    return dict(model=model, num_peaks=1, peak_kernel=3, threshold=threshold, epsilon0=epsilon0,
+                max_iterations=max_iterations, iterate_until=iterate_until)
+
+
 def set_validation(d, num_peaks=3, peak_kernel=3, threshold=2.0, epsilon0=0.1, max_iterations=2,
-                   iterate_until=False):
-    d.validation = VALIDATE_MULTIPEAK_MEDIAN
+                   iterate_until=False, model=None):
+    d.validation = VALIDATE_MULTIPEAK_MEDIAN if model is None else model
     d.num_peaks, d.peak_kernel = num_peaks, peak_kernel
     d.median_threshold, d.median_epsilon0 = threshold, epsilon0
     d.max_correction_iterations, d.iterate_until_no_corrections = max_iterations, int(iterate_until)
@@ -130,12 +144,12 @@ class FlowDesc(ctypes.Structure):
                 ("filter_sigma_ls", ctypes.c_float), ("filter_px_ls", ctypes.c_int), ("window_lk", ctypes.c_int),
                 ("iterations_lk", ctypes.c_int), ("lambda_ls", ctypes.c_float), ("iterations_ls", ctypes.c_int),
                 ("dense_export", ctypes.c_int), ("ignore_piv", ctypes.c_int), ("pyramid_levels", ctypes.c_int),
-                ("reserved", ctypes.c_int * 4)]
+                ("clipping_mode", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 def flow_desc(mode=FLOW_LUCAS_KANADE, filter_sigma_lk=2.0, filter_px_lk=3, filter_sigma_ls=0.48, filter_px_ls=5,
               window_lk=27, iterations_lk=5, lambda_ls=4.0, iterations_ls=60, dense_export=False, ignore_piv=0,
-              pyramid_levels=0):
+              pyramid_levels=0, clipping_mode=CLIP_ALLOWED):
     """Optical flow after PIV (OpticalFlowAfterPIV Lucas-Kanade or Liu-Shen interpolator
     options); dense_export selects whole-pixel evaluation and the dense field export.
     pyramid_levels > 1 runs the Lucas-Kanade stage coarse to fine over that many 2 x 2
@@ -146,6 +160,7 @@ def flow_desc(mode=FLOW_LUCAS_KANADE, filter_sigma_lk=2.0, filter_px_lk=3, filte
         iterations_lk
     d.lambda_ls, d.iterations_ls, d.dense_export = lambda_ls, iterations_ls, int(dense_export)
     d.ignore_piv, d.pyramid_levels = ignore_piv, pyramid_levels
+    d.clipping_mode = clipping_mode
     return d
 
 
@@ -205,7 +220,10 @@ _SIGNATURES = {
     "qlpiv_xcorr_planes": (_i, [_vp, _i, _l, _i, _vp, _vp, _vp, _vp, _i, _vp]),
     "qlpiv_xcorr_peaks": (_i, [_vp, _i, _l, _i, _vp, _vp, _vp, _vp, _i, _i, _vp]),
     "qlpiv_xcorr_multipeaks": (_i, [_vp, _i, _l, _i, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "qlpiv_probe_division": (_i, [_i, ctypes.POINTER(ctypes.c_int64)]),
     "qlpiv_validate": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "qlpiv_validate_tiles": (_i, [_vp, ctypes.POINTER(AdaptiveDesc), _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp,
+                                  _vp, _vp]),
     "qlpiv_pass": (_i, [_vp, ctypes.POINTER(PassDesc), _vp, _vp, _i, _i, _i, _l, _vp, _vp, _vp, _vp, _vp]),
     "qlpiv_pass_device": (_i, [_vp, ctypes.POINTER(PassDesc), _vp, _vp, _i, _i, _i, _l, _vp, _vp, _vp, _vp, _vp]),
     "qlpiv_pass_batch": (_i, [_vp, ctypes.POINTER(PassDesc), _i, _i, _vp, _l, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -270,7 +288,7 @@ def load_library(path=None):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.qlpiv_abi_version() != 3:
+    if lib.qlpiv_abi_version() != 4:
         raise RuntimeError("libqlpiv_gpu.so ABI version mismatch")
     if path is None:
         _lib = lib
@@ -334,6 +352,14 @@ def inherit_noalloc(device, stream, p_ci, p_cj, pu, pv, c_ci, c_cj, cu, cv, pni,
     a = [x if isinstance(x, int) else _addr(x) for x in args]
     _check(load_library().qlpiv_inherit_noalloc(device, stream or None, pni, pnj, a[0], a[1], a[2], a[3], cni, cnj,
                                                 a[4], a[5], int(round_int), a[6], a[7]))
+
+
+def probe_division(device=0):
+    """Quotients of the IA-16 kernel's normalisation division that differ from IEEE division over
+    every integer pixel value and integer maximum below 65536 (0 expected)."""
+    n = ctypes.c_int64()
+    _check(load_library().qlpiv_probe_division(device, ctypes.byref(n)))
+    return n.value
 
 
 def probe_log(x, device=0):
@@ -638,23 +664,34 @@ class Handle:
                                          _addr(mb)))
         return ta, tb, ma, mb
 
-    def validate(self, tops, lefts, u, v, peak_u, peak_v, npeaks, desc):
-        """Multi-peak normalised-median validation of one frame's tiles (host arrays):
-        u, v (ni, nj) with the main peak accumulated, peak_u/peak_v (ni, nj, k), npeaks
-        (ni, nj).  Returns validated copies of (u, v) and the invalid flags."""
+    def validate(self, tops, lefts, u, v, peak_u, peak_v, npeaks, desc, n=None, height=None, width=None):
+        """Vector validation of one frame's tiles (host arrays) with desc.validation's model:
+        u, v (ni, nj) with the main peak accumulated; for the multi-peak model peak_u/peak_v
+        (ni, nj, k) and npeaks (ni, nj), for the others None.  With the tile side n and the
+        image size (required by desc.clipping_mode CLIP_NO_OUT_OF_BOUND) the call goes through
+        qlpiv_validate_tiles.  Returns validated copies of (u, v) and the invalid flags."""
         u = np.array(u, np.float32, order="C", copy=True)
         v = np.array(v, np.float32, order="C", copy=True)
         ni, nj = u.shape
-        pu = np.ascontiguousarray(peak_u, np.float32)
-        pv = np.ascontiguousarray(peak_v, np.float32)
-        if pu.shape != (ni, nj, desc.num_peaks) or pv.shape != pu.shape:
-            raise ValueError("peak arrays must be (ni, nj, num_peaks)")
-        npk = np.ascontiguousarray(npeaks, np.int32)
+        multi = desc.validation == VALIDATE_MULTIPEAK_MEDIAN
+        if multi:
+            pu = np.ascontiguousarray(peak_u, np.float32)
+            pv = np.ascontiguousarray(peak_v, np.float32)
+            if pu.shape != (ni, nj, desc.num_peaks) or pv.shape != pu.shape:
+                raise ValueError("peak arrays must be (ni, nj, num_peaks)")
+            npk = np.ascontiguousarray(npeaks, np.int32)
+            pk = (_addr(pu), _addr(pv), _addr(npk))
+        else:
+            pk = (None, None, None)
         tops = np.ascontiguousarray(tops, np.int32)
         lefts = np.ascontiguousarray(lefts, np.int32)
         inv = np.empty((ni, nj), np.uint8)
-        _check(self._lib.qlpiv_validate(self._h, ctypes.byref(desc), ni, nj, _addr(tops), _addr(lefts), _addr(u),
-                                        _addr(v), _addr(pu), _addr(pv), _addr(npk), _addr(inv)))
+        if n is None:
+            _check(self._lib.qlpiv_validate(self._h, ctypes.byref(desc), ni, nj, _addr(tops), _addr(lefts), _addr(u),
+                                            _addr(v), *pk, _addr(inv)))
+        else:
+            _check(self._lib.qlpiv_validate_tiles(self._h, ctypes.byref(desc), n, height, width, ni, nj, _addr(tops),
+                                                  _addr(lefts), _addr(u), _addr(v), *pk, _addr(inv)))
         return u, v, inv
 
     # -- dense optical flow ------------------------------------------------------

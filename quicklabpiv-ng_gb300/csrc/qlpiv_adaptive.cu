@@ -24,6 +24,7 @@
 #include <stdint.h>
 
 #include "qlpiv_adaptive.h"
+#include "qlpiv_internal.h"
 
 namespace qlpiv {
 
@@ -696,6 +697,19 @@ __global__ void displaced_origins_kernel(long count, const int *a_top, const int
     b_left[k] = java_round((float)a_left[k] + v[k]);
 }
 
+// Inheritance under NoOutOfBoundClipping: a child tile starts at zero and takes its inherited
+// value through Tile.accumulateDisplacement (S/iareas/Tile.java:103-136), which drops a value that
+// would move the tile out of the image (the tile then keeps zero).
+__global__ void clip_inherited_kernel(long count, const int *top, const int *left, int n, int h, int w, float *u,
+                                      float *v) {
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const float nu = __fadd_rn(0.0f, u[k]), nv = __fadd_rn(0.0f, v[k]);
+    const bool ok = tile_inside(n, h, w, top[k], left[k], nu, nv);
+    u[k] = ok ? nu : 0.0f;
+    v[k] = ok ? nv : 0.0f;
+}
+
 // ---------------- launchers ----------------
 
 static inline unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -783,6 +797,13 @@ cudaError_t launch_displaced_origins(cudaStream_t s, long count, const int *a_to
                                      const float *v, int *b_top, int *b_left) {
     if (count == 0) return cudaSuccess;
     displaced_origins_kernel<<<blocks_for(count, 256), 256, 0, s>>>(count, a_top, a_left, u, v, b_top, b_left);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_clip_inherited(cudaStream_t s, long count, const int *top, const int *left, int n, int h, int w,
+                                  float *u, float *v) {
+    if (count == 0) return cudaSuccess;
+    clip_inherited_kernel<<<blocks_for(count, 256), 256, 0, s>>>(count, top, left, n, h, w, u, v);
     return cudaGetLastError();
 }
 

@@ -58,6 +58,10 @@ cudaError_t launch_field(cudaStream_t s, int h, int w, const float *ys, int ni, 
                          SplineCoef coef, float *fu, float *fv, float off_y = 0.0f, float off_x = 0.0f);
 cudaError_t launch_displaced_origins(cudaStream_t s, long count, const int *a_top, const int *a_left, const float *u,
                                      const float *v, int *b_top, int *b_left);
+// NoOutOfBoundClipping of inherited displacements: count tiles with origins top/left (side n) in
+// an h x w image; a value that moves its tile out of the image is replaced by zero.
+cudaError_t launch_clip_inherited(cudaStream_t s, long count, const int *top, const int *left, int n, int h, int w,
+                                  float *u, float *v);
 
 int grid_superposition(int h, int w, const int margins[4], int ia_start, int level, float ofac, qlpiv_grid *g,
                        int32_t *tops, int32_t *lefts, int cap);

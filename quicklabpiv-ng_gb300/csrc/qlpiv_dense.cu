@@ -748,9 +748,12 @@ __global__ void __launch_bounds__(256) ls_pass_kernel(const float *fx, int h, in
 }
 
 // Tile displacements from the dense field (rows vs, columns us) at top + n/2 - 1, left + n/2 - 1,
-// or the 2x2 average there with dense export (Tile.replaceDisplacement(v, u)).
-__global__ void tiles_from_dense_kernel(const float *us, const float *vs, int w, int n, int ni, int nj,
-                                        const int *tops, const int *lefts, int dense, float *tile_u, float *tile_v) {
+// or the 2x2 average there with dense export (Tile.replaceDisplacement(v, u)); with clip
+// (NoOutOfBoundClipping, image h x w) a value that moves the tile out of the image is refused and
+// the tile keeps its displacement.
+__global__ void tiles_from_dense_kernel(const float *us, const float *vs, int h, int w, int n, int ni, int nj,
+                                        const int *tops, const int *lefts, int dense, int clip, float *tile_u,
+                                        float *tile_v) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ni * nj) return;
     const int ti = t / nj, tj = t - ti * nj;
@@ -764,6 +767,7 @@ __global__ void tiles_from_dense_kernel(const float *us, const float *vs, int w,
         u = __fdiv_rn(__fadd_rn(__fadd_rn(__fadd_rn(us[idx], us[idx + 1]), us[idx2]), us[idx2 + 1]), 4.0f);
         v = __fdiv_rn(__fadd_rn(__fadd_rn(__fadd_rn(vs[idx], vs[idx + 1]), vs[idx2]), vs[idx2 + 1]), 4.0f);
     }
+    if (clip && !tile_inside(n, h, w, tops[ti], lefts[tj], v, u)) return;
     tile_u[t] = v;
     tile_v[t] = u;
 }
@@ -800,6 +804,8 @@ const char *check_flow_desc(const qlpiv_flow_desc *d, int h, int w) {
     if (d->iterations_lk <= 0) return "dense Lucas-Kanade: Number of iterations must greater or equal to 1";
     if (d->ignore_piv < QLPIV_IGNORE_PIV_NONE || d->ignore_piv > QLPIV_IGNORE_PIV_AUTO_SMALL)
         return "unknown ignore-PIV mode";
+    if (d->clipping_mode < QLPIV_CLIP_ALLOWED || d->clipping_mode > QLPIV_CLIP_NO_OUT_OF_BOUND)
+        return "unknown clipping mode";
     if (d->filter_px_lk < 1 || d->filter_px_lk % 2 == 0 || d->filter_px_lk > 63) return "Lucas-Kanade filter width";
     if (d->mode == QLPIV_FLOW_LIU_SHEN) {
         if (d->iterations_ls <= 0) return "dense Liu-Shen: Number of iterations must greater or equal to 1";
@@ -1035,8 +1041,9 @@ cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, c
         *launches += 1 + d.iterations_ls;
         mark("flow:liu_shen", false);
     }
-    tiles_from_dense_kernel<<<blocks_of((long)ni * nj, 128), 128, 0, s>>>(us, vs, w, n, ni, nj, tops, lefts,
-                                                                          d.dense_export, tile_u, tile_v);
+    tiles_from_dense_kernel<<<blocks_of((long)ni * nj, 128), 128, 0, s>>>(
+        us, vs, h, w, n, ni, nj, tops, lefts, d.dense_export, d.clipping_mode == QLPIV_CLIP_NO_OUT_OF_BOUND, tile_u,
+        tile_v);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     *launches += 1;
     if (dense_u && (e = cudaMemcpyAsync(dense_u, vs, sizeof(float) * np, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)

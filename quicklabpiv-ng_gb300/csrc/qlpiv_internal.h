@@ -33,6 +33,18 @@ void drop_plan(qlpiv_handle *h);
 // Sub-pixel mode settings (qlpiv_capi.cu): QLPIV_OK or QLPIV_E_ARG with the message set.
 qlpiv_status check_subpix(int mode, int pixels, int iterations);
 
+// Tile.accumulateDisplacement / replaceDisplacement under NoOutOfBoundClipping
+// (S/iareas/Tile.java:103-136,156-189): false when the tile of side n at (top, left), moved by the
+// rounded displacement (FastMath.round: floor(x + 0.5f)), fails the reference's test
+// top + ru < 0, top + n + ru >= h, left + rv < 0, left + n + rv >= w.  n == 0 means clipping is
+// allowed and nothing is refused.  Float compares of small integers, as in the reference.
+__host__ __device__ __forceinline__ bool tile_inside(int n, int h, int w, int top, int left, float u, float v) {
+    if (n == 0) return true;
+    const float ru = floorf(u + 0.5f), rv = floorf(v + 0.5f);
+    return !((float)top + ru < 0.0f || (float)(top + n) + ru >= (float)h || (float)left + rv < 0.0f ||
+             (float)(left + n) + rv >= (float)w);
+}
+
 inline size_t pixel_bytes(int pixel_type) {
     return pixel_type == QLPIV_PIX_U8 ? 1 : (pixel_type == QLPIV_PIX_U16 ? 2 : 4);
 }

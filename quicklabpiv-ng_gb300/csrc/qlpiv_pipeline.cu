@@ -112,18 +112,27 @@ static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type,
         return fail(QLPIV_E_ARG, "unknown velocity inheritance mode %d", d->inherit_mode);
     if (!(d->overlap_factor >= 0.1f && d->overlap_factor <= 0.9f))
         return fail(QLPIV_E_ARG, "Overlap factor must greater than 1/10 and less than 9/10");
-    if (d->validation != QLPIV_VALIDATE_NONE && d->validation != QLPIV_VALIDATE_MULTIPEAK_MEDIAN)
+    if (d->validation < QLPIV_VALIDATE_NONE || d->validation > QLPIV_VALIDATE_MEDIAN)
         return fail(QLPIV_E_ARG, "unknown validation mode %d", d->validation);
+    if (d->clipping_mode < QLPIV_CLIP_ALLOWED || d->clipping_mode > QLPIV_CLIP_NO_OUT_OF_BOUND)
+        return fail(QLPIV_E_ARG, "unknown clipping mode %d", d->clipping_mode);
     if (d->validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN) {
         for (int n = d->ia_start; n >= d->ia_end; n >>= 1)
             if (!multipeak_supported(n, d->num_peaks, d->peak_kernel))
                 return fail(QLPIV_E_ARG, "multi-peak search: %d peaks with cell width %d not supported for IA %d "
                             "(1..%d peaks, cell width >= 2)", d->num_peaks, d->peak_kernel, n, QLPIV_MAX_PEAKS);
+    }
+    if (d->validation != QLPIV_VALIDATE_NONE) {
         if (!(d->median_threshold > 0.0f) || !(d->median_epsilon0 >= 0.0f))
-            return fail(QLPIV_E_ARG, "median threshold must be > 0 and epsilon0 >= 0");
+            return fail(QLPIV_E_ARG, "validation threshold must be > 0 and epsilon0 >= 0");
         if (d->max_correction_iterations < 0) return fail(QLPIV_E_ARG, "max correction iterations < 0");
     }
     return QLPIV_OK;
+}
+
+// Strategies of the validation model: the multi-peak model k, every other model one.
+static int validation_strategies(const qlpiv_adaptive_desc &d) {
+    return d.validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN ? d.num_peaks : 1;
 }
 
 // Per child row and per child column tables of the Direct / Area / Distance inheritance
@@ -302,7 +311,7 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
         std::vector<int32_t> order, rank;
         if (d->validation != QLPIV_VALIDATE_NONE) {
             spiral_rank(ni, nj, order, rank);
-            const long k = d->num_peaks;
+            const long k = validation_strategies(*d);
             if ((e = upload(L.d_order, order.data(), sizeof(int32_t) * cnt, s)) != cudaSuccess ||
                 (e = upload(L.d_rank, rank.data(), sizeof(int32_t) * cnt, s)) != cudaSuccess ||
                 (e = L.d_bu.ensure(sizeof(float) * total)) != cudaSuccess ||
@@ -411,6 +420,13 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
                                          L.d_inh.as<int2>(), d.warp_mode == QLPIV_WARP_NONE, u, v);
             if (e != cudaSuccess) return cuda_fail(e, "inheritance");
             h->launches += spline ? 2 : 1;
+            if (d.clipping_mode == QLPIV_CLIP_NO_OUT_OF_BOUND) {
+                // the child tiles take the inherited value through Tile.accumulateDisplacement
+                if ((e = launch_clip_inherited(s, total, L.d_at.as<int>(), L.d_al.as<int>(), L.g.n, p->height,
+                                               p->width, u, v)) != cudaSuccess)
+                    return cuda_fail(e, "inheritance clipping");
+                h->launches++;
+            }
         }
         const qlpiv_frame *src = frames_dev;
         const int *bt = L.d_at.as<int>(), *bl = L.d_al.as<int>();
@@ -495,9 +511,17 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
         job.subpix_iters = d.subpix_iterations;
         job.acc_u = u;
         job.acc_v = v;
-        const bool validate = d.validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN;
-        if (validate) {
-            // the multi-peak model selects FindMaximumMultiPeaks for every level
+        if (d.clipping_mode == QLPIV_CLIP_NO_OUT_OF_BOUND) {
+            job.clip_top = L.d_at.as<int>();
+            job.clip_left = L.d_al.as<int>();
+            job.clip_n = L.g.n;
+            job.clip_h = p->height;
+            job.clip_w = p->width;
+        }
+        const bool validate = d.validation != QLPIV_VALIDATE_NONE;
+        if (d.validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN) {
+            // the multi-peak model selects FindMaximumMultiPeaks for every level (the others keep
+            // FindMaximumFromCenter)
             job.num_peaks = d.num_peaks;
             job.peak_kernel = d.peak_kernel;
             job.peak_uv = L.d_puv.as<float2>();
@@ -511,8 +535,14 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
         h->launches++;
         if (validate) {
             StageScope sc(h, "validate", (int)lv, L.g.n, 2, total);
-            ValidateParams vp{L.g.tiles_i, L.g.tiles_j, d.num_peaks, d.median_threshold, d.median_epsilon0,
-                              d.max_correction_iterations, d.iterate_until_no_corrections};
+            ValidateParams vp{L.g.tiles_i, L.g.tiles_j, validation_strategies(d), d.median_threshold,
+                              d.median_epsilon0, d.max_correction_iterations, d.iterate_until_no_corrections,
+                              d.validation, 0, 0, 0};
+            if (d.clipping_mode == QLPIV_CLIP_NO_OUT_OF_BOUND) {
+                vp.clip_n = L.g.n;
+                vp.clip_h = p->height;
+                vp.clip_w = p->width;
+            }
             ValidateBufs vb{u, v, L.d_bu.as<float>(), L.d_bv.as<float>(), L.d_puv.as<float2>(),
                             L.d_npk.as<uint8_t>(), L.d_state.as<uint8_t>(), L.d_tops.as<int>(), L.d_lefts.as<int>(),
                             L.d_order.as<int>(), L.d_rank.as<int>(), L.d_list.as<int>(), L.d_done.as<int>(),
@@ -582,7 +612,7 @@ size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int heigh
         if (per_tile_warp(d->warp_mode) && lv > 0)
             total += al(2 * tot * g.n * g.n * pixel_bytes(pixel_type)) + al(8 * tot);
         if (d->validation != QLPIV_VALIDATE_NONE) {
-            const size_t k = d->num_peaks;
+            const size_t k = validation_strategies(*d);
             total += 2 * al(4 * cnt) + 2 * al(4 * tot) + al(8 * tot * k) + 2 * al(tot) + 2 * al(4 * tot) +
                      al(4 * (size_t)pairs);
         }
@@ -923,9 +953,11 @@ qlpiv_status qlpiv_piv_adaptive_device(qlpiv_handle *h, const qlpiv_adaptive_des
 // Queues the optical flow after PIV of every pair on the last level's tiles (in place in
 // d_u/d_v).  frames: host-side copy of the device frame table (image pointers per pair).
 // dense_u/dense_v: device, pairs x height x width, or NULL.
-static qlpiv_status queue_flow(qlpiv_handle *h, const qlpiv_flow_desc &fd, const qlpiv_frame *frames,
+static qlpiv_status queue_flow(qlpiv_handle *h, const qlpiv_flow_desc &flow, const qlpiv_frame *frames,
                                float *dense_u, float *dense_v, std::vector<float> &weights) {
     AdaptivePlan *p = h->plan;
+    qlpiv_flow_desc fd = flow;
+    fd.clipping_mode = p->desc.clipping_mode;  // one PIVInputParameters clipping mode for every stage
     LevelPlan &L = p->levels.back();
     cudaStream_t s = h->stream;
     const int ni = L.g.tiles_i, nj = L.g.tiles_j;
@@ -1099,24 +1131,34 @@ qlpiv_status qlpiv_piv_flow_device(qlpiv_handle *h, const qlpiv_adaptive_desc *p
     return QLPIV_OK;
 }
 
-qlpiv_status qlpiv_validate(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int ni, int nj, const int32_t *tops,
-                            const int32_t *lefts, float *u, float *v, const float *peak_u, const float *peak_v,
-                            const int32_t *npeaks, uint8_t *invalid_out) {
-    if (!h || !desc || !tops || !lefts || !u || !v || !peak_u || !peak_v || !npeaks)
-        return fail(QLPIV_E_ARG, "NULL argument");
+// VectorValidatorJob.compute on host arrays for one frame; clip_n > 0 applies NoOutOfBoundClipping
+// to the replacements (tile side clip_n, image clip_h x clip_w).
+static qlpiv_status validate_host(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int clip_n, int clip_h,
+                                  int clip_w, int ni, int nj, const int32_t *tops, const int32_t *lefts, float *u,
+                                  float *v, const float *peak_u, const float *peak_v, const int32_t *npeaks,
+                                  uint8_t *invalid_out) {
+    if (!h || !desc || !tops || !lefts || !u || !v) return fail(QLPIV_E_ARG, "NULL argument");
     if (ni < 1 || nj < 1) return fail(QLPIV_E_SHAPE, "empty grid");
-    const int k = desc->num_peaks;
+    const int model = desc->validation;
+    if (model < QLPIV_VALIDATE_MULTIPEAK_MEDIAN || model > QLPIV_VALIDATE_MEDIAN)
+        return fail(QLPIV_E_ARG, "unknown validation model %d", model);
+    const bool multi = model == QLPIV_VALIDATE_MULTIPEAK_MEDIAN;
+    if (multi && (!peak_u || !peak_v || !npeaks))
+        return fail(QLPIV_E_ARG, "the multi-peak model needs peak_u, peak_v and npeaks");
+    const int k = multi ? desc->num_peaks : 1;
     if (k < 1 || k > QLPIV_MAX_PEAKS) return fail(QLPIV_E_ARG, "num_peaks must be in 1..%d", QLPIV_MAX_PEAKS);
     if (!(desc->median_threshold > 0.0f) || !(desc->median_epsilon0 >= 0.0f))
-        return fail(QLPIV_E_ARG, "median threshold must be > 0 and epsilon0 >= 0");
+        return fail(QLPIV_E_ARG, "validation threshold must be > 0 and epsilon0 >= 0");
     const long cnt = (long)ni * nj;
-    std::vector<float2> puv(cnt * k);
-    std::vector<uint8_t> npk(cnt);
-    for (long t = 0; t < cnt; t++) {
-        if (npeaks[t] < 0 || npeaks[t] > k) return fail(QLPIV_E_ARG, "npeaks[%ld] = %d outside 0..%d", t, npeaks[t], k);
-        npk[t] = (uint8_t)npeaks[t];
-        for (int q = 0; q < k; q++) puv[t * k + q] = make_float2(peak_u[t * k + q], peak_v[t * k + q]);
-    }
+    std::vector<float2> puv(cnt * k, make_float2(0.0f, 0.0f));
+    std::vector<uint8_t> npk(cnt, 1);
+    if (multi)
+        for (long t = 0; t < cnt; t++) {
+            if (npeaks[t] < 0 || npeaks[t] > k)
+                return fail(QLPIV_E_ARG, "npeaks[%ld] = %d outside 0..%d", t, npeaks[t], k);
+            npk[t] = (uint8_t)npeaks[t];
+            for (int q = 0; q < k; q++) puv[t * k + q] = make_float2(peak_u[t * k + q], peak_v[t * k + q]);
+        }
     std::vector<int32_t> order, rank;
     spiral_rank(ni, nj, order, rank);
     std::lock_guard<std::mutex> lock(h->mu);
@@ -1156,7 +1198,7 @@ qlpiv_status qlpiv_validate(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, in
         (e = cudaMemcpyAsync(dlefts, lefts, sizeof(int32_t) * nj, cudaMemcpyHostToDevice, s)) != cudaSuccess)
         return cuda_fail(e, "validation upload");
     ValidateParams vp{ni, nj, k, desc->median_threshold, desc->median_epsilon0, desc->max_correction_iterations,
-                      desc->iterate_until_no_corrections};
+                      desc->iterate_until_no_corrections, model, clip_n, clip_h, clip_w};
     ValidateBufs vb{du, dv, dbu, dbv, dpuv, dnpk, dst, dtops, dlefts, dorder, drank, dlist, ddone, dsweeps};
     if ((e = launch_validate(s, 1, vp, vb)) != cudaSuccess) return cuda_fail(e, "validation");
     h->launches += 2;
@@ -1169,6 +1211,27 @@ qlpiv_status qlpiv_validate(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, in
     if (invalid_out)
         for (long t = 0; t < cnt; t++) invalid_out[t] = state[t] & 1u;
     return QLPIV_OK;
+}
+
+qlpiv_status qlpiv_validate(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int ni, int nj, const int32_t *tops,
+                            const int32_t *lefts, float *u, float *v, const float *peak_u, const float *peak_v,
+                            const int32_t *npeaks, uint8_t *invalid_out) {
+    if (desc && desc->clipping_mode == QLPIV_CLIP_NO_OUT_OF_BOUND)
+        return fail(QLPIV_E_ARG, "NoOutOfBoundClipping needs the tile side and image size: use qlpiv_validate_tiles");
+    return validate_host(h, desc, 0, 0, 0, ni, nj, tops, lefts, u, v, peak_u, peak_v, npeaks, invalid_out);
+}
+
+qlpiv_status qlpiv_validate_tiles(qlpiv_handle *h, const qlpiv_adaptive_desc *desc, int n, int height, int width,
+                                  int ni, int nj, const int32_t *tops, const int32_t *lefts, float *u, float *v,
+                                  const float *peak_u, const float *peak_v, const int32_t *npeaks,
+                                  uint8_t *invalid_out) {
+    if (!desc) return fail(QLPIV_E_ARG, "NULL argument");
+    if (desc->clipping_mode < QLPIV_CLIP_ALLOWED || desc->clipping_mode > QLPIV_CLIP_NO_OUT_OF_BOUND)
+        return fail(QLPIV_E_ARG, "unknown clipping mode %d", desc->clipping_mode);
+    if (n < 1 || height < 1 || width < 1) return fail(QLPIV_E_SHAPE, "tile side and image size must be positive");
+    const bool clip = desc->clipping_mode == QLPIV_CLIP_NO_OUT_OF_BOUND;
+    return validate_host(h, desc, clip ? n : 0, clip ? height : 0, clip ? width : 0, ni, nj, tops, lefts, u, v,
+                         peak_u, peak_v, npeaks, invalid_out);
 }
 
 qlpiv_status qlpiv_profile_enable(qlpiv_handle *h, int enable) {

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "qlpiv.h"
+#include "qlpiv_div.cuh"
 #include "qlpiv_internal.h"
 #include "qlpiv_logdf.cuh"
 
@@ -102,5 +103,39 @@ extern "C" qlpiv_status qlpiv_probe_log(int device, const float *x, long n, doub
     cudaFree(dx);
     cudaFree(dm);
     cudaFree(dr);
+    return st;
+}
+
+// Instrumentation: the tile normalisation's division (qlpiv_div.cuh) against IEEE division over
+// every integer v in [0, 65535] and divisor m in [1, 65535]; counts the quotients that differ.
+namespace {
+__global__ void division_probe(unsigned long long *mismatches) {
+    const int m = blockIdx.x + 1;  // divisor 1..65535
+    const float fm = (float)m, rm = __frcp_rn(fm);
+    unsigned long long bad = 0;
+    for (int v = threadIdx.x; v < 65536; v += blockDim.x) {
+        const float fv = (float)v;
+        if (__float_as_uint(qlpiv::div_int(fv, fm, rm)) != __float_as_uint(__fdiv_rn(fv, fm))) bad++;
+    }
+    if (bad) atomicAdd(mismatches, bad);
+}
+}  // namespace
+
+extern "C" qlpiv_status qlpiv_probe_division(int device, int64_t *mismatches) {
+    if (!mismatches) return QLPIV_E_ARG;
+    *mismatches = -1;
+    if (cudaSetDevice(device) != cudaSuccess) return QLPIV_E_NO_DEVICE;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess) return QLPIV_E_OOM;
+    qlpiv_status st = QLPIV_OK;
+    unsigned long long h = 0;
+    if (cudaMemset(d, 0, sizeof(*d)) != cudaSuccess) st = QLPIV_E_CUDA;
+    if (st == QLPIV_OK) {
+        division_probe<<<65535, 256>>>(d);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = QLPIV_E_CUDA;
+    }
+    cudaFree(d);
+    if (st == QLPIV_OK) *mismatches = (int64_t)h;
     return st;
 }

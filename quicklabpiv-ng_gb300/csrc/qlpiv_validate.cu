@@ -1,11 +1,14 @@
 // Vector validation and replacement after a correlation level (device code).
 //
-// VectorValidatorJob.compute (S/jobs/validator/VectorValidatorJob.java:242-405) with the
-// multi-peak normalised-median model (the converter's visit of
-// VelocityValidationOptionsMultiPeakNormalizedMedianModel): k strategies, strategy
-// s < k-1 = NormalizedMedianValidator + SecondaryPeakReplacement(peak s+1), strategy k-1
-// = NormalizedMedianValidator + BilinearReplacement.
+// VectorValidatorJob.compute (S/jobs/validator/VectorValidatorJob.java:242-405) with the five
+// models the converter builds (PIVConfigurationConverterVisitor.visit,
+// ui/src/main/java/pt/quickLabPIV/business/transfer/PIVConfigurationConverterVisitor.java:546-641):
+// the multi-peak normalised-median model (k strategies, strategy s < k-1 =
+// NormalizedMedianValidator + SecondaryPeakReplacement(peak s+1), strategy k-1 =
+// NormalizedMedianValidator + BilinearReplacement), and one strategy of DifferenceValidator or
+// NormalizedMedianValidator without or with BilinearReplacement.
 //   NormalizedMedianValidator.validateVector  S/iareas/validation/NormalizedMedianValidator.java:63-136
+//   DifferenceValidator.validateVector        S/iareas/validation/DifferenceValidator.java:30-60
 //   SecondaryPeakReplacement.replaceVector    S/iareas/replacement/SecondaryPeakReplacement.java:41-76
 //   BilinearReplacement.replaceVector         S/iareas/replacement/BilinearReplacement.java:23-420
 //   Tile backup / restore / lock              S/iareas/Tile.java:138-217
@@ -34,6 +37,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "qlpiv.h"
+#include "qlpiv_internal.h"
 #include "qlpiv_validate.h"
 
 namespace qlpiv {
@@ -52,7 +57,19 @@ struct PairView {
     uint8_t *state;
     const int *tops, *lefts;
     int k;
+    int model;
+    int clip_n, clip_h, clip_w;
 };
+
+// Tile.replaceDisplacement: refused under NoOutOfBoundClipping when the rounded displacement
+// moves tile t out of the image.
+__device__ __forceinline__ bool replace_ok(const PairView &p, int t, float u, float v) {
+    return tile_inside(p.clip_n, p.clip_h, p.clip_w, p.tops[t / p.nj], p.lefts[t % p.nj], u, v);
+}
+
+__device__ __forceinline__ bool difference_model(const PairView &p) {
+    return p.model == QLPIV_VALIDATE_DIFFERENCE_ONLY || p.model == QLPIV_VALIDATE_DIFFERENCE;
+}
 
 __device__ __forceinline__ void set_invalid(const PairView &p, int t, bool inv) {
     const uint8_t st = p.state[t];
@@ -120,6 +137,32 @@ __device__ void median_validate(const PairView &p, int t, float threshold, float
     const float du = __fsub_rn(mu, p.u[t]), dv = __fsub_rn(mv, p.v[t]);
     const float dist = __fdiv_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(du, du), __fmul_rn(dv, dv))), __fadd_rn(rmed, eps0));
     set_invalid(p, t, !(dist < threshold));
+}
+
+// DifferenceValidator.validateVector for tile t: adjacents[i][j] for i, j in {0, 1} except
+// (1, 1) -- the top-left, top and left neighbours -- each valid one overwriting the flag with
+// |d|^2 < threshold^2; with no valid one among them the flag is left as it is.
+__device__ void difference_validate(const PairView &p, int t, float threshold) {
+    const float t2 = __fmul_rn(threshold, threshold);
+    const int ti = t / p.nj, tj = t - ti * p.nj;
+    for (int a = -1; a <= 0; a++)
+        for (int b = -1; b <= 0; b++) {
+            if (a == 0 && b == 0) continue;
+            const int i = ti + a, j = tj + b;
+            if (i < 0 || j < 0) continue;
+            const int q = i * p.nj + j;
+            if (p.state[q] & kInvalid) continue;
+            const float du = __fsub_rn(p.u[q], p.u[t]), dv = __fsub_rn(p.v[q], p.v[t]);
+            const float dist = __fadd_rn(__fmul_rn(du, du), __fmul_rn(dv, dv));
+            set_invalid(p, t, !(dist < t2));
+        }
+}
+
+__device__ __forceinline__ void validate_vector(const PairView &p, int t, float threshold, float eps0) {
+    if (difference_model(p))
+        difference_validate(p, t, threshold);
+    else
+        median_validate(p, t, threshold, eps0);
 }
 
 // BilinearReplacement.interpV / interpU: weights along one coordinate of two tiles.
@@ -217,7 +260,7 @@ __device__ void bilinear_replace(const PairView &p, int t) {
             }
         if (pick < 0) {
             set_invalid(p, t, true);
-        } else {
+        } else if (replace_ok(p, t, p.u[pick], p.v[pick])) {
             p.u[t] = p.u[pick];
             p.v[t] = p.v[pick];
             set_invalid(p, t, false);
@@ -232,29 +275,45 @@ __device__ void bilinear_replace(const PairView &p, int t) {
         aU = __fadd_rn(aU, __fmul_rn((float)cU[q], uU[q]));
         wU += cU[q];
     }
-    p.u[t] = __fdiv_rn(aU, (float)wU);
-    p.v[t] = __fdiv_rn(aV, (float)wV);
-    set_invalid(p, t, false);
+    const float nu = __fdiv_rn(aU, (float)wU), nv = __fdiv_rn(aV, (float)wV);
+    if (replace_ok(p, t, nu, nv)) {
+        p.u[t] = nu;
+        p.v[t] = nv;
+    }
+    set_invalid(p, t, false);  // cleared whether or not the value was taken, as the reference does
 }
 
 // The validator visit of one open tile in a correction sweep; true if it was corrected.
+// Strategies: multi-peak model k (secondary peaks 1..k-1, then bilinear), otherwise one
+// (bilinear or no replacement).  Only a strategy with a replacement restores the backup first.
 __device__ bool visit_open_tile(const PairView &p, int t, float threshold, float eps0) {
-    median_validate(p, t, threshold, eps0);
-    for (int s = 0; s < p.k && is_invalid(p, t); s++) {
-        p.u[t] = p.bu[t];  // Tile.restoreDisplacement
-        p.v[t] = p.bv[t];
-        if (s < p.k - 1) {
+    const bool multi = p.model == QLPIV_VALIDATE_MULTIPEAK_MEDIAN;
+    const int nstrat = multi ? p.k : 1;
+    const bool last_bilinear = multi || p.model == QLPIV_VALIDATE_DIFFERENCE || p.model == QLPIV_VALIDATE_MEDIAN;
+    validate_vector(p, t, threshold, eps0);
+    for (int s = 0; s < nstrat && is_invalid(p, t); s++) {
+        const bool secondary = multi && s < nstrat - 1;
+        const bool bilinear = !secondary && last_bilinear;
+        if (secondary || bilinear) {
+            p.u[t] = p.bu[t];  // Tile.restoreDisplacement
+            p.v[t] = p.bv[t];
+        }
+        if (secondary) {
             const int peak = s + 1;
             if ((int)p.npk[t] > peak) {
                 const float2 main = p.puv[(long)t * p.k], sec = p.puv[(long)t * p.k + peak];
-                p.u[t] = __fadd_rn(__fsub_rn(p.u[t], main.x), sec.x);
-                p.v[t] = __fadd_rn(__fsub_rn(p.v[t], main.y), sec.y);
-                set_invalid(p, t, false);
+                const float nu = __fadd_rn(__fsub_rn(p.u[t], main.x), sec.x);
+                const float nv = __fadd_rn(__fsub_rn(p.v[t], main.y), sec.y);
+                if (replace_ok(p, t, nu, nv)) {
+                    p.u[t] = nu;
+                    p.v[t] = nv;
+                    set_invalid(p, t, false);
+                }
             }
-        } else {
+        } else if (bilinear) {
             bilinear_replace(p, t);
         }
-        median_validate(p, t, threshold, eps0);
+        validate_vector(p, t, threshold, eps0);
         if (!is_invalid(p, t)) return true;
     }
     return false;
@@ -275,6 +334,10 @@ __device__ PairView pair_view(const ValidateBufs &b, const ValidateParams &vp, i
     p.state = b.state + base;
     p.tops = b.tops;
     p.lefts = b.lefts;
+    p.model = vp.model;
+    p.clip_n = vp.clip_n;
+    p.clip_h = vp.clip_h;
+    p.clip_w = vp.clip_w;
     return p;
 }
 
@@ -284,9 +347,16 @@ __global__ void validate_init_kernel(ValidateParams vp, ValidateBufs b, int pair
     for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
         const int pair = (int)(idx / cnt), t = (int)(idx - pair * cnt);
         PairView p = pair_view(b, vp, pair);
-        p.state[t] = 0;
-        median_validate(p, t, vp.threshold, vp.epsilon0);
-        if (!is_invalid(p, t)) p.state[t] = kLocked;
+        if (difference_model(p)) {
+            // Every tile starts invalid (the Tile constructors) and the difference validator only
+            // writes a flag when a top-left, top or left neighbour is valid; by induction over the
+            // centre-out visit no tile becomes valid in this pass, whatever the order.
+            p.state[t] = kInvalid;
+        } else {
+            p.state[t] = 0;
+            median_validate(p, t, vp.threshold, vp.epsilon0);  // writes the flag from any state
+            if (!is_invalid(p, t)) p.state[t] = kLocked;
+        }
         b.bu[idx] = p.u[t];  // Tile.backupDisplacement
         b.bv[idx] = p.v[t];
         b.done[idx] = -1;
@@ -385,10 +455,10 @@ __global__ void __launch_bounds__(kSweepThreads) validate_sweep_kernel(ValidateP
             if (!vp.iterate_until_no_corrections && sweeps >= vp.max_iterations) break;
             if (sweeps >= kMaxValidationSweeps) break;  // bound for iterate-until-no-corrections
         }
-        // still-invalid vectors are set to 0 (VectorValidatorJob.java:378-388)
+        // still-invalid vectors are set to 0 (VectorValidatorJob.java:378-388, replaceDisplacement)
         for (int q = tid; q < L; q += T) {
             const int t = list[q];
-            if (p.state[t] & kInvalid) {
+            if ((p.state[t] & kInvalid) && replace_ok(p, t, 0.0f, 0.0f)) {
                 p.u[t] = 0.0f;
                 p.v[t] = 0.0f;
             }

@@ -11,17 +11,19 @@ constexpr int kMaxValidationSweeps = 1000;
 
 struct ValidateParams {
     int ni, nj;          // tiles per axis of one frame
-    int num_peaks;       // k strategies (k - 1 secondary peaks, then bilinear)
+    int num_peaks;       // multi-peak model: k strategies (k - 1 secondary peaks, then bilinear)
     float threshold, epsilon0;
     int max_iterations, iterate_until_no_corrections;
+    int model;           // qlpiv_validation (QLPIV_VALIDATE_MULTIPEAK_MEDIAN .. QLPIV_VALIDATE_MEDIAN)
+    int clip_n, clip_h, clip_w;  // NoOutOfBoundClipping of the replacements (clip_n == 0: allowed)
 };
 
 // Per-level device arrays, [pairs][ni*nj] unless noted.
 struct ValidateBufs {
     float *u, *v;              // accumulated displacements (validated in place)
     float *bu, *bv;            // backups (written)
-    const float2 *peak_uv;     // [pairs][ni*nj][k] peak increments, peak 0 = main
-    const uint8_t *npeaks;     // peaks found per tile
+    const float2 *peak_uv;     // [pairs][ni*nj][k] peak increments, peak 0 = main (multi-peak model)
+    const uint8_t *npeaks;     // peaks found per tile (multi-peak model)
     uint8_t *state;            // bit 0 invalid, bit 1 locked (written)
     const int *tops, *lefts;   // [ni], [nj] tile top / left pixels
     const int *order, *rank;   // [ni*nj] spiral visit order and each tile's rank in it

@@ -1,11 +1,13 @@
 // K1 instantiations (IA side x pixel type) and their launcher; IA 128 runs the two-CTA cluster
 // variant (qlpiv_xcorr_pair.cuh).
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 
 #include "qlpiv_internal.h"
 #include "qlpiv_xcorr.cuh"
 #include "qlpiv_xcorr_pair.cuh"
+#include "qlpiv_xcorr_warp.cuh"
 
 namespace qlpiv {
 
@@ -103,6 +105,45 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
     return cudaGetLastError();
 }
 
+// IA 16: one warp per IA, w16::kWarps warps per CTA, `waves` waves of resident CTAs.
+template <typename Pix, bool PP>
+static cudaError_t launch_warp16(const IaJob &job, cudaStream_t stream, int num_sms) {
+    static std::mutex mu;
+    static int blocks_per_sm[kMaxDevices] = {0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    const size_t base = w16::kWarps * w16::kWarpSmemAligned;
+    int bps;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (blocks_per_sm[dev] == 0) {
+            e = cudaFuncSetAttribute(xcorr16_warp_kernel<Pix, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(base + w16::kWarps * kSubpixSmem));
+            if (e != cudaSuccess) return e;
+            int b = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, xcorr16_warp_kernel<Pix, PP>, w16::kThreads,
+                                                              base);
+            if (e != cudaSuccess) return e;
+            blocks_per_sm[dev] = b < 1 ? 1 : b;
+        }
+        bps = blocks_per_sm[dev];
+    }
+    const cplx *tw = nullptr;
+    if ((e = ensure_twiddles(dev, &tw)) != cudaSuccess) return e;
+    IaJob j = job;
+    j.twiddles = tw + twiddle_offset(32);
+    j.log_tab = log_table(dev);
+    long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? kMultiWaves : 8));
+    const long need = (job.count + w16::kWarps - 1) / w16::kWarps;
+    if (grid > need) grid = need;
+    if (grid < 1) return cudaSuccess;
+    const size_t smem = base + (j.subpix_pixels > 0 ? w16::kWarps * sizeof(float) * 32 * 2 * j.subpix_pixels : 0);
+    xcorr16_warp_kernel<Pix, PP><<<(unsigned)grid, w16::kThreads, smem, stream>>>(j);
+    return cudaGetLastError();
+}
+
 // IA 128: one cluster of two CTAs per IA, one CTA per SM; `waves` clusters per SM pair.
 template <typename Pix, bool PP>
 static cudaError_t launch_pair(const IaJob &job, cudaStream_t stream, int num_sms) {
@@ -153,10 +194,21 @@ static cudaError_t launch_pair(const IaJob &job, cudaStream_t stream, int num_sm
     return cudaGetLastError();
 }
 
+// development switch between two IA-16 kernels (QLPIV_K1_VARIANT=1: the CTA-per-IA kernel)
+static int k1_variant() {
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("QLPIV_K1_VARIANT");
+        v = e ? atoi(e) : 0;
+    }
+    return v;
+}
+
 template <typename Pix, bool PP>
 static cudaError_t launch_pix(const IaJob &job, int n, cudaStream_t stream, int num_sms) {
     switch (n) {
-        case 16: return launch_one<16, Pix, PP>(job, stream, num_sms);
+        case 16: return k1_variant() == 1 ? launch_one<16, Pix, PP>(job, stream, num_sms)
+                                          : launch_warp16<Pix, PP>(job, stream, num_sms);
         case 32: return launch_one<32, Pix, PP>(job, stream, num_sms);
         case 64: return launch_one<64, Pix, PP>(job, stream, num_sms);
         case 128: return launch_pair<Pix, PP>(job, stream, num_sms);

@@ -35,6 +35,7 @@
 //      fit per peak.
 #pragma once
 #include "qlpiv_fft.cuh"
+#include "qlpiv_internal.h"
 #include "qlpiv_logdf.cuh"
 #include "qlpiv.h"
 #include "qlpiv_subpix.cuh"
@@ -121,6 +122,8 @@ struct IaJob {
     qlpiv_vector *out;           // optional per-IA vectors (num_peaks per IA in multi-peak mode)
     float *planes;               // optional (2N-1)^2 planes per IA
     float *acc_u, *acc_v;        // optional: tile displacements += (u, v)  (Tile.accumulateDisplacement)
+    const int *clip_top, *clip_left;  // NoOutOfBoundClipping of the accumulation: per IA tile origin,
+    int clip_n, clip_h, clip_w;       //   tile side and image size (clip_n == 0: clipping allowed)
     int num_peaks;               // 0: FindMaximumFromCenter; k >= 1: FindMaximumMultiPeaks
     int peak_kernel;             // multi-peak cell width
     float2 *peak_uv;             // optional [count][k] displacement increments of every peak
@@ -246,8 +249,13 @@ __device__ void fit_flush(const FitRec *q, const float *fitv, int n, int lane, c
             if (r.slot == 0 && job.npeaks != nullptr) job.npeaks[r.ia] = (uint8_t)r.npk;
         }
         if (job.acc_u != nullptr && r.slot == 0) {
-            job.acc_u[r.ia] += o.u;
-            job.acc_v[r.ia] += o.v;
+            const float nu = job.acc_u[r.ia] + o.u, nv = job.acc_v[r.ia] + o.v;
+            // an increment that would move the tile out of the image is dropped
+            if (job.clip_n == 0 ||
+                tile_inside(job.clip_n, job.clip_h, job.clip_w, job.clip_top[r.ia], job.clip_left[r.ia], nu, nv)) {
+                job.acc_u[r.ia] = nu;
+                job.acc_v[r.ia] = nv;
+            }
         }
     }
     __syncwarp();
@@ -502,7 +510,8 @@ __device__ int mp_replay(const MpGeom &gm, const float *recv, const int *recp, c
 // 32 consecutive records.  KW = cell width, 0 = gm.kw at run time.  All threads.
 template <int D, int T, int KW, typename Plane>
 __device__ __forceinline__ void mp_cells(const MpGeom &gm, const Plane &P, float *recv, int *recp, float *chmax) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // T == 32: one warp works alone on its IA (the warp-per-IA kernel)
+    const int lane = threadIdx.x & 31, warp = T == 32 ? 0 : (int)(threadIdx.x >> 5);
     const int kw = KW > 0 ? KW : gm.kw;
     for (int base = warp * 32; base < gm.nrec; base += T) {
         const int e = base + lane;
@@ -588,16 +597,22 @@ __device__ __forceinline__ void fit_stencil(FitRec &r, const IaJob &job, const P
 // FindMaximumMultiPeaks over a D x D plane read through P(i, j), by a CTA of T threads: the
 // records are staged at `stage` (mp_stage_bytes), the list replayed by warp 0, one fit record
 // queued per slot.
+template <int T>
+__device__ __forceinline__ void group_sync() {
+    if constexpr (T == 32) __syncwarp();
+    else __syncthreads();
+}
+
 template <int D, int T, typename Plane>
 __device__ __forceinline__ void multipeak_core(const IaJob &job, long ia, float minf, const Plane &P, void *stage,
                                                uint64_t *red, FitRec *fitq, float *fitv, int qn, float *mp_lv,
                                                int *mp_li, int *mp_lj) {
     constexpr int NWARPS = T / 32;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lane = threadIdx.x & 31, warp = T == 32 ? 0 : (int)(threadIdx.x >> 5);
     const int multi = job.num_peaks;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
-    __syncthreads();  // plane complete; the FFT scratch is free for the records
+    group_sync<T>();  // plane complete; the FFT scratch is free for the records
     float *redf = reinterpret_cast<float *>(red);
     if (lane == 0) redf[warp] = minf;
     const MpGeom gm = mp_geom(D, job.peak_kernel);
@@ -612,7 +627,7 @@ __device__ __forceinline__ void multipeak_core(const IaJob &job, long ia, float 
     } else {
         mp_cells<D, T, 0>(gm, P, recv, recp, chmax);
     }
-    __syncthreads();
+    group_sync<T>();
     if (warp == 0) {
         float mn = lane < NWARPS ? redf[lane] : 3.402823466e38f;
 #pragma unroll

@@ -27,6 +27,18 @@ def _java_round(x):
     return np.floor(x + np.float32(0.5)).astype(np.int32)
 
 
+def clip_inside(tops, lefts, n, h, w, u, v):
+    """Tile.accumulateDisplacement / replaceDisplacement bounds under NoOutOfBoundClipping
+    (S/iareas/Tile.java:103-136): per tile of the (tops x lefts) grid, whether (u, v) rounded
+    (floor(x + 0.5f)) keeps the tile inside the h x w image by the reference's test."""
+    ru = np.floor(u + np.float32(0.5))
+    rv = np.floor(v + np.float32(0.5))
+    t = np.asarray(tops, np.float32)[:, None]
+    l_ = np.asarray(lefts, np.float32)[None, :]
+    return ~((t + ru < 0) | (t + np.float32(n) + ru >= np.float32(h)) | (l_ + rv < 0) |
+             (l_ + np.float32(n) + rv >= np.float32(w)))
+
+
 def gpu_trace(qp, handle, img_a, img_b, desc):
     """Per-level records of the adaptive loop run through the library's stage calls."""
     a = np.ascontiguousarray(img_a)
@@ -35,9 +47,11 @@ def gpu_trace(qp, handle, img_a, img_b, desc):
     levels = qp.adaptive_levels(desc, h, w)
     fm = desc.fixed_max if desc.fixed_max > 0 else (255.0 if a.dtype == np.uint8 else 65535.0)
     validate = desc.validation != 0
+    multi = desc.validation == qp.VALIDATE_MULTIPEAK_MEDIAN
+    clip = desc.clipping_mode == qp.CLIP_NO_OUT_OF_BOUND
     pass_kw = dict(norm_mode=desc.norm_mode, max_mode=desc.max_mode, fixed_max=(fm, fm),
                    subpix_mode=desc.subpix_mode)
-    if validate:
+    if multi:
         pass_kw.update(num_peaks=desc.num_peaks, peak_kernel=desc.peak_kernel)
     warp = desc.warp_mode == qp.WARP_BOTH_BILINEAR
     assert desc.warp_mode in (qp.WARP_NONE, qp.WARP_BOTH_BILINEAR) and desc.inherit_mode == 0
@@ -57,6 +71,13 @@ def gpu_trace(qp, handle, img_a, img_b, desc):
         else:
             u0, v0 = handle.inherit(prev["cy"], prev["cx"], prev["u"], prev["v"], cy, cx,
                                     round_int=not warp)
+            rec["u_inh"], rec["v_inh"] = u0, v0
+            if clip:   # the new tiles take the inherited value through accumulateDisplacement
+                u0 = np.float32(0.0) + u0
+                v0 = np.float32(0.0) + v0
+                ok = clip_inside(tops, lefts, n, h, w, u0, v0)
+                u0 = np.where(ok, u0, np.float32(0.0)).astype(np.float32)
+                v0 = np.where(ok, v0, np.float32(0.0)).astype(np.float32)
         rec["u_in"], rec["v_in"] = u0, v0
         at = np.repeat(tops, nj)
         al = np.tile(lefts, ni)
@@ -75,14 +96,22 @@ def gpu_trace(qp, handle, img_a, img_b, desc):
         main = vec[:, 0]
         ua = (u0.ravel() + main["u"]).reshape(ni, nj).astype(np.float32)
         va = (v0.ravel() + main["v"]).reshape(ni, nj).astype(np.float32)
+        if clip:   # accumulateDisplacement drops an increment that moves the tile out of the image
+            ok = clip_inside(tops, lefts, n, h, w, ua, va)
+            ua = np.where(ok, ua, u0)
+            va = np.where(ok, va, v0)
         rec["u_acc"], rec["v_acc"] = ua, va
         if validate:
-            present = (vec["flags"] & qp.F_ABSENT) == 0
-            npk = present.sum(axis=1).astype(np.int32).reshape(ni, nj)
-            k = desc.num_peaks
+            if multi:
+                present = (vec["flags"] & qp.F_ABSENT) == 0
+                npk = present.sum(axis=1).astype(np.int32).reshape(ni, nj)
+                k = desc.num_peaks
+                pk = (vec["u"].reshape(ni, nj, k), vec["v"].reshape(ni, nj, k), npk)
+            else:
+                npk = np.ones((ni, nj), np.int32)
+                pk = (None, None, None)
             rec["npk"] = npk
-            u, v, inv = handle.validate(tops, lefts, ua, va, vec["u"].reshape(ni, nj, k),
-                                        vec["v"].reshape(ni, nj, k), npk, desc)
+            u, v, inv = handle.validate(tops, lefts, ua, va, *pk, desc, n=n, height=h, width=w)
         else:
             u, v, inv = ua, va, np.zeros((ni, nj), np.uint8)
         rec["u"], rec["v"], rec["invalid"] = u, v, inv
@@ -106,7 +135,7 @@ def compare_pass(oracle, rec, desc, fixed, nthreads=None):
     n = rec["n"]
     vec = rec["vec"]
     k = vec.shape[1]
-    if k > 1 or desc.validation:
+    if desc.validation == 1:
         ref, npk = oracle.piv_pass_multi(rec["wa"], rec["wb"], n, rec["at"], rec["al"], rec["bt"], rec["bl"],
                                          norm_mode=oracle.NORM_FIXED if fixed else oracle.NORM_MAX_A,
                                          fixed_max=fixed or (255.0, 255.0), precision=64,
@@ -147,13 +176,46 @@ def compare_pass(oracle, rec, desc, fixed, nthreads=None):
         same[ia, :] = False
     cmp = same & ~border
     err = np.maximum(np.abs(vec["u"].astype(np.float64) - ref["u64"]), np.abs(vec["v"].astype(np.float64) - ref["v64"]))
+    # A flat peak (a weak secondary peak) magnifies the plane's rounding through the fit: such a
+    # slot may exceed 1e-3 px, but never the error that the plane tolerance (1e-5 of the plane
+    # maximum) propagates through the 3-point fit's derivatives at the FP64 stencil.
+    flat = 0
+    for ia, sl in np.argwhere(cmp & (err > SUBPIX_TOL)):
+        p = _tile_planes64(oracle, rec["wa"], rec["wb"], n, rec["at"], rec["al"], rec["bt"], rec["bl"], ia, fixed)
+        bound = gauss3_error_bound(p, int(ri[ia, sl, 0]), int(ri[ia, sl, 1]), 1e-5 * float(np.abs(p).max()))
+        if not err[ia, sl] <= max(SUBPIX_TOL, bound):
+            raise AssertionError(f"level {rec['level']} IA {ia} slot {sl}: sub-pixel error {err[ia, sl]:.3e} px "
+                                 f"(conditioning bound {bound:.3e})")
+        flat += 1
+        cmp[ia, sl] = False
     worst = float(err[cmp].max(initial=0.0))
-    if worst > SUBPIX_TOL:
-        ia, s = np.argwhere(cmp & (err == worst))[0]
-        raise AssertionError(f"level {rec['level']} IA {ia} slot {s}: sub-pixel error {worst:.3e} px")
     return {"level": rec["level"], "n": n, "ias": int(vec.shape[0]), "slots": int(cmp.size),
             "compared": int(cmp.sum()), "tie_ias": ties, "border": int((same & border).sum()),
-            "max_err_px": worst, "p99_err_px": float(np.quantile(err[cmp], 0.99)) if cmp.any() else 0.0}
+            "flat_peaks": flat, "max_err_px": worst,
+            "p99_err_px": float(np.quantile(err[cmp], 0.99)) if cmp.any() else 0.0}
+
+
+def gauss3_error_bound(plane, i, j, eps):
+    """Largest change of the 3-point Gaussian (or parabolic fallback) sub-pixel position of the
+    peak at (i, j) when every stencil value moves by up to eps: first-order, summed over the
+    three values of each axis (Gaussian1DPolynomialInterpolator's formulas, +1e-8 included)."""
+    d = plane.shape[0]
+    if i < 1 or j < 1 or i + 1 >= d or j + 1 >= d:
+        return 0.0
+    worst = 0.0
+    for ys in ((plane[i - 1, j], plane[i, j], plane[i + 1, j]), (plane[i, j - 1], plane[i, j], plane[i, j + 1])):
+        y = np.asarray(ys, np.float64) + 1e-8
+        if (y > 0).all():
+            lg = np.log(y)
+            num = lg[0] - lg[2]
+            den = 2 * lg[0] - 4 * lg[1] + 2 * lg[2]
+            g = np.array([(den - 2 * num) / den ** 2, 4 * num / den ** 2, (-den - 2 * num) / den ** 2]) / y
+        else:
+            num = y[0] - y[2]
+            den = 2 * y[0] - 4 * y[1] + 2 * y[2]
+            g = np.array([(den - 2 * num) / den ** 2, 4 * num / den ** 2, (-den - 2 * num) / den ** 2])
+        worst = max(worst, float(np.abs(g).sum()) * eps)
+    return worst
 
 
 def check_stages(qp, oracle, recs, desc, cfg=None, nthreads=None):
@@ -171,7 +233,7 @@ def check_stages(qp, oracle, recs, desc, cfg=None, nthreads=None):
         if prev is not None:
             ou, ov = oracle.inherit(prev["cy"].astype(np.float64), prev["cx"].astype(np.float64), prev["u"], prev["v"],
                                     rec["cy"], rec["cx"], not warp)
-            assert ou.tobytes() == rec["u_in"].tobytes() and ov.tobytes() == rec["v_in"].tobytes(), \
+            assert ou.tobytes() == rec["u_inh"].tobytes() and ov.tobytes() == rec["v_inh"].tobytes(), \
                 f"level {rec['level']}: inheritance differs from the oracle"
             if warp:
                 ys = rec["cy"].astype(np.float64)
@@ -191,9 +253,12 @@ def check_stages(qp, oracle, recs, desc, cfg=None, nthreads=None):
         if desc.validation and cfg is not None:
             k = rec["vec"].shape[1]
             ni, nj = rec["u_acc"].shape
+            lcfg = type(cfg).from_buffer_copy(cfg)
+            if desc.clipping_mode == 2:
+                lcfg.clip_n, lcfg.clip_h, lcfg.clip_w = rec["n"], h, w
             vu, vv, vinv, _ = oracle.validate(rec["tops"], rec["lefts"], rec["u_acc"], rec["v_acc"],
-                                           rec["vec"]["u"].reshape(ni, nj, k), rec["vec"]["v"].reshape(ni, nj, k),
-                                           rec["npk"], cfg)
+                                              rec["vec"]["u"].reshape(ni, nj, k), rec["vec"]["v"].reshape(ni, nj, k),
+                                              rec["npk"], lcfg)
             assert vu.tobytes() == rec["u"].tobytes() and vv.tobytes() == rec["v"].tobytes(), \
                 f"level {rec['level']}: validated field differs from the oracle validator"
             assert np.array_equal(vinv.astype(bool), rec["invalid"].astype(bool))
@@ -209,8 +274,9 @@ def oracle_levels(oracle, img_a, img_b, recs, desc, sched, cfg=None, fixed_max=N
     origins), accumulated and final (u, v), main peaks.  The rebuilt accumulation is checked
     against the pipeline's own vectors, so the intermediates are the pipeline's."""
     n0, n1, ofac = sched
+    clip = desc.clipping_mode == 2
     res = oracle.piv_adaptive(img_a, img_b, n0, n1, ofac, fixed_max=fixed_max, precision=64, validation=cfg,
-                              return_levels=True, warp=warp)
+                              return_levels=True, warp=warp, clip_mode=desc.clipping_mode)
     vec = res[1]
     luv = res[2] if cfg is not None else None
     h, w = img_a.shape
@@ -227,6 +293,10 @@ def oracle_levels(oracle, img_a, img_b, recs, desc, sched, cfg=None, fixed_max=N
         else:
             u_in, v_in = oracle.inherit(prev["cy"].astype(np.float64), prev["cx"].astype(np.float64), prev["u"],
                                         prev["v"], rec["cy"], rec["cx"], not warp, precision=64)
+            if clip:
+                ok = clip_inside(rec["tops"], rec["lefts"], rec["n"], h, w, u_in, v_in)
+                u_in = np.where(ok, np.float32(0.0) + u_in, np.float32(0.0)).astype(np.float32)
+                v_in = np.where(ok, np.float32(0.0) + v_in, np.float32(0.0)).astype(np.float32)
         lv["u_in"], lv["v_in"] = u_in, v_in
         wa, wb = img_a, img_b
         if warp and prev is not None:
@@ -242,6 +312,11 @@ def oracle_levels(oracle, img_a, img_b, recs, desc, sched, cfg=None, fixed_max=N
         lv["peak"] = np.stack([v0["peak_i"], v0["peak_j"]], -1)
         ua = (u_in.ravel().astype(np.float64) + v0["u64"]).astype(np.float32).reshape(ni, nj)
         va = (v_in.ravel().astype(np.float64) + v0["v64"]).astype(np.float32).reshape(ni, nj)
+        lv["u_acc_raw"], lv["v_acc_raw"] = ua, va
+        if clip:
+            ok = clip_inside(rec["tops"], rec["lefts"], rec["n"], h, w, ua, va)
+            ua = np.where(ok, ua, u_in)
+            va = np.where(ok, va, v_in)
         lv["u_acc"], lv["v_acc"] = ua, va
         if luv is not None:
             lv["u"] = luv[2 * off:2 * off + cnt].reshape(ni, nj)
@@ -277,7 +352,16 @@ def cascade_report(recs, olv, desc, tol=1e-3, same_in=1e-4):
         tie = (gpeak != lv["peak"]).any(-1)
         pix_a = rec["wa"] != lv["wa"]
         pix_b = rec["wb"] != lv["wb"]
-        causes = {"inherited": 0, "pixels": 0, "validation": 0, "tie": 0, "unexplained": 0}
+        refusal_flip = np.zeros(err.size, bool)
+        if desc.clipping_mode == 2:
+            # NoOutOfBoundClipping: the two runs refused the increment differently (its rounded
+            # sum sits on a .5 boundary)
+            ng_u = (rec["u_in"].ravel() + rec["vec"]["u"][:, 0]).reshape(rec["u_in"].shape)
+            ng_v = (rec["v_in"].ravel() + rec["vec"]["v"][:, 0]).reshape(rec["u_in"].shape)
+            ok_g = clip_inside(rec["tops"], rec["lefts"], n, h, w, ng_u, ng_v)
+            ok_o = clip_inside(rec["tops"], rec["lefts"], n, h, w, lv["u_acc_raw"], lv["v_acc_raw"])
+            refusal_flip = (ok_g != ok_o).ravel()
+        causes = {"inherited": 0, "pixels": 0, "validation": 0, "tie": 0, "clipping": 0, "unexplained": 0}
         unexplained = []
         for k in np.nonzero(err > tol)[0]:
             t, l_ = int(rec["at"][k]), int(rec["al"][k])
@@ -291,6 +375,8 @@ def cascade_report(recs, olv, desc, tol=1e-3, same_in=1e-4):
                 causes["pixels"] += 1
             elif replaced[k]:
                 causes["validation"] += 1
+            elif refusal_flip[k]:
+                causes["clipping"] += 1
             elif tie[k]:
                 causes["tie"] += 1
             else:

@@ -29,7 +29,7 @@ def test_library_exports_header_symbols(qp):
     for s in syms:
         assert hasattr(lib, s), s
     assert sorted(qp.exported_symbols()) == syms
-    assert qp.load_library().qlpiv_abi_version() == 3
+    assert qp.load_library().qlpiv_abi_version() == 4
 
 
 def test_ctypes_structs_match_header(qp, tmp_path):

@@ -232,3 +232,73 @@ def test_mini_warp_of_a_uniform_field_equals_micro(oracle):
         r2 = oracle.tile_warp(a, b, n, tops, lefts, u, v, mini, 4095.0)
         for x, y in zip(r1, r2):
             np.testing.assert_array_equal(x, y)
+
+
+# ---- the four single-strategy models and NoOutOfBoundClipping of the replacements ----
+
+def _clip_geometry(tops, lefts, n=16):
+    """An image whose last tile row touches the bottom edge and whose last column ends 2 px
+    inside the right edge, so that replacements near the borders are refused."""
+    return n, int(tops[-1]) + n, int(lefts[-1]) + n + 2
+
+
+@pytest.mark.parametrize("model", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("clip", [False, True])
+@pytest.mark.parametrize("seed", range(4))
+def test_validation_models_match_independent_restatement(oracle, model, clip, seed):
+    rng = np.random.default_rng(100 + seed * 7 + model)
+    k = 3 if model == 1 else 1
+    ni, nj = [(9, 11), (12, 12), (5, 7), (16, 13)][seed]
+    tops, lefts, u, v, pu, pv, npk, _, _ = smooth_case(rng, ni, nj, k, [3, 8, 20, 1][seed])
+    geo = _clip_geometry(tops, lefts) if clip else None
+    thr = 1.5 if model in (2, 3) else 2.0
+    cfg = oracle.valid_cfg(num_peaks=k, threshold=thr, epsilon0=0.1, max_iterations=2, model=model, clip=geo)
+    gu, gv, ginv, gs = oracle.validate(tops, lefts, u, v, pu, pv, npk, cfg)
+    eu, ev, einv, es = vref.validate(tops, lefts, u, v, pu, pv, npk, k, thr, 0.1, 2, False, model=model, clip=geo)
+    assert gs == es
+    np.testing.assert_array_equal(ginv, einv)
+    np.testing.assert_array_equal(gu.view(np.uint32), eu.view(np.uint32))
+    np.testing.assert_array_equal(gv.view(np.uint32), ev.view(np.uint32))
+
+
+def test_difference_models_never_validate(oracle):
+    """Every tile starts invalid and the difference validator only looks at valid top-left, top
+    and left neighbours, so no tile is ever validated: every vector ends at 0, except where
+    NoOutOfBoundClipping refuses the 0 (tiles touching the bottom edge keep their value)."""
+    rng = np.random.default_rng(3)
+    tops, lefts, u, v, pu, pv, npk, _, _ = smooth_case(rng, 9, 10, 1, 0)
+    for model in (2, 3):
+        gu, gv, inv, sweeps = oracle.validate(tops, lefts, u, v, pu, pv, npk, oracle.valid_cfg(model=model))
+        assert inv.all() and not gu.any() and not gv.any() and sweeps == 1
+        geo = _clip_geometry(tops, lefts)
+        cu, cv, inv, _ = oracle.validate(tops, lefts, u, v, pu, pv, npk, oracle.valid_cfg(model=model, clip=geo))
+        assert inv.all()
+        assert np.array_equal(cu[-1], u[-1]) and np.array_equal(cv[-1], v[-1])   # 0 refused on the last row
+        assert not cu[:-1].any() and not cv[:-1].any()
+
+
+def test_median_only_zeroes_without_replacing(oracle):
+    rng = np.random.default_rng(4)
+    tops, lefts, u, v, pu, pv, npk, tu, tv = smooth_case(rng, 12, 12, 1, 6)
+    ou, ov, inv, _ = oracle.validate(tops, lefts, u, v, pu, pv, npk, oracle.valid_cfg(model=4))
+    assert inv.sum() >= 6
+    assert not ou[inv.astype(bool)].any()
+    assert np.array_equal(ou[~inv.astype(bool)], u[~inv.astype(bool)])
+    bu, bv, binv, _ = oracle.validate(tops, lefts, u, v, pu, pv, npk, oracle.valid_cfg(model=5))
+    assert binv.sum() < inv.sum()                     # bilinear replacement repairs most of them
+    fixed = inv.astype(bool) & ~binv.astype(bool)
+    assert np.abs(bu[fixed] - tu[fixed]).max() < 1.0
+
+
+def test_clipping_refuses_replacements_that_leave_the_image(oracle):
+    """Bilinear replacement of an outlier on the bottom row under NoOutOfBoundClipping: the value
+    is refused (the tile touches the bottom edge), the revalidation finds the outlier again, and
+    the final zeroing is refused too: the vector keeps its value and stays invalid."""
+    rng = np.random.default_rng(9)
+    tops, lefts, u, v, pu, pv, npk, _, _ = smooth_case(rng, 8, 8, 1, 0)
+    u[-1, 3] += 7.0
+    geo = _clip_geometry(tops, lefts)
+    au, av, ainv, _ = oracle.validate(tops, lefts, u, v, pu, pv, npk, oracle.valid_cfg(model=5))
+    cu, cv, cinv, _ = oracle.validate(tops, lefts, u, v, pu, pv, npk, oracle.valid_cfg(model=5, clip=geo))
+    assert abs(au[-1, 3] - u[-1, 3]) > 5.0            # allowed: replaced by the neighbours' estimate
+    assert cu[-1, 3] == u[-1, 3] and cinv[-1, 3]      # every replacement refused

@@ -8,6 +8,8 @@ Written from the reference sources (S/ = src/main/java/pt/quickLabPIV/):
   * NormalizedMedianValidator.validateVector    S/iareas/validation/NormalizedMedianValidator.java:63-136
   * SecondaryPeakReplacement.replaceVector      S/iareas/replacement/SecondaryPeakReplacement.java:41-76
   * BilinearReplacement.replaceVector           S/iareas/replacement/BilinearReplacement.java:23-420
+  * DifferenceValidator.validateVector          S/iareas/validation/DifferenceValidator.java:30-60
+  * Tile constructors, replaceDisplacement      S/iareas/Tile.java:51-67, 156-189
 Float arithmetic is carried out with numpy float32 scalars so every rounding step is
 Java's single precision.
 """
@@ -139,11 +141,24 @@ def spiral_order(ni, nj):
 
 
 class _Tile:
-    __slots__ = ("i", "j", "top", "left", "u", "v", "bu", "bv", "invalid", "locked")
+    __slots__ = ("i", "j", "top", "left", "u", "v", "bu", "bv", "invalid", "locked", "clip")
 
     def set_invalid(self, state):
         if not self.locked:
             self.invalid = state
+
+    def replace(self, u, v):
+        """Tile.replaceDisplacement: under NoOutOfBoundClipping (clip = (n, h, w)) a displacement
+        whose rounded value moves the tile out of the image is refused."""
+        if self.clip is not None:
+            n, h, w = self.clip
+            ru = f32(math.floor(f32(u + f32(0.5))))
+            rv = f32(math.floor(f32(v + f32(0.5))))
+            if (f32(self.top) + ru < 0 or f32(self.top + n) + ru >= h or f32(self.left) + rv < 0 or
+                    f32(self.left + n) + rv >= w):
+                return False
+        self.u, self.v = f32(u), f32(v)
+        return True
 
 
 def _neighbours(tiles, ti, tj):
@@ -182,6 +197,20 @@ def _median_validate(t, nb, threshold, eps0):
     du, dv = f32(mu - t.u), f32(mv - t.v)
     dist = f32(f32(math.sqrt(f32(du * du + dv * dv))) / f32(rmed + f32(eps0)))
     t.set_invalid(not (dist < f32(threshold)))
+
+
+def _difference_validate(t, nb, threshold):
+    """adjacents [0][0], [0][1], [1][0]: each valid neighbour overwrites the flag."""
+    t2 = f32(f32(threshold) * f32(threshold))
+    for a in range(2):
+        for b in range(2):
+            if a == 1 and b == 1:
+                continue
+            x = nb[a][b]
+            if x is None or x.invalid:
+                continue
+            du, dv = f32(x.u - t.u), f32(x.v - t.v)
+            t.set_invalid(not (f32(du * du + dv * dv) < t2))
 
 
 def _interp(p1, p2, pi, a1, a2):
@@ -245,8 +274,7 @@ def _bilinear(t, nb):
                     break
         if pick is None:
             t.set_invalid(True)
-        else:
-            t.u, t.v = pick.u, pick.v
+        elif t.replace(pick.u, pick.v):
             t.set_invalid(False)
         return
     # classification-weighted mean over the four candidate slots (empty slots weigh 0)
@@ -259,13 +287,16 @@ def _bilinear(t, nb):
         wv += cv
         au = f32(au + f32(f32(cu) * uu))
         wu += cu
-    t.u = f32(au / f32(wu))
-    t.v = f32(av / f32(wv))
+    t.replace(f32(au / f32(wu)), f32(av / f32(wv)))
     t.set_invalid(False)
 
 
 def validate(tops, lefts, u, v, peak_u, peak_v, npeaks, num_peaks, threshold, eps0, max_iterations,
-             iterate_until=False):
+             iterate_until=False, model=1, clip=None):
+    """model 1: multi-peak normalised median (num_peaks strategies: secondary peaks, then
+    bilinear); 2 / 3: difference validator without / with bilinear replacement; 4 / 5:
+    normalised median without / with bilinear replacement.  clip: None or (n, h, w) for
+    NoOutOfBoundClipping of the replacements."""
     ni, nj = u.shape
     tiles = [[None] * nj for _ in range(ni)]
     for i in range(ni):
@@ -274,13 +305,26 @@ def validate(tops, lefts, u, v, peak_u, peak_v, npeaks, num_peaks, threshold, ep
             t.i, t.j, t.top, t.left = i, j, int(tops[i]), int(lefts[j])
             t.u, t.v = f32(u[i, j]), f32(v[i, j])
             t.bu, t.bv = t.u, t.v
-            t.invalid = False
+            t.invalid = True          # Tile constructors
             t.locked = False
+            t.clip = clip
             tiles[i][j] = t
+    strategies = []               # (replacement) per strategy: "peak<p>", "bilinear" or None
+    if model == 1:
+        strategies = [f"peak{s + 1}" for s in range(num_peaks - 1)] + ["bilinear"]
+    else:
+        strategies = ["bilinear" if model in (3, 5) else None]
+
+    def check(t, nb):
+        if model in (2, 3):
+            _difference_validate(t, nb, threshold)
+        else:
+            _median_validate(t, nb, threshold, eps0)
+
     order = spiral_order(ni, nj)
     for k in order:
         t = tiles[k // nj][k % nj]
-        _median_validate(t, _neighbours(tiles, t.i, t.j), threshold, eps0)
+        check(t, _neighbours(tiles, t.i, t.j))
         if not t.invalid:
             t.locked = True
     attempt = 0
@@ -289,24 +333,25 @@ def validate(tops, lefts, u, v, peak_u, peak_v, npeaks, num_peaks, threshold, ep
         for k in order:
             t = tiles[k // nj][k % nj]
             nb = _neighbours(tiles, t.i, t.j)
-            _median_validate(t, nb, threshold, eps0)
-            s = 0
-            while s < num_peaks and t.invalid:
-                t.u, t.v = t.bu, t.bv
-                if s < num_peaks - 1:
-                    p = s + 1
-                    if npeaks[t.i, t.j] > p:
-                        nu = f32(f32(t.u - f32(peak_u[t.i, t.j, 0])) + f32(peak_u[t.i, t.j, p]))
-                        nv = f32(f32(t.v - f32(peak_v[t.i, t.j, 0])) + f32(peak_v[t.i, t.j, p]))
-                        t.u, t.v = nu, nv
-                        t.set_invalid(False)
-                else:
-                    _bilinear(t, nb)
-                _median_validate(t, nb, threshold, eps0)
+            check(t, nb)
+            for repl in strategies:
+                if not t.invalid:
+                    break
+                if repl is not None:
+                    t.u, t.v = t.bu, t.bv          # restoreDisplacement
+                    if repl == "bilinear":
+                        _bilinear(t, nb)
+                    else:
+                        p = int(repl[4:])
+                        if npeaks[t.i, t.j] > p:
+                            nu = f32(f32(t.u - f32(peak_u[t.i, t.j, 0])) + f32(peak_u[t.i, t.j, p]))
+                            nv = f32(f32(t.v - f32(peak_v[t.i, t.j, 0])) + f32(peak_v[t.i, t.j, p]))
+                            if t.replace(nu, nv):
+                                t.set_invalid(False)
+                check(t, nb)
                 if not t.invalid:
                     corrected += 1
                     break
-                s += 1
         attempt += 1
         if corrected == 0 or (not iterate_until and attempt >= max_iterations) or attempt >= 1000:
             break
@@ -317,6 +362,6 @@ def validate(tops, lefts, u, v, peak_u, peak_v, npeaks, num_peaks, threshold, ep
         for j in range(nj):
             t = tiles[i][j]
             if t.invalid:
-                t.u = t.v = f32(0)
+                t.replace(f32(0), f32(0))
             ou[i, j], ov[i, j], inv[i, j] = t.u, t.v, int(t.invalid)
     return ou, ov, inv, attempt
