@@ -513,14 +513,18 @@ __device__ __forceinline__ void mp_cells(const MpGeom &gm, const Plane &P, float
     // T == 32: one warp works alone on its IA (the warp-per-IA kernel)
     const int lane = threadIdx.x & 31, warp = T == 32 ? 0 : (int)(threadIdx.x >> 5);
     const int kw = KW > 0 ? KW : gm.kw;
-    for (int base = warp * 32; base < gm.nrec; base += T) {
+    // with a compile-time cell width the geometry is constant: no run-time division
+    constexpr int kTop = KW > 0 ? ((D + KW - 1) / KW) - ((D + KW - 1) / KW) / 2 : 1;
+    const int top = KW > 0 ? kTop : gm.top;
+    const int nrec = KW > 0 ? 4 * kTop * kTop : gm.nrec;
+    for (int base = warp * 32; base < nrec; base += T) {
         const int e = base + lane;
         float bv = 0.0f;
-        if (e < gm.nrec) {
+        if (e < nrec) {
             int bp = -1;
             const int sl = e >> 2, q = e & 3;
-            const int ci = sl / gm.top + ((q & 2) ? gm.top : 0);
-            const int cj = sl % gm.top + ((q & 1) ? gm.top : 0);
+            const int ci = (KW > 0 ? sl / kTop : sl / top) + ((q & 2) ? top : 0);
+            const int cj = (KW > 0 ? sl % kTop : sl % top) + ((q & 1) ? top : 0);
             const int i0 = ci * kw, j0 = cj * kw;
             if (KW > 0) {
 #pragma unroll
