@@ -29,9 +29,10 @@
  *            normalised-median validation after every level (qlpiv_oracle_validate.c).
  *
  * The reference evaluates both interpolators in double.  The FP32 pipeline here
- * evaluates them in float (spline knot derivatives still solved in double), the
- * formulation of the CUDA kernels, so the GPU stages can be checked bit for bit; the
- * FP64 twin evaluates them in double.
+ * evaluates them in float (spline knot derivatives solved in double-word arithmetic with
+ * precomputed reciprocals of the knot steps, then rounded to float), the formulation of
+ * the CUDA kernels, so the GPU stages can be checked bit for bit; the FP64 twin evaluates
+ * them in double with the divisions of the mathematical definition.
  */
 #define _GNU_SOURCE
 #include <math.h>
@@ -40,6 +41,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "oracle_dword.h"
 #include "oracle_types.h"
 
 /* ---------------- natural cubic spline: first derivative at every knot ---------------- */
@@ -68,9 +70,96 @@ static void natural_spline_deriv(const double *x, const double *y, long ys, int 
     free(m); free(cp); free(dp);
 }
 
+/* The float path's formulation of the same solve (the CUDA kernels'): per-axis factors computed
+ * once per grid in double, kf holding 6 arrays of n:
+ *   h[i] = x[i+1] - x[i], ih[i] = 1 / h[i], h6[i] = h[i] / 6                        (i < n-1)
+ *   den[i] = 2 (h[i-1] + h[i]) - h[i-1] cp[i-1], cp[i] = h[i] / den[i], iden[i] = 1 / den[i]
+ *   rc[i] = 1 / (x[min(i+1, n-1)] - x[max(i-1, 0)])                 (cross-derivative steps)
+ * rounded to double-words, and line solves that multiply by them in double-word arithmetic
+ * (oracle_dword.h, ~44 bits), each derivative rounded to float. */
+enum { KF_H = 0, KF_IH, KF_H6, KF_CP, KF_IDEN, KF_RC, KF_ARRAYS };
+
+static void knot_factors(const double *x, int n, double *kf) {
+    double *h = kf + KF_H * n, *ih = kf + KF_IH * n, *h6 = kf + KF_H6 * n;
+    double *cp = kf + KF_CP * n, *iden = kf + KF_IDEN * n, *rc = kf + KF_RC * n;
+    for (int k = 0; k < KF_ARRAYS * n; k++) kf[k] = 0.0;
+    for (int i = 0; i + 1 < n; i++) {
+        h[i] = x[i + 1] - x[i];
+        ih[i] = 1.0 / h[i];
+        h6[i] = h[i] / 6.0;
+    }
+    for (int i = 1; i + 1 < n; i++) {
+        const double den = 2.0 * (h[i - 1] + h[i]) - h[i - 1] * cp[i - 1];
+        cp[i] = h[i] / den;
+        iden[i] = 1.0 / den;
+    }
+    for (int i = 0; i < n; i++) {
+        const int nx = i + 1 < n ? i + 1 : n - 1, pv = i - 1 >= 0 ? i - 1 : 0;
+        rc[i] = 1.0 / (x[nx] - x[pv]);
+    }
+}
+
+static orc_dw *knot_factors_dw(const double *x, int n) {
+    double *kf = (double *)malloc(sizeof(double) * KF_ARRAYS * (size_t)n);
+    orc_dw *out = (orc_dw *)malloc(sizeof(orc_dw) * KF_ARRAYS * (size_t)n);
+    knot_factors(x, n, kf);
+    for (int k = 0; k < KF_ARRAYS * n; k++) out[k] = dw_of(kf[k]);
+    free(kf);
+    return out;
+}
+
+/* Values y (float) along one line with stride ys:
+ *   s[i]  = (y[i+1] - y[i]) ih[i]          (the float difference is exact as a double-word)
+ *   m[i]  = dp[i] = (6 (s[i] - s[i-1]) - h[i-1] dp[i-1]) iden[i],   dp[0] = 0
+ *   m[i]  = dp[i] - cp[i] m[i+1],   m[0] = m[n-1] = 0
+ *   d[i]  = s[i] - h6[i] (2 m[i] + m[i+1]),   d[n-1] = s[n-2] + h6[n-2] (m[n-2] + 2 m[n-1]) */
+static void natural_spline_deriv_dw(const orc_dw *kf, const float *y, long ys, int n, float *d) {
+    const orc_dw *h = kf + KF_H * n, *ih = kf + KF_IH * n, *h6 = kf + KF_H6 * n;
+    const orc_dw *cp = kf + KF_CP * n, *iden = kf + KF_IDEN * n;
+    const orc_dw zero = {0.0f, 0.0f};
+    orc_dw *m = (orc_dw *)calloc((size_t)n, sizeof(orc_dw));
+    orc_dw *s = (orc_dw *)calloc((size_t)n, sizeof(orc_dw));
+    for (int i = 0; i + 1 < n; i++) s[i] = dw_mul(dw_two_sum(y[(i + 1) * ys], -y[i * ys]), ih[i]);
+    for (int i = 1; i < n - 1; i++)
+        m[i] = dw_mul(dw_sub(dw_mul_f(dw_sub(s[i], s[i - 1]), 6.0f), dw_mul(h[i - 1], m[i - 1])), iden[i]);
+    for (int i = n - 2; i >= 1; i--) m[i] = dw_sub(m[i], dw_mul(cp[i], m[i + 1]));
+    m[0] = zero;
+    m[n - 1] = zero;
+    for (int i = 0; i < n - 1; i++) d[i] = dw_float(dw_sub(s[i], dw_mul(h6[i], dw_add(dw_twice(m[i]), m[i + 1]))));
+    d[n - 1] = dw_float(dw_add(s[n - 2], dw_mul(h6[n - 2], dw_add(m[n - 2], dw_twice(m[n - 1])))));
+    free(m); free(s);
+}
+
+/* Float path of bicubic_nodes: f and the node quadruples in float. */
+static void bicubic_nodes_dw(const double *ys, int ni, const double *xs, int nj, const float *f, float *c4) {
+    const size_t nn = (size_t)ni * nj;
+    orc_dw *kfy = knot_factors_dw(ys, ni), *kfx = knot_factors_dw(xs, nj);
+    float *tmp = (float *)malloc(sizeof(float) * (ni > nj ? ni : nj));
+    for (size_t k = 0; k < nn; k++) c4[4 * k] = f[k];
+    for (int j = 0; j < nj; j++) {
+        natural_spline_deriv_dw(kfy, f + j, nj, ni, tmp);
+        for (int i = 0; i < ni; i++) c4[4 * ((size_t)i * nj + j) + 1] = tmp[i];
+    }
+    for (int i = 0; i < ni; i++) {
+        natural_spline_deriv_dw(kfx, f + (size_t)i * nj, 1, nj, tmp);
+        for (int j = 0; j < nj; j++) c4[4 * ((size_t)i * nj + j) + 2] = tmp[j];
+    }
+    for (int i = 0; i < ni; i++) {
+        const int ni_ = i + 1 < ni ? i + 1 : ni - 1, pi = i - 1 >= 0 ? i - 1 : 0;
+        for (int j = 0; j < nj; j++) {
+            const int nj_ = j + 1 < nj ? j + 1 : nj - 1, pj = j - 1 >= 0 ? j - 1 : 0;
+            orc_dw t = dw_two_sum(f[(size_t)ni_ * nj + nj_], -f[(size_t)ni_ * nj + pj]);
+            t = dw_add_f(t, -f[(size_t)pi * nj + nj_]);
+            t = dw_add_f(t, f[(size_t)pi * nj + pj]);
+            c4[4 * ((size_t)i * nj + j) + 3] = dw_float(dw_mul(dw_mul(t, kfy[KF_RC * ni + i]), kfx[KF_RC * nj + j]));
+        }
+    }
+    free(tmp); free(kfy); free(kfx);
+}
+
 /* Node quadruples (f, fy, fx, fyx) of the bicubic spline surface through f (ni x nj) at
- * knots ys x xs: natural-spline knot derivatives along each grid line (double) and
- * central-difference cross derivatives (one-sided at the border). */
+ * knots ys x xs, in double (the FP64 twin): natural-spline knot derivatives along each grid
+ * line and central-difference cross derivatives (one-sided at the border). */
 static void bicubic_nodes(const double *ys, int ni, const double *xs, int nj, const double *f, double *c4) {
     const size_t nn = (size_t)ni * nj;
     double *tmp = (double *)malloc(sizeof(double) * (ni > nj ? ni : nj));
@@ -168,12 +257,16 @@ void orc_displacement_field_off(const double *ys, int ni, const double *xs, int 
     double *du = (double *)malloc(nn * sizeof(double)), *dv = (double *)malloc(nn * sizeof(double));
     double *cu = (double *)malloc(4 * nn * sizeof(double)), *cv = (double *)malloc(4 * nn * sizeof(double));
     for (size_t k = 0; k < nn; k++) { du[k] = u[k]; dv[k] = v[k]; }
-    bicubic_nodes(ys, ni, xs, nj, du, cu);
-    bicubic_nodes(ys, ni, xs, nj, dv, cv);
     const float ymin = (float)ys[0], ymax = (float)ys[ni - 1], xmin = (float)xs[0], xmax = (float)xs[nj - 1];
     float *fcu = (float *)malloc(4 * nn * sizeof(float)), *fcv = (float *)malloc(4 * nn * sizeof(float));
     float *fys = (float *)malloc(ni * sizeof(float)), *fxs = (float *)malloc(nj * sizeof(float));
-    for (size_t k = 0; k < 4 * nn; k++) { fcu[k] = (float)cu[k]; fcv[k] = (float)cv[k]; }
+    if (precision == 0) {
+        bicubic_nodes_dw(ys, ni, xs, nj, u, fcu);
+        bicubic_nodes_dw(ys, ni, xs, nj, v, fcv);
+    } else {
+        bicubic_nodes(ys, ni, xs, nj, du, cu);
+        bicubic_nodes(ys, ni, xs, nj, dv, cv);
+    }
     for (int i = 0; i < ni; i++) fys[i] = (float)ys[i];
     for (int j = 0; j < nj; j++) fxs[j] = (float)xs[j];
     for (int i = 0; i < h; i++) {

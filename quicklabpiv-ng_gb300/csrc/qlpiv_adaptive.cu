@@ -9,9 +9,10 @@
 //              bicubic spline surface through the current level's tile displacements
 //              (natural-spline knot derivatives, finite-difference cross derivatives,
 //              Hermite patches), evaluated per pixel with coordinates clamped to the
-//              tile-centre box.  Knot derivatives are solved in double; the surface is
-//              evaluated in float (the reference evaluates it in double: GB300's FP64 rate
-//              is ~1/60 of FP32, and float keeps the field within ~1e-6 px).
+//              tile-centre box.  Knot derivatives are solved in double-word (float-float)
+//              arithmetic, ~44 bits, and rounded to float; the surface is evaluated in float
+//              (the reference works in double: GB300's FP64 rate is ~1/64 of FP32, and this
+//              keeps the field within ~1e-6 px of the double one).
 //   B-warp     BiLinearImageWarpingStrategy.warpPixelOnImage (S/images/...:143-265),
 //              BothImages mode: field halved, A sampled at (i-u, j-v), B at (i+u, j+v),
 //              nearest-pixel anchor plus the neighbour on the residual's side, output
@@ -24,6 +25,7 @@
 #include <stdint.h>
 
 #include "qlpiv_adaptive.h"
+#include "qlpiv_dword.cuh"
 #include "qlpiv_internal.h"
 
 namespace qlpiv {
@@ -247,117 +249,165 @@ __global__ void inherit_tiles_kernel(int pairs, int mode, int pn, int pni, int p
 
 // ---------------- B-field spline set-up ----------------
 
-// cp[i] of the natural-spline tridiagonal elimination for knots v[n].
-__host__ __device__ void spline_factor(const double *v, int n, double *cp) {
-    cp[0] = 0.0;
-    for (int i = 1; i < n - 1; i++) {
-        const double h0 = v[i] - v[i - 1], h1 = v[i + 1] - v[i];
-        const double a = h0, b = 2.0 * (h0 + h1), c = h1;
-        const double den = b - a * cp[i - 1];
-        cp[i] = c / den;
+__host__ __device__ void knot_factors(const double *x, int n, double *kf) {
+    double *h = kf + KF_H * n, *ih = kf + KF_IH * n, *h6 = kf + KF_H6 * n;
+    double *cp = kf + KF_CP * n, *iden = kf + KF_IDEN * n, *rc = kf + KF_RC * n;
+    for (int k = 0; k < KF_ARRAYS * n; k++) kf[k] = 0.0;
+    for (int i = 0; i + 1 < n; i++) {
+        h[i] = x[i + 1] - x[i];
+        ih[i] = 1.0 / h[i];
+        h6[i] = h[i] / 6.0;
     }
-    if (n > 1) cp[n - 1] = 0.0;
-}
-
-__global__ void spline_factor_kernel(const double *v, int n, double *cp) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    spline_factor(v, n, cp);
-}
-
-// Knot derivatives of one grid line of f (float values, stride fs) into out (stride os).
-__host__ __device__ void spline_line(const double *x, const double *cp, int n, const float *f, long fs, double *out, long os) {
-    auto Y = [&](int i) -> double { return (double)f[(long)i * fs]; };
-    out[0] = 0.0;
-    double dprev = 0.0;
-    for (int i = 1; i < n - 1; i++) {
-        const double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
-        const double a = h0, b = 2.0 * (h0 + h1);
-        const double r = 6.0 * ((Y(i + 1) - Y(i)) / h1 - (Y(i) - Y(i - 1)) / h0);
-        const double den = b - a * cp[i - 1];
-        const double dp = (r - a * dprev) / den;
-        out[(long)i * os] = dp;
-        dprev = dp;
+    for (int i = 1; i + 1 < n; i++) {
+        const double den = 2.0 * (h[i - 1] + h[i]) - h[i - 1] * cp[i - 1];
+        cp[i] = h[i] / den;
+        iden[i] = 1.0 / den;
     }
-    out[(long)(n - 1) * os] = 0.0;
-    double mnext = 0.0;  // m[n-1]
-    for (int i = n - 2; i >= 1; i--) {
-        const double m = out[(long)i * os] - cp[i] * mnext;
-        out[(long)i * os] = m;
-        mnext = m;
-    }
-    // out now holds m[]; convert to first derivatives in place
-    double mi = out[0];
-    double mlast_prev = 0.0;
-    for (int i = 0; i < n - 1; i++) {
-        const double mi1 = out[(long)(i + 1) * os];
-        const double h = x[i + 1] - x[i];
-        out[(long)i * os] = (Y(i + 1) - Y(i)) / h - h * (2.0 * mi + mi1) / 6.0;
-        mlast_prev = mi;
-        mi = mi1;
-    }
-    {
-        // mi == m[n-1], mlast_prev == m[n-2]
-        const double h = x[n - 1] - x[n - 2];
-        out[(long)(n - 1) * os] = (Y(n - 1) - Y(n - 2)) / h + h * (mlast_prev + 2.0 * mi) / 6.0;
+    for (int i = 0; i < n; i++) {
+        const int nx = i + 1 < n ? i + 1 : n - 1, pv = i - 1 >= 0 ? i - 1 : 0;
+        rc[i] = 1.0 / (x[nx] - x[pv]);
     }
 }
 
-// Line gid of pairs x 2 components x (nj column lines + ni row lines).
-__host__ __device__ void spline_lines_one(long gid, const double *ys, const double *cpy, int ni, const double *xs,
-                                          const double *cpx, int nj, const float *u, const float *v, SplineCoef coef) {
-    const long lines = (long)nj + ni;
-    const int pair = (int)(gid / (lines * 2));
-    const long rem = gid - (long)pair * lines * 2;
-    const int comp = (int)(rem / lines);
-    const long line = rem - (long)comp * lines;
+void knot_factors_dw(const double *x, int n, float2 *out) {
+    double *kf = new double[(size_t)KF_ARRAYS * n];
+    knot_factors(x, n, kf);
+    for (int k = 0; k < KF_ARRAYS * n; k++) {
+        const dword d = dw_of(kf[k]);
+        out[k] = make_float2(d.hi, d.lo);
+    }
+    delete[] kf;
+}
+
+__host__ __device__ __forceinline__ dword dw_at(const float2 *p, int i) {
+    const float2 v = p[i];
+    return dword{v.x, v.y};
+}
+
+// Natural-spline first derivatives at the n knots of one grid line, in double-word arithmetic
+// with factors kf (knot_factors_dw): values y(i) (float), scratch S(i) (float2), float results
+// out(i, d).  A forward elimination, then one backward sweep that forms the second derivatives
+// m (m[0] = m[n-1] = 0) and, from m[i] and m[i+1], the derivative at knot i:
+//   s[i]  = (y[i+1] - y[i]) ih[i]                   (the difference is exact as a double-word)
+//   dp[i] = (6 (s[i] - s[i-1]) - h[i-1] dp[i-1]) iden[i],   dp[0] = 0
+//   m[i]  = dp[i] - cp[i] m[i+1]
+//   d[i]  = s[i] - h6[i] (2 m[i] + m[i+1]),   d[n-1] = s[n-2] + h6[n-2] (m[n-2] + 2 m[n-1])
+// The oracle's float path restates these operations.  The loads of C knots are issued ahead of
+// their part of the dependent chain.
+template <int C, typename YF, typename SF, typename OF>
+__host__ __device__ __forceinline__ void spline_line_dw(const float2 *kf, int n, YF y, SF S, OF out) {
+    const float2 *h = kf + KF_H * n, *ih = kf + KF_IH * n, *h6 = kf + KF_H6 * n;
+    const float2 *cp = kf + KF_CP * n, *iden = kf + KF_IDEN * n;
+    const dword zero{0.0f, 0.0f};
+    float ycur = y(1);
+    dword sp = dw_mul(two_sum(ycur, -y(0)), dw_at(ih, 0));
+    dword dprev = zero;
+    for (int i0 = 1; i0 < n - 1; i0 += C) {
+        float yv[C];
+#pragma unroll
+        for (int k = 0; k < C; k++) yv[k] = i0 + k < n - 1 ? y(i0 + k + 1) : 0.0f;
+#pragma unroll
+        for (int k = 0; k < C; k++) {
+            const int i = i0 + k;
+            if (i < n - 1) {
+                const dword si = dw_mul(two_sum(yv[k], -ycur), dw_at(ih, i));
+                const dword r = dw_mul_f(dw_sub(si, sp), 6.0f);
+                const dword dp = dw_mul(dw_sub(r, dw_mul(dw_at(h, i - 1), dprev)), dw_at(iden, i));
+                S(i) = make_float2(dp.hi, dp.lo);
+                dprev = dp;
+                sp = si;
+                ycur = yv[k];
+            }
+        }
+    }
+    dword mnext = zero;  // m[n-1]
+    float ynext = y(n - 1);
+    for (int i0 = n - 2; i0 >= 1; i0 -= C) {
+        float yv[C];
+        float2 dv[C];
+#pragma unroll
+        for (int k = 0; k < C; k++) {
+            yv[k] = i0 - k >= 1 ? y(i0 - k) : 0.0f;
+            dv[k] = i0 - k >= 1 ? S(i0 - k) : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int k = 0; k < C; k++) {
+            const int i = i0 - k;
+            if (i >= 1) {
+                const dword m = dw_sub(dword{dv[k].x, dv[k].y}, dw_mul(dw_at(cp, i), mnext));
+                const dword si = dw_mul(two_sum(ynext, -yv[k]), dw_at(ih, i));
+                const dword hh = dw_at(h6, i);
+                if (i == n - 2) out(n - 1, dw_float(dw_add(si, dw_mul(hh, dw_add(m, dw_twice(mnext))))));
+                out(i, dw_float(dw_sub(si, dw_mul(hh, dw_add(dw_twice(m), mnext)))));
+                mnext = m;
+                ynext = yv[k];
+            }
+        }
+    }
+    const dword s0 = dw_mul(two_sum(ynext, -y(0)), dw_at(ih, 0));
+    if (n == 2) out(1, dw_float(dw_add(s0, dw_mul(dw_at(h6, 0), dw_add(zero, dw_twice(zero))))));
+    out(0, dw_float(dw_sub(s0, dw_mul(dw_at(h6, 0), dw_add(dw_twice(zero), mnext)))));
+}
+
+// Cross derivative of node (i, j) from the node values around it (central differences,
+// one-sided at the border), in double-word arithmetic: ((a - b - c + d) rcy[i]) rcx[j].
+template <typename FF>
+__host__ __device__ __forceinline__ float spline_cross(FF f, int ni, int nj, int i, int j, const float2 *rcy,
+                                                       const float2 *rcx) {
+    const int in = i + 1 < ni ? i + 1 : ni - 1, ip = i - 1 >= 0 ? i - 1 : 0;
+    const int jn = j + 1 < nj ? j + 1 : nj - 1, jp = j - 1 >= 0 ? j - 1 : 0;
+    dword t = two_sum(f(in, jn), -f(in, jp));
+    t = dw_add_f(t, -f(ip, jn));
+    t = dw_add_f(t, f(ip, jp));
+    return dw_float(dw_mul(dw_mul(t, dw_at(rcy, i)), dw_at(rcx, j)));
+}
+
+// One warp per strip of 32 grid lines of one component of one pair.  Column strips solve the
+// lines along the first coordinate and write the node value, fy and the cross derivative of
+// their 32 columns; row strips solve the lines along the second coordinate and write fx.
+// Lanes walk their own line: per knot the lanes of a column strip touch 32 consecutive nodes;
+// the scratch of a row strip is laid out knot-major (knot, lane) so its accesses stay
+// coalesced.  The two kinds write disjoint floats of the node quadruples.
+__global__ void __launch_bounds__(128) spline_nodes_kernel(int pairs, const float2 *kfy, int ni, const float2 *kfx,
+                                                           int nj, const float *u, const float *v, SplineCoef coef) {
+    const int sj = (nj + 31) / 32, si = (ni + 31) / 32, per = 2 * (sj + si);
+    const long wid = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (wid >= (long)pairs * per) return;
+    const int lane = threadIdx.x & 31;
+    const int pair = (int)(wid / per);
+    int r = (int)(wid - (long)pair * per);
+    const int comp = r / (sj + si);
+    r -= comp * (sj + si);
     const long base = (long)pair * ni * nj;
     const float *f = (comp == 0 ? u : v) + base;
-    if (line < nj) {  // along the first coordinate, column j
-        const int j = (int)line;
-        double *out = (comp == 0 ? coef.fy_u : coef.fy_v) + base + j;
-        spline_line(ys, cpy, ni, f + j, nj, out, nj);
-    } else {          // along the second coordinate, row i
-        const int i = (int)(line - nj);
-        double *out = (comp == 0 ? coef.fx_u : coef.fx_v) + base + (long)i * nj;
-        spline_line(xs, cpx, nj, f + (long)i * nj, 1, out, 1);
+    float *c4 = reinterpret_cast<float *>((comp == 0 ? coef.c4_u : coef.c4_v) + base);
+    if (r < sj) {
+        const int j = r * 32 + lane;
+        if (j >= nj) return;
+        float2 *S = (comp == 0 ? coef.col_u : coef.col_v) + base;
+        const float2 *rcy = kfy + KF_RC * ni, *rcx = kfx + KF_RC * nj;
+        auto F = [&](int a, int b) { return __ldg(f + (long)a * nj + b); };
+        // node values and cross derivatives first: independent of the line solve
+#pragma unroll 4
+        for (int i = 0; i < ni; i++) {
+            const long k = (long)i * nj + j;
+            c4[4 * k] = __ldg(f + k);
+            c4[4 * k + 3] = spline_cross(F, ni, nj, i, j, rcy, rcx);
+        }
+        spline_line_dw<8>(
+            kfy, ni, [&](int i) { return __ldg(f + (long)i * nj + j); },
+            [&](int i) -> float2 & { return S[(long)i * nj + j]; },
+            [&](int i, float d) { c4[4 * ((long)i * nj + j) + 1] = d; });
+    } else {
+        const int i0 = (r - sj) * 32, rows = ni - i0 < 32 ? ni - i0 : 32;
+        if (lane >= rows) return;
+        const int i = i0 + lane;
+        float2 *S = (comp == 0 ? coef.row_u : coef.row_v) + base + (long)i0 * nj;
+        const float *fr = f + (long)i * nj;
+        spline_line_dw<8>(
+            kfx, nj, [&](int j) { return __ldg(fr + j); }, [&](int j) -> float2 & { return S[(long)j * rows + lane]; },
+            [&](int j, float d) { c4[4 * ((long)i * nj + j) + 2] = d; });
     }
-}
-
-__global__ void spline_lines_kernel(int pairs, const double *ys, const double *cpy, int ni, const double *xs,
-                                    const double *cpx, int nj, const float *u, const float *v, SplineCoef coef) {
-    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= ((long)nj + ni) * 2 * pairs) return;
-    spline_lines_one(gid, ys, cpy, ni, xs, cpx, nj, u, v, coef);
-}
-
-// Cross derivatives by central differences (one-sided at the border), node gid; then
-// the node quadruple (f, fy, fx, fyx) rounded to float for the evaluation.
-__host__ __device__ void spline_cross_one(long gid, const double *ys, int ni, const double *xs, int nj, const float *u,
-                                          const float *v, SplineCoef coef) {
-    const long cnt = (long)ni * nj;
-    const int pair = (int)(gid / cnt);
-    const long k = gid - (long)pair * cnt;
-    const int i = (int)(k / nj), j = (int)(k - (long)i * nj);
-    const int ni_ = i + 1 < ni ? i + 1 : ni - 1, pi = i - 1 >= 0 ? i - 1 : 0;
-    const int nj_ = j + 1 < nj ? j + 1 : nj - 1, pj = j - 1 >= 0 ? j - 1 : 0;
-    const long base = (long)pair * cnt;
-    const double den = (ys[ni_] - ys[pi]) * (xs[nj_] - xs[pj]);
-    for (int comp = 0; comp < 2; comp++) {
-        const float *f = (comp == 0 ? u : v) + base;
-        const double a = (double)f[(long)ni_ * nj + nj_], b = (double)f[(long)ni_ * nj + pj];
-        const double c = (double)f[(long)pi * nj + nj_], d = (double)f[(long)pi * nj + pj];
-        const double fyx = (a - b - c + d) / den;
-        const double fy = (comp == 0 ? coef.fy_u : coef.fy_v)[base + k];
-        const double fx = (comp == 0 ? coef.fx_u : coef.fx_v)[base + k];
-        (comp == 0 ? coef.c4_u : coef.c4_v)[base + k] = make_float4(f[k], (float)fy, (float)fx, (float)fyx);
-    }
-}
-
-__global__ void spline_cross_kernel(int pairs, const double *ys, int ni, const double *xs, int nj, const float *u,
-                                    const float *v, SplineCoef coef) {
-    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long)ni * nj * pairs) return;
-    spline_cross_one(gid, ys, ni, xs, nj, u, v, coef);
 }
 
 // ---------------- B-field evaluation + B-warp ----------------
@@ -392,6 +442,53 @@ __host__ __device__ float warp_pixel(const Pix *img, int h, int w, long pitch, f
     const float b = (1.0f - wU) * wV * tr;
     const float c = wU * (1.0f - wV) * bl;
     const float d = wU * wV * br;
+    return (float)java_round(a + b + c + d);
+}
+
+// warp_pixel split in two so that several samples' reads can be in flight at once: the taps
+// (anchor rows p0 / p1, columns pJ / pJ + oJ, weights) and then the same float operations on
+// the four values.
+template <typename Pix>
+struct WarpTap {
+    const Pix *p0, *p1;
+    int pJ, oJ;
+    float wU, wV;
+};
+
+template <typename Pix>
+__device__ __forceinline__ WarpTap<Pix> warp_tap(const Pix *img, int h, int w, long pitch, float u, float v, int i,
+                                                 int j, bool first) {
+    float sI = first ? (float)i - u : (float)i + u;
+    float sJ = first ? (float)j - v : (float)j + v;
+    int pI = (int)(short)java_round(sI), pJ = (int)(short)java_round(sJ);
+    if (pI < 0) { sI = 0.0f; pI = 0; }
+    else if (pI >= h) { sI = (float)(h - 1); pI = h - 1; }
+    if (pJ < 0) { sJ = 0.0f; pJ = 0; }
+    else if (pJ >= w) { sJ = (float)(w - 1); pJ = w - 1; }
+    const float dU = sI - (float)pI, dV = sJ - (float)pJ;
+    int oI = dU >= 0.0f ? 1 : -1, oJ = dV >= 0.0f ? 1 : -1;
+    if (oI + pI < 0 || oI + pI >= h) oI = 0;
+    if (oJ + pJ < 0 || oJ + pJ >= w) oJ = 0;
+    return WarpTap<Pix>{img + (long)pI * pitch, img + (long)(pI + oI) * pitch, pJ, oJ, fabsf(dU), fabsf(dV)};
+}
+
+struct WarpVals {
+    float tl, tr, bl, br;
+};
+
+template <typename Pix>
+__device__ __forceinline__ WarpVals warp_load(const WarpTap<Pix> &t) {
+    return WarpVals{(float)__ldg(t.p0 + t.pJ), (float)__ldg(t.p0 + t.pJ + t.oJ), (float)__ldg(t.p1 + t.pJ),
+                    (float)__ldg(t.p1 + t.pJ + t.oJ)};
+}
+
+template <typename Pix>
+__device__ __forceinline__ float warp_value(const WarpTap<Pix> &t, const WarpVals &q) {
+    const float wU = t.wU, wV = t.wV;
+    const float a = (1.0f - wU) * (1.0f - wV) * q.tl;
+    const float b = (1.0f - wU) * wV * q.tr;
+    const float c = wU * (1.0f - wV) * q.bl;
+    const float d = wU * wV * q.br;
     return (float)java_round(a + b + c + d);
 }
 
@@ -441,55 +538,92 @@ __host__ __device__ __forceinline__ float field_value(const float *ys, int ni, c
     return field_combine(c4, nj, i, j, X, Y);
 }
 
-// One thread per pixel of one pair (blockIdx.z = pair), 32 x 8 pixels per block; src/dst frame
-// tables hold the original and the warped images.  The knot search and Hermite basis of the
-// block's 32 columns and 8 rows are computed once in shared memory (the same operations
-// field_value performs per pixel, so the field is bit-identical).
+// Column weights of patch row i at column basis X: w[a] (values) and w[2 + a] (row
+// derivatives) of node rows i + a, the first half of field_combine.
+__device__ __forceinline__ void field_column(const float4 *c4, int nj, int i, int j, const float X[4], float w[4]) {
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+        const long k0 = (long)(i + a) * nj + j;
+        const float4 n0 = __ldg(c4 + k0), n1 = __ldg(c4 + k0 + 1);
+        w[a] = n0.x * X[0] + n1.x * X[1] + n0.z * X[2] + n1.z * X[3];
+        w[2 + a] = n0.y * X[0] + n1.y * X[1] + n0.w * X[2] + n1.w * X[3];
+    }
+}
+
+// One block per 32 columns x kWarpRows rows of one pair (blockIdx.z = pair): thread (tx, ty)
+// walks column j over kWarpRows / 8 consecutive rows.  The knot search and Hermite basis of the
+// block's columns and rows are computed once in shared memory; a thread forms its column
+// weights once per knot interval of the rows it walks (the weights do not depend on the row
+// inside an interval), so a pixel costs the row combination of field_combine and the two
+// samples.  Same operations as field_value per pixel: the field is bit-identical.
+constexpr int kWarpRows = 64;
+
 template <typename Pix>
 __global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, const qlpiv_frame *dst,
                                                         const float *ys, int ni, const float *xs, int nj,
                                                         const float4 *c4u, const float4 *c4v, int int16_quirk,
                                                         int image_mode) {
-    __shared__ float sx[32][4], sy[8][4];
-    __shared__ int sj[32], si[8];
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int j = blockIdx.x * 32 + tx, i = blockIdx.y * 8 + ty;
+    constexpr int kPer = kWarpRows / 8;
+    __shared__ float sx[32][4];
+    __shared__ float4 sy[kWarpRows];
+    __shared__ int sj[32], si[kWarpRows];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+    const int j = blockIdx.x * 32 + tx, row0 = blockIdx.y * kWarpRows;
     const int pair = blockIdx.z;
-    if (ty == 0) {
-        float x = (float)j;
+    if (tid < 32) {
+        float x = (float)(blockIdx.x * 32 + tid);
         if (x < xs[0]) x = xs[0]; else if (x > xs[nj - 1]) x = xs[nj - 1];
-        sj[tx] = field_basis(xs, nj, x, sx[tx]);
-    } else if (ty == 1 && tx < 8) {
-        float y = (float)(blockIdx.y * 8 + tx);
+        sj[tid] = field_basis(xs, nj, x, sx[tid]);
+    } else if (tid >= 64 && tid < 64 + kWarpRows) {
+        const int r = tid - 64;
+        float y = (float)(row0 + r);
         if (y < ys[0]) y = ys[0]; else if (y > ys[ni - 1]) y = ys[ni - 1];
-        si[tx] = field_basis(ys, ni, y, sy[tx]);
+        float Y[4];
+        si[r] = field_basis(ys, ni, y, Y);
+        sy[r] = make_float4(Y[0], Y[1], Y[2], Y[3]);
     }
     __syncthreads();
     const qlpiv_frame fs = src[pair];
     const int h = fs.height, w = fs.width;
-    if (i >= h || j >= w) return;
+    if (j >= w) return;
     const qlpiv_frame fd = dst[pair];
     const long base = (long)pair * ni * nj;
-    float X[4], Y[4];
+    const float4 *cu = c4u + base, *cv = c4v + base;
+    float X[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        X[k] = sx[tx][k];
-        Y[k] = sy[ty][k];
-    }
-    const float fu = field_combine(c4u + base, nj, si[ty], sj[tx], X, Y);
-    const float fv = field_combine(c4v + base, nj, si[ty], sj[tx], X, Y);
+    for (int k = 0; k < 4; k++) X[k] = sx[tx][k];
+    const int kj = sj[tx];
     const bool both = image_mode == 3;
-    const float hu = both ? fu / 2.0f : fu, hv = both ? fv / 2.0f : fv;
     const Pix *ia = reinterpret_cast<const Pix *>(fs.img_a);
     const Pix *ib = reinterpret_cast<const Pix *>(fs.img_b);
     Pix *oa = reinterpret_cast<Pix *>(const_cast<void *>(fd.img_a));
     Pix *ob = reinterpret_cast<Pix *>(const_cast<void *>(fd.img_b));
-    oa[(long)i * fd.pitch + j] = image_mode & 1
-        ? warp_store<Pix>(warp_pixel(ia, h, w, fs.pitch, hu, hv, i, j, true), int16_quirk)
-        : ia[(long)i * fs.pitch + j];
-    ob[(long)i * fd.pitch + j] = image_mode & 2
-        ? warp_store<Pix>(warp_pixel(ib, h, w, fs.pitch, hu, hv, i, j, false), int16_quirk)
-        : ib[(long)i * fs.pitch + j];
+    int cur = -1;
+    float wu[4], wv[4];
+    for (int q = 0; q < kPer; q++) {
+        const int r = ty * kPer + q, i = row0 + r;
+        if (i >= h) break;
+        const int ki = si[r];
+        if (ki != cur) {
+            field_column(cu, nj, ki, kj, X, wu);
+            field_column(cv, nj, ki, kj, X, wv);
+            cur = ki;
+        }
+        const float4 Y4 = sy[r];
+        const float fu = wu[0] * Y4.x + wu[1] * Y4.y + wu[2] * Y4.z + wu[3] * Y4.w;
+        const float fv = wv[0] * Y4.x + wv[1] * Y4.y + wv[2] * Y4.z + wv[3] * Y4.w;
+        const float hu = both ? fu / 2.0f : fu, hv = both ? fv / 2.0f : fv;
+        // both frames' four reads are issued before the arithmetic that consumes them
+        const WarpTap<Pix> ta = warp_tap(ia, h, w, fs.pitch, hu, hv, i, j, true);
+        const WarpTap<Pix> tb = warp_tap(ib, h, w, fs.pitch, hu, hv, i, j, false);
+        WarpVals va, vb;
+        if (image_mode & 1) va = warp_load(ta);
+        if (image_mode & 2) vb = warp_load(tb);
+        oa[(long)i * fd.pitch + j] =
+            image_mode & 1 ? warp_store<Pix>(warp_value(ta, va), int16_quirk) : ia[(long)i * fs.pitch + j];
+        ob[(long)i * fd.pitch + j] =
+            image_mode & 2 ? warp_store<Pix>(warp_value(tb, vb), int16_quirk) : ib[(long)i * fs.pitch + j];
+    }
 }
 
 // ---------------- micro / mini per-tile warping ----------------
@@ -524,9 +658,11 @@ __global__ void __launch_bounds__(256) tile_warp_kernel(const qlpiv_frame *frame
     const int tid = threadIdx.x, nt = blockDim.x;
 
     // mini: the neighbourhood spline in shared memory
-    __shared__ double s_ys[kMiniR], s_xs[kMiniR], s_cpy[kMiniR], s_cpx[kMiniR];
+    __shared__ double s_ys[kMiniR], s_xs[kMiniR], s_kd[2][KF_ARRAYS * kMiniR];
+    __shared__ float2 s_kfy[KF_ARRAYS * kMiniR], s_kfx[KF_ARRAYS * kMiniR];
     __shared__ float s_fys[kMiniR], s_fxs[kMiniR], s_f[2][kMiniR * kMiniR];
-    __shared__ double s_fy[2][kMiniR * kMiniR], s_fx[2][kMiniR * kMiniR];
+    __shared__ float s_fy[2][kMiniR * kMiniR], s_fx[2][kMiniR * kMiniR];
+    __shared__ float2 s_scr[2][2][kMiniR * kMiniR];
     __shared__ float4 s_c4[2][kMiniR * kMiniR];
     __shared__ int s_max[2];
     const int r2 = kMiniR / 2;
@@ -551,30 +687,44 @@ __global__ void __launch_bounds__(256) tile_warp_kernel(const qlpiv_frame *frame
             s_xs[j] = (double)s_fxs[j];
         }
         __syncthreads();
-        if (tid == 0) spline_factor(s_ys, di, s_cpy);
-        if (tid == 1) spline_factor(s_xs, dj, s_cpx);
+        if (tid == 0) knot_factors(s_ys, di, s_kd[0]);
+        if (tid == 1) knot_factors(s_xs, dj, s_kd[1]);
+        __syncthreads();
+        for (int q = tid; q < KF_ARRAYS * (di + dj); q += nt) {
+            const bool y = q < KF_ARRAYS * di;
+            const int k = y ? q : q - KF_ARRAYS * di;
+            const dword d = dw_of(s_kd[y ? 0 : 1][k]);
+            (y ? s_kfy : s_kfx)[k] = make_float2(d.hi, d.lo);
+        }
         __syncthreads();
         // knot derivatives: column lines (along y) and row lines (along x) of both components
         for (int q = tid; q < 2 * (dj + di); q += nt) {
             const int comp = q / (dj + di), line = q - comp * (dj + di);
-            if (line < dj)
-                spline_line(s_ys, s_cpy, di, s_f[comp] + line, dj, s_fy[comp] + line, dj);
-            else
-                spline_line(s_xs, s_cpx, dj, s_f[comp] + (long)(line - dj) * dj, 1, s_fx[comp] + (long)(line - dj) * dj, 1);
+            const float *f = s_f[comp];
+            if (line < dj) {
+                float2 *scr = s_scr[comp][0] + line;
+                float *o = s_fy[comp] + line;
+                spline_line_dw<1>(
+                    s_kfy, di, [&](int i) { return f[i * dj + line]; }, [&](int i) -> float2 & { return scr[i * dj]; },
+                    [&](int i, float d) { o[i * dj] = d; });
+            } else {
+                const int row = line - dj;
+                float2 *scr = s_scr[comp][1] + row * dj;
+                float *o = s_fx[comp] + row * dj;
+                spline_line_dw<1>(
+                    s_kfx, dj, [&](int j) { return f[row * dj + j]; }, [&](int j) -> float2 & { return scr[j]; },
+                    [&](int j, float d) { o[j] = d; });
+            }
         }
         __syncthreads();
-        // cross derivatives (central differences, one-sided at the border) and float nodes
+        // cross derivatives and float nodes
         for (int q = tid; q < 2 * di * dj; q += nt) {
             const int comp = q / (di * dj), kk = q - comp * di * dj;
             const int i = kk / dj, j = kk - i * dj;
-            const int in = i + 1 < di ? i + 1 : di - 1, ip = i - 1 >= 0 ? i - 1 : 0;
-            const int jn = j + 1 < dj ? j + 1 : dj - 1, jp = j - 1 >= 0 ? j - 1 : 0;
-            const double den = (s_ys[in] - s_ys[ip]) * (s_xs[jn] - s_xs[jp]);
             const float *f = s_f[comp];
-            const double a = (double)f[in * dj + jn], b = (double)f[in * dj + jp];
-            const double c = (double)f[ip * dj + jn], d = (double)f[ip * dj + jp];
-            const double fyx = (a - b - c + d) / den;
-            s_c4[comp][kk] = make_float4(f[kk], (float)s_fy[comp][kk], (float)s_fx[comp][kk], (float)fyx);
+            const float fyx = spline_cross([&](int a, int b) { return f[a * dj + b]; }, di, dj, i, j,
+                                           s_kfy + KF_RC * di, s_kfx + KF_RC * dj);
+            s_c4[comp][kk] = make_float4(f[kk], s_fy[comp][kk], s_fx[comp][kk], fyx);
         }
         __syncthreads();
     }
@@ -742,14 +892,10 @@ cudaError_t launch_inherit_tiles(cudaStream_t s, int pairs, int mode, int pn, in
     return cudaGetLastError();
 }
 
-cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const double *cpy, int ni, const double *xs,
-                          const double *cpx, int nj, const float *u, const float *v, SplineCoef coef) {
-    spline_factor_kernel<<<1, 1, 0, s>>>(ys, ni, const_cast<double *>(cpy));
-    spline_factor_kernel<<<1, 1, 0, s>>>(xs, nj, const_cast<double *>(cpx));
-    const long lines = (long)pairs * 2 * (ni + nj);
-    spline_lines_kernel<<<blocks_for(lines, 64), 64, 0, s>>>(pairs, ys, cpy, ni, xs, cpx, nj, u, v, coef);
-    const long nodes = (long)pairs * ni * nj;
-    spline_cross_kernel<<<blocks_for(nodes, 256), 256, 0, s>>>(pairs, ys, ni, xs, nj, u, v, coef);
+cudaError_t launch_spline(cudaStream_t s, int pairs, const float2 *kfy, int ni, const float2 *kfx, int nj,
+                          const float *u, const float *v, SplineCoef coef) {
+    const long warps = (long)pairs * 2 * ((ni + 31) / 32 + (nj + 31) / 32);
+    spline_nodes_kernel<<<blocks_for(warps * 32, 128), 128, 0, s>>>(pairs, kfy, ni, kfx, nj, u, v, coef);
     return cudaGetLastError();
 }
 
@@ -757,7 +903,7 @@ cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w,
                         const qlpiv_frame *dst, const float *ys, int ni, const float *xs, int nj, SplineCoef coef,
                         int int16_quirk, int image_mode) {
     if (image_mode < 1 || image_mode > 3) return cudaErrorInvalidValue;
-    dim3 blk(32, 8), grd(blocks_for(w, 32), blocks_for(h, 8), pairs);
+    dim3 blk(32, 8), grd(blocks_for(w, 32), blocks_for(h, kWarpRows), pairs);
     if (pixel_type == QLPIV_PIX_U8)
         warp_both_kernel<uint8_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk,
                                                       image_mode);

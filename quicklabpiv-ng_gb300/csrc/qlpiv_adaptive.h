@@ -7,14 +7,36 @@
 
 namespace qlpiv {
 
-// Knot derivatives of the bicubic displacement surfaces, [pairs][ni*nj] each: the
-// double line solves (fy, fx; fyx unused) and the float node quadruples
+// The bicubic displacement surfaces of [pairs][ni*nj] tiles: double-word scratch of the line
+// solves (column lines, row lines; per component) and the float node quadruples
 // (f, fy, fx, fyx) the evaluation reads.
 struct SplineCoef {
-    double *fy_u, *fx_u, *fyx_u;
-    double *fy_v, *fx_v, *fyx_v;
+    float2 *col_u, *row_u, *col_v, *row_v;
     float4 *c4_u, *c4_v;
 };
+inline size_t spline_coef_bytes(long n) { return (size_t)n * (4 * sizeof(float2) + 2 * sizeof(float4)); }
+// base: 16-byte aligned, spline_coef_bytes(n) long.
+inline SplineCoef spline_coef_at(void *base, long n) {
+    float2 *c = reinterpret_cast<float2 *>(base);
+    float4 *q = reinterpret_cast<float4 *>(c + 4 * n);
+    return SplineCoef{c, c + n, c + 2 * n, c + 3 * n, q, q + n};
+}
+inline SplineCoef spline_coef_offset(const SplineCoef &c, long off) {
+    return SplineCoef{c.col_u + off, c.row_u + off, c.col_v + off, c.row_v + off, c.c4_u + off, c.c4_v + off};
+}
+
+// Factors of the natural-spline line solves along one axis with knots x[n] (n >= 2): KF_ARRAYS
+// arrays of n values, computed once per grid in double so that the per-line solves multiply
+// instead of divide:
+//   h[i] = x[i+1] - x[i], ih[i] = 1 / h[i], h6[i] = h[i] / 6                       (i < n-1)
+//   den[i] = 2 (h[i-1] + h[i]) - h[i-1] cp[i-1], cp[i] = h[i] / den[i], iden[i] = 1 / den[i]
+//                                                                              (0 < i < n-1)
+//   rc[i] = 1 / (x[min(i+1, n-1)] - x[max(i-1, 0)])       (the cross-derivative differences)
+// Unused entries are 0.  The solves take them as double-words (knot_factors_dw).
+enum { KF_H = 0, KF_IH, KF_H6, KF_CP, KF_IDEN, KF_RC, KF_ARRAYS };
+__host__ __device__ void knot_factors(const double *x, int n, double *kf);
+// knot_factors rounded to double-words (hi, lo) for the device solves; out: KF_ARRAYS * n.
+void knot_factors_dw(const double *x, int n, float2 *out);
 
 // ru/rv: scratch of pairs x cni x pnj floats (stage-1 row values).
 cudaError_t launch_inherit(cudaStream_t s, int pairs, const float *py, int pni, const float *px, int pnj,
@@ -40,9 +62,10 @@ cudaError_t launch_inherit_tiles(cudaStream_t s, int pairs, int mode, int pn, in
                                  const int *plefts, const float *pu, const float *pv, int cn, int cni, int cnj,
                                  const int *ctops, const int *clefts, const int2 *tables, int round_int, float *cu,
                                  float *cv);
-// cpy/cpx: scratch of ni/nj doubles for the elimination factors.
-cudaError_t launch_spline(cudaStream_t s, int pairs, const double *ys, const double *cpy, int ni, const double *xs,
-                          const double *cpx, int nj, const float *u, const float *v, SplineCoef coef);
+// Node quadruples of every pair's u and v surfaces in one launch; kfy / kfx: device knot
+// factors (knot_factors_dw) of the ni row knots and the nj column knots.
+cudaError_t launch_spline(cudaStream_t s, int pairs, const float2 *kfy, int ni, const float2 *kfx, int nj,
+                          const float *u, const float *v, SplineCoef coef);
 cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
                         const qlpiv_frame *dst, const float *ys, int ni, const float *xs, int nj, SplineCoef coef,
                         int int16_quirk, int image_mode);

@@ -791,7 +791,6 @@ __global__ void ignore_piv_kernel(float *fu, float *fv, long n, int mode, float 
 
 }  // namespace
 
-size_t spline_coef_bytes(long tiles) { return (size_t)tiles * (6 * sizeof(double) + 2 * sizeof(float4)); }
 
 const char *check_flow_desc(const qlpiv_flow_desc *d, int h, int w) {
     if (!d) return "flow descriptor is NULL";
@@ -893,11 +892,6 @@ cudaError_t launch_liu_shen(cudaStream_t s, const float *la, const float *lb, in
     return cudaSuccess;
 }
 
-static SplineCoef coef_view(void *base, long n) {
-    double *c = reinterpret_cast<double *>(base);
-    float4 *q = reinterpret_cast<float4 *>(c + 6 * n);
-    return SplineCoef{c, c + n, c + 2 * n, c + 3 * n, c + 4 * n, c + 5 * n, q, q + n};
-}
 
 // ---------------- Lucas-Kanade pyramid (coarse to fine) ----------------
 // This library's own design (the reference's dense LK runs at full resolution only): 2 x 2 box
@@ -980,7 +974,7 @@ static cudaError_t filter_or_copy(cudaStream_t s, int pixel_type, const void *im
 }
 
 cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, const void *img_a, const void *img_b,
-                     long pitch, int h, int w, int n, int ni, int nj, const double *cy, const double *cx,
+                     long pitch, int h, int w, int n, int ni, int nj, const float2 *kfy, const float2 *kfx,
                      const float *cyf, const float *cxf, const int *tops, const int *lefts, float *tile_u,
                      float *tile_v, float *dense_u, float *dense_v, const FlowBufs &b, long *launches,
                      const FlowMarks *marks, const SplineCoef *given) {
@@ -1012,9 +1006,9 @@ cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, c
     if (given) {  // solved by the caller (all pairs at once)
         coef = *given;
     } else {
-        coef = coef_view(b.coef, (long)ni * nj);
-        if ((e = launch_spline(s, 1, cy, b.cp, ni, cx, b.cp + ni, nj, tile_u, tile_v, coef)) != cudaSuccess) return e;
-        *launches += 4;
+        coef = spline_coef_at(b.coef, (long)ni * nj);
+        if ((e = launch_spline(s, 1, kfy, ni, kfx, nj, tile_u, tile_v, coef)) != cudaSuccess) return e;
+        *launches += 1;
     }
     const float off = d.dense_export ? 0.0f : 0.5f;
     if ((e = launch_field(s, h, w, cyf, ni, cxf, nj, coef, b.fu, b.fv, off, off)) != cudaSuccess) return e;
@@ -1058,8 +1052,7 @@ cudaError_t flow_buffers(DevBuf &buf, int h, int w, int ni, int nj, int iteratio
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t pl = al(sizeof(float) * (size_t)h * w);
     const size_t total = 7 * pl + 10 * pl + 2 * pl + al(ls_err_bytes(h, w, iterations_ls)) + 256 +
-                         2 * al(sizeof(float) * 64) + al(sizeof(double) * (ni + nj)) +
-                         al(spline_coef_bytes((long)ni * nj));
+                         2 * al(sizeof(float) * 64) + al(spline_coef_bytes((long)ni * nj));
     cudaError_t e = buf.ensure(total);
     if (e != cudaSuccess) return e;
     char *c = buf.as<char>();
@@ -1071,7 +1064,6 @@ cudaError_t flow_buffers(DevBuf &buf, int h, int w, int ni, int nj, int iteratio
     b->mx = (unsigned *)c; c += 256;
     b->k_lk = (float *)c; c += al(sizeof(float) * 64);
     b->k_ls = (float *)c; c += al(sizeof(float) * 64);
-    b->cp = (double *)c; c += al(sizeof(double) * (ni + nj));
     b->coef = c;
     return cudaSuccess;
 }
@@ -1272,6 +1264,7 @@ qlpiv_status qlpiv_flow_after_piv(qlpiv_handle *h, const qlpiv_flow_desc *desc, 
         if (lefts[j] + n / 2 < 1 || lefts[j] + n / 2 >= width) return fail(QLPIV_E_SHAPE, "tile column %d outside the image", j);
     const long np = (long)height * width, nt = (long)ni * nj;
     std::vector<double> knots(ni + nj);
+    std::vector<float2> kf((size_t)KF_ARRAYS * (ni + nj));
     std::vector<float> fknots(ni + nj);
     for (int i = 0; i < ni; i++) {
         fknots[i] = (float)tops[i] + (float)n / 2.0f - 0.5f;
@@ -1281,6 +1274,8 @@ qlpiv_status qlpiv_flow_after_piv(qlpiv_handle *h, const qlpiv_flow_desc *desc, 
         fknots[ni + j] = (float)lefts[j] + (float)n / 2.0f - 0.5f;
         knots[ni + j] = fknots[ni + j];
     }
+    knot_factors_dw(knots.data(), ni, kf.data());
+    knot_factors_dw(knots.data() + ni, nj, kf.data() + (size_t)KF_ARRAYS * ni);
     std::lock_guard<std::mutex> lock(h->mu);
     DeviceScope ds(h->device);
     if (ds.err != cudaSuccess) return cuda_fail(ds.err, "cudaSetDevice");
@@ -1291,14 +1286,14 @@ qlpiv_status qlpiv_flow_after_piv(qlpiv_handle *h, const qlpiv_flow_desc *desc, 
     FlowBufs fb;
     if ((e = flow_buffers(sb[9], height, width, ni, nj, desc->iterations_ls, &fb)) != cudaSuccess ||
         (e = sb[0].ensure(2 * ((ib + 255) & ~(size_t)255))) != cudaSuccess ||
-        (e = sb[1].ensure(sizeof(double) * (ni + nj) + sizeof(float) * (ni + nj) + sizeof(int32_t) * (ni + nj) +
+        (e = sb[1].ensure(sizeof(float2) * kf.size() + sizeof(float) * (ni + nj) + sizeof(int32_t) * (ni + nj) +
                           sizeof(float) * 2 * nt + 1024)) != cudaSuccess ||
         (e = sb[2].ensure(sizeof(float) * 2 * np)) != cudaSuccess)
         return cuda_fail(e, "flow buffers");
     char *im = sb[0].as<char>();
     char *ib2 = im + ((ib + 255) & ~(size_t)255);
-    double *dk = sb[1].as<double>();
-    float *dfk = (float *)(dk + ni + nj);
+    float2 *dk = sb[1].as<float2>();
+    float *dfk = (float *)(dk + kf.size());
     int32_t *dtl = (int32_t *)(dfk + ni + nj);
     float *dtu = (float *)(dtl + ni + nj);
     float *dtv = dtu + nt;
@@ -1307,7 +1302,7 @@ qlpiv_status qlpiv_flow_after_piv(qlpiv_handle *h, const qlpiv_flow_desc *desc, 
     std::vector<float> wts;
     if ((e = cudaMemcpyAsync(im, img_a, ib, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(ib2, img_b, ib, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(dk, knots.data(), sizeof(double) * (ni + nj), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dk, kf.data(), sizeof(float2) * kf.size(), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(dfk, fknots.data(), sizeof(float) * (ni + nj), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(dtl, tl.data(), sizeof(int32_t) * (ni + nj), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(dtu, tile_u, sizeof(float) * nt, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
@@ -1316,7 +1311,8 @@ qlpiv_status qlpiv_flow_after_piv(qlpiv_handle *h, const qlpiv_flow_desc *desc, 
         return cuda_fail(e, "flow upload");
     float *du = sb[2].as<float>(), *dv = du + np;
     long launches = 0;
-    if ((e = run_flow(s, *desc, pixel_type, im, ib2, width, height, width, n, ni, nj, dk, dk + ni, dfk, dfk + ni, dtl,
+    if ((e = run_flow(s, *desc, pixel_type, im, ib2, width, height, width, n, ni, nj, dk,
+                      dk + (size_t)KF_ARRAYS * ni, dfk, dfk + ni, dtl,
                       dtl + ni, dtu, dtv, du, dv, fb, &launches, nullptr)) != cudaSuccess)
         return cuda_fail(e, "optical flow after PIV");
     h->launches += launches;

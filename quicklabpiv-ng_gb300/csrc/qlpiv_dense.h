@@ -34,10 +34,8 @@ struct FlowBufs {
     double *err;      // ls_err_bytes(h, w, iterations_ls)
     unsigned *mx;     // one word
     float *k_lk, *k_ls;  // filter weights (device)
-    double *cp;       // ni + nj doubles (spline elimination factors)
     void *coef;       // spline coefficients of ni x nj tiles (spline_coef_bytes)
 };
-size_t spline_coef_bytes(long tiles);
 
 // Optional sub-stage hook of run_flow: fn(ctx, stage, true) before a sub-stage's launches are
 // queued, fn(ctx, stage, false) after them (stage timing).
@@ -47,12 +45,12 @@ struct FlowMarks {
 };
 
 // Optical flow after PIV of one frame pair on the device (see qlpiv_flow_after_piv): frames of
-// pixel_type with `pitch` elements per row; tile grid knots cy/cx (double, ni / nj) and cyf/cxf
-// (float); tops/lefts (device int); tile_u/tile_v (rows, columns) updated in place; dense_u /
-// dense_v (rows, columns) optional.  *launches counts the kernels queued.  given: the spline
+// pixel_type with `pitch` elements per row; knot factors kfy/kfx of the tile grid's ni / nj
+// centres (knot_factors_dw, device) and the centres cyf/cxf (float); tops/lefts (device int);
+// tile_u/tile_v (rows, columns) updated in place; dense_u / dense_v (rows, columns) optional.  *launches counts the kernels queued.  given: the spline
 // coefficients of this pair's tiles when the caller solved them already (else solved here).
 cudaError_t run_flow(cudaStream_t s, const qlpiv_flow_desc &d, int pixel_type, const void *img_a, const void *img_b,
-                     long pitch, int h, int w, int n, int ni, int nj, const double *cy, const double *cx,
+                     long pitch, int h, int w, int n, int ni, int nj, const float2 *kfy, const float2 *kfx,
                      const float *cyf, const float *cxf, const int *tops, const int *lefts, float *tile_u,
                      float *tile_v, float *dense_u, float *dense_v, const FlowBufs &b, long *launches,
                      const FlowMarks *marks = nullptr, const SplineCoef *given = nullptr);

@@ -30,8 +30,9 @@ struct LevelPlan {
     qlpiv_grid g{};
     std::vector<int32_t> tops, lefts;
     std::vector<double> cy, cx;      // tile centres (top + N/2 - 0.5), double
+    std::vector<float2> kfy, kfx;    // their spline knot factors (double-words)
     std::vector<float> cyf, cxf;     // same, float
-    DevBuf d_cy, d_cx, d_cyf, d_cxf, d_cpy, d_cpx;
+    DevBuf d_kfy, d_kfx, d_cyf, d_cxf;  // knot factors of the spline solves (knot_factors), float knots
     DevBuf d_fi, d_at, d_al, d_bt, d_bl;  // flattened work list, pairs x count
     DevBuf d_u, d_v;                       // tile displacements, pairs x count
     DevBuf coef;                           // 6 doubles + 2 float4 per tile and pair
@@ -59,7 +60,7 @@ struct AdaptivePlan {
 void destroy_plan(AdaptivePlan *p) {
     if (!p) return;
     for (LevelPlan &l : p->levels)
-        for (DevBuf *b : {&l.d_cy, &l.d_cx, &l.d_cyf, &l.d_cxf, &l.d_cpy, &l.d_cpx, &l.d_fi, &l.d_at, &l.d_al, &l.d_bt,
+        for (DevBuf *b : {&l.d_kfy, &l.d_kfx, &l.d_cyf, &l.d_cxf, &l.d_fi, &l.d_at, &l.d_al, &l.d_bt,
                           &l.d_bl, &l.d_u, &l.d_v, &l.coef, &l.d_rows, &l.d_inh, &l.d_tops, &l.d_lefts, &l.d_order,
                           &l.d_rank, &l.d_bu, &l.d_bv, &l.d_puv, &l.d_npk, &l.d_state, &l.d_list, &l.d_done,
                           &l.d_sweeps, &l.d_tiles, &l.d_tmax})
@@ -69,14 +70,6 @@ void destroy_plan(AdaptivePlan *p) {
     delete p;
 }
 
-// 6 double line-solve arrays followed by 2 float4 node arrays, n entries each.
-static size_t coef_bytes(long n) { return (size_t)n * (6 * sizeof(double) + 2 * sizeof(float4)); }
-
-static SplineCoef coef_at(void *base, long n) {
-    double *c = reinterpret_cast<double *>(base);
-    float4 *q = reinterpret_cast<float4 *>(c + 6 * n);
-    return SplineCoef{c, c + n, c + 2 * n, c + 3 * n, c + 4 * n, c + 5 * n, q, q + n};
-}
 
 static float full_scale(int pixel_type) { return pixel_type == QLPIV_PIX_U8 ? 255.0f : 65535.0f; }
 
@@ -279,12 +272,14 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
                     al[k] = L.lefts[j];
                 }
         cudaStream_t s = h->stream;
-        if ((e = upload(L.d_cy, L.cy.data(), sizeof(double) * ni, s)) != cudaSuccess ||
-            (e = upload(L.d_cx, L.cx.data(), sizeof(double) * nj, s)) != cudaSuccess ||
+        L.kfy.resize((size_t)KF_ARRAYS * ni);
+        L.kfx.resize((size_t)KF_ARRAYS * nj);
+        knot_factors_dw(L.cy.data(), ni, L.kfy.data());
+        knot_factors_dw(L.cx.data(), nj, L.kfx.data());
+        if ((e = upload(L.d_kfy, L.kfy.data(), sizeof(float2) * L.kfy.size(), s)) != cudaSuccess ||
+            (e = upload(L.d_kfx, L.kfx.data(), sizeof(float2) * L.kfx.size(), s)) != cudaSuccess ||
             (e = upload(L.d_cyf, L.cyf.data(), sizeof(float) * ni, s)) != cudaSuccess ||
             (e = upload(L.d_cxf, L.cxf.data(), sizeof(float) * nj, s)) != cudaSuccess ||
-            (e = L.d_cpy.ensure(sizeof(double) * ni)) != cudaSuccess ||
-            (e = L.d_cpx.ensure(sizeof(double) * nj)) != cudaSuccess ||
             (e = upload(L.d_fi, fi.data(), sizeof(int32_t) * total, s)) != cudaSuccess ||
             (e = upload(L.d_at, at.data(), sizeof(int32_t) * total, s)) != cudaSuccess ||
             (e = upload(L.d_al, al.data(), sizeof(int32_t) * total, s)) != cudaSuccess ||
@@ -292,7 +287,7 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
             (e = L.d_bl.ensure(sizeof(int32_t) * total)) != cudaSuccess ||
             (e = L.d_u.ensure(sizeof(float) * total)) != cudaSuccess ||
             (e = L.d_v.ensure(sizeof(float) * total)) != cudaSuccess ||
-            (e = L.coef.ensure(coef_bytes(total))) != cudaSuccess ||
+            (e = L.coef.ensure(spline_coef_bytes(total))) != cudaSuccess ||
             (lv > 0 && (e = L.d_rows.ensure(sizeof(float) * 2 * (long)pairs * ni *
                                             p->levels[lv - 1].g.tiles_j)) != cudaSuccess))
             return cuda_fail(e, "adaptive plan");
@@ -386,7 +381,7 @@ struct StageScope {
     }
 };
 
-static SplineCoef coef_of(LevelPlan &L, int pairs) { return coef_at(L.coef.p, L.count() * pairs); }
+static SplineCoef coef_of(LevelPlan &L, int pairs) { return spline_coef_at(L.coef.p, L.count() * pairs); }
 
 // Queues the whole level loop; the last level's displacements end in levels.back().d_u/d_v.
 static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
@@ -447,10 +442,9 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
             if (lv > 0) {  // no warping at the first level: displacements are all zero
                 SplineCoef c = coef_of(L, pairs);
                 {
-                    StageScope sc(h, "spline", (int)lv, L.g.n, 4, total);
-                    if ((e = launch_spline(s, pairs, L.d_cy.as<double>(), L.d_cpy.as<double>(), L.g.tiles_i,
-                                           L.d_cx.as<double>(), L.d_cpx.as<double>(), L.g.tiles_j, u, v, c)) !=
-                        cudaSuccess)
+                    StageScope sc(h, "spline", (int)lv, L.g.n, 1, total);
+                    if ((e = launch_spline(s, pairs, L.d_kfy.as<float2>(), L.g.tiles_i, L.d_kfx.as<float2>(),
+                                           L.g.tiles_j, u, v, c)) != cudaSuccess)
                         return cuda_fail(e, "spline");
                 }
                 {
@@ -461,7 +455,7 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
                                          full_image_mode(d.warp_mode))) != cudaSuccess)
                         return cuda_fail(e, "warp");
                 }
-                h->launches += 5;
+                h->launches += 2;
                 src = p->warped_table.as<qlpiv_frame>();
             }
         } else {
@@ -605,7 +599,7 @@ size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int heigh
             return 0;
         const size_t ni = g.tiles_i, nj = g.tiles_j, cnt = ni * nj, tot = cnt * pairs;
         total += al(8 * ni) + al(8 * nj) + al(4 * ni) + al(4 * nj) + al(8 * ni) + al(8 * nj);
-        total += 5 * al(4 * tot) + 2 * al(4 * tot) + al(coef_bytes((long)tot));
+        total += 5 * al(4 * tot) + 2 * al(4 * tot) + al(spline_coef_bytes((long)tot));
         if (lv > 0) total += al(8 * (size_t)pairs * ni * prev_nj);
         if (lv > 0 && d->inherit_mode != QLPIV_INHERIT_BICUBIC_SPLINE) total += al(8 * (ni + nj));
         total += al(4 * ni) + al(4 * nj);
@@ -772,9 +766,9 @@ qlpiv_status qlpiv_inherit_tiles(qlpiv_handle *h, int mode, int pn, int pni, int
     return QLPIV_OK;
 }
 
-// Shared set-up of qlpiv_displacement_field / qlpiv_warp_pair: knots (double for the
-// solve, float for the evaluation) and displacements uploaded, spline nodes computed.
-// Uses scratch[0..5] and scratch[8] (float knots: ni row knots then nj column knots).
+// Shared set-up of qlpiv_displacement_field / qlpiv_warp_pair: knot factors (double, for the
+// solve), float knots (for the evaluation) and displacements uploaded, spline nodes computed.
+// Uses scratch[2..5] and scratch[8] (float knots: ni row knots then nj column knots).
 static qlpiv_status field_setup(qlpiv_handle *h, int ni, int nj, const double *ci, const double *cj, const float *u,
                                 const float *v, SplineCoef *coef) {
     cudaStream_t s = h->stream;
@@ -783,21 +777,22 @@ static qlpiv_status field_setup(qlpiv_handle *h, int ni, int nj, const double *c
     std::vector<float> fk(ni + nj);
     for (int i = 0; i < ni; i++) fk[i] = (float)ci[i];
     for (int j = 0; j < nj; j++) fk[ni + j] = (float)cj[j];
+    std::vector<float2> kf((size_t)KF_ARRAYS * (ni + nj));
+    knot_factors_dw(ci, ni, kf.data());
+    knot_factors_dw(cj, nj, kf.data() + (size_t)KF_ARRAYS * ni);
     cudaError_t e;
-    if ((e = upload(b[0], ci, sizeof(double) * ni, s)) != cudaSuccess ||
-        (e = upload(b[1], cj, sizeof(double) * nj, s)) != cudaSuccess ||
-        (e = upload(b[2], u, sizeof(float) * cnt, s)) != cudaSuccess ||
+    if ((e = upload(b[2], u, sizeof(float) * cnt, s)) != cudaSuccess ||
         (e = upload(b[3], v, sizeof(float) * cnt, s)) != cudaSuccess ||
-        (e = b[4].ensure(sizeof(double) * (ni + nj))) != cudaSuccess ||
-        (e = b[5].ensure(coef_bytes(cnt))) != cudaSuccess ||
+        (e = upload(b[4], kf.data(), sizeof(float2) * kf.size(), s)) != cudaSuccess ||
+        (e = b[5].ensure(spline_coef_bytes(cnt))) != cudaSuccess ||
         (e = upload(b[8], fk.data(), sizeof(float) * (ni + nj), s)) != cudaSuccess)
         return cuda_fail(e, "field upload");
-    *coef = coef_at(b[5].p, cnt);
-    if ((e = launch_spline(s, 1, b[0].as<double>(), b[4].as<double>(), ni, b[1].as<double>(), b[4].as<double>() + ni,
-                           nj, b[2].as<float>(), b[3].as<float>(), *coef)) != cudaSuccess)
+    *coef = spline_coef_at(b[5].p, cnt);
+    if ((e = launch_spline(s, 1, b[4].as<float2>(), ni, b[4].as<float2>() + (size_t)KF_ARRAYS * ni, nj,
+                           b[2].as<float>(), b[3].as<float>(), *coef)) != cudaSuccess)
         return cuda_fail(e, "spline");
-    h->launches += 4;
-    // the float knots must outlive this function's host vector: wait for the upload
+    h->launches += 1;
+    // the host staging must outlive this function's vectors: wait for the uploads
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "field set-up");
     return QLPIV_OK;
 }
@@ -990,18 +985,17 @@ static qlpiv_status queue_flow(qlpiv_handle *h, const qlpiv_flow_desc &flow, con
     // level used the inherited displacements; the coefficients are free again)
     const SplineCoef all = coef_of(L, p->pairs);
     if (h->profiling) on_mark(&mc, "flow:spline", true);
-    if ((e = launch_spline(s, p->pairs, L.d_cy.as<double>(), L.d_cpy.as<double>(), ni, L.d_cx.as<double>(),
-                           L.d_cpx.as<double>(), nj, L.d_u.as<float>(), L.d_v.as<float>(), all)) != cudaSuccess)
+    if ((e = launch_spline(s, p->pairs, L.d_kfy.as<float2>(), ni, L.d_kfx.as<float2>(), nj, L.d_u.as<float>(),
+                           L.d_v.as<float>(), all)) != cudaSuccess)
         return cuda_fail(e, "flow spline");
     if (h->profiling) on_mark(&mc, "flow:spline", false);
-    h->launches += 4;
+    h->launches += 1;
     for (int q = 0; q < p->pairs; q++) {
         long launches = 0;
         const long off = (long)q * cnt;
-        const SplineCoef pc{all.fy_u + off, all.fx_u + off, all.fyx_u + off, all.fy_v + off, all.fx_v + off,
-                            all.fyx_v + off, all.c4_u + off, all.c4_v + off};
+        const SplineCoef pc = spline_coef_offset(all, off);
         if ((e = run_flow(s, fd, p->pixel_type, frames[q].img_a, frames[q].img_b, frames[q].pitch, p->height,
-                          p->width, L.g.n, ni, nj, L.d_cy.as<double>(), L.d_cx.as<double>(), L.d_cyf.as<float>(),
+                          p->width, L.g.n, ni, nj, L.d_kfy.as<float2>(), L.d_kfx.as<float2>(), L.d_cyf.as<float>(),
                           L.d_cxf.as<float>(), L.d_tops.as<int>(), L.d_lefts.as<int>(), L.d_u.as<float>() + q * cnt,
                           L.d_v.as<float>() + q * cnt, dense_u ? dense_u + q * np : nullptr,
                           dense_v ? dense_v + q * np : nullptr, fb, &launches,
