@@ -91,9 +91,31 @@ qlpiv_status check_pixel(int pixel_type) {
 }
 
 qlpiv_status launch(qlpiv_handle *h, const qlpiv::IaJob &job, int n, int pixel_type) {
-    cudaError_t e = qlpiv::launch_xcorr(job, n, pixel_type, h->stream, h->num_sms);
+    qlpiv::IaJob j = job;
+    cudaError_t e;
+    if (j.num_peaks >= 1 && j.num_peaks <= 4 && n <= 64 &&
+        (j.subpix == QLPIV_SUBPIX_NONE || j.subpix == QLPIV_SUBPIX_GAUSS3)) {
+        // the batched multi-peak replay (the handle's buffers: its calls share one stream)
+        if (h->mp_units == 0) {
+            long units = 0;
+            const size_t bytes = qlpiv::xcorr_batch_bytes(h->num_sms, &units);
+            const size_t sb = qlpiv::xcorr_batch_slot_bytes(units);
+            if ((e = h->mp_batch.ensure(bytes)) != cudaSuccess || (e = h->mp_slots.ensure(sb)) != cudaSuccess ||
+                (e = cudaMemsetAsync(h->mp_slots.p, 0, sb, h->stream)) != cudaSuccess)
+                return cuda_fail(e, "multi-peak batch buffers");
+            h->mp_units = units;
+        }
+        if ((e = h->mp_retry.ensure(sizeof(int) * (size_t)(1 + j.count))) != cudaSuccess)
+            return cuda_fail(e, "multi-peak retry list");
+        j.mp_batch = h->mp_batch.as<qlpiv::MpBatch>();
+        j.mp_batch_units = h->mp_units;
+        j.mp_slots = h->mp_slots.as<unsigned>();
+        j.mp_retry = h->mp_retry.as<int>();
+    }
+    int nk = 1;
+    e = qlpiv::launch_xcorr(j, n, pixel_type, h->stream, h->num_sms, &nk);
     if (e != cudaSuccess) return cuda_fail(e, "xcorr kernel launch");
-    h->launches++;
+    h->launches += nk;
     return QLPIV_OK;
 }
 
@@ -296,7 +318,7 @@ qlpiv_status qlpiv_destroy(qlpiv_handle *h) {
             cudaStreamDestroy(h->own_stream);
         }
         for (DevBuf *b : {&h->tiles_a, &h->tiles_b, &h->max_a, &h->max_b, &h->origins, &h->vectors, &h->planes,
-                          &h->frames})
+                          &h->frames, &h->mp_batch, &h->mp_slots, &h->mp_retry})
             b->release();
         for (DevBuf &b : h->scratch) b.release();
         for (qlpiv::StageEvent &ev : h->prof_pending) {

@@ -108,6 +108,10 @@ struct qlpiv_handle {
     long launches = 0;
     qlpiv::DevBuf tiles_a, tiles_b, max_a, max_b, origins, vectors, planes, frames;
     qlpiv::DevBuf scratch[12];           // stage test hooks
+    // batched multi-peak replay of the tile / frame pass entry points (one stream: one set):
+    // batches, their claim bitmask (zeroed when allocated) and the retry list
+    qlpiv::DevBuf mp_batch, mp_slots, mp_retry;
+    long mp_units = 0;
     qlpiv::AdaptivePlan *plan = nullptr; // cached adaptive PIV plan
     bool profiling = false;
     std::vector<qlpiv::StageEvent> prof_pending;

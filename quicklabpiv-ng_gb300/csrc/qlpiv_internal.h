@@ -16,9 +16,16 @@ cudaError_t ensure_twiddles(int dev, const cplx **table);
 // log_fpair table of `dev` (valid after ensure_twiddles on that device).
 const float4 *log_table(int dev);
 
-// K1 fused FFT-PIV over job.count IAs of side n on `stream`.
-cudaError_t launch_xcorr(const IaJob &job, int n, int pixel_type, cudaStream_t stream, int num_sms);
+// K1 fused FFT-PIV over job.count IAs of side n on `stream`; *nlaunch (optional): kernels queued.
+cudaError_t launch_xcorr(const IaJob &job, int n, int pixel_type, cudaStream_t stream, int num_sms,
+                         int *nlaunch = nullptr);
 bool xcorr_size_supported(int n);
+// Device bytes of the batched multi-peak replay buffer (IaJob.mp_batch) for a launch site on a GPU
+// with num_sms SMs; *units = IaJob.mp_batch_units.  The slot bitmask (IaJob.mp_slots, zeroed once;
+// every launch leaves it zero) takes xcorr_batch_slot_bytes(units); the retry list (IaJob.mp_retry)
+// 1 + count ints.
+size_t xcorr_batch_bytes(int num_sms, long *units);
+size_t xcorr_batch_slot_bytes(long units);
 // FindMaximumMultiPeaks settings the kernel supports for IA side n (records fit on chip).
 bool multipeak_supported(int n, int num_peaks, int peak_kernel);
 

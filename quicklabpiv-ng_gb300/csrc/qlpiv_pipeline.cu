@@ -55,6 +55,10 @@ struct AdaptivePlan {
     DevBuf host_table;
     DevBuf flow;          // optical flow after PIV: one pair's planes (FlowBufs)
     DevBuf flow_dense;    // dense field of the host variant, 2 x pairs x height x width
+    DevBuf mp_batch;      // batched multi-peak replay of the correlation passes: batches,
+    DevBuf mp_slots;      //   their claim bitmask (zeroed at allocation, zero between launches)
+    DevBuf mp_retry;      //   and the list of IAs to run again (1 + tiles of the largest level)
+    long mp_units = 0;
 };
 
 void destroy_plan(AdaptivePlan *p) {
@@ -65,7 +69,8 @@ void destroy_plan(AdaptivePlan *p) {
                           &l.d_rank, &l.d_bu, &l.d_bv, &l.d_puv, &l.d_npk, &l.d_state, &l.d_list, &l.d_done,
                           &l.d_sweeps, &l.d_tiles, &l.d_tmax})
             b->release();
-    for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table, &p->flow, &p->flow_dense})
+    for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table, &p->flow, &p->flow_dense,
+                      &p->mp_batch, &p->mp_slots, &p->mp_retry})
         b->release();
     delete p;
 }
@@ -81,6 +86,11 @@ static int full_image_mode(int m) {
     return m == QLPIV_WARP_BOTH_BILINEAR ? 3 : (m == QLPIV_WARP_FIRST_BILINEAR ? 1 : 2);
 }
 static int tile_image_mode(int m) { return (m - QLPIV_WARP_FIRST_MICRO) % 3 + 1; }
+// The correlation passes replay their multi-peak lists in batches (mp_batched).
+static bool batched_replay(const qlpiv_adaptive_desc &d) {
+    return d.validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN && d.num_peaks >= 1 && d.num_peaks <= 4 &&
+           (d.subpix_mode == QLPIV_SUBPIX_NONE || d.subpix_mode == QLPIV_SUBPIX_GAUSS3);
+}
 static bool tile_mini(int m) { return m >= QLPIV_WARP_FIRST_MINI; }
 
 static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type, int height, int width) {
@@ -327,6 +337,18 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
         // the host vectors above die at scope exit: make the copies complete first
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "adaptive plan upload");
     }
+    if (batched_replay(*d)) {
+        long units = 0, most = 0;
+        for (const LevelPlan &l : p->levels) most = l.count() * pairs > most ? l.count() * pairs : most;
+        const size_t batch_bytes = xcorr_batch_bytes(h->num_sms, &units);
+        const size_t slot_bytes = xcorr_batch_slot_bytes(units);
+        if ((e = p->mp_batch.ensure(batch_bytes)) != cudaSuccess ||
+            (e = p->mp_slots.ensure(slot_bytes)) != cudaSuccess ||
+            (e = cudaMemsetAsync(p->mp_slots.p, 0, slot_bytes, h->stream)) != cudaSuccess ||
+            (e = p->mp_retry.ensure(sizeof(int) * (size_t)(1 + most))) != cudaSuccess)
+            return cuda_fail(e, "multi-peak batch buffers");
+        p->mp_units = units;
+    }
     if (full_warp(d->warp_mode)) {
         const size_t img = (size_t)height * width * pixel_bytes(pixel_type);
         const size_t stride = (img + 255) & ~(size_t)255;
@@ -520,13 +542,20 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
             job.peak_kernel = d.peak_kernel;
             job.peak_uv = L.d_puv.as<float2>();
             job.npeaks = L.d_npk.as<uint8_t>();
+            if (p->mp_units > 0) {
+                job.mp_batch = p->mp_batch.as<MpBatch>();
+                job.mp_batch_units = p->mp_units;
+                job.mp_slots = p->mp_slots.as<unsigned>();
+                job.mp_retry = p->mp_retry.as<int>();
+            }
         }
+        int nk = 1;
         {
             StageScope sc(h, "xcorr", (int)lv, L.g.n, 1, total);
-            if ((e = launch_xcorr(job, L.g.n, p->pixel_type, s, h->num_sms)) != cudaSuccess)
+            if ((e = launch_xcorr(job, L.g.n, p->pixel_type, s, h->num_sms, &nk)) != cudaSuccess)
                 return cuda_fail(e, "xcorr");
         }
-        h->launches++;
+        h->launches += nk;
         if (validate) {
             StageScope sc(h, "validate", (int)lv, L.g.n, 2, total);
             ValidateParams vp{L.g.tiles_i, L.g.tiles_j, validation_strategies(d), d.median_threshold,
@@ -598,7 +627,7 @@ size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int heigh
                                0) < -1)
             return 0;
         const size_t ni = g.tiles_i, nj = g.tiles_j, cnt = ni * nj, tot = cnt * pairs;
-        total += al(8 * ni) + al(8 * nj) + al(4 * ni) + al(4 * nj) + al(8 * ni) + al(8 * nj);
+        total += al(8 * KF_ARRAYS * ni) + al(8 * KF_ARRAYS * nj) + al(4 * ni) + al(4 * nj);
         total += 5 * al(4 * tot) + 2 * al(4 * tot) + al(spline_coef_bytes((long)tot));
         if (lv > 0) total += al(8 * (size_t)pairs * ni * prev_nj);
         if (lv > 0 && d->inherit_mode != QLPIV_INHERIT_BICUBIC_SPLINE) total += al(8 * (ni + nj));
@@ -616,6 +645,17 @@ size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int heigh
     const size_t stride = (img + 255) & ~(size_t)255;
     total += al(2 * stride * pairs) + al(sizeof(qlpiv_frame) * pairs);  // frames copied from the host
     if (full_warp(d->warp_mode)) total += al(2 * stride * pairs) + al(sizeof(qlpiv_frame) * pairs);
+    if (batched_replay(*d)) {
+        int dev = 0, sms = 0;
+        long units = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+            total += al(xcorr_batch_bytes(sms, &units)) + al(xcorr_batch_slot_bytes(units));
+        qlpiv_grid g{};
+        if (grid_superposition(height, width, d->margins, d->ia_start, nlev - 1, d->overlap_factor, &g, nullptr,
+                               nullptr, 0) >= -1)
+            total += al(sizeof(int) * (1 + (size_t)g.tiles_i * g.tiles_j * pairs));
+    }
     return total;
 }
 

@@ -64,8 +64,31 @@ constexpr int kMultiWaves = 32;
 
 constexpr size_t kSubpixSmem = sizeof(float) * 32 * 2 * kMaxSubpixPixels;
 
+// The batched multi-peak replay (mp_batched) applies to the job and its buffers were given.
+static bool batch_eligible(const IaJob &job) {
+    return job.mp_batch != nullptr && job.mp_slots != nullptr && job.mp_retry != nullptr && job.mp_batch_units > 0 &&
+           job.ia_list == nullptr && job.num_peaks >= 1 && job.num_peaks <= 4 &&
+           (job.subpix == QLPIV_SUBPIX_NONE || job.subpix == QLPIV_SUBPIX_GAUSS3);
+}
+
+// Batched launch: the retry count is zeroed before the main launch; the IAs it flags run again
+// through the per-IA path in a second launch of `retry_grid` units over the device list.
+template <typename Launch>
+static cudaError_t launch_batched(const IaJob &j, long grid, long retry_grid, cudaStream_t stream, Launch launch,
+                                  int *nlaunch) {
+    cudaError_t e = cudaMemsetAsync(j.mp_retry, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return e;
+    if ((e = launch(j, grid)) != cudaSuccess) return e;
+    IaJob r = j;
+    r.mp_batch = nullptr;
+    r.ia_list = j.mp_retry;
+    if ((e = launch(r, retry_grid)) != cudaSuccess) return e;
+    if (nlaunch) *nlaunch = 2;
+    return cudaSuccess;
+}
+
 template <int N, typename Pix, bool PP>
-static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms) {
+static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms, int *nlaunch) {
     using S = XcorrShape<N>;
     // The shared-memory opt-in is a per-device attribute of the function: set it once
     // per (instantiation, device).
@@ -95,19 +118,26 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
     j.twiddles = tw + twiddle_offset(S::M);
     j.log_tab = log_table(dev);
     // every CTA loops over IAs; eight waves of CTAs balance the single-peak kernel best, 32 the
-    // multi-peak one
+    // multi-peak one; the batched multi-peak replay runs one resident wave (a batch per CTA)
     long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? kMultiWaves : 8));
     if (grid > job.count) grid = job.count;
     if (grid < 1) return cudaSuccess;
     // P-point sub-pixel stencils: 2 P floats per queued fit after the fixed layout
     const size_t smem = S::SMEM + (j.subpix_pixels > 0 ? sizeof(float) * 32 * 2 * j.subpix_pixels : 0);
-    xcorr_kernel<N, Pix, PP><<<(unsigned)grid, S::T, smem, stream>>>(j);
-    return cudaGetLastError();
+    auto launch = [&](const IaJob &jj, long g) {
+        xcorr_kernel<N, Pix, PP><<<(unsigned)g, S::T, smem, stream>>>(jj);
+        return cudaGetLastError();
+    };
+    // the batched replay needs a batch for every resident CTA
+    if (batch_eligible(job) && (long)num_sms * bps <= job.mp_batch_units)
+        return launch_batched(j, grid, (long)num_sms * bps, stream, launch, nlaunch);
+    j.mp_batch = nullptr;
+    return launch(j, grid);
 }
 
 // IA 16: one warp per IA, w16::kWarps warps per CTA, `waves` waves of resident CTAs.
 template <typename Pix, bool PP>
-static cudaError_t launch_warp16(const IaJob &job, cudaStream_t stream, int num_sms) {
+static cudaError_t launch_warp16(const IaJob &job, cudaStream_t stream, int num_sms, int *nlaunch) {
     static std::mutex mu;
     static int blocks_per_sm[kMaxDevices] = {0};
     int dev = 0;
@@ -119,11 +149,14 @@ static cudaError_t launch_warp16(const IaJob &job, cudaStream_t stream, int num_
     {
         std::lock_guard<std::mutex> lock(mu);
         if (blocks_per_sm[dev] == 0) {
-            e = cudaFuncSetAttribute(xcorr16_warp_kernel<Pix, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            e = cudaFuncSetAttribute(xcorr16_warp_kernel<Pix, PP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)(base + w16::kWarps * kSubpixSmem));
+            if (e == cudaSuccess && !PP)
+                e = cudaFuncSetAttribute(xcorr16_warp_kernel<Pix, PP, !PP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(base + w16::kWarps * kSubpixSmem));
             if (e != cudaSuccess) return e;
             int b = 0;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, xcorr16_warp_kernel<Pix, PP>, w16::kThreads,
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, xcorr16_warp_kernel<Pix, PP, false>, w16::kThreads,
                                                               base);
             if (e != cudaSuccess) return e;
             blocks_per_sm[dev] = b < 1 ? 1 : b;
@@ -140,13 +173,25 @@ static cudaError_t launch_warp16(const IaJob &job, cudaStream_t stream, int num_
     if (grid > need) grid = need;
     if (grid < 1) return cudaSuccess;
     const size_t smem = base + (j.subpix_pixels > 0 ? w16::kWarps * sizeof(float) * 32 * 2 * j.subpix_pixels : 0);
-    xcorr16_warp_kernel<Pix, PP><<<(unsigned)grid, w16::kThreads, smem, stream>>>(j);
-    return cudaGetLastError();
+    // the batched main launch runs the BATCH instantiation (P-point fits are never batched), the
+    // retry launch the per-IA one
+    auto launch = [&](const IaJob &jj, long g) {
+        if (!PP && jj.mp_batch != nullptr)
+            xcorr16_warp_kernel<Pix, PP, !PP><<<(unsigned)g, w16::kThreads, smem, stream>>>(jj);
+        else
+            xcorr16_warp_kernel<Pix, PP, false><<<(unsigned)g, w16::kThreads, smem, stream>>>(jj);
+        return cudaGetLastError();
+    };
+    // the batched replay needs a batch for every resident warp
+    if (batch_eligible(job) && (long)num_sms * bps * w16::kWarps <= job.mp_batch_units)
+        return launch_batched(j, grid, (long)num_sms * bps, stream, launch, nlaunch);
+    j.mp_batch = nullptr;
+    return launch(j, grid);
 }
 
 // IA 128: one cluster of two CTAs per IA, one CTA per SM; `waves` clusters per SM pair.
 template <typename Pix, bool PP>
-static cudaError_t launch_pair(const IaJob &job, cudaStream_t stream, int num_sms) {
+static cudaError_t launch_pair(const IaJob &job, cudaStream_t stream, int num_sms, int * /*nlaunch*/) {
     static std::mutex mu;
     static bool ready[kMaxDevices] = {false};
     int dev = 0;
@@ -167,6 +212,7 @@ static cudaError_t launch_pair(const IaJob &job, cudaStream_t stream, int num_sm
     IaJob j = job;
     j.twiddles = tw + twiddle_offset(256);
     j.log_tab = log_table(dev);
+    j.mp_batch = nullptr;
     // multi-peak mode: one resident wave (the fit queue fills between flushes), as K1
     long grid = (long)(num_sms & ~1) * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? 1 : 4));
     if (grid > 2 * job.count) grid = 2 * job.count;
@@ -194,44 +240,43 @@ static cudaError_t launch_pair(const IaJob &job, cudaStream_t stream, int num_sm
     return cudaGetLastError();
 }
 
-// development switch between two IA-16 kernels (QLPIV_K1_VARIANT=1: the CTA-per-IA kernel)
-static int k1_variant() {
-    static int v = -1;
-    if (v < 0) {
-        const char *e = getenv("QLPIV_K1_VARIANT");
-        v = e ? atoi(e) : 0;
-    }
-    return v;
-}
-
 template <typename Pix, bool PP>
-static cudaError_t launch_pix(const IaJob &job, int n, cudaStream_t stream, int num_sms) {
+static cudaError_t launch_pix(const IaJob &job, int n, cudaStream_t stream, int num_sms, int *nlaunch) {
     switch (n) {
-        case 16: return k1_variant() == 1 ? launch_one<16, Pix, PP>(job, stream, num_sms)
-                                          : launch_warp16<Pix, PP>(job, stream, num_sms);
-        case 32: return launch_one<32, Pix, PP>(job, stream, num_sms);
-        case 64: return launch_one<64, Pix, PP>(job, stream, num_sms);
-        case 128: return launch_pair<Pix, PP>(job, stream, num_sms);
+        case 16: return launch_warp16<Pix, PP>(job, stream, num_sms, nlaunch);
+        case 32: return launch_one<32, Pix, PP>(job, stream, num_sms, nlaunch);
+        case 64: return launch_one<64, Pix, PP>(job, stream, num_sms, nlaunch);
+        case 128: return launch_pair<Pix, PP>(job, stream, num_sms, nlaunch);
         default: return cudaErrorInvalidValue;
     }
 }
 
 template <typename Pix>
-static cudaError_t launch_pix(const IaJob &job, int n, cudaStream_t stream, int num_sms) {
-    return job.subpix_pixels > 0 ? launch_pix<Pix, true>(job, n, stream, num_sms)
-                                 : launch_pix<Pix, false>(job, n, stream, num_sms);
+static cudaError_t launch_pix(const IaJob &job, int n, cudaStream_t stream, int num_sms, int *nlaunch) {
+    return job.subpix_pixels > 0 ? launch_pix<Pix, true>(job, n, stream, num_sms, nlaunch)
+                                 : launch_pix<Pix, false>(job, n, stream, num_sms, nlaunch);
 }
 
-cudaError_t launch_xcorr(const IaJob &job, int n, int pixel_type, cudaStream_t stream, int num_sms) {
+cudaError_t launch_xcorr(const IaJob &job, int n, int pixel_type, cudaStream_t stream, int num_sms, int *nlaunch) {
+    if (nlaunch) *nlaunch = 1;
     switch (pixel_type) {
-        case QLPIV_PIX_U8: return launch_pix<uint8_t>(job, n, stream, num_sms);
-        case QLPIV_PIX_U16: return launch_pix<uint16_t>(job, n, stream, num_sms);
-        case QLPIV_PIX_F32: return launch_pix<float>(job, n, stream, num_sms);
+        case QLPIV_PIX_U8: return launch_pix<uint8_t>(job, n, stream, num_sms, nlaunch);
+        case QLPIV_PIX_U16: return launch_pix<uint16_t>(job, n, stream, num_sms, nlaunch);
+        case QLPIV_PIX_F32: return launch_pix<float>(job, n, stream, num_sms, nlaunch);
         default: return cudaErrorInvalidValue;
     }
 }
 
 bool xcorr_size_supported(int n) { return n == 16 || n == 32 || n == 64 || n == 128; }
+
+// Resident batching units per SM at most (16 warps of the IA-16 kernel; the CTA kernels hold
+// fewer CTAs).
+constexpr long kMpUnitsPerSm = 16;
+size_t xcorr_batch_bytes(int num_sms, long *units) {
+    *units = kMpUnitsPerSm * num_sms;
+    return sizeof(MpBatch) * (size_t)*units;
+}
+size_t xcorr_batch_slot_bytes(long units) { return sizeof(unsigned) * (size_t)((units + 31) / 32); }
 
 template <int N>
 static bool multipeak_fits_n(int kw) {

@@ -132,6 +132,14 @@ struct IaJob {
     int waves;                   // grid = SMs x resident CTAs x waves; 0: the default per mode
     float *mp_planes;            // IA 128 multi-peak mode: one (2N-1)^2 plane per cluster (set by the launcher)
     const float4 *log_tab;       // log_fpair table (device, filled once per device with the twiddles)
+    // batched multi-peak replay (NULL mp_batch: every IA replays its own list): mp_batch_units
+    // batches, claimed by the resident warps (IA 16) or CTAs through the zeroed bitmask mp_slots;
+    // IAs whose replay needs records that were not stored go to mp_retry ([0] count, then IAs)
+    struct MpBatch *mp_batch;
+    long mp_batch_units;
+    unsigned *mp_slots;
+    int *mp_retry;
+    const int *ia_list;          // non-NULL: run IAs ia_list[1 .. 1 + ia_list[0]] instead of 0 .. count-1
 };
 
 // Integer peak and 3-point stencil of one IA, queued for the sub-pixel fit.
@@ -669,6 +677,322 @@ __device__ __forceinline__ void multipeak_core(const IaJob &job, long ia, float 
     }
 }
 
+// ---- Batched multi-peak replay ----
+// The list replay of one IA is a short chain of dependent insertions (4 to 9 on the adaptive
+// PIV planes) that a warp runs with every lane doing the same work.  Instead, the records the
+// replay of an IA can reach are stored with the 3-point stencil at their position, kMpBatch
+// IAs to a batch, and one warp replays the whole batch with one IA per lane.  Stored per IA:
+// every record >= t, t = the 4th largest maximum of 32 consecutive records (the run over those
+// records alone is exact whenever it ends with a full list, see mp_replay), and the last
+// kMpTail records, from which the run resumes when its last full-to-room transition lies there.
+// An IA whose replay needs records that were not stored (more than kMpCandMax of them, t == 0,
+// or an earlier resume point) is flagged and run again through the per-IA path.  Used for
+// k <= 4 peaks with the 3-point fit or none (the P-point stencils are not stored).
+constexpr int kMpBatch = 32, kMpCandMax = 24, kMpTail = 8;
+struct __align__(16) MpCand {
+    float v;
+    int code;  // record e << 14 | i << 7 | j (resolved position: planes of side <= 127)
+    float c0, yu, yd, xl, xr, pad;
+};
+struct __align__(16) MpMeta {
+    long ia;
+    float mn, t;
+    int n, retry;
+    int pad[2];
+};
+struct MpBatch {
+    MpMeta meta[kMpBatch];
+    MpCand cand[kMpCandMax][kMpBatch];  // candidate-major: a lane's reads of one slot coalesce
+};
+static_assert(sizeof(MpCand) == 32 && sizeof(MpMeta) == 32, "batch layout");
+
+__device__ __forceinline__ bool mp_batched(const IaJob &job) {
+    return job.mp_batch != nullptr && job.num_peaks >= 1 && job.num_peaks <= 4 &&
+           (job.subpix == QLPIV_SUBPIX_NONE || job.subpix == QLPIV_SUBPIX_GAUSS3);
+}
+
+// Claims a free batch (bit of the zeroed bitmask `slots`, `units` bits) for the calling warp or
+// CTA, starting the search at word `hint`; -1 when a bounded search found none (the caller then
+// replays per IA).  At most `units` warps / CTAs are resident, so one is normally free.
+__device__ __forceinline__ int mp_claim(unsigned *slots, long units, int hint) {
+    const int words = (int)((units + 31) / 32);
+    for (int k = 0; k < 4 * words; k++) {
+        const int w = (hint + k) % words;
+        unsigned avail = ~*reinterpret_cast<volatile unsigned *>(slots + w);
+        if (w == words - 1 && (units & 31) != 0) avail &= (1u << (units & 31)) - 1u;
+        while (avail != 0u) {
+            const unsigned bit = avail & (0u - avail);
+            const unsigned old = atomicOr(slots + w, bit);
+            if ((old & bit) == 0u) return w * 32 + (__ffs(bit) - 1);
+            avail &= ~(old | bit);
+        }
+    }
+    return -1;
+}
+
+// Returns batch s once its last replay is done.
+__device__ __forceinline__ void mp_release(unsigned *slots, int s) {
+    __threadfence();
+    atomicAnd(slots + (s >> 5), ~(1u << (s & 31)));
+}
+
+// Stores IA `ia`'s reachable records (staged by mp_cells) as entry b of the batch.  One full warp.
+template <int D, typename Plane>
+__device__ void mp_extract(const MpGeom &gm, const Plane &P, const float *recv, const int *recp, const float *chmax,
+                           int lane, long ia, float mn, MpBatch *bt, int b) {
+    static_assert(D <= 127, "record positions are packed in 7 bits");
+    // t: 4th largest chunk maximum; keys = float bits + 1 (records are >= +0), 0 = taken
+    unsigned key[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int c = lane + 32 * q;
+        key[q] = c < gm.nchunk ? __float_as_uint(chmax[c]) + 1u : 0u;
+    }
+    unsigned tk = 0u;
+    const int rounds = gm.nchunk < 4 ? gm.nchunk : 4;
+    for (int r = 0; r < rounds; r++) {
+        const unsigned lm = max(max(key[0], key[1]), max(key[2], key[3]));
+        const unsigned wm = __reduce_max_sync(0xffffffffu, lm);
+        const int owner = __ffs(__ballot_sync(0xffffffffu, lm == wm)) - 1;
+        if (lane == owner) {
+            if (key[0] == wm) key[0] = 0u;
+            else if (key[1] == wm) key[1] = 0u;
+            else if (key[2] == wm) key[2] = 0u;
+            else key[3] = 0u;
+        }
+        tk = wm;
+    }
+    const float t = __uint_as_float(tk - 1u);
+    const bool ok = tk > 1u && t > 0.0f;
+    const int tail = gm.nrec - kMpTail;
+    const unsigned lt = (1u << lane) - 1u;
+    int base = 0;
+    if (ok) {
+        for (int c0 = 0; c0 < gm.nchunk; c0 += 32) {
+            const int c = c0 + lane;
+            unsigned todo = __ballot_sync(0xffffffffu, c < gm.nchunk && (chmax[c] >= t || (c + 1) * 32 > tail));
+            while (todo != 0u) {
+                const int cl = __ffs(todo) - 1;
+                todo &= todo - 1u;
+                const int e = (c0 + cl) * 32 + lane;
+                const float v = e < gm.nrec ? recv[e] : 0.0f;
+                const bool take = e < gm.nrec && (v >= t || e >= tail);
+                const unsigned mask = __ballot_sync(0xffffffffu, take);
+                const int idx = base + __popc(mask & lt);
+                if (take && idx < kMpCandMax) {
+                    int pp = recp[e];
+                    if (pp < 0) {  // stale: the quadrant's previous position, else (0, 0)
+                        pp = 0;
+                        for (int e2 = e - 4; e2 >= 0; e2 -= 4)
+                            if (recp[e2] >= 0) { pp = recp[e2]; break; }
+                    }
+                    const int pi = pp >> 16, pj = pp & 0xffff;
+                    MpCand cd;
+                    cd.v = v;
+                    cd.code = (e << 14) | (pi << 7) | pj;
+                    cd.c0 = cd.yu = cd.yd = cd.xl = cd.xr = cd.pad = 0.0f;
+                    if (pi >= 1 && pi <= D - 2 && pj >= 1 && pj <= D - 2) {
+                        cd.c0 = P(pi, pj);
+                        cd.yu = P(pi - 1, pj);
+                        cd.yd = P(pi + 1, pj);
+                        cd.xl = P(pi, pj - 1);
+                        cd.xr = P(pi, pj + 1);
+                    }
+                    bt->cand[idx][b] = cd;
+                }
+                base += __popc(mask);
+            }
+        }
+    }
+    if (lane == 0) {
+        MpMeta m;
+        m.ia = ia;
+        m.mn = mn;
+        m.t = t;
+        m.n = base < kMpCandMax ? base : kMpCandMax;
+        m.retry = (!ok || base > kMpCandMax) ? 1 : 0;
+        m.pad[0] = m.pad[1] = 0;
+        bt->meta[b] = m;
+    }
+    __syncwarp();
+}
+
+// Lane b's replay of batch entry b (b < nb) into lst; true when the entry must be run again.
+template <int K>
+__device__ __forceinline__ bool mp_batch_replay(const MpBatch *bt, int b, int k, float kd, int nrec,
+                                                RegPeakList<K> &lst, MpMeta &m) {
+    m = bt->meta[b];
+    if (m.retry) return true;
+    RegPeakList<K> saved;
+    int e_break = -1;
+    float2 nx = m.n > 0 ? *reinterpret_cast<const float2 *>(&bt->cand[0][b]) : make_float2(0.0f, 0.0f);
+    for (int s = 0; s < m.n; s++) {
+        // (value, code) of entry s; entry s + 1's is on its way meanwhile
+        const MpCand c{nx.x, __float_as_int(nx.y), 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        if (s + 1 < m.n) nx = *reinterpret_cast<const float2 *>(&bt->cand[s + 1][b]);
+        if (!(c.v >= m.t)) continue;
+        const int i = (c.code >> 7) & 127, j = c.code & 127;
+        if (lst.size == k) {
+            const RegPeakList<K> before = lst;
+            lst.insert(0, k, kd, c.v, i, j);
+            if (lst.size < k) {
+                saved = before;
+                e_break = c.code >> 14;
+            }
+        } else {
+            lst.insert(0, k, kd, c.v, i, j);
+        }
+    }
+    if (lst.size < k) {
+        // resume at the last full-to-room transition: every record from there on must be stored
+        if (e_break < 0 || e_break < nrec - kMpTail) return true;
+        lst = saved;
+        for (int s = 0; s < m.n; s++) {
+            const float2 c = *reinterpret_cast<const float2 *>(&bt->cand[s][b]);
+            const int code = __float_as_int(c.y);
+            if ((code >> 14) >= e_break) lst.insert(0, k, kd, c.x, (code >> 7) & 127, code & 127);
+        }
+    }
+    return false;
+}
+
+// Replays the nb entries of the batch (one per lane) and queues/flushes their fits, one peak
+// slot per round through fitq; the entries to run again go to job.mp_retry.  One full warp;
+// fitq must be empty.
+template <int D, int K, bool PP>
+__device__ void mp_batch_run_k(const MpBatch *bt, int nb, int lane, const IaJob &job, FitRec *fitq,
+                                   const float *fitv) {
+    const int k = job.num_peaks;
+    const MpGeom gm = mp_geom(D, job.peak_kernel);
+    const float kd = (float)((gm.kw - 1) * gm.kw);
+    RegPeakList<K> lst;
+    MpMeta m;
+    bool retry = true;
+    if (lane < nb) retry = mp_batch_replay<K>(bt, lane, k, kd, gm.nrec, lst, m);
+    const bool emit = lane < nb && !retry;
+    const unsigned em = __ballot_sync(0xffffffffu, emit);
+    const int slot_q = __popc(em & ((1u << lane) - 1u));
+    // stencils of the list entries: one pass over the stored records
+    float4 sa[K];
+    float sb[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) { sa[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f); sb[q] = 0.0f; }
+    if (emit) {
+        unsigned found = 0u;
+        for (int q2 = 0; q2 < m.n && found != (1u << lst.size) - 1u; q2++) {
+            const float4 *c = reinterpret_cast<const float4 *>(&bt->cand[q2][lane]);
+            const float4 h0 = c[0];
+            const int code = __float_as_int(h0.y) & 0x3fff;
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                if (q < lst.size && !((found >> q) & 1u) && code == ((lst.li[q] << 7) | lst.lj[q])) {
+                    const float4 h1 = c[1];
+                    sa[q] = make_float4(h0.z, h0.w, h1.x, h1.y);  // c0, yu, yd, xl
+                    sb[q] = h1.z;                                 // xr
+                    found |= 1u << q;
+                }
+            }
+        }
+    }
+    for (int s = 0; s < k; s++) {
+        if (emit) {
+            FitRec r;
+            r.ia = m.ia;
+            r.mn = m.mn;
+            r.slot = s;
+            r.npk = lst.size;
+            r.pi = 0;
+            r.pj = 0;
+            r.pv = 0.0f;
+            r.c0 = r.yu = r.yd = r.xl = r.xr = 0.0f;
+            r.kind = 4;
+            int idx = lst.size - 1 - s;
+            if (idx >= 0) {
+                float pv = 0.0f;
+                int pi = 0, pj = 0;
+                float4 st = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                float sx = 0.0f;
+#pragma unroll
+                for (int q = 0; q < K; q++)
+                    if (q == idx) { pv = lst.lv[q]; pi = lst.li[q]; pj = lst.lj[q]; st = sa[q]; sx = sb[q]; }
+                r.pi = pi;
+                r.pj = pj;
+                r.pv = pv;
+                if (!job.subpix) {
+                    r.kind = 3;
+                } else if (pi == 0 && pj == 0) {
+                    r.kind = 1;
+                } else if (pi - 1 < 0 || pi + 1 >= D || pj - 1 < 0 || pj + 1 >= D) {
+                    r.kind = 2;
+                } else {
+                    r.kind = 0;
+                    r.c0 = st.x;
+                    r.yu = st.y;
+                    r.yd = st.z;
+                    r.xl = st.w;
+                    r.xr = sx;
+                }
+            }
+            fitq[slot_q] = r;
+        }
+        fit_flush<D, PP>(fitq, fitv, __popc(em), lane, job);
+    }
+    if (lane < nb && retry) {
+        const int at = atomicAdd(job.mp_retry, 1);
+        job.mp_retry[1 + at] = (int)m.ia;
+    }
+    __syncwarp();
+}
+
+template <int D, bool PP>
+__device__ __noinline__ void mp_batch_run(const MpBatch *bt, int nb, int lane, const IaJob &job, FitRec *fitq,
+                                          const float *fitv) {
+    switch (job.num_peaks) {
+        case 1: mp_batch_run_k<D, 1, PP>(bt, nb, lane, job, fitq, fitv); break;
+        case 2: mp_batch_run_k<D, 2, PP>(bt, nb, lane, job, fitq, fitv); break;
+        case 3: mp_batch_run_k<D, 3, PP>(bt, nb, lane, job, fitq, fitv); break;
+        default: mp_batch_run_k<D, 4, PP>(bt, nb, lane, job, fitq, fitv); break;
+    }
+}
+
+// Step 5' in batched mode for one IA: every thread of the group stages the cell records (as
+// multipeak_core), then warp 0 stores the reachable ones as entry b of the batch.  Inlined into
+// the IA-16 warp kernel (a call per small IA would save its registers around it); the CTA
+// kernels call it out of line (multipeak_stage_call).
+template <int D, int T, typename Plane>
+__device__ __forceinline__ void multipeak_stage(const IaJob &job, long ia, float minf, const Plane &P, void *stage,
+                                                uint64_t *red, MpBatch *bt, int b) {
+    constexpr int NWARPS = T / 32;
+    const int lane = threadIdx.x & 31, warp = T == 32 ? 0 : (int)(threadIdx.x >> 5);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
+    group_sync<T>();
+    float *redf = reinterpret_cast<float *>(red);
+    if (lane == 0) redf[warp] = minf;
+    const MpGeom gm = mp_geom(D, job.peak_kernel);
+    float *recv = reinterpret_cast<float *>(stage);
+    int *recp = reinterpret_cast<int *>(recv + gm.nrec);
+    float *chmax = reinterpret_cast<float *>(recp + gm.nrec);
+    if (gm.kw == 3) {
+        mp_cells<D, T, 3>(gm, P, recv, recp, chmax);
+    } else {
+        mp_cells<D, T, 0>(gm, P, recv, recp, chmax);
+    }
+    group_sync<T>();
+    if (warp == 0) {
+        float mn = lane < NWARPS ? redf[lane] : 3.402823466e38f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mp_extract<D>(gm, P, recv, recp, chmax, lane, ia, mn, bt, b);
+    }
+}
+
+template <int D, int T, typename Plane>
+__device__ __noinline__ void multipeak_stage_call(const IaJob &job, long ia, float minf, const Plane &P, void *stage,
+                                                  uint64_t *red, MpBatch *bt, int b) {
+    multipeak_stage<D, T>(job, ia, minf, P, stage, red, bt, b);
+}
+
 // Step 5' of xcorr_kernel for one IA (kept out of line so that the single-peak path keeps its
 // register allocation): the plane is in the column-pair regions, the records go to the FFT
 // scratch, `multi` fit records are queued at fitq[qn..).  Called by every thread of the CTA.
@@ -715,7 +1039,19 @@ xcorr_kernel(IaJob job) {
     for (int e = tid; e < M; e += T) tw[e] = job.twiddles[e];
     __syncthreads();
 
-    for (long ia = blockIdx.x; ia < job.count; ia += gridDim.x) {
+    // batched multi-peak replay: a batch claimed for this CTA (filled and replayed by warp 0) and
+    // its fill (CTA-uniform)
+    __shared__ int s_slot;
+    MpBatch *mpb = nullptr;
+    if (multi > 0 && mp_batched(job)) {
+        if (tid == 0) s_slot = mp_claim(job.mp_slots, job.mp_batch_units, (int)(blockIdx.x % 1024u));
+        __syncthreads();
+        if (s_slot >= 0) mpb = job.mp_batch + s_slot;
+    }
+    int nb = 0;
+    const long count = job.ia_list != nullptr ? (long)job.ia_list[0] : job.count;
+    for (long k = blockIdx.x; k < count; k += gridDim.x) {
+        const long ia = job.ia_list != nullptr ? (long)job.ia_list[1 + k] : k;
         const Pix *imgA, *imgB;
         long pitch_a, pitch_b;
         int img_h, img_w;
@@ -983,17 +1319,30 @@ xcorr_kernel(IaJob job) {
                     fitq[qn] = r;
                 }
             }
-        } else {
+        } else if (mpb == nullptr) {
             multipeak_select<N>(job, ia, minf, regf, scr, red, fitq, fitv, qn, mp_lv, mp_li, mp_lj);
+        } else {
+            multipeak_stage_call<D, T>(job, ia, minf, P, scr, red, mpb, nb);
+            if (++nb == kMpBatch) {
+                if (warp == 0) mp_batch_run<D, PP>(mpb, nb, lane, job, fitq, fitv);
+                nb = 0;
+            }
         }
-        qn += KQ;
-        if (qn + KQ > 32) {
-            if (warp == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
-            qn = 0;
+        if (mpb == nullptr) {
+            qn += KQ;
+            if (qn + KQ > 32) {
+                if (warp == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
+                qn = 0;
+            }
         }
         __syncthreads();  // regions are rewritten by the next IA
     }
     if (qn > 0 && warp == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
+    if (mpb != nullptr) {
+        if (nb > 0 && warp == 0) mp_batch_run<D, PP>(mpb, nb, lane, job, fitq, fitv);
+        __syncthreads();
+        if (tid == 0) mp_release(job.mp_slots, s_slot);
+    }
 }
 
 }  // namespace qlpiv

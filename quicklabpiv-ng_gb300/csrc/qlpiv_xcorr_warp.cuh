@@ -120,7 +120,9 @@ __device__ __forceinline__ WarpSmem warp_smem(unsigned char *base, int warp) {
 
 }  // namespace w16
 
-template <typename Pix, bool PP>
+// BATCH: the instantiation for the batched multi-peak replay, launched for multi-peak jobs with
+// batch buffers only; a warp that finds no free batch leaves its IAs to the per-IA retry launch.
+template <typename Pix, bool PP, bool BATCH>
 __global__ void __launch_bounds__(w16::kThreads, w16::kMinBlocks) xcorr16_warp_kernel(IaJob job) {
     using namespace w16;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -143,7 +145,26 @@ __global__ void __launch_bounds__(w16::kThreads, w16::kMinBlocks) xcorr16_warp_k
     const int src_mirror = (32 - lane) & 31;               // holder of Z(., -L)
     auto P = [&](int i, int j) -> float { return sm.plane[i * PS + j]; };
 
-    for (long ia = (long)blockIdx.x * kWarps + warp; ia < job.count; ia += warps_total) {
+    // batched multi-peak replay: a batch claimed for this warp and its fill
+    MpBatch *mpb = nullptr;
+    const long count = job.ia_list != nullptr ? (long)job.ia_list[0] : job.count;
+    if (BATCH) {
+        int slot = -1;
+        if (lane == 0 && multi > 0 && mp_batched(job))
+            slot = mp_claim(job.mp_slots, job.mp_batch_units, (int)((blockIdx.x * kWarps + warp) % 1024u));
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (slot < 0) {
+            // no free batch: every IA of this warp runs in the per-IA launch
+            for (long k = (long)blockIdx.x * kWarps + warp + (long)lane * warps_total; k < count;
+                 k += 32 * warps_total)
+                job.mp_retry[1 + atomicAdd(job.mp_retry, 1)] = (int)k;
+            return;
+        }
+        mpb = job.mp_batch + slot;
+    }
+    int nb = 0;
+    for (long k = (long)blockIdx.x * kWarps + warp; k < count; k += warps_total) {
+        const long ia = job.ia_list != nullptr ? (long)job.ia_list[1 + k] : k;
         const Pix *imgA, *imgB;
         long pitch_a, pitch_b;
         int img_h, img_w;
@@ -372,7 +393,7 @@ __global__ void __launch_bounds__(w16::kThreads, w16::kMinBlocks) xcorr16_warp_k
 
         // ---- peak: FindMaximumFromCenter over rows / columns 1..D-1, or FindMaximumMultiPeaks ----
         float minf = 3.402823466e38f;
-        if (multi == 0) {
+        if (!BATCH && multi == 0) {
             float mv = -3.402823466e38f;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
@@ -430,17 +451,31 @@ __global__ void __launch_bounds__(w16::kThreads, w16::kMinBlocks) xcorr16_warp_k
                     if (i2 <= D - 1) minf = fminf(minf, x[m].y);
                 }
             }
-            multipeak_core<D, 32>(job, ia, minf, P, sm.x, sm.red, sm.fitq, fitv, qn, sm.mp_lv, sm.mp_li,
-                                  sm.mp_lj);
+            if (!BATCH) {
+                multipeak_core<D, 32>(job, ia, minf, P, sm.x, sm.red, sm.fitq, fitv, qn, sm.mp_lv, sm.mp_li,
+                                      sm.mp_lj);
+            } else {
+                multipeak_stage<D, 32>(job, ia, minf, P, sm.x, sm.red, mpb, nb);
+                if (++nb == kMpBatch) {
+                    mp_batch_run<D, PP>(mpb, nb, lane, job, sm.fitq, fitv);
+                    nb = 0;
+                }
+            }
         }
-        qn += KQ;
-        if (qn + KQ > 32) {
-            fit_flush<D, PP>(sm.fitq, fitv, qn, lane, job);
-            qn = 0;
+        if (!BATCH) {
+            qn += KQ;
+            if (qn + KQ > 32) {
+                fit_flush<D, PP>(sm.fitq, fitv, qn, lane, job);
+                qn = 0;
+            }
         }
         __syncwarp();  // the exchange buffer and the plane are rewritten by the next IA
     }
-    if (qn > 0) fit_flush<D, PP>(sm.fitq, fitv, qn, lane, job);
+    if (!BATCH && qn > 0) fit_flush<D, PP>(sm.fitq, fitv, qn, lane, job);
+    if (BATCH) {
+        if (nb > 0) mp_batch_run<D, PP>(mpb, nb, lane, job, sm.fitq, fitv);
+        if (lane == 0) mp_release(job.mp_slots, (int)(mpb - job.mp_batch));
+    }
 }
 
 }  // namespace qlpiv

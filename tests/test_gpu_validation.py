@@ -66,6 +66,24 @@ def _tiles(qp, n, count, bits=8, seed=0, sparse=False):
                                                 (128, 3, 2, 3, True)])
 def test_multipeaks_match_oracle_on_kernel_planes(qp, handle, oracle, n, kw, k, norm, sparse):
     ta, tb = _tiles(qp, n, 160, seed=n + kw + k, sparse=sparse)
+    _check_multipeaks(qp, handle, oracle, ta, tb, n, kw, k, norm)
+
+
+@pytest.mark.parametrize("n,k", [(16, 3), (32, 3), (64, 3), (16, 1), (32, 4), (64, 2)])
+def test_batched_replay_reruns_are_exact(qp, handle, oracle, n, k):
+    """Up to 4 peaks with the 3-point fit, the lists are replayed 32 IAs at a time from the
+    records each IA stored; an IA whose list needs records that were not stored runs again per
+    IA.  All-zero planes (no normalisation, empty tiles) always do: their threshold is 0.  Mixed
+    with ordinary tiles in one launch, every IA must still match the oracle's search."""
+    ta, tb = _tiles(qp, n, 200, seed=7 * n + k)
+    zero = np.zeros(len(ta), bool)
+    zero[1::3] = True
+    ta = np.where(zero[:, None, None], 0, ta).astype(ta.dtype)
+    tb = np.where(zero[:, None, None], 0, tb).astype(tb.dtype)
+    _check_multipeaks(qp, handle, oracle, ta, tb, n, 3, k, qp.NORM_NONE)
+
+
+def _check_multipeaks(qp, handle, oracle, ta, tb, n, kw, k, norm):
     planes = handle.xcorr_planes(ta, tb, norm_mode=norm)
     vec = handle.xcorr_multipeaks(ta, tb, norm_mode=norm, num_peaks=k, peak_kernel=kw)
     assert vec.shape == (len(ta), k)
