@@ -1,0 +1,61 @@
+// K1 launch helpers shared by the per-size translation units (qlpiv_xcorr{16,32,64,128}.cu),
+// which compile in parallel; qlpiv_xcorr.cu holds the device tables and the dispatch.
+#pragma once
+#include <mutex>
+
+#include "qlpiv_internal.h"
+#include "qlpiv_xcorr.cuh"
+
+namespace qlpiv {
+
+inline int twiddle_offset(int m) { return m == 32 ? 0 : (m == 64 ? 32 : (m == 128 ? 96 : 224)); }
+
+// Default waves of resident CTAs per launch in multi-peak mode.  Measured on the headline adaptive
+// workload (three multi-peak passes): 1 wave 558 frame-pairs/s, 4: 568, 16: 582, 32: 585, 64: 586.
+constexpr int kMultiWaves = 32;
+
+constexpr size_t kSubpixSmem = sizeof(float) * 32 * 2 * kMaxSubpixPixels;
+
+// The batched multi-peak replay (mp_batched) applies to the job and its buffers were given.
+inline bool batch_eligible(const IaJob &job) {
+    return job.mp_batch != nullptr && job.mp_slots != nullptr && job.mp_retry != nullptr && job.mp_batch_units > 0 &&
+           job.ia_list == nullptr && job.num_peaks >= 1 && job.num_peaks <= 4 &&
+           (job.subpix == QLPIV_SUBPIX_NONE || job.subpix == QLPIV_SUBPIX_GAUSS3);
+}
+
+// Batched launch: the retry count is zeroed before the main launch; the IAs it flags run again
+// through the per-IA path in a second launch of `retry_grid` units over the device list.
+template <typename Launch>
+inline cudaError_t launch_batched(const IaJob &j, long grid, long retry_grid, cudaStream_t stream, Launch launch,
+                                  int *nlaunch) {
+    cudaError_t e = cudaMemsetAsync(j.mp_retry, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return e;
+    if ((e = launch(j, grid)) != cudaSuccess) return e;
+    IaJob r = j;
+    r.mp_batch = nullptr;
+    r.ia_list = j.mp_retry;
+    if ((e = launch(r, retry_grid)) != cudaSuccess) return e;
+    if (nlaunch) *nlaunch = 2;
+    return cudaSuccess;
+}
+
+
+// Per-size launchers (pixel type and the P-point instantiation chosen inside).
+cudaError_t launch_k1_16(const IaJob &job, int pixel_type, cudaStream_t stream, int num_sms, int *nlaunch);
+cudaError_t launch_k1_32(const IaJob &job, int pixel_type, cudaStream_t stream, int num_sms, int *nlaunch);
+cudaError_t launch_k1_64(const IaJob &job, int pixel_type, cudaStream_t stream, int num_sms, int *nlaunch);
+cudaError_t launch_k1_128(const IaJob &job, int pixel_type, cudaStream_t stream, int num_sms, int *nlaunch);
+
+// Calls L<Pix, PP>::run(job, args...) for the job's pixel type and sub-pixel stencil mode.
+template <template <typename, bool> class L, typename... A>
+cudaError_t dispatch_pix(const IaJob &job, int pixel_type, A... args) {
+    const bool pp = job.subpix_pixels > 0;
+    switch (pixel_type) {
+        case QLPIV_PIX_U8: return pp ? L<uint8_t, true>::run(job, args...) : L<uint8_t, false>::run(job, args...);
+        case QLPIV_PIX_U16: return pp ? L<uint16_t, true>::run(job, args...) : L<uint16_t, false>::run(job, args...);
+        case QLPIV_PIX_F32: return pp ? L<float, true>::run(job, args...) : L<float, false>::run(job, args...);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace qlpiv
