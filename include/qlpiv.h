@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define QLPIV_ABI_VERSION 4
+#define QLPIV_ABI_VERSION 5
 
 /* Status codes.  The Java shim maps QLPIV_E_SHAPE/QLPIV_E_ARG to JobAnalyzeException
  * (S/jobs/xcorr/CrossCorrelationFFTTemplate.java:594-642 shape checks) and the others
@@ -192,7 +192,14 @@ typedef struct qlpiv_adaptive_desc {
     int subpix_iterations; /* as qlpiv_pass_desc */
     int inherit_mode;      /* qlpiv_inherit_mode (getVelocityInheritanceStrategy) */
     int clipping_mode;     /* qlpiv_clipping (PIVInputParameters.getClippingMode) */
-    int reserved[1];
+    int superposition_start; /* interrogation-area division: levels before this one split without
+                              superposition (AdaptiveInterAreaStrategyNoSuperPosition), the rest
+                              with it, SuperPosition restarting at this level as at its first
+                              step (AdaptiveInterAreaStrategyMixedSuperPosition,
+                              S/iareas/AdaptiveInterAreaStrategyMixedSuperPosition.java:31-92,
+                              getSuperPositionIterationStepStart).  0: SuperPosition throughout
+                              (AdaptiveInterAreaStrategySuperPosition); >= the level count:
+                              NoSuperPosition throughout.  qlpiv_grid_level gives every level. */
 } qlpiv_adaptive_desc;
 
 /* ClippingModeEnum (S/ClippingModeEnum.java:9-13).  Under QLPIV_CLIP_NO_OUT_OF_BOUND every
@@ -328,6 +335,13 @@ qlpiv_status qlpiv_grid_superposition(int height, int width, const int margins[4
                                       int cap);
 qlpiv_status qlpiv_grid_nosuperposition(int height, int width, const int margins[4], int ia_start, int level,
                                         qlpiv_grid *grid, int32_t *tops, int32_t *lefts, int cap);
+/* The grid of adaptive level `level` under the mixed division (AdaptiveInterAreaStrategy-
+ * MixedSuperPosition, S/iareas/AdaptiveInterAreaStrategyMixedSuperPosition.java:31-92): levels
+ * before superposition_start as qlpiv_grid_nosuperposition, the rest as qlpiv_grid_superposition
+ * of IA ia_start >> superposition_start at level - superposition_start.  Host only. */
+qlpiv_status qlpiv_grid_level(int height, int width, const int margins[4], int ia_start, int level,
+                              float overlap_factor, int superposition_start, qlpiv_grid *grid, int32_t *tops,
+                              int32_t *lefts, int cap);
 
 /* Number of adaptive levels and the grid of each (`grids` may be NULL).  Host only. */
 qlpiv_status qlpiv_adaptive_levels(const qlpiv_adaptive_desc *desc, int height, int width, int *levels,

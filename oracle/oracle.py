@@ -111,7 +111,7 @@ def lib():
         L.orc_validate.argtypes = [c_int, c_int, ip, ip, fp, fp, fp, fp, ip, c_int, ctypes.POINTER(ValidCfg), vp]
         L.orc_piv_adaptive_ex.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_int,
                                           c_int, c_float, c_int, c_int, c_int, ctypes.POINTER(ValidCfg), fp, fp, ip,
-                                          ip, vp, vp, vp]
+                                          ip, vp, vp, vp, c_int]
         L.orc_inherit_tiles.argtypes = [c_int, c_int, c_int, c_int, ip, ip, fp, fp, c_int, c_int, c_int, ip, ip, c_int,
                                         fp, fp]
         L.orc_area_overlap.argtypes = [c_int, c_int, c_int, c_int, c_int, c_int, ip]
@@ -254,6 +254,15 @@ def clip_tile(img, top, left, n):
 class _Grid(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int) for k in
                 ("n", "tiles_i", "tiles_j", "margin_top", "margin_left", "margin_bottom", "margin_right")]
+
+
+def level_grid(h, w, n_start, level, overlap_factor=0.5, margins=(0, 0, 0, 0), superposition_start=0):
+    """Grid of one level under the mixed division: NoSuperPosition before superposition_start,
+    then SuperPosition restarted with IA n_start >> superposition_start
+    (AdaptiveInterAreaStrategyMixedSuperPosition.java:31-92)."""
+    if level < superposition_start:
+        return grid(h, w, n_start, level, overlap_factor, margins, superposition=False)
+    return grid(h, w, n_start >> superposition_start, level - superposition_start, overlap_factor, margins)
 
 
 def grid(h, w, n_start, level=0, overlap_factor=0.5, margins=(0, 0, 0, 0), superposition=True):
@@ -403,10 +412,11 @@ CLIP_ALLOWED, CLIP_LOGGED, CLIP_NO_OUT_OF_BOUND = 0, 1, 2
 
 def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MAX_A, fixed_max=None,
                  int16_quirk=False, precision=32, nthreads=None, return_levels=False, warp=True, validation=None,
-                 inherit=INHERIT_BICUBIC_SPLINE, clip_mode=CLIP_ALLOWED):
+                 inherit=INHERIT_BICUBIC_SPLINE, clip_mode=CLIP_ALLOWED, superposition_start=0):
     """Adaptive multi-pass PIV (warp: False none, True BothImages bilinear, or a micro / mini mode
     4..9 as WARP_*); returns (u, v) of
     the last level, shaped (tiles_i, tiles_j), and optionally all levels' vectors.
+    superposition_start: the mixed division's first SuperPosition level (level_grid).
     validation: a ValidCfg (multi-peak finder + normalised-median validation per level);
     with return_levels the result also carries every level's validated (u, v) and
     invalid flags."""
@@ -419,7 +429,7 @@ def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MA
     total = 0
     lv, n = 0, n_start
     while n >= n_end:
-        g, _, _ = grid(h, w, n_start, lv, overlap_factor)
+        g, _, _ = level_grid(h, w, n_start, lv, overlap_factor, superposition_start=superposition_start)
         total += g["tiles_i"] * g["tiles_j"]
         n >>= 1
         lv += 1
@@ -435,7 +445,7 @@ def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MA
                                    _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), ctypes.byref(ni),
                                    ctypes.byref(nj), vec.ctypes.data if vec is not None else None,
                                    luv.ctypes.data if luv is not None else None,
-                                   linv.ctypes.data if linv is not None else None)
+                                   linv.ctypes.data if linv is not None else None, int(superposition_start))
     if rc != 0:
         raise ValueError("adaptive PIV failed")
     shape = (ni.value, nj.value)

@@ -71,6 +71,8 @@ float orc_clip_tile(const void *img, int h, int w, int pix_bytes, int top, int l
 
 int orc_grid_superposition(int h, int w, int mtop, int mbottom, int mleft, int mright, int n_start, int level,
                            float overlap_factor, orc_grid *g, int *tops, int *lefts, int cap);
+int orc_grid_nosuperposition(int h, int w, int mtop, int mbottom, int mleft, int mright, int n_start, int level,
+                             orc_grid *g, int *tops, int *lefts, int cap);
 int orc_piv_pass(const void *img_a, const void *img_b, int h, int w, int pix_bytes, int n, long count,
                  const int *a_top, const int *a_left, const int *b_top, const int *b_left, int norm_mode,
                  float fixed_max_a, float fixed_max_b, int subpix, int precision, orc_vector *out, int nthreads);

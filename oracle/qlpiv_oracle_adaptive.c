@@ -473,7 +473,8 @@ void orc_inherit(const double *py, int pni, const double *px, int pnj, const flo
     free(du); free(dv); free(fpy); free(fpx);
 }
 
-/* Adaptive multi-pass PIV with BothImages bilinear warping (SuperPosition grids, SimpleStrategy).
+/* Adaptive multi-pass PIV with BothImages bilinear warping (SimpleStrategy); SuperPosition grids
+ * from level sp_start on, NoSuperPosition grids before (0: SuperPosition throughout).
  * Level L uses IA n_start >> L.  warp_mode 1 = BothImages bilinear warping, 0 = no
  * warping (B tiles displaced by the rounded inherited displacement).  Tile maxima are
  * fixed_max when > 0 (full-image-warp tiles: 255 / 65535), else the tile max.
@@ -483,7 +484,7 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
                         float overlap_factor, int warp_mode, int inherit_mode, int clip_mode, int norm_mode,
                         float fixed_max, int int16_quirk, int precision, int nthreads, const orc_valid_cfg *val,
                         float *out_u, float *out_v, int *out_ni, int *out_nj, orc_vector *level_vectors,
-                        float *level_uv, unsigned char *level_invalid) {
+                        float *level_uv, unsigned char *level_invalid, int sp_start) {
     const int validate = val != NULL && val->enabled;
     /* the multi-peak model searches num_peaks peaks (FindMaximumMultiPeaks); the other models keep
      * FindMaximumFromCenter and one validation strategy */
@@ -506,8 +507,14 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
     long vec_off = 0;
     int rc = 0;
     for (int lv = 0; lv < levels; lv++) {
+        /* the mixed division (AdaptiveInterAreaStrategyMixedSuperPosition.java:31-92): NoSuperPosition
+         * before sp_start, then SuperPosition restarted with IA n_start >> sp_start */
         orc_grid g;
-        if (orc_grid_superposition(h, w, 0, 0, 0, 0, n_start, lv, overlap_factor, &g, tops, lefts, cap) != 0) {
+        const int grc = lv < sp_start
+                            ? orc_grid_nosuperposition(h, w, 0, 0, 0, 0, n_start, lv, &g, tops, lefts, cap)
+                            : orc_grid_superposition(h, w, 0, 0, 0, 0, n_start >> sp_start, lv - sp_start,
+                                                     overlap_factor, &g, tops, lefts, cap);
+        if (grc != 0) {
             rc = -1;
             break;
         }
@@ -658,5 +665,5 @@ int orc_piv_adaptive(const void *img_a, const void *img_b, int h, int w, int pix
                      int nthreads, float *out_u, float *out_v, int *out_ni, int *out_nj, orc_vector *level_vectors) {
     return orc_piv_adaptive_ex(img_a, img_b, h, w, pix_bytes, n_start, n_end, overlap_factor, warp_mode, 0, 0,
                                norm_mode, fixed_max, int16_quirk, precision, nthreads, NULL, out_u, out_v, out_ni,
-                               out_nj, level_vectors, NULL, NULL);
+                               out_nj, level_vectors, NULL, NULL, 0);
 }

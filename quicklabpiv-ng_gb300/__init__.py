@@ -81,7 +81,7 @@ class AdaptiveDesc(ctypes.Structure):
                 ("median_epsilon0", ctypes.c_float), ("max_correction_iterations", ctypes.c_int),
                 ("iterate_until_no_corrections", ctypes.c_int), ("subpix_pixels", ctypes.c_int),
                 ("subpix_iterations", ctypes.c_int), ("inherit_mode", ctypes.c_int), ("clipping_mode", ctypes.c_int),
-                ("reserved", ctypes.c_int * 1)]
+                ("superposition_start", ctypes.c_int)]
 
 
 CLIP_ALLOWED, CLIP_LOGGED, CLIP_NO_OUT_OF_BOUND = 0, 1, 2
@@ -90,9 +90,11 @@ CLIP_ALLOWED, CLIP_LOGGED, CLIP_NO_OUT_OF_BOUND = 0, 1, 2
 def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_mode=WARP_BOTH_BILINEAR,
                   norm_mode=NORM_MAX_A, max_mode=MAX_FIXED, fixed_max=0.0, subpix_mode=SUBPIX_GAUSS3,
                   int16_warp_quirk=False, validation=None, subpix_pixels=3, subpix_iterations=20,
-                  inherit_mode=0, clipping_mode=CLIP_ALLOWED):
+                  inherit_mode=0, clipping_mode=CLIP_ALLOWED, superposition_start=0):
     """Adaptive PIV parameters; the defaults follow the reference's BothImages bilinear
     warping (tiles copied from the warped image keep the full-scale maximum).
+    superposition_start: the level from which the interrogation areas overlap (the mixed
+    division; 0: SuperPosition throughout, >= the level count: NoSuperPosition).
     validation: None, or a dict with keys model (VALIDATE_*; default the multi-peak
     normalised-median model), num_peaks, peak_kernel, threshold, epsilon0, max_iterations,
     iterate_until (see multipeak_validation() and validation_model()).  clipping_mode:
@@ -105,6 +107,7 @@ def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_m
     d.subpix_pixels, d.subpix_iterations = subpix_pixels, subpix_iterations
     d.inherit_mode = inherit_mode
     d.clipping_mode = clipping_mode
+    d.superposition_start = superposition_start
     if validation is not None:
         set_validation(d, **validation)
     return d
@@ -233,6 +236,7 @@ _SIGNATURES = {
     "qlpiv_measure_fp32_peak": (_i, [_i, ctypes.POINTER(ctypes.c_double)]),
     "qlpiv_grid_superposition": (_i, [_i, _i, _vp, _i, _i, _f, ctypes.POINTER(Grid), _vp, _vp, _i]),
     "qlpiv_grid_nosuperposition": (_i, [_i, _i, _vp, _i, _i, ctypes.POINTER(Grid), _vp, _vp, _i]),
+    "qlpiv_grid_level": (_i, [_i, _i, _vp, _i, _i, ctypes.c_float, _i, ctypes.POINTER(Grid), _vp, _vp, _i]),
     "qlpiv_adaptive_levels": (_i, [ctypes.POINTER(AdaptiveDesc), _i, _i, ctypes.POINTER(_i), _vp, _i]),
     "qlpiv_inherit": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _i, _vp, _vp]),
     "qlpiv_inherit_tiles": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),
@@ -288,7 +292,7 @@ def load_library(path=None):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.qlpiv_abi_version() != 4:
+    if lib.qlpiv_abi_version() != 5:
         raise RuntimeError("libqlpiv_gpu.so ABI version mismatch")
     if path is None:
         _lib = lib
@@ -304,15 +308,20 @@ def _check(status):
         raise QlpivError(status, load_library().qlpiv_last_error().decode())
 
 
-def library_grid(height, width, ia_start, level, overlap_factor, margins=(0, 0, 0, 0), superposition=True):
-    """IA grid computed by the library (host code of libqlpiv_gpu.so)."""
+def library_grid(height, width, ia_start, level, overlap_factor, margins=(0, 0, 0, 0), superposition=True,
+                 superposition_start=None):
+    """IA grid computed by the library (host code of libqlpiv_gpu.so); with superposition_start,
+    the mixed division's grid of that level (qlpiv_grid_level)."""
     lib = load_library()
     g = Grid()
     m = (ctypes.c_int * 4)(*margins)
     cap = 1 << 16
     tops = np.zeros(cap, np.int32)
     lefts = np.zeros(cap, np.int32)
-    if superposition:
+    if superposition_start is not None:
+        _check(lib.qlpiv_grid_level(height, width, m, ia_start, level, overlap_factor, superposition_start,
+                                    ctypes.byref(g), _addr(tops), _addr(lefts), cap))
+    elif superposition:
         _check(lib.qlpiv_grid_superposition(height, width, m, ia_start, level, overlap_factor, ctypes.byref(g),
                                             _addr(tops), _addr(lefts), cap))
     else:

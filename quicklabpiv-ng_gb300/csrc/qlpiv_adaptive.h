@@ -90,5 +90,9 @@ int grid_superposition(int h, int w, const int margins[4], int ia_start, int lev
                        int32_t *tops, int32_t *lefts, int cap);
 int grid_nosuperposition(int h, int w, const int margins[4], int ia_start, int level, qlpiv_grid *g, int32_t *tops,
                          int32_t *lefts, int cap);
+// The grid of adaptive level `level` with SuperPosition starting at level sp_start (the mixed
+// division; 0: SuperPosition throughout).
+int grid_level(int h, int w, const int margins[4], int ia_start, int level, float ofac, int sp_start, qlpiv_grid *g,
+               int32_t *tops, int32_t *lefts, int cap);
 
 }  // namespace qlpiv

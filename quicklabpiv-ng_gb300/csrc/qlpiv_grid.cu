@@ -74,4 +74,16 @@ int grid_nosuperposition(int h, int w, const int margins[4], int ia_start, int l
     return 0;
 }
 
+// AdaptiveInterAreaStrategyMixedSuperPosition.createIterationStepTilesParameters
+// (S/iareas/AdaptiveInterAreaStrategyMixedSuperPosition.java:31-92): levels before sp_start use
+// the NoSuperPosition division; at sp_start the SuperPosition division starts as at its first step
+// with IA ia_start >> sp_start (createIterationStepTilesParametersInternal with the step offset,
+// S/iareas/AdaptiveInterAreaStrategySuperPosition.java:31-190) and halves from there.
+// sp_start == 0 is the plain SuperPosition division, sp_start >= the level count NoSuperPosition.
+int grid_level(int h, int w, const int margins[4], int ia_start, int level, float ofac, int sp_start, qlpiv_grid *g,
+               int32_t *tops, int32_t *lefts, int cap) {
+    if (level < sp_start) return grid_nosuperposition(h, w, margins, ia_start, level, g, tops, lefts, cap);
+    return grid_superposition(h, w, margins, ia_start >> sp_start, level - sp_start, ofac, g, tops, lefts, cap);
+}
+
 }  // namespace qlpiv

@@ -119,6 +119,7 @@ static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type,
         return fail(QLPIV_E_ARG, "unknown validation mode %d", d->validation);
     if (d->clipping_mode < QLPIV_CLIP_ALLOWED || d->clipping_mode > QLPIV_CLIP_NO_OUT_OF_BOUND)
         return fail(QLPIV_E_ARG, "unknown clipping mode %d", d->clipping_mode);
+    if (d->superposition_start < 0) return fail(QLPIV_E_ARG, "superposition start level %d < 0", d->superposition_start);
     if (d->validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN) {
         for (int n = d->ia_start; n >= d->ia_end; n >>= 1)
             if (!multipeak_supported(n, d->num_peaks, d->peak_kernel))
@@ -247,8 +248,8 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
     p->levels.resize(nlev);
     for (int lv = 0; lv < nlev; lv++) {
         LevelPlan &L = p->levels[lv];
-        if (grid_superposition(height, width, d->margins, d->ia_start, lv, d->overlap_factor, &L.g, nullptr, nullptr,
-                               0) < -1)
+        if (grid_level(height, width, d->margins, d->ia_start, lv, d->overlap_factor, d->superposition_start, &L.g,
+                       nullptr, nullptr, 0) < -1)
             return fail(QLPIV_E_SHAPE, "image too small for IA %d at level %d", d->ia_start >> lv, lv);
         if ((full_warp(d->warp_mode) || per_tile_warp(d->warp_mode)) && lv > 0 &&
             (L.g.tiles_i < 3 || L.g.tiles_j < 3))
@@ -256,8 +257,8 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
                         L.g.tiles_i, L.g.tiles_j);
         L.tops.resize(L.g.tiles_i);
         L.lefts.resize(L.g.tiles_j);
-        grid_superposition(height, width, d->margins, d->ia_start, lv, d->overlap_factor, &L.g, L.tops.data(),
-                           L.lefts.data(), 1 << 30);
+        grid_level(height, width, d->margins, d->ia_start, lv, d->overlap_factor, d->superposition_start, &L.g,
+                   L.tops.data(), L.lefts.data(), 1 << 30);
         const int n = L.g.n, ni = L.g.tiles_i, nj = L.g.tiles_j;
         L.cyf.resize(ni);
         L.cxf.resize(nj);
@@ -618,14 +619,15 @@ static qlpiv_status upload_host_frames(qlpiv_handle *h, const qlpiv_frame *frame
 // rounded to 256 B) plus the device copies of host frames: the request server's admission estimate.
 size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int height, int width, int pairs) {
     auto al = [](size_t x) { return ((x < 256 ? 256 : x) + 255) & ~(size_t)255; };
-    size_t total = 0;
+    size_t total = 0, most = 0;
     const int nlev = level_count(d);
     int prev_nj = 0;
     for (int lv = 0; lv < nlev; lv++) {
         qlpiv_grid g{};
-        if (grid_superposition(height, width, d->margins, d->ia_start, lv, d->overlap_factor, &g, nullptr, nullptr,
-                               0) < -1)
+        if (grid_level(height, width, d->margins, d->ia_start, lv, d->overlap_factor, d->superposition_start, &g,
+                       nullptr, nullptr, 0) < -1)
             return 0;
+        most = (size_t)g.tiles_i * g.tiles_j * pairs > most ? (size_t)g.tiles_i * g.tiles_j * pairs : most;
         const size_t ni = g.tiles_i, nj = g.tiles_j, cnt = ni * nj, tot = cnt * pairs;
         total += al(8 * KF_ARRAYS * ni) + al(8 * KF_ARRAYS * nj) + al(4 * ni) + al(4 * nj);
         total += 5 * al(4 * tot) + 2 * al(4 * tot) + al(spline_coef_bytes((long)tot));
@@ -651,10 +653,7 @@ size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int heigh
         if (cudaGetDevice(&dev) == cudaSuccess &&
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
             total += al(xcorr_batch_bytes(sms, &units)) + al(xcorr_batch_slot_bytes(units));
-        qlpiv_grid g{};
-        if (grid_superposition(height, width, d->margins, d->ia_start, nlev - 1, d->overlap_factor, &g, nullptr,
-                               nullptr, 0) >= -1)
-            total += al(sizeof(int) * (1 + (size_t)g.tiles_i * g.tiles_j * pairs));
+        total += al(sizeof(int) * (1 + most));
     }
     return total;
 }
@@ -716,6 +715,19 @@ qlpiv_status qlpiv_grid_nosuperposition(int height, int width, const int margins
     return QLPIV_OK;
 }
 
+qlpiv_status qlpiv_grid_level(int height, int width, const int margins[4], int ia_start, int level,
+                              float overlap_factor, int superposition_start, qlpiv_grid *grid, int32_t *tops,
+                              int32_t *lefts, int cap) {
+    if (!grid || !margins) return fail(QLPIV_E_ARG, "NULL argument");
+    if (superposition_start < 0) return fail(QLPIV_E_ARG, "superposition start level %d < 0", superposition_start);
+    const int r = qlpiv::grid_level(height, width, margins, ia_start, level, overlap_factor, superposition_start, grid,
+                                    tops, lefts, cap);
+    if (r == -2) return fail(QLPIV_E_ARG, "Overlap factor must greater than 1/10 and less than 9/10");
+    if (r == -3) return fail(QLPIV_E_SHAPE, "no IA of size %d fits the image", ia_start >> level);
+    if (r == -1) return fail(QLPIV_E_SHAPE, "grid larger than the given capacity %d", cap);
+    return QLPIV_OK;
+}
+
 qlpiv_status qlpiv_adaptive_levels(const qlpiv_adaptive_desc *desc, int height, int width, int *levels,
                                    qlpiv_grid *grids, int max_levels) {
     if (!levels) return fail(QLPIV_E_ARG, "levels is NULL");
@@ -724,8 +736,8 @@ qlpiv_status qlpiv_adaptive_levels(const qlpiv_adaptive_desc *desc, int height, 
     *levels = level_count(desc);
     if (grids) {
         for (int lv = 0; lv < *levels && lv < max_levels; lv++)
-            if (qlpiv::grid_superposition(height, width, desc->margins, desc->ia_start, lv, desc->overlap_factor,
-                                          &grids[lv], nullptr, nullptr, 0) < -1)
+            if (qlpiv::grid_level(height, width, desc->margins, desc->ia_start, lv, desc->overlap_factor,
+                                  desc->superposition_start, &grids[lv], nullptr, nullptr, 0) < -1)
                 return fail(QLPIV_E_SHAPE, "image too small for level %d", lv);
     }
     return QLPIV_OK;

@@ -109,3 +109,16 @@ def adaptive_levels(ia_start, ia_end):
     if 2 ** steps != ratio:
         raise ValueError("step sizes ratio is not a power of two")
     return steps + 1
+
+
+def level(height, width, ia_start, level, overlap_factor, margins=(0, 0, 0, 0), superposition_start=0):
+    """Grid of `level` under AdaptiveInterAreaStrategyMixedSuperPosition
+    (S/iareas/AdaptiveInterAreaStrategyMixedSuperPosition.java:31-92): NoSuperPosition before
+    superposition_start; from there SuperPosition restarted as at its first step with IA
+    ia_start >> superposition_start.  superposition_start 0 is plain SuperPosition."""
+    if level < superposition_start:
+        return nosuperposition(height, width, ia_start, level, margins)
+    g = superposition(height, width, ia_start >> superposition_start, level - superposition_start, overlap_factor,
+                      margins)
+    g.level = level
+    return g

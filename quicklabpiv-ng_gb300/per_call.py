@@ -53,7 +53,8 @@ def piv_adaptive_per_call(handle, img_a, img_b, desc):
     prev = None
     for lv, g in enumerate(levels):
         n = g["n"]
-        st = grid.superposition(h, w, desc.ia_start, lv, desc.overlap_factor, margins)
+        st = grid.level(h, w, desc.ia_start, lv, desc.overlap_factor, margins,
+                        superposition_start=desc.superposition_start)
         assert (st.n, st.tiles_i, st.tiles_j) == (n, g["tiles_i"], g["tiles_j"])
         tops = np.asarray(st.tops, np.int32)
         lefts = np.asarray(st.lefts, np.int32)

@@ -58,7 +58,8 @@ def gpu_trace(qp, handle, img_a, img_b, desc):
     recs = []
     prev = None
     for lv, g in enumerate(levels):
-        st = qp.grid.superposition(h, w, desc.ia_start, lv, desc.overlap_factor, list(desc.margins))
+        st = qp.grid.level(h, w, desc.ia_start, lv, desc.overlap_factor, list(desc.margins),
+                           superposition_start=desc.superposition_start)
         n = st.n
         tops = np.asarray(st.tops, np.int32)
         lefts = np.asarray(st.lefts, np.int32)
@@ -276,7 +277,8 @@ def oracle_levels(oracle, img_a, img_b, recs, desc, sched, cfg=None, fixed_max=N
     n0, n1, ofac = sched
     clip = desc.clipping_mode == 2
     res = oracle.piv_adaptive(img_a, img_b, n0, n1, ofac, fixed_max=fixed_max, precision=64, validation=cfg,
-                              return_levels=True, warp=warp, clip_mode=desc.clipping_mode)
+                              return_levels=True, warp=warp, clip_mode=desc.clipping_mode,
+                              superposition_start=desc.superposition_start)
     vec = res[1]
     luv = res[2] if cfg is not None else None
     h, w = img_a.shape

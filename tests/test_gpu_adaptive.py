@@ -205,3 +205,39 @@ def test_adaptive_from_ia128(qp, handle, oracle, warp):
         rep = adaptive_trace.cascade_report(recs, olv, desc)
         assert all(r["causes"]["unexplained"] == 0 for r in rep), rep
         assert rep[-1]["over_tol"] <= 0.005 * rep[-1]["vectors"], rep
+
+
+@pytest.mark.parametrize("start", [1, 3])
+def test_adaptive_mixed_division(qp, handle, oracle, start):
+    """AdaptiveInterAreaStrategyMixedSuperPosition (S/iareas/AdaptiveInterAreaStrategyMixedSuperPosition.java:31-92):
+    levels before `start` split without superposition, the rest with it, SuperPosition restarted
+    at `start` (3 of 3 levels: NoSuperPosition throughout).  With warping and multi-peak
+    validation: stage by stage against the oracle, end to end against the FP64 pipeline with
+    every vector beyond 1e-3 px traced to an upstream cause, bit for bit against the plain
+    per-call path."""
+    h, w = 256, 320
+    flow = qp.synth.Flow(vmax=5.0, rc=48.0, shear=0.01)
+    pairs = [qp.synth.particle_pair((h, w), flow, ppp=0.02, diam=2.5, diam_sd=0.3, noise=4.0, bits=8, seed=40 + k)
+             for k in range(2)]
+    desc = qp.adaptive_desc(64, 16, 0.5, fixed_max=255.0, superposition_start=start,
+                            validation=qp.multipeak_validation())
+    u, v = handle.piv_adaptive([p[0] for p in pairs], [p[1] for p in pairs], desc)
+    g = qp.grid.level(h, w, 64, 2, 0.5, superposition_start=start)
+    assert u.shape == (2, g.tiles_i, g.tiles_j)
+    # the first level is split without superposition
+    g0, plain0 = qp.grid.level(h, w, 64, 0, 0.5, superposition_start=start), qp.grid.superposition(h, w, 64, 0, 0.5)
+    assert (g0.tiles_i, g0.tiles_j) != (plain0.tiles_i, plain0.tiles_j)
+    cfg = oracle.valid_cfg(num_peaks=3, kernel_width=3, threshold=2.0, epsilon0=0.1, max_iterations=2)
+    for q, (a, b) in enumerate(pairs):
+        recs = adaptive_trace.gpu_trace(qp, handle, a, b, desc)
+        assert recs[-1]["u"].tobytes() == u[q].tobytes() and recs[-1]["v"].tobytes() == v[q].tobytes()
+        adaptive_trace.check_stages(qp, oracle, recs, desc, cfg)
+        olv = adaptive_trace.oracle_levels(oracle, a, b, recs, desc, (64, 16, 0.5), cfg=cfg, fixed_max=255.0)
+        rep = adaptive_trace.cascade_report(recs, olv, desc)
+        assert all(r["causes"]["unexplained"] == 0 for r in rep), rep
+    pu, pv = qp.per_call.piv_adaptive_per_call(handle, pairs[0][0], pairs[0][1], desc)
+    assert pu.tobytes() == u[0].tobytes() and pv.tobytes() == v[0].tobytes()
+    gy, gx = g.centres()
+    yy, xx = np.meshgrid(gy, gx, indexing="ij")
+    tr, tc = flow.displacement(yy, xx, (h, w))
+    assert np.median(np.hypot(u[0] - tr, v[0] - tc)) < 0.3

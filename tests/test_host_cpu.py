@@ -29,7 +29,7 @@ def test_library_exports_header_symbols(qp):
     for s in syms:
         assert hasattr(lib, s), s
     assert sorted(qp.exported_symbols()) == syms
-    assert qp.load_library().qlpiv_abi_version() == 4
+    assert qp.load_library().qlpiv_abi_version() == 5
 
 
 def test_ctypes_structs_match_header(qp, tmp_path):
@@ -174,6 +174,36 @@ def test_library_grid_matches_oracle(qp, oracle, h, w, n, levels, ofac, margins)
         g2, t2, l2 = qp.library_grid(h, w, n, lv, ofac, margins, superposition=False)
         o2, ot2, ol2 = oracle.grid(h, w, n, lv, margins=margins, superposition=False)
         assert g2 == o2 and (t2 == ot2).all() and (l2 == ol2).all()
+
+
+@pytest.mark.parametrize("h,w,n,levels,ofac,margins", [
+    (1024, 1024, 64, 3, 0.25, (0, 0, 0, 0)),
+    (600, 800, 128, 4, 0.5, (3, 5, 7, 11)),
+    (777, 333, 32, 2, 0.3, (1, 2, 3, 4)),
+])
+def test_mixed_division_grids(qp, oracle, h, w, n, levels, ofac, margins):
+    """AdaptiveInterAreaStrategyMixedSuperPosition: NoSuperPosition levels before the start
+    level, then SuperPosition restarted with IA n >> start.  Library, Python restatement and
+    oracle agree level by level; start 0 is SuperPosition and start >= levels NoSuperPosition."""
+    for start in range(levels + 1):
+        for lv in range(levels):
+            g, tops, lefts = qp.library_grid(h, w, n, lv, ofac, margins, superposition_start=start)
+            o, ot, ol = oracle.level_grid(h, w, n, lv, ofac, margins, superposition_start=start)
+            st = qp.grid.level(h, w, n, lv, ofac, margins, superposition_start=start)
+            assert g == o and (tops == ot).all() and (lefts == ol).all()
+            assert (np.asarray(st.tops) == tops).all() and (np.asarray(st.lefts) == lefts).all()
+            assert g["n"] == n >> lv
+            ref = qp.library_grid(h, w, n, lv, ofac, margins, superposition=lv >= start)
+            if start in (0, levels):
+                assert g == ref[0] and (tops == ref[1]).all()
+        d = qp.adaptive_desc(n, n >> (levels - 1), ofac, margins=margins, superposition_start=start)
+        got = qp.adaptive_levels(d, h, w)
+        assert [x["tiles_i"] * x["tiles_j"] for x in got] == [
+            qp.library_grid(h, w, n, lv, ofac, margins, superposition_start=start)[0]["tiles_i"] *
+            qp.library_grid(h, w, n, lv, ofac, margins, superposition_start=start)[0]["tiles_j"]
+            for lv in range(levels)]
+    with pytest.raises(qp.QlpivError):
+        qp.library_grid(h, w, n, 0, ofac, margins, superposition_start=-1)
 
 
 def test_adaptive_levels_config2(qp):
