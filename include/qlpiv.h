@@ -200,7 +200,27 @@ typedef struct qlpiv_adaptive_desc {
                               getSuperPositionIterationStepStart).  0: SuperPosition throughout
                               (AdaptiveInterAreaStrategySuperPosition); >= the level count:
                               NoSuperPosition throughout.  qlpiv_grid_level gives every level. */
+    int stable_mode;       /* qlpiv_stable: when a level's correlation is repeated */
+    float stable_max_displacement;  /* QLPIV_STABLE_MAX_DISPLACEMENT: getMaxDisplacement (px) */
+    int stable_max_retries;         /* QLPIV_STABLE_MAX_DISPLACEMENT: getMaxRetries (>= 1) */
+    int reserved[5];
 } qlpiv_adaptive_desc;
+
+/* Tile stabilisation per level (InterAreaStableStrategiesFactoryEnum,
+ * S/iareas/InterAreaStableStrategiesFactoryEnum.java:9-27; the loop of
+ * S/jobs/LocalPIVOpenCLGpuJob.java:233-405).  Pass r = 1, 2, ... of a level re-warps the frames
+ * with every tile's current displacement (no warping at the first level), correlates the tiles
+ * still EVALUATING and accumulates their increments; a tile's state then follows
+ * InterAreaDisplacementStableStrategy.computeStableState (S/iareas/InterAreaDisplacementStableStrategy.java:19-36):
+ * |increment| = (float) sqrt(du^2 + dv^2) in double above the maximum keeps it EVALUATING while
+ * r < max_retries (UNSTABLE at r = max_retries), else it is STABLE.  At the first level the
+ * BothImages strategy does not warp, so a repeated pass correlates the same tiles again and adds
+ * the same increment, as the reference does.  Not combined with vector validation (the
+ * reference's validator then visits only the re-correlated tiles): QLPIV_E_ARG. */
+typedef enum {
+    QLPIV_STABLE_SIMPLE = 0,            /* InterAreaSimpleStableStrategy: one correlation per level */
+    QLPIV_STABLE_MAX_DISPLACEMENT = 1   /* InterAreaDisplacementStableStrategy */
+} qlpiv_stable;
 
 /* ClippingModeEnum (S/ClippingModeEnum.java:9-13).  Under QLPIV_CLIP_NO_OUT_OF_BOUND every
  * displacement update of a tile -- inheritance, the correlation increment, a validation

@@ -111,7 +111,7 @@ def lib():
         L.orc_validate.argtypes = [c_int, c_int, ip, ip, fp, fp, fp, fp, ip, c_int, ctypes.POINTER(ValidCfg), vp]
         L.orc_piv_adaptive_ex.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_int,
                                           c_int, c_float, c_int, c_int, c_int, ctypes.POINTER(ValidCfg), fp, fp, ip,
-                                          ip, vp, vp, vp, c_int]
+                                          ip, vp, vp, vp, c_int, c_int, c_float]
         L.orc_inherit_tiles.argtypes = [c_int, c_int, c_int, c_int, ip, ip, fp, fp, c_int, c_int, c_int, ip, ip, c_int,
                                         fp, fp]
         L.orc_area_overlap.argtypes = [c_int, c_int, c_int, c_int, c_int, c_int, ip]
@@ -412,11 +412,14 @@ CLIP_ALLOWED, CLIP_LOGGED, CLIP_NO_OUT_OF_BOUND = 0, 1, 2
 
 def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MAX_A, fixed_max=None,
                  int16_quirk=False, precision=32, nthreads=None, return_levels=False, warp=True, validation=None,
-                 inherit=INHERIT_BICUBIC_SPLINE, clip_mode=CLIP_ALLOWED, superposition_start=0):
+                 inherit=INHERIT_BICUBIC_SPLINE, clip_mode=CLIP_ALLOWED, superposition_start=0, stable_max=None,
+                 stable_retries=1):
     """Adaptive multi-pass PIV (warp: False none, True BothImages bilinear, or a micro / mini mode
     4..9 as WARP_*); returns (u, v) of
     the last level, shaped (tiles_i, tiles_j), and optionally all levels' vectors.
     superposition_start: the mixed division's first SuperPosition level (level_grid).
+    stable_max / stable_retries: InterAreaDisplacementStableStrategy (passes repeated per level
+    while a tile's increment exceeds stable_max, at most stable_retries passes; no validation).
     validation: a ValidCfg (multi-peak finder + normalised-median validation per level);
     with return_levels the result also carries every level's validated (u, v) and
     invalid flags."""
@@ -445,7 +448,9 @@ def piv_adaptive(img_a, img_b, n_start, n_end, overlap_factor, norm_mode=NORM_MA
                                    _ptr(u, ctypes.c_float), _ptr(v, ctypes.c_float), ctypes.byref(ni),
                                    ctypes.byref(nj), vec.ctypes.data if vec is not None else None,
                                    luv.ctypes.data if luv is not None else None,
-                                   linv.ctypes.data if linv is not None else None, int(superposition_start))
+                                   linv.ctypes.data if linv is not None else None, int(superposition_start),
+                                   int(stable_retries) if stable_max is not None else 1,
+                                   float(stable_max or 0.0))
     if rc != 0:
         raise ValueError("adaptive PIV failed")
     shape = (ni.value, nj.value)

@@ -484,7 +484,8 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
                         float overlap_factor, int warp_mode, int inherit_mode, int clip_mode, int norm_mode,
                         float fixed_max, int int16_quirk, int precision, int nthreads, const orc_valid_cfg *val,
                         float *out_u, float *out_v, int *out_ni, int *out_nj, orc_vector *level_vectors,
-                        float *level_uv, unsigned char *level_invalid, int sp_start) {
+                        float *level_uv, unsigned char *level_invalid, int sp_start, int stab_retries,
+                        float stab_max) {
     const int validate = val != NULL && val->enabled;
     /* the multi-peak model searches num_peaks peaks (FindMaximumMultiPeaks); the other models keep
      * FindMaximumFromCenter and one validation strategy */
@@ -615,6 +616,54 @@ int orc_piv_adaptive_ex(const void *img_a, const void *img_b, int h, int w, int 
             /* Tile.accumulateDisplacement drops an increment that moves the tile out of the image */
             if (!clip || orc_clip_ok(n, h, w, tops[k / nj], lefts[k % nj], nu, nv)) { cu[k] = nu; cv[k] = nv; }
         }
+        if (stab_retries > 1) {
+            /* InterAreaDisplacementStableStrategy (S/iareas/InterAreaDisplacementStableStrategy.java:19-36)
+             * in the loop of S/jobs/LocalPIVOpenCLGpuJob.java:233-405: pass r re-warps with every
+             * tile's current displacement (not at the first level), correlates the EVALUATING tiles and
+             * accumulates; a tile stays EVALUATING while |increment| > stab_max and r < stab_retries */
+            unsigned char *ev = (unsigned char *)malloc((size_t)cnt);
+            int *idx = (int *)malloc(sizeof(int) * cnt);
+            orc_vector *v2 = (orc_vector *)malloc(sizeof(orc_vector) * cnt);
+            long nev = 0;
+            for (long k = 0; k < cnt; k++) {
+                const double du = precision == 0 ? vec[k].u : (float)vec[k].u64;
+                const double dv = precision == 0 ? vec[k].v : (float)vec[k].v64;
+                ev[k] = (float)sqrt(du * du + dv * dv) > stab_max && 1 < stab_retries;
+                nev += ev[k];
+            }
+            for (int r = 2; r <= stab_retries && nev > 0; r++) {
+                if (lv > 0 && warp_mode >= 1 && warp_mode <= 3) {
+                    orc_displacement_field(cyd, ni, cxd, nj, cu, cv, h, w, precision, fu, fv);
+                    orc_warp_full(img_a, img_b, h, w, pix_bytes, fu, fv, int16_quirk,
+                                  warp_mode == 1 ? 3 : (warp_mode == 2 ? 1 : 2), wa, wb);
+                }
+                long m = 0;
+                for (long k = 0; k < cnt; k++) {
+                    if (!ev[k]) continue;
+                    const int i = (int)(k / nj), j = (int)(k % nj);
+                    idx[m] = (int)k;
+                    at[m] = tops[i];
+                    al[m] = lefts[j];
+                    bt[m] = warp_mode == 0 ? java_round((float)tops[i] + cu[k]) : tops[i];
+                    bl[m] = warp_mode == 0 ? java_round((float)lefts[j] + cv[k]) : lefts[j];
+                    m++;
+                }
+                orc_piv_pass(sa, sb, h, w, pix_bytes, n, m, at, al, bt, bl, nm, fma, fmb, 1, precision, v2, nthreads);
+                nev = 0;
+                for (long q = 0; q < m; q++) {
+                    const long k = idx[q];
+                    float nu, nv;
+                    if (precision == 0) { nu = cu[k] + v2[q].u; nv = cv[k] + v2[q].v; }
+                    else { nu = (float)((double)cu[k] + v2[q].u64); nv = (float)((double)cv[k] + v2[q].v64); }
+                    if (!clip || orc_clip_ok(n, h, w, tops[k / nj], lefts[k % nj], nu, nv)) { cu[k] = nu; cv[k] = nv; }
+                    const double du = precision == 0 ? v2[q].u : (float)v2[q].u64;
+                    const double dv = precision == 0 ? v2[q].v : (float)v2[q].v64;
+                    ev[k] = (float)sqrt(du * du + dv * dv) > stab_max && r < stab_retries;
+                    nev += ev[k];
+                }
+            }
+            free(ev); free(idx); free(v2);
+        }
         if (validate) {
             /* VectorValidatorJob after IterationStepTiles.updateDisplacementsFromMaxCrossResults
              * (S/jobs/LocalPIVOpenCLGpuJob.java:384-402) */
@@ -665,5 +714,5 @@ int orc_piv_adaptive(const void *img_a, const void *img_b, int h, int w, int pix
                      int nthreads, float *out_u, float *out_v, int *out_ni, int *out_nj, orc_vector *level_vectors) {
     return orc_piv_adaptive_ex(img_a, img_b, h, w, pix_bytes, n_start, n_end, overlap_factor, warp_mode, 0, 0,
                                norm_mode, fixed_max, int16_quirk, precision, nthreads, NULL, out_u, out_v, out_ni,
-                               out_nj, level_vectors, NULL, NULL, 0);
+                               out_nj, level_vectors, NULL, NULL, 0, 1, 0.0f);
 }

@@ -81,7 +81,12 @@ class AdaptiveDesc(ctypes.Structure):
                 ("median_epsilon0", ctypes.c_float), ("max_correction_iterations", ctypes.c_int),
                 ("iterate_until_no_corrections", ctypes.c_int), ("subpix_pixels", ctypes.c_int),
                 ("subpix_iterations", ctypes.c_int), ("inherit_mode", ctypes.c_int), ("clipping_mode", ctypes.c_int),
-                ("superposition_start", ctypes.c_int)]
+                ("superposition_start", ctypes.c_int), ("stable_mode", ctypes.c_int),
+                ("stable_max_displacement", ctypes.c_float), ("stable_max_retries", ctypes.c_int),
+                ("reserved", ctypes.c_int * 5)]
+
+
+STABLE_SIMPLE, STABLE_MAX_DISPLACEMENT = 0, 1
 
 
 CLIP_ALLOWED, CLIP_LOGGED, CLIP_NO_OUT_OF_BOUND = 0, 1, 2
@@ -90,11 +95,15 @@ CLIP_ALLOWED, CLIP_LOGGED, CLIP_NO_OUT_OF_BOUND = 0, 1, 2
 def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_mode=WARP_BOTH_BILINEAR,
                   norm_mode=NORM_MAX_A, max_mode=MAX_FIXED, fixed_max=0.0, subpix_mode=SUBPIX_GAUSS3,
                   int16_warp_quirk=False, validation=None, subpix_pixels=3, subpix_iterations=20,
-                  inherit_mode=0, clipping_mode=CLIP_ALLOWED, superposition_start=0):
+                  inherit_mode=0, clipping_mode=CLIP_ALLOWED, superposition_start=0, stable_max_displacement=None,
+                  stable_max_retries=0):
     """Adaptive PIV parameters; the defaults follow the reference's BothImages bilinear
     warping (tiles copied from the warped image keep the full-scale maximum).
     superposition_start: the level from which the interrogation areas overlap (the mixed
     division; 0: SuperPosition throughout, >= the level count: NoSuperPosition).
+    stable_max_displacement / stable_max_retries: InterAreaDisplacementStableStrategy (a level's
+    tiles are correlated again while their increment exceeds the maximum, at most
+    stable_max_retries passes); None: one correlation per level.
     validation: None, or a dict with keys model (VALIDATE_*; default the multi-peak
     normalised-median model), num_peaks, peak_kernel, threshold, epsilon0, max_iterations,
     iterate_until (see multipeak_validation() and validation_model()).  clipping_mode:
@@ -108,6 +117,10 @@ def adaptive_desc(ia_start, ia_end, overlap_factor, margins=(0, 0, 0, 0), warp_m
     d.inherit_mode = inherit_mode
     d.clipping_mode = clipping_mode
     d.superposition_start = superposition_start
+    if stable_max_displacement is not None:
+        d.stable_mode = STABLE_MAX_DISPLACEMENT
+        d.stable_max_displacement = stable_max_displacement
+        d.stable_max_retries = stable_max_retries
     if validation is not None:
         set_validation(d, **validation)
     return d

@@ -369,7 +369,9 @@ __host__ __device__ __forceinline__ float spline_cross(FF f, int ni, int nj, int
 // the scratch of a row strip is laid out knot-major (knot, lane) so its accesses stay
 // coalesced.  The two kinds write disjoint floats of the node quadruples.
 __global__ void __launch_bounds__(128) spline_nodes_kernel(int pairs, const float2 *kfy, int ni, const float2 *kfx,
-                                                           int nj, const float *u, const float *v, SplineCoef coef) {
+                                                           int nj, const float *u, const float *v, SplineCoef coef,
+                                                           const int *gate) {
+    if (gate != nullptr && *gate == 0) return;
     const int sj = (nj + 31) / 32, si = (ni + 31) / 32, per = 2 * (sj + si);
     const long wid = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (wid >= (long)pairs * per) return;
@@ -562,7 +564,8 @@ template <typename Pix>
 __global__ void __launch_bounds__(256) warp_both_kernel(const qlpiv_frame *src, const qlpiv_frame *dst,
                                                         const float *ys, int ni, const float *xs, int nj,
                                                         const float4 *c4u, const float4 *c4v, int int16_quirk,
-                                                        int image_mode) {
+                                                        int image_mode, const int *gate) {
+    if (gate != nullptr && *gate == 0) return;
     constexpr int kPer = kWarpRows / 8;
     __shared__ float sx[32][4];
     __shared__ float4 sy[kWarpRows];
@@ -893,23 +896,23 @@ cudaError_t launch_inherit_tiles(cudaStream_t s, int pairs, int mode, int pn, in
 }
 
 cudaError_t launch_spline(cudaStream_t s, int pairs, const float2 *kfy, int ni, const float2 *kfx, int nj,
-                          const float *u, const float *v, SplineCoef coef) {
+                          const float *u, const float *v, SplineCoef coef, const int *gate) {
     const long warps = (long)pairs * 2 * ((ni + 31) / 32 + (nj + 31) / 32);
-    spline_nodes_kernel<<<blocks_for(warps * 32, 128), 128, 0, s>>>(pairs, kfy, ni, kfx, nj, u, v, coef);
+    spline_nodes_kernel<<<blocks_for(warps * 32, 128), 128, 0, s>>>(pairs, kfy, ni, kfx, nj, u, v, coef, gate);
     return cudaGetLastError();
 }
 
 cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
                         const qlpiv_frame *dst, const float *ys, int ni, const float *xs, int nj, SplineCoef coef,
-                        int int16_quirk, int image_mode) {
+                        int int16_quirk, int image_mode, const int *gate) {
     if (image_mode < 1 || image_mode > 3) return cudaErrorInvalidValue;
     dim3 blk(32, 8), grd(blocks_for(w, 32), blocks_for(h, kWarpRows), pairs);
     if (pixel_type == QLPIV_PIX_U8)
         warp_both_kernel<uint8_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk,
-                                                      image_mode);
+                                                      image_mode, gate);
     else if (pixel_type == QLPIV_PIX_U16)
         warp_both_kernel<uint16_t><<<grd, blk, 0, s>>>(src, dst, ys, ni, xs, nj, coef.c4_u, coef.c4_v, int16_quirk,
-                                                       image_mode);
+                                                       image_mode, gate);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();
@@ -943,6 +946,30 @@ cudaError_t launch_displaced_origins(cudaStream_t s, long count, const int *a_to
                                      const float *v, int *b_top, int *b_left) {
     if (count == 0) return cudaSuccess;
     displaced_origins_kernel<<<blocks_for(count, 256), 256, 0, s>>>(count, a_top, a_left, u, v, b_top, b_left);
+    return cudaGetLastError();
+}
+
+// InterAreaDisplacementStableStrategy.computeStableState (S/iareas/InterAreaDisplacementStableStrategy.java:19-36)
+// after pass `pass` of a level: the tiles of in_list (all `count` tiles when NULL) whose
+// increment out[ia].(u, v) has (float) sqrt(u^2 + v^2) (double) above max_disp stay EVALUATING
+// while pass < max_retries and are listed in out_list ([0] count, then tiles; zeroed before).
+__global__ void stable_update_kernel(int pass, int max_retries, float max_disp, const qlpiv_vector *out,
+                                     const int *in_list, long count, int *out_list) {
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long n = in_list != nullptr ? (long)in_list[0] : count;
+    if (k >= n) return;
+    const long ia = in_list != nullptr ? (long)in_list[1 + k] : k;
+    const double du = (double)out[ia].u, dv = (double)out[ia].v;
+    const float norm = (float)sqrt(du * du + dv * dv);
+    if (norm > max_disp && pass < max_retries) out_list[1 + atomicAdd(out_list, 1)] = (int)ia;
+}
+
+cudaError_t launch_stable_update(cudaStream_t s, int pass, int max_retries, float max_disp, const qlpiv_vector *out,
+                                 const int *in_list, long count, int *out_list) {
+    cudaError_t e = cudaMemsetAsync(out_list, 0, sizeof(int), s);
+    if (e != cudaSuccess || count == 0) return e;
+    stable_update_kernel<<<blocks_for(count, 256), 256, 0, s>>>(pass, max_retries, max_disp, out, in_list, count,
+                                                                  out_list);
     return cudaGetLastError();
 }
 

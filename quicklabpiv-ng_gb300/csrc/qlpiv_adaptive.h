@@ -64,11 +64,16 @@ cudaError_t launch_inherit_tiles(cudaStream_t s, int pairs, int mode, int pn, in
                                  float *cv);
 // Node quadruples of every pair's u and v surfaces in one launch; kfy / kfx: device knot
 // factors (knot_factors_dw) of the ni row knots and the nj column knots.
+// gate (optional, device): nothing is done when *gate == 0.
 cudaError_t launch_spline(cudaStream_t s, int pairs, const float2 *kfy, int ni, const float2 *kfx, int nj,
-                          const float *u, const float *v, SplineCoef coef);
+                          const float *u, const float *v, SplineCoef coef, const int *gate = nullptr);
 cudaError_t launch_warp(cudaStream_t s, int pixel_type, int pairs, int h, int w, const qlpiv_frame *src,
                         const qlpiv_frame *dst, const float *ys, int ni, const float *xs, int nj, SplineCoef coef,
-                        int int16_quirk, int image_mode);
+                        int int16_quirk, int image_mode, const int *gate = nullptr);
+// Tile states after a stabilisation pass (InterAreaDisplacementStableStrategy): the tiles of
+// in_list ([0] count, then tiles; NULL = all `count`) still EVALUATING go to out_list.
+cudaError_t launch_stable_update(cudaStream_t s, int pass, int max_retries, float max_disp, const qlpiv_vector *out,
+                                 const int *in_list, long count, int *out_list);
 // Micro / mini per-tile warping of every pair's tiles (grid tops[ni] x lefts[nj], side n; tile
 // displacements cu / cv [pairs][ni*nj]); image_mode 1 first, 2 second, 3 both.  Writes
 // [pairs][tiles][n][n] pixels of pixel_type and per-tile maxima.

@@ -59,6 +59,9 @@ struct AdaptivePlan {
     DevBuf mp_slots;      //   their claim bitmask (zeroed at allocation, zero between launches)
     DevBuf mp_retry;      //   and the list of IAs to run again (1 + tiles of the largest level)
     long mp_units = 0;
+    DevBuf stab_list;     // tile stabilisation: two lists of 1 + stab_cap ints (EVALUATING tiles)
+    DevBuf stab_vec;      //   and the increments of the last pass (stab_cap vectors)
+    long stab_cap = 0;
 };
 
 void destroy_plan(AdaptivePlan *p) {
@@ -70,7 +73,7 @@ void destroy_plan(AdaptivePlan *p) {
                           &l.d_sweeps, &l.d_tiles, &l.d_tmax})
             b->release();
     for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table, &p->flow, &p->flow_dense,
-                      &p->mp_batch, &p->mp_slots, &p->mp_retry})
+                      &p->mp_batch, &p->mp_slots, &p->mp_retry, &p->stab_list, &p->stab_vec})
         b->release();
     delete p;
 }
@@ -120,6 +123,16 @@ static qlpiv_status check_adaptive(const qlpiv_adaptive_desc *d, int pixel_type,
     if (d->clipping_mode < QLPIV_CLIP_ALLOWED || d->clipping_mode > QLPIV_CLIP_NO_OUT_OF_BOUND)
         return fail(QLPIV_E_ARG, "unknown clipping mode %d", d->clipping_mode);
     if (d->superposition_start < 0) return fail(QLPIV_E_ARG, "superposition start level %d < 0", d->superposition_start);
+    if (d->stable_mode != QLPIV_STABLE_SIMPLE && d->stable_mode != QLPIV_STABLE_MAX_DISPLACEMENT)
+        return fail(QLPIV_E_ARG, "unknown tile stabilisation mode %d", d->stable_mode);
+    if (d->stable_mode == QLPIV_STABLE_MAX_DISPLACEMENT) {
+        if (d->stable_max_retries < 1 || !(d->stable_max_displacement >= 0.0f))
+            return fail(QLPIV_E_ARG, "stabilisation needs max retries >= 1 and a maximum displacement >= 0");
+        if (d->validation != QLPIV_VALIDATE_NONE)
+            return fail(QLPIV_E_ARG, "tile stabilisation with vector validation is not supported");
+        if (per_tile_warp(d->warp_mode))
+            return fail(QLPIV_E_ARG, "tile stabilisation with micro / mini warping is not supported");
+    }
     if (d->validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN) {
         for (int n = d->ia_start; n >= d->ia_end; n >>= 1)
             if (!multipeak_supported(n, d->num_peaks, d->peak_kernel))
@@ -338,6 +351,14 @@ static qlpiv_status build_plan_inner(qlpiv_handle *h, const qlpiv_adaptive_desc 
         // the host vectors above die at scope exit: make the copies complete first
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "adaptive plan upload");
     }
+    if (d->stable_mode == QLPIV_STABLE_MAX_DISPLACEMENT && d->stable_max_retries > 1) {
+        long most = 0;
+        for (const LevelPlan &l : p->levels) most = l.count() * pairs > most ? l.count() * pairs : most;
+        if ((e = p->stab_list.ensure(sizeof(int) * 2 * (size_t)(1 + most))) != cudaSuccess ||
+            (e = p->stab_vec.ensure(sizeof(qlpiv_vector) * (size_t)most)) != cudaSuccess)
+            return cuda_fail(e, "stabilisation buffers");
+        p->stab_cap = most;
+    }
     if (batched_replay(*d)) {
         long units = 0, most = 0;
         for (const LevelPlan &l : p->levels) most = l.count() * pairs > most ? l.count() * pairs : most;
@@ -446,117 +467,136 @@ static qlpiv_status run_levels(qlpiv_handle *h, const qlpiv_frame *frames_dev) {
                 h->launches++;
             }
         }
-        const qlpiv_frame *src = frames_dev;
-        const int *bt = L.d_at.as<int>(), *bl = L.d_al.as<int>();
-        const bool tiles = per_tile_warp(d.warp_mode) && lv > 0;
-        if (tiles) {
-            StageScope sc(h, "tile-warp", (int)lv, L.g.n, 1, total);
-            const size_t tb = (size_t)total * L.g.n * L.g.n * pixel_bytes(p->pixel_type);
-            char *ta = L.d_tiles.as<char>();
-            float *mx = L.d_tmax.as<float>();
-            if ((e = launch_tile_warp(s, p->pixel_type, pairs, frames_dev, L.g.n, L.g.tiles_i, L.g.tiles_j,
-                                      L.d_tops.as<int>(), L.d_lefts.as<int>(), u, v, tile_image_mode(d.warp_mode),
-                                      tile_mini(d.warp_mode), fm, ta, ta + tb, mx, mx + total)) != cudaSuccess)
-                return cuda_fail(e, "tile warp");
-            h->launches++;
-        } else if (per_tile_warp(d.warp_mode)) {
-            // level 0: both tiles clipped at the grid (the displacements are zero)
-        } else if (full_warp(d.warp_mode)) {
-            if (lv > 0) {  // no warping at the first level: displacements are all zero
-                SplineCoef c = coef_of(L, pairs);
-                {
-                    StageScope sc(h, "spline", (int)lv, L.g.n, 1, total);
-                    if ((e = launch_spline(s, pairs, L.d_kfy.as<float2>(), L.g.tiles_i, L.d_kfx.as<float2>(),
-                                           L.g.tiles_j, u, v, c)) != cudaSuccess)
-                        return cuda_fail(e, "spline");
-                }
-                {
-                    StageScope sc(h, "warp", (int)lv, L.g.n, 1, (long)pairs * p->height * p->width);
-                    if ((e = launch_warp(s, p->pixel_type, pairs, p->height, p->width, frames_dev,
-                                         p->warped_table.as<qlpiv_frame>(), L.d_cyf.as<float>(), L.g.tiles_i,
-                                         L.d_cxf.as<float>(), L.g.tiles_j, c, d.int16_warp_quirk,
-                                         full_image_mode(d.warp_mode))) != cudaSuccess)
-                        return cuda_fail(e, "warp");
-                }
-                h->launches += 2;
-                src = p->warped_table.as<qlpiv_frame>();
-            }
-        } else {
-            StageScope sc(h, "origins", (int)lv, L.g.n, 1, total);
-            if ((e = launch_displaced_origins(s, total, L.d_at.as<int>(), L.d_al.as<int>(), u, v, L.d_bt.as<int>(),
-                                              L.d_bl.as<int>())) != cudaSuccess)
-                return cuda_fail(e, "displaced origins");
-            h->launches++;
-            bt = L.d_bt.as<int>();
-            bl = L.d_bl.as<int>();
-        }
-        IaJob job{};
-        job.frames = src;
-        job.frame_idx = L.d_fi.as<int>();
-        job.num_frames = pairs;
-        job.a_top = L.d_at.as<int>();
-        job.a_left = L.d_al.as<int>();
-        job.b_top = bt;
-        job.b_left = bl;
-        job.count = total;
-        job.norm_mode = d.norm_mode;
-        job.max_mode = d.max_mode;
-        job.fixed_max_a = job.fixed_max_b = fm;
-        // FirstImage / SecondImage: tiles cut from the warped (or, at level 0, the whole) frame keep
-        // the fixed maximum, tiles clipped from the other frame their own (Image.clipImageMatrix)
-        if (d.max_mode == QLPIV_MAX_FIXED && d.warp_mode == QLPIV_WARP_FIRST_BILINEAR) job.max_mode = QLPIV_MAX_FIXED_A;
-        if (d.max_mode == QLPIV_MAX_FIXED && d.warp_mode == QLPIV_WARP_SECOND_BILINEAR) job.max_mode = QLPIV_MAX_FIXED_B;
-        if (per_tile_warp(d.warp_mode)) {
-            job.max_mode = QLPIV_MAX_COMPUTE;  // level 0: clipped tiles
-            if (tiles) {  // the warped tiles, contiguous, with their maxima
-                const size_t tb = (size_t)total * L.g.n * L.g.n * pixel_bytes(p->pixel_type);
-                job.frames = nullptr;
-                job.frame_idx = nullptr;
-                job.img_a = L.d_tiles.p;
-                job.img_b = L.d_tiles.as<char>() + tb;
-                job.pitch_a = job.pitch_b = L.g.n;
-                job.h = (int)(total * L.g.n);
-                job.w = L.g.n;
-                job.a_top = job.a_left = job.b_top = job.b_left = nullptr;
-                job.max_mode = QLPIV_MAX_GIVEN;
-                job.max_a = L.d_tmax.as<float>();
-                job.max_b = L.d_tmax.as<float>() + total;
-            }
-        }
-        job.subpix = d.subpix_mode;
-        job.subpix_pixels = d.subpix_mode >= QLPIV_SUBPIX_GAUSS_LM ? d.subpix_pixels : 0;
-        job.subpix_iters = d.subpix_iterations;
-        job.acc_u = u;
-        job.acc_v = v;
-        if (d.clipping_mode == QLPIV_CLIP_NO_OUT_OF_BOUND) {
-            job.clip_top = L.d_at.as<int>();
-            job.clip_left = L.d_al.as<int>();
-            job.clip_n = L.g.n;
-            job.clip_h = p->height;
-            job.clip_w = p->width;
-        }
+        // tile stabilisation: pass r of the level (InterAreaDisplacementStableStrategy repeats the
+        // warp and the correlation of the tiles still EVALUATING, listed on the device; a pass
+        // whose list is empty does nothing)
+        const bool stab = d.stable_mode == QLPIV_STABLE_MAX_DISPLACEMENT && d.stable_max_retries > 1;
+        const int passes = stab ? d.stable_max_retries : 1;
+        int *lists[2] = {p->stab_list.as<int>(), p->stab_list.as<int>() + 1 + p->stab_cap};
         const bool validate = d.validation != QLPIV_VALIDATE_NONE;
-        if (d.validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN) {
-            // the multi-peak model selects FindMaximumMultiPeaks for every level (the others keep
-            // FindMaximumFromCenter)
-            job.num_peaks = d.num_peaks;
-            job.peak_kernel = d.peak_kernel;
-            job.peak_uv = L.d_puv.as<float2>();
-            job.npeaks = L.d_npk.as<uint8_t>();
-            if (p->mp_units > 0) {
-                job.mp_batch = p->mp_batch.as<MpBatch>();
-                job.mp_batch_units = p->mp_units;
-                job.mp_slots = p->mp_slots.as<unsigned>();
-                job.mp_retry = p->mp_retry.as<int>();
+        for (int pass = 1; pass <= passes; pass++) {
+            const int *list = pass == 1 ? nullptr : lists[pass & 1];  // EVALUATING tiles after pass - 1
+            const qlpiv_frame *src = frames_dev;
+            const int *bt = L.d_at.as<int>(), *bl = L.d_al.as<int>();
+            const bool tiles = per_tile_warp(d.warp_mode) && lv > 0;
+            if (tiles) {
+                StageScope sc(h, "tile-warp", (int)lv, L.g.n, 1, total);
+                const size_t tb = (size_t)total * L.g.n * L.g.n * pixel_bytes(p->pixel_type);
+                char *ta = L.d_tiles.as<char>();
+                float *mx = L.d_tmax.as<float>();
+                if ((e = launch_tile_warp(s, p->pixel_type, pairs, frames_dev, L.g.n, L.g.tiles_i, L.g.tiles_j,
+                                          L.d_tops.as<int>(), L.d_lefts.as<int>(), u, v, tile_image_mode(d.warp_mode),
+                                          tile_mini(d.warp_mode), fm, ta, ta + tb, mx, mx + total)) != cudaSuccess)
+                    return cuda_fail(e, "tile warp");
+                h->launches++;
+            } else if (per_tile_warp(d.warp_mode)) {
+                // level 0: both tiles clipped at the grid (the displacements are zero)
+            } else if (full_warp(d.warp_mode)) {
+                if (lv > 0) {  // no warping at the first level: displacements are all zero
+                    SplineCoef c = coef_of(L, pairs);
+                    {
+                        StageScope sc(h, "spline", (int)lv, L.g.n, 1, total);
+                        if ((e = launch_spline(s, pairs, L.d_kfy.as<float2>(), L.g.tiles_i, L.d_kfx.as<float2>(),
+                                               L.g.tiles_j, u, v, c, list)) != cudaSuccess)
+                            return cuda_fail(e, "spline");
+                    }
+                    {
+                        StageScope sc(h, "warp", (int)lv, L.g.n, 1, (long)pairs * p->height * p->width);
+                        if ((e = launch_warp(s, p->pixel_type, pairs, p->height, p->width, frames_dev,
+                                             p->warped_table.as<qlpiv_frame>(), L.d_cyf.as<float>(), L.g.tiles_i,
+                                             L.d_cxf.as<float>(), L.g.tiles_j, c, d.int16_warp_quirk,
+                                             full_image_mode(d.warp_mode), list)) != cudaSuccess)
+                            return cuda_fail(e, "warp");
+                    }
+                    h->launches += 2;
+                    src = p->warped_table.as<qlpiv_frame>();
+                }
+            } else {
+                StageScope sc(h, "origins", (int)lv, L.g.n, 1, total);
+                if ((e = launch_displaced_origins(s, total, L.d_at.as<int>(), L.d_al.as<int>(), u, v, L.d_bt.as<int>(),
+                                                  L.d_bl.as<int>())) != cudaSuccess)
+                    return cuda_fail(e, "displaced origins");
+                h->launches++;
+                bt = L.d_bt.as<int>();
+                bl = L.d_bl.as<int>();
+            }
+            IaJob job{};
+            job.frames = src;
+            job.frame_idx = L.d_fi.as<int>();
+            job.num_frames = pairs;
+            job.a_top = L.d_at.as<int>();
+            job.a_left = L.d_al.as<int>();
+            job.b_top = bt;
+            job.b_left = bl;
+            job.count = total;
+            job.norm_mode = d.norm_mode;
+            job.max_mode = d.max_mode;
+            job.fixed_max_a = job.fixed_max_b = fm;
+            // FirstImage / SecondImage: tiles cut from the warped (or, at level 0, the whole) frame keep
+            // the fixed maximum, tiles clipped from the other frame their own (Image.clipImageMatrix)
+            if (d.max_mode == QLPIV_MAX_FIXED && d.warp_mode == QLPIV_WARP_FIRST_BILINEAR) job.max_mode = QLPIV_MAX_FIXED_A;
+            if (d.max_mode == QLPIV_MAX_FIXED && d.warp_mode == QLPIV_WARP_SECOND_BILINEAR) job.max_mode = QLPIV_MAX_FIXED_B;
+            if (per_tile_warp(d.warp_mode)) {
+                job.max_mode = QLPIV_MAX_COMPUTE;  // level 0: clipped tiles
+                if (tiles) {  // the warped tiles, contiguous, with their maxima
+                    const size_t tb = (size_t)total * L.g.n * L.g.n * pixel_bytes(p->pixel_type);
+                    job.frames = nullptr;
+                    job.frame_idx = nullptr;
+                    job.img_a = L.d_tiles.p;
+                    job.img_b = L.d_tiles.as<char>() + tb;
+                    job.pitch_a = job.pitch_b = L.g.n;
+                    job.h = (int)(total * L.g.n);
+                    job.w = L.g.n;
+                    job.a_top = job.a_left = job.b_top = job.b_left = nullptr;
+                    job.max_mode = QLPIV_MAX_GIVEN;
+                    job.max_a = L.d_tmax.as<float>();
+                    job.max_b = L.d_tmax.as<float>() + total;
+                }
+            }
+            job.subpix = d.subpix_mode;
+            job.subpix_pixels = d.subpix_mode >= QLPIV_SUBPIX_GAUSS_LM ? d.subpix_pixels : 0;
+            job.subpix_iters = d.subpix_iterations;
+            job.acc_u = u;
+            job.acc_v = v;
+            if (d.clipping_mode == QLPIV_CLIP_NO_OUT_OF_BOUND) {
+                job.clip_top = L.d_at.as<int>();
+                job.clip_left = L.d_al.as<int>();
+                job.clip_n = L.g.n;
+                job.clip_h = p->height;
+                job.clip_w = p->width;
+            }
+            if (d.validation == QLPIV_VALIDATE_MULTIPEAK_MEDIAN) {
+                // the multi-peak model selects FindMaximumMultiPeaks for every level (the others keep
+                // FindMaximumFromCenter)
+                job.num_peaks = d.num_peaks;
+                job.peak_kernel = d.peak_kernel;
+                job.peak_uv = L.d_puv.as<float2>();
+                job.npeaks = L.d_npk.as<uint8_t>();
+                if (p->mp_units > 0) {
+                    job.mp_batch = p->mp_batch.as<MpBatch>();
+                    job.mp_batch_units = p->mp_units;
+                    job.mp_slots = p->mp_slots.as<unsigned>();
+                    job.mp_retry = p->mp_retry.as<int>();
+                }
+            }
+            if (stab) {
+                job.ia_list = list;
+                job.out = p->stab_vec.as<qlpiv_vector>();
+            }
+            int nk = 1;
+            {
+                StageScope sc(h, "xcorr", (int)lv, L.g.n, 1, total);
+                if ((e = launch_xcorr(job, L.g.n, p->pixel_type, s, h->num_sms, &nk)) != cudaSuccess)
+                    return cuda_fail(e, "xcorr");
+            }
+            h->launches += nk;
+            if (stab && pass < passes) {
+                if ((e = launch_stable_update(s, pass, passes, d.stable_max_displacement, job.out, list, total,
+                                              lists[(pass + 1) & 1])) != cudaSuccess)
+                    return cuda_fail(e, "tile stabilisation");
+                h->launches++;
             }
         }
-        int nk = 1;
-        {
-            StageScope sc(h, "xcorr", (int)lv, L.g.n, 1, total);
-            if ((e = launch_xcorr(job, L.g.n, p->pixel_type, s, h->num_sms, &nk)) != cudaSuccess)
-                return cuda_fail(e, "xcorr");
-        }
-        h->launches += nk;
         if (validate) {
             StageScope sc(h, "validate", (int)lv, L.g.n, 2, total);
             ValidateParams vp{L.g.tiles_i, L.g.tiles_j, validation_strategies(d), d.median_threshold,
@@ -647,6 +687,8 @@ size_t plan_device_bytes(const qlpiv_adaptive_desc *d, int pixel_type, int heigh
     const size_t stride = (img + 255) & ~(size_t)255;
     total += al(2 * stride * pairs) + al(sizeof(qlpiv_frame) * pairs);  // frames copied from the host
     if (full_warp(d->warp_mode)) total += al(2 * stride * pairs) + al(sizeof(qlpiv_frame) * pairs);
+    if (d->stable_mode == QLPIV_STABLE_MAX_DISPLACEMENT && d->stable_max_retries > 1)
+        total += al(sizeof(int) * 2 * (1 + most)) + al(sizeof(qlpiv_vector) * most);
     if (batched_replay(*d)) {
         int dev = 0, sms = 0;
         long units = 0;

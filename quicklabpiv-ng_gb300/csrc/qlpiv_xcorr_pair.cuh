@@ -140,7 +140,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
     __syncthreads();
     cl.sync();  // both CTAs are running before any distributed shared memory access
 
-    for (long ia = blockIdx.x / 2; ia < job.count; ia += gridDim.x / 2) {
+    const long count = job.ia_list != nullptr ? (long)job.ia_list[0] : job.count;
+    for (long k = blockIdx.x / 2; k < count; k += gridDim.x / 2) {
+        const long ia = job.ia_list != nullptr ? (long)job.ia_list[1 + k] : k;
         const Pix *imgA, *imgB;
         long pitch_a, pitch_b;
         int img_h, img_w;

@@ -241,3 +241,60 @@ def test_adaptive_mixed_division(qp, handle, oracle, start):
     yy, xx = np.meshgrid(gy, gx, indexing="ij")
     tr, tc = flow.displacement(yy, xx, (h, w))
     assert np.median(np.hypot(u[0] - tr, v[0] - tc)) < 0.3
+
+
+def _shifted(qp, h, w, di, dj, seed):
+    a, _ = qp.synth.particle_pair((h, w), qp.synth.Flow(vmax=0.0), ppp=0.03, diam=2.5, diam_sd=0.2, bits=8, seed=seed)
+    b = np.zeros_like(a)
+    b[di:, dj:] = a[:h - di, :w - dj]
+    return a, b
+
+
+@pytest.mark.parametrize("warp", [True, False])
+def test_adaptive_stabilisation_uniform_shift(qp, handle, oracle, warp):
+    """InterAreaDisplacementStableStrategy on a uniform (3, 2) px shift, every increment far from the
+    1 px maximum.  BothImages: the first level repeats the same correlation (no warping there) and
+    adds the increment on each of its 3 passes; the second level walks back to the shift in two.
+    No warping: the displaced B tiles meet the shift on the second pass.  The device loop matches
+    the oracle's on every vector and recovers the shift away from the borders."""
+    h, w = 256, 288
+    a, b = _shifted(qp, h, w, 3, 2, 11)
+    wm = qp.WARP_BOTH_BILINEAR if warp else qp.WARP_NONE
+    desc = qp.adaptive_desc(64, 32, 0.5, warp_mode=wm, fixed_max=255.0 if warp else 0.0,
+                            max_mode=qp.MAX_FIXED if warp else qp.MAX_COMPUTE, stable_max_displacement=1.0,
+                            stable_max_retries=3)
+    u, v = handle.piv_adaptive([a], [b], desc)
+    ou, ov = oracle.piv_adaptive(a, b, 64, 32, 0.5, fixed_max=255.0 if warp else None, warp=warp, stable_max=1.0,
+                                 stable_retries=3)
+    err = np.maximum(np.abs(u[0] - ou), np.abs(v[0] - ov))
+    assert err.max() <= 1e-3, float(err.max())
+    # (BothImages: full-scale tile maxima bias the level-1 correction of the 6 px the first level
+    # over-accumulated by up to ~0.2 px)
+    inner = (slice(1, -1), slice(1, -1))
+    tol = 0.3 if warp else 1e-3
+    assert np.abs(u[0][inner] - 3.0).max() < tol and np.abs(v[0][inner] - 2.0).max() < tol
+    # without stabilisation the first level's single pass is all the second level inherits
+    plain = qp.adaptive_desc(64, 32, 0.5, warp_mode=wm, fixed_max=255.0 if warp else 0.0,
+                             max_mode=qp.MAX_FIXED if warp else qp.MAX_COMPUTE)
+    pu, _ = handle.piv_adaptive([a], [b], plain)
+    if warp:
+        assert not np.array_equal(pu, u)
+
+
+def test_adaptive_stabilisation_vortex(qp, handle, oracle):
+    """Stabilisation on a vortex, three levels with BothImages warping: device and oracle loops
+    agree except where an increment lies within rounding of the maximum (the pass counts can then
+    differ); the result stays a vortex."""
+    h, w = 256, 320
+    flow = qp.synth.Flow(vmax=5.0, rc=48.0, shear=0.01)
+    a, b = qp.synth.particle_pair((h, w), flow, ppp=0.02, diam=2.5, diam_sd=0.3, noise=4.0, bits=8, seed=77)
+    desc = qp.adaptive_desc(64, 16, 0.5, fixed_max=255.0, stable_max_displacement=0.3, stable_max_retries=3)
+    u, v = handle.piv_adaptive([a], [b], desc)
+    ou, ov = oracle.piv_adaptive(a, b, 64, 16, 0.5, fixed_max=255.0, stable_max=0.3, stable_retries=3)
+    err = np.maximum(np.abs(u[0] - ou), np.abs(v[0] - ov))
+    assert np.mean(err <= 1e-3) >= 0.95 and np.median(err) < 1e-4, (float(np.mean(err <= 1e-3)), float(err.max()))
+    g = qp.grid.superposition(h, w, 64, 2, 0.5)
+    cy, cx = g.centres()
+    yy, xx = np.meshgrid(cy, cx, indexing="ij")
+    tr, tc = flow.displacement(yy, xx, (h, w))
+    assert np.median(np.hypot(u[0] - tr, v[0] - tc)) < 0.3
