@@ -684,7 +684,16 @@ typedef struct qlpiv_mat_export_params {
     int mark_invalid_as_nan;    /* invalid vectors written as NaN */
     const char *export_date;    /* NULL: the current UTC time */
     int layout;                 /* qlpiv_mat_layout */
-    int reserved[3];
+    int maps_per_file;          /* multi-volume export (ExecuteLocalPIVWorker's split exports,
+                                   ui/.../business/transfer/ExecuteLocalPIVWorker.java:172-215): with
+                                   0 < maps_per_file < frames (RUN / DENSE layouts) the frames go to
+                                   volumes of maps_per_file maps, volume k written to `path` with its
+                                   "_MV0.mat" replaced by "_MV<k>.mat"; each records
+                                   multiVolumeExport = 1, totalNumberOfVelocityMaps = frames,
+                                   multiVolumeLastVolume and (but the last) multiVolumeNextFilename,
+                                   and its velocities structs multiVolumeStartOffset (the first frame
+                                   index).  0: one file. */
+    int reserved[2];
 } qlpiv_mat_export_params;
 
 typedef struct qlpiv_mat_velocity_map {

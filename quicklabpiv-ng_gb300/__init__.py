@@ -215,7 +215,8 @@ class MatExportParams(ctypes.Structure):
     _fields_ = [("image_width", ctypes.c_int), ("image_height", ctypes.c_int), ("ia_start", ctypes.c_int),
                 ("ia_end", ctypes.c_int), ("overlap_factor", ctypes.c_float), ("frames", ctypes.c_int),
                 ("swap_uv", ctypes.c_int), ("mark_invalid_as_nan", ctypes.c_int),
-                ("export_date", ctypes.c_char_p), ("layout", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("export_date", ctypes.c_char_p), ("layout", ctypes.c_int), ("maps_per_file", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class MatVelocityMap(ctypes.Structure):
@@ -855,14 +856,15 @@ MAT_RUN, MAT_STEP, MAT_DENSE = 0, 1, 2
 
 
 def export_mat(path, maps, image_height, image_width, ia_start, ia_end, overlap_factor, swap_uv=False,
-               mark_invalid_as_nan=False, export_date=None, layout=MAT_RUN):
+               mark_invalid_as_nan=False, export_date=None, layout=MAT_RUN, maps_per_file=0):
     """Write the vector maps as a MATLAB level-5 file with the variables of
     S/exporter/StructMultiFrameFloatVelocityExporter.java.
 
     maps: one dict per IA size with u (row displacements) and v (column displacements), frames x
     tiles_i x tiles_j float32, ia (height, width), margins (top, left, bottom, right), optionally
     adaptive_step (MAT_STEP layout) and invalid (same shape, bool).  MAT_RUN (the end-of-run
-    export) stores the column displacement as `u` unless swap_uv, as PIVMap does."""
+    export) stores the column displacement as `u` unless swap_uv, as PIVMap does.
+    maps_per_file: split the frames into volumes (path with _MV0.mat, volume k as _MV<k>.mat)."""
     keep, table = [], (MatVelocityMap * max(1, len(maps)))()
     frames = None
     for k, m in enumerate(maps):
@@ -888,7 +890,8 @@ def export_mat(path, maps, image_height, image_width, ia_start, ia_end, overlap_
     p = MatExportParams(image_width=image_width, image_height=image_height, ia_start=ia_start, ia_end=ia_end,
                         overlap_factor=overlap_factor, frames=1 if frames is None else frames, swap_uv=int(bool(swap_uv)),
                         mark_invalid_as_nan=int(bool(mark_invalid_as_nan)), layout=layout,
-                        export_date=None if export_date is None else export_date.encode())
+                        export_date=None if export_date is None else export_date.encode(),
+                        maps_per_file=int(maps_per_file))
     _check(load_library().qlpiv_mat_export(os.fsencode(path), ctypes.byref(p), len(maps), table))
 
 

@@ -345,9 +345,39 @@ qlpiv_status qlpiv_tiff_read(const char *path, void *pixels, int64_t capacity_by
     }
 }
 
+// One MAT file holding frames [f0, f0 + nf) of the maps; multi: one volume of a multi-volume export
+// (next: the following volume's file name, empty for the last volume).
+static qlpiv_status write_volume(const char *path, const qlpiv_mat_export_params *p, int num_maps,
+                                 const qlpiv_mat_velocity_map *maps, int f0, int nf, bool multi,
+                                 const std::string &next);
+
 static qlpiv_status mat_export_body(const char *path, const qlpiv_mat_export_params *p, int num_maps,
                                     const qlpiv_mat_velocity_map *maps) {
     if (!path || !p || (num_maps > 0 && !maps)) return fail(QLPIV_E_ARG, "NULL argument");
+    if (p->maps_per_file < 0) return fail(QLPIV_E_ARG, "maps_per_file < 0");
+    if (p->maps_per_file == 0 || p->maps_per_file >= p->frames)
+        return write_volume(path, p, num_maps, maps, 0, p->frames, false, "");
+    if (p->layout == QLPIV_MAT_STEP) return fail(QLPIV_E_ARG, "the per-step layout is not split into volumes");
+    const std::string base(path);
+    const size_t at = base.find("_MV0.mat");
+    if (at == std::string::npos) return fail(QLPIV_E_ARG, "a multi-volume export path must contain _MV0.mat");
+    auto volume = [&](int k) {
+        return base.substr(0, at) + "_MV" + std::to_string(k) + ".mat" + base.substr(at + 8);
+    };
+    const int volumes = (p->frames + p->maps_per_file - 1) / p->maps_per_file;
+    for (int k = 0; k < volumes; k++) {
+        const int f0 = k * p->maps_per_file;
+        const int nf = p->frames - f0 < p->maps_per_file ? p->frames - f0 : p->maps_per_file;
+        const qlpiv_status st =
+            write_volume(volume(k).c_str(), p, num_maps, maps, f0, nf, true, k + 1 < volumes ? volume(k + 1) : "");
+        if (st != QLPIV_OK) return st;
+    }
+    return QLPIV_OK;
+}
+
+static qlpiv_status write_volume(const char *path, const qlpiv_mat_export_params *p, int num_maps,
+                                 const qlpiv_mat_velocity_map *maps, int f0, int nf, bool multi,
+                                 const std::string &next) {
     if (num_maps < 0 || p->frames <= 0) return fail(QLPIV_E_ARG, "num_maps < 0 or frames <= 0");
     if (p->layout != QLPIV_MAT_RUN && p->layout != QLPIV_MAT_STEP && p->layout != QLPIV_MAT_DENSE)
         return fail(QLPIV_E_ARG, "layout %d", p->layout);
@@ -388,6 +418,7 @@ static qlpiv_status mat_export_body(const char *path, const qlpiv_mat_export_par
         std::vector<std::string> names = {"imageWidth", "imageHeight", "iaStartI", "iaEndI", "iaStartJ", "iaEndJ",
                                           "overlapFactor", "hasSwappedUVVectors", "markInvalidAsNaN",
                                           "totalNumberOfVelocityMaps", "multiVolumeExport", "multiVolumeLastVolume"};
+        if (multi && !next.empty()) names.push_back("multiVolumeNextFilename");
         int32_scalar(v, "", p->image_width);
         int32_scalar(v, "", p->image_height);
         int32_scalar(v, "", p->ia_start);
@@ -398,8 +429,9 @@ static qlpiv_status mat_export_body(const char *path, const qlpiv_mat_export_par
         int32_scalar(v, "", p->swap_uv ? 1 : 0);
         int32_scalar(v, "", p->mark_invalid_as_nan ? 1 : 0);
         int32_scalar(v, "", p->frames);
-        int32_scalar(v, "", 0);
-        int32_scalar(v, "", 1);
+        int32_scalar(v, "", multi ? 1 : 0);
+        int32_scalar(v, "", multi && !next.empty() ? 0 : 1);
+        if (multi && !next.empty()) text(v, "", next);
         structure(out, "parameters", names, v);
     }
     for (int m = 0; m < num_maps; m++) {
@@ -412,7 +444,8 @@ static qlpiv_status mat_export_body(const char *path, const qlpiv_mat_export_par
         const int cols_out = dense ? mp.tiles_j - mp.margins[1] - mp.margins[3] : mp.tiles_j;
         int32_scalar(v, "", mp.ia_height);
         int32_scalar(v, "", mp.ia_width);
-        int32_scalar(v, "", run ? 0 : mp.adaptive_step);  // multiVolumeExport: one volume
+        int32_scalar(v, "", run ? (multi ? 1 : 0) : mp.adaptive_step);  // multiVolumeExport or adaptiveStep
+        if (multi) int32_scalar(v, "", f0);                              // multiVolumeStartOffset
         {
             Buf mv;
             int32_scalar(mv, "", mp.margins[0]);
@@ -427,9 +460,9 @@ static qlpiv_status mat_export_body(const char *path, const qlpiv_mat_export_par
             const bool rows = run ? (comp == 0) == (p->swap_uv != 0) : comp == 0;
             const float *src = rows ? mp.u : mp.v;
             // MATLAB order: i fastest, then j, then the frame
-            std::vector<float> col((size_t)rows_out * cols_out * p->frames);
+            std::vector<float> col((size_t)rows_out * cols_out * nf);
             size_t k = 0;
-            for (int f = 0; f < p->frames; f++)
+            for (int f = f0; f < f0 + nf; f++)
                 for (int j = 0; j < cols_out; j++)
                     for (int i = 0; i < rows_out; i++) {
                         const size_t s = f * per + (size_t)(i + r0) * mp.tiles_j + (j + c0);
@@ -438,12 +471,14 @@ static qlpiv_status mat_export_body(const char *path, const qlpiv_mat_export_par
                     }
             Buf body;
             body.element(miSINGLE, col.data(), sizeof(float) * col.size());
-            matrix(v, mxSINGLE, {rows_out, cols_out, p->frames}, "", body);
+            matrix(v, mxSINGLE, {rows_out, cols_out, nf}, "", body);
         }
         const std::string name = dense ? std::string("velocities")
                                        : "velocities" + std::to_string(mp.ia_height) + "x" + std::to_string(mp.ia_width);
-        structure(out, name, {"iaHeight", "iaWidth", run ? "multiVolumeExport" : "adaptiveStep", "margins", "u", "v"},
-                  v);
+        std::vector<std::string> fields = {"iaHeight", "iaWidth", run ? "multiVolumeExport" : "adaptiveStep"};
+        if (multi) fields.push_back("multiVolumeStartOffset");
+        for (const char *f : {"margins", "u", "v"}) fields.push_back(f);
+        structure(out, name, fields, v);
     }
     FILE *f = std::fopen(path, "wb");
     if (!f) return fail(QLPIV_E_ARG, "cannot create %s", path);

@@ -327,3 +327,43 @@ def test_mat_dense_export(qp, tmp_path):
     with pytest.raises(qp.QlpivError):
         qp.export_mat(tmp_path / "x.mat", [dict(u=du, v=dv, ia=(32, 32), margins=(0, 0, 0, 0))] * 2, h, w, 64, 32,
                       0.5, layout=qp.MAT_DENSE)
+
+
+@pytest.mark.parametrize("layout", [0, 2])
+def test_mat_export_multi_volume(qp, tmp_path, layout):
+    """Split exports (ExecuteLocalPIVWorker.java:172-215, StructMultiFrameFloatVelocityExporter.java:80-115,
+    185-262): 7 frames at 3 maps per file give _MV0, _MV1 (3 frames each) and _MV2 (1 frame); each
+    volume names the next one and records its first frame, the last one is flagged."""
+    sio = pytest.importorskip("scipy.io")
+    rng = np.random.default_rng(5 + layout)
+    maps = _maps(rng, frames=7)
+    if layout == qp.MAT_DENSE:
+        maps = maps[1:]
+    p = tmp_path / "run_MV0.mat"
+    qp.export_mat(p, maps, image_height=300, image_width=340, ia_start=32, ia_end=16, overlap_factor=0.5,
+                  export_date="Thu Dec 03 12:00:00 UTC 2026", layout=layout, maps_per_file=3)
+    for k, (f0, nf) in enumerate([(0, 3), (3, 3), (6, 1)]):
+        m = sio.loadmat(tmp_path / f"run_MV{k}.mat", squeeze_me=False, struct_as_record=True)
+        par = m["parameters"][0, 0]
+        last = k == 2
+        names = ("imageWidth", "imageHeight", "iaStartI", "iaEndI", "iaStartJ", "iaEndJ", "overlapFactor",
+                 "hasSwappedUVVectors", "markInvalidAsNaN", "totalNumberOfVelocityMaps", "multiVolumeExport",
+                 "multiVolumeLastVolume") + (() if last else ("multiVolumeNextFilename",))
+        assert par.dtype.names == names
+        assert par["totalNumberOfVelocityMaps"][0, 0] == 7 and par["multiVolumeExport"][0, 0] == 1
+        assert par["multiVolumeLastVolume"][0, 0] == int(last)
+        if not last:
+            assert str(par["multiVolumeNextFilename"][0]) == str(tmp_path / f"run_MV{k + 1}.mat")
+        for mp in maps:
+            name = "velocities" if layout == qp.MAT_DENSE else f"velocities{mp['ia'][0]}x{mp['ia'][1]}"
+            s = m[name][0, 0]
+            assert s.dtype.names == ("iaHeight", "iaWidth", "multiVolumeExport", "multiVolumeStartOffset",
+                                     "margins", "u", "v")
+            assert s["multiVolumeExport"][0, 0] == 1 and s["multiVolumeStartOffset"][0, 0] == f0
+            g = mp["margins"] if layout == qp.MAT_DENSE else (0, 0, 0, 0)
+            cols = np.moveaxis(mp["v"], 0, -1)[g[0]:mp["v"].shape[1] - g[2], g[1]:mp["v"].shape[2] - g[3]]
+            np.testing.assert_array_equal(s["u"], cols[:, :, f0:f0 + nf])
+    assert not (tmp_path / "run_MV3.mat").exists()
+    with pytest.raises(qp.QlpivError):   # the volume names come from _MV0.mat
+        qp.export_mat(tmp_path / "run.mat", maps, image_height=300, image_width=340, ia_start=32, ia_end=16,
+                      overlap_factor=0.5, layout=layout, maps_per_file=3)
