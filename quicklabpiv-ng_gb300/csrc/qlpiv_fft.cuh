@@ -8,8 +8,7 @@
 // from which the next pass reads the stride-G layout again.  The last pass leaves
 // the natural-order result in stride-G layout, so forward and inverse transforms
 // chain without data movement.  Groups never span warps, so the exchanges need only
-// __syncwarp().  Buffer index e is padded to e + (e >> 3) to spread the radix-8
-// writes over banks.
+// __syncwarp().  Buffer indices are padded (xpad) to spread the accesses over banks.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -32,6 +31,24 @@ __device__ __forceinline__ cplx mul_mi(cplx a) {
 }
 
 __device__ __forceinline__ int pad8(int e) { return e + (e >> 3); }
+
+// Exchange-buffer index of element e written by pass PASS of a length-M transform, layout L.
+// Layout 0: e + e/8 after every pass.  Layout 1 makes the 8-byte accesses of a 16-lane half-warp
+// hit 16 distinct bank pairs when one group fills the half-warp (M >= 128):
+//   pass 0 (radix 8) writes x[8g + t], the next pass reads x[g + G m]:     e + e/16;
+//   pass 1 (radix 8 after radix 8) writes x[64a + 8t + b] from lane 8a + b: e + 4 (e/32).
+// For M = 64 (two groups per half-warp) e + e/8 is conflict-free when the two groups' buffers
+// start 8 (mod 16) complex apart.
+template <int M, int L, int PASS>
+__device__ __forceinline__ int xpad(int e) {
+    if constexpr (L == 1 && M >= 128) return PASS == 0 ? e + (e >> 4) : e + 4 * (e >> 5);
+    else return e + (e >> 3);
+}
+// Complex elements an exchange buffer of layout L must hold.
+template <int M, int L>
+constexpr int xbuf_size() {
+    return L == 1 && M >= 128 ? M + 4 * (M / 32 - 1) : M + M / 8;
+}
 
 // Radix kernels, forward (e^{-2 pi i/R}) or inverse (e^{+2 pi i/R}), in place.
 template <bool INV>
@@ -80,7 +97,7 @@ __device__ __forceinline__ void dft8(cplx *v) {
 // M-th root of unity in `tw`), transformed, and output t goes to y[(i-k)*R + k + t*p].
 // If LAST, p*R == M and the output is y[i + t*p] = stride-G layout: kept in v[].
 // Otherwise the outputs are written to buf (padded index).
-template <int M, int R, int P, bool INV, bool LAST>
+template <int M, int R, int P, bool INV, bool LAST, int L = 0, int PASS = 0>
 __device__ __forceinline__ void stockham_pass(cplx *v, int g, cplx *buf, const cplx *tw) {
     constexpr int G = M / 8;
     constexpr int B = 8 / R;  // butterflies per lane
@@ -117,33 +134,33 @@ __device__ __forceinline__ void stockham_pass(cplx *v, int g, cplx *buf, const c
             const int k = i & (P - 1);
             const int j = (i - k) * R + k;
 #pragma unroll
-            for (int t = 0; t < R; t++) buf[pad8(j + t * P)] = u[s * R + t];
+            for (int t = 0; t < R; t++) buf[xpad<M, L, PASS>(j + t * P)] = u[s * R + t];
         }
         __syncwarp();
 #pragma unroll
-        for (int m = 0; m < 8; m++) v[m] = buf[pad8(g + G * m)];
+        for (int m = 0; m < 8; m++) v[m] = buf[xpad<M, L, PASS>(g + G * m)];
     }
 }
 
-// Full length-M FFT on stride-G layout data (in and out), using buf (M + M/8
+// Full length-M FFT on stride-G layout data (in and out), using buf (xbuf_size<M, L>()
 // complex, private to the group) for the exchanges.
-template <int M, bool INV>
+template <int M, bool INV, int L = 0>
 __device__ __forceinline__ void fft_group(cplx *v, int g, cplx *buf, const cplx *tw) {
     static_assert(M == 32 || M == 64 || M == 128 || M == 256, "unsupported FFT size");
     if constexpr (M == 32) {
-        stockham_pass<32, 8, 1, INV, false>(v, g, buf, tw);
-        stockham_pass<32, 4, 8, INV, true>(v, g, buf, tw);
+        stockham_pass<32, 8, 1, INV, false, L, 0>(v, g, buf, tw);
+        stockham_pass<32, 4, 8, INV, true, L, 1>(v, g, buf, tw);
     } else if constexpr (M == 64) {
-        stockham_pass<64, 8, 1, INV, false>(v, g, buf, tw);
-        stockham_pass<64, 8, 8, INV, true>(v, g, buf, tw);
+        stockham_pass<64, 8, 1, INV, false, L, 0>(v, g, buf, tw);
+        stockham_pass<64, 8, 8, INV, true, L, 1>(v, g, buf, tw);
     } else if constexpr (M == 128) {
-        stockham_pass<128, 8, 1, INV, false>(v, g, buf, tw);
-        stockham_pass<128, 8, 8, INV, false>(v, g, buf, tw);
-        stockham_pass<128, 2, 64, INV, true>(v, g, buf, tw);
+        stockham_pass<128, 8, 1, INV, false, L, 0>(v, g, buf, tw);
+        stockham_pass<128, 8, 8, INV, false, L, 1>(v, g, buf, tw);
+        stockham_pass<128, 2, 64, INV, true, L, 2>(v, g, buf, tw);
     } else {
-        stockham_pass<256, 8, 1, INV, false>(v, g, buf, tw);
-        stockham_pass<256, 8, 8, INV, false>(v, g, buf, tw);
-        stockham_pass<256, 4, 64, INV, true>(v, g, buf, tw);
+        stockham_pass<256, 8, 1, INV, false, L, 0>(v, g, buf, tw);
+        stockham_pass<256, 8, 8, INV, false, L, 1>(v, g, buf, tw);
+        stockham_pass<256, 4, 64, INV, true, L, 2>(v, g, buf, tw);
     }
 }
 

@@ -50,11 +50,28 @@ struct XcorrShape {
     static constexpr int T = N == 16 ? 64 : (N == 32 ? 256 : 512);  // threads per CTA
     static constexpr int NG = T / G;                   // concurrent transforms
     static constexpr int ROUNDS = N / NG;              // tasks per group per phase
-    static constexpr int RP = M + M / 8 + 1;           // region pitch (complex), odd
+    // Shared-memory layouts (8-byte accesses of a 16-lane half-warp should touch 16 distinct bank
+    // pairs).  Regions: slot s of a column-pair region at rslot(s), region pitch RP odd; FFT
+    // exchanges in per-group buffers of pitch SP, layout L (qlpiv_fft.cuh).  N = 32: two groups
+    // per half-warp, SP = 8 (mod 16) and the group-to-task maps below keep them on disjoint banks.
+    static constexpr int L = N >= 32 ? 1 : 0;
+    static constexpr int RP = N >= 32 ? M + 1 : M + M / 8 + 1;
+    static constexpr int SP = N == 64 ? xbuf_size<M, 1>() : (N == 32 ? 72 : RP);
     static constexpr int MIN_BLOCKS = N == 16 ? 16 : (N == 32 ? 4 : 2);
-    static constexpr size_t SCR_BYTES = sizeof(cplx) * (size_t)(NG * RP);
+    static constexpr size_t SCR_BYTES = sizeof(cplx) * (size_t)(NG * SP);
     static constexpr size_t SMEM = sizeof(cplx) * (size_t)(M + N * RP) + SCR_BYTES + 64 * sizeof(uint64_t) +
                                    32 * 56 /* fit queue */ + 256 /* multi-peak list */;
+    __device__ static __forceinline__ int rslot(int s) { return N >= 32 ? s : pad8(s); }
+    // Task of group grp in round r: the row of the row pass, the column pair of the column pass,
+    // the row pair of the row-pair pass.  N = 32 (region pitch 65 = 1 mod 16): the two groups of a
+    // half-warp take rows / columns 8 apart and row pairs 4 apart.  N = 64: the two groups of a
+    // warp take row pairs 4 apart (their 4-byte plane stores land on disjoint banks).
+    __device__ static __forceinline__ int task_row(int grp, int r) {
+        return N == 32 ? ((grp >> 1) & 7) + 16 * (grp >> 4) + 8 * (grp & 1) : grp + NG * r;
+    }
+    __device__ static __forceinline__ int task_pair(int grp, int r) {
+        return N >= 32 ? ((grp >> 1) & 3) + 8 * (grp >> 3) + 4 * (grp & 1) + NG * r : grp + NG * r;
+    }
 };
 
 // FindMaximumMultiPeaks geometry of a d x d plane: slices = ceil(d / kw) per axis, the
@@ -1002,22 +1019,27 @@ __device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float m
                                               int *mp_li, int *mp_lj) {
     using S = XcorrShape<N>;
     constexpr int RP = S::RP;
-    auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)]; };
+    auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + S::rslot(i)) + (j & 1)]; };
     multipeak_core<S::D, S::T>(job, ia, minf, P, scr, red, fitq, fitv, qn, mp_lv, mp_li, mp_lj);
 }
 
 // PP: the P-point sub-pixel interpolators are compiled in (their out-of-line double-precision
 // fits cost the common instantiation registers even when unused).
+template <typename S>
+__device__ __forceinline__ int grp_of(int tid) { return tid / S::G; }
+
 template <int N, typename Pix, bool PP>
 __global__ void __launch_bounds__(XcorrShape<N>::T, XcorrShape<N>::MIN_BLOCKS)
 xcorr_kernel(IaJob job) {
     using S = XcorrShape<N>;
-    constexpr int M = S::M, D = S::D, G = S::G, NG = S::NG, ROUNDS = S::ROUNDS, RP = S::RP, T = S::T;
+    constexpr int M = S::M, D = S::D, G = S::G, NG = S::NG, ROUNDS = S::ROUNDS, RP = S::RP, SP = S::SP, T = S::T;
+    constexpr int L = S::L;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx *tw = reinterpret_cast<cplx *>(smem_raw);
     cplx *reg = tw + M;           // N regions of RP complex
-    cplx *scr = reg + N * RP;     // NG scratch buffers of RP complex
-    uint64_t *red = reinterpret_cast<uint64_t *>(scr + NG * RP);  // 64 words
+    cplx *scr = reg + N * RP;     // NG exchange buffers of SP complex
+    cplx *xb = scr + grp_of<S>(threadIdx.x) * SP;                  // this group's exchange buffer
+    uint64_t *red = reinterpret_cast<uint64_t *>(scr + NG * SP);  // 64 words
     FitRec *fitq = reinterpret_cast<FitRec *>(red + 64);           // 32 queued fits
     float *mp_lv = reinterpret_cast<float *>(fitq + 32);           // multi-peak list (ascending)
     int *mp_li = reinterpret_cast<int *>(mp_lv + QLPIV_MAX_PEAKS + 1);
@@ -1085,7 +1107,7 @@ xcorr_kernel(IaJob job) {
         float mxa = 0.0f, mxb = 0.0f;
 #pragma unroll
         for (int r = 0; r < ROUNDS; r++) {
-            const int n1 = grp + NG * r;
+            const int n1 = S::task_row(grp, r);
 #pragma unroll
             for (int m = 0; m < 4; m++) {
                 const int n2 = g + G * m;
@@ -1124,7 +1146,7 @@ xcorr_kernel(IaJob job) {
         // ---- 2. row pass ----
 #pragma unroll
         for (int r = 0; r < ROUNDS; r++) {
-            const int n1 = grp + NG * r;
+            const int n1 = S::task_row(grp, r);
             cplx v[8];
 #pragma unroll
             for (int m = 0; m < 4; m++) {
@@ -1137,7 +1159,7 @@ xcorr_kernel(IaJob job) {
                 v[m] = {a, b};
                 v[m + 4] = {0.0f, 0.0f};
             }
-            fft_group<M, false>(v, g, scr + grp * RP, tw);
+            fft_group<M, false, L>(v, g, xb, tw);
 #pragma unroll
             for (int m = 0; m < 8; m++) {
                 const int k2 = g + G * m;
@@ -1146,7 +1168,7 @@ xcorr_kernel(IaJob job) {
                 else if (k2 == N) { region = 0; slot = N + n1; }
                 else if (k2 < N) { region = k2; slot = n1; }
                 else { region = M - k2; slot = N + n1; }
-                reg[region * RP + pad8(slot)] = v[m];
+                reg[region * RP + S::rslot(slot)] = v[m];
             }
         }
         __syncthreads();
@@ -1154,19 +1176,18 @@ xcorr_kernel(IaJob job) {
         // ---- 3. column tasks ----
 #pragma unroll
         for (int r = 0; r < ROUNDS; r++) {
-            const int c = grp + NG * r;
+            const int c = S::task_row(grp, r);
             cplx *rg = reg + c * RP;
             cplx z1[8], z2[8];
 #pragma unroll
             for (int m = 0; m < 4; m++) {
-                z1[m] = rg[pad8(g + G * m)];
-                z2[m] = rg[pad8(N + g + G * m)];
+                z1[m] = rg[S::rslot(g + G * m)];
+                z2[m] = rg[S::rslot(N + g + G * m)];
                 z1[m + 4] = {0.0f, 0.0f};
                 z2[m + 4] = {0.0f, 0.0f};
             }
-            __syncwarp();
-            fft_group<M, false>(z1, g, rg, tw);
-            fft_group<M, false>(z2, g, rg, tw);
+            fft_group<M, false, L>(z1, g, xb, tw);
+            fft_group<M, false, L>(z2, g, xb, tw);
             // P(k1) = F*G/M^2, F = (Z1 + conj Zm)/2, G = (Z1 - conj Zm)/(2i), where Zm is the
             // mirror element Z(M-k1, M-c): held by lane (G-g)%G at m' = 7-m (g>0) or (8-m)%8.
             const int src = gbase + ((G - g) & (G - 1));
@@ -1202,10 +1223,9 @@ xcorr_kernel(IaJob job) {
                     p[m] = {p[m].x - pn.y, p[m].y + pn.x};  // P0 + i * PN
                 }
             }
-            fft_group<M, true>(p, g, rg, tw);
-            __syncwarp();
+            fft_group<M, true, L>(p, g, xb, tw);
 #pragma unroll
-            for (int m = 0; m < 8; m++) rg[pad8(g + G * m)] = p[m];
+            for (int m = 0; m < 8; m++) rg[S::rslot(g + G * m)] = p[m];
         }
         __syncthreads();
 
@@ -1216,32 +1236,31 @@ xcorr_kernel(IaJob job) {
         float *regf = reinterpret_cast<float *>(reg);
 #pragma unroll
         for (int r = 0; r < ROUNDS; r++) {
-            const int pr = grp + NG * r;
+            const int pr = S::task_pair(grp, r);
             const int ra_ = 2 * pr, rb_ = 2 * pr + 1;
             cplx y[8];
 #pragma unroll
             for (int m = 0; m < 8; m++) {
                 const int k2 = g + G * m;
                 if (k2 == 0 || k2 == N) {
-                    const cplx qa = reg[pad8(ra_)], qb = reg[pad8(rb_)];
+                    const cplx qa = reg[S::rslot(ra_)], qb = reg[S::rslot(rb_)];
                     y[m] = (k2 == 0) ? cplx{qa.x, qb.x} : cplx{qa.y, qb.y};
                 } else if (k2 < N) {
-                    const cplx qa = reg[k2 * RP + pad8(ra_)], qb = reg[k2 * RP + pad8(rb_)];
+                    const cplx qa = reg[k2 * RP + S::rslot(ra_)], qb = reg[k2 * RP + S::rslot(rb_)];
                     y[m] = {qa.x - qb.y, qa.y + qb.x};
                 } else {
                     const int cc = M - k2;
-                    const cplx qa = reg[cc * RP + pad8(ra_)], qb = reg[cc * RP + pad8(rb_)];
+                    const cplx qa = reg[cc * RP + S::rslot(ra_)], qb = reg[cc * RP + S::rslot(rb_)];
                     y[m] = {qa.x + qb.y, qb.x - qa.y};
                 }
             }
-            fft_group<M, true>(y, g, scr + grp * RP, tw);
-            __syncwarp();
+            fft_group<M, true, L>(y, g, xb, tw);
 #pragma unroll
             for (int m = 0; m < 8; m++) {
                 const int n2 = g + G * m;
                 // keep the plane in the row slots this pair has consumed
-                regf[2 * ((n2 >> 1) * RP + pad8(ra_)) + (n2 & 1)] = y[m].x;
-                regf[2 * ((n2 >> 1) * RP + pad8(rb_)) + (n2 & 1)] = y[m].y;
+                regf[2 * ((n2 >> 1) * RP + S::rslot(ra_)) + (n2 & 1)] = y[m].x;
+                regf[2 * ((n2 >> 1) * RP + S::rslot(rb_)) + (n2 & 1)] = y[m].y;
                 if (multi > 0) {
                     // FindMaximumMultiPeaks visits every cell of the (2N-1)^2 plane
                     if (n2 <= M - 2) {
@@ -1269,7 +1288,7 @@ xcorr_kernel(IaJob job) {
         }
 
         // ---- 5. CTA reduction; the fit is queued and run 32 IAs at a time ----
-        auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + pad8(i)) + (j & 1)]; };
+        auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + S::rslot(i)) + (j & 1)]; };
         if (multi == 0) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
