@@ -37,7 +37,8 @@ constexpr int kMinBlocks = 4;        // 16 warps per SM
 constexpr int N = 16, M = 32, D = 31;
 constexpr int XS = 17;               // exchange stride A -> B (complex), odd
 constexpr int QS = 34;               // exchange stride B -> C (complex), even: 16-byte row pairs
-constexpr int PS = 33;               // plane row stride (floats)
+constexpr int PS = 43;               // plane row stride (floats), odd: the multi-peak cell reads
+                                     // (3 x 3 cells of 32 records) spread over the banks
 constexpr int kXchgCplx = (32 * XS > 17 * QS ? 32 * XS : 17 * QS);  // 578
 constexpr int kPlaneFloats = D * PS;
 // per-warp shared memory (bytes): exchange, plane, reduction words, fit queue, multi-peak list
@@ -338,14 +339,20 @@ __global__ void __launch_bounds__(w16::kThreads, w16::kMinBlocks) xcorr16_warp_k
         // q(i) = e(i) + w32^-i o(i), q(i + 16) = e(i) - w32^-i o(i)
         __syncwarp();    // every lane has read its column from the exchange buffer
 #pragma unroll
-        for (int i = 0; i < 16; i++) {
-            cplx other;
-            other.x = __shfl_sync(0xffffffffu, E[i].x, partner);
-            other.y = __shfl_sync(0xffffffffu, E[i].y, partner);
-            const cplx e = role_o ? other : E[i];
-            const cplx o = tw32<true>(role_o ? E[i] : other, i);
-            const cplx q = role_o ? cplx{e.x - o.x, e.y - o.y} : cplx{e.x + o.x, e.y + o.y};
-            X[colL * QS + (role_o ? 16 : 0) + i] = q;
+        for (int i = 0; i < 16; i += 2) {
+            // two consecutive rows per 16-byte store (8 lanes per wavefront, no bank conflict)
+            cplx q2[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                cplx other;
+                other.x = __shfl_sync(0xffffffffu, E[i + h].x, partner);
+                other.y = __shfl_sync(0xffffffffu, E[i + h].y, partner);
+                const cplx e = role_o ? other : E[i + h];
+                const cplx o = tw32<true>(role_o ? E[i + h] : other, i + h);
+                q2[h] = role_o ? cplx{e.x - o.x, e.y - o.y} : cplx{e.x + o.x, e.y + o.y};
+            }
+            *reinterpret_cast<float4 *>(X + colL * QS + (role_o ? 16 : 0) + i) =
+                make_float4(q2[0].x, q2[0].y, q2[1].x, q2[1].y);
         }
         __syncwarp();
 
