@@ -546,19 +546,29 @@ def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64
         table[k] = (ta.data_ptr(), tb.data_ptr(), s_, s_, s_)
     h = pkg.Handle(dev.index)
     hs = torch.cuda.ExternalStream(h.stream, device=dev)
+    def time_plan(pl):
+        for _ in range(warmup):
+            pl.run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(hs)
+        for _ in range(steps):
+            pl.run()
+        e1.record(hs)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    # the two schedules with default grids, then the autotuned plan (the reported one)
+    schedules_ms = {}
+    for name, mode in (("per_size_default_grids", pkg.AUTOTUNE_OFF), ("persistent", pkg.AUTOTUNE_PERSISTENT)):
+        alt = pkg.MixedPlan(h, table, sizes, ofac, pkg.PIX_U8, autotune=mode)
+        schedules_ms[name] = time_plan(alt)
+        alt.close()
     t0 = time.perf_counter()
-    plan = pkg.MixedPlan(h, table, sizes, ofac, pkg.PIX_U8, autotune=True)
+    plan = pkg.MixedPlan(h, table, sizes, ofac, pkg.PIX_U8, autotune=pkg.AUTOTUNE_ON)
     plan_s = time.perf_counter() - t0
-    for _ in range(warmup):
-        plan.run()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(hs)
-    for _ in range(steps):
-        plan.run()
-    e1.record(hs)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
+    ms = time_plan(plan)
+    schedules_ms["autotuned"] = ms
     total = plan.total
     ia_by_n = {n: int(sum(plan.tiles[q][0] * plan.tiles[q][1] for q in range(count) if sizes[q] == n))
                for n in (16, 32, 64, 128)}
@@ -596,6 +606,8 @@ def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64
             "ia_vectors_per_s": total / (ms * 1e-3), "fp32_tflops": flops / (ms * 1e-3) / 1e12,
             "algorithmic_gbs": bytes_ / (ms * 1e-3) / 1e9, "plan_seconds": plan_s,
             "autotuned_waves": {str(n): int(plan.waves[k]) for k, n in enumerate((16, 32, 64, 128))},
+            "autotuned_schedule": "persistent" if plan.schedule == pkg.SCHEDULE_PERSISTENT else "per_size",
+            "schedules_ms_per_step": schedules_ms,
             "accuracy": accuracy,
             "plain_per_call": {"frame_pairs_per_s": per_call_pairs, "rounds_frame_pairs_per_s": rounds,
                                "ia_vectors_per_s": sample_ias * per_call_pairs / len(sample),

@@ -560,17 +560,29 @@ qlpiv_status qlpiv_piv_flow_device(qlpiv_handle *h, const qlpiv_adaptive_desc *p
                                    float *out_u, float *out_v, float *dense_u, float *dense_v);
 
 /* ---------------- mixed batches ----------------
- * Many frame pairs of uneven sizes, each with its own IA size (16, 32, 64) and overlap factor,
- * correlated as one flattened work list per IA size (the pair's level-0 SuperPosition grid),
- * launched from one captured CUDA graph whose branches run the sizes concurrently.  `frames`
- * is a host table of device images; the plan keeps a device copy and the output.  With
- * autotune the grid of each size's launch is chosen by timing 1, 2, 4, 8, 16 and 32 waves of
- * resident CTAs on its work list.  Output vectors are size-major and pair-contiguous: pair q's
- * tiles_i x tiles_j tiles (row-major) start at pair_offset[q]. */
+ * Many frame pairs of uneven sizes, each with its own IA size (16, 32, 64, 128) and overlap
+ * factor, correlated as one flattened work list per IA size (the pair's level-0 SuperPosition
+ * grid) and replayed from one captured CUDA graph.  Two schedules:
+ *   QLPIV_SCHEDULE_PER_SIZE    one launch per IA size, each on its own graph branch (the sizes
+ *                              run concurrently);
+ *   QLPIV_SCHEDULE_PERSISTENT  IA 16, 32 and 64 in one persistent launch (one CTA per SM drains
+ *                              the three work lists, largest IAs first), IA 128 on its own branch;
+ *                              FindMaximumFromCenter with the 3-point (or no) sub-pixel fit.
+ * Both write the same vectors.  `autotune`: QLPIV_AUTOTUNE_OFF (per-size launches, default
+ * grids), QLPIV_AUTOTUNE_ON (the grid of each size's launch chosen by timing 1, 2, 4, 8, 16 and
+ * 32 waves of resident CTAs on its work list, then the faster schedule over the whole batch),
+ * QLPIV_AUTOTUNE_PERSISTENT (the persistent schedule where it applies, default grids).
+ * `frames` is a host table of device images; the plan keeps a device copy and the output.
+ * Output vectors are size-major and pair-contiguous: pair q's tiles_i x tiles_j tiles
+ * (row-major) start at pair_offset[q]. */
 typedef struct qlpiv_mixed_plan qlpiv_mixed_plan;
+enum qlpiv_autotune { QLPIV_AUTOTUNE_OFF = 0, QLPIV_AUTOTUNE_ON = 1, QLPIV_AUTOTUNE_PERSISTENT = 2 };
+enum qlpiv_schedule { QLPIV_SCHEDULE_PER_SIZE = 0, QLPIV_SCHEDULE_PERSISTENT = 1 };
 qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmpl, int pixel_type, int num_pairs,
                                      const qlpiv_frame *frames, const int32_t *ia_size, const float *overlap_factor,
                                      int autotune, qlpiv_mixed_plan **plan);
+/* The schedule the plan's graph runs (qlpiv_schedule). */
+qlpiv_status qlpiv_mixed_plan_schedule(const qlpiv_mixed_plan *plan, int32_t *schedule);
 /* total_vectors; pair_offset[num_pairs + 1] (the last entry = total); tiles_ij[2 num_pairs]
  * (tiles_i, tiles_j); waves[4]
  * chosen for sizes 16, 32, 64, 128 (0: default).  Any output may be NULL. */

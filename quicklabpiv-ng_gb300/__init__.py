@@ -87,6 +87,9 @@ class AdaptiveDesc(ctypes.Structure):
 
 
 STABLE_SIMPLE, STABLE_MAX_DISPLACEMENT = 0, 1
+# mixed batch plans: autotune modes and schedules
+AUTOTUNE_OFF, AUTOTUNE_ON, AUTOTUNE_PERSISTENT = 0, 1, 2
+SCHEDULE_PER_SIZE, SCHEDULE_PERSISTENT = 0, 1
 
 
 CLIP_ALLOWED, CLIP_LOGGED, CLIP_NO_OUT_OF_BOUND = 0, 1, 2
@@ -272,6 +275,7 @@ _SIGNATURES = {
                                    _vp, _vp, _vp, _vp]),
     "qlpiv_mixed_plan_create": (_i, [_vp, ctypes.POINTER(PassDesc), _i, _i, _vp, _vp, _vp, _i, ctypes.POINTER(_vp)]),
     "qlpiv_mixed_plan_info": (_i, [_vp, ctypes.POINTER(ctypes.c_int64), _vp, _vp, _vp]),
+    "qlpiv_mixed_plan_schedule": (_i, [_vp, ctypes.POINTER(ctypes.c_int32)]),
     "qlpiv_mixed_plan_run": (_i, [_vp, _vp, ctypes.POINTER(_vp)]),
     "qlpiv_mixed_plan_download": (_i, [_vp, _vp, _vp]),
     "qlpiv_mixed_plan_destroy": (_i, [_vp]),
@@ -917,7 +921,9 @@ def export_dense_mat(path, desc, height, width, dense_u, dense_v, **kw):
 
 class MixedPlan:
     """Mixed batch plan (qlpiv_mixed_plan_*): pairs of uneven sizes, each with its own IA size
-    and overlap, one graph launch per batch.  frames: FRAME_DTYPE table of device images."""
+    and overlap, one graph launch per batch.  frames: FRAME_DTYPE table of device images;
+    autotune: AUTOTUNE_OFF / AUTOTUNE_ON (True) / AUTOTUNE_PERSISTENT.  `schedule` is the one
+    the graph runs (SCHEDULE_PER_SIZE or SCHEDULE_PERSISTENT)."""
 
     def __init__(self, handle, frames, ia_sizes, overlap_factors, pixel_type, autotune=True, **desc_kw):
         self._h = handle
@@ -939,6 +945,9 @@ class MixedPlan:
         _check(self._lib.qlpiv_mixed_plan_info(p, ctypes.byref(tot), _addr(self.pair_offset), _addr(self.tiles),
                                                _addr(self.waves)))
         self.total = tot.value
+        sched = ctypes.c_int32()
+        _check(self._lib.qlpiv_mixed_plan_schedule(p, ctypes.byref(sched)))
+        self.schedule = sched.value
 
     def run(self):
         """Queues the batch on the handle's stream; returns the device address of the vectors."""

@@ -6,10 +6,12 @@
 // job per thread, OpenClGpuManager.java:121-148).  Here every pair's level-0 grid
 // (AdaptiveInterAreaStrategySuperPosition, as qlpiv_grid_superposition) is appended to the work
 // list of its IA size; the plan launches K1 once per size, each launch on its own branch of the
-// graph so the sizes run concurrently, and the graph is replayed per batch.  The autotuner times
-// each size's launch over its real work list with 1, 2, 4, 8, 16 and 32 waves of resident CTAs
-// and keeps the fastest.  Vectors come out size-major (16, 32, 64, 128) and pair-contiguous
-// inside a size.
+// graph so the sizes run concurrently, and the graph is replayed per batch (schedule
+// QLPIV_SCHEDULE_PER_SIZE); or IA 16, 32 and 64 in one persistent launch that drains the three
+// work lists (qlpiv_xcorr_mixed.cu) beside the IA-128 launch (QLPIV_SCHEDULE_PERSISTENT).  The
+// autotuner times each size's launch over its real work list with 1, 2, 4, 8, 16 and 32 waves of
+// resident CTAs and keeps the fastest, then times both schedules over the whole batch and keeps
+// the faster.  Vectors come out size-major (16, 32, 64, 128) and pair-contiguous inside a size.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -19,6 +21,7 @@
 #include "qlpiv_handle.h"
 #include "qlpiv_internal.h"
 #include "qlpiv_xcorr.cuh"
+#include "qlpiv_xcorr_launch.h"
 
 using namespace qlpiv;
 
@@ -46,6 +49,10 @@ struct qlpiv_mixed_plan {
     std::vector<int64_t> pair_offset;
     std::vector<int32_t> tiles_ij;
     int64_t total = 0;
+    int schedule = QLPIV_SCHEDULE_PER_SIZE;
+    DevBuf next;  // the persistent launch's work counters
+    cudaStream_t mixed_side = nullptr;
+    cudaEvent_t mixed_done = nullptr;
     cudaEvent_t fork = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -74,11 +81,52 @@ IaJob group_job(const qlpiv_mixed_plan *p, const Group &g) {
     return job;
 }
 
+// The persistent launch covers IA 16, 32 and 64 (IA 128 keeps its own launch).
+bool persistent_supported(const qlpiv_mixed_plan *p) {
+    bool any = false;
+    for (int k = 0; k < 3; k++) {
+        const Group &g = p->groups[k];
+        if (g.count == 0) continue;
+        any = true;
+        if (!mixed_kernel_supported(group_job(p, g))) return false;
+    }
+    return any;
+}
+
+// Queues one batch on s with the given schedule: every launch on its own branch forked from s,
+// joined back into s (also the body of the captured graph).
+cudaError_t enqueue(qlpiv_mixed_plan *p, cudaStream_t s, int num_sms, int schedule) {
+    cudaError_t e = cudaEventRecord(p->fork, s);
+    for (Group &g : p->groups) {
+        if (g.count == 0 || e != cudaSuccess) continue;
+        if (schedule == QLPIV_SCHEDULE_PERSISTENT && g.n != 128) continue;
+        if ((e = cudaStreamWaitEvent(g.side, p->fork, 0)) != cudaSuccess) break;
+        IaJob job = group_job(p, g);
+        if ((e = launch_xcorr(job, g.n, p->pixel_type, g.side, num_sms)) != cudaSuccess) break;
+        if ((e = cudaEventRecord(g.done, g.side)) != cudaSuccess) break;
+        if ((e = cudaStreamWaitEvent(s, g.done, 0)) != cudaSuccess) break;
+    }
+    if (e == cudaSuccess && schedule == QLPIV_SCHEDULE_PERSISTENT) {
+        MixedJob mj{};
+        const int order[3] = {2, 1, 0};  // IA 64, 32, 16
+        for (int k = 0; k < 3; k++) mj.job[k] = group_job(p, p->groups[order[k]]);
+        mj.next = p->next.as<unsigned>();
+        if ((e = cudaStreamWaitEvent(p->mixed_side, p->fork, 0)) == cudaSuccess &&
+            (e = launch_k1_mixed(mj, p->pixel_type, p->mixed_side, num_sms)) == cudaSuccess &&
+            (e = cudaEventRecord(p->mixed_done, p->mixed_side)) == cudaSuccess)
+            e = cudaStreamWaitEvent(s, p->mixed_done, 0);
+    }
+    return e;
+}
+
 void release(qlpiv_mixed_plan *p) {
     if (!p) return;
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->fork) cudaEventDestroy(p->fork);
+    if (p->mixed_side) cudaStreamDestroy(p->mixed_side);
+    if (p->mixed_done) cudaEventDestroy(p->mixed_done);
+    p->next.release();
     for (Group &g : p->groups) {
         if (g.side) cudaStreamDestroy(g.side);
         if (g.done) cudaEventDestroy(g.done);
@@ -195,6 +243,7 @@ qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmp
     }
     // autotune the waves of each size on its own work list (also the launches' first-use set-up,
     // which must not happen inside the capture)
+    const bool tune = autotune == QLPIV_AUTOTUNE_ON;
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
@@ -203,8 +252,8 @@ qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmp
         const int cands[6] = {1, 2, 4, 8, 16, 32};
         float best = 1e30f;
         int best_w = 8;
-        for (int c = 0; c < (autotune ? 6 : 1); c++) {
-            g.waves = autotune ? cands[c] : 0;
+        for (int c = 0; c < (tune ? 6 : 1); c++) {
+            g.waves = tune ? cands[c] : 0;
             IaJob job = group_job(p, g);
             if ((e = launch_xcorr(job, g.n, pixel_type, s, h->num_sms)) != cudaSuccess) break;  // warm-up
             cudaEventRecord(t0, s);
@@ -219,7 +268,27 @@ qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmp
             }
         }
         if (e != cudaSuccess) break;
-        g.waves = autotune ? best_w : 0;
+        g.waves = tune ? best_w : 0;
+    }
+    // the schedule: per-size launches, or the persistent launch (timed over the whole batch)
+    if (e == cudaSuccess && autotune != QLPIV_AUTOTUNE_OFF && persistent_supported(p)) {
+        if ((e = p->next.ensure(4 * sizeof(unsigned))) == cudaSuccess &&
+            (e = cudaStreamCreateWithFlags(&p->mixed_side, cudaStreamNonBlocking)) == cudaSuccess)
+            e = cudaEventCreateWithFlags(&p->mixed_done, cudaEventDisableTiming);
+        float ms_sched[2] = {1e30f, 1e30f};
+        for (int sc = 0; sc < 2 && e == cudaSuccess; sc++) {
+            if (!tune && sc != QLPIV_SCHEDULE_PERSISTENT) continue;
+            if ((e = enqueue(p, s, h->num_sms, sc)) != cudaSuccess) break;  // warm-up
+            cudaEventRecord(t0, s);
+            for (int r = 0; r < 3 && e == cudaSuccess; r++) e = enqueue(p, s, h->num_sms, sc);
+            cudaEventRecord(t1, s);
+            if (e != cudaSuccess || (e = cudaEventSynchronize(t1)) != cudaSuccess) break;
+            cudaEventElapsedTime(&ms_sched[sc], t0, t1);
+        }
+        if (e == cudaSuccess)
+            p->schedule = ms_sched[QLPIV_SCHEDULE_PERSISTENT] < ms_sched[QLPIV_SCHEDULE_PER_SIZE]
+                              ? QLPIV_SCHEDULE_PERSISTENT
+                              : QLPIV_SCHEDULE_PER_SIZE;
     }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
@@ -227,20 +296,12 @@ qlpiv_status qlpiv_mixed_plan_create(qlpiv_handle *h, const qlpiv_pass_desc *tmp
         release(p);
         return cuda_fail(e, "autotune");
     }
-    // capture: fork one branch per size from the handle's stream, join back
+    // capture: fork one branch per launch from the handle's stream, join back
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
         release(p);
         return cuda_fail(e, "graph capture");
     }
-    cudaError_t ce = cudaEventRecord(p->fork, s);
-    for (Group &g : p->groups) {
-        if (g.count == 0 || ce != cudaSuccess) continue;
-        if ((ce = cudaStreamWaitEvent(g.side, p->fork, 0)) != cudaSuccess) break;
-        IaJob job = group_job(p, g);
-        if ((ce = launch_xcorr(job, g.n, pixel_type, g.side, h->num_sms)) != cudaSuccess) break;
-        if ((ce = cudaEventRecord(g.done, g.side)) != cudaSuccess) break;
-        if ((ce = cudaStreamWaitEvent(s, g.done, 0)) != cudaSuccess) break;
-    }
+    cudaError_t ce = enqueue(p, s, h->num_sms, p->schedule);
     e = cudaStreamEndCapture(s, &p->graph);
     if (ce != cudaSuccess || e != cudaSuccess ||
         (e = cudaGraphInstantiate(&p->exec, p->graph, 0)) != cudaSuccess) {
@@ -262,6 +323,12 @@ qlpiv_status qlpiv_mixed_plan_info(const qlpiv_mixed_plan *p, int64_t *total_vec
     return QLPIV_OK;
 }
 
+qlpiv_status qlpiv_mixed_plan_schedule(const qlpiv_mixed_plan *p, int32_t *schedule) {
+    if (!p || !schedule) return fail(QLPIV_E_ARG, "NULL argument");
+    *schedule = p->schedule;
+    return QLPIV_OK;
+}
+
 qlpiv_status qlpiv_mixed_plan_run(qlpiv_handle *h, qlpiv_mixed_plan *p, qlpiv_vector **device_out) {
     if (!h || !p) return fail(QLPIV_E_ARG, "NULL argument");
     if (h->device != p->device) return fail(QLPIV_E_ARG, "plan belongs to device %d", p->device);
@@ -269,7 +336,9 @@ qlpiv_status qlpiv_mixed_plan_run(qlpiv_handle *h, qlpiv_mixed_plan *p, qlpiv_ve
     DeviceScope ds(h->device);
     const cudaError_t e = cudaGraphLaunch(p->exec, h->stream);
     if (e != cudaSuccess) return cuda_fail(e, "graph launch");
-    for (const Group &g : p->groups) h->launches += g.count > 0 ? 1 : 0;
+    for (const Group &g : p->groups)
+        h->launches += g.count > 0 && (p->schedule == QLPIV_SCHEDULE_PER_SIZE || g.n == 128) ? 1 : 0;
+    if (p->schedule == QLPIV_SCHEDULE_PERSISTENT) h->launches += 1;
     if (device_out) *device_out = p->out.as<qlpiv_vector>();
     return QLPIV_OK;
 }

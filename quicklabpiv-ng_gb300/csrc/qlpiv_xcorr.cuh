@@ -1025,31 +1025,63 @@ __device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float m
 
 // PP: the P-point sub-pixel interpolators are compiled in (their out-of-line double-precision
 // fits cost the common instantiation registers even when unused).
-template <typename S>
-__device__ __forceinline__ int grp_of(int tid) { return tid / S::G; }
-
-template <int N, typename Pix, bool PP>
-__global__ void __launch_bounds__(XcorrShape<N>::T, XcorrShape<N>::MIN_BLOCKS)
-xcorr_kernel(IaJob job) {
+// Shared memory of one group of the CTA kernel (the T threads that work on one IA): twiddles,
+// column-pair regions, exchange buffers, reduction words, fit queue, multi-peak list, P-point
+// stencils (2 P floats per queued fit at the end).
+template <int N>
+struct CtaSmem {
+    cplx *tw, *reg, *scr;
+    uint64_t *red;
+    FitRec *fitq;
+    float *mp_lv;
+    int *mp_li, *mp_lj;
+    float *fitv;
+};
+template <int N>
+__device__ __forceinline__ CtaSmem<N> cta_smem(unsigned char *base) {
     using S = XcorrShape<N>;
-    constexpr int M = S::M, D = S::D, G = S::G, NG = S::NG, ROUNDS = S::ROUNDS, RP = S::RP, SP = S::SP, T = S::T;
-    constexpr int L = S::L;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    cplx *tw = reinterpret_cast<cplx *>(smem_raw);
-    cplx *reg = tw + M;           // N regions of RP complex
-    cplx *scr = reg + N * RP;     // NG exchange buffers of SP complex
-    cplx *xb = scr + grp_of<S>(threadIdx.x) * SP;                  // this group's exchange buffer
-    uint64_t *red = reinterpret_cast<uint64_t *>(scr + NG * SP);  // 64 words
-    FitRec *fitq = reinterpret_cast<FitRec *>(red + 64);           // 32 queued fits
-    float *mp_lv = reinterpret_cast<float *>(fitq + 32);           // multi-peak list (ascending)
-    int *mp_li = reinterpret_cast<int *>(mp_lv + QLPIV_MAX_PEAKS + 1);
-    int *mp_lj = mp_li + QLPIV_MAX_PEAKS + 1;
-    float *fitv = reinterpret_cast<float *>(mp_lj + QLPIV_MAX_PEAKS + 1);  // P-point stencils
-    int qn = 0;                                                    // uniform across the CTA
-    const int multi = job.num_peaks;                               // 0: FindMaximumFromCenter
-    const int KQ = multi > 0 ? multi : 1;                          // fit records per IA
+    CtaSmem<N> sm;
+    sm.tw = reinterpret_cast<cplx *>(base);
+    sm.reg = sm.tw + S::M;                                      // N regions of RP complex
+    sm.scr = sm.reg + N * S::RP;                                // NG exchange buffers of SP complex
+    sm.red = reinterpret_cast<uint64_t *>(sm.scr + S::NG * S::SP);  // 64 words
+    sm.fitq = reinterpret_cast<FitRec *>(sm.red + 64);          // 32 queued fits
+    sm.mp_lv = reinterpret_cast<float *>(sm.fitq + 32);         // multi-peak list (ascending)
+    sm.mp_li = reinterpret_cast<int *>(sm.mp_lv + QLPIV_MAX_PEAKS + 1);
+    sm.mp_lj = sm.mp_li + QLPIV_MAX_PEAKS + 1;
+    sm.fitv = reinterpret_cast<float *>(sm.mp_lj + QLPIV_MAX_PEAKS + 1);
+    return sm;
+}
 
-    const int tid = threadIdx.x;
+// Barrier of a group of T threads: the whole CTA (NAMED false) or named barrier `bar` (the
+// persistent mixed-size kernel runs two 256-thread groups per CTA).
+template <int T, bool NAMED>
+__device__ __forceinline__ void bar_sync(int bar) {
+    if constexpr (NAMED) asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(T) : "memory");
+    else __syncthreads();
+}
+
+// Steps 1-5 of the CTA kernel for IA `ia` by the T threads of one group (tid = 0..T-1): the fit
+// records are queued at fitq[qn..) and flushed by the group's warp 0 every 32 (or, batched
+// multi-peak, staged as entry nb of mpb).  Multi-peak modes need the whole CTA (NAMED false).
+template <int N, typename Pix, bool PP, bool NAMED>
+__device__ __forceinline__ void xcorr_cta_ia(const IaJob &job, long ia, const CtaSmem<N> &sm, int tid, int bar,
+                                             int &qn, MpBatch *mpb, int &nb) {
+    using S = XcorrShape<N>;
+    constexpr int M = S::M, D = S::D, G = S::G, NG = S::NG, ROUNDS = S::ROUNDS, RP = S::RP, T = S::T;
+    constexpr int L = S::L;
+    cplx *const tw = sm.tw;
+    cplx *const reg = sm.reg;
+    cplx *const scr = sm.scr;
+    cplx *const xb = scr + (tid / G) * S::SP;  // this group's exchange buffer
+    uint64_t *const red = sm.red;
+    FitRec *const fitq = sm.fitq;
+    float *const fitv = sm.fitv;
+    float *const mp_lv = sm.mp_lv;
+    int *const mp_li = sm.mp_li;
+    int *const mp_lj = sm.mp_lj;
+    const int multi = NAMED ? 0 : job.num_peaks;  // 0: FindMaximumFromCenter
+    const int KQ = multi > 0 ? multi : 1;         // fit records per IA
     const int g = tid % G;
     const int grp = tid / G;
     const int lane = tid & 31;
@@ -1057,8 +1089,304 @@ xcorr_kernel(IaJob job) {
     constexpr int NWARPS = T / 32;
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
     const int gbase = lane & ~(G - 1);
+    const Pix *imgA, *imgB;
+    long pitch_a, pitch_b;
+    int img_h, img_w;
+    if (job.frames != nullptr) {
+        const int fi = job.frame_idx[ia];
+        const qlpiv_frame fr = (unsigned)fi < (unsigned)job.num_frames ? job.frames[fi] : qlpiv_frame{};
+        imgA = reinterpret_cast<const Pix *>(fr.img_a);
+        imgB = reinterpret_cast<const Pix *>(fr.img_b);
+        pitch_a = pitch_b = (long)fr.pitch;
+        img_h = fr.height;
+        img_w = fr.width;
+    } else {
+        imgA = reinterpret_cast<const Pix *>(job.img_a);
+        imgB = reinterpret_cast<const Pix *>(job.img_b);
+        pitch_a = job.pitch_a;
+        pitch_b = job.pitch_b;
+        img_h = job.h;
+        img_w = job.w;
+    }
+    int at, al, bt, bl;
+    if (job.a_top != nullptr) {
+        at = job.a_top[ia]; al = job.a_left[ia];
+        bt = job.b_top[ia]; bl = job.b_left[ia];
+    } else {  // contiguous tiles: tile ia is rows [ia*N, ia*N + N) of an N-wide image
+        at = bt = (int)(ia * N);
+        al = bl = 0;
+    }
 
-    for (int e = tid; e < M; e += T) tw[e] = job.twiddles[e];
+    // ---- 1. raw tile pixels for this thread's row transforms ----
+    float ra[ROUNDS][4], rb[ROUNDS][4];
+    float mxa = 0.0f, mxb = 0.0f;
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++) {
+        const int n1 = S::task_row(grp, r);
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const int n2 = g + G * m;
+            ra[r][m] = load_pix(imgA, pitch_a, img_h, img_w, at + (N - 1 - n1), al + (N - 1 - n2));
+            rb[r][m] = load_pix(imgB, pitch_b, img_h, img_w, bt + n1, bl + n2);
+            mxa = fmaxf(mxa, ra[r][m]);
+            mxb = fmaxf(mxb, rb[r][m]);
+        }
+    }
+    float maxA, maxB;
+    if (job.max_mode == QLPIV_MAX_COMPUTE || job.max_mode == QLPIV_MAX_FIXED_A ||
+        job.max_mode == QLPIV_MAX_FIXED_B) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mxa = fmaxf(mxa, __shfl_xor_sync(0xffffffffu, mxa, o));
+            mxb = fmaxf(mxb, __shfl_xor_sync(0xffffffffu, mxb, o));
+        }
+        float *redf = reinterpret_cast<float *>(red);
+        if (lane == 0) { redf[warp] = mxa; redf[32 + warp] = mxb; }
+        bar_sync<T, NAMED>(bar);
+        mxa = 0.0f; mxb = 0.0f;
+#pragma unroll
+        for (int k = 0; k < NWARPS; k++) { mxa = fmaxf(mxa, redf[k]); mxb = fmaxf(mxb, redf[32 + k]); }
+        maxA = job.max_mode == QLPIV_MAX_FIXED_A ? job.fixed_max_a : fmaxf(mxa, 16.0f);
+        maxB = job.max_mode == QLPIV_MAX_FIXED_B ? job.fixed_max_b : fmaxf(mxb, 16.0f);
+    } else if (job.max_mode == QLPIV_MAX_GIVEN) {
+        maxA = job.max_a[ia];
+        maxB = job.max_b[ia];
+    } else {
+        maxA = job.fixed_max_a;
+        maxB = job.fixed_max_b;
+    }
+    if (job.norm_mode == QLPIV_NORM_MAX_A) maxB = maxA;
+    const bool normalize = job.norm_mode != QLPIV_NORM_NONE;
+
+    // ---- 2. row pass ----
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++) {
+        const int n1 = S::task_row(grp, r);
+        cplx v[8];
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            float a = ra[r][m], b = rb[r][m];
+            if (normalize) {
+                // (v / max) * 16 + 1 with IEEE single operations, as in Java
+                a = __fadd_rn(__fmul_rn(__fdiv_rn(a, maxA), 16.0f), 1.0f);
+                b = __fadd_rn(__fmul_rn(__fdiv_rn(b, maxB), 16.0f), 1.0f);
+            }
+            v[m] = {a, b};
+            v[m + 4] = {0.0f, 0.0f};
+        }
+        fft_group<M, false, L>(v, g, xb, tw);
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            const int k2 = g + G * m;
+            int region, slot;
+            if (k2 == 0) { region = 0; slot = n1; }
+            else if (k2 == N) { region = 0; slot = N + n1; }
+            else if (k2 < N) { region = k2; slot = n1; }
+            else { region = M - k2; slot = N + n1; }
+            reg[region * RP + S::rslot(slot)] = v[m];
+        }
+    }
+    bar_sync<T, NAMED>(bar);
+
+    // ---- 3. column tasks ----
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++) {
+        const int c = S::task_row(grp, r);
+        cplx *rg = reg + c * RP;
+        cplx z1[8], z2[8];
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            z1[m] = rg[S::rslot(g + G * m)];
+            z2[m] = rg[S::rslot(N + g + G * m)];
+            z1[m + 4] = {0.0f, 0.0f};
+            z2[m + 4] = {0.0f, 0.0f};
+        }
+        fft_group<M, false, L>(z1, g, xb, tw);
+        fft_group<M, false, L>(z2, g, xb, tw);
+        // P(k1) = F*G/M^2, F = (Z1 + conj Zm)/2, G = (Z1 - conj Zm)/(2i), where Zm is the
+        // mirror element Z(M-k1, M-c): held by lane (G-g)%G at m' = 7-m (g>0) or (8-m)%8.
+        const int src = gbase + ((G - g) & (G - 1));
+        const float scale = 0.5f * 0.5f / (float)(M * M);
+        cplx p[8];
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            // c == 0: both columns are self-mirrored; otherwise the mirror is in z2
+            const cplx s2 = (g == 0) ? z2[(8 - m) & 7] : z2[7 - m];
+            const cplx s1 = (g == 0) ? z1[(8 - m) & 7] : z1[7 - m];
+            cplx snd = (c == 0) ? s1 : s2;
+            cplx zm;
+            zm.x = __shfl_sync(0xffffffffu, snd.x, src);
+            zm.y = __shfl_sync(0xffffffffu, snd.y, src);
+            const cplx a = z1[m];
+            // F*2 = (a.x + zm.x, a.y - zm.y);  G*2 = (a.y + zm.y, -(a.x - zm.x))
+            const float fr = a.x + zm.x, fi = a.y - zm.y;
+            const float gr = a.y + zm.y, gi = zm.x - a.x;
+            p[m] = {(fr * gr - fi * gi) * scale, (fr * gi + fi * gr) * scale};
+        }
+        if (c == 0) {
+            // second self-mirrored column (k2 = N): P_N packed as the imaginary part
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                const cplx snd = (g == 0) ? z2[(8 - m) & 7] : z2[7 - m];
+                cplx zm;
+                zm.x = __shfl_sync(gmask, snd.x, src);
+                zm.y = __shfl_sync(gmask, snd.y, src);
+                const cplx a = z2[m];
+                const float fr = a.x + zm.x, fi = a.y - zm.y;
+                const float gr = a.y + zm.y, gi = zm.x - a.x;
+                const cplx pn = {(fr * gr - fi * gi) * scale, (fr * gi + fi * gr) * scale};
+                p[m] = {p[m].x - pn.y, p[m].y + pn.x};  // P0 + i * PN
+            }
+        }
+        fft_group<M, true, L>(p, g, xb, tw);
+#pragma unroll
+        for (int m = 0; m < 8; m++) rg[S::rslot(g + G * m)] = p[m];
+    }
+    bar_sync<T, NAMED>(bar);
+
+    // ---- 4. row-pair pass + per-lane peak scoring ----
+    uint64_t best = 0ull;
+    uint32_t best_ij = 0u;
+    float minf = 3.402823466e38f;
+    float *regf = reinterpret_cast<float *>(reg);
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++) {
+        const int pr = S::task_pair(grp, r);
+        const int ra_ = 2 * pr, rb_ = 2 * pr + 1;
+        cplx y[8];
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            const int k2 = g + G * m;
+            if (k2 == 0 || k2 == N) {
+                const cplx qa = reg[S::rslot(ra_)], qb = reg[S::rslot(rb_)];
+                y[m] = (k2 == 0) ? cplx{qa.x, qb.x} : cplx{qa.y, qb.y};
+            } else if (k2 < N) {
+                const cplx qa = reg[k2 * RP + S::rslot(ra_)], qb = reg[k2 * RP + S::rslot(rb_)];
+                y[m] = {qa.x - qb.y, qa.y + qb.x};
+            } else {
+                const int cc = M - k2;
+                const cplx qa = reg[cc * RP + S::rslot(ra_)], qb = reg[cc * RP + S::rslot(rb_)];
+                y[m] = {qa.x + qb.y, qb.x - qa.y};
+            }
+        }
+        fft_group<M, true, L>(y, g, xb, tw);
+#pragma unroll
+        for (int m = 0; m < 8; m++) {
+            const int n2 = g + G * m;
+            // keep the plane in the row slots this pair has consumed
+            regf[2 * ((n2 >> 1) * RP + S::rslot(ra_)) + (n2 & 1)] = y[m].x;
+            regf[2 * ((n2 >> 1) * RP + S::rslot(rb_)) + (n2 & 1)] = y[m].y;
+            if (multi > 0) {
+                // FindMaximumMultiPeaks visits every cell of the (2N-1)^2 plane
+                if (n2 <= M - 2) {
+                    minf = fminf(minf, y[m].x);
+                    if (rb_ <= M - 2) minf = fminf(minf, y[m].y);
+                }
+            } else if (n2 >= 1 && n2 <= M - 2) {
+                if (ra_ >= 1) {
+                    minf = fminf(minf, y[m].x);
+                    const uint64_t k = peak_key(y[m].x, ra_, n2, N);
+                    if (k > best) { best = k; best_ij = ((uint32_t)ra_ << 16) | (uint32_t)n2; }
+                }
+                if (rb_ <= M - 2) {
+                    minf = fminf(minf, y[m].y);
+                    const uint64_t k = peak_key(y[m].y, rb_, n2, N);
+                    if (k > best) { best = k; best_ij = ((uint32_t)rb_ << 16) | (uint32_t)n2; }
+                }
+            }
+            if (job.planes != nullptr && n2 < D) {
+                float *pl = job.planes + ia * (long)(D * D);
+                pl[ra_ * D + n2] = y[m].x;
+                if (rb_ < D) pl[rb_ * D + n2] = y[m].y;
+            }
+        }
+    }
+
+    // ---- 5. CTA reduction; the fit is queued and run 32 IAs at a time ----
+    auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + S::rslot(i)) + (j & 1)]; };
+    if (multi == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint64_t ok = __shfl_xor_sync(0xffffffffu, best, o);
+            const uint32_t oij = __shfl_xor_sync(0xffffffffu, best_ij, o);
+            if (ok > best) { best = ok; best_ij = oij; }
+            minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
+        }
+        bar_sync<T, NAMED>(bar);  // red[] reuse after the max reduction
+        if (lane == 0) {
+            red[warp] = best;
+            red[32 + warp] = ((uint64_t)best_ij << 32) | (uint64_t)__float_as_uint(minf);
+        }
+        bar_sync<T, NAMED>(bar);
+        if (warp == 0) {
+            uint64_t bk = 0ull;
+            uint32_t bij = 0u;
+            float mn = 3.402823466e38f;
+            if (lane < NWARPS) {
+                bk = red[lane];
+                bij = (uint32_t)(red[32 + lane] >> 32);
+                mn = __uint_as_float((uint32_t)red[32 + lane]);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const uint64_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
+                const uint32_t oij = __shfl_xor_sync(0xffffffffu, bij, o);
+                // ties on the full key cannot occur between distinct cells (the rank is unique)
+                if (ok > bk) { bk = ok; bij = oij; }
+                mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            }
+            if (lane == 0) {
+                FitRec r;
+                r.ia = ia;
+                r.mn = mn;
+                r.pi = 0;
+                r.pj = 0;
+                r.pv = 0.0f;
+                if (bk != 0ull) {
+                    r.pi = (int)(bij >> 16);
+                    r.pj = (int)(bij & 0xffffu);
+                    r.pv = __uint_as_float((uint32_t)(bk >> 32));
+                }
+                r.slot = 0;
+                r.npk = 1;
+                fit_stencil<D>(r, job, P, fitv + qn * 2 * job.subpix_pixels);
+                fitq[qn] = r;
+            }
+        }
+    } else if (mpb == nullptr) {
+        multipeak_select<N>(job, ia, minf, regf, scr, red, fitq, fitv, qn, mp_lv, mp_li, mp_lj);
+    } else {
+        multipeak_stage_call<D, T>(job, ia, minf, P, scr, red, mpb, nb);
+        if (++nb == kMpBatch) {
+            if (warp == 0) mp_batch_run<D, PP>(mpb, nb, lane, job, fitq, fitv);
+            nb = 0;
+        }
+    }
+    if (mpb == nullptr) {
+        qn += KQ;
+        if (qn + KQ > 32) {
+            if (warp == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
+            qn = 0;
+        }
+    }
+    bar_sync<T, NAMED>(bar);  // regions are rewritten by the next IA
+}
+
+template <int N, typename Pix, bool PP>
+__global__ void __launch_bounds__(XcorrShape<N>::T, XcorrShape<N>::MIN_BLOCKS)
+xcorr_kernel(IaJob job) {
+    using S = XcorrShape<N>;
+    constexpr int T = S::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const CtaSmem<N> sm = cta_smem<N>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int D = S::D;
+    FitRec *const fitq = sm.fitq;
+    float *const fitv = sm.fitv;
+    int qn = 0;  // uniform across the CTA
+    const int multi = job.num_peaks;
+
+    for (int e = tid; e < S::M; e += T) sm.tw[e] = job.twiddles[e];
     __syncthreads();
 
     // batched multi-peak replay: a batch claimed for this CTA (filled and replayed by warp 0) and
@@ -1074,287 +1402,7 @@ xcorr_kernel(IaJob job) {
     const long count = job.ia_list != nullptr ? (long)job.ia_list[0] : job.count;
     for (long k = blockIdx.x; k < count; k += gridDim.x) {
         const long ia = job.ia_list != nullptr ? (long)job.ia_list[1 + k] : k;
-        const Pix *imgA, *imgB;
-        long pitch_a, pitch_b;
-        int img_h, img_w;
-        if (job.frames != nullptr) {
-            const int fi = job.frame_idx[ia];
-            const qlpiv_frame fr = (unsigned)fi < (unsigned)job.num_frames ? job.frames[fi] : qlpiv_frame{};
-            imgA = reinterpret_cast<const Pix *>(fr.img_a);
-            imgB = reinterpret_cast<const Pix *>(fr.img_b);
-            pitch_a = pitch_b = (long)fr.pitch;
-            img_h = fr.height;
-            img_w = fr.width;
-        } else {
-            imgA = reinterpret_cast<const Pix *>(job.img_a);
-            imgB = reinterpret_cast<const Pix *>(job.img_b);
-            pitch_a = job.pitch_a;
-            pitch_b = job.pitch_b;
-            img_h = job.h;
-            img_w = job.w;
-        }
-        int at, al, bt, bl;
-        if (job.a_top != nullptr) {
-            at = job.a_top[ia]; al = job.a_left[ia];
-            bt = job.b_top[ia]; bl = job.b_left[ia];
-        } else {  // contiguous tiles: tile ia is rows [ia*N, ia*N + N) of an N-wide image
-            at = bt = (int)(ia * N);
-            al = bl = 0;
-        }
-
-        // ---- 1. raw tile pixels for this thread's row transforms ----
-        float ra[ROUNDS][4], rb[ROUNDS][4];
-        float mxa = 0.0f, mxb = 0.0f;
-#pragma unroll
-        for (int r = 0; r < ROUNDS; r++) {
-            const int n1 = S::task_row(grp, r);
-#pragma unroll
-            for (int m = 0; m < 4; m++) {
-                const int n2 = g + G * m;
-                ra[r][m] = load_pix(imgA, pitch_a, img_h, img_w, at + (N - 1 - n1), al + (N - 1 - n2));
-                rb[r][m] = load_pix(imgB, pitch_b, img_h, img_w, bt + n1, bl + n2);
-                mxa = fmaxf(mxa, ra[r][m]);
-                mxb = fmaxf(mxb, rb[r][m]);
-            }
-        }
-        float maxA, maxB;
-        if (job.max_mode == QLPIV_MAX_COMPUTE || job.max_mode == QLPIV_MAX_FIXED_A ||
-            job.max_mode == QLPIV_MAX_FIXED_B) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                mxa = fmaxf(mxa, __shfl_xor_sync(0xffffffffu, mxa, o));
-                mxb = fmaxf(mxb, __shfl_xor_sync(0xffffffffu, mxb, o));
-            }
-            float *redf = reinterpret_cast<float *>(red);
-            if (lane == 0) { redf[warp] = mxa; redf[32 + warp] = mxb; }
-            __syncthreads();
-            mxa = 0.0f; mxb = 0.0f;
-#pragma unroll
-            for (int k = 0; k < NWARPS; k++) { mxa = fmaxf(mxa, redf[k]); mxb = fmaxf(mxb, redf[32 + k]); }
-            maxA = job.max_mode == QLPIV_MAX_FIXED_A ? job.fixed_max_a : fmaxf(mxa, 16.0f);
-            maxB = job.max_mode == QLPIV_MAX_FIXED_B ? job.fixed_max_b : fmaxf(mxb, 16.0f);
-        } else if (job.max_mode == QLPIV_MAX_GIVEN) {
-            maxA = job.max_a[ia];
-            maxB = job.max_b[ia];
-        } else {
-            maxA = job.fixed_max_a;
-            maxB = job.fixed_max_b;
-        }
-        if (job.norm_mode == QLPIV_NORM_MAX_A) maxB = maxA;
-        const bool normalize = job.norm_mode != QLPIV_NORM_NONE;
-
-        // ---- 2. row pass ----
-#pragma unroll
-        for (int r = 0; r < ROUNDS; r++) {
-            const int n1 = S::task_row(grp, r);
-            cplx v[8];
-#pragma unroll
-            for (int m = 0; m < 4; m++) {
-                float a = ra[r][m], b = rb[r][m];
-                if (normalize) {
-                    // (v / max) * 16 + 1 with IEEE single operations, as in Java
-                    a = __fadd_rn(__fmul_rn(__fdiv_rn(a, maxA), 16.0f), 1.0f);
-                    b = __fadd_rn(__fmul_rn(__fdiv_rn(b, maxB), 16.0f), 1.0f);
-                }
-                v[m] = {a, b};
-                v[m + 4] = {0.0f, 0.0f};
-            }
-            fft_group<M, false, L>(v, g, xb, tw);
-#pragma unroll
-            for (int m = 0; m < 8; m++) {
-                const int k2 = g + G * m;
-                int region, slot;
-                if (k2 == 0) { region = 0; slot = n1; }
-                else if (k2 == N) { region = 0; slot = N + n1; }
-                else if (k2 < N) { region = k2; slot = n1; }
-                else { region = M - k2; slot = N + n1; }
-                reg[region * RP + S::rslot(slot)] = v[m];
-            }
-        }
-        __syncthreads();
-
-        // ---- 3. column tasks ----
-#pragma unroll
-        for (int r = 0; r < ROUNDS; r++) {
-            const int c = S::task_row(grp, r);
-            cplx *rg = reg + c * RP;
-            cplx z1[8], z2[8];
-#pragma unroll
-            for (int m = 0; m < 4; m++) {
-                z1[m] = rg[S::rslot(g + G * m)];
-                z2[m] = rg[S::rslot(N + g + G * m)];
-                z1[m + 4] = {0.0f, 0.0f};
-                z2[m + 4] = {0.0f, 0.0f};
-            }
-            fft_group<M, false, L>(z1, g, xb, tw);
-            fft_group<M, false, L>(z2, g, xb, tw);
-            // P(k1) = F*G/M^2, F = (Z1 + conj Zm)/2, G = (Z1 - conj Zm)/(2i), where Zm is the
-            // mirror element Z(M-k1, M-c): held by lane (G-g)%G at m' = 7-m (g>0) or (8-m)%8.
-            const int src = gbase + ((G - g) & (G - 1));
-            const float scale = 0.5f * 0.5f / (float)(M * M);
-            cplx p[8];
-#pragma unroll
-            for (int m = 0; m < 8; m++) {
-                // c == 0: both columns are self-mirrored; otherwise the mirror is in z2
-                const cplx s2 = (g == 0) ? z2[(8 - m) & 7] : z2[7 - m];
-                const cplx s1 = (g == 0) ? z1[(8 - m) & 7] : z1[7 - m];
-                cplx snd = (c == 0) ? s1 : s2;
-                cplx zm;
-                zm.x = __shfl_sync(0xffffffffu, snd.x, src);
-                zm.y = __shfl_sync(0xffffffffu, snd.y, src);
-                const cplx a = z1[m];
-                // F*2 = (a.x + zm.x, a.y - zm.y);  G*2 = (a.y + zm.y, -(a.x - zm.x))
-                const float fr = a.x + zm.x, fi = a.y - zm.y;
-                const float gr = a.y + zm.y, gi = zm.x - a.x;
-                p[m] = {(fr * gr - fi * gi) * scale, (fr * gi + fi * gr) * scale};
-            }
-            if (c == 0) {
-                // second self-mirrored column (k2 = N): P_N packed as the imaginary part
-#pragma unroll
-                for (int m = 0; m < 8; m++) {
-                    const cplx snd = (g == 0) ? z2[(8 - m) & 7] : z2[7 - m];
-                    cplx zm;
-                    zm.x = __shfl_sync(gmask, snd.x, src);
-                    zm.y = __shfl_sync(gmask, snd.y, src);
-                    const cplx a = z2[m];
-                    const float fr = a.x + zm.x, fi = a.y - zm.y;
-                    const float gr = a.y + zm.y, gi = zm.x - a.x;
-                    const cplx pn = {(fr * gr - fi * gi) * scale, (fr * gi + fi * gr) * scale};
-                    p[m] = {p[m].x - pn.y, p[m].y + pn.x};  // P0 + i * PN
-                }
-            }
-            fft_group<M, true, L>(p, g, xb, tw);
-#pragma unroll
-            for (int m = 0; m < 8; m++) rg[S::rslot(g + G * m)] = p[m];
-        }
-        __syncthreads();
-
-        // ---- 4. row-pair pass + per-lane peak scoring ----
-        uint64_t best = 0ull;
-        uint32_t best_ij = 0u;
-        float minf = 3.402823466e38f;
-        float *regf = reinterpret_cast<float *>(reg);
-#pragma unroll
-        for (int r = 0; r < ROUNDS; r++) {
-            const int pr = S::task_pair(grp, r);
-            const int ra_ = 2 * pr, rb_ = 2 * pr + 1;
-            cplx y[8];
-#pragma unroll
-            for (int m = 0; m < 8; m++) {
-                const int k2 = g + G * m;
-                if (k2 == 0 || k2 == N) {
-                    const cplx qa = reg[S::rslot(ra_)], qb = reg[S::rslot(rb_)];
-                    y[m] = (k2 == 0) ? cplx{qa.x, qb.x} : cplx{qa.y, qb.y};
-                } else if (k2 < N) {
-                    const cplx qa = reg[k2 * RP + S::rslot(ra_)], qb = reg[k2 * RP + S::rslot(rb_)];
-                    y[m] = {qa.x - qb.y, qa.y + qb.x};
-                } else {
-                    const int cc = M - k2;
-                    const cplx qa = reg[cc * RP + S::rslot(ra_)], qb = reg[cc * RP + S::rslot(rb_)];
-                    y[m] = {qa.x + qb.y, qb.x - qa.y};
-                }
-            }
-            fft_group<M, true, L>(y, g, xb, tw);
-#pragma unroll
-            for (int m = 0; m < 8; m++) {
-                const int n2 = g + G * m;
-                // keep the plane in the row slots this pair has consumed
-                regf[2 * ((n2 >> 1) * RP + S::rslot(ra_)) + (n2 & 1)] = y[m].x;
-                regf[2 * ((n2 >> 1) * RP + S::rslot(rb_)) + (n2 & 1)] = y[m].y;
-                if (multi > 0) {
-                    // FindMaximumMultiPeaks visits every cell of the (2N-1)^2 plane
-                    if (n2 <= M - 2) {
-                        minf = fminf(minf, y[m].x);
-                        if (rb_ <= M - 2) minf = fminf(minf, y[m].y);
-                    }
-                } else if (n2 >= 1 && n2 <= M - 2) {
-                    if (ra_ >= 1) {
-                        minf = fminf(minf, y[m].x);
-                        const uint64_t k = peak_key(y[m].x, ra_, n2, N);
-                        if (k > best) { best = k; best_ij = ((uint32_t)ra_ << 16) | (uint32_t)n2; }
-                    }
-                    if (rb_ <= M - 2) {
-                        minf = fminf(minf, y[m].y);
-                        const uint64_t k = peak_key(y[m].y, rb_, n2, N);
-                        if (k > best) { best = k; best_ij = ((uint32_t)rb_ << 16) | (uint32_t)n2; }
-                    }
-                }
-                if (job.planes != nullptr && n2 < D) {
-                    float *pl = job.planes + ia * (long)(D * D);
-                    pl[ra_ * D + n2] = y[m].x;
-                    if (rb_ < D) pl[rb_ * D + n2] = y[m].y;
-                }
-            }
-        }
-
-        // ---- 5. CTA reduction; the fit is queued and run 32 IAs at a time ----
-        auto P = [&](int i, int j) -> float { return regf[2 * ((j >> 1) * RP + S::rslot(i)) + (j & 1)]; };
-        if (multi == 0) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const uint64_t ok = __shfl_xor_sync(0xffffffffu, best, o);
-                const uint32_t oij = __shfl_xor_sync(0xffffffffu, best_ij, o);
-                if (ok > best) { best = ok; best_ij = oij; }
-                minf = fminf(minf, __shfl_xor_sync(0xffffffffu, minf, o));
-            }
-            __syncthreads();  // red[] reuse after the max reduction
-            if (lane == 0) {
-                red[warp] = best;
-                red[32 + warp] = ((uint64_t)best_ij << 32) | (uint64_t)__float_as_uint(minf);
-            }
-            __syncthreads();
-            if (warp == 0) {
-                uint64_t bk = 0ull;
-                uint32_t bij = 0u;
-                float mn = 3.402823466e38f;
-                if (lane < NWARPS) {
-                    bk = red[lane];
-                    bij = (uint32_t)(red[32 + lane] >> 32);
-                    mn = __uint_as_float((uint32_t)red[32 + lane]);
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const uint64_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
-                    const uint32_t oij = __shfl_xor_sync(0xffffffffu, bij, o);
-                    // ties on the full key cannot occur between distinct cells (the rank is unique)
-                    if (ok > bk) { bk = ok; bij = oij; }
-                    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-                }
-                if (lane == 0) {
-                    FitRec r;
-                    r.ia = ia;
-                    r.mn = mn;
-                    r.pi = 0;
-                    r.pj = 0;
-                    r.pv = 0.0f;
-                    if (bk != 0ull) {
-                        r.pi = (int)(bij >> 16);
-                        r.pj = (int)(bij & 0xffffu);
-                        r.pv = __uint_as_float((uint32_t)(bk >> 32));
-                    }
-                    r.slot = 0;
-                    r.npk = 1;
-                    fit_stencil<D>(r, job, P, fitv + qn * 2 * job.subpix_pixels);
-                    fitq[qn] = r;
-                }
-            }
-        } else if (mpb == nullptr) {
-            multipeak_select<N>(job, ia, minf, regf, scr, red, fitq, fitv, qn, mp_lv, mp_li, mp_lj);
-        } else {
-            multipeak_stage_call<D, T>(job, ia, minf, P, scr, red, mpb, nb);
-            if (++nb == kMpBatch) {
-                if (warp == 0) mp_batch_run<D, PP>(mpb, nb, lane, job, fitq, fitv);
-                nb = 0;
-            }
-        }
-        if (mpb == nullptr) {
-            qn += KQ;
-            if (qn + KQ > 32) {
-                if (warp == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
-                qn = 0;
-            }
-        }
-        __syncthreads();  // regions are rewritten by the next IA
+        xcorr_cta_ia<N, Pix, PP, false>(job, ia, sm, tid, 0, qn, mpb, nb);
     }
     if (qn > 0 && warp == 0) fit_flush<D, PP>(fitq, fitv, qn, lane, job);
     if (mpb != nullptr) {

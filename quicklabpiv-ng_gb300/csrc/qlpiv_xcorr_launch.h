@@ -46,6 +46,15 @@ cudaError_t launch_k1_32(const IaJob &job, int pixel_type, cudaStream_t stream, 
 cudaError_t launch_k1_64(const IaJob &job, int pixel_type, cudaStream_t stream, int num_sms, int *nlaunch);
 cudaError_t launch_k1_128(const IaJob &job, int pixel_type, cudaStream_t stream, int num_sms, int *nlaunch);
 
+// The persistent mixed-size K1 (qlpiv_xcorr_mixed.cu): job[0..2] = the IA 64, 32 and 16 work
+// lists (count 0: none), next = 3 device counters (zeroed by the launch).  One CTA per SM.
+struct MixedJob {
+    IaJob job[3];
+    unsigned *next;
+};
+bool mixed_kernel_supported(const IaJob &tmpl);
+cudaError_t launch_k1_mixed(const MixedJob &mj, int pixel_type, cudaStream_t stream, int num_sms);
+
 // Calls L<Pix, PP>::run(job, args...) for the job's pixel type and sub-pixel stencil mode.
 template <template <typename, bool> class L, typename... A>
 cudaError_t dispatch_pix(const IaJob &job, int pixel_type, A... args) {

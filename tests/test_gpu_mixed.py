@@ -99,3 +99,45 @@ def test_mixed_plan_rejects(qp, handle):
     with pytest.raises(qp.QlpivError) as e:
         qp.MixedPlan(handle, table, sizes, ofac, qp.PIX_U8, num_peaks=3)
     assert e.value.status == qp.E_ARG
+
+
+@pytest.mark.parametrize("bits,kw", [(8, {}), (12, {"max_mode": 2, "fixed_max": (4095.0, 4095.0)}),
+                                     (8, {"subpix_mode": 0})])
+def test_persistent_schedule_equals_single_passes(qp, handle, bits, kw):
+    """IA 16 / 32 / 64 in one persistent launch (one CTA per SM drains the three work lists),
+    IA 128 beside it: every pair's vectors equal its single-pair pass bit for bit."""
+    pairs, sizes, ofac = _batch(qp, bits, 18, seed=40 + bits + len(kw))
+    keep, table = _device_table(qp, pairs)
+    pt = qp.PIX_U8 if bits == 8 else qp.PIX_U16
+    plan = qp.MixedPlan(handle, table, sizes, ofac, pt, autotune=qp.AUTOTUNE_PERSISTENT, **kw)
+    assert plan.schedule == qp.SCHEDULE_PERSISTENT
+    assert {16, 32, 64, 128} <= set(sizes)
+    for rep in range(2):   # the graph replay resets the work counters
+        plan.run()
+        vec = plan.vectors()
+        for q, (a, b) in enumerate(pairs):
+            g = qp.grid.superposition(a.shape[0], a.shape[1], sizes[q], 0, ofac[q])
+            at, al = g.origins()
+            ref = handle.piv_pass(a, b, sizes[q], at, al, **kw)
+            assert plan.pair_vectors(vec, q).ravel().tobytes() == ref.tobytes(), (rep, q)
+    plan.close()
+
+
+def test_autotuned_schedule(qp, handle):
+    """The autotuner times both schedules and keeps one; P-point sub-pixel fits keep the per-size
+    launches (the persistent kernel runs the 3-point fit only)."""
+    pairs, sizes, ofac = _batch(qp, 8, 10, seed=77)
+    keep, table = _device_table(qp, pairs)
+    plan = qp.MixedPlan(handle, table, sizes, ofac, qp.PIX_U8, autotune=qp.AUTOTUNE_ON)
+    assert plan.schedule in (qp.SCHEDULE_PER_SIZE, qp.SCHEDULE_PERSISTENT)
+    plan.run()
+    vec = plan.vectors()
+    ref_plan = qp.MixedPlan(handle, table, sizes, ofac, qp.PIX_U8, autotune=qp.AUTOTUNE_OFF)
+    assert ref_plan.schedule == qp.SCHEDULE_PER_SIZE
+    ref_plan.run()
+    assert ref_plan.vectors().tobytes() == vec.tobytes()
+    lm = qp.MixedPlan(handle, table, sizes, ofac, qp.PIX_U8, autotune=qp.AUTOTUNE_PERSISTENT,
+                      subpix_mode=qp.SUBPIX_GAUSS_LM, subpix_pixels=5)
+    assert lm.schedule == qp.SCHEDULE_PER_SIZE
+    for p in (plan, ref_plan, lm):
+        p.close()
