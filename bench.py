@@ -213,6 +213,27 @@ def hybrid_accuracy(pkg, h, pair, dense_u, dense_v):
             "max_px": float(max(np.abs(eu).max(), np.abs(ev).max()))}
 
 
+def hybrid_cpu_baseline(pkg, pair):
+    """The oracle's FP32 hybrid on one pair with all host threads: the 32 x 32 pass (FP32 single
+    pass), then the flow stage (prefilters, LK over the 2-level pyramid, Liu-Shen, dense field)."""
+    orc = load_oracle()
+    threads = os.cpu_count() or 1
+    a, b = pair
+    _, tops, lefts = orc.grid(H, W, 32, 0, 0.5)
+    t0 = time.perf_counter()
+    vec = orc.piv_pass(a, b, 32, np.repeat(tops, len(lefts)), np.tile(lefts, len(tops)), precision=32,
+                       nthreads=threads)
+    tu = vec["u"].reshape(len(tops), len(lefts))
+    tv = vec["v"].reshape(len(tops), len(lefts))
+    orc.flow_after_piv(a, b, 32, tops, lefts, tu, tv, mode=2, sigma_lk=2.0, px_lk=3, sigma_ls=0.48, px_ls=5,
+                       window=27, iterations_lk=5, lam=4.0, iterations_ls=60, dense_export=True, pyramid_levels=2,
+                       precision=32)
+    secs = time.perf_counter() - t0
+    return {"value": 1.0 / secs, "unit": "frame-pairs/s", "cores": threads, "kind": "port",
+            "sample": "one 1024x1024 pair: the oracle's FP32 32x32 pass and flow stage (LK pyramid, Liu-Shen, "
+                      f"dense field), {secs:.1f} s"}
+
+
 def run_hybrid(pkg, h, dev, stream, steps, warmup, accuracy=False):
     """Config-4 step: PIV + flow of HYBRID_PAIRS pairs resident in HBM, dense field out."""
     import torch
@@ -262,6 +283,7 @@ def run_hybrid(pkg, h, dev, stream, steps, warmup, accuracy=False):
     fb = [pairs[k % len(pairs)][1] for k in range(hp)]
     res = h.piv_flow(fa, fb, piv, flow, dense=True)
     acc = hybrid_accuracy(pkg, h, pairs[0], res[2][0], res[3][0]) if accuracy else None
+    cpu_line = hybrid_cpu_baseline(pkg, pairs[0]) if accuracy else None
     e2e_steps = 2
     tt = time.perf_counter()
     for _ in range(e2e_steps):
@@ -277,6 +299,8 @@ def run_hybrid(pkg, h, dev, stream, steps, warmup, accuracy=False):
     }
     if acc is not None:
         out["accuracy"] = acc
+    if cpu_line is not None:
+        out["cpu_baseline"] = cpu_line
     return out
 
 
@@ -528,7 +552,29 @@ def batch_accuracy(pkg, plan, vec, host, sizes, ofac, picks):
             "frac_within_1e-3": float(np.mean(e <= 1e-3))}
 
 
-def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64, 128)):
+def batch_cpu_baseline(pkg, host, sizes, ofac, picks, batch_flops, count):
+    """The oracle's FP32 single pass on the sampled pairs with all host threads; the batch's time
+    is extrapolated from the sample by the FFT-formula work (F(2N) per IA)."""
+    orc = load_oracle()
+    threads = os.cpu_count() or 1
+    secs = work = 0.0
+    for q in picks:
+        a, b = host[q]
+        n = int(sizes[q])
+        g = pkg.grid.superposition(a.shape[0], a.shape[1], n, 0, float(ofac[q]))
+        at, al = g.origins()
+        t0 = time.perf_counter()
+        orc.piv_pass(a, b, n, at, al, precision=32, nthreads=threads)
+        secs += time.perf_counter() - t0
+        work += flops_per_ia(n) * g.count
+    batch_s = batch_flops / (work / secs)
+    return {"value": count / batch_s, "unit": "frame-pairs/s", "cores": threads, "kind": "port",
+            "sample": f"{len(picks)} pairs of the batch (sides {sorted({int(host[q][0].shape[0]) for q in picks})}, "
+                      f"every IA size) through the oracle's FP32 pass, {secs:.1f} s; the 256-pair batch "
+                      f"extrapolated by formula work"}
+
+
+def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64, 128), cpu=True):
     import torch
     rng = np.random.default_rng(3)
     a0, _ = pkg.synth.particle_pair((2048, 2048), pkg.synth.Flow(vmax=0.0), ppp=0.02, diam=3.0, bits=8, seed=33)
@@ -580,6 +626,7 @@ def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64
     for n in ia_sizes:
         picks += [q for q in range(count) if sizes[q] == n and sides[q] <= 1024][:2]
     accuracy = batch_accuracy(pkg, plan, vec, host, sizes, ofac, picks)
+    cpu_line = batch_cpu_baseline(pkg, host, sizes, ofac, picks, flops, count) if cpu else None
     # plain per-call: one synchronous frame pass per pair through the host API, frames in pinned
     # host memory; three timed rounds over the sample give the spread
     sample = list(range(0, count, 8))
@@ -614,7 +661,8 @@ def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64
                                "sample": f"{len(sample)} pairs, one synchronous qlpiv_pass per pair, frames in "
                                          f"pinned host memory, median of 3 rounds"},
             "vs_per_call_pairs": fps / per_call_pairs,
-            "vs_per_call_pairs_range": [fps / max(rounds), fps / min(rounds)]}
+            "vs_per_call_pairs_range": [fps / max(rounds), fps / min(rounds)],
+            "cpu_baseline": cpu_line}
 
 
 def run_reference(args, rank):
@@ -811,7 +859,8 @@ def run_gpu(args, rank, world):
         result["hybrid"] = run_hybrid(pkg, h, dev, stream, max(2, min(args.steps, 5)), max(3, args.warmup),
                                       accuracy=rank == 0 and not args.no_cpu)
     if not args.no_batched:
-        result["batched"] = run_batched(pkg, dev, stream, max(3, min(args.steps, 10)), max(3, args.warmup))
+        result["batched"] = run_batched(pkg, dev, stream, max(3, min(args.steps, 10)), max(3, args.warmup),
+                                        cpu=rank == 0 and not args.no_cpu)
     if not args.no_serving and world == 1:
         result["serving"] = run_serving(pkg, dev)
     if rank == 0 and world == 1 and not args.no_cpu:
