@@ -425,10 +425,10 @@ def serving_schedules(pkg):
             pkg.adaptive_desc(64, 16, 0.5, warp_mode=pkg.WARP_BOTH_BILINEAR)]
 
 
-def run_serving(pkg, dev, count=48, loads=(0.25, 0.5, 0.75, 0.9, 1.1), per_load=48):
-    """Saturation throughput of the request server, the plain per-call paths on the same requests,
-    and p50 / p99 latency (submit -> results on the host) under Poisson arrivals at fractions of
-    the saturation rate."""
+def run_serving(pkg, dev, count=48, loads=(0.25, 0.5, 0.75, 0.9, 1.1), per_load=48, clients=4):
+    """Saturation throughput of the request server (`clients` submitting threads, and one), the
+    plain per-call paths on the same requests, and p50 / p99 latency (arrival -> results on the
+    host) under Poisson arrivals at fractions of the saturation rate."""
     reqs = serving_requests(pkg, count)
     sch = serving_schedules(pkg)
     px = sum(a.size for a, _, _ in reqs)
@@ -441,59 +441,69 @@ def run_serving(pkg, dev, count=48, loads=(0.25, 0.5, 0.75, 0.9, 1.1), per_load=
     for a, b, k in reqs:
         h.piv_adaptive([a], [b], sch[k])
     per_call = count / (time.perf_counter() - t0)
-    sample = reqs[:8]
-    t0 = time.perf_counter()
-    for a, b, k in sample:
+    for a, b, k in reqs[:3]:
         pkg.per_call.piv_adaptive_per_call(h, a, b, sch[k])
-    per_stage = len(sample) / (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    for a, b, k in reqs:
+        pkg.per_call.piv_adaptive_per_call(h, a, b, sch[k])
+    per_stage = count / (time.perf_counter() - t0)
     h.close()
 
+    from concurrent.futures import ThreadPoolExecutor
     srv = pkg.Server(dev.index, slots=16, staging_bytes=4 << 30)
+    pool = ThreadPoolExecutor(clients)
     try:
-        def closed_loop():
+        def closed_loop(nc):
+            # nc client threads submit their share of the requests (each submit copies the pair into
+            # pinned staging in the client's thread, the GIL released), then every result is polled
             t = time.perf_counter()
-            tickets = [srv.submit(a, b, sch[k]) for a, b, k in reqs]
+            futs = [pool.submit(lambda part: [srv.submit(a, b, sch[k]) for a, b, k in part], reqs[i::nc])
+                    for i in range(nc)]
+            tickets = [tk for f in futs for tk in f.result()]
             for tk in tickets:
                 srv.poll(tk)
             return count / (time.perf_counter() - t)
 
-        closed_loop()                       # warm-up: plans, pools
-        saturation = closed_loop()
+        closed_loop(clients)                # warm-up: plans, pools
+        saturation_one = closed_loop(1)
+        saturation = closed_loop(clients)
         sweep = []
         rng = np.random.default_rng(9)
+
+        def arrive(due, a, b, k):
+            tk = srv.submit(a, b, sch[k])
+            return tk, time.perf_counter() - due   # arrival -> request staged (s)
+
         for load in loads:
             rate = load * saturation
             gaps = rng.exponential(1.0 / rate, per_load)
             order = rng.integers(0, count, per_load)
-            lat = []
             start = time.perf_counter()
             due = start
-            pend = []
+            futs = []
             for g, idx in zip(gaps, order):
                 due += g
                 while time.perf_counter() < due:
                     time.sleep(min(0.0005, max(0.0, due - time.perf_counter())))
                 a, b, k = reqs[idx]
-                pend.append(srv.submit(a, b, sch[k]))
-                # collect whatever finished meanwhile
-                while pend:
-                    r = srv.poll(pend[0], timeout_ms=0)
-                    if r is None:
-                        break
-                    lat.append(r[2]["total_ms"])
-                    pend.pop(0)
-            for tk in pend:
-                lat.append(srv.poll(tk)[2]["total_ms"])
+                futs.append(pool.submit(arrive, due, a, b, k))
+            lat = []
+            for f in futs:
+                tk, staged = f.result()
+                lat.append(staged * 1e3 + srv.poll(tk)[2]["total_ms"])
             elapsed = time.perf_counter() - start
             sweep.append({"offered_pairs_per_s": rate, "achieved_pairs_per_s": per_load / elapsed,
                           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))})
     finally:
+        pool.shutdown()
         srv.close()
     return {"workload": SERVING_WORKLOAD, "requests": count, "megapixels_per_request": px / count / 1e6,
-            "saturation_pairs_per_s": saturation, "plain_per_call_pairs_per_s": per_call,
+            "clients": clients, "saturation_pairs_per_s": saturation, "saturation_one_client_pairs_per_s":
+            saturation_one, "plain_per_call_pairs_per_s": per_call,
             "plain_per_stage_pairs_per_s": per_stage, "vs_per_call": saturation / per_call,
             "vs_per_stage": saturation / per_stage, "sweep": sweep,
-            "latency": "submit -> displacements on the host (qlpiv_poll), Poisson arrivals"}
+            "latency": f"arrival -> displacements on the host: Poisson arrivals handed to {clients} client threads "
+                       "(each submit copies the pair into pinned staging), plus the server's submit -> done time"}
 
 
 # Batched launch: 256 pairs of sizes from {256^2, 512^2, 1024^2, 2048^2} u8, each with its own IA
