@@ -14,6 +14,8 @@
 // Everything stays on the device; only the last level's displacements leave it.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstring>
 #include <vector>
 
@@ -53,7 +55,12 @@ struct AdaptivePlan {
     DevBuf warped_table;  // pairs qlpiv_frame entries
     DevBuf host_frames;   // images uploaded by qlpiv_piv_adaptive (host variant)
     DevBuf host_table;
-    DevBuf flow;          // optical flow after PIV: one pair's planes (FlowBufs)
+    // optical flow after PIV: kFlowLanes pairs in flight, each lane with its own planes (FlowBufs)
+    // and stream, forked from and joined back into the handle's stream
+    static constexpr int kFlowLanes = 4;
+    DevBuf flow[kFlowLanes];
+    cudaStream_t flow_side[kFlowLanes] = {};
+    cudaEvent_t flow_fork = nullptr, flow_done[kFlowLanes] = {};
     DevBuf flow_dense;    // dense field of the host variant, 2 x pairs x height x width
     DevBuf mp_batch;      // batched multi-peak replay of the correlation passes: batches,
     DevBuf mp_slots;      //   their claim bitmask (zeroed at allocation, zero between launches)
@@ -72,9 +79,15 @@ void destroy_plan(AdaptivePlan *p) {
                           &l.d_rank, &l.d_bu, &l.d_bv, &l.d_puv, &l.d_npk, &l.d_state, &l.d_list, &l.d_done,
                           &l.d_sweeps, &l.d_tiles, &l.d_tmax})
             b->release();
-    for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table, &p->flow, &p->flow_dense,
+    for (DevBuf *b : {&p->warped, &p->warped_table, &p->host_frames, &p->host_table, &p->flow_dense,
                       &p->mp_batch, &p->mp_slots, &p->mp_retry, &p->stab_list, &p->stab_vec})
         b->release();
+    for (int k = 0; k < AdaptivePlan::kFlowLanes; k++) {
+        p->flow[k].release();
+        if (p->flow_side[k]) cudaStreamDestroy(p->flow_side[k]);
+        if (p->flow_done[k]) cudaEventDestroy(p->flow_done[k]);
+    }
+    if (p->flow_fork) cudaEventDestroy(p->flow_fork);
     delete p;
 }
 
@@ -1051,11 +1064,23 @@ static qlpiv_status queue_flow(qlpiv_handle *h, const qlpiv_flow_desc &flow, con
     cudaStream_t s = h->stream;
     const int ni = L.g.tiles_i, nj = L.g.tiles_j;
     const long cnt = L.count(), np = (long)p->height * p->width;
-    FlowBufs fb;
-    cudaError_t e;
-    if ((e = flow_buffers(p->flow, p->height, p->width, ni, nj, fd.iterations_ls, &fb)) != cudaSuccess ||
-        (e = upload_flow_weights(s, fd, fb, weights)) != cudaSuccess)
-        return cuda_fail(e, "flow buffers");
+    // pairs run on up to kFlowLanes streams at once (one lane with the stage profiler, whose
+    // events sit on the handle's stream)
+    const int lanes = h->profiling ? 1 : std::min(p->pairs, AdaptivePlan::kFlowLanes);
+    FlowBufs fb[AdaptivePlan::kFlowLanes];
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < lanes && e == cudaSuccess; k++) {
+        if ((e = flow_buffers(p->flow[k], p->height, p->width, ni, nj, fd.iterations_ls, &fb[k])) != cudaSuccess ||
+            (e = upload_flow_weights(s, fd, fb[k], weights)) != cudaSuccess)
+            break;
+        if (lanes > 1 && !p->flow_side[k] &&
+            ((e = cudaStreamCreateWithFlags(&p->flow_side[k], cudaStreamNonBlocking)) != cudaSuccess ||
+             (e = cudaEventCreateWithFlags(&p->flow_done[k], cudaEventDisableTiming)) != cudaSuccess))
+            break;
+    }
+    if (e == cudaSuccess && lanes > 1 && !p->flow_fork)
+        e = cudaEventCreateWithFlags(&p->flow_fork, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "flow buffers");
     struct MarkCtx {
         qlpiv_handle *h;
         int level, n;
@@ -1084,19 +1109,32 @@ static qlpiv_status queue_flow(qlpiv_handle *h, const qlpiv_flow_desc &flow, con
         return cuda_fail(e, "flow spline");
     if (h->profiling) on_mark(&mc, "flow:spline", false);
     h->launches += 1;
+    if (lanes > 1) {
+        if ((e = cudaEventRecord(p->flow_fork, s)) != cudaSuccess) return cuda_fail(e, "flow fork");
+        for (int k = 0; k < lanes; k++)
+            if ((e = cudaStreamWaitEvent(p->flow_side[k], p->flow_fork, 0)) != cudaSuccess)
+                return cuda_fail(e, "flow fork");
+    }
     for (int q = 0; q < p->pairs; q++) {
         long launches = 0;
         const long off = (long)q * cnt;
         const SplineCoef pc = spline_coef_offset(all, off);
-        if ((e = run_flow(s, fd, p->pixel_type, frames[q].img_a, frames[q].img_b, frames[q].pitch, p->height,
+        const int k = q % lanes;
+        cudaStream_t ls = lanes > 1 ? p->flow_side[k] : s;
+        if ((e = run_flow(ls, fd, p->pixel_type, frames[q].img_a, frames[q].img_b, frames[q].pitch, p->height,
                           p->width, L.g.n, ni, nj, L.d_kfy.as<float2>(), L.d_kfx.as<float2>(), L.d_cyf.as<float>(),
                           L.d_cxf.as<float>(), L.d_tops.as<int>(), L.d_lefts.as<int>(), L.d_u.as<float>() + q * cnt,
                           L.d_v.as<float>() + q * cnt, dense_u ? dense_u + q * np : nullptr,
-                          dense_v ? dense_v + q * np : nullptr, fb, &launches,
+                          dense_v ? dense_v + q * np : nullptr, fb[k], &launches,
                           h->profiling ? &marks : nullptr, &pc)) != cudaSuccess)
             return cuda_fail(e, "optical flow after PIV");
         h->launches += launches;
     }
+    if (lanes > 1)
+        for (int k = 0; k < lanes; k++)
+            if ((e = cudaEventRecord(p->flow_done[k], p->flow_side[k])) != cudaSuccess ||
+                (e = cudaStreamWaitEvent(s, p->flow_done[k], 0)) != cudaSuccess)
+                return cuda_fail(e, "flow join");
     return QLPIV_OK;
 }
 
