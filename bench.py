@@ -579,9 +579,10 @@ def batch_cpu_baseline(pkg, host, sizes, ofac, picks, batch_flops, count):
         work += flops_per_ia(n) * g.count
     batch_s = batch_flops / (work / secs)
     return {"value": count / batch_s, "unit": "frame-pairs/s", "cores": threads, "kind": "port",
-            "sample": f"{len(picks)} pairs of the batch (sides {sorted({int(host[q][0].shape[0]) for q in picks})}, "
-                      f"every IA size) through the oracle's FP32 pass, {secs:.1f} s; the 256-pair batch "
-                      f"extrapolated by formula work"}
+            "sample": f"{len(picks)} pairs of the batch (every 8th: sides "
+                      f"{sorted({int(host[q][0].shape[0]) for q in picks})}, IA sizes "
+                      f"{sorted({int(sizes[q]) for q in picks})}) through the oracle's FP32 pass, {secs:.1f} s; the "
+                      f"{count}-pair batch extrapolated by formula work"}
 
 
 def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64, 128), cpu=True):
@@ -636,7 +637,7 @@ def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64
     for n in ia_sizes:
         picks += [q for q in range(count) if sizes[q] == n and sides[q] <= 1024][:2]
     accuracy = batch_accuracy(pkg, plan, vec, host, sizes, ofac, picks)
-    cpu_line = batch_cpu_baseline(pkg, host, sizes, ofac, picks, flops, count) if cpu else None
+    cpu_line = batch_cpu_baseline(pkg, host, sizes, ofac, list(range(0, count, 8)), flops, count) if cpu else None
     # plain per-call: one synchronous frame pass per pair through the host API, frames in pinned
     # host memory; three timed rounds over the sample give the spread
     sample = list(range(0, count, 8))
