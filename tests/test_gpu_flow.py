@@ -193,3 +193,18 @@ def test_piv_flow_device_matches_host(qp, handle):
     handle.synchronize()
     assert ou.cpu().numpy().tobytes() == u.tobytes() and ov.cpu().numpy().tobytes() == v.tobytes()
     assert odu.cpu().numpy().tobytes() == du.tobytes() and odv.cpu().numpy().tobytes() == dv.tobytes()
+
+
+def test_piv_flow_more_pairs_than_lanes(qp, handle):
+    """Six pairs share the flow stage's four lanes (streams with their own planes): every pair's
+    tiles and dense field equal the pair run alone."""
+    h, w = 160, 192
+    pairs = [_pair(qp, h, w, bits=8, seed=90 + k) for k in range(6)]
+    fa, fb = [p[0] for p in pairs], [p[1] for p in pairs]
+    desc = qp.adaptive_desc(32, 16, 0.5)
+    fd = qp.flow_desc(mode=2, iterations_ls=12, dense_export=True)
+    u, v, du, dv = handle.piv_flow(fa, fb, desc, fd, dense=True)
+    for k in range(len(pairs)):
+        u1, v1, du1, dv1 = handle.piv_flow([fa[k]], [fb[k]], desc, fd, dense=True)
+        assert u[k].tobytes() == u1[0].tobytes() and v[k].tobytes() == v1[0].tobytes(), k
+        assert du[k].tobytes() == du1[0].tobytes() and dv[k].tobytes() == dv1[0].tobytes(), k
