@@ -42,6 +42,9 @@ struct PairShape {
     static constexpr int RP1 = 128 + 16 + 1;     // scratch pitch of a 128-point transform
     static constexpr size_t SMEM = sizeof(cplx) * (size_t)(M + M / 2 + NR * RP + NG1 * RP1) +
                                    64 * sizeof(uint64_t) + 32 * sizeof(FitRec) + 256 /* multi-peak list */;
+    // the FFT exchanges use layout 1 (qlpiv_fft.cuh): the 256-point column transforms exchange in
+    // their region, the 128-point row transforms in their scratch
+    static_assert(xbuf_size<M, 1>() <= RP && xbuf_size<M / 2, 1>() <= RP1, "exchange buffers too small");
 };
 
 __device__ __forceinline__ uint32_t cluster_addr(const void *p, unsigned rank) {
@@ -222,7 +225,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
                 }
                 v[m] = q ? cmul(cplx{a, b}, tw[n2]) : cplx{a, b};
             }
-            fft_group<M / 2, false>(v, g1, scr + grp1 * RP1, tw1);
+            fft_group<M / 2, false, 1>(v, g1, scr + grp1 * RP1, tw1);
 #pragma unroll
             for (int m = 0; m < 8; m++) {
                 const int k2 = 2 * (g1 + G1 * m) + q;
@@ -252,8 +255,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
                 z2[m + 4] = {0.0f, 0.0f};
             }
             __syncwarp();
-            fft_group<M, false>(z1, g2, rg, tw);
-            fft_group<M, false>(z2, g2, rg, tw);
+            fft_group<M, false, 1>(z1, g2, rg, tw);
+            fft_group<M, false, 1>(z2, g2, rg, tw);
             const int src = (G2 - g2) & (G2 - 1);
             const float scale = 0.5f * 0.5f / (float)(M * M);
             cplx p[8];
@@ -284,7 +287,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
                     p[m] = {p[m].x - pn.y, p[m].y + pn.x};
                 }
             }
-            fft_group<M, true>(p, g2, rg, tw);
+            fft_group<M, true, 1>(p, g2, rg, tw);
             __syncwarp();
 #pragma unroll
             for (int m = 0; m < 8; m++) rg[pad8(g2 + G2 * m)] = p[m];
@@ -314,7 +317,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape::T, 1) xco
                     y[m] = {qa.x + qb.y, qb.x - qa.y};
                 }
             }
-            fft_group<M / 2, true>(y, g1, scr + grp1 * RP1, tw1);
+            fft_group<M / 2, true, 1>(y, g1, scr + grp1 * RP1, tw1);
             __syncwarp();
 #pragma unroll
             for (int m = 0; m < 8; m++) reg[pair_slot(pr, g1 + G1 * m)] = y[m];
