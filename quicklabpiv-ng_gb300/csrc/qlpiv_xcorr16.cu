@@ -40,7 +40,7 @@ static cudaError_t launch_warp16(const IaJob &job, cudaStream_t stream, int num_
     IaJob j = job;
     j.twiddles = tw + twiddle_offset(32);
     j.log_tab = log_table(dev);
-    long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? kMultiWaves : 8));
+    long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? multi_waves<16>() : 8));
     const long need = (job.count + w16::kWarps - 1) / w16::kWarps;
     if (grid > need) grid = need;
     if (grid < 1) return cudaSuccess;

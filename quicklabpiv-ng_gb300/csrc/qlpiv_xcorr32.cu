@@ -36,9 +36,9 @@ static cudaError_t launch_one(const IaJob &job, cudaStream_t stream, int num_sms
     IaJob j = job;
     j.twiddles = tw + twiddle_offset(S::M);
     j.log_tab = log_table(dev);
-    // every CTA loops over IAs; eight waves of CTAs balance the single-peak kernel best, 32 the
-    // multi-peak one; the batched multi-peak replay runs one resident wave (a batch per CTA)
-    long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? kMultiWaves : 8));
+    // every CTA loops over IAs; eight waves of CTAs balance the single-peak kernel best, the
+    // multi-peak ones multi_waves<N>() (qlpiv_xcorr_launch.h)
+    long grid = (long)num_sms * bps * (job.waves > 0 ? job.waves : (job.num_peaks > 0 ? multi_waves<32>() : 8));
     if (grid > job.count) grid = job.count;
     if (grid < 1) return cudaSuccess;
     // P-point sub-pixel stencils: 2 P floats per queued fit after the fixed layout

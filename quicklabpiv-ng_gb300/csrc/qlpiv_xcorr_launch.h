@@ -8,11 +8,19 @@
 
 namespace qlpiv {
 
+constexpr int kMultiWaves16 = 2;
+
 inline int twiddle_offset(int m) { return m == 32 ? 0 : (m == 64 ? 32 : (m == 128 ? 96 : 224)); }
 
-// Default waves of resident CTAs per launch in multi-peak mode.  Measured on the headline adaptive
-// workload (three multi-peak passes): 1 wave 558 frame-pairs/s, 4: 568, 16: 582, 32: 585, 64: 586.
-constexpr int kMultiWaves = 32;
+// Default waves of resident CTAs (IA 16: warps) per launch in multi-peak mode, per IA size.  With
+// the batched list replay a unit replays its IAs 32 at a time, so fewer waves fill more batches;
+// measured on the headline adaptive workload (pass times in ms at 2 / 4 / 8 / 16 / 32 waves):
+// IA 16 18.63 / 18.74 / 19.0 / 19.40 / 20.10; IA 32 (8 / 16 / 32) 17.68 / 17.61 / 17.75;
+// IA 64 (8 / 16 / 32) 18.69 / 18.62 / 18.60.
+template <int N>
+constexpr int multi_waves() {
+    return N == 16 ? kMultiWaves16 : (N == 32 ? 16 : 32);
+}
 
 constexpr size_t kSubpixSmem = sizeof(float) * 32 * 2 * kMaxSubpixPixels;
 
