@@ -458,10 +458,14 @@ qlpiv_status qlpiv_pass_batch(qlpiv_handle *h, const qlpiv_pass_desc *desc, int 
         off += (bytes + 255) & ~(size_t)255;
         char *db = base + off;
         off += (bytes + 255) & ~(size_t)255;
-        if ((e = cudaMemcpy2DAsync(da, row, fr.img_a, (size_t)fr.pitch * pb, row, fr.height, cudaMemcpyHostToDevice,
-                                   h->stream)) != cudaSuccess ||
-            (e = cudaMemcpy2DAsync(db, row, fr.img_b, (size_t)fr.pitch * pb, row, fr.height, cudaMemcpyHostToDevice,
-                                   h->stream)) != cudaSuccess)
+        // rows packed in the host image (pitch == width): one linear copy per image
+        const size_t spitch = (size_t)fr.pitch * pb;
+        auto upload = [&](char *d, const void *src) {
+            return spitch == row ? cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, h->stream)
+                                 : cudaMemcpy2DAsync(d, row, src, spitch, row, fr.height, cudaMemcpyHostToDevice,
+                                                     h->stream);
+        };
+        if ((e = upload(da, fr.img_a)) != cudaSuccess || (e = upload(db, fr.img_b)) != cudaSuccess)
             return cuda_fail(e, "frame upload");
         dev_frames[f] = {da, db, fr.height, fr.width, (int64_t)fr.width};
     }

@@ -653,12 +653,16 @@ static qlpiv_status upload_host_frames(qlpiv_handle *h, const qlpiv_frame *frame
         return cuda_fail(e, "frame buffers");
     t.resize(num_pairs);
     char *base = p->host_frames.as<char>();
+    // rows packed in the host image (pitch == width): one linear copy per image
+    auto upload = [&](char *d, const void *src, size_t spitch) {
+        return spitch == row ? cudaMemcpyAsync(d, src, img, cudaMemcpyHostToDevice, s)
+                             : cudaMemcpy2DAsync(d, row, src, spitch, row, height, cudaMemcpyHostToDevice, s);
+    };
     for (int q = 0; q < num_pairs; q++) {
         char *da = base + 2 * q * stride, *db = base + (2 * q + 1) * stride;
-        if ((e = cudaMemcpy2DAsync(da, row, frames[q].img_a, (size_t)frames[q].pitch * pb, row, height,
-                                   cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-            (e = cudaMemcpy2DAsync(db, row, frames[q].img_b, (size_t)frames[q].pitch * pb, row, height,
-                                   cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        const size_t spitch = (size_t)frames[q].pitch * pb;
+        if ((e = upload(da, frames[q].img_a, spitch)) != cudaSuccess ||
+            (e = upload(db, frames[q].img_b, spitch)) != cudaSuccess)
             return cuda_fail(e, "frame upload");
         t[q] = {da, db, height, width, (int64_t)width};
     }
