@@ -47,7 +47,7 @@ def _device_table(qp, pairs):
     dev = torch.device("cuda:0")
     keep, table = [], np.zeros(len(pairs), qp.FRAME_DTYPE)
     for k, (a, b) in enumerate(pairs):
-        view = np.int16 if a.dtype == np.uint16 else np.uint8
+        view = {np.dtype(np.uint16): np.int16, np.dtype(np.uint8): np.uint8}.get(a.dtype, a.dtype)
         ta = torch.from_numpy(a.view(view).copy()).to(dev)
         tb = torch.from_numpy(b.view(view).copy()).to(dev)
         keep.append((ta, tb))
@@ -102,13 +102,19 @@ def test_mixed_plan_rejects(qp, handle):
 
 
 @pytest.mark.parametrize("bits,kw", [(8, {}), (12, {"max_mode": 2, "fixed_max": (4095.0, 4095.0)}),
-                                     (8, {"subpix_mode": 0})])
+                                     (8, {"subpix_mode": 0}), ("f32", {})])
 def test_persistent_schedule_equals_single_passes(qp, handle, bits, kw):
     """IA 16 / 32 / 64 in one persistent launch (one CTA per SM drains the three work lists),
-    IA 128 beside it: every pair's vectors equal its single-pair pass bit for bit."""
-    pairs, sizes, ofac = _batch(qp, bits, 18, seed=40 + bits + len(kw))
+    IA 128 beside it: every pair's vectors equal its single-pair pass bit for bit (u8, 12-bit in
+    u16, float32 frames)."""
+    if bits == "f32":
+        pairs, sizes, ofac = _batch(qp, 8, 18, seed=71)
+        pairs = [(a.astype(np.float32), b.astype(np.float32)) for a, b in pairs]
+        pt = qp.PIX_F32
+    else:
+        pairs, sizes, ofac = _batch(qp, bits, 18, seed=40 + bits + len(kw))
+        pt = qp.PIX_U8 if bits == 8 else qp.PIX_U16
     keep, table = _device_table(qp, pairs)
-    pt = qp.PIX_U8 if bits == 8 else qp.PIX_U16
     plan = qp.MixedPlan(handle, table, sizes, ofac, pt, autotune=qp.AUTOTUNE_PERSISTENT, **kw)
     assert plan.schedule == qp.SCHEDULE_PERSISTENT
     assert {16, 32, 64, 128} <= set(sizes)

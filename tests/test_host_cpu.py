@@ -275,3 +275,40 @@ def test_inherit_noalloc_checks_tensors_before_the_call(qp):
     t = torch.zeros(16, dtype=torch.float32)
     with pytest.raises(ValueError, match="CUDA tensor"):
         qp.inherit_noalloc(0, 0, t, t, t, t, t, t, t, t, 4, 4, 4, 4)
+
+
+def _xpad(m, layout, pas, e):
+    """Exchange-buffer index of qlpiv_fft.cuh's xpad<M, L, PASS>."""
+    if layout == 1 and m >= 128:
+        return e + (e >> 4) if pas == 0 else e + 4 * (e >> 5)
+    return e + (e >> 3)
+
+
+def _wavefronts8(addrs):
+    """Shared-memory wavefronts of one warp's 8-byte accesses (complex indices; 16-lane halves)."""
+    total = 0
+    for half in (addrs[:16], addrs[16:]):
+        banks = {}
+        for a in half:
+            for w in (2 * a, 2 * a + 1):
+                banks.setdefault(w % 32, set()).add(w)
+        total += max(len(v) for v in banks.values())
+    return total
+
+
+@pytest.mark.parametrize("m,g,pitch", [(128, 16, 140), (64, 8, 72), (256, 32, 289)])
+def test_fft_exchange_layouts_conflict_free(m, g, pitch):
+    """The K1 exchange layouts (layout 1, the group buffers `pitch` complex apart) give every
+    8-byte store and load of the radix-8 Stockham passes one wavefront per half-warp."""
+    passes = {64: [(8, 1)], 128: [(8, 1), (8, 8)], 256: [(8, 1), (8, 8)]}[m]
+    for pas, (r, p) in enumerate(passes):
+        for t in range(r):   # stores: lane g writes output t of its butterfly i = g
+            addrs = []
+            for lane in range(32):
+                gg = lane % g
+                k = gg & (p - 1)
+                addrs.append((lane // g) * pitch + _xpad(m, 1, pas, (gg - k) * r + k + t * p))
+            assert _wavefronts8(addrs) == 2, (m, pas, t)
+        for mm in range(8):  # loads of the stride-G layout
+            addrs = [(lane // g) * pitch + _xpad(m, 1, pas, lane % g + g * mm) for lane in range(32)]
+            assert _wavefronts8(addrs) == 2, (m, pas, mm)
