@@ -594,6 +594,32 @@ qlpiv_status qlpiv_mixed_plan_run(qlpiv_handle *h, qlpiv_mixed_plan *plan, qlpiv
 qlpiv_status qlpiv_mixed_plan_download(qlpiv_handle *h, qlpiv_mixed_plan *plan, qlpiv_vector *host_out);
 qlpiv_status qlpiv_mixed_plan_destroy(qlpiv_mixed_plan *plan);
 
+/* ---------------- adaptive batches ----------------
+ * Frame pairs of uneven sizes, each with its own adaptive schedule (one of num_schedules
+ * descriptors, schedule_of_pair[q]), replayed from one captured CUDA graph.  The pairs that share
+ * frame size and schedule form a group that runs qlpiv_piv_adaptive_device's loop over all its
+ * pairs (every level one flattened work list); the groups are branches of the graph, forked from
+ * and joined into the handle's stream.  `frames` is a host table of device images (u8 or u16);
+ * the batch keeps a device copy per group.  Outputs: the last level's displacements of every
+ * pair, pair q's tiles_i x tiles_j tiles (row-major) at pair_offset[q], each pair's the same as
+ * qlpiv_piv_adaptive gives for it alone.  The reference runs one such job per pair and host
+ * thread (S/jobs/OpenClGpuManager.java:121-148). */
+typedef struct qlpiv_adaptive_batch qlpiv_adaptive_batch;
+qlpiv_status qlpiv_adaptive_batch_create(qlpiv_handle *h, int pixel_type, int num_pairs, const qlpiv_frame *frames,
+                                         const qlpiv_adaptive_desc *schedules, int num_schedules,
+                                         const int32_t *schedule_of_pair, qlpiv_adaptive_batch **batch);
+/* total_tiles; pair_offset[num_pairs + 1]; tiles_ij[2 num_pairs]; groups.  Any output may be NULL. */
+qlpiv_status qlpiv_adaptive_batch_info(const qlpiv_adaptive_batch *batch, int64_t *total_tiles,
+                                       int64_t *pair_offset, int32_t *tiles_ij, int32_t *groups);
+/* Queues the batch's graph on the handle's stream; *device_u / *device_v receive the device
+ * displacements (rows, columns). */
+qlpiv_status qlpiv_adaptive_batch_run(qlpiv_handle *h, qlpiv_adaptive_batch *batch, float **device_u,
+                                      float **device_v);
+/* Waits for the handle's stream and copies the displacements to the host. */
+qlpiv_status qlpiv_adaptive_batch_download(qlpiv_handle *h, qlpiv_adaptive_batch *batch, float *host_u,
+                                           float *host_v);
+qlpiv_status qlpiv_adaptive_batch_destroy(qlpiv_adaptive_batch *batch);
+
 /* ---------------- request server (continuous batching) ----------------
  * The reference runs one job per frame pair and host thread (S/jobs/LocalPIVOpenCLGpuJob.java,
  * pooled by OpenClGpuManager.java:121-148); it has no server.  A qlpiv_server owns one device

@@ -276,6 +276,12 @@ _SIGNATURES = {
     "qlpiv_mixed_plan_create": (_i, [_vp, ctypes.POINTER(PassDesc), _i, _i, _vp, _vp, _vp, _i, ctypes.POINTER(_vp)]),
     "qlpiv_mixed_plan_info": (_i, [_vp, ctypes.POINTER(ctypes.c_int64), _vp, _vp, _vp]),
     "qlpiv_mixed_plan_schedule": (_i, [_vp, ctypes.POINTER(ctypes.c_int32)]),
+    "qlpiv_adaptive_batch_create": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp, ctypes.POINTER(_vp)]),
+    "qlpiv_adaptive_batch_info": (_i, [_vp, ctypes.POINTER(ctypes.c_int64), _vp, _vp,
+                                       ctypes.POINTER(ctypes.c_int32)]),
+    "qlpiv_adaptive_batch_run": (_i, [_vp, _vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
+    "qlpiv_adaptive_batch_download": (_i, [_vp, _vp, _vp, _vp]),
+    "qlpiv_adaptive_batch_destroy": (_i, [_vp]),
     "qlpiv_mixed_plan_run": (_i, [_vp, _vp, ctypes.POINTER(_vp)]),
     "qlpiv_mixed_plan_download": (_i, [_vp, _vp, _vp]),
     "qlpiv_mixed_plan_destroy": (_i, [_vp]),
@@ -917,6 +923,60 @@ def export_dense_mat(path, desc, height, width, dense_u, dense_v, **kw):
     m = dict(u=dense_u, v=dense_v, ia=(g["n"], g["n"]),
              margins=(g["margin_top"], g["margin_left"], g["margin_bottom"], g["margin_right"]))
     export_mat(path, [m], height, width, desc.ia_start, desc.ia_end, desc.overlap_factor, layout=MAT_DENSE, **kw)
+
+
+class AdaptiveBatch:
+    """Adaptive batch (qlpiv_adaptive_batch_*): pairs of uneven sizes, each with its own adaptive
+    schedule (schedules[schedule_of_pair[q]]), one graph launch per batch; pairs of one size and
+    schedule share a group.  frames: FRAME_DTYPE table of device images."""
+
+    def __init__(self, handle, frames, pixel_type, schedules, schedule_of_pair):
+        self._h = handle
+        self._lib = handle._lib
+        table = np.ascontiguousarray(frames, FRAME_DTYPE)
+        self.num_pairs = len(table)
+        descs = (AdaptiveDesc * len(schedules))(*schedules)
+        sidx = np.ascontiguousarray(schedule_of_pair, np.int32)
+        p = ctypes.c_void_p()
+        _check(self._lib.qlpiv_adaptive_batch_create(handle._h, pixel_type, self.num_pairs, table.ctypes.data,
+                                                     descs, len(schedules), _addr(sidx), ctypes.byref(p)))
+        self._p = p
+        tot = ctypes.c_int64()
+        groups = ctypes.c_int32()
+        self.pair_offset = np.empty(self.num_pairs + 1, np.int64)
+        self.tiles = np.empty((self.num_pairs, 2), np.int32)
+        _check(self._lib.qlpiv_adaptive_batch_info(p, ctypes.byref(tot), _addr(self.pair_offset),
+                                                   _addr(self.tiles), ctypes.byref(groups)))
+        self.total = tot.value
+        self.groups = groups.value
+
+    def run(self):
+        """Queues the batch on the handle's stream; returns the device addresses of (u, v)."""
+        u, v = ctypes.c_void_p(), ctypes.c_void_p()
+        _check(self._lib.qlpiv_adaptive_batch_run(self._h._h, self._p, ctypes.byref(u), ctypes.byref(v)))
+        return u.value, v.value
+
+    def displacements(self):
+        u = np.empty(self.total, np.float32)
+        v = np.empty(self.total, np.float32)
+        _check(self._lib.qlpiv_adaptive_batch_download(self._h._h, self._p, _addr(u), _addr(v)))
+        return u, v
+
+    def pair(self, arr, q):
+        ti, tj = int(self.tiles[q][0]), int(self.tiles[q][1])
+        o = int(self.pair_offset[q])
+        return arr[o:o + ti * tj].reshape(ti, tj)
+
+    def close(self):
+        if getattr(self, "_p", None):
+            self._lib.qlpiv_adaptive_batch_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class MixedPlan:
