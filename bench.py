@@ -638,6 +638,32 @@ def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64
         picks += [q for q in range(count) if sizes[q] == n and sides[q] <= 1024][:2]
     accuracy = batch_accuracy(pkg, plan, vec, host, sizes, ofac, picks)
     cpu_line = batch_cpu_baseline(pkg, host, sizes, ofac, list(range(0, count, 8)), flops, count) if cpu else None
+    # adaptive batch: the same pairs, each with one of the served schedules (single 32 | 64->32 |
+    # 64->32->16 + warp), groups of one size and schedule as graph branches; against one
+    # synchronous qlpiv_piv_adaptive per pair with pinned frames
+    sch = serving_schedules(pkg)
+    sidx = np.random.default_rng(11).integers(0, len(sch), count)
+    ab = pkg.AdaptiveBatch(h, table, pkg.PIX_U8, sch, sidx)
+    ab_ms = time_plan(ab)
+    ab_groups, ab_tiles = ab.groups, ab.total
+    ab.close()
+    # sorted by size and schedule, so that consecutive calls reuse the handle's plan
+    ab_sample = sorted(range(0, count, 4), key=lambda q: (int(sides[q]), int(sidx[q])))
+    ab_pinned = {q: tuple(torch.from_numpy(x).pin_memory().numpy() for x in host[q]) for q in ab_sample}
+    for q in ab_sample[:2]:
+        h.piv_adaptive([ab_pinned[q][0]], [ab_pinned[q][1]], sch[sidx[q]])
+    tt = time.perf_counter()
+    for q in ab_sample:
+        h.piv_adaptive([ab_pinned[q][0]], [ab_pinned[q][1]], sch[sidx[q]])
+    ab_per_call = len(ab_sample) / (time.perf_counter() - tt)
+    adaptive = {"schedules": "single 32 | 64->32 | 64->32->16 + BothImages warp, 50 % overlap, one per pair "
+                             "(seeded)", "groups": ab_groups, "tiles_per_step": ab_tiles, "ms_per_step": ab_ms,
+                "frame_pairs_per_s": count / (ab_ms * 1e-3),
+                "plain_per_call": {"frame_pairs_per_s": ab_per_call,
+                                   "sample": f"{len(ab_sample)} pairs (every 4th, ordered by size and "
+                                             "schedule), one synchronous qlpiv_piv_adaptive per pair, frames in "
+                                             "pinned host memory"},
+                "vs_per_call": count / (ab_ms * 1e-3) / ab_per_call}
     # plain per-call: one synchronous frame pass per pair through the host API, frames in pinned
     # host memory; three timed rounds over the sample give the spread
     sample = list(range(0, count, 8))
@@ -673,7 +699,7 @@ def run_batched(pkg, dev, stream, steps, warmup, count=256, ia_sizes=(16, 32, 64
                                          f"pinned host memory, median of 3 rounds"},
             "vs_per_call_pairs": fps / per_call_pairs,
             "vs_per_call_pairs_range": [fps / max(rounds), fps / min(rounds)],
-            "cpu_baseline": cpu_line}
+            "cpu_baseline": cpu_line, "adaptive": adaptive}
 
 
 def run_reference(args, rank):
