@@ -961,6 +961,8 @@ __device__ void mp_batch_run_k(const MpBatch *bt, int nb, int lane, const IaJob 
     __syncwarp();
 }
 
+// Out of line: it runs once per 32 IAs, and inlined it made every K1 pass slower (headline 875 ->
+// 852 frame-pairs/s).
 template <int D, bool PP>
 __device__ __noinline__ void mp_batch_run(const MpBatch *bt, int nb, int lane, const IaJob &job, FitRec *fitq,
                                           const float *fitv) {
@@ -1005,11 +1007,12 @@ __device__ __forceinline__ void multipeak_stage(const IaJob &job, long ia, float
     }
 }
 
-// Step 5' of xcorr_kernel for one IA (kept out of line so that the single-peak path keeps its
-// register allocation): the plane is in the column-pair regions, the records go to the FFT
-// scratch, `multi` fit records are queued at fitq[qn..).  Called by every thread of the CTA.
+// Step 5' of xcorr_kernel for one IA, per-IA list replay: the plane is in the column-pair regions,
+// the records go to the FFT scratch, `multi` fit records are queued at fitq[qn..).  Called by every
+// thread of the CTA.  Inlined: as a call it cost the IA-64 kernel 3 % (single-peak 16.05 -> 15.64
+// ms with it inlined, batched multi-peak 17.52 -> 16.94 ms), the IA-32 kernel nothing.
 template <int N>
-__device__ __noinline__ void multipeak_select(const IaJob &job, long ia, float minf, const float *regf, cplx *scr,
+__device__ __forceinline__ void multipeak_select(const IaJob &job, long ia, float minf, const float *regf, cplx *scr,
                                               uint64_t *red, FitRec *fitq, float *fitv, int qn, float *mp_lv,
                                               int *mp_li, int *mp_lj) {
     using S = XcorrShape<N>;
