@@ -79,8 +79,9 @@ __device__ __forceinline__ int pair_slot(int p, int np) {
     return (np >> 1) * PairShape::RP + pad8(2 * p + (np & 1));
 }
 
-// Multi-peak mode of step 5 (out of line: the single-peak path keeps its registers).  Both CTAs
-// have written their row pairs of the plane to the cluster's global scratch `mp`; rank 1 hands its
+// Multi-peak mode of step 5 (out of line; inlined it measured the same on single-peak passes).
+// Both CTAs have written their row pairs of the plane to the cluster's global scratch `mp`; rank 1
+// hands its
 // min floor to rank 0, and rank 0 runs FindMaximumMultiPeaks over the plane (L2 reads), staging the
 // cell records in its regions (the partials are no longer needed) and queueing one fit per peak.
 // Called by every thread of both CTAs.
