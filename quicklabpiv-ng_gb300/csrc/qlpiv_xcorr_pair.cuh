@@ -81,10 +81,9 @@ __device__ __forceinline__ int pair_slot(int p, int np) {
 
 // Multi-peak mode of step 5 (out of line; inlined it measured the same on single-peak passes).
 // Both CTAs have written their row pairs of the plane to the cluster's global scratch `mp`; rank 1
-// hands its
-// min floor to rank 0, and rank 0 runs FindMaximumMultiPeaks over the plane (L2 reads), staging the
-// cell records in its regions (the partials are no longer needed) and queueing one fit per peak.
-// Called by every thread of both CTAs.
+// hands its min floor to rank 0, and rank 0 runs FindMaximumMultiPeaks over the plane (L2 reads),
+// staging the cell records in its regions (the partials are no longer needed) and queueing one fit
+// per peak.  Called by every thread of both CTAs.
 static __device__ __noinline__ void pair_multipeak(const IaJob &job, long ia, float minf, const float *mp, cplx *reg,
                                                    uint64_t *red, FitRec *fitq, float *fitv, int qn, float *mp_lv,
                                                    int *mp_li, int *mp_lj, int q, uint32_t xch0) {
